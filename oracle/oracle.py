@@ -1,0 +1,355 @@
+"""Test infrastructure only: ctypes bindings for the two CPU checkers.
+
+* ``port()`` -- oracle/port/tg_oracle.c, the C restatement of Tangerine's CPU export path
+  (builds anywhere, including the GPU host).
+* ``reference()`` -- Tangerine's own CPU code compiled from its sources by
+  ``make -C oracle ref`` (only where the reference sources are present).
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg import this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_SO = HERE / "_build" / "libtg_oracle.so"
+REF_SO = HERE / "_ref" / "libtangerine_ref.so"
+REFERENCE_SOURCES = Path(os.environ.get("TANGERINE_REFERENCE", "/root/reference"))
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    return PORT_SO
+
+
+def build_reference() -> Path | None:
+    if not (REFERENCE_SOURCES / "tangerine" / "sdf_evaluator.cpp").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_SOURCES}", "-j8"], check=True)
+    return REF_SO
+
+
+class Mesh:
+    """An exported mesh: vertices (V,3) f32, active cube index per vertex (V,) u64,
+    faces (F,3) u64 vertex indices, optional normals (V,3) f32 and colours (V,3) u8."""
+
+    def __init__(self, vertices, cubes, faces, normals=None, colors=None, seconds=0.0):
+        self.vertices = vertices
+        self.cubes = cubes
+        self.faces = faces
+        self.normals = normals
+        self.colors = colors
+        self.seconds = seconds
+
+
+class CpuOracle:
+    def __init__(self, path: Path, prefix: str):
+        self.path = Path(path)
+        self.prefix = prefix
+        self.lib = C.CDLL(str(path))
+        self._bind()
+
+    def _fn(self, name, res, args):
+        f = getattr(self.lib, self.prefix + name)
+        f.restype = res
+        f.argtypes = args
+        return f
+
+    def _bind(self):
+        vp, i64, f, i = C.c_void_p, C.c_int64, C.c_float, C.c_int
+        self._build = self._fn("build", vp, [_f32p, i])
+        self._free = self._fn("free", None, [vp])
+        self._free_buffer = self._fn("free_buffer", None, [vp])
+        self._stack_size = self._fn("stack_size", i, [vp])
+        self._has_paint = self._fn("has_paint", i, [vp])
+        self._finite = self._fn("has_finite_bounds", i, [vp])
+        self._leaf_count = self._fn("leaf_count", i, [vp])
+        self._bounds = self._fn("bounds", None, [vp, _f32p, i])
+        self._eval = self._fn("eval", None, [vp, i64, _f32p, _f32p])
+        self._gradient = self._fn("gradient", None, [vp, i64, _f32p, _f32p])
+        self._color = self._fn("color", None, [vp, i64, _f32p, _u8p])
+        self._compile = self._fn("compile", i, [vp, _u32p, i])
+        self._interp = self._fn("interp_eval", None, [vp, i64, _f32p, _f32p])
+        self._clip = self._fn("clip", vp, [vp, f, f, f, f])
+        self._equal = self._fn("equal", i, [vp, vp])
+        self._oct_create = self._fn("octree_create", vp, [vp, f, i, i])
+        self._oct_free = self._fn("octree_free", None, [vp])
+        self._oct_dump = self._fn("octree_dump", i, [vp, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_int32)),
+                                                      C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_int)])
+        self._oct_eval = self._fn("octree_eval", None, [vp, i64, _f32p, i, _f32p])
+        self._oct_grad = self._fn("octree_gradient", None, [vp, i64, _f32p, _f32p])
+        self._oct_color = self._fn("octree_color", None, [vp, i64, _f32p, _u8p])
+        self._oct_grid = None
+        self._raymarch = None
+
+    # -- trees ----------------------------------------------------------------------
+    def build(self, spec) -> int:
+        spec = np.ascontiguousarray(spec, dtype=np.float32)
+        h = self._build(spec, spec.size)
+        if not h:
+            raise ValueError("malformed tree spec")
+        return h
+
+    def free(self, h):
+        self._free(h)
+
+    def stack_size(self, h):
+        return self._stack_size(h)
+
+    def has_paint(self, h):
+        return bool(self._has_paint(h))
+
+    def has_finite_bounds(self, h):
+        return bool(self._finite(h))
+
+    def leaf_count(self, h):
+        return self._leaf_count(h)
+
+    def bounds(self, h, inner=False):
+        out = np.zeros(6, np.float32)
+        self._bounds(h, out, int(inner))
+        return out
+
+    @staticmethod
+    def _pts(points):
+        return np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+
+    def eval(self, h, points):
+        p = self._pts(points)
+        out = np.empty(p.shape[0], np.float32)
+        self._eval(h, p.shape[0], p, out)
+        return out
+
+    def gradient(self, h, points):
+        p = self._pts(points)
+        out = np.empty_like(p)
+        self._gradient(h, p.shape[0], p, out)
+        return out
+
+    def color(self, h, points):
+        p = self._pts(points)
+        out = np.empty(p.shape, np.uint8)
+        self._color(h, p.shape[0], p, out)
+        return out
+
+    def compile(self, h):
+        n = self._compile(h, np.zeros(1, np.uint32), 0)
+        out = np.zeros(n, np.uint32)
+        self._compile(h, out, n)
+        return out
+
+    def interp_eval(self, h, points):
+        p = self._pts(points)
+        out = np.empty(p.shape[0], np.float32)
+        self._interp(h, p.shape[0], p, out)
+        return out
+
+    def clip(self, h, point, radius):
+        return self._clip(h, float(point[0]), float(point[1]), float(point[2]), float(radius)) or None
+
+    def equal(self, a, b):
+        return bool(self._equal(a, b))
+
+    # -- octree ---------------------------------------------------------------------
+    def octree(self, h, target=0.25, coalesce=True, max_depth=-1):
+        o = self._oct_create(h, target, int(coalesce), max_depth)
+        return o or None
+
+    def octree_free(self, o):
+        self._oct_free(o)
+
+    def octree_dump(self, o):
+        nodes = C.POINTER(C.c_float)()
+        children = C.POINTER(C.c_int32)()
+        words = C.POINTER(C.c_uint32)()
+        wc = C.c_int()
+        n = self._oct_dump(o, C.byref(nodes), C.byref(children), C.byref(words), C.byref(wc))
+        N = np.ctypeslib.as_array(nodes, shape=(n * 14,)).reshape(n, 14).copy()
+        Ch = np.ctypeslib.as_array(children, shape=(n * 8,)).reshape(n, 8).copy()
+        W = np.ctypeslib.as_array(words, shape=(max(1, wc.value),))[: wc.value].copy()
+        for b in (nodes, children, words):
+            self._free_buffer(C.cast(b, C.c_void_p))
+        return N, Ch, W
+
+    def octree_eval(self, o, points, exact=True):
+        p = self._pts(points)
+        out = np.empty(p.shape[0], np.float32)
+        self._oct_eval(o, p.shape[0], p, int(exact), out)
+        return out
+
+    def octree_gradient(self, o, points):
+        p = self._pts(points)
+        out = np.empty_like(p)
+        self._oct_grad(o, p.shape[0], p, out)
+        return out
+
+    def octree_color(self, o, points):
+        p = self._pts(points)
+        out = np.empty(p.shape, np.uint8)
+        self._oct_color(o, p.shape[0], p, out)
+        return out
+
+
+class PortOracle(CpuOracle):
+    def __init__(self, path: Path = PORT_SO):
+        super().__init__(path, "tgo_")
+        vp, i64, f, i = C.c_void_p, C.c_int64, C.c_float, C.c_int
+        self._oct_grid = self._fn("octree_grid", None, [vp, f, f, f, f, f, f, i64, i64, i64, i, _f32p])
+        self._sn = self._fn("surface_nets", i64, [vp, f, f, f, f, f, f, i64, i64, i64, i, i,
+                                                  C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_uint64)),
+                                                  C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(C.c_int64), C.POINTER(C.c_double)])
+        self._attrs = self._fn("vertex_attributes", None, [vp, i64, _f32p, i, _f32p, C.c_void_p])
+        self._oct_paint = self._fn("octree_has_paint", i, [vp])
+        self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
+        self._hw = self._fn("hardware_threads", i, [])
+
+    def hardware_threads(self):
+        return self._hw()
+
+    def octree_grid(self, o, grid, threads=0):
+        nx, ny, nz = grid.sx + 1, grid.sy + 1, grid.sz + 1
+        out = np.empty(nx * ny * nz, np.float32)
+        self._oct_grid(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, nx, ny, nz, threads, out)
+        return out.reshape(nz, ny, nx)
+
+    def surface_nets(self, o, grid, threads=0, faithful=False) -> Mesh:
+        V = C.POINTER(C.c_float)()
+        Cb = C.POINTER(C.c_uint64)()
+        F = C.POINTER(C.c_uint64)()
+        nf = C.c_int64()
+        secs = C.c_double()
+        nv = self._sn(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, grid.sx, grid.sy, grid.sz,
+                      threads, int(faithful), C.byref(V), C.byref(Cb), C.byref(F), C.byref(nf), C.byref(secs))
+        if nv < 0:
+            raise ValueError("grid with a strictly longest axis is not restated")
+        verts = np.ctypeslib.as_array(V, shape=(max(1, nv) * 3,))[: nv * 3].reshape(nv, 3).copy()
+        cubes = np.ctypeslib.as_array(Cb, shape=(max(1, nv),))[:nv].copy()
+        faces = np.ctypeslib.as_array(F, shape=(max(1, nf.value) * 3,))[: nf.value * 3].reshape(nf.value, 3).copy()
+        for b in (V, Cb, F):
+            self._free_buffer(C.cast(b, C.c_void_p))
+        return Mesh(verts, cubes, faces, seconds=secs.value)
+
+    def vertex_attributes(self, o, vertices, threads=0):
+        v = self._pts(vertices)
+        normals = np.empty_like(v)
+        colors = np.empty(v.shape, np.uint8) if self._oct_paint(o) else None
+        self._attrs(o, v.shape[0], v, threads, normals,
+                    colors.ctypes.data_as(C.c_void_p) if colors is not None else None)
+        return normals, colors
+
+    def export_mesh(self, spec, grid, threads=0, faithful=False) -> Mesh:
+        """Octree(0.25) -> surface nets -> gradient normals + colours, as MeshExportThread
+        and WritePLY(Octree, ...) do (export.cpp:283-381)."""
+        h = self.build(spec)
+        try:
+            o = self.octree(h)
+            if o is None:
+                raise ValueError("tree has infinite or empty bounds")
+            try:
+                m = self.surface_nets(o, grid, threads, faithful)
+                m.normals, m.colors = self.vertex_attributes(o, m.vertices, threads)
+                return m
+            finally:
+                self.octree_free(o)
+        finally:
+            self.free(h)
+
+    def raymarch(self, h, origins, dirs, iterations=100, epsilon=1e-3, threads=0):
+        o = self._pts(origins)
+        d = self._pts(dirs)
+        n = o.shape[0]
+        hit = np.empty(n, np.uint8)
+        travel = np.empty(n, np.float32)
+        pos = np.empty((n, 3), np.float32)
+        self._raymarch(h, n, o, d, iterations, epsilon, threads, hit, travel, pos)
+        return hit.astype(bool), travel, pos
+
+
+class ReferenceOracle(CpuOracle):
+    def __init__(self, path: Path = REF_SO):
+        super().__init__(path, "ref_")
+        vp, i64, f, i = C.c_void_p, C.c_int64, C.c_float, C.c_int
+        self._oct_grid = self._fn("octree_grid", None, [vp, f, f, f, f, f, f, i64, i64, i64, _f32p])
+        self._sn = self._fn("surface_nets", i64, [vp, f, f, f, f, f, f, i64, i64, i64, i,
+                                                  C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_uint64)),
+                                                  C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(C.c_int64), C.POINTER(C.c_double)])
+        self._export_file = self._fn("mesh_export_file", None, [vp, f, f, f, f, f, f, f, i, C.c_char_p])
+        self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
+
+    def octree_grid(self, o, grid):
+        nx, ny, nz = grid.sx + 1, grid.sy + 1, grid.sz + 1
+        out = np.empty(nx * ny * nz, np.float32)
+        self._oct_grid(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, nx, ny, nz, out)
+        return out.reshape(nz, ny, nx)
+
+    def surface_nets(self, o, grid, threads=1) -> Mesh:
+        V = C.POINTER(C.c_float)()
+        Cb = C.POINTER(C.c_uint64)()
+        F = C.POINTER(C.c_uint64)()
+        nf = C.c_int64()
+        secs = C.c_double()
+        nv = self._sn(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, grid.sx, grid.sy, grid.sz,
+                      threads, C.byref(V), C.byref(Cb), C.byref(F), C.byref(nf), C.byref(secs))
+        verts = np.ctypeslib.as_array(V, shape=(max(1, nv) * 3,))[: nv * 3].reshape(nv, 3).copy()
+        cubes = np.ctypeslib.as_array(Cb, shape=(max(1, nv),))[:nv].copy()
+        faces = np.ctypeslib.as_array(F, shape=(max(1, nf.value) * 3,))[: nf.value * 3].reshape(nf.value, 3).copy()
+        for b in (V, Cb, F):
+            self._free_buffer(C.cast(b, C.c_void_p))
+        return Mesh(verts, cubes, faces, seconds=secs.value)
+
+    def export_file(self, h, lo, hi, step, path, fmt="ply"):
+        self._export_file(h, *[float(v) for v in lo], *[float(v) for v in hi], float(step),
+                          1 if fmt == "ply" else 0, str(path).encode())
+
+    def raymarch(self, h, origins, dirs, iterations=100, epsilon=1e-3, threads=0):
+        o = self._pts(origins)
+        d = self._pts(dirs)
+        n = o.shape[0]
+        hit = np.empty(n, np.uint8)
+        travel = np.empty(n, np.float32)
+        pos = np.empty((n, 3), np.float32)
+        self._raymarch(h, n, o, d, iterations, epsilon, threads, hit, travel, pos)
+        return hit.astype(bool), travel, pos
+
+
+def port() -> PortOracle:
+    if not PORT_SO.exists():
+        build_port()
+    return PortOracle()
+
+
+def reference() -> ReferenceOracle | None:
+    if not REF_SO.exists():
+        if build_reference() is None:
+            return None
+    return ReferenceOracle()
+
+
+def read_ply(path):
+    """Parses the binary PLY that WritePLY (tangerine/export.cpp:198-280) writes."""
+    data = Path(path).read_bytes()
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    header = data[:end].decode()
+    nv = nf = 0
+    color = "property uchar red" in header
+    for line in header.splitlines():
+        if line.startswith("element vertex"):
+            nv = int(line.split()[-1])
+        if line.startswith("element face"):
+            nf = int(line.split()[-1])
+    vdt = [("p", "<f4", 3), ("n", "<f4", 3)] + ([("c", "u1", 3)] if color else [])
+    vert = np.frombuffer(data, dtype=np.dtype(vdt), count=nv, offset=end)
+    off = end + vert.nbytes
+    fdt = np.dtype([("k", "u1"), ("i", "<u4", 3)])
+    faces = np.frombuffer(data, dtype=fdt, count=nf, offset=off)
+    return header, vert["p"].copy(), vert["n"].copy(), (vert["c"].copy() if color else None), faces["i"].astype(np.uint64)

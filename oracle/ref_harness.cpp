@@ -1,0 +1,583 @@
+// Test infrastructure only: a thin extern "C" harness over Tangerine's own CPU code,
+// compiled together with the reference sources (tangerine/sdf_evaluator.cpp, export.cpp,
+// third_party/naive-surface-nets, ...) by oracle/Makefile into oracle/_ref/.
+// It is used to pin the C restatement in oracle/port and to write the golden fixtures
+// under tests/golden.  Nothing in the product links or loads it.
+//
+// Trees are built from a "tree spec": a postfix word stream (float32 words, opcodes are
+// small integers stored as floats) that is executed on a stack of SDFNodeShared using the
+// reference's SDF:: constructors and SDFNode mutators (tangerine/sdf_evaluator.h:223-264).
+
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <chrono>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "sdf_evaluator.h"
+#include "material.h"
+#include "export.h"
+#include "painting_set.h"
+#include "threadpool.h"
+#include <surface_nets.h>
+
+using namespace glm;
+
+// painting_set.h declares this; the export path we call never uses it (MeshExport with
+// an explicit evaluator does not read the painting set).
+void PaintingSet::GlobalApply(std::function<void(SDFModelShared)>& Thunk) {}
+
+// Globals owned by tangerine/export.cpp (export.cpp:48-57).
+extern std::atomic_bool ExportActive;
+extern std::atomic_int ExportState;
+extern std::atomic_int VoxelCount;
+extern std::atomic_int GenerationProgress;
+extern std::atomic_int RefinementProgress;
+extern std::atomic_int WriteProgress;
+void MeshExportThread(SDFNodeShared Evaluator, vec3 ModelMin, vec3 ModelMax, vec3 Step, int RefineIterations, std::string Path, ExportFormat Format, float Scale);
+
+namespace
+{
+	enum SpecOp
+	{
+		S_SPHERE = 1, S_ELLIPSOID, S_BOX, S_TORUS, S_CYLINDER, S_PLANE, S_CONE, S_CONINDER,
+		S_UNION, S_DIFF, S_INTER, S_BUNION, S_BDIFF, S_BINTER, S_FLATE,
+		S_MOVE, S_ROTATE, S_SCALE, S_PAINT, S_ALIGN, S_STENCIL,
+	};
+
+	struct RefTree
+	{
+		SDFNodeShared Root;
+	};
+
+	struct RefOctree
+	{
+		SDFOctreeShared Octree;
+	};
+
+	int Arity(int Op)
+	{
+		switch (Op)
+		{
+		case S_SPHERE: return 1;
+		case S_ELLIPSOID: case S_BOX: case S_PLANE: return 3;
+		case S_TORUS: case S_CYLINDER: case S_CONE: return 2;
+		case S_CONINDER: return 3;
+		case S_UNION: case S_DIFF: case S_INTER: return 0;
+		case S_BUNION: case S_BDIFF: case S_BINTER: case S_FLATE: return 1;
+		case S_MOVE: return 3;
+		case S_ROTATE: return 4;
+		case S_SCALE: return 1;
+		case S_PAINT: return 3;
+		case S_ALIGN: return 3;
+		case S_STENCIL: return 4;
+		default: return -1;
+		}
+	}
+
+	SDFNodeShared BuildSpec(const float* Spec, int Count)
+	{
+		std::vector<SDFNodeShared> Stack;
+		int i = 0;
+		while (i < Count)
+		{
+			const int Op = (int)Spec[i++];
+			const int N = Arity(Op);
+			if (N < 0 || i + N > Count)
+			{
+				return nullptr;
+			}
+			const float* P = Spec + i;
+			i += N;
+			auto Pop = [&]() -> SDFNodeShared
+			{
+				SDFNodeShared Top = Stack.back();
+				Stack.pop_back();
+				return Top;
+			};
+			switch (Op)
+			{
+			case S_SPHERE: Stack.push_back(SDF::Sphere(P[0])); break;
+			case S_ELLIPSOID: Stack.push_back(SDF::Ellipsoid(P[0], P[1], P[2])); break;
+			case S_BOX: Stack.push_back(SDF::Box(P[0], P[1], P[2])); break;
+			case S_TORUS: Stack.push_back(SDF::Torus(P[0], P[1])); break;
+			case S_CYLINDER: Stack.push_back(SDF::Cylinder(P[0], P[1])); break;
+			case S_PLANE: Stack.push_back(SDF::Plane(P[0], P[1], P[2])); break;
+			case S_CONE: Stack.push_back(SDF::Cone(P[0], P[1])); break;
+			case S_CONINDER: Stack.push_back(SDF::Coninder(P[0], P[1], P[2])); break;
+			case S_UNION: case S_DIFF: case S_INTER:
+			case S_BUNION: case S_BDIFF: case S_BINTER:
+			{
+				if (Stack.size() < 2) return nullptr;
+				SDFNodeShared RHS = Pop();
+				SDFNodeShared LHS = Pop();
+				SDFNodeShared Out;
+				if (Op == S_UNION) Out = SDF::Union(LHS, RHS);
+				else if (Op == S_DIFF) Out = SDF::Diff(LHS, RHS);
+				else if (Op == S_INTER) Out = SDF::Inter(LHS, RHS);
+				else if (Op == S_BUNION) Out = SDF::BlendUnion(P[0], LHS, RHS);
+				else if (Op == S_BDIFF) Out = SDF::BlendDiff(P[0], LHS, RHS);
+				else Out = SDF::BlendInter(P[0], LHS, RHS);
+				Stack.push_back(Out);
+				break;
+			}
+			case S_FLATE:
+			{
+				if (Stack.empty()) return nullptr;
+				SDFNodeShared Child = Pop();
+				Stack.push_back(SDF::Flate(Child, P[0]));
+				break;
+			}
+			case S_MOVE:
+				if (Stack.empty()) return nullptr;
+				Stack.back()->Move(vec3(P[0], P[1], P[2]));
+				break;
+			case S_ROTATE:
+				// Same argument order as RotateTree (c_sdf.cpp:93-98): quat(W, X, Y, Z).
+				if (Stack.empty()) return nullptr;
+				Stack.back()->Rotate(quat(P[3], P[0], P[1], P[2]));
+				break;
+			case S_SCALE:
+				if (Stack.empty()) return nullptr;
+				Stack.back()->Scale(P[0]);
+				break;
+			case S_PAINT:
+			{
+				if (Stack.empty()) return nullptr;
+				MaterialShared Material = MaterialShared(new MaterialPBRBR(ColorPoint(vec3(P[0], P[1], P[2]))));
+				Stack.back()->ApplyMaterial(Material, false);
+				break;
+			}
+			case S_ALIGN:
+				if (Stack.empty()) return nullptr;
+				SDF::Align(Stack.back(), vec3(P[0], P[1], P[2]));
+				break;
+			case S_STENCIL:
+			{
+				if (Stack.size() < 2) return nullptr;
+				SDFNodeShared Mask = Pop();
+				SDFNodeShared Node = Pop();
+				MaterialShared Material = MaterialShared(new MaterialPBRBR(ColorPoint(vec3(P[1], P[2], P[3]))));
+				Stack.push_back(SDF::Stencil(Node, Mask, Material, P[0] != 0.0f));
+				break;
+			}
+			default:
+				return nullptr;
+			}
+		}
+		if (Stack.size() != 1)
+		{
+			return nullptr;
+		}
+		return Stack.back();
+	}
+
+	void ColorBytes(MaterialShared Material, uint8_t* Out)
+	{
+		// Same arithmetic as WritePLY(Octree, ...) (export.cpp:303-311).
+		vec3 Color = vec3(1.0f);
+		if (Material)
+		{
+			Color = SampleColor(Material->GuessColor());
+		}
+		Out[0] = 0xFF * Color.r;
+		Out[1] = 0xFF * Color.g;
+		Out[2] = 0xFF * Color.b;
+	}
+
+	struct OctreeDump
+	{
+		std::vector<float> Nodes;        // per node: pivot xyz, bounds min xyz, max xyz, terminus, has_eval, program offset, program length, stack size
+		std::vector<int32_t> Children;   // per node: 8 child indices (-1 = none)
+		std::vector<uint32_t> Words;     // concatenated programs
+	};
+
+	int DumpNode(SDFOctree* Node, OctreeDump& Out)
+	{
+		const int Index = (int)(Out.Children.size() / 8);
+		for (int c = 0; c < 8; ++c) Out.Children.push_back(-1);
+		const size_t Base = Out.Nodes.size();
+		Out.Nodes.resize(Base + 14);
+		float* N = &Out.Nodes[Base];
+		N[0] = Node->Pivot.x; N[1] = Node->Pivot.y; N[2] = Node->Pivot.z;
+		N[3] = Node->Bounds.Min.x; N[4] = Node->Bounds.Min.y; N[5] = Node->Bounds.Min.z;
+		N[6] = Node->Bounds.Max.x; N[7] = Node->Bounds.Max.y; N[8] = Node->Bounds.Max.z;
+		N[9] = Node->Terminus ? 1.0f : 0.0f;
+		N[10] = Node->Evaluator ? 1.0f : 0.0f;
+		N[11] = (float)Out.Words.size();
+		N[12] = 0.0f;
+		N[13] = 0.0f;
+		if (Node->Interpreter)
+		{
+			const ProgramBuffer& Program = Node->Interpreter->Program;
+			for (size_t w = 0; w < Program.Size(); ++w)
+			{
+				uint32_t Bits;
+				std::memcpy(&Bits, &Program.Words[w], 4);
+				Out.Words.push_back(Bits);
+			}
+			Out.Nodes[Base + 12] = (float)Program.Size();
+			Out.Nodes[Base + 13] = (float)Node->Interpreter->StackSize;
+		}
+		if (!Node->Terminus)
+		{
+			for (int c = 0; c < 8; ++c)
+			{
+				if (Node->Children[c])
+				{
+					const int ChildIndex = DumpNode(Node->Children[c], Out);
+					Out.Children[Index * 8 + c] = ChildIndex;
+				}
+			}
+		}
+		return Index;
+	}
+
+	template<typename T>
+	T* CopyOut(const std::vector<T>& In)
+	{
+		T* Out = (T*)std::malloc(std::max<size_t>(1, In.size()) * sizeof(T));
+		if (!In.empty()) std::memcpy(Out, In.data(), In.size() * sizeof(T));
+		return Out;
+	}
+
+	struct MeshOut
+	{
+		std::vector<float> Vertices;
+		std::vector<uint64_t> CubeOfVertex;
+		std::vector<uint64_t> Faces;
+	};
+}
+
+extern "C"
+{
+	void* ref_build(const float* Spec, int Count)
+	{
+		SDFNodeShared Root = BuildSpec(Spec, Count);
+		if (!Root) return nullptr;
+		return new RefTree{ Root };
+	}
+
+	void ref_free(void* Handle)
+	{
+		delete (RefTree*)Handle;
+	}
+
+	void ref_free_buffer(void* Buffer)
+	{
+		std::free(Buffer);
+	}
+
+	int ref_stack_size(void* Handle)
+	{
+		return (int)((RefTree*)Handle)->Root->StackSize;
+	}
+
+	int ref_has_paint(void* Handle)
+	{
+		return ((RefTree*)Handle)->Root->HasPaint() ? 1 : 0;
+	}
+
+	int ref_has_finite_bounds(void* Handle)
+	{
+		return ((RefTree*)Handle)->Root->HasFiniteBounds() ? 1 : 0;
+	}
+
+	int ref_leaf_count(void* Handle)
+	{
+		return ((RefTree*)Handle)->Root->LeafCount();
+	}
+
+	void ref_bounds(void* Handle, float* Out, int Inner)
+	{
+		SDFNodeShared& Root = ((RefTree*)Handle)->Root;
+		AABB B = Inner ? Root->InnerBounds() : Root->Bounds();
+		Out[0] = B.Min.x; Out[1] = B.Min.y; Out[2] = B.Min.z;
+		Out[3] = B.Max.x; Out[4] = B.Max.y; Out[5] = B.Max.z;
+	}
+
+	// Virtual SDFNode::Eval over n points.
+	void ref_eval(void* Handle, int64_t Count, const float* Points, float* Out)
+	{
+		SDFNodeShared& Root = ((RefTree*)Handle)->Root;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			Out[i] = Root->Eval(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2]));
+		}
+	}
+
+	void ref_gradient(void* Handle, int64_t Count, const float* Points, float* Out)
+	{
+		SDFNodeShared& Root = ((RefTree*)Handle)->Root;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			vec3 G = Root->Gradient(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2]));
+			Out[i * 3 + 0] = G.x; Out[i * 3 + 1] = G.y; Out[i * 3 + 2] = G.z;
+		}
+	}
+
+	void ref_color(void* Handle, int64_t Count, const float* Points, uint8_t* Out)
+	{
+		SDFNodeShared& Root = ((RefTree*)Handle)->Root;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			ColorBytes(Root->GetMaterial(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2])), Out + i * 3);
+		}
+	}
+
+	// Full-tree program words (SDFInterpreter ctor, sdf_evaluator.cpp:1376-1383).
+	int ref_compile(void* Handle, uint32_t* Out, int Capacity)
+	{
+		SDFInterpreter Interpreter(((RefTree*)Handle)->Root);
+		const int Size = (int)Interpreter.Program.Size();
+		for (int i = 0; i < Size && i < Capacity; ++i)
+		{
+			std::memcpy(&Out[i], &Interpreter.Program.Words[i], 4);
+		}
+		return Size;
+	}
+
+	void ref_interp_eval(void* Handle, int64_t Count, const float* Points, float* Out)
+	{
+		SDFInterpreter Interpreter(((RefTree*)Handle)->Root);
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			Out[i] = Interpreter.Eval(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2]));
+		}
+	}
+
+	void* ref_clip(void* Handle, float X, float Y, float Z, float Radius)
+	{
+		SDFNodeShared Clipped = ((RefTree*)Handle)->Root->Clip(vec3(X, Y, Z), Radius);
+		if (!Clipped) return nullptr;
+		return new RefTree{ Clipped };
+	}
+
+	int ref_equal(void* A, void* B)
+	{
+		return (*((RefTree*)A)->Root == *((RefTree*)B)->Root) ? 1 : 0;
+	}
+
+	void* ref_octree_create(void* Handle, float TargetSize, int Coalesce, int MaxDepth)
+	{
+		SDFOctreeShared Octree = SDFOctree::Create(((RefTree*)Handle)->Root, TargetSize, Coalesce != 0, MaxDepth);
+		if (!Octree) return nullptr;
+		return new RefOctree{ Octree };
+	}
+
+	void ref_octree_free(void* Handle)
+	{
+		delete (RefOctree*)Handle;
+	}
+
+	// Dumps the octree in depth-first order.  Returns the node count; the three buffers
+	// are malloc'd and must be released with ref_free_buffer.
+	int ref_octree_dump(void* Handle, float** Nodes, int32_t** Children, uint32_t** Words, int* WordCount)
+	{
+		OctreeDump Dump;
+		DumpNode(((RefOctree*)Handle)->Octree.get(), Dump);
+		*Nodes = CopyOut(Dump.Nodes);
+		*Children = CopyOut(Dump.Children);
+		*Words = CopyOut(Dump.Words);
+		*WordCount = (int)Dump.Words.size();
+		return (int)(Dump.Children.size() / 8);
+	}
+
+	void ref_octree_eval(void* Handle, int64_t Count, const float* Points, int Exact, float* Out)
+	{
+		SDFOctreeShared& Octree = ((RefOctree*)Handle)->Octree;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			Out[i] = Octree->Eval(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2]), Exact != 0);
+		}
+	}
+
+	// Evaluates SDFOctree::Eval(p, Exact=true) on the export lattice
+	// p = (x0 + i*dx, y0 + j*dy, z0 + k*dz), i fastest, using all host threads.
+	void ref_octree_grid(void* Handle, float X0, float Y0, float Z0, float DX, float DY, float DZ,
+		int64_t NX, int64_t NY, int64_t NZ, float* Out)
+	{
+		SDFOctreeShared& Octree = ((RefOctree*)Handle)->Octree;
+		std::atomic<int64_t> NextSlice(0);
+		Pool([&]()
+		{
+			for (int64_t k = NextSlice.fetch_add(1); k < NZ; k = NextSlice.fetch_add(1))
+			{
+				const float Z = Z0 + static_cast<float>(k) * DZ;
+				for (int64_t j = 0; j < NY; ++j)
+				{
+					const float Y = Y0 + static_cast<float>(j) * DY;
+					for (int64_t i = 0; i < NX; ++i)
+					{
+						const float X = X0 + static_cast<float>(i) * DX;
+						Out[(k * NY + j) * NX + i] = Octree->Eval(vec3(X, Y, Z));
+					}
+				}
+			}
+		});
+	}
+
+	void ref_octree_gradient(void* Handle, int64_t Count, const float* Points, float* Out)
+	{
+		SDFOctreeShared& Octree = ((RefOctree*)Handle)->Octree;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			vec3 G = Octree->Gradient(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2]));
+			Out[i * 3 + 0] = G.x; Out[i * 3 + 1] = G.y; Out[i * 3 + 2] = G.z;
+		}
+	}
+
+	void ref_octree_color(void* Handle, int64_t Count, const float* Points, uint8_t* Out)
+	{
+		SDFOctreeShared& Octree = ((RefOctree*)Handle)->Octree;
+		for (int64_t i = 0; i < Count; ++i)
+		{
+			ColorBytes(Octree->GetMaterial(vec3(Points[i * 3 + 0], Points[i * 3 + 1], Points[i * 3 + 2])), Out + i * 3);
+		}
+	}
+
+	// Runs Tangerine's naive surface nets (the AsyncParallelSurfaceNets thunks that
+	// par_surface_nets drives, surface_nets.cpp:1148-1205) over the export octree, with
+	// the z-slices and then the active-cell map entries spread over Pool() threads.
+	// Returns the vertex count; vertex positions (3 floats each), the active cube index of
+	// each vertex and the faces (3 vertex indices each) are malloc'd.
+	int64_t ref_surface_nets(void* Handle, float X0, float Y0, float Z0, float DX, float DY, float DZ,
+		int64_t SX, int64_t SY, int64_t SZ, int Threads,
+		float** Vertices, uint64_t** Cubes, uint64_t** Faces, int64_t* FaceCount, double* Seconds)
+	{
+		SDFOctreeShared Octree = ((RefOctree*)Handle)->Octree;
+		auto Start = std::chrono::steady_clock::now();
+
+		isosurface::AsyncParallelSurfaceNets Task;
+		Task.ImplicitFunction = [Octree](float X, float Y, float Z) -> float
+		{
+			return Octree->Eval(vec3(X, Y, Z));
+		};
+		Task.Grid.x = X0; Task.Grid.y = Y0; Task.Grid.z = Z0;
+		Task.Grid.dx = DX; Task.Grid.dy = DY; Task.Grid.dz = DZ;
+		Task.Grid.sx = SX; Task.Grid.sy = SY; Task.Grid.sz = SZ;
+		Task.Setup();
+
+		auto RunThreads = [&](const std::function<void()>& Thunk)
+		{
+			if (Threads <= 0)
+			{
+				Pool(Thunk);
+			}
+			else
+			{
+				std::vector<std::thread> Workers;
+				for (int t = 0; t < Threads; ++t) Workers.emplace_back(Thunk);
+				for (auto& W : Workers) W.join();
+			}
+		};
+
+		std::atomic<size_t> Next(0);
+		RunThreads([&]()
+		{
+			for (size_t n = Next.fetch_add(1); n < Task.FirstLoopDomain.size(); n = Next.fetch_add(1))
+			{
+				Task.FirstLoopThunk(Task, Task.FirstLoopDomain[n]);
+			}
+		});
+
+		std::vector<std::pair<const size_t, uint64_t>*> Entries;
+		Entries.reserve(Task.SecondLoopDomain.size());
+		for (auto& Entry : Task.SecondLoopDomain) Entries.push_back(&Entry);
+		Next.store(0);
+		RunThreads([&]()
+		{
+			for (size_t n = Next.fetch_add(1); n < Entries.size(); n = Next.fetch_add(1))
+			{
+				Task.SecondLoopThunk(Task, *Entries[n]);
+			}
+		});
+
+		*Seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - Start).count();
+
+		const size_t VertexCount = Task.OutputMesh.vertices_.size();
+		std::vector<float> V(VertexCount * 3);
+		std::vector<uint64_t> C(VertexCount, ~uint64_t(0));
+		for (size_t v = 0; v < VertexCount; ++v)
+		{
+			V[v * 3 + 0] = Task.OutputMesh.vertices_[v].x;
+			V[v * 3 + 1] = Task.OutputMesh.vertices_[v].y;
+			V[v * 3 + 2] = Task.OutputMesh.vertices_[v].z;
+		}
+		for (auto& Entry : Task.SecondLoopDomain)
+		{
+			C[Entry.second] = Entry.first;
+		}
+		std::vector<uint64_t> F;
+		F.reserve(Task.OutputMesh.faces_.size() * 3);
+		for (auto& Face : Task.OutputMesh.faces_)
+		{
+			F.push_back(Face.v0); F.push_back(Face.v1); F.push_back(Face.v2);
+		}
+		*Vertices = CopyOut(V);
+		*Cubes = CopyOut(C);
+		*Faces = CopyOut(F);
+		*FaceCount = (int64_t)Task.OutputMesh.faces_.size();
+		return (int64_t)VertexCount;
+	}
+
+	// The reference's own export entry (export.cpp:320-381) writing a PLY or STL file:
+	// octree, surface nets, gradient normals, material colours, writer.
+	void ref_mesh_export_file(void* Handle, float MinX, float MinY, float MinZ, float MaxX, float MaxY, float MaxZ,
+		float Step, int Format, const char* Path)
+	{
+		ExportActive.store(true);
+		ExportState.store(1);
+		GenerationProgress.store(0);
+		RefinementProgress.store(0);
+		WriteProgress.store(0);
+		MeshExportThread(((RefTree*)Handle)->Root, vec3(MinX, MinY, MinZ), vec3(MaxX, MaxY, MaxZ), vec3(Step), 0,
+			std::string(Path), Format == 0 ? ExportFormat::STL : ExportFormat::PLY, 1.0f);
+	}
+
+	// SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the full tree.
+	void ref_raymarch(void* Handle, int64_t Count, const float* Origins, const float* Dirs, int MaxIterations, float Epsilon,
+		int Threads, uint8_t* Hit, float* Travel, float* Position)
+	{
+		SDFNodeShared Root = ((RefTree*)Handle)->Root;
+		std::atomic<int64_t> Next(0);
+		auto Thunk = [&]()
+		{
+			for (int64_t i = Next.fetch_add(64); i < Count; i = Next.fetch_add(64))
+			{
+				for (int64_t r = i; r < std::min<int64_t>(Count, i + 64); ++r)
+				{
+					RayHit H = Root->RayMarch(vec3(Origins[r * 3], Origins[r * 3 + 1], Origins[r * 3 + 2]),
+						vec3(Dirs[r * 3], Dirs[r * 3 + 1], Dirs[r * 3 + 2]), MaxIterations, Epsilon);
+					Hit[r] = H.Hit ? 1 : 0;
+					Travel[r] = H.Travel;
+					Position[r * 3 + 0] = H.Position.x;
+					Position[r * 3 + 1] = H.Position.y;
+					Position[r * 3 + 2] = H.Position.z;
+				}
+			}
+		};
+		if (Threads <= 0)
+		{
+			Pool(Thunk);
+		}
+		else
+		{
+			std::vector<std::thread> Workers;
+			for (int t = 0; t < Threads; ++t) Workers.emplace_back(Thunk);
+			for (auto& W : Workers) W.join();
+		}
+	}
+
+	int ref_hardware_threads()
+	{
+		return (int)std::thread::hardware_concurrency();
+	}
+}
