@@ -1,0 +1,228 @@
+/*
+ * tangerine_gb300 -- C ABI of the GB300 (sm_103a) CSG evaluation and export-meshing engine.
+ *
+ * Two layers:
+ *
+ *  1. Tangerine's own C API for CSG trees (tangerine/c_sdf.cpp:27-180 and the export entry
+ *     points tangerine/export.cpp:611-621), which the reference ships disabled (#if 0) and
+ *     which its Racket FFI binds (package/tangerine/eval.rkt:39-68, export.rkt:26-28).
+ *     Same names, argument order and meaning.  Handles are reference-counted trees: an
+ *     operator (Make*Op) takes over the references of its operand handles, as the raw
+ *     pointer API did, so a caller discards only the root.  ClipTree returns a new handle.
+ *
+ *  2. The GPU-native entry points (tg_*): compile a tree into octree cells and record
+ *     programs once, then evaluate lattices and export meshes on the GPU.  Every tg_* call
+ *     returns a tg_status (0 = success); tg_last_error() describes the last failure on the
+ *     calling thread.  Calls on one program are thread-compatible, not thread-safe.
+ *
+ * All pointers are plain host pointers unless a parameter says "device".  `stream` is a
+ * cudaStream_t (NULL: the library's own stream); calls return after their work on that
+ * stream has finished.
+ */
+#ifndef TANGERINE_GB300_H
+#define TANGERINE_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define TANGERINE_API __declspec(dllexport)
+#else
+#define TANGERINE_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Tangerine's C API (tangerine/c_sdf.cpp) ----------------------------------------- */
+
+/* SDFNode::RayMarch result (tangerine/sdf_evaluator.h:75-80). */
+typedef struct RayHit
+{
+	bool Hit;
+	float Travel;
+	float Position[3];
+} RayHit;
+
+/* EvalTree: SDFNode::Eval at one point (c_sdf.cpp:30-34). */
+TANGERINE_API float EvalTree(void* Handle, float X, float Y, float Z);
+/* ClipTree: the subtree that can matter within Radius of the point; NULL when nothing
+ * does, or when the clipped tree's distance there exceeds Radius (c_sdf.cpp:38-53). */
+TANGERINE_API void* ClipTree(void* Handle, float X, float Y, float Z, float Radius);
+/* RayMarchTree: sphere tracing on the full tree (c_sdf.cpp:56-66). */
+TANGERINE_API RayHit RayMarchTree(void* Handle, float RayStartX, float RayStartY, float RayStartZ,
+                                  float RayDirX, float RayDirY, float RayDirZ, int MaxIterations, float Epsilon);
+/* DiscardTree: drop this handle's reference (c_sdf.cpp:70-74). */
+TANGERINE_API void DiscardTree(void* Handle);
+/* TreeHasFiniteBounds (c_sdf.cpp:77-80). */
+TANGERINE_API bool TreeHasFiniteBounds(void* Handle);
+/* MoveTree / RotateTree (quat(W, X, Y, Z)) / AlignTree (c_sdf.cpp:86-106). */
+TANGERINE_API void MoveTree(void* Handle, float X, float Y, float Z);
+TANGERINE_API void RotateTree(void* Handle, float X, float Y, float Z, float W);
+TANGERINE_API void AlignTree(void* Handle, float X, float Y, float Z);
+/* PaintTree: a new sRGB material on every unpainted brush (c_sdf.cpp:110-114). */
+TANGERINE_API void PaintTree(float Red, float Green, float Blue, void* Handle);
+/* Brushes (c_sdf.cpp:118-146): half-extents and radii as SDF:: takes them. */
+TANGERINE_API void* MakeSphereBrush(float Radius);
+TANGERINE_API void* MakeEllipsoidBrush(float RadipodeX, float RadipodeY, float RadipodeZ);
+TANGERINE_API void* MakeBoxBrush(float ExtentX, float ExtentY, float ExtentZ);
+TANGERINE_API void* MakeTorusBrush(float MajorRadius, float MinorRadius);
+TANGERINE_API void* MakeCylinderBrush(float Radius, float Extent);
+TANGERINE_API void* MakePlaneOperand(float NormalX, float NormalY, float NormalZ);
+/* Set operators (c_sdf.cpp:150-178); they take over the operand handles. */
+TANGERINE_API void* MakeUnionOp(void* LHS, void* RHS);
+TANGERINE_API void* MakeDiffOp(void* LHS, void* RHS);
+TANGERINE_API void* MakeInterOp(void* LHS, void* RHS);
+TANGERINE_API void* MakeBlendUnionOp(float Threshold, void* LHS, void* RHS);
+TANGERINE_API void* MakeBlendDiffOp(float Threshold, void* LHS, void* RHS);
+TANGERINE_API void* MakeBlendInterOp(float Threshold, void* LHS, void* RHS);
+
+/* The rest of SDF:: (tangerine/sdf_evaluator.h:223-264) that c_sdf.cpp never exposed. */
+TANGERINE_API void* MakeConeBrush(float Radius, float Height);
+TANGERINE_API void* MakeConinderBrush(float RadiusL, float RadiusH, float Height);
+TANGERINE_API void* MakeFlateOp(void* Handle, float Radius);
+TANGERINE_API void* MakeStencilOp(void* Handle, void* Mask, float Red, float Green, float Blue, bool ApplyToNegative);
+TANGERINE_API void ScaleTree(void* Handle, float Scale);
+/* Replays a tree spec: the postfix construction word stream tangerine_gb300.workloads
+ * writes (op codes there).  NULL on a malformed spec (tg_last_error explains). */
+TANGERINE_API void* BuildTreeFromSpec(const float* Spec, int Count);
+
+/* Export the tree's bounds at 1/GridSize spacing to a file, synchronously
+ * (ExportCommon + MeshExportThread, tangerine/export.cpp:320-381, 595-621).
+ * RefineIterations is accepted and unused, as in the reference mesh export. */
+TANGERINE_API void ExportSTL(void* Handle, float GridSize, int RefineIterations, const char* Path);
+TANGERINE_API void ExportPLY(void* Handle, float GridSize, int RefineIterations, const char* Path);
+
+/* ---- GPU-native API ----------------------------------------------------------------- */
+
+typedef int tg_status;
+enum
+{
+	TG_OK = 0,
+	TG_ERR_INVALID = 1,      /* bad argument */
+	TG_ERR_UNBOUNDED = 2,    /* tree has infinite or empty bounds */
+	TG_ERR_CUDA = 3,         /* CUDA runtime error (no GPU, launch failure, ...) */
+	TG_ERR_MEMORY = 4,       /* host or device allocation failed */
+	TG_ERR_IO = 5,           /* file could not be written */
+	TG_ERR_UNSUPPORTED = 6,  /* input outside what the kernels handle */
+};
+
+typedef struct tg_program tg_program;
+
+/* Lattice of sample points x0 + i*step (i < nx), likewise y, z; x varies fastest. */
+typedef struct tg_grid
+{
+	float x0, y0, z0;
+	float step;
+	int64_t nx, ny, nz;
+} tg_grid;
+
+typedef struct tg_program_info
+{
+	int32_t octree_cells;
+	int32_t code_quads;
+	int32_t materials;
+	int32_t has_paint;          /* colours are exported */
+	int32_t max_stack;
+	float bounds_min[3], bounds_max[3];
+	double compile_seconds;
+	int64_t distance_quads;     /* summed over all cells */
+} tg_program_info;
+
+/* A mesh in host memory (library-allocated; release with tg_mesh_free).  Vertex v is the
+ * vertex of active cube cubes[v] (x + y*sx + z*sx*sy); faces are vertex index triples. */
+typedef struct tg_mesh
+{
+	uint64_t vertex_count;
+	uint64_t face_count;
+	float* vertices;            /* 3 per vertex */
+	float* normals;             /* 3 per vertex */
+	uint8_t* colors;            /* 3 per vertex, NULL when the tree has no paint */
+	uint32_t* faces;            /* 3 per face */
+	uint32_t* cubes;            /* 1 per vertex */
+} tg_mesh;
+
+/* The same mesh left in device memory owned by the library (valid until the next export
+ * call on this thread's engine). */
+typedef struct tg_device_mesh
+{
+	uint64_t vertex_count;
+	uint64_t face_count;
+	const float* vertices;      /* device */
+	const float* normals;       /* device */
+	const uint8_t* colors;      /* device, NULL without paint */
+	const uint32_t* faces;      /* device */
+	const uint32_t* cubes;      /* device */
+} tg_device_mesh;
+
+enum
+{
+	TG_MESH_ATTRIBUTES = 1u,    /* compute gradient normals and colours */
+};
+
+/* Builds the export octree (target size 0.25, coalescing) and compiles every cell's
+ * clipped subtree; uploads them to the current device. */
+TANGERINE_API tg_status tg_compile(void* tree, tg_program** out);
+TANGERINE_API void tg_program_free(tg_program* program);
+TANGERINE_API tg_status tg_program_get_info(const tg_program* program, tg_program_info* out);
+/* Distance program words of the whole tree exactly as Tangerine's SDFInterpreter holds
+ * them (for checking).  Returns the word count; copies at most `capacity`. */
+TANGERINE_API int64_t tg_tree_reference_words(void* tree, uint32_t* out, int64_t capacity);
+
+/* Host-only check of the export octree (no GPU needed): the cells depth-first, 14 floats
+ * each (pivot xyz, bounds min xyz, max xyz, terminus, has evaluator, first word, word
+ * count, stack size), 8 child indices each (-1: none), and every cell's distance program
+ * words concatenated.  Returns the cell count (-1 when SDFOctree::Create would fail);
+ * copies at most the given capacities. */
+TANGERINE_API int64_t tg_debug_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
+                                      uint32_t* words, int64_t word_capacity, int64_t* word_count);
+
+/* The lattice MeshExportThread builds for (min, max, step): min moves down two steps;
+ * ceil((max - min) / step) cells, one more lattice point, per axis (export.cpp:324-337). */
+TANGERINE_API tg_status tg_export_grid(const float model_min[3], const float model_max[3], float step, tg_grid* out);
+
+/* SDFOctree::Eval(p, Exact = true) at every lattice point.  `out` holds nx*ny*nz floats,
+ * host memory, or device memory when out_is_device is nonzero. */
+TANGERINE_API tg_status tg_eval_grid(tg_program* program, const tg_grid* grid, float* out, int out_is_device, void* stream);
+
+/* Octree distances at n arbitrary points (host arrays, 3 floats per point). */
+TANGERINE_API tg_status tg_eval_points(tg_program* program, const float* points, int64_t n, float* out, void* stream);
+
+/* Naive surface nets over the lattice (cells between lattice points), then gradient
+ * normals and colours per vertex.  Results in host memory. */
+TANGERINE_API tg_status tg_export_mesh(tg_program* program, const tg_grid* grid, uint32_t flags, tg_mesh* out, void* stream);
+/* Same, results left on the device. */
+TANGERINE_API tg_status tg_export_mesh_device(tg_program* program, const tg_grid* grid, uint32_t flags, tg_device_mesh* out, void* stream);
+TANGERINE_API void tg_mesh_free(tg_mesh* mesh);
+
+/* Whole reference export path from a tree: octree + compile, lattice, surface nets,
+ * normals, colours, copy back to the host (MeshExportThread minus the file write). */
+TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], const float model_max[3], float step,
+                                       tg_mesh* out, void* stream);
+
+/* Files in the reference's byte layout (WritePLY / WriteSTL, export.cpp:60-317).
+ * The STL writer needs the program for its per-face gradient normals. */
+TANGERINE_API tg_status tg_write_ply(const tg_mesh* mesh, const char* path, float scale);
+TANGERINE_API tg_status tg_write_stl(tg_program* program, const tg_mesh* mesh, const char* path, float scale, void* stream);
+
+/* Per-kernel device time of the export pipeline, accumulated while enabled (CUDA events
+ * on the launching stream).  Names: "eval_grid", "cell_flags", "scan", "cell_vertices",
+ * "faces", "attributes", "face_normals", "eval_points". */
+TANGERINE_API void tg_profile_enable(int enable);
+TANGERINE_API int tg_profile_read(const char* kernel, double* total_ms, int64_t* launches);
+TANGERINE_API void tg_profile_reset(void);
+
+/* Measures this GPU's FP32 fused-multiply-add throughput in TFLOP/s (2 flops per FMA):
+ * the compute roofline of the distance interpreter. */
+TANGERINE_API tg_status tg_measure_fp32_peak(double* tflops, void* stream);
+
+TANGERINE_API const char* tg_last_error(void);
+TANGERINE_API const char* tg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

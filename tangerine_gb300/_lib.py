@@ -1,0 +1,132 @@
+"""ctypes binding of libtangerine_gb300.so (the C ABI in include/tangerine_gb300.h).
+
+The library must have been built (``tangerine_gb300.build.build()``); loading fails
+loudly otherwise -- there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libtangerine_gb300.so"
+
+
+class RayHit(C.Structure):
+    _fields_ = [("Hit", C.c_bool), ("Travel", C.c_float), ("Position", C.c_float * 3)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("x0", C.c_float), ("y0", C.c_float), ("z0", C.c_float), ("step", C.c_float),
+                ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64)]
+
+
+class ProgramInfo(C.Structure):
+    _fields_ = [("octree_cells", C.c_int32), ("code_quads", C.c_int32), ("materials", C.c_int32),
+                ("has_paint", C.c_int32), ("max_stack", C.c_int32),
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("compile_seconds", C.c_double), ("distance_quads", C.c_int64)]
+
+
+class HostMesh(C.Structure):
+    _fields_ = [("vertex_count", C.c_uint64), ("face_count", C.c_uint64),
+                ("vertices", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("colors", C.POINTER(C.c_uint8)), ("faces", C.POINTER(C.c_uint32)),
+                ("cubes", C.POINTER(C.c_uint32))]
+
+
+class DeviceMesh(C.Structure):
+    _fields_ = [("vertex_count", C.c_uint64), ("face_count", C.c_uint64),
+                ("vertices", C.c_void_p), ("normals", C.c_void_p), ("colors", C.c_void_p),
+                ("faces", C.c_void_p), ("cubes", C.c_void_p)]
+
+
+# Every exported symbol with its signature: (restype, argtypes).
+_vp, _f, _i, _i64, _u32 = C.c_void_p, C.c_float, C.c_int, C.c_int64, C.c_uint32
+SIGNATURES = {
+    "EvalTree": (_f, [_vp, _f, _f, _f]),
+    "ClipTree": (_vp, [_vp, _f, _f, _f, _f]),
+    "RayMarchTree": (RayHit, [_vp, _f, _f, _f, _f, _f, _f, _i, _f]),
+    "DiscardTree": (None, [_vp]),
+    "TreeHasFiniteBounds": (C.c_bool, [_vp]),
+    "MoveTree": (None, [_vp, _f, _f, _f]),
+    "RotateTree": (None, [_vp, _f, _f, _f, _f]),
+    "AlignTree": (None, [_vp, _f, _f, _f]),
+    "PaintTree": (None, [_f, _f, _f, _vp]),
+    "MakeSphereBrush": (_vp, [_f]),
+    "MakeEllipsoidBrush": (_vp, [_f, _f, _f]),
+    "MakeBoxBrush": (_vp, [_f, _f, _f]),
+    "MakeTorusBrush": (_vp, [_f, _f]),
+    "MakeCylinderBrush": (_vp, [_f, _f]),
+    "MakePlaneOperand": (_vp, [_f, _f, _f]),
+    "MakeUnionOp": (_vp, [_vp, _vp]),
+    "MakeDiffOp": (_vp, [_vp, _vp]),
+    "MakeInterOp": (_vp, [_vp, _vp]),
+    "MakeBlendUnionOp": (_vp, [_f, _vp, _vp]),
+    "MakeBlendDiffOp": (_vp, [_f, _vp, _vp]),
+    "MakeBlendInterOp": (_vp, [_f, _vp, _vp]),
+    "MakeConeBrush": (_vp, [_f, _f]),
+    "MakeConinderBrush": (_vp, [_f, _f, _f]),
+    "MakeFlateOp": (_vp, [_vp, _f]),
+    "MakeStencilOp": (_vp, [_vp, _vp, _f, _f, _f, C.c_bool]),
+    "ScaleTree": (None, [_vp, _f]),
+    "BuildTreeFromSpec": (_vp, [_vp, _i]),
+    "ExportSTL": (None, [_vp, _f, _i, C.c_char_p]),
+    "ExportPLY": (None, [_vp, _f, _i, C.c_char_p]),
+    "tg_compile": (_i, [_vp, C.POINTER(_vp)]),
+    "tg_program_free": (None, [_vp]),
+    "tg_program_get_info": (_i, [_vp, C.POINTER(ProgramInfo)]),
+    "tg_tree_reference_words": (_i64, [_vp, _vp, _i64]),
+    "tg_debug_octree": (_i64, [_vp, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i64)]),
+    "tg_export_grid": (_i, [_vp, _vp, _f, C.POINTER(Grid)]),
+    "tg_eval_grid": (_i, [_vp, C.POINTER(Grid), _vp, _i, _vp]),
+    "tg_eval_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
+    "tg_export_mesh": (_i, [_vp, C.POINTER(Grid), _u32, C.POINTER(HostMesh), _vp]),
+    "tg_export_mesh_device": (_i, [_vp, C.POINTER(Grid), _u32, C.POINTER(DeviceMesh), _vp]),
+    "tg_mesh_free": (None, [C.POINTER(HostMesh)]),
+    "tg_export_tree": (_i, [_vp, _vp, _vp, _f, C.POINTER(HostMesh), _vp]),
+    "tg_write_ply": (_i, [C.POINTER(HostMesh), C.c_char_p, _f]),
+    "tg_write_stl": (_i, [_vp, C.POINTER(HostMesh), C.c_char_p, _f, _vp]),
+    "tg_profile_enable": (None, [_i]),
+    "tg_profile_read": (_i, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),
+    "tg_profile_reset": (None, []),
+    "tg_measure_fp32_peak": (_i, [C.POINTER(C.c_double), _vp]),
+    "tg_last_error": (C.c_char_p, []),
+    "tg_version": (C.c_char_p, []),
+}
+
+_LIB = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Loads the in-tree library and binds every entry point; raises if it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is not built: run tangerine_gb300.build.build() (the GPU path has no fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+class TangerineError(RuntimeError):
+    pass
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        msg = load().tg_last_error()
+        raise TangerineError(f"{what or 'call'} failed (status {status}): {msg.decode() if msg else ''}")
+
+
+def as_ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)

@@ -1,0 +1,513 @@
+// The C ABI (include/tangerine_gb300.h): Tangerine's tree API re-enabled over
+// reference-counted trees, and the GPU-native tg_* entry points.
+#include "../../../include/tangerine_gb300.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "tg_engine.hpp"
+#include "tg_octree.hpp"
+#include "tg_tree.hpp"
+
+using namespace tg;
+
+struct tg_program : public tg::Program {};
+
+namespace
+{
+	Node* AsNode(void* h) { return static_cast<Node*>(h); }
+	NodeRef Borrow(void* h) { return NodeRef::Share(AsNode(h)); }     // caller keeps its reference
+	NodeRef Adopt(void* h) { return NodeRef(AsNode(h)); }             // take over the caller's reference
+	void* Hand(NodeRef r) { return r.release(); }
+
+	tg_status CudaFail(cudaError_t e, const char* what)
+	{
+		SetError(std::string(what) + ": " + cudaGetErrorString(e));
+		return TG_ERR_CUDA;
+	}
+
+	cudaStream_t StreamOf(void* s) { return s ? static_cast<cudaStream_t>(s) : Engine::Get().DefaultStream(); }
+
+	bool ToGridSpec(const tg_grid* g, GridSpec& out)
+	{
+		if (!g || g->nx < 2 || g->ny < 2 || g->nz < 2 || !(g->step > 0.0f))
+		{
+			SetError("a lattice needs at least 2 points per axis and a positive step");
+			return false;
+		}
+		if (g->nx > (1 << 20) || g->ny > (1 << 20) || g->nz > (1 << 20) ||
+			(double)(g->nx - 1) * (double)(g->ny - 1) * (double)(g->nz - 1) >= 4294967296.0)
+		{
+			SetError("lattice too large: cube indices must fit in 32 bits");
+			return false;
+		}
+		out = GridSpec{ g->x0, g->y0, g->z0, g->step, (int)g->nx, (int)g->ny, (int)g->nz };
+		return true;
+	}
+
+	// MeshExportThread's lattice (export.cpp:324-337).
+	void ExportLattice(Vec3 lo, Vec3 hi, float step, tg_grid& g)
+	{
+		lo = lo - Vec3(step) * Vec3(2.0f);
+		const Vec3 ext = (hi - lo) / step;
+		g.x0 = lo.x; g.y0 = lo.y; g.z0 = lo.z;
+		g.step = step;
+		g.nx = (int64_t)std::ceil(ext.x) + 1;
+		g.ny = (int64_t)std::ceil(ext.y) + 1;
+		g.nz = (int64_t)std::ceil(ext.z) + 1;
+	}
+
+	tg_status CopyMeshToHost(const DeviceMesh& dm, tg_mesh* out, cudaStream_t s)
+	{
+		std::memset(out, 0, sizeof *out);
+		out->vertex_count = dm.VertexCount;
+		out->face_count = dm.FaceCount;
+		const size_t v = dm.VertexCount ? dm.VertexCount : 1, f = dm.FaceCount ? dm.FaceCount : 1;
+		out->vertices = (float*)std::malloc(v * 12);
+		out->normals = (float*)std::malloc(v * 12);
+		out->faces = (uint32_t*)std::malloc(f * 12);
+		out->cubes = (uint32_t*)std::malloc(v * 4);
+		out->colors = dm.Colors ? (uint8_t*)std::malloc(v * 3) : nullptr;
+		if (!out->vertices || !out->normals || !out->faces || !out->cubes || (dm.Colors && !out->colors))
+		{
+			tg_mesh_free(out);
+			SetError("out of host memory for the mesh");
+			return TG_ERR_MEMORY;
+		}
+		cudaError_t e = cudaSuccess;
+		if (dm.VertexCount)
+		{
+			e = cudaMemcpyAsync(out->vertices, dm.Vertices, dm.VertexCount * 12, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess && dm.Normals) e = cudaMemcpyAsync(out->normals, dm.Normals, dm.VertexCount * 12, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(out->cubes, dm.Cubes, dm.VertexCount * 4, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess && dm.Colors) e = cudaMemcpyAsync(out->colors, dm.Colors, dm.VertexCount * 3, cudaMemcpyDeviceToHost, s);
+		}
+		if (e == cudaSuccess && dm.FaceCount) e = cudaMemcpyAsync(out->faces, dm.Faces, dm.FaceCount * 12, cudaMemcpyDeviceToHost, s);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+		if (e != cudaSuccess)
+		{
+			tg_mesh_free(out);
+			return CudaFail(e, "copying the mesh to the host");
+		}
+		if (!dm.Normals) std::memset(out->normals, 0, v * 12);
+		return TG_OK;
+	}
+
+	tg_status CompileInto(void* tree, std::unique_ptr<tg_program>& prog)
+	{
+		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
+		prog.reset(new (std::nothrow) tg_program());
+		if (!prog) { SetError("out of host memory"); return TG_ERR_MEMORY; }
+		std::string err;
+		if (!CompileTree(Borrow(tree), prog->Host, err))
+		{
+			SetError(err);
+			return TG_ERR_UNBOUNDED;
+		}
+		cudaError_t e = Engine::Get().Upload(*prog);
+		if (e != cudaSuccess) return CudaFail(e, "uploading the program");
+		return TG_OK;
+	}
+
+	void WriteFileError(const char* path) { SetError(std::string("cannot write ") + (path ? path : "(null)")); }
+}
+
+extern "C"
+{
+	// ---- tree API (tangerine/c_sdf.cpp) -------------------------------------------------
+	TANGERINE_API float EvalTree(void* h, float x, float y, float z)
+	{
+		return AsNode(h)->Eval(Vec3(x, y, z));
+	}
+
+	TANGERINE_API void* ClipTree(void* h, float x, float y, float z, float radius)
+	{
+		const Vec3 p(x, y, z);
+		NodeRef clipped = AsNode(h)->Clip(p, radius);
+		if (clipped && std::fabs(clipped->Eval(p)) > radius) return nullptr;
+		return Hand(std::move(clipped));
+	}
+
+	TANGERINE_API ::RayHit RayMarchTree(void* h, float sx, float sy, float sz, float dx, float dy, float dz, int iters, float eps)
+	{
+		const tg::RayHit r = RayMarch(*AsNode(h), Vec3(sx, sy, sz), Vec3(dx, dy, dz), iters, eps);
+		::RayHit out;
+		out.Hit = r.Hit;
+		out.Travel = r.Travel;
+		out.Position[0] = r.Position.x;
+		out.Position[1] = r.Position.y;
+		out.Position[2] = r.Position.z;
+		return out;
+	}
+
+	TANGERINE_API void DiscardTree(void* h) { if (h) Adopt(h); }
+	TANGERINE_API bool TreeHasFiniteBounds(void* h) { return AsNode(h)->HasFiniteBounds(); }
+	TANGERINE_API void MoveTree(void* h, float x, float y, float z) { AsNode(h)->Move(Vec3(x, y, z)); }
+	TANGERINE_API void RotateTree(void* h, float x, float y, float z, float w) { AsNode(h)->Rotate(Quat{ w, x, y, z }); }
+	TANGERINE_API void AlignTree(void* h, float x, float y, float z) { SDF::Align(*AsNode(h), Vec3(x, y, z)); }
+	TANGERINE_API void ScaleTree(void* h, float s) { AsNode(h)->Scale(s); }
+
+	TANGERINE_API void PaintTree(float r, float g, float b, void* h)
+	{
+		auto m = std::make_shared<Material>();
+		m->Rgb[0] = r; m->Rgb[1] = g; m->Rgb[2] = b;
+		AsNode(h)->ApplyMaterial(m, false);
+	}
+
+	TANGERINE_API void* MakeSphereBrush(float r) { return Hand(SDF::Sphere(r)); }
+	TANGERINE_API void* MakeEllipsoidBrush(float x, float y, float z) { return Hand(SDF::Ellipsoid(x, y, z)); }
+	TANGERINE_API void* MakeBoxBrush(float x, float y, float z) { return Hand(SDF::Box(x, y, z)); }
+	TANGERINE_API void* MakeTorusBrush(float major, float minor) { return Hand(SDF::Torus(major, minor)); }
+	TANGERINE_API void* MakeCylinderBrush(float r, float e) { return Hand(SDF::Cylinder(r, e)); }
+	TANGERINE_API void* MakePlaneOperand(float x, float y, float z) { return Hand(SDF::Plane(x, y, z)); }
+	TANGERINE_API void* MakeConeBrush(float r, float h) { return Hand(SDF::Cone(r, h)); }
+	TANGERINE_API void* MakeConinderBrush(float rl, float rh, float h) { return Hand(SDF::Coninder(rl, rh, h)); }
+
+	TANGERINE_API void* MakeUnionOp(void* l, void* r) { return Hand(SDF::Union(Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeDiffOp(void* l, void* r) { return Hand(SDF::Diff(Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeInterOp(void* l, void* r) { return Hand(SDF::Inter(Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeBlendUnionOp(float k, void* l, void* r) { return Hand(SDF::BlendUnion(k, Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeBlendDiffOp(float k, void* l, void* r) { return Hand(SDF::BlendDiff(k, Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeBlendInterOp(float k, void* l, void* r) { return Hand(SDF::BlendInter(k, Adopt(l), Adopt(r))); }
+	TANGERINE_API void* MakeFlateOp(void* h, float r) { return Hand(SDF::Flate(Adopt(h), r)); }
+
+	TANGERINE_API void* MakeStencilOp(void* h, void* mask, float r, float g, float b, bool negative)
+	{
+		auto m = std::make_shared<Material>();
+		m->Rgb[0] = r; m->Rgb[1] = g; m->Rgb[2] = b;
+		return Hand(SDF::Stencil(Adopt(h), Adopt(mask), m, negative));
+	}
+
+	TANGERINE_API void* BuildTreeFromSpec(const float* spec, int count)
+	{
+		if (!spec || count <= 0) { SetError("empty tree spec"); return nullptr; }
+		const char* err = nullptr;
+		NodeRef t = BuildFromSpec(spec, count, &err);
+		if (!t) { SetError(err ? err : "malformed tree spec"); return nullptr; }
+		return Hand(std::move(t));
+	}
+
+	// ---- GPU-native API ------------------------------------------------------------------
+	TANGERINE_API tg_status tg_compile(void* tree, tg_program** out)
+	{
+		if (!out) { SetError("null output"); return TG_ERR_INVALID; }
+		*out = nullptr;
+		std::unique_ptr<tg_program> prog;
+		std::lock_guard<std::mutex> lock(Engine::Get().Mutex);
+		const tg_status st = CompileInto(tree, prog);
+		if (st == TG_OK) *out = prog.release();
+		return st;
+	}
+
+	TANGERINE_API void tg_program_free(tg_program* p) { delete p; }
+
+	TANGERINE_API tg_status tg_program_get_info(const tg_program* p, tg_program_info* out)
+	{
+		if (!p || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		out->octree_cells = p->Host.Header.NodeCount;
+		out->code_quads = p->Host.Header.CodeQuads;
+		out->materials = p->Host.Header.MaterialCount;
+		out->has_paint = p->Host.Header.HasPaint;
+		out->max_stack = p->Host.Header.MaxStack;
+		out->bounds_min[0] = p->Host.Bounds.Min.x; out->bounds_min[1] = p->Host.Bounds.Min.y; out->bounds_min[2] = p->Host.Bounds.Min.z;
+		out->bounds_max[0] = p->Host.Bounds.Max.x; out->bounds_max[1] = p->Host.Bounds.Max.y; out->bounds_max[2] = p->Host.Bounds.Max.z;
+		out->compile_seconds = p->Host.BuildSeconds;
+		out->distance_quads = p->Host.DistanceQuadsTotal;
+		return TG_OK;
+	}
+
+	TANGERINE_API int64_t tg_tree_reference_words(void* tree, uint32_t* out, int64_t capacity)
+	{
+		if (!tree) return 0;
+		const std::vector<uint32_t> w = CompileReferenceWords(*AsNode(tree));
+		for (int64_t i = 0; i < (int64_t)w.size() && i < capacity; ++i) out[i] = w[i];
+		return (int64_t)w.size();
+	}
+
+	TANGERINE_API int64_t tg_debug_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
+		uint32_t* words, int64_t word_capacity, int64_t* word_count)
+	{
+		if (!tree) return -1;
+		Octree o;
+		if (!o.Build(Borrow(tree))) return -1;
+		int64_t w = 0;
+		for (size_t i = 0; i < o.Cells.size(); ++i)
+		{
+			const Octree::Cell& c = o.Cells[i];
+			std::vector<uint32_t> prog;
+			if (c.Evaluator) prog = CompileReferenceWords(*c.Evaluator);
+			if ((int64_t)i < cell_capacity && cells)
+			{
+				float* n = cells + i * 14;
+				n[0] = c.Pivot.x; n[1] = c.Pivot.y; n[2] = c.Pivot.z;
+				n[3] = c.Bounds.Min.x; n[4] = c.Bounds.Min.y; n[5] = c.Bounds.Min.z;
+				n[6] = c.Bounds.Max.x; n[7] = c.Bounds.Max.y; n[8] = c.Bounds.Max.z;
+				n[9] = c.Terminus ? 1.0f : 0.0f;
+				n[10] = c.Evaluator ? 1.0f : 0.0f;
+				n[11] = (float)w;
+				n[12] = (float)prog.size();
+				n[13] = c.Evaluator ? (float)c.Evaluator->StackSize : 0.0f;
+			}
+			if ((int64_t)i < cell_capacity && children)
+			{
+				for (int k = 0; k < 8; ++k) children[i * 8 + k] = c.Children[k];
+			}
+			for (uint32_t v : prog)
+			{
+				if (words && w < word_capacity) words[w] = v;
+				++w;
+			}
+		}
+		if (word_count) *word_count = w;
+		return (int64_t)o.Cells.size();
+	}
+
+	TANGERINE_API tg_status tg_export_grid(const float lo[3], const float hi[3], float step, tg_grid* out)
+	{
+		if (!lo || !hi || !out || !(step > 0.0f)) { SetError("invalid export bounds"); return TG_ERR_INVALID; }
+		ExportLattice(Vec3(lo[0], lo[1], lo[2]), Vec3(hi[0], hi[1], hi[2]), step, *out);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_eval_grid(tg_program* p, const tg_grid* g, float* out, int out_is_device, void* stream)
+	{
+		if (!p || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		GridSpec gs;
+		if (!ToGridSpec(g, gs)) return TG_ERR_INVALID;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t s = StreamOf(stream);
+		const size_t bytes = (size_t)g->nx * g->ny * g->nz * sizeof(float);
+		float* dst = out;
+		if (!out_is_device)
+		{
+			cudaError_t e = eng.Lattice().Reserve(bytes);
+			if (e != cudaSuccess) return CudaFail(e, "allocating the lattice");
+			dst = eng.Lattice().As<float>();
+		}
+		cudaError_t e = eng.EvalGrid(*p, gs, dst, s);
+		if (e == cudaSuccess && !out_is_device) e = cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, s);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+		if (e != cudaSuccess) return CudaFail(e, "evaluating the lattice");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_eval_points(tg_program* p, const float* points, int64_t n, float* out, void* stream)
+	{
+		if (!p || (n > 0 && (!points || !out))) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.EvalPoints(*p, points, n, out, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "evaluating points");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_export_mesh_device(tg_program* p, const tg_grid* g, uint32_t flags, tg_device_mesh* out, void* stream)
+	{
+		if (!p || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		GridSpec gs;
+		if (!ToGridSpec(g, gs)) return TG_ERR_INVALID;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		DeviceMesh dm;
+		cudaError_t e = eng.Export(*p, gs, (flags & TG_MESH_ATTRIBUTES) != 0, dm, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		out->vertex_count = dm.VertexCount;
+		out->face_count = dm.FaceCount;
+		out->vertices = dm.Vertices;
+		out->normals = dm.Normals;
+		out->colors = dm.Colors;
+		out->faces = dm.Faces;
+		out->cubes = dm.Cubes;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_export_mesh(tg_program* p, const tg_grid* g, uint32_t flags, tg_mesh* out, void* stream)
+	{
+		if (!p || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		GridSpec gs;
+		if (!ToGridSpec(g, gs)) return TG_ERR_INVALID;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t s = StreamOf(stream);
+		DeviceMesh dm;
+		cudaError_t e = eng.Export(*p, gs, (flags & TG_MESH_ATTRIBUTES) != 0, dm, s);
+		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		return CopyMeshToHost(dm, out, s);
+	}
+
+	TANGERINE_API void tg_mesh_free(tg_mesh* m)
+	{
+		if (!m) return;
+		std::free(m->vertices);
+		std::free(m->normals);
+		std::free(m->colors);
+		std::free(m->faces);
+		std::free(m->cubes);
+		std::memset(m, 0, sizeof *m);
+	}
+
+	TANGERINE_API tg_status tg_export_tree(void* tree, const float lo[3], const float hi[3], float step, tg_mesh* out, void* stream)
+	{
+		if (!out || !lo || !hi) { SetError("null argument"); return TG_ERR_INVALID; }
+		tg_grid g;
+		tg_status st = tg_export_grid(lo, hi, step, &g);
+		if (st != TG_OK) return st;
+		GridSpec gs;
+		if (!ToGridSpec(&g, gs)) return TG_ERR_INVALID;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		std::unique_ptr<tg_program> prog;
+		st = CompileInto(tree, prog);
+		if (st != TG_OK) return st;
+		const cudaStream_t s = StreamOf(stream);
+		DeviceMesh dm;
+		cudaError_t e = eng.Export(*prog, gs, true, dm, s);
+		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		return CopyMeshToHost(dm, out, s);
+	}
+
+	// WritePLY (export.cpp:198-280): header, then x y z nx ny nz [r g b] per vertex, then
+	// "3 i j k" per face, little endian.  Positions are multiplied by `scale`.
+	TANGERINE_API tg_status tg_write_ply(const tg_mesh* m, const char* path, float scale)
+	{
+		if (!m || !path) { SetError("null argument"); return TG_ERR_INVALID; }
+		FILE* f = std::fopen(path, "wb");
+		if (!f) { WriteFileError(path); return TG_ERR_IO; }
+		const bool color = m->colors != nullptr;
+		std::string header = "ply\nformat binary_little_endian 1.0\ncomment Created by Tangerine\n";
+		header += "element vertex " + std::to_string(m->vertex_count) + "\n";
+		header += "property float x\nproperty float y\nproperty float z\n";
+		header += "property float nx\nproperty float ny\nproperty float nz\n";
+		if (color) header += "property uchar red\nproperty uchar green\nproperty uchar blue\n";
+		if (m->face_count > 0)
+		{
+			header += "element face " + std::to_string(m->face_count) + "\n";
+			header += "property list uchar uint vertex_indices\n";
+		}
+		header += "end_header\n";
+		bool ok = std::fwrite(header.data(), 1, header.size(), f) == header.size();
+		const size_t stride = color ? 27 : 24;
+		std::vector<uint8_t> buf(stride * (size_t)(m->vertex_count < 65536 ? m->vertex_count : 65536) + 16);
+		for (uint64_t v0 = 0; ok && v0 < m->vertex_count; v0 += 65536)
+		{
+			const uint64_t n = (m->vertex_count - v0) < 65536 ? (m->vertex_count - v0) : 65536;
+			uint8_t* o = buf.data();
+			for (uint64_t v = v0; v < v0 + n; ++v)
+			{
+				const float pos[3] = { m->vertices[v * 3] * scale, m->vertices[v * 3 + 1] * scale, m->vertices[v * 3 + 2] * scale };
+				std::memcpy(o, pos, 12);
+				std::memcpy(o + 12, m->normals + v * 3, 12);
+				if (color) std::memcpy(o + 24, m->colors + v * 3, 3);
+				o += stride;
+			}
+			ok = std::fwrite(buf.data(), 1, (size_t)(o - buf.data()), f) == (size_t)(o - buf.data());
+		}
+		std::vector<uint8_t> fb(13 * 65536);
+		for (uint64_t t0 = 0; ok && t0 < m->face_count; t0 += 65536)
+		{
+			const uint64_t n = (m->face_count - t0) < 65536 ? (m->face_count - t0) : 65536;
+			uint8_t* o = fb.data();
+			for (uint64_t t = t0; t < t0 + n; ++t)
+			{
+				*o = 3;
+				std::memcpy(o + 1, m->faces + t * 3, 12);
+				o += 13;
+			}
+			ok = std::fwrite(fb.data(), 1, (size_t)(o - fb.data()), f) == (size_t)(o - fb.data());
+		}
+		ok = (std::fclose(f) == 0) && ok;
+		if (!ok) { WriteFileError(path); return TG_ERR_IO; }
+		return TG_OK;
+	}
+
+	// WriteSTL(Octree, ...) (export.cpp:111-179): 80-byte header, count, then per triangle
+	// the gradient at its centroid, its three corners (times `scale`) and a zero word.
+	TANGERINE_API tg_status tg_write_stl(tg_program* p, const tg_mesh* m, const char* path, float scale, void* stream)
+	{
+		if (!p || !m || !path) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::vector<float> normals((size_t)m->face_count * 3);
+		{
+			Engine& eng = Engine::Get();
+			std::lock_guard<std::mutex> lock(eng.Mutex);
+			cudaError_t e = eng.FaceNormals(*p, m->vertices, m->vertex_count, m->faces, m->face_count, normals.data(), StreamOf(stream));
+			if (e != cudaSuccess) return CudaFail(e, "computing face normals");
+		}
+		FILE* f = std::fopen(path, "wb");
+		if (!f) { WriteFileError(path); return TG_ERR_IO; }
+		char header[80];
+		std::memset(header, 0, sizeof header);
+		const char* title = "STL generated by TangerineCSG";
+		std::memcpy(header, title, std::strlen(title));
+		bool ok = std::fwrite(header, 1, 80, f) == 80;
+		const uint32_t count = (uint32_t)m->face_count;
+		ok = ok && std::fwrite(&count, 4, 1, f) == 1;
+		std::vector<uint8_t> rec(50);
+		for (uint64_t t = 0; ok && t < m->face_count; ++t)
+		{
+			std::memcpy(rec.data(), normals.data() + t * 3, 12);
+			for (int c = 0; c < 3; ++c)
+			{
+				const uint32_t v = m->faces[t * 3 + c];
+				const float pos[3] = { m->vertices[(size_t)v * 3] * scale, m->vertices[(size_t)v * 3 + 1] * scale, m->vertices[(size_t)v * 3 + 2] * scale };
+				std::memcpy(rec.data() + 12 + 12 * c, pos, 12);
+			}
+			rec[48] = 0; rec[49] = 0;
+			ok = std::fwrite(rec.data(), 1, 50, f) == 50;
+		}
+		ok = (std::fclose(f) == 0) && ok;
+		if (!ok) { WriteFileError(path); return TG_ERR_IO; }
+		return TG_OK;
+	}
+
+	// ExportCommon (export.cpp:595-607): the tree's bounds at a 1/GridSize step.
+	static void ExportToFile(void* h, float grid_size, const char* path, bool ply)
+	{
+		if (!h || !path || !(grid_size > 0.0f)) { SetError("invalid export arguments"); return; }
+		const AABB b = AsNode(h)->Bounds();
+		const float step = (float)(1.0 / (double)grid_size);
+		const float lo[3] = { b.Min.x, b.Min.y, b.Min.z }, hi[3] = { b.Max.x, b.Max.y, b.Max.z };
+		tg_program* prog = nullptr;
+		if (tg_compile(h, &prog) != TG_OK) return;
+		tg_grid g;
+		tg_mesh m;
+		if (tg_export_grid(lo, hi, step, &g) == TG_OK && tg_export_mesh(prog, &g, TG_MESH_ATTRIBUTES, &m, nullptr) == TG_OK)
+		{
+			if (ply) tg_write_ply(&m, path, 1.0f);
+			else tg_write_stl(prog, &m, path, 1.0f, nullptr);
+			tg_mesh_free(&m);
+		}
+		tg_program_free(prog);
+	}
+
+	TANGERINE_API void ExportSTL(void* h, float grid_size, int, const char* path) { ExportToFile(h, grid_size, path, false); }
+	TANGERINE_API void ExportPLY(void* h, float grid_size, int, const char* path) { ExportToFile(h, grid_size, path, true); }
+
+	TANGERINE_API void tg_profile_enable(int on) { Engine::Get().SetProfiling(on != 0); }
+	TANGERINE_API int tg_profile_read(const char* name, double* ms, int64_t* launches)
+	{
+		double m = 0.0; int64_t n = 0;
+		const bool found = Engine::Get().ReadProfile(name ? name : "", m, n);
+		if (ms) *ms = m;
+		if (launches) *launches = n;
+		return found ? 1 : 0;
+	}
+	TANGERINE_API void tg_profile_reset(void) { Engine::Get().ResetProfile(); }
+
+	TANGERINE_API tg_status tg_measure_fp32_peak(double* tflops, void* stream)
+	{
+		if (!tflops) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::lock_guard<std::mutex> lock(Engine::Get().Mutex);
+		cudaError_t e = MeasureFp32Peak(tflops, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "measuring FP32 throughput");
+		return TG_OK;
+	}
+
+	TANGERINE_API const char* tg_last_error(void) { return LastError().c_str(); }
+	TANGERINE_API const char* tg_version(void) { return "tangerine_gb300 0.1 (sm_103a)"; }
+}

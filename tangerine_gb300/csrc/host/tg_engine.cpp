@@ -1,0 +1,256 @@
+// GPU engine: device buffers, the export pipeline and the kernel profiler.
+#include "tg_engine.hpp"
+
+#include <cstring>
+
+namespace tg
+{
+	std::string& LastError()
+	{
+		static thread_local std::string msg;
+		return msg;
+	}
+
+	void SetError(const std::string& msg) { LastError() = msg; }
+
+	cudaError_t DeviceBuffer::Reserve(size_t bytes)
+	{
+		if (bytes <= Bytes && Ptr) return cudaSuccess;
+		Release();
+		size_t want = bytes < 256 ? 256 : bytes;
+		cudaError_t e = cudaMalloc(&Ptr, want);
+		if (e != cudaSuccess) { Ptr = nullptr; Bytes = 0; return e; }
+		Bytes = want;
+		return cudaSuccess;
+	}
+
+	void DeviceBuffer::Release()
+	{
+		if (Ptr) cudaFree(Ptr);
+		Ptr = nullptr;
+		Bytes = 0;
+	}
+
+	Program::~Program()
+	{
+		if (Device) cudaFree(Device);
+	}
+
+	Engine& Engine::Get()
+	{
+		static Engine* engine = new Engine();   // lives until exit; device memory goes with the context
+		return *engine;
+	}
+
+	cudaStream_t Engine::DefaultStream()
+	{
+		if (!Stream) cudaStreamCreateWithFlags(&Stream, cudaStreamNonBlocking);
+		return Stream;
+	}
+
+	namespace
+	{
+		inline size_t AlignUp(size_t v, size_t a) { return (v + a - 1) / a * a; }
+	}
+
+	// One allocation: nodes (64-byte records), code quads, colour bytes.
+	cudaError_t Engine::Upload(Program& p)
+	{
+		const size_t nodeBytes = p.Host.Nodes.size() * sizeof(OctNode);
+		const size_t codeOff = AlignUp(nodeBytes, 256);
+		const size_t codeBytes = p.Host.Code.size() * sizeof(float);
+		const size_t colorOff = AlignUp(codeOff + codeBytes, 256);
+		const size_t colorBytes = p.Host.Colors.size() ? p.Host.Colors.size() : 4;
+		const size_t total = colorOff + colorBytes;
+		cudaError_t e = cudaGetDevice(&p.DeviceId);
+		if (e != cudaSuccess) return e;
+		e = cudaMalloc(&p.Device, total);
+		if (e != cudaSuccess) { p.Device = nullptr; return e; }
+		std::vector<uint8_t> staging(total, 0);
+		std::memcpy(staging.data(), p.Host.Nodes.data(), nodeBytes);
+		std::memcpy(staging.data() + codeOff, p.Host.Code.data(), codeBytes);
+		if (!p.Host.Colors.empty()) std::memcpy(staging.data() + colorOff, p.Host.Colors.data(), p.Host.Colors.size());
+		e = cudaMemcpy(p.Device, staging.data(), total, cudaMemcpyHostToDevice);
+		if (e != cudaSuccess) return e;
+		uint8_t* base = static_cast<uint8_t*>(p.Device);
+		p.View.Nodes = reinterpret_cast<const OctNode*>(base);
+		p.View.Code = reinterpret_cast<const float4*>(base + codeOff);
+		p.View.Colors = reinterpret_cast<const uchar4*>(base + colorOff);
+		p.View.MaxStack = p.Host.Header.MaxStack;
+		return cudaSuccess;
+	}
+
+	void Engine::SetProfiling(bool on) { Profiling = on; }
+
+	void Engine::ResetProfile()
+	{
+		Collect();
+		Totals.clear();
+	}
+
+	void Engine::Begin(const char* name, cudaStream_t s)
+	{
+		if (!Profiling) return;
+		Mark m{ name, nullptr, nullptr };
+		cudaEventCreate(&m.Start);
+		cudaEventCreate(&m.Stop);
+		cudaEventRecord(m.Start, s);
+		Pending.push_back(m);
+	}
+
+	void Engine::End(cudaStream_t s)
+	{
+		if (!Profiling || Pending.empty()) return;
+		cudaEventRecord(Pending.back().Stop, s);
+	}
+
+	void Engine::Collect()
+	{
+		for (Mark& m : Pending)
+		{
+			float ms = 0.0f;
+			if (cudaEventSynchronize(m.Stop) == cudaSuccess) cudaEventElapsedTime(&ms, m.Start, m.Stop);
+			cudaEventDestroy(m.Start);
+			cudaEventDestroy(m.Stop);
+			bool found = false;
+			for (Total& t : Totals)
+			{
+				if (t.Name == m.Name) { t.Ms += ms; t.Launches += 1; found = true; break; }
+			}
+			if (!found) Totals.push_back({ m.Name, (double)ms, 1 });
+		}
+		Pending.clear();
+	}
+
+	bool Engine::ReadProfile(const std::string& name, double& ms, int64_t& launches)
+	{
+		Collect();
+		for (const Total& t : Totals)
+		{
+			if (t.Name == name) { ms = t.Ms; launches = t.Launches; return true; }
+		}
+		ms = 0.0;
+		launches = 0;
+		return false;
+	}
+
+#define TG_TRY(expr) do { cudaError_t _e = (expr); if (_e != cudaSuccess) return _e; } while (0)
+
+	cudaError_t Engine::EvalGrid(const Program& p, const GridSpec& g, float* out, cudaStream_t s)
+	{
+		Begin("eval_grid", s);
+		cudaError_t e = LaunchEvalGrid(p.View, g, out, s);
+		End(s);
+		return e;
+	}
+
+	cudaError_t Engine::EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s)
+	{
+		if (n <= 0) return cudaSuccess;
+		TG_TRY(Points.Reserve((size_t)n * 12));
+		TG_TRY(PointOut.Reserve((size_t)n * 4));
+		TG_TRY(cudaMemcpyAsync(Points.Ptr, host_points, (size_t)n * 12, cudaMemcpyHostToDevice, s));
+		Begin("eval_points", s);
+		TG_TRY(LaunchEvalPoints(p.View, Points.As<float>(), n, PointOut.As<float>(), s));
+		End(s);
+		TG_TRY(cudaMemcpyAsync(host_out, PointOut.Ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaStreamSynchronize(s));
+		Collect();
+		return cudaSuccess;
+	}
+
+	cudaError_t Engine::Export(const Program& p, const GridSpec& g, bool attributes, DeviceMesh& out, cudaStream_t s)
+	{
+		out = DeviceMesh();
+		const int64_t lattice = (int64_t)g.NX * g.NY * g.NZ;
+		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
+		const int64_t words = (cells + 31) / 32;
+		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 4 * sizeof(uint32_t)));
+
+		TG_TRY(LatticeBuf.Reserve((size_t)lattice * sizeof(float)));
+		TG_TRY(Words.Reserve((size_t)words * 4));
+		TG_TRY(WordBase.Reserve((size_t)words * 4));
+		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
+		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4));
+
+		Begin("eval_grid", s);
+		TG_TRY(LaunchEvalGrid(p.View, g, LatticeBuf.As<float>(), s));
+		End(s);
+		Begin("cell_flags", s);
+		TG_TRY(LaunchCellFlags(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), s));
+		End(s);
+		Begin("scan", s);
+		TG_TRY(LaunchExclusiveScan(Words.As<uint32_t>(), words, true, WordBase.As<uint32_t>(), Counts.As<uint32_t>(), Scratch.As<uint32_t>(), s));
+		End(s);
+		TG_TRY(cudaMemcpyAsync(HostCounts, Counts.Ptr, 4, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaStreamSynchronize(s));
+		const uint32_t vcount = HostCounts[0];
+
+		TG_TRY(Vertices.Reserve((size_t)vcount * 12));
+		TG_TRY(Cubes.Reserve((size_t)vcount * 4));
+		TG_TRY(FaceCounts.Reserve((size_t)vcount * 4));
+		TG_TRY(FaceBase.Reserve((size_t)vcount * 4));
+		TG_TRY(Scratch.Reserve(ScanScratchWords(vcount) * 4));
+		Begin("cell_vertices", s);
+		TG_TRY(LaunchCellVertices(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Vertices.As<float>(),
+			Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), cells, s));
+		End(s);
+		Begin("scan", s);
+		TG_TRY(LaunchExclusiveScan(FaceCounts.As<uint32_t>(), vcount, false, FaceBase.As<uint32_t>(), Counts.As<uint32_t>() + 1,
+			Scratch.As<uint32_t>(), s));
+		End(s);
+		TG_TRY(cudaMemcpyAsync(HostCounts + 1, Counts.As<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaStreamSynchronize(s));
+		const uint32_t fcount = HostCounts[1];
+
+		TG_TRY(Faces.Reserve((size_t)fcount * 12));
+		Begin("faces", s);
+		TG_TRY(LaunchFaces(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Cubes.As<uint32_t>(),
+			FaceBase.As<uint32_t>(), vcount, Faces.As<uint32_t>(), s));
+		End(s);
+
+		out.VertexCount = vcount;
+		out.FaceCount = fcount;
+		out.Vertices = Vertices.As<float>();
+		out.Cubes = Cubes.As<uint32_t>();
+		out.Faces = Faces.As<uint32_t>();
+		if (attributes)
+		{
+			TG_TRY(Normals.Reserve((size_t)vcount * 12));
+			uint8_t* colors = nullptr;
+			if (p.Host.Header.HasPaint)
+			{
+				TG_TRY(Colors.Reserve((size_t)vcount * 3));
+				colors = Colors.As<uint8_t>();
+			}
+			Begin("attributes", s);
+			TG_TRY(LaunchVertexAttributes(p.View, Vertices.As<float>(), vcount, Normals.As<float>(), colors, s));
+			End(s);
+			out.Normals = Normals.As<float>();
+			out.Colors = colors;
+		}
+		TG_TRY(cudaStreamSynchronize(s));
+		Collect();
+		return cudaSuccess;
+	}
+
+	cudaError_t Engine::FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
+		uint64_t face_count, float* host_normals, cudaStream_t s)
+	{
+		if (face_count == 0) return cudaSuccess;
+		DeviceBuffer v, f, n;
+		TG_TRY(v.Reserve(vertex_count * 12));
+		TG_TRY(f.Reserve(face_count * 12));
+		TG_TRY(n.Reserve(face_count * 12));
+		cudaError_t e = cudaMemcpyAsync(v.Ptr, host_vertices, vertex_count * 12, cudaMemcpyHostToDevice, s);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(f.Ptr, host_faces, face_count * 12, cudaMemcpyHostToDevice, s);
+		Begin("face_normals", s);
+		if (e == cudaSuccess) e = LaunchFaceNormals(p.View, v.As<float>(), f.As<uint32_t>(), face_count, n.As<float>(), s);
+		End(s);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(host_normals, n.Ptr, face_count * 12, cudaMemcpyDeviceToHost, s);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+		Collect();
+		v.Release(); f.Release(); n.Release();
+		return e;
+	}
+}

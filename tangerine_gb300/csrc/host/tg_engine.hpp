@@ -1,0 +1,87 @@
+// Per-process GPU engine: device buffers reused across calls, the export pipeline and an
+// optional per-kernel profiler.
+#pragma once
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "tg_layout.hpp"
+#include "tg_octree.hpp"
+#include "../kernels/tg_kernels.hpp"
+
+namespace tg
+{
+	// A grow-only device allocation.
+	struct DeviceBuffer
+	{
+		void* Ptr = nullptr;
+		size_t Bytes = 0;
+		cudaError_t Reserve(size_t bytes);
+		void Release();
+		template<typename T> T* As() const { return static_cast<T*>(Ptr); }
+	};
+
+	struct Program
+	{
+		CompiledTree Host;
+		void* Device = nullptr;
+		DeviceProgram View{};
+		int DeviceId = 0;
+		~Program();
+	};
+
+	struct DeviceMesh
+	{
+		uint64_t VertexCount = 0;
+		uint64_t FaceCount = 0;
+		float* Vertices = nullptr;
+		float* Normals = nullptr;
+		uint8_t* Colors = nullptr;
+		uint32_t* Faces = nullptr;
+		uint32_t* Cubes = nullptr;
+	};
+
+	class Engine
+	{
+	public:
+		static Engine& Get();
+
+		cudaStream_t DefaultStream();
+		cudaError_t Upload(Program& p);
+		cudaError_t EvalGrid(const Program& p, const GridSpec& g, float* device_out, cudaStream_t s);
+		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
+		cudaError_t Export(const Program& p, const GridSpec& g, bool attributes, DeviceMesh& out, cudaStream_t s);
+		cudaError_t FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
+			uint64_t face_count, float* host_normals, cudaStream_t s);
+		DeviceBuffer& Lattice() { return LatticeBuf; }
+
+		// Profiling of kernel launches (CUDA events on the launching stream).
+		void SetProfiling(bool on);
+		bool ReadProfile(const std::string& name, double& ms, int64_t& launches);
+		void ResetProfile();
+		std::mutex Mutex;   // engine calls are serialised
+
+	private:
+		Engine() = default;
+		struct Mark { std::string Name; cudaEvent_t Start, Stop; };
+		struct Total { std::string Name; double Ms; int64_t Launches; };
+		void Begin(const char* name, cudaStream_t s);
+		void End(cudaStream_t s);
+		void Collect();
+		bool Profiling = false;
+		std::vector<Mark> Pending;
+		std::vector<Total> Totals;
+
+		cudaStream_t Stream = nullptr;
+		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
+		DeviceBuffer Points, PointOut;
+		uint32_t* HostCounts = nullptr;
+	};
+
+	std::string& LastError();
+	void SetError(const std::string& msg);
+}

@@ -1,0 +1,471 @@
+// Export octree construction and compilation of each octree cell's clipped subtree into
+// the GPU record format (tg_layout.hpp).
+#include "tg_octree.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <memory>
+#include <unordered_map>
+
+namespace tg
+{
+	namespace
+	{
+		struct TmpCell
+		{
+			AABB Bounds;
+			Vec3 Pivot;
+			bool Terminus = false;
+			bool Incomplete = false;
+			int Leaves = 0;
+			NodeRef Eval;
+			std::unique_ptr<TmpCell> Kids[8];
+		};
+
+		struct BuildParams
+		{
+			float Target;
+			bool Coalesce;
+			int MaxDepth;
+			int ParallelDepth;
+		};
+
+		void Populate(TmpCell& c, const BuildParams& bp, int depth);
+
+		// SDFOctree ctor (sdf_evaluator.cpp:1641-1700): the cell's pivot is its min corner
+		// plus half the longest side; its evaluator is the parent's clipped to the sphere
+		// through the cube's corners.
+		std::unique_ptr<TmpCell> MakeCell(const NodeRef& in, AABB bounds, const BuildParams& bp, int depth)
+		{
+			auto c = std::make_unique<TmpCell>();
+			c->Bounds = bounds;
+			const Vec3 e = bounds.Max - bounds.Min;
+			const float span = fmaxf(fmaxf(e.x, e.y), e.z);
+			const float half = (float)((double)span * 0.5);
+			c->Pivot = Vec3(half) + bounds.Min;
+			const float radius = (float)((double)Length(Vec3(span)) * 0.5);
+			c->Eval = in->Clip(c->Pivot, radius);
+			c->Leaves = c->Eval ? c->Eval->LeafCount() : 0;
+			c->Terminus = span <= bp.Target || !c->Eval;
+			if (!c->Terminus)
+			{
+				c->Incomplete = true;
+				if (bp.Coalesce || bp.MaxDepth == -1 || depth < bp.MaxDepth)
+				{
+					Populate(*c, bp, depth);
+				}
+			}
+			return c;
+		}
+
+		// SDFOctree::Populate (sdf_evaluator.cpp:1703-1783): split at the pivot, drop empty
+		// children, shrink the bounds to the live ones, and merge the children back into
+		// this cell when they all ended and share one evaluator, or when few brushes remain.
+		void Populate(TmpCell& c, const BuildParams& bp, int depth)
+		{
+			if (!c.Incomplete) return;
+			c.Incomplete = false;
+			AABB childBounds[8];
+			for (int i = 0; i < 8; ++i)
+			{
+				AABB b = c.Bounds;
+				if (i & 1) b.Min.x = c.Pivot.x; else b.Max.x = c.Pivot.x;
+				if (i & 2) b.Min.y = c.Pivot.y; else b.Max.y = c.Pivot.y;
+				if (i & 4) b.Min.z = c.Pivot.z; else b.Max.z = c.Pivot.z;
+				childBounds[i] = b;
+			}
+			if (depth < bp.ParallelDepth)
+			{
+				std::future<std::unique_ptr<TmpCell>> jobs[8];
+				for (int i = 0; i < 8; ++i)
+				{
+					jobs[i] = std::async(std::launch::async, [&, i]() { return MakeCell(c.Eval, childBounds[i], bp, depth + 1); });
+				}
+				for (int i = 0; i < 8; ++i) c.Kids[i] = jobs[i].get();
+			}
+			else
+			{
+				for (int i = 0; i < 8; ++i) c.Kids[i] = MakeCell(c.Eval, childBounds[i], bp, depth + 1);
+			}
+
+			bool uniform = true, penultimate = true;
+			int live = 0;
+			for (int i = 0; i < 8; ++i)
+			{
+				if (!c.Kids[i]->Eval)
+				{
+					c.Kids[i].reset();
+					continue;
+				}
+				uniform = uniform && c.Eval->Equals(*c.Kids[i]->Eval);
+				penultimate = penultimate && c.Kids[i]->Terminus;
+				if (live == 0)
+				{
+					c.Bounds = c.Kids[i]->Bounds;
+				}
+				else
+				{
+					c.Bounds.Min = TernaryMin(c.Bounds.Min, c.Kids[i]->Bounds.Min);
+					c.Bounds.Max = TernaryMax(c.Bounds.Max, c.Kids[i]->Bounds.Max);
+				}
+				++live;
+			}
+			if (live == 0)
+			{
+				c.Eval = NodeRef();
+				c.Terminus = true;
+				return;
+			}
+			const int limit = depth > 3 ? depth : 3;
+			if (bp.Coalesce && ((penultimate && uniform) || c.Leaves <= limit))
+			{
+				for (auto& k : c.Kids) k.reset();
+				c.Terminus = true;
+			}
+		}
+
+		void Flatten(TmpCell& t, std::vector<Octree::Cell>& out)
+		{
+			const int index = (int)out.size();
+			out.emplace_back();
+			{
+				Octree::Cell& c = out.back();
+				c.Bounds = t.Bounds;
+				c.Pivot = t.Pivot;
+				c.Terminus = t.Terminus;
+				c.Incomplete = t.Incomplete;
+				c.EvaluatorLeaves = t.Leaves;
+				c.Evaluator = t.Eval;
+			}
+			if (t.Terminus) return;
+			for (int i = 0; i < 8; ++i)
+			{
+				if (t.Kids[i])
+				{
+					const int child = (int)out.size();
+					Flatten(*t.Kids[i], out);
+					out[index].Children[i] = child;
+				}
+			}
+		}
+	}
+
+	bool Octree::Build(const NodeRef& root, float target, bool coalesce, int max_depth)
+	{
+		Cells.clear();
+		if (!root || !root->HasFiniteBounds()) return false;
+		// Bounds().BoundingCube() + 0 margin (sdf_evaluator.cpp:1616).
+		AABB cube = root->Bounds().BoundingCube();
+		if (!cube.Degenerate())
+		{
+			cube.Min = cube.Min - Vec3(0.0f);
+			cube.Max = cube.Max + Vec3(0.0f);
+		}
+		if (cube.Volume() == 0.0f) return false;
+		BuildParams bp{ target, coalesce, max_depth, 3 };
+		std::unique_ptr<TmpCell> top = MakeCell(root, cube, bp, 1);
+		if (!top->Eval) return false;
+		Flatten(*top, Cells);
+		return true;
+	}
+
+	int Octree::Descend(Vec3 p) const
+	{
+		int at = 0;
+		for (;;)
+		{
+			const Cell& c = Cells[at];
+			if (c.Terminus) return at;
+			int i = 0;
+			if (p.x > c.Pivot.x) i |= 1;
+			if (p.y > c.Pivot.y) i |= 2;
+			if (p.z > c.Pivot.z) i |= 4;
+			if (c.Children[i] < 0) return at;
+			at = c.Children[i];
+		}
+	}
+
+	namespace
+	{
+		void PushWord(std::vector<uint32_t>& w, float f) { w.push_back(FloatBits(f)); }
+
+		// SDFNode::Compile (sdf_evaluator.cpp:409-429, 495-507, 632-635, 915-924, 1098-1103).
+		void ReferenceWords(const Node& n, std::vector<uint32_t>& w)
+		{
+			switch (n.Kind)
+			{
+			case NodeKind::Brush:
+			{
+				const Transform& t = n.Xf;
+				const bool rot = !t.Rotation.IsIdentity();
+				const bool scl = t.Scalation != 1.0f;
+				const bool trn = !(t.Translation.x == 0.0f && t.Translation.y == 0.0f && t.Translation.z == 0.0f);
+				if (rot || scl)
+				{
+					const Mat4 inv = MatInverse(t.ToMatrix());
+					w.push_back(OpMatrix);
+					for (float v : inv.m) PushWord(w, v);
+				}
+				else if (trn)
+				{
+					w.push_back(OpOffset);
+					PushWord(w, -t.Translation.x); PushWord(w, -t.Translation.y); PushWord(w, -t.Translation.z);
+				}
+				w.push_back(n.Op);
+				for (int i = 0; i < BrushParamCount(n.Op); ++i) PushWord(w, n.Params[i]);
+				if (scl)
+				{
+					w.push_back(OpScaleField);
+					PushWord(w, t.Scalation);
+				}
+				break;
+			}
+			case NodeKind::Set:
+				ReferenceWords(*n.Lhs, w);
+				ReferenceWords(*n.Rhs, w);
+				w.push_back(n.Op);
+				if (IsBlendOp(n.Op)) PushWord(w, n.Threshold);
+				break;
+			case NodeKind::Flate:
+				ReferenceWords(*n.Lhs, w);
+				w.push_back(OpFlate);
+				PushWord(w, n.Threshold);
+				break;
+			case NodeKind::Stencil:
+				ReferenceWords(*n.Lhs, w);
+				break;
+			}
+		}
+
+		struct Emitter
+		{
+			std::vector<float>& Code;
+			std::unordered_map<const Material*, int>& Materials;
+			std::vector<const Material*>& MaterialList;
+
+			void Quad(uint32_t head, float a, float b, float c)
+			{
+				Code.push_back(BitsFloat(head));
+				Code.push_back(a);
+				Code.push_back(b);
+				Code.push_back(c);
+			}
+			void Quad4(float a, float b, float c, float d)
+			{
+				Code.push_back(a); Code.push_back(b); Code.push_back(c); Code.push_back(d);
+			}
+			int MaterialIndex(const Material* m)
+			{
+				if (!m) return -1;
+				auto it = Materials.find(m);
+				if (it != Materials.end()) return it->second;
+				const int idx = (int)MaterialList.size();
+				Materials.emplace(m, idx);
+				MaterialList.push_back(m);
+				return idx;
+			}
+
+			// Distance program: Tangerine's postfix program with each brush's transform,
+			// primitive and field scale fused into one record.
+			void Distance(const Node& n)
+			{
+				switch (n.Kind)
+				{
+				case NodeKind::Brush:
+				{
+					const Transform& t = n.Xf;
+					const bool rot = !t.Rotation.IsIdentity();
+					const bool scl = t.Scalation != 1.0f;
+					const bool trn = !(t.Translation.x == 0.0f && t.Translation.y == 0.0f && t.Translation.z == 0.0f);
+					uint32_t flags = 0;
+					if (rot || scl) flags |= RecMatrix;
+					else if (trn) flags |= RecOffset;
+					if (scl) flags |= RecScale;
+					Quad(n.Op | flags, n.Params[0], n.Params[1], n.Params[2]);
+					if (flags & RecMatrix)
+					{
+						const Mat4 inv = MatInverse(t.ToMatrix());
+						// Row r of the 3x4 affine part: (m[0][r], m[1][r], m[2][r], m[3][r]).
+						for (int r = 0; r < 3; ++r) Quad4(inv.at(0, r), inv.at(1, r), inv.at(2, r), inv.at(3, r));
+					}
+					else if (flags & RecOffset)
+					{
+						Quad4(-t.Translation.x, -t.Translation.y, -t.Translation.z, 0.0f);
+					}
+					if (flags & RecScale) Quad4(t.Scalation, 0.0f, 0.0f, 0.0f);
+					break;
+				}
+				case NodeKind::Set:
+					Distance(*n.Lhs);
+					Distance(*n.Rhs);
+					Quad(n.Op, IsBlendOp(n.Op) ? n.Threshold : 0.0f, 0.0f, 0.0f);
+					break;
+				case NodeKind::Flate:
+					Distance(*n.Lhs);
+					Quad(OpFlate, n.Threshold, 0.0f, 0.0f);
+					break;
+				case NodeKind::Stencil:
+					Distance(*n.Lhs);
+					break;
+				}
+			}
+
+			// Surface program: the subtree as SDFNode::Eval / GetMaterial walk it.
+			void Surface(const Node& n)
+			{
+				switch (n.Kind)
+				{
+				case NodeKind::Brush:
+				{
+					const Transform& t = n.Xf;
+					const Quat qi = Inverse(t.Rotation);
+					Quad(n.Op, n.Params[0], n.Params[1], n.Params[2]);
+					Quad4(qi.w, qi.x, qi.y, qi.z);
+					Quad4(t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
+					Quad((uint32_t)MaterialIndex(n.Mat.get()), 0.0f, 0.0f, 0.0f);
+					break;
+				}
+				case NodeKind::Set:
+				{
+					Surface(*n.Lhs);
+					Surface(*n.Rhs);
+					uint32_t flags = 0;
+					if (n.Lhs->HasPaint()) flags |= RecLhsPaint;
+					if (n.Rhs->HasPaint()) flags |= RecRhsPaint;
+					Quad(n.Op | flags, n.Threshold, 0.0f, 0.0f);
+					break;
+				}
+				case NodeKind::Flate:
+					Surface(*n.Lhs);
+					Quad(OpFlate, n.Threshold, 0.0f, 0.0f);
+					break;
+				case NodeKind::Stencil:
+				{
+					Surface(*n.Lhs);
+					const size_t begin = Code.size();
+					Quad(OpMaskBegin, 0.0f, 0.0f, 0.0f);
+					Surface(*n.Mask);
+					Quad(OpStencilEnd | (n.Negative ? RecNegative : 0u), BitsFloat((uint32_t)MaterialIndex(n.Mat.get())), 0.0f, 0.0f);
+					// Quads to skip after the MaskBegin record when only distances are needed.
+					const int skip = (int)((Code.size() - begin) / 4) - 1;
+					Code[begin + 1] = BitsFloat((uint32_t)skip);
+					break;
+				}
+				}
+			}
+		};
+
+		// Deepest stack a record program reaches (accumulator + spilled operands).
+		int ProgramDepth(const float* code, int start)
+		{
+			int depth = 0, peak = 0;
+			for (int q = start;; )
+			{
+				const uint32_t head = FloatBits(code[q * 4]);
+				const uint32_t op = head & 0xFFu;
+				if (op == OpStop) break;
+				if (IsBrushOp(op))
+				{
+					++depth;
+					if (depth > peak) peak = depth;
+					int extra = 0;
+					if (head & RecMatrix) extra += 3;
+					if (head & RecOffset) extra += 1;
+					if (head & RecScale) extra += 1;
+					q += 1 + extra;
+				}
+				else if (IsSetOp(op)) { --depth; q += 1; }
+				else if (op == OpStencilEnd) { --depth; q += 1; }
+				else { q += 1; }
+			}
+			return peak;
+		}
+
+		int SurfaceDepth(const float* code, int start)
+		{
+			int depth = 0, peak = 0;
+			for (int q = start;; )
+			{
+				const uint32_t op = FloatBits(code[q * 4]) & 0xFFu;
+				if (op == OpStop) break;
+				if (IsBrushOp(op)) { ++depth; if (depth > peak) peak = depth; q += 4; }
+				else if (IsSetOp(op) || op == OpStencilEnd) { --depth; q += 1; }
+				else q += 1;
+			}
+			return peak;
+		}
+	}
+
+	std::vector<uint32_t> CompileReferenceWords(const Node& tree)
+	{
+		std::vector<uint32_t> w;
+		ReferenceWords(tree, w);
+		w.push_back(OpStop);
+		return w;
+	}
+
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error)
+	{
+		const auto t0 = std::chrono::steady_clock::now();
+		Octree octree;
+		if (!octree.Build(root))
+		{
+			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
+			return false;
+		}
+		out = CompiledTree();
+		out.Bounds = root->Bounds();
+		std::unordered_map<const Material*, int> materials;
+		std::vector<const Material*> materialList;
+		Emitter em{ out.Code, materials, materialList };
+		int maxStack = 0;
+		out.Nodes.resize(octree.Cells.size());
+		for (size_t i = 0; i < octree.Cells.size(); ++i)
+		{
+			const Octree::Cell& c = octree.Cells[i];
+			OctNode& n = out.Nodes[i];
+			n.Pivot[0] = c.Pivot.x; n.Pivot[1] = c.Pivot.y; n.Pivot[2] = c.Pivot.z;
+			n.Terminus = c.Terminus ? 1 : 0;
+			for (int k = 0; k < 8; ++k) n.Child[k] = c.Children[k];
+			n.Reserved = 0;
+			const int dist = (int)(out.Code.size() / 4);
+			em.Distance(*c.Evaluator);
+			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+			const int surf = (int)(out.Code.size() / 4);
+			em.Surface(*c.Evaluator);
+			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+			n.DistanceCode = dist;
+			n.SurfaceCode = surf;
+			const int d1 = ProgramDepth(out.Code.data(), dist);
+			const int d2 = SurfaceDepth(out.Code.data(), surf);
+			n.StackSize = d1 > d2 ? d1 : d2;
+			if (n.StackSize > maxStack) maxStack = n.StackSize;
+			out.DistanceQuadsTotal += surf - dist;
+		}
+		if (maxStack > kMaxStack)
+		{
+			error = "tree needs a deeper evaluation stack than the kernels hold";
+			return false;
+		}
+		out.Colors.resize(materialList.size() * 4);
+		for (size_t m = 0; m < materialList.size(); ++m)
+		{
+			for (int ch = 0; ch < 3; ++ch)
+			{
+				// uint8_t(0xFF * c): truncation, as WritePLY(Octree, ...) stores it (export.cpp:309-311).
+				const float v = 255.0f * materialList[m]->Rgb[ch];
+				out.Colors[m * 4 + ch] = (uint8_t)v;
+			}
+			out.Colors[m * 4 + 3] = 255;
+		}
+		out.Header.NodeCount = (int32_t)out.Nodes.size();
+		out.Header.CodeQuads = (int32_t)(out.Code.size() / 4);
+		out.Header.MaterialCount = (int32_t)materialList.size();
+		out.Header.HasPaint = octree.Cells[0].Evaluator->HasPaint() ? 1 : 0;
+		out.Header.MaxStack = maxStack;
+		out.BuildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+		return true;
+	}
+}

@@ -1,0 +1,510 @@
+// CSG tree semantics (see tg_tree.hpp).  Each member names the reference behaviour it
+// reproduces; the float arithmetic matches the reference operation for operation.
+#include "tg_tree.hpp"
+
+#include <cmath>
+#include <limits>
+
+namespace tg
+{
+	NodeRef::NodeRef(const NodeRef& o) : P(o.P)
+	{
+		if (P) P->Refs.fetch_add(1, std::memory_order_relaxed);
+	}
+
+	NodeRef::~NodeRef()
+	{
+		if (P && P->Refs.fetch_sub(1, std::memory_order_acq_rel) == 1) delete P;
+	}
+
+	NodeRef NodeRef::Share(Node* n)
+	{
+		if (n) n->Refs.fetch_add(1, std::memory_order_relaxed);
+		return NodeRef(n);
+	}
+
+	// Virtual Eval (sdf_evaluator.cpp:463-466, 598-601, 774-780, 1059-1062): brushes map
+	// the point through the inverse transform (quaternion form) and rescale the distance.
+	float Node::Eval(Vec3 p) const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: return BrushDistance(Op, Params, Xf.ApplyInv(p)) * Xf.Scalation;
+		case NodeKind::Set: return SetDistance(Op, Lhs->Eval(p), Rhs->Eval(p), Threshold);
+		case NodeKind::Flate: return Lhs->Eval(p) - Threshold;
+		case NodeKind::Stencil: return Lhs->Eval(p);
+		}
+		return 0.0f;
+	}
+
+	// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
+	// that can matter inside the sphere (p, radius).  Union keeps whichever side is near,
+	// Diff keeps its left side, Inter needs both; blending widens the sphere by k.
+	NodeRef Node::Clip(Vec3 p, float radius) const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush:
+			return Eval(p) <= radius ? NodeRef::Share(const_cast<Node*>(this)) : NodeRef();
+		case NodeKind::Stencil:
+		{
+			NodeRef child = Lhs->Clip(p, radius);
+			if (!child) return NodeRef();
+			return SDF::Stencil(std::move(child), Mask, Mat, Negative);
+		}
+		case NodeKind::Flate:
+		{
+			if (!(Eval(p) <= radius)) return NodeRef();
+			NodeRef child = Lhs->Clip(p, radius + Threshold);
+			if (!child) return NodeRef();
+			return SDF::Flate(std::move(child), Threshold);
+		}
+		case NodeKind::Set:
+		{
+			if (!(Eval(p) <= radius)) return NodeRef();
+			const bool unionFamily = (Op == OpUnion || Op == OpBlendUnion);
+			const bool diffFamily = (Op == OpDiff || Op == OpBlendDiff);
+			if (IsBlendOp(Op))
+			{
+				const float wide = radius + Threshold;
+				NodeRef l = Lhs->Clip(p, wide);
+				NodeRef r = Rhs->Clip(p, wide);
+				if (l && r) return SDF::MakeSet(Op, std::move(l), std::move(r), Threshold);
+				if (!unionFamily && !diffFamily) return NodeRef();
+			}
+			NodeRef l = Lhs->Clip(p, radius);
+			NodeRef r = Rhs->Clip(p, radius);
+			if (l && r) return SDF::MakeSet(Op, std::move(l), std::move(r), Threshold);
+			if (unionFamily) return l ? l : r;
+			if (diffFamily) return l;
+			return NodeRef();
+		}
+		}
+		return NodeRef();
+	}
+
+	AABB Node::Bounds() const { return BoundsImpl(false); }
+	AABB Node::InnerBounds() const { return BoundsImpl(true); }
+
+	// Bounds / InnerBounds (sdf_evaluator.cpp:485-493, 622-630, 857-913, 1082-1096).
+	AABB Node::BoundsImpl(bool inner) const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: return Xf.ApplyBounds(BrushBox);
+		case NodeKind::Stencil: return Lhs->BoundsImpl(inner);
+		case NodeKind::Flate:
+		{
+			AABB b = Lhs->BoundsImpl(inner);
+			const float r2 = Threshold * 2.0f;
+			b.Max = b.Max + Vec3(r2);
+			b.Min = b.Min - Vec3(r2);
+			return b;
+		}
+		case NodeKind::Set:
+		{
+			const AABB l = Lhs->BoundsImpl(inner), r = Rhs->BoundsImpl(inner);
+			AABB c;
+			if (Op == OpUnion || Op == OpBlendUnion) { c.Min = TernaryMin(l.Min, r.Min); c.Max = TernaryMax(l.Max, r.Max); }
+			else if (Op == OpDiff || Op == OpBlendDiff) { c = l; }
+			else { c.Min = TernaryMax(l.Min, r.Min); c.Max = TernaryMin(l.Max, r.Max); }
+			if (IsBlendOp(Op) && !inner)
+			{
+				const Vec3 k(Threshold);
+				const Vec3 limMin = TernaryMax(l.Min, r.Min) - k;
+				const Vec3 limMax = TernaryMin(l.Max, r.Max) + k;
+				c.Min = TernaryMin(c.Min, limMin);
+				c.Max = TernaryMax(c.Max, limMax);
+			}
+			return c;
+		}
+		}
+		return {};
+	}
+
+	void Node::Move(Vec3 by)
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: Xf.Move(by); break;
+		case NodeKind::Set: Lhs->Move(by); Rhs->Move(by); break;
+		case NodeKind::Flate: Lhs->Move(by); break;
+		case NodeKind::Stencil: Lhs->Move(by); Mask->Move(by); break;
+		}
+	}
+
+	void Node::Rotate(Quat by)
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: Xf.Rotate(by); break;
+		case NodeKind::Set: Lhs->Rotate(by); Rhs->Rotate(by); break;
+		case NodeKind::Flate: Lhs->Rotate(by); break;
+		case NodeKind::Stencil: Lhs->Rotate(by); Mask->Rotate(by); break;
+		}
+	}
+
+	// Set operators scale their blend threshold too; Flate keeps its radius
+	// (sdf_evaluator.cpp:938-943, 1115-1118).
+	void Node::Scale(float by)
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: Xf.Scale(by); break;
+		case NodeKind::Set: Threshold = Threshold * by; Lhs->Scale(by); Rhs->Scale(by); break;
+		case NodeKind::Flate: Lhs->Scale(by); break;
+		case NodeKind::Stencil: Lhs->Scale(by); Mask->Scale(by); break;
+		}
+	}
+
+	// Paint only brushes without paint unless forced; stencils ignore it
+	// (sdf_evaluator.cpp:524-530, 655-658, 945-949).
+	void Node::ApplyMaterial(const MaterialRef& m, bool force)
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: if (!Mat || force) Mat = m; break;
+		case NodeKind::Set: Lhs->ApplyMaterial(m, force); Rhs->ApplyMaterial(m, force); break;
+		case NodeKind::Flate: Lhs->ApplyMaterial(m, force); break;
+		case NodeKind::Stencil: break;
+		}
+	}
+
+	bool Node::HasPaint() const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: return Mat != nullptr;
+		case NodeKind::Set: return Lhs->HasPaint() || Rhs->HasPaint();
+		case NodeKind::Flate: return Lhs->HasPaint();
+		case NodeKind::Stencil: return true;
+		}
+		return false;
+	}
+
+	bool Node::HasFiniteBounds() const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush:
+			for (int i = 0; i < 3; ++i)
+				if (std::isinf(BrushBox.Min[i]) || std::isinf(BrushBox.Max[i])) return false;
+			return true;
+		case NodeKind::Set: return Lhs->HasFiniteBounds() || Rhs->HasFiniteBounds();
+		default: return Lhs->HasFiniteBounds();
+		}
+	}
+
+	int Node::LeafCount() const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: return 1;
+		case NodeKind::Set: return Lhs->LeafCount() + Rhs->LeafCount();
+		default: return Lhs->LeafCount();
+		}
+	}
+
+	// Structural equality with material identity (sdf_evaluator.cpp:564-579, 696-709,
+	// 1029-1037, 1150-1154).
+	bool Node::Equals(const Node& o) const
+	{
+		if (this == &o) return true;
+		if (Kind != o.Kind) return false;
+		switch (Kind)
+		{
+		case NodeKind::Brush:
+			if (Op != o.Op || Mat != o.Mat || !(Xf == o.Xf)) return false;
+			for (int i = 0; i < BrushParamCount(Op); ++i)
+				if (Params[i] != o.Params[i]) return false;
+			return true;
+		case NodeKind::Set:
+			return Op == o.Op && Threshold == o.Threshold && Lhs->Equals(*o.Lhs) && Rhs->Equals(*o.Rhs);
+		case NodeKind::Flate:
+			return Threshold == o.Threshold && Lhs->Equals(*o.Lhs);
+		case NodeKind::Stencil:
+			return Negative == o.Negative && Mat == o.Mat && Lhs->Equals(*o.Lhs) && Mask->Equals(*o.Mask);
+		}
+		return false;
+	}
+
+	// Tetrahedral gradient with h = 1e-4, forward differences if it vanishes
+	// (sdf_evaluator.cpp:298-333).
+	Vec3 Node::Gradient(Vec3 p) const
+	{
+		const float h = 0.0001f;
+		const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+		Vec3 g = xyy * Eval(p + xyy);
+		g = g + yyx * Eval(p + yyx);
+		g = g + yxy * Eval(p + yxy);
+		g = g + xxx * Eval(p + xxx);
+		const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+		if (ls == 0.0f)
+		{
+			const float d = Eval(p);
+			return Normalize(Vec3(Eval(p + xyy) - d, Eval(p + yxy) - d, Eval(p + yyx) - d));
+		}
+		return g / sqrtf(ls);
+	}
+
+	// GetMaterial (sdf_evaluator.cpp:537-547, 666-679, 957-1012, 1130-1133).
+	const Material* Node::GetMaterial(Vec3 p) const
+	{
+		switch (Kind)
+		{
+		case NodeKind::Brush: return Mat.get();
+		case NodeKind::Flate: return Lhs->GetMaterial(p);
+		case NodeKind::Stencil:
+		{
+			const bool interior = Mask->Eval(p) < 0.0f;
+			return interior == Negative ? Mat.get() : Lhs->GetMaterial(p);
+		}
+		case NodeKind::Set:
+		{
+			if (Op == OpDiff || Op == OpBlendDiff) return Lhs->GetMaterial(p);
+			const float el = Lhs->Eval(p);
+			const float er = Rhs->Eval(p);
+			const float d = SetDistance(Op, el, er, Threshold);
+			const bool takeLeft = IsBlendOp(Op) ? (fabsf(el - d) <= fabsf(er - d)) : (d == el);
+			if (Op == OpUnion || Op == OpBlendUnion) return takeLeft ? Lhs->GetMaterial(p) : Rhs->GetMaterial(p);
+			const Material* ml = Lhs->GetMaterial(p);
+			const Material* mr = Rhs->GetMaterial(p);
+			const bool lv = Lhs->HasPaint(), rv = Rhs->HasPaint();
+			if (lv && rv) return takeLeft ? ml : mr;
+			return lv ? ml : mr;
+		}
+		}
+		return nullptr;
+	}
+
+	// SDFNode::RayMarch (sdf_evaluator.cpp:336-353).
+	RayHit RayMarch(const Node& tree, Vec3 start, Vec3 dir, int max_iterations, float epsilon)
+	{
+		dir = Normalize(dir);
+		Vec3 pos = start;
+		float travel = 0.0f;
+		for (int i = 0; i < max_iterations; ++i)
+		{
+			const float d = tree.Eval(pos);
+			if (d <= epsilon) return { true, travel, pos };
+			travel = travel + d;
+			pos = dir * travel + start;
+		}
+		return { false, std::numeric_limits<float>::infinity(), pos };
+	}
+
+	namespace
+	{
+		NodeRef MakeBrush(uint32_t op, const float* params, AABB box)
+		{
+			Node* n = new Node();
+			n->Kind = NodeKind::Brush;
+			n->Op = op;
+			for (int i = 0; i < BrushParamCount(op); ++i) n->Params[i] = params[i];
+			n->BrushBox = box;
+			n->StackSize = 1;
+			return NodeRef(n);
+		}
+
+		AABB Symmetric(Vec3 h) { return { h * Vec3(-1.0f), h }; }
+	}
+
+	namespace SDF
+	{
+		NodeRef Sphere(float r) { const float p[1] = { r }; return MakeBrush(OpSphere, p, Symmetric(Vec3(r))); }
+		NodeRef Ellipsoid(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpEllipsoid, p, Symmetric(Vec3(x, y, z))); }
+		NodeRef Box(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpBox, p, Symmetric(Vec3(x, y, z))); }
+		NodeRef Torus(float major, float minor)
+		{
+			const float p[2] = { major, minor };
+			const float r = major + minor;
+			return MakeBrush(OpTorus, p, Symmetric(Vec3(r, r, minor)));
+		}
+		NodeRef Cylinder(float radius, float extent)
+		{
+			const float p[2] = { radius, extent };
+			return MakeBrush(OpCylinder, p, Symmetric(Vec3(radius, radius, extent)));
+		}
+		// Unit normal; infinite bounds, halved when the normal is an axis (sdf_evaluator.cpp:1260-1294).
+		NodeRef Plane(float nx, float ny, float nz)
+		{
+			const Vec3 n = Normalize(Vec3(nx, ny, nz));
+			const float p[3] = { n.x, n.y, n.z };
+			const float inf = std::numeric_limits<float>::infinity();
+			AABB b = Symmetric(Vec3(inf));
+			if (n.x == -1.0f) b.Min.x = 0.0f;
+			else if (n.x == 1.0f) b.Max.x = 0.0f;
+			else if (n.y == -1.0f) b.Min.y = 0.0f;
+			else if (n.y == 1.0f) b.Max.y = 0.0f;
+			else if (n.z == -1.0f) b.Min.z = 0.0f;
+			else if (n.z == 1.0f) b.Max.z = 0.0f;
+			return MakeBrush(OpPlane, p, b);
+		}
+		NodeRef Cone(float radius, float height)
+		{
+			const float p[2] = { radius / height, height };
+			return MakeBrush(OpCone, p, Symmetric(Vec3(radius, radius, (float)((double)height * 0.5))));
+		}
+		NodeRef Coninder(float rl, float rh, float height)
+		{
+			const float half = (float)((double)height * 0.5);
+			const float p[3] = { rl, rh, half };
+			const float mr = fmaxf(rl, rh);
+			return MakeBrush(OpConinder, p, Symmetric(Vec3(mr, mr, half)));
+		}
+
+		// Non-Diff operators put the operand with the deeper stack on the left
+		// (sdf_evaluator.cpp:759-771); the stack need is max(L, R + 1).
+		NodeRef MakeSet(uint32_t op, NodeRef lhs, NodeRef rhs, float k)
+		{
+			const bool diff = (op == OpDiff || op == OpBlendDiff);
+			if (!diff && rhs->StackSize > lhs->StackSize) std::swap(lhs, rhs);
+			Node* n = new Node();
+			n->Kind = NodeKind::Set;
+			n->Op = op;
+			n->Threshold = k;
+			n->StackSize = lhs->StackSize > rhs->StackSize + 1 ? lhs->StackSize : rhs->StackSize + 1;
+			n->Lhs = std::move(lhs);
+			n->Rhs = std::move(rhs);
+			return NodeRef(n);
+		}
+		NodeRef Union(NodeRef l, NodeRef r) { return MakeSet(OpUnion, std::move(l), std::move(r), 0.0f); }
+		NodeRef Diff(NodeRef l, NodeRef r) { return MakeSet(OpDiff, std::move(l), std::move(r), 0.0f); }
+		NodeRef Inter(NodeRef l, NodeRef r) { return MakeSet(OpInter, std::move(l), std::move(r), 0.0f); }
+		NodeRef BlendUnion(float k, NodeRef l, NodeRef r) { return MakeSet(OpBlendUnion, std::move(l), std::move(r), k); }
+		NodeRef BlendDiff(float k, NodeRef l, NodeRef r) { return MakeSet(OpBlendDiff, std::move(l), std::move(r), k); }
+		NodeRef BlendInter(float k, NodeRef l, NodeRef r) { return MakeSet(OpBlendInter, std::move(l), std::move(r), k); }
+
+		NodeRef Flate(NodeRef node, float radius)
+		{
+			Node* n = new Node();
+			n->Kind = NodeKind::Flate;
+			n->StackSize = node->StackSize;
+			n->Threshold = radius;
+			n->Lhs = std::move(node);
+			return NodeRef(n);
+		}
+
+		NodeRef Stencil(NodeRef node, NodeRef mask, MaterialRef material, bool negative)
+		{
+			Node* n = new Node();
+			n->Kind = NodeKind::Stencil;
+			n->StackSize = node->StackSize;
+			n->Mat = std::move(material);
+			n->Negative = negative;
+			n->Lhs = std::move(node);
+			n->Mask = std::move(mask);
+			return NodeRef(n);
+		}
+
+		// Move the tree so the anchor point of its inner bounds sits at the origin;
+		// anchors are in [-1, 1] per axis (sdf_evaluator.cpp:1171-1177).
+		void Align(Node& tree, Vec3 anchors)
+		{
+			const Vec3 a = anchors * Vec3(0.5f) + Vec3(0.5f);
+			const AABB b = tree.InnerBounds();
+			const Vec3 mixed = b.Min * (Vec3(1.0f) - a) + b.Max * a;
+			tree.Move(mixed * Vec3(-1.0f));
+		}
+
+		static void RotateAxis(Node& tree, int axis, float degrees)
+		{
+			const float r = (float)((double)(degrees * 0.01745329251994329576923690768489f) * .5);
+			const float s = sinf(r), c = cosf(r);
+			Quat q{ c, 0.0f, 0.0f, 0.0f };
+			(&q.x)[axis] = s;
+			tree.Rotate(q);
+		}
+		void RotateX(Node& tree, float degrees) { RotateAxis(tree, 0, degrees); }
+		void RotateY(Node& tree, float degrees) { RotateAxis(tree, 1, degrees); }
+		void RotateZ(Node& tree, float degrees) { RotateAxis(tree, 2, degrees); }
+	}
+
+	// Tree spec op codes (tangerine_gb300/workloads.py).
+	namespace
+	{
+		enum SpecOp
+		{
+			SpecSphere = 1, SpecEllipsoid, SpecBox, SpecTorus, SpecCylinder, SpecPlane, SpecCone, SpecConinder,
+			SpecUnion, SpecDiff, SpecInter, SpecBlendUnion, SpecBlendDiff, SpecBlendInter, SpecFlate,
+			SpecMove, SpecRotate, SpecScale, SpecPaint, SpecAlign, SpecStencil,
+		};
+
+		int SpecArity(int op)
+		{
+			switch (op)
+			{
+			case SpecSphere: return 1;
+			case SpecEllipsoid: case SpecBox: case SpecPlane: case SpecConinder: return 3;
+			case SpecTorus: case SpecCylinder: case SpecCone: return 2;
+			case SpecUnion: case SpecDiff: case SpecInter: return 0;
+			case SpecBlendUnion: case SpecBlendDiff: case SpecBlendInter: case SpecFlate: return 1;
+			case SpecMove: case SpecPaint: case SpecAlign: return 3;
+			case SpecRotate: case SpecStencil: return 4;
+			case SpecScale: return 1;
+			default: return -1;
+			}
+		}
+	}
+
+	NodeRef BuildFromSpec(const float* spec, int count, const char** error)
+	{
+		std::vector<NodeRef> stack;
+		int i = 0;
+		auto fail = [&](const char* why) { if (error) *error = why; return NodeRef(); };
+		while (i < count)
+		{
+			const int op = (int)spec[i++];
+			const int arity = SpecArity(op);
+			if (arity < 0) return fail("unknown tree spec op");
+			if (i + arity > count) return fail("truncated tree spec");
+			const float* P = spec + i;
+			i += arity;
+			const size_t need = (op >= SpecUnion && op <= SpecBlendInter) || op == SpecStencil ? 2 :
+				(op >= SpecFlate ? 1 : 0);
+			if (stack.size() < need) return fail("tree spec stack underflow");
+			switch (op)
+			{
+			case SpecSphere: stack.push_back(SDF::Sphere(P[0])); break;
+			case SpecEllipsoid: stack.push_back(SDF::Ellipsoid(P[0], P[1], P[2])); break;
+			case SpecBox: stack.push_back(SDF::Box(P[0], P[1], P[2])); break;
+			case SpecTorus: stack.push_back(SDF::Torus(P[0], P[1])); break;
+			case SpecCylinder: stack.push_back(SDF::Cylinder(P[0], P[1])); break;
+			case SpecPlane: stack.push_back(SDF::Plane(P[0], P[1], P[2])); break;
+			case SpecCone: stack.push_back(SDF::Cone(P[0], P[1])); break;
+			case SpecConinder: stack.push_back(SDF::Coninder(P[0], P[1], P[2])); break;
+			case SpecUnion: case SpecDiff: case SpecInter: case SpecBlendUnion: case SpecBlendDiff: case SpecBlendInter:
+			{
+				static const uint32_t map[] = { OpUnion, OpDiff, OpInter, OpBlendUnion, OpBlendDiff, OpBlendInter };
+				NodeRef r = std::move(stack.back()); stack.pop_back();
+				NodeRef l = std::move(stack.back()); stack.pop_back();
+				stack.push_back(SDF::MakeSet(map[op - SpecUnion], std::move(l), std::move(r), op >= SpecBlendUnion ? P[0] : 0.0f));
+				break;
+			}
+			case SpecFlate: stack.back() = SDF::Flate(std::move(stack.back()), P[0]); break;
+			case SpecMove: stack.back()->Move(Vec3(P[0], P[1], P[2])); break;
+			case SpecRotate: stack.back()->Rotate(Quat{ P[3], P[0], P[1], P[2] }); break;
+			case SpecScale: stack.back()->Scale(P[0]); break;
+			case SpecPaint:
+			{
+				auto m = std::make_shared<Material>();
+				m->Rgb[0] = P[0]; m->Rgb[1] = P[1]; m->Rgb[2] = P[2];
+				stack.back()->ApplyMaterial(m, false);
+				break;
+			}
+			case SpecAlign: SDF::Align(*stack.back(), Vec3(P[0], P[1], P[2])); break;
+			case SpecStencil:
+			{
+				NodeRef mask = std::move(stack.back()); stack.pop_back();
+				NodeRef node = std::move(stack.back()); stack.pop_back();
+				auto m = std::make_shared<Material>();
+				m->Rgb[0] = P[1]; m->Rgb[1] = P[2]; m->Rgb[2] = P[3];
+				stack.push_back(SDF::Stencil(std::move(node), std::move(mask), m, P[0] != 0.0f));
+				break;
+			}
+			}
+		}
+		if (stack.size() != 1) return fail("tree spec does not reduce to one tree");
+		return std::move(stack.back());
+	}
+}

@@ -1,0 +1,123 @@
+// CSG trees: the host-side model of Tangerine's SDFNode hierarchy
+// (tangerine/sdf_evaluator.h:171-264).  A tree is built from brushes and operators,
+// mutated by Move/Rotate/Scale/ApplyMaterial while it is being assembled, and then only
+// read: clipping makes new nodes that share the unchanged subtrees.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "tg_math.hpp"
+#include "tg_sdfmath.hpp"
+
+namespace tg
+{
+	// A material is an sRGB base colour; two materials are the same material only if they
+	// are the same object (MaterialInterface::operator==, sdf_evaluator.h:66-67).
+	struct Material
+	{
+		float Rgb[3];
+	};
+	using MaterialRef = std::shared_ptr<const Material>;
+
+	enum class NodeKind : uint8_t { Brush, Set, Flate, Stencil };
+
+	struct Node;
+
+	// Intrusive reference: the C ABI hands these out as plain pointers.
+	class NodeRef
+	{
+	public:
+		NodeRef() = default;
+		explicit NodeRef(Node* adopt) : P(adopt) {}
+		NodeRef(const NodeRef& o);
+		NodeRef(NodeRef&& o) noexcept : P(o.P) { o.P = nullptr; }
+		NodeRef& operator=(NodeRef o) { std::swap(P, o.P); return *this; }
+		~NodeRef();
+		Node* get() const { return P; }
+		Node* operator->() const { return P; }
+		Node& operator*() const { return *P; }
+		explicit operator bool() const { return P != nullptr; }
+		Node* release() { Node* r = P; P = nullptr; return r; }
+		static NodeRef Share(Node* n);
+	private:
+		Node* P = nullptr;
+	};
+
+	struct Node
+	{
+		std::atomic<int> Refs{ 1 };
+		NodeKind Kind = NodeKind::Brush;
+		uint32_t Op = OpStop;
+		int StackSize = 1;
+
+		// Brush
+		float Params[3] = { 0.0f, 0.0f, 0.0f };
+		AABB BrushBox{};
+		Transform Xf;
+		MaterialRef Mat;
+
+		// Set (Lhs, Rhs, Threshold), Flate (Lhs = child, Threshold = radius),
+		// Stencil (Lhs = child, Mask, Mat, Negative).
+		NodeRef Lhs, Rhs, Mask;
+		float Threshold = 0.0f;
+		bool Negative = false;
+
+		float Eval(Vec3 p) const;
+		NodeRef Clip(Vec3 p, float radius) const;
+		AABB Bounds() const;
+		AABB InnerBounds() const;
+		void Move(Vec3 by);
+		void Rotate(Quat by);
+		void Scale(float by);
+		void ApplyMaterial(const MaterialRef& m, bool force);
+		bool HasPaint() const;
+		bool HasFiniteBounds() const;
+		int LeafCount() const;
+		bool Equals(const Node& o) const;
+		Vec3 Gradient(Vec3 p) const;
+		const Material* GetMaterial(Vec3 p) const;   // nullptr: the default white
+	private:
+		AABB BoundsImpl(bool inner) const;
+	};
+
+	struct RayHit
+	{
+		bool Hit;
+		float Travel;
+		Vec3 Position;
+	};
+	RayHit RayMarch(const Node& tree, Vec3 start, Vec3 dir, int max_iterations, float epsilon);
+
+	// Constructors and helpers with the SDF:: semantics (sdf_evaluator.cpp:1169-1372).
+	namespace SDF
+	{
+		NodeRef Sphere(float radius);
+		NodeRef Ellipsoid(float rx, float ry, float rz);
+		NodeRef Box(float ex, float ey, float ez);
+		NodeRef Torus(float major, float minor);
+		NodeRef Cylinder(float radius, float extent);
+		NodeRef Plane(float nx, float ny, float nz);
+		NodeRef Cone(float radius, float height);
+		NodeRef Coninder(float radius_low, float radius_high, float height);
+		NodeRef Union(NodeRef lhs, NodeRef rhs);
+		NodeRef Diff(NodeRef lhs, NodeRef rhs);
+		NodeRef Inter(NodeRef lhs, NodeRef rhs);
+		NodeRef BlendUnion(float k, NodeRef lhs, NodeRef rhs);
+		NodeRef BlendDiff(float k, NodeRef lhs, NodeRef rhs);
+		NodeRef BlendInter(float k, NodeRef lhs, NodeRef rhs);
+		NodeRef Flate(NodeRef node, float radius);
+		NodeRef Stencil(NodeRef node, NodeRef mask, MaterialRef material, bool apply_to_negative);
+		void Align(Node& tree, Vec3 anchors);
+		void RotateX(Node& tree, float degrees);
+		void RotateY(Node& tree, float degrees);
+		void RotateZ(Node& tree, float degrees);
+		NodeRef MakeSet(uint32_t op, NodeRef lhs, NodeRef rhs, float k);
+	}
+
+	// Builds a tree from a postfix tree spec (the word stream tangerine_gb300.workloads
+	// writes).  Returns an empty ref and fills `error` on a malformed spec.
+	NodeRef BuildFromSpec(const float* spec, int count, const char** error);
+}

@@ -1,0 +1,248 @@
+// Device-side evaluation of compiled trees (record format: tg_layout.hpp).
+//
+// Every kernel translation unit that includes this header is compiled with -fmad=false:
+// the reference's x86-64 Release build never fuses a multiply and an add, and bit-exact
+// distances need the same roundings.  Division and square root are IEEE (no fast math).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../host/tg_layout.hpp"
+#include "../host/tg_sdfmath.hpp"
+
+namespace tg
+{
+	// World coordinate of lattice index i: x0 + float(i) * step, the rounding the export
+	// grid uses (surface_nets.cpp get_world_point_of / get_voxel_corner_world_positions).
+	__device__ __forceinline__ float LatticeCoord(float origin, int i, float step)
+	{
+		return origin + static_cast<float>(i) * step;
+	}
+
+	// SDFOctree::Descend(Point, Exact = true) (sdf_evaluator.cpp:1801-1835): follow the
+	// pivot octant while a child exists; a missing child means this cell's own evaluator.
+	__device__ __forceinline__ int DescendOctree(const OctNode* __restrict__ nodes, float x, float y, float z)
+	{
+		int at = 0;
+		for (int guard = 0; guard < 64; ++guard)
+		{
+			const float4 a = __ldg(reinterpret_cast<const float4*>(nodes + at));
+			if (__float_as_int(a.w) != 0) break;          // Terminus
+			const int octant = (x > a.x ? 1 : 0) | (y > a.y ? 2 : 0) | (z > a.z ? 4 : 0);
+			const int child = __ldg(&nodes[at].Child[octant]);
+			if (child < 0) break;
+			at = child;
+		}
+		return at;
+	}
+
+	__device__ __forceinline__ float4 LoadQuad(const float4* __restrict__ code, int q)
+	{
+		return __ldg(code + q);
+	}
+
+	// Runs a distance program for K points at once (one record stream, K accumulators).
+	// `spill` is this thread's column of the operand stack in shared memory: entry
+	// (depth, lane) lives at spill[(depth * K + lane) * stride].
+	template<int K>
+	__device__ __forceinline__ void RunDistance(const float4* __restrict__ code, int pc,
+		const float (&px)[K], const float (&py)[K], const float (&pz)[K], float (&out)[K],
+		float* spill, int stride)
+	{
+		float acc[K];
+#pragma unroll
+		for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+		int depth = 0;
+		for (int guard = 0; guard < (1 << 24); ++guard)
+		{
+			const float4 h = LoadQuad(code, pc++);
+			const uint32_t head = __float_as_uint(h.x);
+			const uint32_t op = head & 0xFFu;
+			if (op >= OpSphere && op <= OpPlane)
+			{
+				if (depth > 0)
+				{
+#pragma unroll
+					for (int k = 0; k < K; ++k) spill[((depth - 1) * K + k) * stride] = acc[k];
+				}
+				++depth;
+				float qx[K], qy[K], qz[K];
+				if (head & RecMatrix)
+				{
+					const float4 X = LoadQuad(code, pc), Y = LoadQuad(code, pc + 1), Z = LoadQuad(code, pc + 2);
+					pc += 3;
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+					{
+						// (M * vec4(p, 1)).xyz = (m0*x + m1*y) + (m2*z + m3)
+						qx[k] = (X.x * px[k] + X.y * py[k]) + (X.z * pz[k] + X.w);
+						qy[k] = (Y.x * px[k] + Y.y * py[k]) + (Y.z * pz[k] + Y.w);
+						qz[k] = (Z.x * px[k] + Z.y * py[k]) + (Z.z * pz[k] + Z.w);
+					}
+				}
+				else if (head & RecOffset)
+				{
+					const float4 O = LoadQuad(code, pc++);
+#pragma unroll
+					for (int k = 0; k < K; ++k) { qx[k] = px[k] + O.x; qy[k] = py[k] + O.y; qz[k] = pz[k] + O.z; }
+				}
+				else
+				{
+#pragma unroll
+					for (int k = 0; k < K; ++k) { qx[k] = px[k]; qy[k] = py[k]; qz[k] = pz[k]; }
+				}
+				const float prm[3] = { h.y, h.z, h.w };
+				switch (op)
+				{
+				case OpSphere:
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = SdSphere(Vec3(qx[k], qy[k], qz[k]), prm[0]);
+					break;
+				case OpBox:
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = SdBox(Vec3(qx[k], qy[k], qz[k]), Vec3(prm[0], prm[1], prm[2]));
+					break;
+				case OpTorus:
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = SdTorus(Vec3(qx[k], qy[k], qz[k]), prm[0], prm[1]);
+					break;
+				case OpCylinder:
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = SdCylinder(Vec3(qx[k], qy[k], qz[k]), prm[0], prm[1]);
+					break;
+				default:
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = BrushDistance(op, prm, Vec3(qx[k], qy[k], qz[k]));
+					break;
+				}
+				if (head & RecScale)
+				{
+					const float4 S = LoadQuad(code, pc++);
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = acc[k] * S.x;
+				}
+			}
+			else if (op >= OpUnion && op <= OpBlendDiff)
+			{
+				--depth;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					const float l = spill[((depth - 1) * K + k) * stride];
+					acc[k] = SetDistance(op, l, acc[k], h.y);
+				}
+			}
+			else if (op == OpFlate)
+			{
+#pragma unroll
+				for (int k = 0; k < K; ++k) acc[k] = acc[k] - h.y;
+			}
+			else
+			{
+				break;   // OpStop
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < K; ++k) out[k] = acc[k];
+	}
+
+	// Surface program: SDFNode::Eval (and, with `material`, GetMaterial) at one point.
+	// Returns the distance; *material receives the material index (-1: default white).
+	__device__ __forceinline__ float RunSurface(const float4* __restrict__ code, int pc, Vec3 p, bool material, int* material_out)
+	{
+		float dst[kMaxStack];
+		int mat[kMaxStack];
+		int depth = 0;
+		for (int guard = 0; guard < (1 << 24); ++guard)
+		{
+			const float4 h = LoadQuad(code, pc++);
+			const uint32_t head = __float_as_uint(h.x);
+			const uint32_t op = head & 0xFFu;
+			if (op >= OpSphere && op <= OpPlane)
+			{
+				const float4 Q = LoadQuad(code, pc);
+				const float4 T = LoadQuad(code, pc + 1);
+				const float4 M = LoadQuad(code, pc + 2);
+				pc += 3;
+				// BrushFn(ApplyInv(p)) * s, ApplyInv(p) = rotate(inverse(q), p - t) / s
+				const Quat qi{ Q.x, Q.y, Q.z, Q.w };
+				const Vec3 local = Rotate(qi, p - Vec3(T.x, T.y, T.z)) / T.w;
+				const float prm[3] = { h.y, h.z, h.w };
+				dst[depth] = BrushDistance(op, prm, local) * T.w;
+				mat[depth] = __float_as_int(M.x);
+				++depth;
+			}
+			else if (op >= OpUnion && op <= OpBlendDiff)
+			{
+				--depth;
+				const float r = dst[depth], l = dst[depth - 1];
+				const float d = SetDistance(op, l, r, h.y);
+				if (material)
+				{
+					// SetNode::GetMaterial (sdf_evaluator.cpp:957-1012).
+					int m;
+					if (op == OpDiff || op == OpBlendDiff) m = mat[depth - 1];
+					else
+					{
+						const bool blend = (op == OpBlendUnion || op == OpBlendInter);
+						const bool takeLeft = blend ? (fabsf(l - d) <= fabsf(r - d)) : (d == l);
+						if (op == OpUnion || op == OpBlendUnion) m = takeLeft ? mat[depth - 1] : mat[depth];
+						else
+						{
+							const bool lv = (head & RecLhsPaint) != 0, rv = (head & RecRhsPaint) != 0;
+							if (lv && rv) m = takeLeft ? mat[depth - 1] : mat[depth];
+							else m = lv ? mat[depth - 1] : mat[depth];
+						}
+					}
+					mat[depth - 1] = m;
+				}
+				dst[depth - 1] = d;
+			}
+			else if (op == OpFlate)
+			{
+				dst[depth - 1] = dst[depth - 1] - h.y;
+			}
+			else if (op == OpMaskBegin)
+			{
+				if (!material) pc += (int)__float_as_uint(h.y);
+			}
+			else if (op == OpStencilEnd)
+			{
+				// StencilMaskNode::GetMaterial (sdf_evaluator.cpp:666-679).
+				--depth;
+				const bool interior = dst[depth] < 0.0f;
+				const bool negative = (head & RecNegative) != 0;
+				if (interior == negative) mat[depth - 1] = (int)__float_as_uint(h.y);
+			}
+			else
+			{
+				break;   // OpStop
+			}
+		}
+		if (material_out) *material_out = mat[0];
+		return dst[0];
+	}
+
+	// SDFNode::Gradient (sdf_evaluator.cpp:298-333) on a surface program.
+	__device__ __forceinline__ Vec3 SurfaceGradient(const float4* __restrict__ code, int pc, Vec3 p)
+	{
+		const float h = 0.0001f;
+		const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+		const float e0 = RunSurface(code, pc, p + xyy, false, nullptr);
+		const float e1 = RunSurface(code, pc, p + yyx, false, nullptr);
+		const float e2 = RunSurface(code, pc, p + yxy, false, nullptr);
+		const float e3 = RunSurface(code, pc, p + xxx, false, nullptr);
+		Vec3 g = xyy * e0;
+		g = g + yyx * e1;
+		g = g + yxy * e2;
+		g = g + xxx * e3;
+		const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+		if (ls == 0.0f)
+		{
+			const float d = RunSurface(code, pc, p, false, nullptr);
+			return Normalize(Vec3(e0 - d, e2 - d, e1 - d));
+		}
+		return g / sqrtf(ls);
+	}
+}

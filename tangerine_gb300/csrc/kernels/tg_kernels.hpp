@@ -1,0 +1,55 @@
+// Host-callable launchers for the export kernels.  All take device pointers and a
+// stream and return a cudaError_t; none allocates.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../host/tg_layout.hpp"
+
+namespace tg
+{
+	struct DeviceProgram
+	{
+		const OctNode* Nodes;
+		const float4* Code;
+		const uchar4* Colors;
+		int MaxStack;
+	};
+
+	// Distances at every lattice point (x fastest), SDFOctree::Eval(p, Exact = true).
+	cudaError_t LaunchEvalGrid(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream);
+
+	// Surface nets, cell pass part 1: one bit per cell (x fastest) set when the cell's
+	// eight corners do not all share a sign.  `words` holds ceil(cells / 32) words.
+	cudaError_t LaunchCellFlags(const float* lattice, const GridSpec& grid, uint32_t* words, cudaStream_t stream);
+
+	// Exclusive prefix sum of popcount(words[i]) (popcount = true) or of counts[i].
+	// `scratch` needs ScanScratchWords(n) words.  `total` (device) receives the sum.
+	size_t ScanScratchWords(int64_t n);
+	cudaError_t LaunchExclusiveScan(const uint32_t* in, int64_t n, bool popcount, uint32_t* out, uint32_t* total,
+		uint32_t* scratch, cudaStream_t stream);
+
+	// Cell pass part 2: vertex of every active cell at its rank (cell order), its cube
+	// index, and how many triangles the face pass will emit for it.
+	cudaError_t LaunchCellVertices(const float* lattice, const GridSpec& grid, const uint32_t* words, const uint32_t* word_base,
+		float* vertices, uint32_t* cubes, uint32_t* face_counts, int64_t cells, cudaStream_t stream);
+
+	// Face pass: triangles (v0, v1, v2) per active cell, at face_base[vertex].
+	cudaError_t LaunchFaces(const float* lattice, const GridSpec& grid, const uint32_t* words, const uint32_t* word_base,
+		const uint32_t* cubes, const uint32_t* face_base, uint32_t vertex_count, uint32_t* faces, cudaStream_t stream);
+
+	// Octree distances at arbitrary points (3 floats per point).
+	cudaError_t LaunchEvalPoints(const DeviceProgram& prog, const float* points, int64_t n, float* out, cudaStream_t stream);
+
+	// Gradient normal at each triangle's centroid, as WriteSTL(Octree, ...) writes it.
+	cudaError_t LaunchFaceNormals(const DeviceProgram& prog, const float* vertices, const uint32_t* faces, uint64_t face_count,
+		float* normals, cudaStream_t stream);
+
+	// Achieved FP32 fused-multiply-add throughput of this GPU (TFLOP/s, 2 flops per FMA).
+	cudaError_t MeasureFp32Peak(double* tflops, cudaStream_t stream);
+
+	// Gradient normal and colour bytes per vertex (SDFOctree::Gradient / GetMaterial).
+	cudaError_t LaunchVertexAttributes(const DeviceProgram& prog, const float* vertices, uint32_t vertex_count,
+		float* normals, uint8_t* colors, cudaStream_t stream);
+}

@@ -1,0 +1,270 @@
+"""Python face of the engine: CSG trees through Tangerine's C API and GPU export through
+the tg_* entry points (include/tangerine_gb300.h).
+
+    tree = sdf.from_spec(workloads.random_tree(1, 256))
+    with sdf.compile(tree) as prog:
+        mesh = prog.export_mesh(workloads.export_grid(resolution=512))
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load
+
+
+class Tree:
+    """A reference-counted CSG tree handle (c_sdf.cpp's `void*` trees)."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise _lib.TangerineError(load().tg_last_error().decode() or "null tree")
+        self.handle = C.c_void_p(handle)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and h.value and _lib._LIB is not None:
+            _lib._LIB.DiscardTree(h)
+            self.handle = C.c_void_p(None)
+
+    def _give(self):
+        """Hands this handle's reference to an operator (the Python object is emptied)."""
+        h = self.handle
+        self.handle = C.c_void_p(None)
+        return h
+
+    def eval(self, x, y, z) -> float:
+        return load().EvalTree(self.handle, x, y, z)
+
+    def clip(self, point, radius):
+        h = load().ClipTree(self.handle, float(point[0]), float(point[1]), float(point[2]), float(radius))
+        return Tree(h) if h else None
+
+    def ray_march(self, start, direction, iterations=100, epsilon=1e-3):
+        r = load().RayMarchTree(self.handle, *map(float, start), *map(float, direction), iterations, epsilon)
+        return bool(r.Hit), float(r.Travel), tuple(r.Position)
+
+    def finite(self) -> bool:
+        return bool(load().TreeHasFiniteBounds(self.handle))
+
+    def move(self, x, y, z):
+        load().MoveTree(self.handle, x, y, z)
+        return self
+
+    def rotate(self, x, y, z, w):
+        load().RotateTree(self.handle, x, y, z, w)
+        return self
+
+    def align(self, x, y, z):
+        load().AlignTree(self.handle, x, y, z)
+        return self
+
+    def scale(self, s):
+        load().ScaleTree(self.handle, s)
+        return self
+
+    def paint(self, r, g, b):
+        load().PaintTree(r, g, b, self.handle)
+        return self
+
+    def debug_octree(self):
+        """Host-built export octree in the oracle's dump layout: (cells, children, words)."""
+        lib = load()
+        wc = C.c_int64()
+        n = lib.tg_debug_octree(self.handle, None, None, 0, None, 0, C.byref(wc))
+        if n < 0:
+            return None
+        cells = np.zeros((n, 14), np.float32)
+        kids = np.zeros((n, 8), np.int32)
+        words = np.zeros(max(1, wc.value), np.uint32)
+        lib.tg_debug_octree(self.handle, _lib.as_ptr(cells), _lib.as_ptr(kids), n, _lib.as_ptr(words), wc.value, C.byref(wc))
+        return cells, kids, words[: wc.value]
+
+    def reference_words(self) -> np.ndarray:
+        lib = load()
+        n = lib.tg_tree_reference_words(self.handle, None, 0)
+        out = np.zeros(n, np.uint32)
+        lib.tg_tree_reference_words(self.handle, _lib.as_ptr(out), n)
+        return out
+
+
+def sphere(r): return Tree(load().MakeSphereBrush(r))
+def ellipsoid(x, y, z): return Tree(load().MakeEllipsoidBrush(x, y, z))
+def box(x, y, z): return Tree(load().MakeBoxBrush(x, y, z))
+def torus(major, minor): return Tree(load().MakeTorusBrush(major, minor))
+def cylinder(r, e): return Tree(load().MakeCylinderBrush(r, e))
+def plane(x, y, z): return Tree(load().MakePlaneOperand(x, y, z))
+def cone(r, h): return Tree(load().MakeConeBrush(r, h))
+def coninder(rl, rh, h): return Tree(load().MakeConinderBrush(rl, rh, h))
+def union(a: Tree, b: Tree): return Tree(load().MakeUnionOp(a._give(), b._give()))
+def diff(a: Tree, b: Tree): return Tree(load().MakeDiffOp(a._give(), b._give()))
+def inter(a: Tree, b: Tree): return Tree(load().MakeInterOp(a._give(), b._give()))
+def blend_union(k, a: Tree, b: Tree): return Tree(load().MakeBlendUnionOp(k, a._give(), b._give()))
+def blend_diff(k, a: Tree, b: Tree): return Tree(load().MakeBlendDiffOp(k, a._give(), b._give()))
+def blend_inter(k, a: Tree, b: Tree): return Tree(load().MakeBlendInterOp(k, a._give(), b._give()))
+def flate(a: Tree, r): return Tree(load().MakeFlateOp(a._give(), r))
+def stencil(a: Tree, mask: Tree, rgb, negative=False):
+    return Tree(load().MakeStencilOp(a._give(), mask._give(), *map(float, rgb), bool(negative)))
+
+
+def from_spec(spec) -> Tree:
+    spec = np.ascontiguousarray(spec, dtype=np.float32)
+    return Tree(load().BuildTreeFromSpec(_lib.as_ptr(spec), int(spec.size)))
+
+
+@dataclass
+class Mesh:
+    vertices: np.ndarray          # (V, 3) float32
+    normals: np.ndarray           # (V, 3) float32
+    colors: np.ndarray | None     # (V, 3) uint8
+    faces: np.ndarray             # (F, 3) uint32
+    cubes: np.ndarray             # (V,) uint32
+
+
+def _grid(g) -> _lib.Grid:
+    if isinstance(g, _lib.Grid):
+        return g
+    # workloads.ExportGrid: cells -> lattice points
+    return _lib.Grid(g.x0, g.y0, g.z0, g.step, g.sx + 1, g.sy + 1, g.sz + 1)
+
+
+def _take_mesh(hm: _lib.HostMesh) -> Mesh:
+    v, f = int(hm.vertex_count), int(hm.face_count)
+
+    def arr(ptr, n, dtype):
+        if n == 0:
+            return np.zeros(0, dtype)
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+    m = Mesh(arr(hm.vertices, v * 3, np.float32).reshape(v, 3),
+             arr(hm.normals, v * 3, np.float32).reshape(v, 3),
+             arr(hm.colors, v * 3, np.uint8).reshape(v, 3) if hm.colors else None,
+             arr(hm.faces, f * 3, np.uint32).reshape(f, 3),
+             arr(hm.cubes, v, np.uint32))
+    load().tg_mesh_free(C.byref(hm))
+    return m
+
+
+class Program:
+    """A tree compiled for the GPU: export octree + per-cell record programs."""
+
+    def __init__(self, tree: Tree):
+        self.ptr = C.c_void_p()
+        check(load().tg_compile(tree.handle, C.byref(self.ptr)), "tg_compile")
+
+    def close(self):
+        if self.ptr and self.ptr.value:
+            load().tg_program_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        if _lib._LIB is not None:
+            self.close()
+
+    def info(self) -> _lib.ProgramInfo:
+        out = _lib.ProgramInfo()
+        check(load().tg_program_get_info(self.ptr, C.byref(out)), "tg_program_get_info")
+        return out
+
+    def eval_grid(self, grid, out=None, stream=None) -> np.ndarray:
+        g = _grid(grid)
+        if out is None:
+            out = np.empty((g.nz, g.ny, g.nx), np.float32)
+        check(load().tg_eval_grid(self.ptr, C.byref(g), _lib.as_ptr(out), 0, stream), "tg_eval_grid")
+        return out
+
+    def eval_grid_device(self, grid, device_ptr: int, stream=None) -> None:
+        g = _grid(grid)
+        check(load().tg_eval_grid(self.ptr, C.byref(g), C.c_void_p(device_ptr), 1, stream), "tg_eval_grid")
+
+    def eval_points(self, points, stream=None) -> np.ndarray:
+        p = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+        out = np.empty(p.shape[0], np.float32)
+        check(load().tg_eval_points(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), stream), "tg_eval_points")
+        return out
+
+    def export_mesh(self, grid, attributes=True, stream=None) -> Mesh:
+        g = _grid(grid)
+        hm = _lib.HostMesh()
+        check(load().tg_export_mesh(self.ptr, C.byref(g), 1 if attributes else 0, C.byref(hm), stream), "tg_export_mesh")
+        return _take_mesh(hm)
+
+    def export_mesh_device(self, grid, attributes=True, stream=None) -> _lib.DeviceMesh:
+        g = _grid(grid)
+        dm = _lib.DeviceMesh()
+        check(load().tg_export_mesh_device(self.ptr, C.byref(g), 1 if attributes else 0, C.byref(dm), stream),
+              "tg_export_mesh_device")
+        return dm
+
+
+def compile(tree: Tree) -> Program:  # noqa: A001 - mirrors tg_compile
+    return Program(tree)
+
+
+def export_tree(tree: Tree, lo, hi, step, stream=None) -> Mesh:
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    hm = _lib.HostMesh()
+    check(load().tg_export_tree(tree.handle, _lib.as_ptr(lo), _lib.as_ptr(hi), float(step), C.byref(hm), stream),
+          "tg_export_tree")
+    return _take_mesh(hm)
+
+
+def export_grid(lo, hi, step) -> _lib.Grid:
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    g = _lib.Grid()
+    check(load().tg_export_grid(_lib.as_ptr(lo), _lib.as_ptr(hi), float(step), C.byref(g)), "tg_export_grid")
+    return g
+
+
+def write_ply(mesh: Mesh, path, scale=1.0):
+    hm = _host_mesh_view(mesh)
+    check(load().tg_write_ply(C.byref(hm), str(path).encode(), scale), "tg_write_ply")
+
+
+def write_stl(program: Program, mesh: Mesh, path, scale=1.0):
+    hm = _host_mesh_view(mesh)
+    check(load().tg_write_stl(program.ptr, C.byref(hm), str(path).encode(), scale, None), "tg_write_stl")
+
+
+def _host_mesh_view(mesh: Mesh) -> _lib.HostMesh:
+    """A tg_mesh that points into the numpy arrays (kept alive by `mesh`)."""
+    hm = _lib.HostMesh()
+    hm.vertex_count = mesh.vertices.shape[0]
+    hm.face_count = mesh.faces.shape[0]
+    mesh.vertices = np.ascontiguousarray(mesh.vertices, np.float32)
+    mesh.normals = np.ascontiguousarray(mesh.normals, np.float32)
+    mesh.faces = np.ascontiguousarray(mesh.faces, np.uint32)
+    hm.vertices = mesh.vertices.ctypes.data_as(C.POINTER(C.c_float))
+    hm.normals = mesh.normals.ctypes.data_as(C.POINTER(C.c_float))
+    hm.faces = mesh.faces.ctypes.data_as(C.POINTER(C.c_uint32))
+    if mesh.colors is not None:
+        mesh.colors = np.ascontiguousarray(mesh.colors, np.uint8)
+        hm.colors = mesh.colors.ctypes.data_as(C.POINTER(C.c_uint8))
+    return hm
+
+
+def profile_enable(on=True):
+    load().tg_profile_enable(1 if on else 0)
+
+
+def profile_reset():
+    load().tg_profile_reset()
+
+
+def profile_read(kernel: str):
+    ms = C.c_double()
+    n = C.c_int64()
+    load().tg_profile_read(kernel.encode(), C.byref(ms), C.byref(n))
+    return ms.value, n.value

@@ -1,0 +1,98 @@
+"""Writes the golden fixtures in this folder from Tangerine's own CPU code.
+
+Run here, where the reference sources are: it builds oracle/_ref/libtangerine_ref.so
+(``make -C oracle ref``) and records, for a handful of seeded and hand-made CSG trees,
+what the reference computes: program words, the export octree, point distances,
+gradients and colours, naive-surface-nets meshes on small export lattices (with the
+reference's gradient normals and colours per vertex) and RayMarch hits.  The reference
+sources do not travel to the GPU host; these fixtures do.
+
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+from tangerine_gb300 import workloads as W  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def exotic_specs():
+    X = W
+    q = W.axis_quaternion
+    return {
+        "ellipsoid_cone": [X.ELLIPSOID, .5, .3, .7, X.ROTATE, *q(0, 30), X.PAINT, .2, .4, .6,
+                           X.CONE, .4, .8, X.MOVE, .3, .1, -.2, X.PAINT, .9, .1, .1, X.BLEND_INTER, .15],
+        "coninder_flate_scale": [X.CONINDER, .3, .5, .9, X.SCALE, 1.3, X.FLATE, .1, X.BOX, .3, .2, .4, X.ROTATE, *q(2, 47),
+                                 X.PAINT, .5, .5, .1, X.BLEND_DIFF, .2, X.MOVE, .1, .2, .3],
+        "plane_inter": [X.SPHERE, .8, X.PAINT, 1, 0, 0, X.PLANE, .3, 1., .2, X.PAINT, 0, 1, 0, X.INTER,
+                        X.TORUS, .6, .2, X.ROTATE, *q(1, 20), X.UNION],
+        "stencil_align": [X.BOX, .6, .5, .4, X.PAINT, .1, .2, .3, X.SPHERE, .5, X.MOVE, .4, 0, 0, X.STENCIL, 1, .7, .8, .9,
+                          X.ALIGN, -1, 0, 1, X.CYLINDER, .2, .8, X.SCALE, .7, X.UNION],
+        "scaled_blend": [X.SPHERE, .5, X.SPHERE, .4, X.MOVE, .5, 0, 0, X.BLEND_UNION, .2, X.SCALE, 1.7,
+                         X.ROTATE, *q(2, 33), X.TORUS, .5, .1, X.DIFF],
+        "unpainted_union": [X.BOX, .5, .5, .5, X.SPHERE, .6, X.MOVE, .3, .3, .3, X.UNION],
+    }
+
+
+def cases():
+    out = {}
+    for seed in (1, 5, 9):
+        out[f"cfg1_seed{seed}"] = (W.random_tree(seed, 16, ops=W.OPS_UNIFORM4), 48)
+    out["mix64_seed7"] = (W.random_tree(7, 64), 40)
+    for name, spec in exotic_specs().items():
+        out[name] = (np.asarray(spec, np.float32), 40)
+    return out
+
+
+def main():
+    R = O.reference()
+    if R is None:
+        raise SystemExit("the reference sources are not available here")
+    rng = np.random.RandomState(1234)
+    points = rng.uniform(-2.0, 2.0, (2048, 3)).astype(np.float32)
+    ray_o = W.camera_poses(77, 256, radius=4.0)
+    ray_d = (rng.uniform(-0.3, 0.3, (256, 3)) - ray_o / 4.0).astype(np.float32)
+    for name, (spec, res) in cases().items():
+        h = R.build(spec)
+        rec = {"spec": spec, "points": points, "resolution": np.int32(res)}
+        rec["words"] = R.compile(h)
+        rec["stack_size"] = np.int32(R.stack_size(h))
+        rec["bounds"] = R.bounds(h)
+        rec["inner_bounds"] = R.bounds(h, inner=True)
+        rec["eval"] = R.eval(h, points)
+        rec["interp_eval"] = R.interp_eval(h, points)
+        rec["gradient"] = R.gradient(h, points[:512])
+        rec["color"] = R.color(h, points[:512])
+        hit, travel, pos = R.raymarch(h, ray_o, ray_d, iterations=256, epsilon=1e-4, threads=1)
+        rec.update(ray_origins=ray_o, ray_dirs=ray_d, ray_hit=hit, ray_travel=travel, ray_position=pos)
+        o = R.octree(h)
+        if o is not None:
+            nodes, children, words = R.octree_dump(o)
+            rec.update(octree_nodes=nodes, octree_children=children, octree_words=words)
+            rec["octree_eval"] = R.octree_eval(o, points)
+            g = W.export_grid(resolution=res)
+            m = R.surface_nets(o, g, threads=1)
+            rec["grid"] = np.array([g.x0, g.y0, g.z0, g.step, g.sx, g.sy, g.sz], np.float64)
+            rec["mesh_vertices"] = m.vertices
+            rec["mesh_cubes"] = m.cubes
+            rec["mesh_faces"] = m.faces
+            rec["mesh_normals"] = R.octree_gradient(o, m.vertices)
+            rec["mesh_colors"] = R.octree_color(o, m.vertices)
+            R.octree_free(o)
+        R.free(h)
+        np.savez_compressed(OUT / f"{name}.npz", **rec)
+        print(name, "vertices", rec.get("mesh_vertices", np.zeros((0, 3))).shape[0])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,90 @@
+"""Host-side logic of the product library against the reference fixtures: the tree API,
+program words and the export octree are computed on the CPU and must be bit-exact.
+No kernel runs here."""
+
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden_names
+from tangerine_gb300 import _lib, sdf
+from tangerine_gb300 import workloads as W
+
+
+def test_every_declared_symbol_is_exported(lib):
+    header = (ROOT / "include" / "tangerine_gb300.h").read_text()
+    declared = re.findall(r"^TANGERINE_API\s+[^;(]*?\b(\w+)\s*\(", header, flags=re.M)
+    assert len(declared) >= 45
+    for name in declared:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, name
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_tree_api_matches_reference(lib, golden, name):
+    g = golden[name]
+    t = sdf.from_spec(g["spec"])
+    np.testing.assert_array_equal(t.reference_words(), g["words"])
+    got = np.array([t.eval(*p) for p in g["points"][:256]], np.float32)
+    np.testing.assert_array_equal(got, g["eval"][:256])
+    for i in range(0, 256, 16):
+        hit, travel, pos = t.ray_march(g["ray_origins"][i], g["ray_dirs"][i], 256, 1e-4)
+        assert hit == bool(g["ray_hit"][i])
+        assert np.float32(travel) == g["ray_travel"][i]
+        np.testing.assert_array_equal(np.array(pos, np.float32), g["ray_position"][i])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_host_octree_matches_reference(lib, golden, name):
+    g = golden[name]
+    t = sdf.from_spec(g["spec"])
+    dump = t.debug_octree()
+    if "octree_nodes" not in g:
+        assert dump is None
+        return
+    cells, children, words = dump
+    np.testing.assert_array_equal(cells, g["octree_nodes"])
+    np.testing.assert_array_equal(children, g["octree_children"])
+    np.testing.assert_array_equal(words, g["octree_words"])
+
+
+def test_operators_take_over_operands(lib):
+    a = sdf.sphere(0.5)
+    b = sdf.box(0.3, 0.3, 0.3).move(0.4, 0, 0)
+    u = sdf.union(a, b)
+    assert a.handle.value is None and b.handle.value is None
+    assert u.eval(0, 0, 0) == pytest.approx(-0.5)
+    assert u.finite()
+
+
+def test_clip_tree_semantics(lib):
+    t = sdf.union(sdf.sphere(0.5), sdf.sphere(0.5).move(3, 0, 0))
+    near = t.clip((0, 0, 0), 0.6)
+    assert near is not None
+    assert near.eval(3, 0, 0) == pytest.approx(2.5)       # far sphere clipped away
+    assert t.clip((10, 10, 10), 0.1) is None
+
+
+def test_plane_only_tree_has_no_octree(lib):
+    t = sdf.plane(0, 0, 1)
+    assert not t.finite()
+    assert t.debug_octree() is None
+
+
+def test_malformed_spec_is_rejected(lib):
+    with pytest.raises(_lib.TangerineError):
+        sdf.from_spec(np.array([W.UNION], np.float32))
+    with pytest.raises(_lib.TangerineError):
+        sdf.from_spec(np.array([W.SPHERE, 0.5, W.SPHERE, 0.2], np.float32))
+    with pytest.raises(_lib.TangerineError):
+        sdf.from_spec(np.array([99.0], np.float32))
+
+
+def test_export_lattice_matches_mesh_export_thread(lib):
+    for res, cells in ((128, 130), (512, 514), (1024, 1026)):
+        g = sdf.export_grid((-2, -2, -2), (2, 2, 2), 4.0 / res)
+        assert (g.nx, g.ny, g.nz) == (cells + 1,) * 3
+        w = W.export_grid(resolution=res)
+        assert (w.sx, w.x0, w.step) == (cells, g.x0, g.step)

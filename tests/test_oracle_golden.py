@@ -1,0 +1,77 @@
+"""The C restatement (oracle/port) against fixtures written by Tangerine's own code.
+
+Everything here is bit-exact: the oracle keeps the reference's float operation order."""
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, sorted_faces
+from tangerine_gb300 import workloads as W
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_tree_semantics(port, golden, name):
+    g = golden[name]
+    h = port.build(g["spec"])
+    try:
+        np.testing.assert_array_equal(port.compile(h), g["words"])
+        assert port.stack_size(h) == int(g["stack_size"])
+        np.testing.assert_array_equal(port.bounds(h), g["bounds"])
+        np.testing.assert_array_equal(port.bounds(h, inner=True), g["inner_bounds"])
+        np.testing.assert_array_equal(port.eval(h, g["points"]), g["eval"])
+        np.testing.assert_array_equal(port.interp_eval(h, g["points"]), g["interp_eval"])
+        np.testing.assert_array_equal(port.gradient(h, g["points"][:512]), g["gradient"])
+        np.testing.assert_array_equal(port.color(h, g["points"][:512]), g["color"])
+        hit, travel, pos = port.raymarch(h, g["ray_origins"], g["ray_dirs"], iterations=256, epsilon=1e-4, threads=1)
+        np.testing.assert_array_equal(hit, g["ray_hit"])
+        np.testing.assert_array_equal(travel, g["ray_travel"])
+        np.testing.assert_array_equal(pos, g["ray_position"])
+    finally:
+        port.free(h)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_octree_and_mesh(port, golden, name):
+    g = golden[name]
+    if "octree_nodes" not in g:
+        pytest.skip("no octree for this tree")
+    h = port.build(g["spec"])
+    o = port.octree(h)
+    try:
+        nodes, children, words = port.octree_dump(o)
+        np.testing.assert_array_equal(nodes, g["octree_nodes"])
+        np.testing.assert_array_equal(children, g["octree_children"])
+        np.testing.assert_array_equal(words, g["octree_words"])
+        np.testing.assert_array_equal(port.octree_eval(o, g["points"]), g["octree_eval"])
+        x0, y0, z0, step, sx, sy, sz = g["grid"]
+        grid = W.ExportGrid(float(x0), float(y0), float(z0), float(step), int(sx), int(sy), int(sz))
+        for faithful in (False, True):
+            m = port.surface_nets(o, grid, threads=2, faithful=faithful)
+            np.testing.assert_array_equal(m.vertices, g["mesh_vertices"])
+            np.testing.assert_array_equal(m.cubes, g["mesh_cubes"])
+            np.testing.assert_array_equal(sorted_faces(m.faces), sorted_faces(g["mesh_faces"]))
+        normals, colors = port.vertex_attributes(o, g["mesh_vertices"], threads=2)
+        np.testing.assert_array_equal(normals, g["mesh_normals"])
+        if colors is not None:
+            np.testing.assert_array_equal(colors, g["mesh_colors"])
+    finally:
+        port.octree_free(o)
+        port.free(h)
+
+
+def test_planted_mistake_is_caught(port, golden):
+    """Primitive sizes 0.1% off in the oracle's input must change what the checks compare."""
+    g = golden["cfg1_seed1"]
+    spec = np.array(g["spec"], np.float32)
+    i = 0
+    while i < spec.size:
+        op = int(spec[i])
+        if op <= W.CONINDER:
+            spec[i + 1] *= np.float32(1.001)
+        i += 1 + W.ARITY[op]
+    h = port.build(spec)
+    try:
+        assert not np.array_equal(port.eval(h, g["points"]), g["eval"])
+        assert not np.array_equal(port.compile(h), g["words"])
+    finally:
+        port.free(h)
