@@ -310,29 +310,31 @@ def our_arm(args, rank, world, local_rank):
     launches_per_step = 11
 
     # End to end through the C ABI: tree handle in, host mesh out, every step.
-    e2e_steps = max(3, min(args.steps, 10))
-    lo = np.array([-2, -2, -2], np.float32)
-    hi = np.array([2, 2, 2], np.float32)
-    sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)     # warm
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        m = sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)
-    torch.cuda.synchronize()
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
-    d2h = m.vertices.nbytes + m.normals.nbytes + (m.colors.nbytes if m.colors is not None else 0) + \
-        m.faces.nbytes + m.cubes.nbytes
-    e2e = {"value": world * samples * e2e_steps / e2e_s, "unit": "samples/s",
-           "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
-           "meshes_per_s": world * e2e_steps / e2e_s,
-           "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}
+    e2e_steps = 0 if args.skip_e2e else max(3, min(args.steps, 10))
+    e2e = None
+    if e2e_steps:
+        lo = np.array([-2, -2, -2], np.float32)
+        hi = np.array([2, 2, 2], np.float32)
+        sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)     # warm
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            m = sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
+        d2h = m.vertices.nbytes + m.normals.nbytes + (m.colors.nbytes if m.colors is not None else 0) + \
+            m.faces.nbytes + m.cubes.nbytes
+        e2e = {"value": world * samples * e2e_steps / e2e_s, "unit": "samples/s",
+               "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
+               "meshes_per_s": world * e2e_steps / e2e_s,
+               "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}
 
     # Roofline of the dominant kernel (the distance interpreter): exact algorithmic flops.
     cells, children, words = tree.debug_octree()
@@ -384,13 +386,20 @@ def our_arm(args, rank, world, local_rank):
 
 
 def main():
+    global RES, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--resolution", type=int, default=RES,
+                    help="grid resolution (512 is the benchmark; smaller values are profiling cases)")
     args = ap.parse_args()
+    if args.resolution != RES:
+        WORKLOAD = WORKLOAD.replace(f"{RES}^3", f"{args.resolution}^3").replace(f"({RES + 3}^3", f"({args.resolution + 3}^3")
+        RES = args.resolution
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
