@@ -197,6 +197,30 @@ TANGERINE_API tg_status tg_export_mesh(tg_program* program, const tg_grid* grid,
 TANGERINE_API tg_status tg_export_mesh_device(tg_program* program, const tg_grid* grid, uint32_t flags, tg_device_mesh* out, void* stream);
 TANGERINE_API void tg_mesh_free(tg_mesh* mesh);
 
+/* tg_export_mesh for callers that must not allocate GPU memory once running (an
+ * application that gives all device memory to its own pool at start-up, or a thread that
+ * cannot absorb cudaMalloc's device-wide synchronisation).  No counterpart in the
+ * reference: Tangerine's export runs on the CPU and allocates freely.
+ *
+ * Same kernels and the same results as tg_export_mesh, but nothing is allocated: the
+ * outputs are the caller's device buffers (vertices and normals 3 floats per vertex,
+ * colors 3 bytes per vertex, faces 3 uint32 per face, cubes 1 uint32 per vertex) and the
+ * scratch (lattice, active-cell bitmask, prefix sums) lives in one fixed 64 MiB device
+ * array inside the library -- about a 240^3 lattice at most.  Larger inputs fail with
+ * TG_ERR_UNSUPPORTED; too small an output capacity fails with TG_ERR_INVALID after
+ * counts[0] (vertices) / counts[1] (faces) report the size needed.  `normals` may be NULL
+ * without TG_MESH_ATTRIBUTES, `colors` when the tree has no paint.
+ *  - Every GPU that loads the library holds the 64 MiB array until the process exits.
+ *  - The first call on a device looks up the array's address (cudaGetSymbolAddress with
+ *    that device current); make that first call before any stream capture.
+ *  - All calls share the array, which keeps the last call's contents.  Calls that overlap
+ *    on the GPU (several threads or streams at once) race on it: serialise them.
+ *  - stream NULL is the default stream. */
+TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, const tg_grid* grid, uint32_t flags,
+                                               float* vertices, float* normals, uint8_t* colors, uint32_t* faces,
+                                               uint32_t* cubes, uint64_t vertex_capacity, uint64_t face_capacity,
+                                               uint64_t* counts, void* stream);
+
 /* Whole reference export path from a tree: octree + compile, lattice, surface nets,
  * normals, colours, copy back to the host (MeshExportThread minus the file write). */
 TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], const float model_max[3], float step,

@@ -86,6 +86,8 @@ SIGNATURES = {
     "tg_export_mesh": (_i, [_vp, C.POINTER(Grid), _u32, C.POINTER(HostMesh), _vp]),
     "tg_export_mesh_device": (_i, [_vp, C.POINTER(Grid), _u32, C.POINTER(DeviceMesh), _vp]),
     "tg_mesh_free": (None, [C.POINTER(HostMesh)]),
+    "tg_export_mesh_noalloc": (_i, [_vp, C.POINTER(Grid), _u32, _vp, _vp, _vp, _vp, _vp, C.c_uint64, C.c_uint64,
+                                    C.POINTER(C.c_uint64), _vp]),
     "tg_export_tree": (_i, [_vp, _vp, _vp, _f, C.POINTER(HostMesh), _vp]),
     "tg_write_ply": (_i, [C.POINTER(HostMesh), C.c_char_p, _f]),
     "tg_write_stl": (_i, [_vp, C.POINTER(HostMesh), C.c_char_p, _f, _vp]),

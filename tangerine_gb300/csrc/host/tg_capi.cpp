@@ -16,8 +16,6 @@
 
 using namespace tg;
 
-struct tg_program : public tg::Program {};
-
 namespace
 {
 	Node* AsNode(void* h) { return static_cast<Node*>(h); }

@@ -85,3 +85,6 @@ namespace tg
 	std::string& LastError();
 	void SetError(const std::string& msg);
 }
+
+// The opaque handle of the C ABI (include/tangerine_gb300.h) is a compiled program.
+struct tg_program : public tg::Program {};
