@@ -160,6 +160,10 @@ typedef struct tg_device_mesh
 enum
 {
 	TG_MESH_ATTRIBUTES = 1u,    /* compute gradient normals and colours */
+	TG_MESH_DENSE = 2u,         /* evaluate every lattice point, as the reference does; by
+	                               default bricks that provably hold no surface are skipped
+	                               (same mesh, bit for bit) */
+	/* bits 8..15: brick edge in cells for the culled export (1..15; 0 = 7) */
 };
 
 /* Builds the export octree (target size 0.25, coalescing) and compiles every cell's
@@ -231,9 +235,12 @@ TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], con
 TANGERINE_API tg_status tg_write_ply(const tg_mesh* mesh, const char* path, float scale);
 TANGERINE_API tg_status tg_write_stl(tg_program* program, const tg_mesh* mesh, const char* path, float scale, void* stream);
 
+/* Bricks in the last culled export on this process's engine and how many were evaluated. */
+TANGERINE_API tg_status tg_last_export_stats(int64_t* bricks, int64_t* active_bricks);
+
 /* Per-kernel device time of the export pipeline, accumulated while enabled (CUDA events
  * on the launching stream).  Names: "eval_grid", "cell_flags", "scan", "cell_vertices",
- * "faces", "attributes", "face_normals", "eval_points". */
+ * "faces", "attributes", "face_normals", "eval_points", "classify_bricks", "eval_bricks". */
 TANGERINE_API void tg_profile_enable(int enable);
 TANGERINE_API int tg_profile_read(const char* kernel, double* total_ms, int64_t* launches);
 TANGERINE_API void tg_profile_reset(void);

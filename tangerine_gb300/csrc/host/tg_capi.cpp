@@ -96,6 +96,16 @@ namespace
 		return TG_OK;
 	}
 
+	ExportOptions OptionsOf(uint32_t flags)
+	{
+		ExportOptions o;
+		o.Attributes = (flags & TG_MESH_ATTRIBUTES) != 0;
+		o.Dense = (flags & TG_MESH_DENSE) != 0;
+		const int b = (int)((flags >> 8) & 0xFFu);
+		o.BrickSize = b == 0 ? 7 : b;
+		return o;
+	}
+
 	tg_status CompileInto(void* tree, std::unique_ptr<tg_program>& prog)
 	{
 		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
@@ -313,7 +323,8 @@ extern "C"
 		Engine& eng = Engine::Get();
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		DeviceMesh dm;
-		cudaError_t e = eng.Export(*p, gs, (flags & TG_MESH_ATTRIBUTES) != 0, dm, StreamOf(stream));
+		if (((flags >> 8) & 0xFFu) > 15) { SetError("brick size must be 1..15 cells"); return TG_ERR_INVALID; }
+		cudaError_t e = eng.Export(*p, gs, OptionsOf(flags), dm, StreamOf(stream));
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
 		out->vertex_count = dm.VertexCount;
 		out->face_count = dm.FaceCount;
@@ -334,7 +345,8 @@ extern "C"
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		const cudaStream_t s = StreamOf(stream);
 		DeviceMesh dm;
-		cudaError_t e = eng.Export(*p, gs, (flags & TG_MESH_ATTRIBUTES) != 0, dm, s);
+		if (((flags >> 8) & 0xFFu) > 15) { SetError("brick size must be 1..15 cells"); return TG_ERR_INVALID; }
+		cudaError_t e = eng.Export(*p, gs, OptionsOf(flags), dm, s);
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
 		return CopyMeshToHost(dm, out, s);
 	}
@@ -365,7 +377,7 @@ extern "C"
 		if (st != TG_OK) return st;
 		const cudaStream_t s = StreamOf(stream);
 		DeviceMesh dm;
-		cudaError_t e = eng.Export(*prog, gs, true, dm, s);
+		cudaError_t e = eng.Export(*prog, gs, OptionsOf(TG_MESH_ATTRIBUTES), dm, s);
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
 		return CopyMeshToHost(dm, out, s);
 	}
@@ -485,6 +497,13 @@ extern "C"
 
 	TANGERINE_API void ExportSTL(void* h, float grid_size, int, const char* path) { ExportToFile(h, grid_size, path, false); }
 	TANGERINE_API void ExportPLY(void* h, float grid_size, int, const char* path) { ExportToFile(h, grid_size, path, true); }
+
+	TANGERINE_API tg_status tg_last_export_stats(int64_t* bricks, int64_t* active_bricks)
+	{
+		if (bricks) *bricks = Engine::Get().LastBricks();
+		if (active_bricks) *active_bricks = Engine::Get().LastActiveBricks();
+		return TG_OK;
+	}
 
 	TANGERINE_API void tg_profile_enable(int on) { Engine::Get().SetProfiling(on != 0); }
 	TANGERINE_API int tg_profile_read(const char* name, double* ms, int64_t* launches)

@@ -159,7 +159,7 @@ namespace tg
 		return cudaSuccess;
 	}
 
-	cudaError_t Engine::Export(const Program& p, const GridSpec& g, bool attributes, DeviceMesh& out, cudaStream_t s)
+	cudaError_t Engine::Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s)
 	{
 		out = DeviceMesh();
 		const int64_t lattice = (int64_t)g.NX * g.NY * g.NZ;
@@ -173,18 +173,49 @@ namespace tg
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4));
 
-		Begin("eval_grid", s);
-		TG_TRY(LaunchEvalGrid(p.View, g, LatticeBuf.As<float>(), s));
-		End(s);
-		Begin("cell_flags", s);
-		TG_TRY(LaunchCellFlags(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), s));
-		End(s);
+		if (opt.Dense)
+		{
+			Bricks = ActiveBricks = 0;
+			Begin("eval_grid", s);
+			TG_TRY(LaunchEvalGrid(p.View, g, LatticeBuf.As<float>(), s));
+			End(s);
+			Begin("cell_flags", s);
+			TG_TRY(LaunchCellFlags(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), s));
+			End(s);
+		}
+		else
+		{
+			const int B = opt.BrickSize;
+			const int64_t nb = BrickCount(g, B);
+			TG_TRY(BrickBits.Reserve((size_t)((nb + 31) / 32) * 4));
+			TG_TRY(BrickList.Reserve((size_t)nb * 4));
+			if (!PersistentBlocks)
+			{
+				int dev = 0, sms = 0;
+				TG_TRY(cudaGetDevice(&dev));
+				TG_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+				PersistentBlocks = sms * 8;
+			}
+			uint32_t* brickCount = Counts.As<uint32_t>() + 2;
+			Begin("classify_bricks", s);
+			TG_TRY(LaunchClassifyBricks(p.View, g, B, BrickBits.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
+			End(s);
+			Begin("eval_bricks", s);
+			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s));
+			End(s);
+			Begin("cell_flags", s);
+			TG_TRY(LaunchCellFlagsBricks(LatticeBuf.As<float>(), g, B, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), s));
+			End(s);
+			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 4, cudaMemcpyDeviceToHost, s));
+			Bricks = nb;
+		}
 		Begin("scan", s);
 		TG_TRY(LaunchExclusiveScan(Words.As<uint32_t>(), words, true, WordBase.As<uint32_t>(), Counts.As<uint32_t>(), Scratch.As<uint32_t>(), s));
 		End(s);
 		TG_TRY(cudaMemcpyAsync(HostCounts, Counts.Ptr, 4, cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaStreamSynchronize(s));
 		const uint32_t vcount = HostCounts[0];
+		if (!opt.Dense) ActiveBricks = HostCounts[2];
 
 		TG_TRY(Vertices.Reserve((size_t)vcount * 12));
 		TG_TRY(Cubes.Reserve((size_t)vcount * 4));
@@ -214,7 +245,7 @@ namespace tg
 		out.Vertices = Vertices.As<float>();
 		out.Cubes = Cubes.As<uint32_t>();
 		out.Faces = Faces.As<uint32_t>();
-		if (attributes)
+		if (opt.Attributes)
 		{
 			TG_TRY(Normals.Reserve((size_t)vcount * 12));
 			uint8_t* colors = nullptr;

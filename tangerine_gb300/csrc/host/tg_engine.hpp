@@ -45,6 +45,13 @@ namespace tg
 		uint32_t* Cubes = nullptr;
 	};
 
+	struct ExportOptions
+	{
+		bool Attributes = true;     // gradient normals and colours
+		bool Dense = false;         // evaluate every lattice point (no brick culling)
+		int BrickSize = 7;          // cells per brick edge when culling (1..15)
+	};
+
 	class Engine
 	{
 	public:
@@ -54,7 +61,9 @@ namespace tg
 		cudaError_t Upload(Program& p);
 		cudaError_t EvalGrid(const Program& p, const GridSpec& g, float* device_out, cudaStream_t s);
 		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
-		cudaError_t Export(const Program& p, const GridSpec& g, bool attributes, DeviceMesh& out, cudaStream_t s);
+		cudaError_t Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s);
+		int64_t LastActiveBricks() const { return ActiveBricks; }
+		int64_t LastBricks() const { return Bricks; }
 		cudaError_t FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
 			uint64_t face_count, float* host_normals, cudaStream_t s);
 		DeviceBuffer& Lattice() { return LatticeBuf; }
@@ -78,8 +87,10 @@ namespace tg
 
 		cudaStream_t Stream = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
-		DeviceBuffer Points, PointOut;
+		DeviceBuffer Points, PointOut, BrickBits, BrickList;
 		uint32_t* HostCounts = nullptr;
+		int PersistentBlocks = 0;
+		int64_t ActiveBricks = 0, Bricks = 0;
 	};
 
 	std::string& LastError();

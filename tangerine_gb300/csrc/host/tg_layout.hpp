@@ -44,7 +44,8 @@ namespace tg
 		int32_t DistanceCode;       // quad offset of the distance program
 		int32_t SurfaceCode;        // quad offset of the surface program
 		int32_t StackSize;
-		int32_t Reserved;
+		float ClipRadius;           // radius of the sphere the cell's evaluator was clipped to;
+		                            // negated when the program is not 1-Lipschitz (ellipsoid)
 	};
 	static_assert(sizeof(OctNode) == 64, "OctNode is one 64-byte line");
 

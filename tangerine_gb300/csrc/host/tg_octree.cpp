@@ -17,6 +17,7 @@ namespace tg
 		{
 			AABB Bounds;
 			Vec3 Pivot;
+			float Radius = 0.0f;
 			bool Terminus = false;
 			bool Incomplete = false;
 			int Leaves = 0;
@@ -46,6 +47,7 @@ namespace tg
 			const float half = (float)((double)span * 0.5);
 			c->Pivot = Vec3(half) + bounds.Min;
 			const float radius = (float)((double)Length(Vec3(span)) * 0.5);
+			c->Radius = radius;
 			c->Eval = in->Clip(c->Pivot, radius);
 			c->Leaves = c->Eval ? c->Eval->LeafCount() : 0;
 			c->Terminus = span <= bp.Target || !c->Eval;
@@ -134,6 +136,7 @@ namespace tg
 				Octree::Cell& c = out.back();
 				c.Bounds = t.Bounds;
 				c.Pivot = t.Pivot;
+				c.ClipRadius = t.Radius;
 				c.Terminus = t.Terminus;
 				c.Incomplete = t.Incomplete;
 				c.EvaluatorLeaves = t.Leaves;
@@ -398,6 +401,20 @@ namespace tg
 		}
 	}
 
+	// Ellipsoid distances are a bound estimate, not 1-Lipschitz; every other primitive and
+	// every set operator here is.
+	bool HasNonLipschitzBrush(const Node& n)
+	{
+		switch (n.Kind)
+		{
+		case NodeKind::Brush: return n.Op == OpEllipsoid;
+		case NodeKind::Set: return HasNonLipschitzBrush(*n.Lhs) || HasNonLipschitzBrush(*n.Rhs);
+		case NodeKind::Flate: return HasNonLipschitzBrush(*n.Lhs);
+		case NodeKind::Stencil: return HasNonLipschitzBrush(*n.Lhs);
+		}
+		return true;
+	}
+
 	std::vector<uint32_t> CompileReferenceWords(const Node& tree)
 	{
 		std::vector<uint32_t> w;
@@ -429,7 +446,7 @@ namespace tg
 			n.Pivot[0] = c.Pivot.x; n.Pivot[1] = c.Pivot.y; n.Pivot[2] = c.Pivot.z;
 			n.Terminus = c.Terminus ? 1 : 0;
 			for (int k = 0; k < 8; ++k) n.Child[k] = c.Children[k];
-			n.Reserved = 0;
+			n.ClipRadius = HasNonLipschitzBrush(*c.Evaluator) ? -c.ClipRadius : c.ClipRadius;
 			const int dist = (int)(out.Code.size() / 4);
 			em.Distance(*c.Evaluator);
 			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);

@@ -18,6 +18,7 @@ namespace tg
 		{
 			AABB Bounds;
 			Vec3 Pivot;
+			float ClipRadius = 0.0f;
 			bool Terminus = false;
 			bool Incomplete = false;
 			int EvaluatorLeaves = 0;
@@ -35,6 +36,7 @@ namespace tg
 	// Distance program words exactly as Tangerine's SDFInterpreter holds them
 	// (SDFNode::Compile + Stop), for checking against the reference.
 	std::vector<uint32_t> CompileReferenceWords(const Node& tree);
+	bool HasNonLipschitzBrush(const Node& tree);
 
 	struct CompiledTree
 	{

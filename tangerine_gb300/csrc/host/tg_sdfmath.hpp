@@ -107,7 +107,18 @@ namespace tg
 	}
 
 	// The smooth operators are the polynomial blend: h = max(k - |l -+ r|, 0), then
-	// min/max(l, r) -+ h*h/4k.
+	// min/max(l, r) -+ h*h/4k, evaluated in double as the reference's double literal makes
+	// it.  Where the operands are at least k apart (h = 0, nearly everywhere) the double
+	// term is +0 and the result is m -+ 0 rounded to float, which one float add or
+	// subtract of 0 reproduces exactly (signed zeros included); only k > 0 takes that
+	// shortcut, since 0/0 must stay NaN.
+	TG_HD float BlendTerm(float m, float h, float k, bool subtract)
+	{
+		if (h == 0.0f && k > 0.0f) return subtract ? m - 0.0f : m + 0.0f;
+		const double q = (double)(h * h) * 0.25 / (double)k;
+		return (float)(subtract ? (double)m - q : (double)m + q);
+	}
+
 	TG_HD float SetDistance(uint32_t op, float l, float r, float k)
 	{
 		switch (op)
@@ -115,21 +126,9 @@ namespace tg
 		case OpUnion: return fminf(l, r);
 		case OpInter: return fmaxf(l, r);
 		case OpDiff: return fmaxf(l, -r);
-		case OpBlendUnion:
-		{
-			const float h = fmaxf(k - fabsf(l - r), 0.0f);
-			return (float)((double)fminf(l, r) - (double)(h * h) * 0.25 / (double)k);
-		}
-		case OpBlendInter:
-		{
-			const float h = fmaxf(k - fabsf(l - r), 0.0f);
-			return (float)((double)fmaxf(l, r) + (double)(h * h) * 0.25 / (double)k);
-		}
-		case OpBlendDiff:
-		{
-			const float h = fmaxf(k - fabsf(l + r), 0.0f);
-			return (float)((double)fmaxf(l, -r) + (double)(h * h) * 0.25 / (double)k);
-		}
+		case OpBlendUnion: return BlendTerm(fminf(l, r), fmaxf(k - fabsf(l - r), 0.0f), k, true);
+		case OpBlendInter: return BlendTerm(fmaxf(l, r), fmaxf(k - fabsf(l - r), 0.0f), k, false);
+		case OpBlendDiff: return BlendTerm(fmaxf(l, -r), fmaxf(k - fabsf(l + r), 0.0f), k, false);
 		default: return 0.0f;
 		}
 	}

@@ -24,6 +24,16 @@ namespace tg
 	// eight corners do not all share a sign.  `words` holds ceil(cells / 32) words.
 	cudaError_t LaunchCellFlags(const float* lattice, const GridSpec& grid, uint32_t* words, cudaStream_t stream);
 
+	// Exact brick culling (tg_cull.cu): bricks of B^3 cells that provably hold no sign
+	// change are skipped.  brick_bits: one bit per brick; list/count: surviving bricks.
+	int64_t BrickCount(const GridSpec& g, int B);
+	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, uint32_t* list,
+		uint32_t* count, cudaStream_t stream);
+	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		float* lattice, int grid_blocks, cudaStream_t stream);
+	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
+		cudaStream_t stream);
+
 	// Exclusive prefix sum of popcount(words[i]) (popcount = true) or of counts[i].
 	// `scratch` needs ScanScratchWords(n) words.  `total` (device) receives the sum.
 	size_t ScanScratchWords(int64_t n);

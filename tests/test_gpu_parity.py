@@ -151,6 +151,35 @@ def test_full_size_export_properties(lib, port):
         port.free(h)
 
 
+@pytest.mark.parametrize("brick", [1, 4, 7, 15])
+def test_culled_export_equals_dense_export(lib, brick):
+    """Brick culling skips only bricks that provably hold no surface: same mesh, bit for bit."""
+    for seed, prims, res in ((1, 16, 128), (3, 256, 96)):
+        spec = W.random_tree(seed, prims, ops=W.OPS_UNIFORM4 if prims == 16 else W.OPS_60_20_10_10)
+        grid = W.export_grid(resolution=res)
+        with sdf.compile(sdf.from_spec(spec)) as prog:
+            dense = prog.export_mesh(grid, dense=True)
+            culled = prog.export_mesh(grid, brick=brick)
+            bricks, active = sdf.last_export_stats()
+        assert 0 < active <= bricks
+        for a, b in ((dense.vertices, culled.vertices), (dense.faces, culled.faces), (dense.normals, culled.normals),
+                     (dense.colors, culled.colors), (dense.cubes, culled.cubes)):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_culled_export_full_size(lib):
+    spec = W.random_tree(1, 256)
+    grid = W.export_grid(resolution=512)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        dense = prog.export_mesh(grid, dense=True)
+        culled = prog.export_mesh(grid)
+        bricks, active = sdf.last_export_stats()
+    assert active < bricks // 3
+    for a, b in ((dense.vertices, culled.vertices), (dense.faces, culled.faces), (dense.normals, culled.normals),
+                 (dense.colors, culled.colors)):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_export_tree_matches_program_export(lib):
     spec = W.random_tree(5, 16, ops=W.OPS_UNIFORM4)
     grid = W.export_grid(resolution=64)
