@@ -334,12 +334,21 @@ def our_arm(args, rank, world, local_rank):
     if e2e_steps:
         lo = np.array([-2, -2, -2], np.float32)
         hi = np.array([2, 2, 2], np.float32)
-        sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)     # warm
+        # The C ABI call itself: tg_export_tree fills a tg_mesh in host memory, which the
+        # caller releases with tg_mesh_free.
+        def c_export():
+            hm = _lib.HostMesh()
+            _lib.check(lib.tg_export_tree(tree.handle, _lib.as_ptr(lo), _lib.as_ptr(hi), float(4.0 / RES),
+                                          _lib.C.byref(hm), _lib.C.c_void_p(sp)), "tg_export_tree")
+            counts = (int(hm.vertex_count), int(hm.face_count), bool(hm.colors))
+            lib.tg_mesh_free(_lib.C.byref(hm))
+            return counts
+        c_export()     # warm
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            m = sdf.export_tree(tree, lo, hi, 4.0 / RES, stream=sp)
+            nv, nf, has_colors = c_export()
         torch.cuda.synchronize()
         barrier()
         e2e_s = time.perf_counter() - t0
@@ -348,9 +357,11 @@ def our_arm(args, rank, world, local_rank):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
         prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
-        d2h = m.vertices.nbytes + m.normals.nbytes + (m.colors.nbytes if m.colors is not None else 0) + \
-            m.faces.nbytes + m.cubes.nbytes
+        d2h = nv * (12 + 12 + 4 + (3 if has_colors else 0)) + nf * 12
+        phases = sdf.last_export_timing()
         e2e = {"value": world * samples * e2e_steps / e2e_s, "unit": "samples/s",
+               "last_call_phases_s": {"octree_compile": phases[0], "upload": phases[1], "gpu_export": phases[2],
+                                      "copy_to_host": phases[3]},
                "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
                "meshes_per_s": world * e2e_steps / e2e_s,
                "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}

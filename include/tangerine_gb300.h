@@ -131,7 +131,8 @@ typedef struct tg_program_info
 	int64_t distance_quads;     /* summed over all cells */
 } tg_program_info;
 
-/* A mesh in host memory (library-allocated; release with tg_mesh_free).  Vertex v is the
+/* A mesh in host memory (library-allocated, page-locked when possible; release with
+ * tg_mesh_free, which recycles the blocks for later exports).  Vertex v is the
  * vertex of active cube cubes[v] (x + y*sx + z*sx*sy); faces are vertex index triples. */
 typedef struct tg_mesh
 {
@@ -237,6 +238,10 @@ TANGERINE_API tg_status tg_write_stl(tg_program* program, const tg_mesh* mesh, c
 
 /* Bricks in the last culled export on this process's engine and how many were evaluated. */
 TANGERINE_API tg_status tg_last_export_stats(int64_t* bricks, int64_t* active_bricks);
+
+/* Host wall time of the phases of the last tg_export_tree on this thread: octree build +
+ * compile, upload, GPU export, copy back. */
+TANGERINE_API tg_status tg_last_export_timing(double* compile_s, double* upload_s, double* gpu_s, double* copy_s);
 
 /* Per-kernel device time of the export pipeline, accumulated while enabled (CUDA events
  * on the launching stream).  Names: "eval_grid", "cell_flags", "scan", "cell_vertices",

@@ -2,6 +2,7 @@
 // reference-counted trees, and the GPU-native tg_* entry points.
 #include "../../../include/tangerine_gb300.h"
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -66,11 +67,16 @@ namespace
 		out->vertex_count = dm.VertexCount;
 		out->face_count = dm.FaceCount;
 		const size_t v = dm.VertexCount ? dm.VertexCount : 1, f = dm.FaceCount ? dm.FaceCount : 1;
-		out->vertices = (float*)std::malloc(v * 12);
-		out->normals = (float*)std::malloc(v * 12);
-		out->faces = (uint32_t*)std::malloc(f * 12);
-		out->cubes = (uint32_t*)std::malloc(v * 4);
-		out->colors = dm.Colors ? (uint8_t*)std::malloc(v * 3) : nullptr;
+		auto take = [](size_t bytes) -> void*
+		{
+			void* p = HostPool::Get().Take(bytes);
+			return p ? p : std::malloc(bytes);
+		};
+		out->vertices = (float*)take(v * 12);
+		out->normals = (float*)take(v * 12);
+		out->faces = (uint32_t*)take(f * 12);
+		out->cubes = (uint32_t*)take(v * 4);
+		out->colors = dm.Colors ? (uint8_t*)take(v * 3) : nullptr;
 		if (!out->vertices || !out->normals || !out->faces || !out->cubes || (dm.Colors && !out->colors))
 		{
 			tg_mesh_free(out);
@@ -354,11 +360,11 @@ extern "C"
 	TANGERINE_API void tg_mesh_free(tg_mesh* m)
 	{
 		if (!m) return;
-		std::free(m->vertices);
-		std::free(m->normals);
-		std::free(m->colors);
-		std::free(m->faces);
-		std::free(m->cubes);
+		void* blocks[5] = { m->vertices, m->normals, m->colors, m->faces, m->cubes };
+		for (void* b : blocks)
+		{
+			if (!HostPool::Get().Give(b)) std::free(b);
+		}
 		std::memset(m, 0, sizeof *m);
 	}
 
@@ -372,14 +378,29 @@ extern "C"
 		if (!ToGridSpec(&g, gs)) return TG_ERR_INVALID;
 		Engine& eng = Engine::Get();
 		std::lock_guard<std::mutex> lock(eng.Mutex);
+		ExportTiming& tm = LastTiming();
+		auto clock = []() { return std::chrono::steady_clock::now(); };
+		auto secs = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b)
+		{
+			return std::chrono::duration<double>(b - a).count();
+		};
+		const auto t0 = clock();
 		std::unique_ptr<tg_program> prog;
 		st = CompileInto(tree, prog);
 		if (st != TG_OK) return st;
+		const auto t1 = clock();
 		const cudaStream_t s = StreamOf(stream);
 		DeviceMesh dm;
 		cudaError_t e = eng.Export(*prog, gs, OptionsOf(TG_MESH_ATTRIBUTES), dm, s);
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
-		return CopyMeshToHost(dm, out, s);
+		const auto t2 = clock();
+		st = CopyMeshToHost(dm, out, s);
+		const auto t3 = clock();
+		tm.CompileSeconds = prog->Host.BuildSeconds;
+		tm.UploadSeconds = secs(t0, t1) - prog->Host.BuildSeconds;
+		tm.GpuSeconds = secs(t1, t2);
+		tm.CopySeconds = secs(t2, t3);
+		return st;
 	}
 
 	// WritePLY (export.cpp:198-280): header, then x y z nx ny nz [r g b] per vertex, then
@@ -502,6 +523,16 @@ extern "C"
 	{
 		if (bricks) *bricks = Engine::Get().LastBricks();
 		if (active_bricks) *active_bricks = Engine::Get().LastActiveBricks();
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_last_export_timing(double* compile_s, double* upload_s, double* gpu_s, double* copy_s)
+	{
+		const ExportTiming& t = LastTiming();
+		if (compile_s) *compile_s = t.CompileSeconds;
+		if (upload_s) *upload_s = t.UploadSeconds;
+		if (gpu_s) *gpu_s = t.GpuSeconds;
+		if (copy_s) *copy_s = t.CopySeconds;
 		return TG_OK;
 	}
 

@@ -13,6 +13,56 @@ namespace tg
 
 	void SetError(const std::string& msg) { LastError() = msg; }
 
+	ExportTiming& LastTiming()
+	{
+		static thread_local ExportTiming t;
+		return t;
+	}
+
+	HostPool& HostPool::Get()
+	{
+		static HostPool* pool = new HostPool();
+		return *pool;
+	}
+
+	void* HostPool::Take(size_t bytes)
+	{
+		std::lock_guard<std::mutex> lock(Mutex);
+		size_t best = (size_t)-1;
+		for (size_t i = 0; i < Free.size(); ++i)
+		{
+			if (Free[i].second >= bytes && (best == (size_t)-1 || Free[i].second < Free[best].second)) best = i;
+		}
+		if (best != (size_t)-1)
+		{
+			auto blk = Free[best];
+			Free.erase(Free.begin() + (long)best);
+			Used.push_back(blk);
+			return blk.first;
+		}
+		void* p = nullptr;
+		const size_t want = bytes < 4096 ? 4096 : bytes + bytes / 8;
+		if (cudaMallocHost(&p, want) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+		Used.push_back({ p, want });
+		return p;
+	}
+
+	bool HostPool::Give(void* p)
+	{
+		if (!p) return true;
+		std::lock_guard<std::mutex> lock(Mutex);
+		for (size_t i = 0; i < Used.size(); ++i)
+		{
+			if (Used[i].first == p)
+			{
+				Free.push_back(Used[i]);
+				Used.erase(Used.begin() + (long)i);
+				return true;
+			}
+		}
+		return false;
+	}
+
 	cudaError_t DeviceBuffer::Reserve(size_t bytes)
 	{
 		if (bytes <= Bytes && Ptr) return cudaSuccess;
@@ -204,7 +254,8 @@ namespace tg
 			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s));
 			End(s);
 			Begin("cell_flags", s);
-			TG_TRY(LaunchCellFlagsBricks(LatticeBuf.As<float>(), g, B, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), s));
+			TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
+				PersistentBlocks, s));
 			End(s);
 			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 4, cudaMemcpyDeviceToHost, s));
 			Bricks = nb;
@@ -223,8 +274,17 @@ namespace tg
 		TG_TRY(FaceBase.Reserve((size_t)vcount * 4));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(vcount) * 4));
 		Begin("cell_vertices", s);
-		TG_TRY(LaunchCellVertices(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Vertices.As<float>(),
-			Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), cells, s));
+		if (opt.Dense)
+		{
+			TG_TRY(LaunchCellVertices(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Vertices.As<float>(),
+				Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), cells, s));
+		}
+		else
+		{
+			TG_TRY(LaunchCellVerticesListed(LatticeBuf.As<float>(), g, opt.BrickSize, BrickList.As<uint32_t>(),
+				Counts.As<uint32_t>() + 2, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Vertices.As<float>(),
+				Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), PersistentBlocks, s));
+		}
 		End(s);
 		Begin("scan", s);
 		TG_TRY(LaunchExclusiveScan(FaceCounts.As<uint32_t>(), vcount, false, FaceBase.As<uint32_t>(), Counts.As<uint32_t>() + 1,

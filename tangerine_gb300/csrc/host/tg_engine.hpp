@@ -93,6 +93,26 @@ namespace tg
 		int64_t ActiveBricks = 0, Bricks = 0;
 	};
 
+	// Pinned host blocks handed out as mesh outputs and taken back by tg_mesh_free, so the
+	// device-to-host copies run at full link speed without pinning memory on every call.
+	class HostPool
+	{
+	public:
+		static HostPool& Get();
+		void* Take(size_t bytes);            // nullptr when pinned memory is unavailable
+		bool Give(void* p);                  // false: p is not from this pool
+	private:
+		std::mutex Mutex;
+		std::vector<std::pair<void*, size_t>> Free;
+		std::vector<std::pair<void*, size_t>> Used;
+	};
+
+	struct ExportTiming
+	{
+		double CompileSeconds = 0, UploadSeconds = 0, GpuSeconds = 0, CopySeconds = 0;
+	};
+	ExportTiming& LastTiming();
+
 	std::string& LastError();
 	void SetError(const std::string& msg);
 }

@@ -167,7 +167,7 @@ namespace tg
 			cube.Max = cube.Max + Vec3(0.0f);
 		}
 		if (cube.Volume() == 0.0f) return false;
-		BuildParams bp{ target, coalesce, max_depth, 3 };
+		BuildParams bp{ target, coalesce, max_depth, 2 };
 		std::unique_ptr<TmpCell> top = MakeCell(root, cube, bp, 1);
 		if (!top->Eval) return false;
 		Flatten(*top, Cells);

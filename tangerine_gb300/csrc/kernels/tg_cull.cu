@@ -17,6 +17,7 @@
 // cells of skipped bricks as inactive without reading their corners.
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
+#include "tg_surface.cuh"
 
 namespace tg
 {
@@ -213,6 +214,76 @@ namespace tg
 			if ((threadIdx.x & 31) == 0 && c < cells) words[c >> 5] = ballot;
 		}
 
+		// The cells of listed bricks, a CTA per brick with a grid stride over the list.
+		// Cells of unlisted bricks hold no surface and are never visited: the active-cell
+		// bitmask starts zeroed and only listed cells can set their bit.
+		struct BrickCells
+		{
+			int64_t i0, j0, k0;
+			int nx, ny, nz;
+		};
+
+		__device__ __forceinline__ BrickCells CellsOf(uint32_t b, const BrickGrid& bg, const CellGeom& cg)
+		{
+			const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
+			const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
+			BrickCells bc;
+			bc.i0 = (int64_t)bx * bg.B; bc.j0 = (int64_t)by * bg.B; bc.k0 = (int64_t)bz * bg.B;
+			bc.nx = (int)min((int64_t)bg.B, cg.sx - bc.i0);
+			bc.ny = (int)min((int64_t)bg.B, cg.sy - bc.j0);
+			bc.nz = (int)min((int64_t)bg.B, cg.sz - bc.k0);
+			return bc;
+		}
+
+		__global__ void __launch_bounds__(128) CellFlagsListedKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words)
+		{
+			const CellGeom cg = Geom(g);
+			const uint32_t n = *count;
+			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
+			{
+				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
+				const int total = bc.nx * bc.ny * bc.nz;
+				for (int t = threadIdx.x; t < total; t += blockDim.x)
+				{
+					const int64_t i = bc.i0 + t % bc.nx, j = bc.j0 + (t / bc.nx) % bc.ny, k = bc.k0 + t / (bc.nx * bc.ny);
+					float v[8];
+					LoadCorners(lat, cg, i, j, k, v);
+					unsigned pos = 0;
+#pragma unroll
+					for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+					if (pos != 0u && pos != 0xFFu)
+					{
+						const int64_t c = i + j * cg.sx + k * cg.sx * cg.sy;
+						atomicOr(words + (c >> 5), 1u << (c & 31));
+					}
+				}
+			}
+		}
+
+		__global__ void __launch_bounds__(128) CellVerticesListedKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, const uint32_t* __restrict__ words,
+			const uint32_t* __restrict__ base, float* __restrict__ vertices, uint32_t* __restrict__ cubes,
+			uint32_t* __restrict__ face_counts)
+		{
+			const CellGeom cg = Geom(g);
+			const uint32_t n = *count;
+			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
+			{
+				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
+				const int total = bc.nx * bc.ny * bc.nz;
+				for (int t = threadIdx.x; t < total; t += blockDim.x)
+				{
+					const int64_t i = bc.i0 + t % bc.nx, j = bc.j0 + (t / bc.nx) % bc.ny, k = bc.k0 + t / (bc.nx * bc.ny);
+					const int64_t c = i + j * cg.sx + k * cg.sx * cg.sy;
+					const uint32_t w = __ldg(words + (c >> 5));
+					if (!((w >> (c & 31)) & 1u)) continue;
+					const uint32_t vid = __ldg(base + (c >> 5)) + __popc(w & ((1u << (c & 31)) - 1u));
+					EmitCellVertex(lat, g, cg, words, c, i, j, k, vid, vertices, cubes, face_counts);
+				}
+			}
+		}
+
 		BrickGrid MakeBrickGrid(const GridSpec& g, int B)
 		{
 			return { B, (g.NX - 1 + B - 1) / B, (g.NY - 1 + B - 1) / B, (g.NZ - 1 + B - 1) / B };
@@ -269,6 +340,25 @@ namespace tg
 		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
 		if (cells <= 0) return cudaSuccess;
 		CellFlagsBricksKernel<<<(unsigned)((cells + 255) / 256), 256, 0, stream>>>(lattice, g, bg, brick_bits, words, cells);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		uint32_t* words, int grid_blocks, cudaStream_t stream)
+	{
+		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
+		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((cells + 31) / 32) * 4, stream);
+		if (e != cudaSuccess) return e;
+		CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts,
+		int grid_blocks, cudaStream_t stream)
+	{
+		CellVerticesListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, word_base,
+			vertices, cubes, face_counts);
 		return cudaGetLastError();
 	}
 }

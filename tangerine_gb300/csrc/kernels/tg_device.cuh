@@ -224,6 +224,147 @@ namespace tg
 		return dst[0];
 	}
 
+	// Surface program at K points in one pass over the records (SDFNode::Eval per point);
+	// lane `mat_lane` (or none, when negative) also follows GetMaterial and its result goes
+	// to *material_out.  Operands below the top of the stack spill to shared memory:
+	// distance (depth, lane) at spill[(depth * (K + 1) + lane) * stride] and the material
+	// lane's material index at spill[(depth * (K + 1) + K) * stride].
+	template<int K>
+	__device__ __forceinline__ void RunSurfaceBatch(const float4* __restrict__ code, int pc,
+		const float (&px)[K], const float (&py)[K], const float (&pz)[K], float (&out)[K],
+		int mat_lane, int* material_out, float* spill, int stride)
+	{
+		float acc[K];
+#pragma unroll
+		for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+		int macc = -1;
+		int depth = 0;
+		const bool withMaterial = mat_lane >= 0;
+		auto slot = [&](int d, int lane) -> float& { return spill[(d * (K + 1) + lane) * stride]; };
+		for (int guard = 0; guard < (1 << 24); ++guard)
+		{
+			const float4 h = LoadQuad(code, pc++);
+			const uint32_t head = __float_as_uint(h.x);
+			const uint32_t op = head & 0xFFu;
+			if (op >= OpSphere && op <= OpPlane)
+			{
+				if (depth > 0)
+				{
+#pragma unroll
+					for (int k = 0; k < K; ++k) slot(depth - 1, k) = acc[k];
+					slot(depth - 1, K) = __int_as_float(macc);
+				}
+				++depth;
+				const float4 Q = LoadQuad(code, pc);
+				const float4 T = LoadQuad(code, pc + 1);
+				const float4 M = LoadQuad(code, pc + 2);
+				pc += 3;
+				const Quat qi{ Q.x, Q.y, Q.z, Q.w };
+				const Vec3 t(T.x, T.y, T.z);
+				const float prm[3] = { h.y, h.z, h.w };
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					// BrushFn(ApplyInv(p)) * s with ApplyInv(p) = rotate(inverse(q), p - t) / s
+					const Vec3 local = Rotate(qi, Vec3(px[k], py[k], pz[k]) - t) / T.w;
+					acc[k] = BrushDistance(op, prm, local) * T.w;
+				}
+				macc = __float_as_int(M.x);
+			}
+			else if (op >= OpUnion && op <= OpBlendDiff)
+			{
+				--depth;
+				float lm = 0.0f, rm = 0.0f, dm = 0.0f;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					const float l = slot(depth - 1, k);
+					const float d = SetDistance(op, l, acc[k], h.y);
+					if (k == mat_lane) { lm = l; rm = acc[k]; dm = d; }
+					acc[k] = d;
+				}
+				if (withMaterial)
+				{
+					// SetNode::GetMaterial (sdf_evaluator.cpp:957-1012).
+					const int ml = __float_as_int(slot(depth - 1, K));
+					const int mr = macc;
+					if (op == OpDiff || op == OpBlendDiff) macc = ml;
+					else
+					{
+						const bool blend = (op == OpBlendUnion || op == OpBlendInter);
+						const bool takeLeft = blend ? (fabsf(lm - dm) <= fabsf(rm - dm)) : (dm == lm);
+						if (op == OpUnion || op == OpBlendUnion) macc = takeLeft ? ml : mr;
+						else
+						{
+							const bool lv = (head & RecLhsPaint) != 0, rv = (head & RecRhsPaint) != 0;
+							if (lv && rv) macc = takeLeft ? ml : mr;
+							else macc = lv ? ml : mr;
+						}
+					}
+				}
+			}
+			else if (op == OpFlate)
+			{
+#pragma unroll
+				for (int k = 0; k < K; ++k) acc[k] = acc[k] - h.y;
+			}
+			else if (op == OpMaskBegin)
+			{
+				if (!withMaterial) pc += (int)__float_as_uint(h.y);
+			}
+			else if (op == OpStencilEnd)
+			{
+				// StencilMaskNode::GetMaterial (sdf_evaluator.cpp:666-679): the mask's value is
+				// on top, the child's below it.
+				--depth;
+				float maskValue = 0.0f;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					if (k == mat_lane) maskValue = acc[k];
+					acc[k] = slot(depth - 1, k);
+				}
+				const int childMat = __float_as_int(slot(depth - 1, K));
+				const bool interior = maskValue < 0.0f;
+				const bool negative = (head & RecNegative) != 0;
+				macc = (interior == negative) ? (int)__float_as_uint(h.y) : childMat;
+			}
+			else
+			{
+				break;   // OpStop
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < K; ++k) out[k] = acc[k];
+		if (material_out) *material_out = macc;
+	}
+
+	// Gradient (and, optionally, material) at p with one batched pass: lanes 0..3 are the
+	// tetrahedral points, lane 4 is p itself (SDFNode::Gradient, sdf_evaluator.cpp:298-333).
+	__device__ __forceinline__ Vec3 SurfaceGradientBatch(const float4* __restrict__ code, int pc, Vec3 p, bool material,
+		int* material_out, float* spill, int stride)
+	{
+		const float h = 0.0001f;
+		const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+		const Vec3 q0 = p + xyy, q1 = p + yyx, q2 = p + yxy, q3 = p + xxx;
+		const float px[5] = { q0.x, q1.x, q2.x, q3.x, p.x };
+		const float py[5] = { q0.y, q1.y, q2.y, q3.y, p.y };
+		const float pz[5] = { q0.z, q1.z, q2.z, q3.z, p.z };
+		float e[5];
+		RunSurfaceBatch<5>(code, pc, px, py, pz, e, material ? 4 : -1, material_out, spill, stride);
+		Vec3 g = xyy * e[0];
+		g = g + yyx * e[1];
+		g = g + yxy * e[2];
+		g = g + xxx * e[3];
+		const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+		if (ls == 0.0f)
+		{
+			const float d = e[4];
+			return Normalize(Vec3(e[0] - d, e[2] - d, e[1] - d));
+		}
+		return g / sqrtf(ls);
+	}
+
 	// SDFNode::Gradient (sdf_evaluator.cpp:298-333) on a surface program.
 	__device__ __forceinline__ Vec3 SurfaceGradient(const float4* __restrict__ code, int pc, Vec3 p)
 	{

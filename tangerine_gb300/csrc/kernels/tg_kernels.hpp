@@ -33,6 +33,12 @@ namespace tg
 		float* lattice, int grid_blocks, cudaStream_t stream);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
 		cudaStream_t stream);
+	// Cell passes over the cells of listed bricks only (the bitmask is cleared first).
+	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		uint32_t* words, int grid_blocks, cudaStream_t stream);
+	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts,
+		int grid_blocks, cudaStream_t stream);
 
 	// Exclusive prefix sum of popcount(words[i]) (popcount = true) or of counts[i].
 	// `scratch` needs ScanScratchWords(n) words.  `total` (device) receives the sum.

@@ -8,56 +8,12 @@
 // popcount-rank lookup in that bitmask, so no map is built.
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
+#include "tg_surface.cuh"
 
 namespace tg
 {
 	namespace
 	{
-		struct CellGeom
-		{
-			int64_t sx, sy, sz;     // cells per axis
-			int64_t nx, ny;         // lattice points per axis (x, y)
-		};
-
-		__device__ __forceinline__ CellGeom Geom(const GridSpec& g)
-		{
-			return { g.NX - 1, g.NY - 1, g.NZ - 1, g.NX, g.NY };
-		}
-
-		__device__ __forceinline__ float Corner(const float* __restrict__ lat, const CellGeom& cg, int64_t i, int64_t j, int64_t k)
-		{
-			return __ldg(lat + (k * cg.ny + j) * cg.nx + i);
-		}
-
-		// Corner order and edge list of the reference (surface_nets.cpp:889-901).
-		__constant__ int8_t kCornerOfs[8][3] = { {0,0,0},{1,0,0},{1,1,0},{0,1,0},{0,0,1},{1,0,1},{1,1,1},{0,1,1} };
-		__constant__ int8_t kEdges[12][2] = { {0,1},{1,2},{2,3},{3,0},{4,5},{5,6},{6,7},{7,4},{0,4},{1,5},{2,6},{3,7} };
-
-		__device__ __forceinline__ void LoadCorners(const float* __restrict__ lat, const CellGeom& cg, int64_t i, int64_t j, int64_t k, float (&v)[8])
-		{
-			const int64_t base = (k * cg.ny + j) * cg.nx + i;
-			const int64_t dy = cg.nx, dz = cg.nx * cg.ny;
-			v[0] = __ldg(lat + base);
-			v[1] = __ldg(lat + base + 1);
-			v[2] = __ldg(lat + base + dy + 1);
-			v[3] = __ldg(lat + base + dy);
-			v[4] = __ldg(lat + base + dz);
-			v[5] = __ldg(lat + base + dz + 1);
-			v[6] = __ldg(lat + base + dz + dy + 1);
-			v[7] = __ldg(lat + base + dz + dy);
-		}
-
-		__device__ __forceinline__ bool IsActive(const uint32_t* __restrict__ words, int64_t cell)
-		{
-			return (__ldg(words + (cell >> 5)) >> (cell & 31)) & 1u;
-		}
-
-		__device__ __forceinline__ uint32_t VertexOf(const uint32_t* __restrict__ words, const uint32_t* __restrict__ base, int64_t cell)
-		{
-			const uint32_t w = __ldg(words + (cell >> 5));
-			return __ldg(base + (cell >> 5)) + __popc(w & ((1u << (cell & 31)) - 1u));
-		}
-
 		__global__ void CellFlagsKernel(const float* __restrict__ lat, GridSpec g, uint32_t* __restrict__ words, int64_t cells)
 		{
 			const CellGeom cg = Geom(g);
@@ -80,8 +36,6 @@ namespace tg
 			if ((threadIdx.x & 31) == 0 && c < cells) words[c >> 5] = ballot;
 		}
 
-		// FirstLoopInnerThunk's vertex (surface_nets.cpp:915-965) and the number of
-		// triangles SecondLoopThunk will emit for the cell (surface_nets.cpp:1016-1115).
 		__global__ void CellVerticesKernel(const float* __restrict__ lat, GridSpec g, const uint32_t* __restrict__ words,
 			const uint32_t* __restrict__ base, float* __restrict__ vertices, uint32_t* __restrict__ cubes,
 			uint32_t* __restrict__ face_counts, int64_t cells)
@@ -95,47 +49,7 @@ namespace tg
 			const int64_t i = c % cg.sx;
 			const int64_t j = (c / cg.sx) % cg.sy;
 			const int64_t k = c / (cg.sx * cg.sy);
-			float v[8];
-			LoadCorners(lat, cg, i, j, k, v);
-
-			const float fi = (float)i, fj = (float)j, fk = (float)k;
-			float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-			int count = 0;
-#pragma unroll
-			for (int e = 0; e < 12; ++e)
-			{
-				const int a = kEdges[e][0], b = kEdges[e][1];
-				const float s1 = v[a], s2 = v[b];
-				if ((s1 >= 0.0f) == (s2 >= 0.0f)) continue;
-				const float p1x = fi + (float)kCornerOfs[a][0], p1y = fj + (float)kCornerOfs[a][1], p1z = fk + (float)kCornerOfs[a][2];
-				const float p2x = fi + (float)kCornerOfs[b][0], p2y = fj + (float)kCornerOfs[b][1], p2z = fk + (float)kCornerOfs[b][2];
-				const float t = (0.0f - s1) / (s2 - s1);
-				sx = sx + (p1x + t * (p2x - p1x));
-				sy = sy + (p1y + t * (p2y - p1y));
-				sz = sz + (p1z + t * (p2z - p1z));
-				++count;
-			}
-			const float n = (float)count;
-			const float cx = sx / n, cy = sy / n, cz = sz / n;
-			const float fsx = (float)cg.sx, fsy = (float)cg.sy, fsz = (float)cg.sz;
-			const float maxx = g.X0 + fsx * g.Step, maxy = g.Y0 + fsy * g.Step, maxz = g.Z0 + fsz * g.Step;
-			vertices[(int64_t)vid * 3 + 0] = g.X0 + (maxx - g.X0) * (cx - 0.0f) / (fsx - 0.0f);
-			vertices[(int64_t)vid * 3 + 1] = g.Y0 + (maxy - g.Y0) * (cy - 0.0f) / (fsy - 0.0f);
-			vertices[(int64_t)vid * 3 + 2] = g.Z0 + (maxz - g.Z0) * (cz - 0.0f) / (fsz - 0.0f);
-			cubes[vid] = (uint32_t)c;
-
-			uint32_t faces = 0;
-			if (i > 0 && j > 0 && k > 0)
-			{
-				const int64_t dy = cg.sx, dz = cg.sx * cg.sy;
-				// neighbours 0..5: (i-1,j,k) (i-1,j-1,k) (i,j-1,k) (i,j-1,k-1) (i,j,k-1) (i-1,j,k-1)
-				const bool n0 = IsActive(words, c - 1), n1 = IsActive(words, c - 1 - dy), n2 = IsActive(words, c - dy);
-				const bool n3 = IsActive(words, c - dy - dz), n4 = IsActive(words, c - dz), n5 = IsActive(words, c - 1 - dz);
-				if (n0 && n1 && n2) faces += 2;
-				if (n0 && n5 && n4) faces += 2;
-				if (n2 && n3 && n4) faces += 2;
-			}
-			face_counts[vid] = faces;
+			EmitCellVertex(lat, g, cg, words, c, i, j, k, vid, vertices, cubes, face_counts);
 		}
 
 		__global__ void FacesKernel(const float* __restrict__ lat, GridSpec g, const uint32_t* __restrict__ words,
@@ -172,22 +86,24 @@ namespace tg
 			}
 		}
 
-		__global__ void VertexAttributesKernel(DeviceProgram prog, const float* __restrict__ vertices, uint32_t n,
-			float* __restrict__ normals, uint8_t* __restrict__ colors)
+		constexpr int kAttribThreads = 128;
+
+		__global__ void __launch_bounds__(kAttribThreads) VertexAttributesKernel(DeviceProgram prog, const float* __restrict__ vertices,
+			uint32_t n, float* __restrict__ normals, uint8_t* __restrict__ colors)
 		{
+			extern __shared__ float spill[];
 			const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
 			if (v >= n) return;
 			const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
 			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
 			const int pc = __ldg(&prog.Nodes[cell].SurfaceCode);
-			const Vec3 g = SurfaceGradient(prog.Code, pc, p);
+			int m = -1;
+			const Vec3 g = SurfaceGradientBatch(prog.Code, pc, p, colors != nullptr, &m, spill + threadIdx.x, kAttribThreads);
 			normals[(int64_t)v * 3 + 0] = g.x;
 			normals[(int64_t)v * 3 + 1] = g.y;
 			normals[(int64_t)v * 3 + 2] = g.z;
 			if (colors)
 			{
-				int m = -1;
-				RunSurface(prog.Code, pc, p, true, &m);
 				const uchar4 c = m >= 0 ? prog.Colors[m] : make_uchar4(255, 255, 255, 255);
 				colors[(int64_t)v * 3 + 0] = c.x;
 				colors[(int64_t)v * 3 + 1] = c.y;
@@ -208,9 +124,10 @@ namespace tg
 		}
 
 		// WriteSTL(Octree, ...) (export.cpp:140-148): the gradient at (a + b + c) / 3.
-		__global__ void FaceNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices, const uint32_t* __restrict__ faces,
-			uint64_t n, float* __restrict__ normals)
+		__global__ void __launch_bounds__(128) FaceNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
+			const uint32_t* __restrict__ faces, uint64_t n, float* __restrict__ normals)
 		{
+			extern __shared__ float spill[];
 			const uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
 			if (f >= n) return;
 			const uint32_t a = faces[f * 3], b = faces[f * 3 + 1], c = faces[f * 3 + 2];
@@ -220,7 +137,8 @@ namespace tg
 			const Vec3 s = (va + vb) + vc;
 			const Vec3 center(s.x / 3.0f, s.y / 3.0f, s.z / 3.0f);
 			const int cell = DescendOctree(prog.Nodes, center.x, center.y, center.z);
-			const Vec3 g = SurfaceGradient(prog.Code, __ldg(&prog.Nodes[cell].SurfaceCode), center);
+			const Vec3 g = SurfaceGradientBatch(prog.Code, __ldg(&prog.Nodes[cell].SurfaceCode), center, false, nullptr,
+				spill + threadIdx.x, 128);
 			normals[f * 3] = g.x;
 			normals[f * 3 + 1] = g.y;
 			normals[f * 3 + 2] = g.z;
@@ -375,11 +293,20 @@ namespace tg
 		return cudaGetLastError();
 	}
 
+	// Shared memory of the batched surface evaluation: 5 distances + 1 material per level.
+	static size_t SurfaceSpillBytes(const DeviceProgram& prog, int threads)
+	{
+		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+		return (size_t)depth * 6 * threads * sizeof(float);
+	}
+
 	cudaError_t LaunchFaceNormals(const DeviceProgram& prog, const float* vertices, const uint32_t* faces, uint64_t face_count,
 		float* normals, cudaStream_t stream)
 	{
 		if (face_count == 0) return cudaSuccess;
-		FaceNormalsKernel<<<Blocks((int64_t)face_count, 128), 128, 0, stream>>>(prog, vertices, faces, face_count, normals);
+		const size_t smem = SurfaceSpillBytes(prog, 128);
+		if (smem > 48 * 1024) cudaFuncSetAttribute(FaceNormalsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		FaceNormalsKernel<<<Blocks((int64_t)face_count, 128), 128, smem, stream>>>(prog, vertices, faces, face_count, normals);
 		return cudaGetLastError();
 	}
 
@@ -387,7 +314,10 @@ namespace tg
 		float* normals, uint8_t* colors, cudaStream_t stream)
 	{
 		if (vertex_count == 0) return cudaSuccess;
-		VertexAttributesKernel<<<Blocks(vertex_count, 128), 128, 0, stream>>>(prog, vertices, vertex_count, normals, colors);
+		const size_t smem = SurfaceSpillBytes(prog, kAttribThreads);
+		if (smem > 48 * 1024) cudaFuncSetAttribute(VertexAttributesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		VertexAttributesKernel<<<Blocks(vertex_count, kAttribThreads), kAttribThreads, smem, stream>>>(prog, vertices, vertex_count,
+			normals, colors);
 		return cudaGetLastError();
 	}
 }

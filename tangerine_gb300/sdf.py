@@ -143,6 +143,13 @@ def last_export_stats():
     return b.value, a.value
 
 
+def last_export_timing():
+    """Host seconds of the last tg_export_tree: (compile, upload, gpu, copy)."""
+    v = [C.c_double() for _ in range(4)]
+    load().tg_last_export_timing(*[C.byref(x) for x in v])
+    return tuple(x.value for x in v)
+
+
 def _take_mesh(hm: _lib.HostMesh) -> Mesh:
     v, f = int(hm.vertex_count), int(hm.face_count)
 
