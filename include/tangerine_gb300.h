@@ -164,7 +164,9 @@ enum
 	TG_MESH_DENSE = 2u,         /* evaluate every lattice point, as the reference does; by
 	                               default bricks that provably hold no surface are skipped
 	                               (same mesh, bit for bit) */
-	/* bits 8..15: brick edge in cells for the culled export (1..15; 0 = 7) */
+	/* bits 8..15: brick edge in cells for the culled export (1..15; 0 = 7)
+	   bits 16..19: lattice points per thread sharing one pass over the records (1, 2, 4;
+	   0 = 2 culled, 4 dense) */
 };
 
 /* Builds the export octree (target size 0.25, coalescing) and compiles every cell's

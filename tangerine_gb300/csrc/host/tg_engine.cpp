@@ -83,7 +83,7 @@ namespace tg
 
 	Program::~Program()
 	{
-		if (Device) cudaFree(Device);
+		if (Device && OwnsDevice) cudaFree(Device);
 	}
 
 	Engine& Engine::Get()
@@ -101,6 +101,68 @@ namespace tg
 	namespace
 	{
 		inline size_t AlignUp(size_t v, size_t a) { return (v + a - 1) / a * a; }
+	}
+
+	namespace
+	{
+		struct ProgramLayout
+		{
+			size_t NodeBytes, CodeOff, CodeBytes, ColorOff, Total;
+		};
+
+		ProgramLayout LayoutOf(const Program& p)
+		{
+			ProgramLayout l;
+			l.NodeBytes = p.Host.Nodes.size() * sizeof(OctNode);
+			l.CodeOff = (l.NodeBytes + 255) / 256 * 256;
+			l.CodeBytes = p.Host.Code.size() * sizeof(float);
+			l.ColorOff = (l.CodeOff + l.CodeBytes + 255) / 256 * 256;
+			l.Total = l.ColorOff + (p.Host.Colors.size() ? p.Host.Colors.size() : 4);
+			return l;
+		}
+
+		void Pack(const Program& p, const ProgramLayout& l, uint8_t* dst)
+		{
+			std::memcpy(dst, p.Host.Nodes.data(), l.NodeBytes);
+			std::memcpy(dst + l.CodeOff, p.Host.Code.data(), l.CodeBytes);
+			if (!p.Host.Colors.empty()) std::memcpy(dst + l.ColorOff, p.Host.Colors.data(), p.Host.Colors.size());
+		}
+
+		void Bind(Program& p, const ProgramLayout& l, void* device)
+		{
+			uint8_t* base = static_cast<uint8_t*>(device);
+			p.View.Nodes = reinterpret_cast<const OctNode*>(base);
+			p.View.Code = reinterpret_cast<const float4*>(base + l.CodeOff);
+			p.View.Colors = reinterpret_cast<const uchar4*>(base + l.ColorOff);
+			p.View.MaxStack = p.Host.Header.MaxStack;
+		}
+	}
+
+	cudaError_t Engine::UploadScratch(Program& p, cudaStream_t s)
+	{
+		const ProgramLayout l = LayoutOf(p);
+		cudaError_t e = cudaGetDevice(&p.DeviceId);
+		if (e != cudaSuccess) return e;
+		e = ProgramScratch.Reserve(l.Total);
+		if (e != cudaSuccess) return e;
+		if (StagingBytes < l.Total)
+		{
+			if (Staging) cudaFreeHost(Staging);
+			Staging = nullptr;
+			StagingBytes = 0;
+			e = cudaMallocHost(&Staging, l.Total + l.Total / 4);
+			if (e != cudaSuccess) { Staging = nullptr; return e; }
+			StagingBytes = l.Total + l.Total / 4;
+		}
+		// The previous call's copy out of the staging buffer has finished: every export
+		// synchronises its stream before returning.
+		Pack(p, l, static_cast<uint8_t*>(Staging));
+		e = cudaMemcpyAsync(ProgramScratch.Ptr, Staging, l.Total, cudaMemcpyHostToDevice, s);
+		if (e != cudaSuccess) return e;
+		p.Device = ProgramScratch.Ptr;
+		p.OwnsDevice = false;
+		Bind(p, l, p.Device);
+		return cudaSuccess;
 	}
 
 	// One allocation: nodes (64-byte records), code quads, colour bytes.
@@ -227,7 +289,7 @@ namespace tg
 		{
 			Bricks = ActiveBricks = 0;
 			Begin("eval_grid", s);
-			TG_TRY(LaunchEvalGrid(p.View, g, LatticeBuf.As<float>(), s));
+			TG_TRY(LaunchEvalGrid(p.View, g, LatticeBuf.As<float>(), s, opt.Lanes));
 			End(s);
 			Begin("cell_flags", s);
 			TG_TRY(LaunchCellFlags(LatticeBuf.As<float>(), g, Words.As<uint32_t>(), s));
@@ -251,13 +313,16 @@ namespace tg
 			TG_TRY(LaunchClassifyBricks(p.View, g, B, BrickBits.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
 			End(s);
 			Begin("eval_bricks", s);
-			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s));
+			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s,
+				opt.Lanes));
 			End(s);
+			// Active cells lie in listed bricks: bound the list by the bricks' cells.
+			TG_TRY(ActiveCells.Reserve((size_t)(nb * (int64_t)B * B * B < cells ? nb * (int64_t)B * B * B : cells) * 4));
 			Begin("cell_flags", s);
 			TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
-				PersistentBlocks, s));
+				ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, PersistentBlocks, s));
 			End(s);
-			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 4, cudaMemcpyDeviceToHost, s));
+			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 8, cudaMemcpyDeviceToHost, s));
 			Bricks = nb;
 		}
 		Begin("scan", s);
@@ -281,9 +346,8 @@ namespace tg
 		}
 		else
 		{
-			TG_TRY(LaunchCellVerticesListed(LatticeBuf.As<float>(), g, opt.BrickSize, BrickList.As<uint32_t>(),
-				Counts.As<uint32_t>() + 2, Words.As<uint32_t>(), WordBase.As<uint32_t>(), Vertices.As<float>(),
-				Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), PersistentBlocks, s));
+			TG_TRY(LaunchCellVerticesListed(LatticeBuf.As<float>(), g, ActiveCells.As<uint32_t>(), HostCounts[3], Words.As<uint32_t>(),
+				WordBase.As<uint32_t>(), Vertices.As<float>(), Cubes.As<uint32_t>(), FaceCounts.As<uint32_t>(), s));
 		}
 		End(s);
 		Begin("scan", s);

@@ -31,6 +31,7 @@ namespace tg
 		void* Device = nullptr;
 		DeviceProgram View{};
 		int DeviceId = 0;
+		bool OwnsDevice = true;      // false: the bytes live in the engine's scratch program buffer
 		~Program();
 	};
 
@@ -50,6 +51,7 @@ namespace tg
 		bool Attributes = true;     // gradient normals and colours
 		bool Dense = false;         // evaluate every lattice point (no brick culling)
 		int BrickSize = 7;          // cells per brick edge when culling (1..15)
+		int Lanes = 2;              // lattice points per thread sharing one pass over records
 	};
 
 	class Engine
@@ -59,6 +61,9 @@ namespace tg
 
 		cudaStream_t DefaultStream();
 		cudaError_t Upload(Program& p);
+		// Upload into the engine's reusable program buffer, asynchronously on `s` (for a
+		// program used by one call only, such as tg_export_tree's).
+		cudaError_t UploadScratch(Program& p, cudaStream_t s);
 		cudaError_t EvalGrid(const Program& p, const GridSpec& g, float* device_out, cudaStream_t s);
 		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
 		cudaError_t Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s);
@@ -87,7 +92,9 @@ namespace tg
 
 		cudaStream_t Stream = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
-		DeviceBuffer Points, PointOut, BrickBits, BrickList;
+		DeviceBuffer Points, PointOut, BrickBits, BrickList, ProgramScratch, ActiveCells;
+		void* Staging = nullptr;
+		size_t StagingBytes = 0;
 		uint32_t* HostCounts = nullptr;
 		int PersistentBlocks = 0;
 		int64_t ActiveBricks = 0, Bricks = 0;

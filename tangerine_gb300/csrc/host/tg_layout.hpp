@@ -35,11 +35,13 @@ namespace tg
 	};
 
 	constexpr int kMaxStack = 32;   // deepest postfix stack a program may need
+	constexpr int32_t kNodeTerminus = 1;
 
 	struct OctNode
 	{
 		float Pivot[3];
-		int32_t Terminus;
+		int32_t Flags;              // bit 0: terminus; bits 8..15: octants whose clip returned
+		                            // null (the evaluator exceeds the octant sphere's radius)
 		int32_t Child[8];           // -1: no child there
 		int32_t DistanceCode;       // quad offset of the distance program
 		int32_t SurfaceCode;        // quad offset of the surface program

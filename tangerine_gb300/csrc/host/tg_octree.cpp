@@ -2,10 +2,12 @@
 // the GPU record format (tg_layout.hpp).
 #include "tg_octree.hpp"
 
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <thread>
 #include <memory>
 #include <unordered_map>
 
@@ -20,6 +22,8 @@ namespace tg
 			float Radius = 0.0f;
 			bool Terminus = false;
 			bool Incomplete = false;
+			bool ClippedAway = false;   // the clip to this cell's sphere returned null
+			uint32_t NullOctants = 0;   // children whose clip returned null
 			int Leaves = 0;
 			NodeRef Eval;
 			std::unique_ptr<TmpCell> Kids[8];
@@ -49,6 +53,7 @@ namespace tg
 			const float radius = (float)((double)Length(Vec3(span)) * 0.5);
 			c->Radius = radius;
 			c->Eval = in->Clip(c->Pivot, radius);
+			c->ClippedAway = !c->Eval;
 			c->Leaves = c->Eval ? c->Eval->LeafCount() : 0;
 			c->Terminus = span <= bp.Target || !c->Eval;
 			if (!c->Terminus)
@@ -98,6 +103,7 @@ namespace tg
 			{
 				if (!c.Kids[i]->Eval)
 				{
+					if (c.Kids[i]->ClippedAway) c.NullOctants |= 1u << i;
 					c.Kids[i].reset();
 					continue;
 				}
@@ -137,6 +143,7 @@ namespace tg
 				c.Bounds = t.Bounds;
 				c.Pivot = t.Pivot;
 				c.ClipRadius = t.Radius;
+				c.NullOctants = t.NullOctants;
 				c.Terminus = t.Terminus;
 				c.Incomplete = t.Incomplete;
 				c.EvaluatorLeaves = t.Leaves;
@@ -242,11 +249,39 @@ namespace tg
 			}
 		}
 
+		// Emits record programs.  Clipped trees share their brush nodes with the full tree,
+		// so one brush appears in many cells' programs: its records (an inverse matrix is
+		// ~200 flops to build) and every subtree's paint flag are computed once per compile.
 		struct Emitter
 		{
 			std::vector<float>& Code;
-			std::unordered_map<const Material*, int>& Materials;
-			std::vector<const Material*>& MaterialList;
+			const std::unordered_map<const Material*, int>& Materials;
+			uint32_t Epoch;
+			std::vector<std::vector<float>> DistanceRecords;
+			std::vector<std::vector<float>> SurfaceRecords;
+			bool NonLipschitz = false;
+
+			static uint32_t NextEpoch()
+			{
+				static std::atomic<uint32_t> counter{ 0 };
+				uint32_t e = counter.fetch_add(1) + 1;
+				return e == 0 ? counter.fetch_add(1) + 1 : e;
+			}
+
+			// Slot of this node in the per-compile caches (created on first use).
+			void Touch(const Node& n)
+			{
+				if (n.CacheEpoch == Epoch) return;
+				n.CacheEpoch = Epoch;
+				n.CacheRecord = -1;
+				switch (n.Kind)
+				{
+				case NodeKind::Brush: n.CachePaint = n.Mat != nullptr; break;
+				case NodeKind::Set: n.CachePaint = HasPaint(*n.Lhs) || HasPaint(*n.Rhs); break;
+				case NodeKind::Flate: n.CachePaint = HasPaint(*n.Lhs); break;
+				case NodeKind::Stencil: n.CachePaint = true; break;
+				}
+			}
 
 			void Quad(uint32_t head, float a, float b, float c)
 			{
@@ -255,20 +290,63 @@ namespace tg
 				Code.push_back(b);
 				Code.push_back(c);
 			}
-			void Quad4(float a, float b, float c, float d)
+			static void Quad(std::vector<float>& v, uint32_t head, float a, float b, float c)
 			{
-				Code.push_back(a); Code.push_back(b); Code.push_back(c); Code.push_back(d);
+				v.push_back(BitsFloat(head)); v.push_back(a); v.push_back(b); v.push_back(c);
 			}
-			int MaterialIndex(const Material* m)
+			static void Quad4(std::vector<float>& v, float a, float b, float c, float d)
+			{
+				v.push_back(a); v.push_back(b); v.push_back(c); v.push_back(d);
+			}
+			int MaterialIndex(const Material* m) const
 			{
 				if (!m) return -1;
 				auto it = Materials.find(m);
-				if (it != Materials.end()) return it->second;
-				const int idx = (int)MaterialList.size();
-				Materials.emplace(m, idx);
-				MaterialList.push_back(m);
-				return idx;
+				return it == Materials.end() ? -1 : it->second;
 			}
+			bool HasPaint(const Node& n)
+			{
+				Touch(n);
+				return n.CachePaint;
+			}
+
+			// Records of one brush: [distance quads, surface quads], built once per compile.
+			int Records(const Node& n)
+			{
+				Touch(n);
+				if (n.CacheRecord >= 0) return n.CacheRecord;
+				std::vector<float> dist, surf;
+				const Transform& t = n.Xf;
+				const bool rot = !t.Rotation.IsIdentity();
+				const bool scl = t.Scalation != 1.0f;
+				const bool trn = !(t.Translation.x == 0.0f && t.Translation.y == 0.0f && t.Translation.z == 0.0f);
+				uint32_t flags = 0;
+				if (rot || scl) flags |= RecMatrix;
+				else if (trn) flags |= RecOffset;
+				if (scl) flags |= RecScale;
+				Quad(dist, n.Op | flags, n.Params[0], n.Params[1], n.Params[2]);
+				if (flags & RecMatrix)
+				{
+					const Mat4 inv = MatInverse(t.ToMatrix());
+					// Row r of the 3x4 affine part: (m[0][r], m[1][r], m[2][r], m[3][r]).
+					for (int r = 0; r < 3; ++r) Quad4(dist, inv.at(0, r), inv.at(1, r), inv.at(2, r), inv.at(3, r));
+				}
+				else if (flags & RecOffset)
+				{
+					Quad4(dist, -t.Translation.x, -t.Translation.y, -t.Translation.z, 0.0f);
+				}
+				if (flags & RecScale) Quad4(dist, t.Scalation, 0.0f, 0.0f, 0.0f);
+				const Quat qi = Inverse(t.Rotation);
+				Quad(surf, n.Op, n.Params[0], n.Params[1], n.Params[2]);
+				Quad4(surf, qi.w, qi.x, qi.y, qi.z);
+				Quad4(surf, t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
+				Quad(surf, (uint32_t)MaterialIndex(n.Mat.get()), 0.0f, 0.0f, 0.0f);
+				n.CacheRecord = (int32_t)DistanceRecords.size();
+				DistanceRecords.push_back(std::move(dist));
+				SurfaceRecords.push_back(std::move(surf));
+				return n.CacheRecord;
+			}
+			void Append(const std::vector<float>& rec) { Code.insert(Code.end(), rec.begin(), rec.end()); }
 
 			// Distance program: Tangerine's postfix program with each brush's transform,
 			// primitive and field scale fused into one record.
@@ -277,29 +355,9 @@ namespace tg
 				switch (n.Kind)
 				{
 				case NodeKind::Brush:
-				{
-					const Transform& t = n.Xf;
-					const bool rot = !t.Rotation.IsIdentity();
-					const bool scl = t.Scalation != 1.0f;
-					const bool trn = !(t.Translation.x == 0.0f && t.Translation.y == 0.0f && t.Translation.z == 0.0f);
-					uint32_t flags = 0;
-					if (rot || scl) flags |= RecMatrix;
-					else if (trn) flags |= RecOffset;
-					if (scl) flags |= RecScale;
-					Quad(n.Op | flags, n.Params[0], n.Params[1], n.Params[2]);
-					if (flags & RecMatrix)
-					{
-						const Mat4 inv = MatInverse(t.ToMatrix());
-						// Row r of the 3x4 affine part: (m[0][r], m[1][r], m[2][r], m[3][r]).
-						for (int r = 0; r < 3; ++r) Quad4(inv.at(0, r), inv.at(1, r), inv.at(2, r), inv.at(3, r));
-					}
-					else if (flags & RecOffset)
-					{
-						Quad4(-t.Translation.x, -t.Translation.y, -t.Translation.z, 0.0f);
-					}
-					if (flags & RecScale) Quad4(t.Scalation, 0.0f, 0.0f, 0.0f);
+					if (n.Op == OpEllipsoid) NonLipschitz = true;
+					Append(DistanceRecords[Records(n)]);
 					break;
-				}
 				case NodeKind::Set:
 					Distance(*n.Lhs);
 					Distance(*n.Rhs);
@@ -321,22 +379,15 @@ namespace tg
 				switch (n.Kind)
 				{
 				case NodeKind::Brush:
-				{
-					const Transform& t = n.Xf;
-					const Quat qi = Inverse(t.Rotation);
-					Quad(n.Op, n.Params[0], n.Params[1], n.Params[2]);
-					Quad4(qi.w, qi.x, qi.y, qi.z);
-					Quad4(t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
-					Quad((uint32_t)MaterialIndex(n.Mat.get()), 0.0f, 0.0f, 0.0f);
+					Append(SurfaceRecords[Records(n)]);
 					break;
-				}
 				case NodeKind::Set:
 				{
 					Surface(*n.Lhs);
 					Surface(*n.Rhs);
 					uint32_t flags = 0;
-					if (n.Lhs->HasPaint()) flags |= RecLhsPaint;
-					if (n.Rhs->HasPaint()) flags |= RecRhsPaint;
+					if (HasPaint(*n.Lhs)) flags |= RecLhsPaint;
+					if (HasPaint(*n.Rhs)) flags |= RecRhsPaint;
 					Quad(n.Op | flags, n.Threshold, 0.0f, 0.0f);
 					break;
 				}
@@ -359,6 +410,27 @@ namespace tg
 				}
 			}
 		};
+
+		// Material indices in depth-first order of the full tree: every clipped tree shares
+		// its brushes (and their materials) with it.
+		void CollectMaterials(const Node& n, std::unordered_map<const Material*, int>& index, std::vector<const Material*>& list)
+		{
+			auto add = [&](const Material* m)
+			{
+				if (m && index.emplace(m, (int)list.size()).second) list.push_back(m);
+			};
+			switch (n.Kind)
+			{
+			case NodeKind::Brush: add(n.Mat.get()); break;
+			case NodeKind::Set: CollectMaterials(*n.Lhs, index, list); CollectMaterials(*n.Rhs, index, list); break;
+			case NodeKind::Flate: CollectMaterials(*n.Lhs, index, list); break;
+			case NodeKind::Stencil:
+				CollectMaterials(*n.Lhs, index, list);
+				CollectMaterials(*n.Mask, index, list);
+				add(n.Mat.get());
+				break;
+			}
+		}
 
 		// Deepest stack a record program reaches (accumulator + spilled operands).
 		int ProgramDepth(const float* code, int start)
@@ -436,7 +508,9 @@ namespace tg
 		out.Bounds = root->Bounds();
 		std::unordered_map<const Material*, int> materials;
 		std::vector<const Material*> materialList;
-		Emitter em{ out.Code, materials, materialList };
+		CollectMaterials(*root, materials, materialList);
+		out.Code.reserve(1 << 20);
+		Emitter em{ out.Code, materials, Emitter::NextEpoch(), {}, {}, false };
 		int maxStack = 0;
 		out.Nodes.resize(octree.Cells.size());
 		for (size_t i = 0; i < octree.Cells.size(); ++i)
@@ -444,11 +518,12 @@ namespace tg
 			const Octree::Cell& c = octree.Cells[i];
 			OctNode& n = out.Nodes[i];
 			n.Pivot[0] = c.Pivot.x; n.Pivot[1] = c.Pivot.y; n.Pivot[2] = c.Pivot.z;
-			n.Terminus = c.Terminus ? 1 : 0;
+			n.Flags = (c.Terminus ? kNodeTerminus : 0) | (int32_t)(c.NullOctants << 8);
 			for (int k = 0; k < 8; ++k) n.Child[k] = c.Children[k];
-			n.ClipRadius = HasNonLipschitzBrush(*c.Evaluator) ? -c.ClipRadius : c.ClipRadius;
 			const int dist = (int)(out.Code.size() / 4);
+			em.NonLipschitz = false;
 			em.Distance(*c.Evaluator);
+			n.ClipRadius = em.NonLipschitz ? -c.ClipRadius : c.ClipRadius;
 			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
 			const int surf = (int)(out.Code.size() / 4);
 			em.Surface(*c.Evaluator);
@@ -483,6 +558,9 @@ namespace tg
 		out.Header.HasPaint = octree.Cells[0].Evaluator->HasPaint() ? 1 : 0;
 		out.Header.MaxStack = maxStack;
 		out.BuildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+		// Releasing thousands of clipped subtrees takes about a millisecond; the caller does
+		// not need to wait for it (node reference counts are atomic).
+		std::thread([cells = std::move(octree.Cells)]() mutable { cells.clear(); }).detach();
 		return true;
 	}
 }

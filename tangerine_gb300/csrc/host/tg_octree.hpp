@@ -19,6 +19,7 @@ namespace tg
 			AABB Bounds;
 			Vec3 Pivot;
 			float ClipRadius = 0.0f;
+			uint32_t NullOctants = 0;   // children whose clip returned null
 			bool Terminus = false;
 			bool Incomplete = false;
 			int EvaluatorLeaves = 0;

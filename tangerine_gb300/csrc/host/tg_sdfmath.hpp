@@ -112,11 +112,24 @@ namespace tg
 	// term is +0 and the result is m -+ 0 rounded to float, which one float add or
 	// subtract of 0 reproduces exactly (signed zeros included); only k > 0 takes that
 	// shortcut, since 0/0 must stay NaN.
+	// The double-precision path is kept out of line so the compiler cannot evaluate it
+	// speculatively alongside the common shortcut (GB300 issues FP64 at a small fraction
+	// of the FP32 rate).
+#if defined(__CUDACC__)
+	static __host__ __device__ __noinline__
+#else
+	inline
+#endif
+	float BlendTermDouble(float m, float h, float k, bool subtract)
+	{
+		const double q = (double)(h * h) * 0.25 / (double)k;
+		return (float)(subtract ? (double)m - q : (double)m + q);
+	}
+
 	TG_HD float BlendTerm(float m, float h, float k, bool subtract)
 	{
 		if (h == 0.0f && k > 0.0f) return subtract ? m - 0.0f : m + 0.0f;
-		const double q = (double)(h * h) * 0.25 / (double)k;
-		return (float)(subtract ? (double)m - q : (double)m + q);
+		return BlendTermDouble(m, h, k, subtract);
 	}
 
 	TG_HD float SetDistance(uint32_t op, float l, float r, float k)

@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <limits>
+#include <unordered_map>
 
 namespace tg
 {
@@ -37,50 +38,85 @@ namespace tg
 		return 0.0f;
 	}
 
-	// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
-	// that can matter inside the sphere (p, radius).  Union keeps whichever side is near,
-	// Diff keeps its left side, Inter needs both; blending widens the sphere by k.
-	NodeRef Node::Clip(Vec3 p, float radius) const
+	namespace
 	{
-		switch (Kind)
+		// Distances of every subtree at one point, each computed once.  The reference's
+		// Clip calls the virtual Eval at every level of the recursion, re-evaluating each
+		// subtree once per ancestor; caching gives the same floats (same operations, same
+		// order) in time linear in the tree.
+		struct PointEvaluations
 		{
-		case NodeKind::Brush:
-			return Eval(p) <= radius ? NodeRef::Share(const_cast<Node*>(this)) : NodeRef();
-		case NodeKind::Stencil:
-		{
-			NodeRef child = Lhs->Clip(p, radius);
-			if (!child) return NodeRef();
-			return SDF::Stencil(std::move(child), Mask, Mat, Negative);
-		}
-		case NodeKind::Flate:
-		{
-			if (!(Eval(p) <= radius)) return NodeRef();
-			NodeRef child = Lhs->Clip(p, radius + Threshold);
-			if (!child) return NodeRef();
-			return SDF::Flate(std::move(child), Threshold);
-		}
-		case NodeKind::Set:
-		{
-			if (!(Eval(p) <= radius)) return NodeRef();
-			const bool unionFamily = (Op == OpUnion || Op == OpBlendUnion);
-			const bool diffFamily = (Op == OpDiff || Op == OpBlendDiff);
-			if (IsBlendOp(Op))
+			Vec3 P;
+			std::unordered_map<const Node*, float> Values;
+
+			float At(const Node& n)
 			{
-				const float wide = radius + Threshold;
-				NodeRef l = Lhs->Clip(p, wide);
-				NodeRef r = Rhs->Clip(p, wide);
-				if (l && r) return SDF::MakeSet(Op, std::move(l), std::move(r), Threshold);
-				if (!unionFamily && !diffFamily) return NodeRef();
+				auto it = Values.find(&n);
+				if (it != Values.end()) return it->second;
+				float v = 0.0f;
+				switch (n.Kind)
+				{
+				case NodeKind::Brush: v = BrushDistance(n.Op, n.Params, n.Xf.ApplyInv(P)) * n.Xf.Scalation; break;
+				case NodeKind::Set: v = SetDistance(n.Op, At(*n.Lhs), At(*n.Rhs), n.Threshold); break;
+				case NodeKind::Flate: v = At(*n.Lhs) - n.Threshold; break;
+				case NodeKind::Stencil: v = At(*n.Lhs); break;
+				}
+				Values.emplace(&n, v);
+				return v;
 			}
-			NodeRef l = Lhs->Clip(p, radius);
-			NodeRef r = Rhs->Clip(p, radius);
-			if (l && r) return SDF::MakeSet(Op, std::move(l), std::move(r), Threshold);
-			if (unionFamily) return l ? l : r;
-			if (diffFamily) return l;
+		};
+
+		// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
+		// that can matter inside the sphere (p, radius).  Union keeps whichever side is near,
+		// Diff keeps its left side, Inter needs both; blending widens the sphere by k.
+		NodeRef ClipAt(const Node& n, float radius, PointEvaluations& ev)
+		{
+			switch (n.Kind)
+			{
+			case NodeKind::Brush:
+				return ev.At(n) <= radius ? NodeRef::Share(const_cast<Node*>(&n)) : NodeRef();
+			case NodeKind::Stencil:
+			{
+				NodeRef child = ClipAt(*n.Lhs, radius, ev);
+				if (!child) return NodeRef();
+				return SDF::Stencil(std::move(child), n.Mask, n.Mat, n.Negative);
+			}
+			case NodeKind::Flate:
+			{
+				if (!(ev.At(n) <= radius)) return NodeRef();
+				NodeRef child = ClipAt(*n.Lhs, radius + n.Threshold, ev);
+				if (!child) return NodeRef();
+				return SDF::Flate(std::move(child), n.Threshold);
+			}
+			case NodeKind::Set:
+			{
+				if (!(ev.At(n) <= radius)) return NodeRef();
+				const bool unionFamily = (n.Op == OpUnion || n.Op == OpBlendUnion);
+				const bool diffFamily = (n.Op == OpDiff || n.Op == OpBlendDiff);
+				if (IsBlendOp(n.Op))
+				{
+					const float wide = radius + n.Threshold;
+					NodeRef l = ClipAt(*n.Lhs, wide, ev);
+					NodeRef r = ClipAt(*n.Rhs, wide, ev);
+					if (l && r) return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
+					if (!unionFamily && !diffFamily) return NodeRef();
+				}
+				NodeRef l = ClipAt(*n.Lhs, radius, ev);
+				NodeRef r = ClipAt(*n.Rhs, radius, ev);
+				if (l && r) return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
+				if (unionFamily) return l ? l : r;
+				if (diffFamily) return l;
+				return NodeRef();
+			}
+			}
 			return NodeRef();
 		}
-		}
-		return NodeRef();
+	}
+
+	NodeRef Node::Clip(Vec3 p, float radius) const
+	{
+		PointEvaluations ev{ p, {} };
+		return ClipAt(*this, radius, ev);
 	}
 
 	AABB Node::Bounds() const { return BoundsImpl(false); }

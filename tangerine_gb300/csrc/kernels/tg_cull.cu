@@ -32,6 +32,77 @@ namespace tg
 			int NBX, NBY, NBZ;      // bricks per axis
 		};
 
+		// Whether the lattice box [i0, i1] x [j0, j1] x [k0, k1] (corner indices) may hold a
+		// sign change of the reference's distances; false only when that is proven.
+		__device__ __forceinline__ bool BoxMayHoldSurface(const DeviceProgram& prog, const GridSpec& g,
+			int i0, int i1, int j0, int j1, int k0, int k1, float* spill, int stride)
+		{
+			const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
+			const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
+			const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
+			const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
+			const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);
+			// Ball through the box's corners, widened for the rounding of the centre.
+			const float r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
+			const float rootClip = __ldg(&prog.Nodes[0].ClipRadius);
+			const float margin = 1e-4f * (1.0f + fabsf(cx) + fabsf(cy) + fabsf(cz) + fabsf(rootClip));
+			// Outside the root cube every brush, and so every clipped program, is positive
+			// (the cube holds the tree's bounds): a ball missing the cube has no surface.
+			const float half = fabsf(rootClip) * 0.57736f;           // span / 2 = radius / sqrt(3), rounded up
+			const float ox = fmaxf(fabsf(cx - __ldg(&prog.Nodes[0].Pivot[0])) - half, 0.0f);
+			const float oy = fmaxf(fabsf(cy - __ldg(&prog.Nodes[0].Pivot[1])) - half, 0.0f);
+			const float oz = fmaxf(fabsf(cz - __ldg(&prog.Nodes[0].Pivot[2])) - half, 0.0f);
+			if (sqrtf(ox * ox + oy * oy + oz * oz) > r + margin) return false;
+			// Deepest cell on the centre's descent path whose clip sphere holds the ball.
+			int path[48];
+			int depth = 0;
+			int at = 0;
+			path[depth++] = 0;
+			for (int guard = 0; guard < 47; ++guard)
+			{
+				const OctNode* n = prog.Nodes + at;
+				const int32_t flags = __ldg(&n->Flags);
+				if (flags & kNodeTerminus) break;
+				const float px = __ldg(&n->Pivot[0]), py = __ldg(&n->Pivot[1]), pz = __ldg(&n->Pivot[2]);
+				const int octant = (cx > px ? 1 : 0) | (cy > py ? 2 : 0) | (cz > pz ? 4 : 0);
+				const int child = __ldg(&n->Child[octant]);
+				if (child < 0)
+				{
+					// The octree dropped this octant because its clip returned null: the parent's
+					// program exceeds the octant sphere's radius at its centre, so (1-Lipschitz) it
+					// stays above the margin inside that sphere shrunk by the margin.  The octant
+					// sphere sits inside the parent's, where the parent's program has the tree's
+					// sign.  (Octants dropped because all their own children clipped away prove
+					// only their cube, without margin, and are not used.)
+					const float clip = __ldg(&n->ClipRadius);
+					if (clip > 0.0f && ((flags >> (8 + octant)) & 1))
+					{
+						const float q = clip * 0.28867513f;               // span / 4 = radius / (2 sqrt 3)
+						const float qx = px + ((octant & 1) ? q : -q), qy = py + ((octant & 2) ? q : -q), qz = pz + ((octant & 4) ? q : -q);
+						const float dx = cx - qx, dy = cy - qy, dz = cz - qz;
+						if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip * 0.4999f) return false;
+					}
+					break;
+				}
+				at = child;
+				path[depth++] = at;
+			}
+			int holder = -1;
+			for (int d = depth - 1; d >= 0; --d)
+			{
+				const OctNode* n = prog.Nodes + path[d];
+				const float clip = __ldg(&n->ClipRadius);
+				if (clip < 0.0f) break;                           // not 1-Lipschitz here or above
+				const float dx = cx - __ldg(&n->Pivot[0]), dy = cy - __ldg(&n->Pivot[1]), dz = cz - __ldg(&n->Pivot[2]);
+				if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip) { holder = path[d]; break; }
+			}
+			if (holder < 0) return true;
+			const float px[1] = { cx }, py[1] = { cy }, pz[1] = { cz };
+			float f[1];
+			RunDistance<1>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill, stride);
+			return !(fabsf(f[0]) > r + margin);
+		}
+
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ list, uint32_t* __restrict__ count)
 		{
@@ -44,64 +115,8 @@ namespace tg
 				const int bx = (int)(b % bg.NBX), by = (int)((b / bg.NBX) % bg.NBY), bz = (int)(b / ((int64_t)bg.NBX * bg.NBY));
 				const int sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
-				const int i1 = min(i0 + bg.B, sx), j1 = min(j0 + bg.B, sy), k1 = min(k0 + bg.B, sz);
-				const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
-				const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
-				const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
-				const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
-				const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);
-				// Ball through the brick's corners, widened for the rounding of the centre.
-				const float r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
-				const float rootClip = __ldg(&prog.Nodes[0].ClipRadius);
-				const float margin = 1e-4f * (1.0f + fabsf(cx) + fabsf(cy) + fabsf(cz) + fabsf(rootClip));
-				// Outside the root cube every brush, and so every clipped program, is positive
-				// (the cube holds the tree's bounds): a ball missing the cube has no surface.
-				const float half = fabsf(rootClip) * 0.57736f;           // span / 2 = radius / sqrt(3), rounded up
-				const float ox = fmaxf(fabsf(cx - __ldg(&prog.Nodes[0].Pivot[0])) - half, 0.0f);
-				const float oy = fmaxf(fabsf(cy - __ldg(&prog.Nodes[0].Pivot[1])) - half, 0.0f);
-				const float oz = fmaxf(fabsf(cz - __ldg(&prog.Nodes[0].Pivot[2])) - half, 0.0f);
-				if (sqrtf(ox * ox + oy * oy + oz * oz) > r + margin)
-				{
-					active = false;
-				}
-				else
-				{
-					// Deepest cell on the centre's descent path whose clip sphere holds the ball.
-					int path[48];
-					int depth = 0;
-					int at = 0;
-					path[depth++] = 0;
-					for (int guard = 0; guard < 47; ++guard)
-					{
-						const OctNode* n = prog.Nodes + at;
-						if (__ldg(&n->Terminus)) break;
-						const int octant = (cx > __ldg(&n->Pivot[0]) ? 1 : 0) | (cy > __ldg(&n->Pivot[1]) ? 2 : 0) | (cz > __ldg(&n->Pivot[2]) ? 4 : 0);
-						const int child = __ldg(&n->Child[octant]);
-						if (child < 0) break;
-						at = child;
-						path[depth++] = at;
-					}
-					int holder = -1;
-					for (int d = depth - 1; d >= 0; --d)
-					{
-						const OctNode* n = prog.Nodes + path[d];
-						const float clip = __ldg(&n->ClipRadius);
-						if (clip < 0.0f) break;                           // not 1-Lipschitz here or above
-						const float dx = cx - __ldg(&n->Pivot[0]), dy = cy - __ldg(&n->Pivot[1]), dz = cz - __ldg(&n->Pivot[2]);
-						if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip) { holder = path[d]; break; }
-					}
-					if (holder < 0)
-					{
-						active = true;
-					}
-					else
-					{
-						const float px[1] = { cx }, py[1] = { cy }, pz[1] = { cz };
-						float f[1];
-						RunDistance<1>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill + threadIdx.x, kClassifyThreads);
-						active = !(fabsf(f[0]) > r + margin);
-					}
-				}
+				active = BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, sx), j0, min(j0 + bg.B, sy), k0, min(k0 + bg.B, sz),
+					spill + threadIdx.x, kClassifyThreads);
 			}
 			const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
 			const int lane = threadIdx.x & 31;
@@ -115,12 +130,14 @@ namespace tg
 		// Lattice points of every listed brick: corners [i0, i0 + B] per axis, clamped to the
 		// lattice.  A CTA takes bricks from the list with a grid stride; each thread runs
 		// four z-consecutive points through one pass over their octree cell's records.
-		template<int C>
+		// A CTA is 8 x 8 columns x (128 / 64) z-groups; each thread runs K z-consecutive
+		// points, so one pass covers an 8 x 8 x 2K chunk of the brick's lattice box.
+		template<int C, int K>
 		__global__ void __launch_bounds__(kBrickThreads) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice)
 		{
 			extern __shared__ float spill[];
-			constexpr int K = 4;
+			constexpr int ZSpan = 2 * K;
 			const uint32_t n = *count;
 			const int tx = threadIdx.x & 7, ty = (threadIdx.x >> 3) & 7, tz = threadIdx.x >> 6;
 			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
@@ -130,7 +147,7 @@ namespace tg
 				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
 				const int i1 = min(i0 + bg.B, g.NX - 1), j1 = min(j0 + bg.B, g.NY - 1), k1 = min(k0 + bg.B, g.NZ - 1);
-				for (int oz = 0; oz < C; oz += 8)
+				for (int oz = 0; oz < C; oz += ZSpan)
 				for (int oy = 0; oy < C; oy += 8)
 				for (int ox = 0; ox < C; ox += 8)
 				{
@@ -235,53 +252,61 @@ namespace tg
 			return bc;
 		}
 
+		// Also appends each active cell's index to `cells` (in no particular order: vertex
+		// numbers come from the bitmask rank, which is independent of this order).
 		__global__ void __launch_bounds__(128) CellFlagsListedKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words)
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words,
+			uint32_t* __restrict__ cells, uint32_t* __restrict__ cell_count)
 		{
 			const CellGeom cg = Geom(g);
 			const uint32_t n = *count;
+			const int lane = threadIdx.x & 31;
 			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
 			{
 				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
 				const int total = bc.nx * bc.ny * bc.nz;
-				for (int t = threadIdx.x; t < total; t += blockDim.x)
+				const int rounds = (total + (int)blockDim.x - 1) / (int)blockDim.x;
+				for (int r = 0; r < rounds; ++r)
 				{
-					const int64_t i = bc.i0 + t % bc.nx, j = bc.j0 + (t / bc.nx) % bc.ny, k = bc.k0 + t / (bc.nx * bc.ny);
-					float v[8];
-					LoadCorners(lat, cg, i, j, k, v);
-					unsigned pos = 0;
-#pragma unroll
-					for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
-					if (pos != 0u && pos != 0xFFu)
+					const int t = r * (int)blockDim.x + (int)threadIdx.x;
+					bool active = false;
+					int64_t c = 0;
+					if (t < total)
 					{
-						const int64_t c = i + j * cg.sx + k * cg.sx * cg.sy;
-						atomicOr(words + (c >> 5), 1u << (c & 31));
+						const int64_t i = bc.i0 + t % bc.nx, j = bc.j0 + (t / bc.nx) % bc.ny, k = bc.k0 + t / (bc.nx * bc.ny);
+						float v[8];
+						LoadCorners(lat, cg, i, j, k, v);
+						unsigned pos = 0;
+#pragma unroll
+						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+						active = pos != 0u && pos != 0xFFu;
+						c = i + j * cg.sx + k * cg.sx * cg.sy;
+						if (active) atomicOr(words + (c >> 5), 1u << (c & 31));
 					}
+					const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
+					uint32_t base = 0;
+					if (lane == 0 && ballot) base = atomicAdd(cell_count, (uint32_t)__popc(ballot));
+					base = __shfl_sync(0xFFFFFFFFu, base, 0);
+					if (active) cells[base + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)c;
 				}
 			}
 		}
 
-		__global__ void __launch_bounds__(128) CellVerticesListedKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, const uint32_t* __restrict__ words,
+		// One thread per active cell of the list: its vertex number is its rank in the
+		// bitmask, so the output is in cell order whatever the list order.
+		__global__ void __launch_bounds__(128) CellVerticesListedKernel(const float* __restrict__ lat, GridSpec g,
+			const uint32_t* __restrict__ cells, uint32_t cell_count, const uint32_t* __restrict__ words,
 			const uint32_t* __restrict__ base, float* __restrict__ vertices, uint32_t* __restrict__ cubes,
 			uint32_t* __restrict__ face_counts)
 		{
 			const CellGeom cg = Geom(g);
-			const uint32_t n = *count;
-			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
-			{
-				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
-				const int total = bc.nx * bc.ny * bc.nz;
-				for (int t = threadIdx.x; t < total; t += blockDim.x)
-				{
-					const int64_t i = bc.i0 + t % bc.nx, j = bc.j0 + (t / bc.nx) % bc.ny, k = bc.k0 + t / (bc.nx * bc.ny);
-					const int64_t c = i + j * cg.sx + k * cg.sx * cg.sy;
-					const uint32_t w = __ldg(words + (c >> 5));
-					if (!((w >> (c & 31)) & 1u)) continue;
-					const uint32_t vid = __ldg(base + (c >> 5)) + __popc(w & ((1u << (c & 31)) - 1u));
-					EmitCellVertex(lat, g, cg, words, c, i, j, k, vid, vertices, cubes, face_counts);
-				}
-			}
+			const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+			if (t >= cell_count) return;
+			const int64_t c = __ldg(cells + t);
+			const uint32_t w = __ldg(words + (c >> 5));
+			const uint32_t vid = __ldg(base + (c >> 5)) + __popc(w & ((1u << (c & 31)) - 1u));
+			const int64_t i = c % cg.sx, j = (c / cg.sx) % cg.sy, k = c / (cg.sx * cg.sy);
+			EmitCellVertex(lat, g, cg, words, c, i, j, k, vid, vertices, cubes, face_counts);
 		}
 
 		BrickGrid MakeBrickGrid(const GridSpec& g, int B)
@@ -305,32 +330,48 @@ namespace tg
 		if (e != cudaSuccess) return e;
 		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 		const size_t smem = (size_t)depth * kClassifyThreads * sizeof(float);
+		if (smem > 48 * 1024) cudaFuncSetAttribute(ClassifyBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		ClassifyBricksKernel<<<(unsigned)((nb + kClassifyThreads - 1) / kClassifyThreads), kClassifyThreads, smem, stream>>>(
 			prog, g, bg, brick_bits, list, count);
 		return cudaGetLastError();
 	}
 
-	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int grid_blocks, cudaStream_t stream)
+	namespace
 	{
-		const BrickGrid bg = MakeBrickGrid(g, B);
-		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-		const size_t smem = (size_t)depth * 4 * kBrickThreads * sizeof(float);
-		if (B + 1 <= 8)
+		template<int C, int K>
+		cudaError_t LaunchEvalBricksCK(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+			float* lattice, int grid_blocks, cudaStream_t stream)
 		{
-			if (smem > 48 * 1024) cudaFuncSetAttribute(EvalBricksKernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-			EvalBricksKernel<8><<<grid_blocks, kBrickThreads, smem, stream>>>(prog, g, bg, list, count, lattice);
+			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+			const size_t smem = (size_t)depth * K * kBrickThreads * sizeof(float);
+			if (smem > 48 * 1024)
+			{
+				cudaError_t e = cudaFuncSetAttribute(EvalBricksKernel<C, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+				if (e != cudaSuccess) return e;
+			}
+			EvalBricksKernel<C, K><<<grid_blocks, kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list, count, lattice);
+			return cudaGetLastError();
 		}
-		else if (B + 1 <= 16)
+
+		template<int C>
+		cudaError_t LaunchEvalBricksC(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+			float* lattice, int grid_blocks, cudaStream_t stream, int lanes)
 		{
-			if (smem > 48 * 1024) cudaFuncSetAttribute(EvalBricksKernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-			EvalBricksKernel<16><<<grid_blocks, kBrickThreads, smem, stream>>>(prog, g, bg, list, count, lattice);
+			switch (lanes)
+			{
+			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, grid_blocks, stream);
+			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, grid_blocks, stream);
+			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, grid_blocks, stream);
+			}
 		}
-		else
-		{
-			return cudaErrorInvalidValue;
-		}
-		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		float* lattice, int grid_blocks, cudaStream_t stream, int lanes)
+	{
+		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
+		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
+		return cudaErrorInvalidValue;
 	}
 
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
@@ -344,20 +385,21 @@ namespace tg
 	}
 
 	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* words, int grid_blocks, cudaStream_t stream)
+		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int grid_blocks, cudaStream_t stream)
 	{
-		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
-		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((cells + 31) / 32) * 4, stream);
+		const int64_t total = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
+		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((total + 31) / 32) * 4, stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(cell_count, 0, sizeof(uint32_t), stream);
 		if (e != cudaSuccess) return e;
-		CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words);
+		CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
 		return cudaGetLastError();
 	}
 
-	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts,
-		int grid_blocks, cudaStream_t stream)
+	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, const uint32_t* cells, uint32_t cell_count,
+		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts, cudaStream_t stream)
 	{
-		CellVerticesListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, word_base,
+		if (cell_count == 0) return cudaSuccess;
+		CellVerticesListedKernel<<<(cell_count + 127) / 128, 128, 0, stream>>>(lattice, g, cells, cell_count, words, word_base,
 			vertices, cubes, face_counts);
 		return cudaGetLastError();
 	}

@@ -28,7 +28,7 @@ namespace tg
 		for (int guard = 0; guard < 64; ++guard)
 		{
 			const float4 a = __ldg(reinterpret_cast<const float4*>(nodes + at));
-			if (__float_as_int(a.w) != 0) break;          // Terminus
+			if (__float_as_int(a.w) & kNodeTerminus) break;
 			const int octant = (x > a.x ? 1 : 0) | (y > a.y ? 2 : 0) | (z > a.z ? 4 : 0);
 			const int child = __ldg(&nodes[at].Child[octant]);
 			if (child < 0) break;

@@ -77,18 +77,31 @@ namespace tg
 		}
 	}
 
-	cudaError_t LaunchEvalGrid(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream)
+	namespace
 	{
-		constexpr int K = 4;
-		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-		const size_t smem = (size_t)depth * K * kThreads * sizeof(float);
-		if (smem > 48 * 1024)
+		template<int K>
+		cudaError_t LaunchEvalGridK(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream)
 		{
-			cudaError_t e = cudaFuncSetAttribute(EvalGridKernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-			if (e != cudaSuccess) return e;
+			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+			const size_t smem = (size_t)depth * K * kThreads * sizeof(float);
+			if (smem > 48 * 1024)
+			{
+				cudaError_t e = cudaFuncSetAttribute(EvalGridKernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+				if (e != cudaSuccess) return e;
+			}
+			const dim3 blocks((grid.NX + kTileX - 1) / kTileX, (grid.NY + kTileY - 1) / kTileY, (grid.NZ + K - 1) / K);
+			EvalGridKernel<K><<<blocks, kThreads, smem, stream>>>(prog, grid, out);
+			return cudaGetLastError();
 		}
-		const dim3 blocks((grid.NX + kTileX - 1) / kTileX, (grid.NY + kTileY - 1) / kTileY, (grid.NZ + K - 1) / K);
-		EvalGridKernel<K><<<blocks, kThreads, smem, stream>>>(prog, grid, out);
-		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchEvalGrid(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream, int lanes)
+	{
+		switch (lanes)
+		{
+		case 1: return LaunchEvalGridK<1>(prog, grid, out, stream);
+		case 2: return LaunchEvalGridK<2>(prog, grid, out, stream);
+		default: return LaunchEvalGridK<4>(prog, grid, out, stream);
+		}
 	}
 }

@@ -18,7 +18,8 @@ namespace tg
 	};
 
 	// Distances at every lattice point (x fastest), SDFOctree::Eval(p, Exact = true).
-	cudaError_t LaunchEvalGrid(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream);
+	// `lanes` points per thread (1, 2 or 4) share one pass over the records.
+	cudaError_t LaunchEvalGrid(const DeviceProgram& prog, const GridSpec& grid, float* out, cudaStream_t stream, int lanes = 4);
 
 	// Surface nets, cell pass part 1: one bit per cell (x fastest) set when the cell's
 	// eight corners do not all share a sign.  `words` holds ceil(cells / 32) words.
@@ -30,15 +31,16 @@ namespace tg
 	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, uint32_t* list,
 		uint32_t* count, cudaStream_t stream);
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int grid_blocks, cudaStream_t stream);
+		float* lattice, int grid_blocks, cudaStream_t stream, int lanes = 4);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
 		cudaStream_t stream);
-	// Cell passes over the cells of listed bricks only (the bitmask is cleared first).
+	// Cell pass over the cells of listed bricks only: clears and fills the bitmask and
+	// lists the active cells (`cells` holds up to the lattice's cell count).
 	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* words, int grid_blocks, cudaStream_t stream);
-	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts,
-		int grid_blocks, cudaStream_t stream);
+		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int grid_blocks, cudaStream_t stream);
+	// Vertex pass over the listed active cells (one thread each).
+	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, const uint32_t* cells, uint32_t cell_count,
+		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts, cudaStream_t stream);
 
 	// Exclusive prefix sum of popcount(words[i]) (popcount = true) or of counts[i].
 	// `scratch` needs ScanScratchWords(n) words.  `total` (device) receives the sum.

@@ -86,28 +86,115 @@ namespace tg
 			}
 		}
 
-		constexpr int kAttribThreads = 128;
+		// Normals and colours: five threads per point (the four tetrahedral offsets of
+		// SDFNode::Gradient and the point itself, which also follows GetMaterial), each a
+		// single pass over the point's surface program; lane 0 combines them.  One lane per
+		// evaluation keeps the interpreter's code small enough for the instruction cache.
+		constexpr int kPointsPerBlock = 32;
+		constexpr int kAttribThreads = kPointsPerBlock * 5;
+
+		__device__ __forceinline__ Vec3 TetraPoint(Vec3 p, int lane)
+		{
+			const float h = 0.0001f;
+			switch (lane)
+			{
+			case 0: return p + Vec3(h, -h, -h);
+			case 1: return p + Vec3(-h, -h, h);
+			case 2: return p + Vec3(-h, h, -h);
+			case 3: return p + Vec3(h, h, h);
+			default: return p;
+			}
+		}
+
+		// SDFNode::Gradient (sdf_evaluator.cpp:298-333) from the five evaluations.
+		__device__ __forceinline__ Vec3 GradientOf(const float* e)
+		{
+			const float h = 0.0001f;
+			const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+			Vec3 g = xyy * e[0];
+			g = g + yyx * e[1];
+			g = g + yxy * e[2];
+			g = g + xxx * e[3];
+			const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+			if (ls == 0.0f)
+			{
+				const float d = e[4];
+				return Normalize(Vec3(e[0] - d, e[2] - d, e[1] - d));
+			}
+			return g / sqrtf(ls);
+		}
+
+		// One evaluation lane: distance at TetraPoint(p, lane); lane 4 with `material` also
+		// returns the material index.
+		__device__ __forceinline__ float EvaluationLane(const DeviceProgram& prog, Vec3 p, int lane, bool material, int* m, float* spill)
+		{
+			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
+			const int pc = __ldg(&prog.Nodes[cell].SurfaceCode);
+			const Vec3 q = TetraPoint(p, lane);
+			const float px[1] = { q.x }, py[1] = { q.y }, pz[1] = { q.z };
+			float e[1];
+			RunSurfaceBatch<1>(prog.Code, pc, px, py, pz, e, (lane == 4 && material) ? 0 : -1, m, spill, kAttribThreads);
+			return e[0];
+		}
 
 		__global__ void __launch_bounds__(kAttribThreads) VertexAttributesKernel(DeviceProgram prog, const float* __restrict__ vertices,
 			uint32_t n, float* __restrict__ normals, uint8_t* __restrict__ colors)
 		{
 			extern __shared__ float spill[];
-			const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-			if (v >= n) return;
-			const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
-			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
-			const int pc = __ldg(&prog.Nodes[cell].SurfaceCode);
-			int m = -1;
-			const Vec3 g = SurfaceGradientBatch(prog.Code, pc, p, colors != nullptr, &m, spill + threadIdx.x, kAttribThreads);
-			normals[(int64_t)v * 3 + 0] = g.x;
-			normals[(int64_t)v * 3 + 1] = g.y;
-			normals[(int64_t)v * 3 + 2] = g.z;
-			if (colors)
+			__shared__ float evals[kAttribThreads];
+			__shared__ int mats[kPointsPerBlock];
+			const int local = threadIdx.x / 5, lane = threadIdx.x % 5;
+			const uint32_t v = blockIdx.x * kPointsPerBlock + local;
+			if (v < n)
 			{
-				const uchar4 c = m >= 0 ? prog.Colors[m] : make_uchar4(255, 255, 255, 255);
-				colors[(int64_t)v * 3 + 0] = c.x;
-				colors[(int64_t)v * 3 + 1] = c.y;
-				colors[(int64_t)v * 3 + 2] = c.z;
+				const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
+				int m = -1;
+				evals[threadIdx.x] = EvaluationLane(prog, p, lane, colors != nullptr, &m, spill + threadIdx.x);
+				if (lane == 4) mats[local] = m;
+			}
+			__syncthreads();
+			if (v < n && lane == 0)
+			{
+				const Vec3 g = GradientOf(evals + local * 5);
+				normals[(int64_t)v * 3 + 0] = g.x;
+				normals[(int64_t)v * 3 + 1] = g.y;
+				normals[(int64_t)v * 3 + 2] = g.z;
+				if (colors)
+				{
+					const int m = mats[local];
+					const uchar4 c = m >= 0 ? prog.Colors[m] : make_uchar4(255, 255, 255, 255);
+					colors[(int64_t)v * 3 + 0] = c.x;
+					colors[(int64_t)v * 3 + 1] = c.y;
+					colors[(int64_t)v * 3 + 2] = c.z;
+				}
+			}
+		}
+
+		// WriteSTL(Octree, ...) (export.cpp:140-148): the gradient at (a + b + c) / 3.
+		__global__ void __launch_bounds__(kAttribThreads) FaceNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
+			const uint32_t* __restrict__ faces, uint64_t n, float* __restrict__ normals)
+		{
+			extern __shared__ float spill[];
+			__shared__ float evals[kAttribThreads];
+			const int local = threadIdx.x / 5, lane = threadIdx.x % 5;
+			const uint64_t f = (uint64_t)blockIdx.x * kPointsPerBlock + local;
+			if (f < n)
+			{
+				const uint32_t a = faces[f * 3], b = faces[f * 3 + 1], c = faces[f * 3 + 2];
+				const Vec3 va(vertices[(int64_t)a * 3], vertices[(int64_t)a * 3 + 1], vertices[(int64_t)a * 3 + 2]);
+				const Vec3 vb(vertices[(int64_t)b * 3], vertices[(int64_t)b * 3 + 1], vertices[(int64_t)b * 3 + 2]);
+				const Vec3 vc(vertices[(int64_t)c * 3], vertices[(int64_t)c * 3 + 1], vertices[(int64_t)c * 3 + 2]);
+				const Vec3 s = (va + vb) + vc;
+				const Vec3 center(s.x / 3.0f, s.y / 3.0f, s.z / 3.0f);
+				evals[threadIdx.x] = EvaluationLane(prog, center, lane, false, nullptr, spill + threadIdx.x);
+			}
+			__syncthreads();
+			if (f < n && lane == 0)
+			{
+				const Vec3 g = GradientOf(evals + local * 5);
+				normals[f * 3] = g.x;
+				normals[f * 3 + 1] = g.y;
+				normals[f * 3 + 2] = g.z;
 			}
 		}
 
@@ -121,27 +208,6 @@ namespace tg
 			const int cell = DescendOctree(prog.Nodes, px[0], py[0], pz[0]);
 			RunDistance<1>(prog.Code, __ldg(&prog.Nodes[cell].DistanceCode), px, py, pz, r, spill, 1);
 			out[t] = r[0];
-		}
-
-		// WriteSTL(Octree, ...) (export.cpp:140-148): the gradient at (a + b + c) / 3.
-		__global__ void __launch_bounds__(128) FaceNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
-			const uint32_t* __restrict__ faces, uint64_t n, float* __restrict__ normals)
-		{
-			extern __shared__ float spill[];
-			const uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-			if (f >= n) return;
-			const uint32_t a = faces[f * 3], b = faces[f * 3 + 1], c = faces[f * 3 + 2];
-			const Vec3 va(vertices[(int64_t)a * 3], vertices[(int64_t)a * 3 + 1], vertices[(int64_t)a * 3 + 2]);
-			const Vec3 vb(vertices[(int64_t)b * 3], vertices[(int64_t)b * 3 + 1], vertices[(int64_t)b * 3 + 2]);
-			const Vec3 vc(vertices[(int64_t)c * 3], vertices[(int64_t)c * 3 + 1], vertices[(int64_t)c * 3 + 2]);
-			const Vec3 s = (va + vb) + vc;
-			const Vec3 center(s.x / 3.0f, s.y / 3.0f, s.z / 3.0f);
-			const int cell = DescendOctree(prog.Nodes, center.x, center.y, center.z);
-			const Vec3 g = SurfaceGradientBatch(prog.Code, __ldg(&prog.Nodes[cell].SurfaceCode), center, false, nullptr,
-				spill + threadIdx.x, 128);
-			normals[f * 3] = g.x;
-			normals[f * 3 + 1] = g.y;
-			normals[f * 3 + 2] = g.z;
 		}
 
 		// ---- exclusive scan: 1024 threads x 4 items per block -------------------------
@@ -293,20 +359,21 @@ namespace tg
 		return cudaGetLastError();
 	}
 
-	// Shared memory of the batched surface evaluation: 5 distances + 1 material per level.
+	// Shared memory of the single-lane surface evaluation: distance + material per level.
 	static size_t SurfaceSpillBytes(const DeviceProgram& prog, int threads)
 	{
 		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-		return (size_t)depth * 6 * threads * sizeof(float);
+		return (size_t)depth * 2 * threads * sizeof(float);
 	}
 
 	cudaError_t LaunchFaceNormals(const DeviceProgram& prog, const float* vertices, const uint32_t* faces, uint64_t face_count,
 		float* normals, cudaStream_t stream)
 	{
 		if (face_count == 0) return cudaSuccess;
-		const size_t smem = SurfaceSpillBytes(prog, 128);
-		if (smem > 48 * 1024) cudaFuncSetAttribute(FaceNormalsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		FaceNormalsKernel<<<Blocks((int64_t)face_count, 128), 128, smem, stream>>>(prog, vertices, faces, face_count, normals);
+		const size_t smem = SurfaceSpillBytes(prog, kAttribThreads);
+		if (smem > 40 * 1024) cudaFuncSetAttribute(FaceNormalsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		FaceNormalsKernel<<<Blocks((int64_t)face_count, kPointsPerBlock), kAttribThreads, smem, stream>>>(prog, vertices, faces,
+			face_count, normals);
 		return cudaGetLastError();
 	}
 
@@ -315,8 +382,8 @@ namespace tg
 	{
 		if (vertex_count == 0) return cudaSuccess;
 		const size_t smem = SurfaceSpillBytes(prog, kAttribThreads);
-		if (smem > 48 * 1024) cudaFuncSetAttribute(VertexAttributesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		VertexAttributesKernel<<<Blocks(vertex_count, kAttribThreads), kAttribThreads, smem, stream>>>(prog, vertices, vertex_count,
+		if (smem > 40 * 1024) cudaFuncSetAttribute(VertexAttributesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		VertexAttributesKernel<<<Blocks(vertex_count, kPointsPerBlock), kAttribThreads, smem, stream>>>(prog, vertices, vertex_count,
 			normals, colors);
 		return cudaGetLastError();
 	}

@@ -132,8 +132,8 @@ def _grid(g) -> _lib.Grid:
     return _lib.Grid(g.x0, g.y0, g.z0, g.step, g.sx + 1, g.sy + 1, g.sz + 1)
 
 
-def _flags(attributes=True, dense=False, brick=0) -> int:
-    return (1 if attributes else 0) | (2 if dense else 0) | ((int(brick) & 0xFF) << 8)
+def _flags(attributes=True, dense=False, brick=0, lanes=0) -> int:
+    return (1 if attributes else 0) | (2 if dense else 0) | ((int(brick) & 0xFF) << 8) | ((int(lanes) & 0xF) << 16)
 
 
 def last_export_stats():
@@ -211,17 +211,17 @@ class Program:
         check(load().tg_eval_points(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), stream), "tg_eval_points")
         return out
 
-    def export_mesh(self, grid, attributes=True, dense=False, brick=0, stream=None) -> Mesh:
+    def export_mesh(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None) -> Mesh:
         g = _grid(grid)
         hm = _lib.HostMesh()
-        check(load().tg_export_mesh(self.ptr, C.byref(g), _flags(attributes, dense, brick), C.byref(hm), stream),
+        check(load().tg_export_mesh(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes), C.byref(hm), stream),
               "tg_export_mesh")
         return _take_mesh(hm)
 
-    def export_mesh_device(self, grid, attributes=True, dense=False, brick=0, stream=None) -> _lib.DeviceMesh:
+    def export_mesh_device(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None) -> _lib.DeviceMesh:
         g = _grid(grid)
         dm = _lib.DeviceMesh()
-        check(load().tg_export_mesh_device(self.ptr, C.byref(g), _flags(attributes, dense, brick), C.byref(dm), stream),
+        check(load().tg_export_mesh_device(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes), C.byref(dm), stream),
               "tg_export_mesh_device")
         return dm
 
