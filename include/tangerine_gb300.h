@@ -233,6 +233,40 @@ TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, const tg_gri
 TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], const float model_max[3], float step,
                                        tg_mesh* out, void* stream);
 
+/* SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the whole tree for n rays, on the GPU:
+ * the reference's step sequence, so hit flags, travel (+inf on a miss) and end positions
+ * match it bit for bit.  Host arrays, 3 floats per origin / direction / position. */
+TANGERINE_API tg_status tg_ray_march(tg_program* program, const float* origins, const float* dirs, int64_t n,
+                                     int max_iterations, float epsilon, uint8_t* hit, float* travel, float* position,
+                                     void* stream);
+
+/* Pinhole camera looking from `position` at `target`; `up` fixes the roll; tan_half_fov is
+ * tan(vertical field of view / 2).  Pixel (x, y) of a W x H image looks along
+ * forward + right*u + up'*v, u = (2(x+0.5)/W - 1) * tan_half_fov * W/H,
+ * v = (1 - 2(y+0.5)/H) * tan_half_fov, with forward = normalize(target - position),
+ * right = normalize(cross(forward, up)), up' = cross(right, forward). */
+typedef struct tg_camera
+{
+	float position[3];
+	float target[3];
+	float up[3];
+	float tan_half_fov;
+} tg_camera;
+
+enum
+{
+	TG_RENDER_EXACT = 1u,       /* every step on the whole tree, as SDFNode::RayMarch; else
+	                               octree-bounded steps (same hits, fewer operations) */
+};
+
+/* Sphere-traced depth (travel along the normalised ray, +inf on a miss), gradient normal
+ * (0 on a miss) and colour bytes (0 on a miss) for `count` cameras, image after image,
+ * rows top to bottom.  depth: count*W*H floats, normals: 3 per pixel, colors: 3 per pixel
+ * or NULL.  Host buffers, or device buffers when out_is_device is nonzero. */
+TANGERINE_API tg_status tg_render(tg_program* program, const tg_camera* cameras, int count, int width, int height,
+                                  int max_steps, float epsilon, uint32_t flags, float* depth, float* normals,
+                                  uint8_t* colors, int out_is_device, void* stream);
+
 /* Files in the reference's byte layout (WritePLY / WriteSTL, export.cpp:60-317).
  * The STL writer needs the program for its per-face gradient normals. */
 TANGERINE_API tg_status tg_write_ply(const tg_mesh* mesh, const char* path, float scale);
@@ -247,7 +281,8 @@ TANGERINE_API tg_status tg_last_export_timing(double* compile_s, double* upload_
 
 /* Per-kernel device time of the export pipeline, accumulated while enabled (CUDA events
  * on the launching stream).  Names: "eval_grid", "cell_flags", "scan", "cell_vertices",
- * "faces", "attributes", "face_normals", "eval_points", "classify_bricks", "eval_bricks". */
+ * "faces", "attributes", "face_normals", "eval_points", "classify_bricks", "eval_bricks",
+ * "ray_march", "render". */
 TANGERINE_API void tg_profile_enable(int enable);
 TANGERINE_API int tg_profile_read(const char* kernel, double* total_ms, int64_t* launches);
 TANGERINE_API void tg_profile_reset(void);

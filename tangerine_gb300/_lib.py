@@ -23,6 +23,10 @@ class Grid(C.Structure):
                 ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("tan_half_fov", C.c_float)]
+
+
 class ProgramInfo(C.Structure):
     _fields_ = [("octree_cells", C.c_int32), ("code_quads", C.c_int32), ("materials", C.c_int32),
                 ("has_paint", C.c_int32), ("max_stack", C.c_int32),
@@ -89,6 +93,8 @@ SIGNATURES = {
     "tg_export_mesh_noalloc": (_i, [_vp, C.POINTER(Grid), _u32, _vp, _vp, _vp, _vp, _vp, C.c_uint64, C.c_uint64,
                                     C.POINTER(C.c_uint64), _vp]),
     "tg_export_tree": (_i, [_vp, _vp, _vp, _f, C.POINTER(HostMesh), _vp]),
+    "tg_ray_march": (_i, [_vp, _vp, _vp, _i64, _i, _f, _vp, _vp, _vp, _vp]),
+    "tg_render": (_i, [_vp, C.POINTER(Camera), _i, _i, _i, _i, _f, _u32, _vp, _vp, _vp, _i, _vp]),
     "tg_write_ply": (_i, [C.POINTER(HostMesh), C.c_char_p, _f]),
     "tg_write_stl": (_i, [_vp, C.POINTER(HostMesh), C.c_char_p, _f, _vp]),
     "tg_last_export_stats": (_i, [C.POINTER(_i64), C.POINTER(_i64)]),

@@ -10,6 +10,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "tg_engine.hpp"
 #include "tg_octree.hpp"
@@ -412,6 +413,49 @@ extern "C"
 		tm.GpuSeconds = secs(t1, t2);
 		tm.CopySeconds = secs(t2, t3);
 		return st;
+	}
+
+	TANGERINE_API tg_status tg_ray_march(tg_program* p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
+		uint8_t* hit, float* travel, float* position, void* stream)
+	{
+		if (!p || (n > 0 && (!origins || !dirs || !hit || !travel || !position))) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (iterations < 0) { SetError("negative iteration count"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.RayMarch(*p, origins, dirs, n, iterations, epsilon, hit, travel, position, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "ray marching");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_render(tg_program* p, const tg_camera* cameras, int count, int width, int height, int max_steps,
+		float epsilon, uint32_t flags, float* depth, float* normals, uint8_t* colors, int out_is_device, void* stream)
+	{
+		if (!p || !cameras || !depth || !normals) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (count < 0 || width <= 0 || height <= 0 || max_steps < 0) { SetError("invalid image size or step count"); return TG_ERR_INVALID; }
+		std::vector<CameraBasis> basis((size_t)count);
+		for (int c = 0; c < count; ++c)
+		{
+			const tg_camera& cam = cameras[c];
+			const Vec3 pos(cam.position[0], cam.position[1], cam.position[2]);
+			const Vec3 fwd = Normalize(Vec3(cam.target[0], cam.target[1], cam.target[2]) - pos);
+			const Vec3 right = Normalize(Cross(fwd, Vec3(cam.up[0], cam.up[1], cam.up[2])));
+			const Vec3 up = Cross(right, fwd);
+			CameraBasis& b = basis[(size_t)c];
+			b.Position[0] = pos.x; b.Position[1] = pos.y; b.Position[2] = pos.z;
+			b.Forward[0] = fwd.x; b.Forward[1] = fwd.y; b.Forward[2] = fwd.z;
+			b.Right[0] = right.x; b.Right[1] = right.y; b.Right[2] = right.z;
+			b.Up[0] = up.x; b.Up[1] = up.y; b.Up[2] = up.z;
+			b.TanHalfFov = cam.tan_half_fov;
+			b.Aspect = (float)width / (float)height;
+		}
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.Render(*p, basis.data(), count, width, height, max_steps, epsilon, (flags & TG_RENDER_EXACT) != 0, depth,
+			normals, p->Host.Header.HasPaint ? colors : nullptr, out_is_device != 0, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "rendering");
+		if (colors && !p->Host.Header.HasPaint && !out_is_device)
+			std::memset(colors, 255, (size_t)width * height * count * 3);
+		return TG_OK;
 	}
 
 	// WritePLY (export.cpp:198-280): header, then x y z nx ny nz [r g b] per vertex, then

@@ -135,6 +135,8 @@ namespace tg
 			p.View.Code = reinterpret_cast<const float4*>(base + l.CodeOff);
 			p.View.Colors = reinterpret_cast<const uchar4*>(base + l.ColorOff);
 			p.View.MaxStack = p.Host.Header.MaxStack;
+			p.View.FullSurfaceCode = p.Host.Header.FullSurfaceCode;
+			p.View.Lipschitz = p.Host.Header.Lipschitz;
 		}
 	}
 
@@ -189,6 +191,8 @@ namespace tg
 		p.View.Code = reinterpret_cast<const float4*>(base + codeOff);
 		p.View.Colors = reinterpret_cast<const uchar4*>(base + colorOff);
 		p.View.MaxStack = p.Host.Header.MaxStack;
+		p.View.FullSurfaceCode = p.Host.Header.FullSurfaceCode;
+		p.View.Lipschitz = p.Host.Header.Lipschitz;
 		return cudaSuccess;
 	}
 
@@ -407,5 +411,61 @@ namespace tg
 		Collect();
 		v.Release(); f.Release(); n.Release();
 		return e;
+	}
+
+	cudaError_t Engine::RayMarch(const Program& p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
+		uint8_t* hit, float* travel, float* position, cudaStream_t s)
+	{
+		if (n <= 0) return cudaSuccess;
+		const size_t in = (size_t)n * 12;
+		TG_TRY(RayIn.Reserve(2 * in));
+		TG_TRY(RayOut.Reserve((size_t)n * 17));
+		float* dOrig = RayIn.As<float>();
+		float* dDir = dOrig + n * 3;
+		float* dTravel = RayOut.As<float>();
+		float* dPos = dTravel + n;
+		uint8_t* dHit = reinterpret_cast<uint8_t*>(dPos + n * 3);
+		TG_TRY(cudaMemcpyAsync(dOrig, origins, in, cudaMemcpyHostToDevice, s));
+		TG_TRY(cudaMemcpyAsync(dDir, dirs, in, cudaMemcpyHostToDevice, s));
+		Begin("ray_march", s);
+		TG_TRY(LaunchRayMarch(p.View, dOrig, dDir, n, iterations, epsilon, dHit, dTravel, dPos, s));
+		End(s);
+		TG_TRY(cudaMemcpyAsync(hit, dHit, (size_t)n, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaMemcpyAsync(travel, dTravel, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaMemcpyAsync(position, dPos, in, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaStreamSynchronize(s));
+		Collect();
+		return cudaSuccess;
+	}
+
+	cudaError_t Engine::Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
+		bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s)
+	{
+		const int64_t px = (int64_t)width * height * count;
+		if (px <= 0) return cudaSuccess;
+		TG_TRY(Cameras.Reserve(sizeof(CameraBasis) * (size_t)count));
+		TG_TRY(cudaMemcpyAsync(Cameras.Ptr, cams, sizeof(CameraBasis) * (size_t)count, cudaMemcpyHostToDevice, s));
+		float* dDepth = depth;
+		float* dNormals = normals;
+		uint8_t* dColors = colors;
+		if (!out_is_device)
+		{
+			TG_TRY(Image.Reserve((size_t)px * (4 + 12 + 3)));
+			dDepth = Image.As<float>();
+			dNormals = dDepth + px;
+			dColors = colors ? reinterpret_cast<uint8_t*>(dNormals + px * 3) : nullptr;
+		}
+		Begin("render", s);
+		TG_TRY(LaunchRender(p.View, Cameras.As<CameraBasis>(), count, width, height, steps, epsilon, exact, dDepth, dNormals, dColors, s));
+		End(s);
+		if (!out_is_device)
+		{
+			TG_TRY(cudaMemcpyAsync(depth, dDepth, (size_t)px * 4, cudaMemcpyDeviceToHost, s));
+			TG_TRY(cudaMemcpyAsync(normals, dNormals, (size_t)px * 12, cudaMemcpyDeviceToHost, s));
+			if (colors) TG_TRY(cudaMemcpyAsync(colors, dColors, (size_t)px * 3, cudaMemcpyDeviceToHost, s));
+		}
+		TG_TRY(cudaStreamSynchronize(s));
+		Collect();
+		return cudaSuccess;
 	}
 }

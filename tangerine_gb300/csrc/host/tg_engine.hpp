@@ -71,6 +71,10 @@ namespace tg
 		int64_t LastBricks() const { return Bricks; }
 		cudaError_t FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
 			uint64_t face_count, float* host_normals, cudaStream_t s);
+		cudaError_t RayMarch(const Program& p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
+			uint8_t* hit, float* travel, float* position, cudaStream_t s);
+		cudaError_t Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
+			bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s);
 		DeviceBuffer& Lattice() { return LatticeBuf; }
 
 		// Profiling of kernel launches (CUDA events on the launching stream).
@@ -93,6 +97,7 @@ namespace tg
 		cudaStream_t Stream = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
 		DeviceBuffer Points, PointOut, BrickBits, BrickList, ProgramScratch, ActiveCells;
+		DeviceBuffer RayIn, RayOut, Cameras, Image;
 		void* Staging = nullptr;
 		size_t StagingBytes = 0;
 		uint32_t* HostCounts = nullptr;

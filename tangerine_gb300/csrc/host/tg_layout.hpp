@@ -66,6 +66,8 @@ namespace tg
 		int32_t MaterialCount;
 		int32_t HasPaint;           // root evaluator HasPaint(): colours are exported
 		int32_t MaxStack;
-		int32_t Reserved[3];
+		int32_t FullSurfaceCode;    // quad offset of the whole tree's surface program
+		int32_t Lipschitz;          // 1 when every brush is 1-Lipschitz (no ellipsoid)
+		int32_t Reserved;
 	};
 }

@@ -536,6 +536,17 @@ namespace tg
 			if (n.StackSize > maxStack) maxStack = n.StackSize;
 			out.DistanceQuadsTotal += surf - dist;
 		}
+		// The whole tree's surface program, for SDFNode::RayMarch / Eval on the full tree.
+		const int full = (int)(out.Code.size() / 4);
+		em.NonLipschitz = false;
+		em.Surface(*root);
+		em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+		{
+			const int d = SurfaceDepth(out.Code.data(), full);
+			if (d > maxStack) maxStack = d;
+		}
+		out.Header.FullSurfaceCode = full;
+		out.Header.Lipschitz = HasNonLipschitzBrush(*root) ? 0 : 1;
 		if (maxStack > kMaxStack)
 		{
 			error = "tree needs a deeper evaluation stack than the kernels hold";

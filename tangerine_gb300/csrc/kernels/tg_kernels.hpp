@@ -15,7 +15,30 @@ namespace tg
 		const float4* Code;
 		const uchar4* Colors;
 		int MaxStack;
+		int FullSurfaceCode;    // the whole tree's surface program
+		int Lipschitz;          // every brush 1-Lipschitz
 	};
+
+	// Pinhole camera: pixel (x, y) looks along forward + right*u + up*v with
+	// u = (2(x + 0.5)/W - 1) * tan_half_fov * W/H and v = (1 - 2(y + 0.5)/H) * tan_half_fov.
+	struct CameraBasis
+	{
+		float Position[3];
+		float Forward[3];
+		float Right[3];
+		float Up[3];
+		float TanHalfFov;
+		float Aspect;
+	};
+
+	// SDFNode::RayMarch on the whole tree for n rays (reference step sequence).
+	cudaError_t LaunchRayMarch(const DeviceProgram& prog, const float* origins, const float* dirs, int64_t n, int max_iterations,
+		float epsilon, uint8_t* hit, float* travel, float* position, cudaStream_t stream);
+
+	// Depth (travel, +inf on a miss), gradient normal and colour per pixel for `count`
+	// cameras.  exact: the reference's full-tree steps; otherwise octree-bounded steps.
+	cudaError_t LaunchRender(const DeviceProgram& prog, const CameraBasis* cameras, int count, int width, int height,
+		int max_steps, float epsilon, bool exact, float* depth, float* normals, uint8_t* colors, cudaStream_t stream);
 
 	// Distances at every lattice point (x fastest), SDFOctree::Eval(p, Exact = true).
 	// `lanes` points per thread (1, 2 or 4) share one pass over the records.

@@ -226,6 +226,47 @@ class Program:
         return dm
 
 
+def _program_ray_march(self, origins, dirs, iterations=100, epsilon=1e-3, stream=None):
+    """SDFNode::RayMarch on the GPU: (hit, travel, position) per ray."""
+    o = np.ascontiguousarray(np.asarray(origins, np.float32).reshape(-1, 3))
+    d = np.ascontiguousarray(np.asarray(dirs, np.float32).reshape(-1, 3))
+    n = o.shape[0]
+    hit = np.empty(n, np.uint8)
+    travel = np.empty(n, np.float32)
+    pos = np.empty((n, 3), np.float32)
+    check(load().tg_ray_march(self.ptr, _lib.as_ptr(o), _lib.as_ptr(d), n, iterations, epsilon, _lib.as_ptr(hit),
+                              _lib.as_ptr(travel), _lib.as_ptr(pos), stream), "tg_ray_march")
+    return hit.astype(bool), travel, pos
+
+
+def cameras(positions, target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_y_degrees=60.0):
+    """tg_camera array looking at `target` from each position."""
+    import math
+    arr = (_lib.Camera * len(positions))()
+    t = float(np.float32(math.tan(math.radians(fov_y_degrees) * 0.5)))
+    for i, p in enumerate(positions):
+        arr[i].position[:] = [float(v) for v in p]
+        arr[i].target[:] = [float(v) for v in target]
+        arr[i].up[:] = [float(v) for v in up]
+        arr[i].tan_half_fov = t
+    return arr
+
+
+def _program_render(self, cams, width, height, steps=256, epsilon=1e-4, exact=False, stream=None):
+    """(depth, normals, colors) images, one per camera."""
+    n = len(cams)
+    depth = np.empty((n, height, width), np.float32)
+    normals = np.empty((n, height, width, 3), np.float32)
+    colors = np.empty((n, height, width, 3), np.uint8)
+    check(load().tg_render(self.ptr, cams, n, width, height, steps, epsilon, 1 if exact else 0, _lib.as_ptr(depth),
+                           _lib.as_ptr(normals), _lib.as_ptr(colors), 0, stream), "tg_render")
+    return depth, normals, colors
+
+
+Program.ray_march = _program_ray_march
+Program.render = _program_render
+
+
 def compile(tree: Tree) -> Program:  # noqa: A001 - mirrors tg_compile
     return Program(tree)
 
