@@ -197,7 +197,7 @@ def cpu_baseline(spec, grid, seconds_target=12.0):
             secs += dt
             slab *= 2
         return {"value": done_samples / secs, "unit": "samples/s", "cores": threads, "kind": "port",
-                "sample": f"z-slabs of the same {RES}^3 export ({done_samples} lattice samples, {secs:.1f} s): "
+                "sample": f"z-slabs of the same {grid.sx - 2}^3 export ({done_samples} lattice samples, {secs:.1f} s): "
                           f"C restatement of the reference export, 8 corner evaluations per cell and 6 per "
                           f"face check as the reference makes, then per-vertex gradient + colour",
                 "seconds": secs}
@@ -234,6 +234,72 @@ def reference_arm(args, rank):
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
+
+
+def mesh_difference(a, b):
+    """(identical, symmetric Hausdorff distance between the vertex sets)."""
+    same = (a.vertices.shape == b.vertices.shape and np.array_equal(a.vertices, b.vertices)
+            and np.array_equal(a.faces, b.faces))
+    if same:
+        return True, 0.0
+    from scipy.spatial import cKDTree
+    if len(a.vertices) == 0 or len(b.vertices) == 0:
+        return False, float("inf")
+    d1 = cKDTree(b.vertices).query(a.vertices)[0].max()
+    d2 = cKDTree(a.vertices).query(b.vertices)[0].max()
+    return False, float(max(d1, d2))
+
+
+def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_ms, world, brick=0):
+    """Trains the network on the program, then times the culled export with it deciding
+    which bricks to skip: alone, and with the exact test on the bricks it keeps."""
+    import torch
+    from tangerine_gb300 import sdf
+    sur = sdf.Surrogate()
+    info = sur.fit(prog)
+    exact_mesh = prog.export_mesh(grid, brick=brick)
+    out = {"train_seconds": info.train_seconds, "data_seconds": info.data_seconds, "samples": int(info.samples),
+           "steps": int(info.steps), "max_error": info.max_error, "p99_error": info.p99_error,
+           "mean_error": info.mean_error, "final_loss": info.final_loss, "modes": {}}
+    bsize = brick or 7
+    out["margin"] = sur.margin(0.8660254 * bsize * grid.step)
+    for mode, only in (("network alone", True), ("network + exact test", False)):
+        m = sur.export_mesh(prog, grid, brick=brick, only=only)
+        same, hausdorff = mesh_difference(m, exact_mesh)
+        bricks, kept = sdf.last_export_stats()
+        for _ in range(2):
+            sur.export_mesh_device(prog, grid, brick=brick, only=only, stream=sp)
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            st[i].record(stream)
+            sur.export_mesh_device(prog, grid, brick=brick, only=only, stream=sp)
+            en[i].record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.sum([a.elapsed_time(b) for a, b in zip(st, en)]))
+        out["modes"][mode] = {"value": world * samples * args.steps / (ms * 1e-3), "unit": "samples/s",
+                              "ms_per_step": ms / args.steps, "bricks_evaluated": kept, "bricks": bricks,
+                              "same_mesh_as_exact": same, "hausdorff": hausdorff,
+                              "hausdorff_over_bbox_diagonal": hausdorff / (4.0 * 3 ** 0.5),
+                              "vs_exact_culled": exact_ms / ms, "vs_dense": dense_ms / ms}
+    best_mode = max(out["modes"], key=lambda k: out["modes"][k]["value"])
+    out["value"] = out["modes"][best_mode]["value"]
+    out["unit"] = "samples/s"
+    # End to end through the C ABI: tg_export_mesh_surrogate, mesh copied to host memory.
+    only = best_mode == "network alone"
+    reps = 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        m = sur.export_mesh(prog, grid, brick=brick, only=only, stream=sp)
+    secs = time.perf_counter() - t0
+    d2h = m.vertices.nbytes + m.normals.nbytes + m.faces.nbytes + m.cubes.nbytes + (m.colors.nbytes if m.colors is not None else 0)
+    out["e2e"] = {"value": world * samples * reps / secs, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                  "d2h_bytes_per_step": int(d2h), "call": f"tg_export_mesh_surrogate ({best_mode}), host mesh out"}
+    sur.close()
+    return out
 
 
 def our_arm(args, rank, world, local_rank):
@@ -302,7 +368,7 @@ def our_arm(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     kernels = {}
-    for name in ("classify_bricks", "eval_bricks", "cell_flags", "scan", "cell_vertices", "faces", "attributes"):
+    for name in ("classify_bricks", "list_bricks", "eval_bricks", "cell_flags", "scan", "cell_vertices", "faces", "attributes"):
         ms, n = sdf.profile_read(name)
         kernels[name] = {"ms_per_step": ms / args.steps, "launches": n}
     vertex_count, face_count = int(dm.vertex_count), int(dm.face_count)
@@ -324,9 +390,14 @@ def our_arm(args, rank, world, local_rank):
     eval_grid_ms = sdf.profile_read("eval_grid")[0] / args.steps
 
     value = world * samples * args.steps / (total_ms * 1e-3)
-    # Launches of our kernels per step: classify, eval bricks, flags, scan (3), vertices,
-    # scan (3), faces, attributes.
-    launches_per_step = 12
+    # Launches of our kernels per step: classify, brick list (scan 3 + compaction), eval
+    # bricks, cell flags, scan (3), vertices, scan (3), faces, attributes.
+    launches_per_step = 16
+
+    # The surrogate-culled form: the network trained on this tree decides which bricks to
+    # skip (alone, or followed by the exact test); same mesh required.
+    surrogate = None if args.skip_surrogate else surrogate_leg(prog, grid, samples, args, stream, sp, flush, total_ms, dense_ms,
+                                                                world)
 
     # End to end through the C ABI: tree handle in, host mesh out, every step.
     e2e_steps = 0 if args.skip_e2e else max(3, min(args.steps, 10))
@@ -403,6 +474,7 @@ def our_arm(args, rank, world, local_rank):
             "meshes_per_s": world * args.steps / (total_ms * 1e-3),
             "bricks": {"size_cells": 7, "total": bricks, "evaluated": active_bricks,
                        "evaluated_fraction": active_bricks / max(1, bricks)},
+            "surrogate_culled": surrogate,
             "dense_export": {"value": world * samples * args.steps / (dense_ms * 1e-3), "unit": "samples/s",
                              "ms_per_step": dense_ms / args.steps, "eval_grid_ms": eval_grid_ms,
                              "note": "every lattice point evaluated (the reference's work); identical mesh"},
@@ -420,6 +492,167 @@ def our_arm(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def render_arm(args, rank, world, local_rank):
+    """Sphere-traced depth + normal + colour, 64 seeded poses at radius 4 around a
+    1024-primitive tree, 1920x1080, 256 steps, epsilon 1e-4, 60 degree vertical FOV."""
+    import torch
+    from tangerine_gb300 import build as B
+    B.build()
+    from tangerine_gb300 import _lib, sdf
+    from tangerine_gb300 import workloads as W
+    torch.cuda.set_device(local_rank)
+    width, height, poses_n, steps, eps = 1920, 1080, 64, 256, 1e-4
+    spec = W.random_tree(5, 1024)
+    tree = sdf.from_spec(spec)
+    prog = sdf.compile(tree)
+    poses = W.camera_poses(5, poses_n, radius=4.0)
+    cams = sdf.cameras(poses, fov_y_degrees=60.0)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    px = width * height
+    depth = torch.empty(poses_n * px, dtype=torch.float32, device="cuda")
+    normals = torch.empty(poses_n * px * 3, dtype=torch.float32, device="cuda")
+    colors = torch.empty(poses_n * px * 3, dtype=torch.uint8, device="cuda")
+
+    def render(count, exact, cam_array):
+        _lib.check(lib.tg_render(prog.ptr, cam_array, count, width, height, steps, eps, 1 if exact else 0,
+                                 _lib.C.c_void_p(depth.data_ptr()), _lib.C.c_void_p(normals.data_ptr()),
+                                 _lib.C.c_void_p(colors.data_ptr()), 1, _lib.C.c_void_p(sp)), "tg_render")
+
+    for _ in range(args.warmup):
+        render(4, False, cams)
+    sdf.profile_reset()
+    sdf.profile_enable(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        render(poses_n, False, cams)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sdf.profile_enable(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    hits = float(torch.isfinite(depth).float().mean().item())
+    rays = poses_n * px
+    # Exact (reference step sequence on the whole tree) on two poses.
+    exact_cams = sdf.cameras(poses[:2], fov_y_degrees=60.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    render(2, True, exact_cams)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    exact_rays_s = 2 * px / (e0.elapsed_time(e1) * 1e-3)
+    # End to end: host buffers, all poses.
+    hd = np.empty(rays, np.float32)
+    hn = np.empty(rays * 3, np.float32)
+    hc = np.empty(rays * 3, np.uint8)
+    t = time.perf_counter()
+    _lib.check(lib.tg_render(prog.ptr, cams, poses_n, width, height, steps, eps, 0, _lib.as_ptr(hd), _lib.as_ptr(hn),
+                             _lib.as_ptr(hc), 0, _lib.C.c_void_p(sp)), "tg_render")
+    e2e_s = time.perf_counter() - t
+    cpu = None
+    if not args.skip_cpu:
+        from oracle import oracle as O
+        port = O.port()
+        h = port.build(spec)
+        try:
+            stride = 997
+            o, d = W.camera_rays(poses[0], width, height, cams[0].tan_half_fov)
+            idx = np.arange(px)[::stride]
+            o, d = np.ascontiguousarray(o[idx]), np.ascontiguousarray(d[idx])
+            t = time.perf_counter()
+            hit, travel, pos = port.raymarch(h, o, d, steps, eps, threads=0)
+            if hit.any():
+                port.gradient(h, pos[hit])
+                port.color(h, pos[hit])
+            secs = time.perf_counter() - t
+            cpu = {"value": len(idx) / secs, "unit": "rays/s", "cores": port.hardware_threads(), "kind": "port",
+                   "sample": f"every {stride}th pixel of pose 0 ({len(idx)} rays, {secs:.1f} s): SDFNode::RayMarch + "
+                             f"Gradient + GetMaterial on the whole tree, C restatement"}
+        finally:
+            port.free(h)
+    line = {"metric": "rays/s: sphere-traced depth+normal+colour (1024-primitive tree, 64 poses, 1920x1080)",
+            "value": rays / (ms * 1e-3), "unit": "rays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "render: seeded 1024-primitive tree (seed 5), 64 seeded poses on a radius-4 sphere, "
+                                   "1920x1080, 60 deg vertical FOV, 256 steps, epsilon 1e-4, octree-bounded steps",
+                       "hit_fraction": hits},
+            "exact_rays_per_s": exact_rays_s,
+            "e2e": {"value": rays / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": rays * 19},
+            "cpu_baseline": cpu, "gpu_launches": args.steps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    prog.close()
+
+
+def surrogate_arm(args, rank, world, local_rank):
+    """The 256-primitive tree on a 1024^3 grid in 32^3 bricks: dense exact, exact-culled and
+    surrogate-culled exports (same mesh), samples/s."""
+    import torch
+    from tangerine_gb300 import build as B
+    B.build()
+    from tangerine_gb300 import sdf
+    from tangerine_gb300 import workloads as W
+    torch.cuda.set_device(local_rank)
+    res, brick = 1024, 32
+    spec = W.random_tree(SEED, PRIMS)
+    grid = W.export_grid(resolution=res)
+    samples = grid.corners
+    prog = sdf.compile(sdf.from_spec(spec))
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            st[i].record(stream)
+            fn()
+            en[i].record(stream)
+        torch.cuda.synchronize()
+        return float(np.sum([a.elapsed_time(b) for a, b in zip(st, en)]))
+
+    dense_ms = timed(lambda: prog.export_mesh_device(grid, dense=True, stream=sp))
+    exact_ms = timed(lambda: prog.export_mesh_device(grid, brick=brick, stream=sp))
+    _, exact_kept = sdf.last_export_stats()
+    with ClockSampler(None) as clocks:
+        sur = surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_ms, world, brick=brick)
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cb = cpu_baseline(spec, grid)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    best_mode = max(sur["modes"], key=lambda k: sur["modes"][k]["value"])
+    best = sur["modes"][best_mode]
+    ms = best["ms_per_step"]
+    line = {"metric": f"samples/s: surrogate-culled export, {PRIMS}-primitive tree, {res}^3 grid in {brick}^3 bricks (same mesh)",
+            "value": best["value"], "unit": "samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"seeded {PRIMS}-primitive tree (seed {SEED}), {res}^3 grid over [-2,2]^3 "
+                                   f"({res + 3}^3 lattice samples) in {brick}^3-cell bricks; network: 16-level hash grid "
+                                   f"+ 3x64 BF16 layers trained on 2^22 exact samples (half uniform, half |d|<0.05); "
+                                   f"mode: {best_mode}",
+                       "l2": "flushed between steps"},
+            "meshes_per_s": 1e3 / ms,
+            "exact_culled": {"value": world * samples * args.steps / (exact_ms * 1e-3), "ms_per_step": exact_ms / args.steps,
+                             "bricks_evaluated": exact_kept},
+            "dense_exact": {"value": world * samples * args.steps / (dense_ms * 1e-3), "ms_per_step": dense_ms / args.steps},
+            "surrogate": sur, "cpu_baseline": cpu,
+            "e2e": sur["e2e"], "gpu_launches": (16 if best_mode == "network alone" else 21) * args.steps,
+            "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    prog.close()
+
+
 def main():
     global RES, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -429,6 +662,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate"],
+                    help="export: the 512^3 mesh export (the benchmark); render: the sphere-tracing workload; "
+                         "surrogate: the 1024^3 export in 32^3 bricks with the learned bound")
+    ap.add_argument("--skip-surrogate", action="store_true", help="skip the surrogate-culled leg of the export")
     ap.add_argument("--resolution", type=int, default=RES,
                     help="grid resolution (512 is the benchmark; smaller values are profiling cases)")
     args = ap.parse_args()
@@ -440,6 +677,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         reference_arm(args, rank)
+    elif args.workload == "render":
+        render_arm(args, rank, world, local_rank)
+    elif args.workload == "surrogate":
+        surrogate_arm(args, rank, world, local_rank)
     else:
         our_arm(args, rank, world, local_rank)
 

@@ -164,7 +164,7 @@ enum
 	TG_MESH_DENSE = 2u,         /* evaluate every lattice point, as the reference does; by
 	                               default bricks that provably hold no surface are skipped
 	                               (same mesh, bit for bit) */
-	/* bits 8..15: brick edge in cells for the culled export (1..15; 0 = 7)
+	/* bits 8..15: brick edge in cells for the culled export (1..32; 0 = 7)
 	   bits 16..19: lattice points per thread sharing one pass over the records (1, 2, 4;
 	   0 = 2 culled, 4 dense) */
 };
@@ -290,6 +290,95 @@ TANGERINE_API void tg_profile_reset(void);
 /* Measures this GPU's FP32 fused-multiply-add throughput in TFLOP/s (2 flops per FMA):
  * the compute roofline of the distance interpreter. */
 TANGERINE_API tg_status tg_measure_fp32_peak(double* tflops, void* stream);
+
+/* ---- learned distance bound ---------------------------------------------------------
+ * No counterpart in the reference.  A per-tree network -- a 16-level hash grid (2 features
+ * per level) feeding 3 hidden ReLU layers of 64, BF16 weights on the tensor cores with FP32
+ * accumulation -- trained on the GPU by this library's own forward, backward and Adam
+ * kernels on distances of the whole tree (SDFNode::Eval).  It bounds the distance for
+ * brick culling: a brick is skipped only when |net(centre)| exceeds the brick's ball radius
+ * plus a margin (safety x the largest error seen on held-out samples), and every kept
+ * brick is evaluated exactly, so the exact program decides every sign.  Trees with a
+ * non-1-Lipschitz brush (ellipsoid) are never culled by it. */
+typedef struct tg_surrogate tg_surrogate;
+
+typedef struct tg_surrogate_options
+{
+	int log2_table;             /* entries per level = 2^log2_table (default 18) */
+	int base_resolution;        /* cells per axis, coarsest level (16) */
+	int max_resolution;         /* finest level (1024) */
+	float domain_min[3];        /* box the grid covers ([-2, 2]^3) */
+	float domain_max[3];
+	float clamp;                /* the network approximates clamp(d, -clamp, clamp) (0.5) */
+	int64_t samples;            /* training samples, half uniform, half |d| < band (2^22) */
+	float band;                 /* (0.05) */
+	int64_t batch;              /* samples per Adam step (2^18) */
+	int steps;                  /* Adam steps (2000) */
+	float learning_rate;        /* (1e-2, decaying to 1e-3 over the second half) */
+	int64_t validation;         /* held-out samples, same mix (2^20) */
+	float safety;               /* margin = safety x max held-out error (2) */
+	uint64_t seed;
+} tg_surrogate_options;
+
+typedef struct tg_surrogate_info
+{
+	float max_error, p99_error, mean_error;   /* held-out |net - clamp(d)| */
+	float margin;                             /* safety x max_error (tg_surrogate_margin gives the one used) */
+	float final_loss;                         /* mean squared error of the last batch */
+	double data_seconds, train_seconds;
+	int64_t samples;
+	int steps;
+	int resolutions[16];
+	uint32_t table_size;
+	uint32_t dense_levels;                    /* bit l: level l indexed densely */
+	int64_t table_floats;                     /* 16 x table_size x 2 */
+	int64_t mlp_floats;                       /* 10497: W1[64][32] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4 */
+} tg_surrogate_info;
+
+TANGERINE_API void tg_surrogate_default_options(tg_surrogate_options* out);
+/* Allocates the network on the current device with seeded initial parameters. */
+TANGERINE_API tg_status tg_surrogate_create(const tg_surrogate_options* options, tg_surrogate** out);
+TANGERINE_API void tg_surrogate_free(tg_surrogate* s);
+/* Builds the training set from the program's whole tree, trains, measures the held-out
+ * error and sets the margin. */
+TANGERINE_API tg_status tg_surrogate_fit(tg_surrogate* s, tg_program* program, void* stream);
+TANGERINE_API tg_status tg_surrogate_get_info(const tg_surrogate* s, tg_surrogate_info* out);
+/* Parameters as FP32 host arrays (table: level-major, entry-major, 2 features). */
+TANGERINE_API tg_status tg_surrogate_get_params(tg_surrogate* s, float* table, float* mlp);
+TANGERINE_API tg_status tg_surrogate_set_params(tg_surrogate* s, const float* table, const float* mlp);
+/* Network output at n points (3 floats each); host arrays, or device when io_is_device. */
+TANGERINE_API tg_status tg_surrogate_eval(tg_surrogate* s, const float* points, int64_t n, float* out, int io_is_device,
+                                          void* stream);
+/* Gradients of the mean squared error against clamp(d) over n samples (x, y, z, d; host
+ * arrays), into host arrays shaped like the parameters; *loss = sum of squared errors. */
+TANGERINE_API tg_status tg_surrogate_gradients(tg_surrogate* s, const float* samples, int64_t n, float* table_grad,
+                                               float* mlp_grad, float* loss);
+/* `steps` Adam steps over consecutive batches of the given samples (host x, y, z, d). */
+TANGERINE_API tg_status tg_surrogate_train(tg_surrogate* s, const float* samples, int64_t n, int steps, void* stream);
+/* Margin of the brick test |net(centre)| > r + margin for bricks whose ball has radius r.
+ * The test is wrong only for a centre with |d| <= r where the network says more than
+ * r + margin, so it comes from the held-out samples with |clamp(d)| <= r:
+ * safety x max(their largest |net| - r, the held-out p99 error). */
+TANGERINE_API tg_status tg_surrogate_margin(const tg_surrogate* s, float radius, float* margin);
+/* Fixes the margin of the culled export for every brick size (negative: back to the
+ * held-out calibration above). */
+TANGERINE_API tg_status tg_surrogate_set_margin(tg_surrogate* s, float margin);
+/* tg_export_mesh / tg_export_mesh_device with the network deciding which bricks to skip:
+ * a brick it does not rule out also takes the exact brick test (the network saves that
+ * test's cost on the bricks it rules out), unless TG_MESH_SURROGATE_ONLY is set. */
+enum
+{
+	TG_MESH_SURROGATE_ONLY = 1u << 20,
+};
+TANGERINE_API tg_status tg_export_mesh_surrogate(tg_program* program, tg_surrogate* s, const tg_grid* grid, uint32_t flags,
+                                                 tg_mesh* out, void* stream);
+TANGERINE_API tg_status tg_export_mesh_surrogate_device(tg_program* program, tg_surrogate* s, const tg_grid* grid,
+                                                        uint32_t flags, tg_device_mesh* out, void* stream);
+/* Check of the tensor-core operand layouts: D = A B^T through the descriptors the network
+ * kernels use (mode 0: a 128x64, b 64x64, both K-major, D 128x64; mode 1: D = a^T b for
+ * a 128x128, b 128x144, D 128x144; mode 2: D = a b for a 128x64, b 64x64, D 128x64).
+ * Host FP32 arrays, inputs rounded to BF16. */
+TANGERINE_API tg_status tg_debug_mma(int mode, const float* a, const float* b, float* d);
 
 TANGERINE_API const char* tg_last_error(void);
 TANGERINE_API const char* tg_version(void);

@@ -47,6 +47,20 @@ class DeviceMesh(C.Structure):
                 ("faces", C.c_void_p), ("cubes", C.c_void_p)]
 
 
+class SurrogateOptions(C.Structure):
+    _fields_ = [("log2_table", C.c_int), ("base_resolution", C.c_int), ("max_resolution", C.c_int),
+                ("domain_min", C.c_float * 3), ("domain_max", C.c_float * 3), ("clamp", C.c_float),
+                ("samples", C.c_int64), ("band", C.c_float), ("batch", C.c_int64), ("steps", C.c_int),
+                ("learning_rate", C.c_float), ("validation", C.c_int64), ("safety", C.c_float), ("seed", C.c_uint64)]
+
+
+class SurrogateInfo(C.Structure):
+    _fields_ = [("max_error", C.c_float), ("p99_error", C.c_float), ("mean_error", C.c_float), ("margin", C.c_float),
+                ("final_loss", C.c_float), ("data_seconds", C.c_double), ("train_seconds", C.c_double),
+                ("samples", C.c_int64), ("steps", C.c_int), ("resolutions", C.c_int * 16), ("table_size", C.c_uint32),
+                ("dense_levels", C.c_uint32), ("table_floats", C.c_int64), ("mlp_floats", C.c_int64)]
+
+
 # Every exported symbol with its signature: (restype, argtypes).
 _vp, _f, _i, _i64, _u32 = C.c_void_p, C.c_float, C.c_int, C.c_int64, C.c_uint32
 SIGNATURES = {
@@ -103,6 +117,21 @@ SIGNATURES = {
     "tg_profile_read": (_i, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "tg_profile_reset": (None, []),
     "tg_measure_fp32_peak": (_i, [C.POINTER(C.c_double), _vp]),
+    "tg_surrogate_default_options": (None, [C.POINTER(SurrogateOptions)]),
+    "tg_surrogate_create": (_i, [C.POINTER(SurrogateOptions), C.POINTER(_vp)]),
+    "tg_surrogate_free": (None, [_vp]),
+    "tg_surrogate_fit": (_i, [_vp, _vp, _vp]),
+    "tg_surrogate_get_info": (_i, [_vp, C.POINTER(SurrogateInfo)]),
+    "tg_surrogate_get_params": (_i, [_vp, _vp, _vp]),
+    "tg_surrogate_set_params": (_i, [_vp, _vp, _vp]),
+    "tg_surrogate_eval": (_i, [_vp, _vp, _i64, _vp, _i, _vp]),
+    "tg_surrogate_gradients": (_i, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "tg_surrogate_train": (_i, [_vp, _vp, _i64, _i, _vp]),
+    "tg_surrogate_set_margin": (_i, [_vp, _f]),
+    "tg_surrogate_margin": (_i, [_vp, _f, C.POINTER(_f)]),
+    "tg_export_mesh_surrogate": (_i, [_vp, _vp, C.POINTER(Grid), _u32, C.POINTER(HostMesh), _vp]),
+    "tg_export_mesh_surrogate_device": (_i, [_vp, _vp, C.POINTER(Grid), _u32, C.POINTER(DeviceMesh), _vp]),
+    "tg_debug_mma": (_i, [_i, _vp, _vp, _vp]),
     "tg_last_error": (C.c_char_p, []),
     "tg_version": (C.c_char_p, []),
 }

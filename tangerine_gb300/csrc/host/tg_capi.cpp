@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "tg_engine.hpp"
+#include "tg_surrogate.hpp"
 #include "tg_octree.hpp"
 #include "tg_tree.hpp"
 
@@ -333,7 +334,7 @@ extern "C"
 		Engine& eng = Engine::Get();
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		DeviceMesh dm;
-		if (((flags >> 8) & 0xFFu) > 15) { SetError("brick size must be 1..15 cells"); return TG_ERR_INVALID; }
+		if (((flags >> 8) & 0xFFu) > 32) { SetError("brick size must be 1..32 cells"); return TG_ERR_INVALID; }
 		cudaError_t e = eng.Export(*p, gs, OptionsOf(flags), dm, StreamOf(stream));
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
 		out->vertex_count = dm.VertexCount;
@@ -355,7 +356,7 @@ extern "C"
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		const cudaStream_t s = StreamOf(stream);
 		DeviceMesh dm;
-		if (((flags >> 8) & 0xFFu) > 15) { SetError("brick size must be 1..15 cells"); return TG_ERR_INVALID; }
+		if (((flags >> 8) & 0xFFu) > 32) { SetError("brick size must be 1..32 cells"); return TG_ERR_INVALID; }
 		cudaError_t e = eng.Export(*p, gs, OptionsOf(flags), dm, s);
 		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
 		return CopyMeshToHost(dm, out, s);
@@ -608,6 +609,270 @@ extern "C"
 		std::lock_guard<std::mutex> lock(Engine::Get().Mutex);
 		cudaError_t e = MeasureFp32Peak(tflops, StreamOf(stream));
 		if (e != cudaSuccess) return CudaFail(e, "measuring FP32 throughput");
+		return TG_OK;
+	}
+
+	// ---- learned distance bound ---------------------------------------------------------
+
+	TANGERINE_API void tg_surrogate_default_options(tg_surrogate_options* o)
+	{
+		if (!o) return;
+		const FieldOptions d;
+		o->log2_table = d.Log2Table;
+		o->base_resolution = d.BaseRes;
+		o->max_resolution = d.MaxRes;
+		for (int a = 0; a < 3; ++a) { o->domain_min[a] = d.Lo[a]; o->domain_max[a] = d.Hi[a]; }
+		o->clamp = d.Clamp;
+		o->samples = d.Samples;
+		o->band = d.Band;
+		o->batch = d.Batch;
+		o->steps = d.Steps;
+		o->learning_rate = d.Rate;
+		o->validation = d.Validation;
+		o->safety = d.Safety;
+		o->seed = d.Seed;
+	}
+
+	TANGERINE_API tg_status tg_surrogate_create(const tg_surrogate_options* o, tg_surrogate** out)
+	{
+		if (!out) { SetError("null argument"); return TG_ERR_INVALID; }
+		*out = nullptr;
+		tg_surrogate_options def;
+		tg_surrogate_default_options(&def);
+		if (!o) o = &def;
+		if (o->log2_table < 10 || o->log2_table > 24 || o->base_resolution < 1 || o->max_resolution < o->base_resolution ||
+			o->max_resolution > (1 << 20) || !(o->clamp > 0.0f) || o->samples < 2 || o->batch < 1 || o->steps < 0 ||
+			o->validation < 2 || !(o->safety >= 0.0f) || !(o->band > 0.0f))
+		{
+			SetError("invalid surrogate options");
+			return TG_ERR_INVALID;
+		}
+		FieldOptions f;
+		f.Log2Table = o->log2_table;
+		f.BaseRes = o->base_resolution;
+		f.MaxRes = o->max_resolution;
+		for (int a = 0; a < 3; ++a)
+		{
+			if (!(o->domain_max[a] > o->domain_min[a])) { SetError("empty surrogate domain"); return TG_ERR_INVALID; }
+			f.Lo[a] = o->domain_min[a];
+			f.Hi[a] = o->domain_max[a];
+		}
+		f.Clamp = o->clamp;
+		f.Samples = o->samples;
+		f.Band = o->band;
+		f.Batch = o->batch;
+		f.Steps = o->steps;
+		f.Rate = o->learning_rate;
+		f.Validation = o->validation;
+		f.Safety = o->safety;
+		f.Seed = o->seed;
+		std::unique_ptr<tg_surrogate> s(new (std::nothrow) tg_surrogate(f));
+		if (!s) { SetError("out of host memory"); return TG_ERR_MEMORY; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = s->Init(eng.DefaultStream());
+		if (e != cudaSuccess) return CudaFail(e, "allocating the surrogate");
+		*out = s.release();
+		return TG_OK;
+	}
+
+	TANGERINE_API void tg_surrogate_free(tg_surrogate* s) { delete s; }
+
+	TANGERINE_API tg_status tg_surrogate_fit(tg_surrogate* s, tg_program* p, void* stream)
+	{
+		if (!s || !p) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = s->Fit(*p, StreamOf(stream));
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		if (e != cudaSuccess) return CudaFail(e, "training the surrogate");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_surrogate_get_info(const tg_surrogate* s, tg_surrogate_info* out)
+	{
+		if (!s || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::memset(out, 0, sizeof *out);
+		out->max_error = s->Info.MaxError;
+		out->p99_error = s->Info.P99Error;
+		out->mean_error = s->Info.MeanError;
+		out->margin = s->Info.Margin;
+		out->final_loss = s->Info.FinalLoss;
+		out->data_seconds = s->Info.DataSeconds;
+		out->train_seconds = s->Info.TrainSeconds;
+		out->samples = s->Info.Samples;
+		out->steps = s->Info.Steps;
+		for (int l = 0; l < kFieldLevels; ++l) out->resolutions[l] = s->Grid.Res[l];
+		out->table_size = s->Grid.TableSize;
+		out->dense_levels = s->Grid.DenseLevels;
+		out->table_floats = s->TableFloats;
+		out->mlp_floats = kFieldParams;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_surrogate_get_params(tg_surrogate* s, float* table, float* mlp)
+	{
+		if (!s) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = s->GetParams(table, mlp, eng.DefaultStream());
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "reading surrogate parameters");
+	}
+
+	TANGERINE_API tg_status tg_surrogate_set_params(tg_surrogate* s, const float* table, const float* mlp)
+	{
+		if (!s) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = s->SetParams(table, mlp, eng.DefaultStream());
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "writing surrogate parameters");
+	}
+
+	TANGERINE_API tg_status tg_surrogate_eval(tg_surrogate* s, const float* points, int64_t n, float* out, int io_is_device, void* stream)
+	{
+		if (!s || (n > 0 && (!points || !out)) || n < 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (n == 0) return TG_OK;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = StreamOf(stream);
+		cudaError_t e = cudaSuccess;
+		if (io_is_device) e = s->Eval(points, n, 3, out, st);
+		else
+		{
+			DeviceBuffer dp, dout;
+			e = dp.Reserve((size_t)n * 12);
+			if (e == cudaSuccess) e = dout.Reserve((size_t)n * 4);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(dp.Ptr, points, (size_t)n * 12, cudaMemcpyHostToDevice, st);
+			if (e == cudaSuccess) e = s->Eval(dp.As<float>(), n, 3, dout.As<float>(), st);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.Ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+			dp.Release();
+			dout.Release();
+		}
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "evaluating the surrogate");
+	}
+
+	TANGERINE_API tg_status tg_surrogate_gradients(tg_surrogate* s, const float* samples, int64_t n, float* table_grad, float* mlp_grad,
+		float* loss)
+	{
+		if (!s || !samples || n <= 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = eng.DefaultStream();
+		DeviceBuffer d;
+		cudaError_t e = d.Reserve((size_t)n * 16);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(d.Ptr, samples, (size_t)n * 16, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess) e = s->Gradients(d.As<float4>(), n, table_grad, mlp_grad, loss, st);
+		d.Release();
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "surrogate gradients");
+	}
+
+	TANGERINE_API tg_status tg_surrogate_train(tg_surrogate* s, const float* samples, int64_t n, int steps, void* stream)
+	{
+		if (!s || !samples || n <= 0 || steps < 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = StreamOf(stream);
+		DeviceBuffer d;
+		cudaError_t e = d.Reserve((size_t)n * 16);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(d.Ptr, samples, (size_t)n * 16, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess) e = s->Train(d.As<float4>(), n, steps, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		d.Release();
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "training the surrogate");
+	}
+
+	TANGERINE_API tg_status tg_surrogate_margin(const tg_surrogate* s, float radius, float* margin)
+	{
+		if (!s || !margin) { SetError("null argument"); return TG_ERR_INVALID; }
+		*margin = s->MarginFor(radius);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_surrogate_set_margin(tg_surrogate* s, float margin)
+	{
+		if (!s || margin != margin) { SetError("invalid argument"); return TG_ERR_INVALID; }
+		s->Info.MarginOverride = margin >= 0.0f ? margin : -1.0f;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_export_mesh_surrogate_device(tg_program* p, tg_surrogate* sur, const tg_grid* g, uint32_t flags,
+		tg_device_mesh* out, void* stream)
+	{
+		if (!p || !sur || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (flags & TG_MESH_DENSE) { SetError("the surrogate export culls bricks: TG_MESH_DENSE does not apply"); return TG_ERR_INVALID; }
+		GridSpec gs;
+		if (!ToGridSpec(g, gs)) return TG_ERR_INVALID;
+		if (((flags >> 8) & 0xFFu) > 32) { SetError("brick size must be 1..32 cells"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		ExportOptions opt = OptionsOf(flags);
+		opt.Field = sur;
+		opt.Refine = (flags & TG_MESH_SURROGATE_ONLY) == 0;
+		DeviceMesh dm;
+		cudaError_t e = eng.Export(*p, gs, opt, dm, StreamOf(stream));
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		out->vertex_count = dm.VertexCount;
+		out->face_count = dm.FaceCount;
+		out->vertices = dm.Vertices;
+		out->normals = dm.Normals;
+		out->colors = dm.Colors;
+		out->faces = dm.Faces;
+		out->cubes = dm.Cubes;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_export_mesh_surrogate(tg_program* p, tg_surrogate* sur, const tg_grid* g, uint32_t flags, tg_mesh* out,
+		void* stream)
+	{
+		if (!p || !sur || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (flags & TG_MESH_DENSE) { SetError("the surrogate export culls bricks: TG_MESH_DENSE does not apply"); return TG_ERR_INVALID; }
+		GridSpec gs;
+		if (!ToGridSpec(g, gs)) return TG_ERR_INVALID;
+		if (((flags >> 8) & 0xFFu) > 32) { SetError("brick size must be 1..32 cells"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t s = StreamOf(stream);
+		ExportOptions opt = OptionsOf(flags);
+		opt.Field = sur;
+		opt.Refine = (flags & TG_MESH_SURROGATE_ONLY) == 0;
+		DeviceMesh dm;
+		cudaError_t e = eng.Export(*p, gs, opt, dm, s);
+		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
+		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		return CopyMeshToHost(dm, out, s);
+	}
+
+	TANGERINE_API tg_status tg_debug_mma(int mode, const float* a, const float* b, float* d)
+	{
+		if (!a || !b || !d || mode < 0 || mode > 2) { SetError("invalid argument"); return TG_ERR_INVALID; }
+		const size_t na = mode == 1 ? 128 * 128 : 128 * 64;
+		const size_t nb = mode == 1 ? 128 * 144 : 64 * 64;
+		const size_t nd = mode == 1 ? 128 * 144 : 128 * 64;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = eng.DefaultStream();
+		DeviceBuffer da, db, dd, ds;
+		cudaError_t e = da.Reserve(na * 4);
+		if (e == cudaSuccess) e = db.Reserve(nb * 4);
+		if (e == cudaSuccess) e = dd.Reserve(nd * 4);
+		if (e == cudaSuccess) e = ds.Reserve(4);
+		if (e == cudaSuccess) e = cudaMemsetAsync(ds.Ptr, 0, 4, st);
+		if (e == cudaSuccess) e = cudaMemsetAsync(dd.Ptr, 0, nd * 4, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(da.Ptr, a, na * 4, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(db.Ptr, b, nb * 4, cudaMemcpyHostToDevice, st);
+		if (e == cudaSuccess) e = LaunchDebugMma(mode, da.As<float>(), db.As<float>(), dd.As<float>(), ds.As<int>(), st);
+		int status = 0;
+		if (e == cudaSuccess) e = cudaMemcpyAsync(d, dd.Ptr, nd * 4, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(&status, ds.Ptr, 4, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		da.Release(); db.Release(); dd.Release(); ds.Release();
+		if (e != cudaSuccess) return CudaFail(e, "tensor-core layout check");
+		if (status) { SetError("a tensor-core wait timed out"); return TG_ERR_CUDA; }
 		return TG_OK;
 	}
 

@@ -1,5 +1,6 @@
 // GPU engine: device buffers, the export pipeline and the kernel profiler.
 #include "tg_engine.hpp"
+#include "tg_surrogate.hpp"
 
 #include <cstring>
 
@@ -313,8 +314,33 @@ namespace tg
 				PersistentBlocks = sms * 8;
 			}
 			uint32_t* brickCount = Counts.As<uint32_t>() + 2;
-			Begin("classify_bricks", s);
-			TG_TRY(LaunchClassifyBricks(p.View, g, B, BrickBits.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
+			uint32_t* bits = BrickBits.As<uint32_t>();
+			if (opt.Field)
+			{
+				// Ball radius of a whole brick: half its diagonal.
+				const float radius = 0.8660254f * (float)B * g.Step;
+				Begin("classify_field", s);
+				TG_TRY(LaunchFieldClassifyBricks(p.View, g, B, opt.Field->Grid, opt.Field->TablePtr(), opt.Field->ImagePtr(),
+					opt.Field->MarginFor(radius), bits, opt.Field->StatusPtr(), s));
+				End(s);
+				if (opt.Refine)
+				{
+					Begin("list_bricks", s);
+					TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
+					End(s);
+					Begin("refine_bricks", s);
+					TG_TRY(LaunchRefineBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, bits, PersistentBlocks, s));
+					End(s);
+				}
+			}
+			else
+			{
+				Begin("classify_bricks", s);
+				TG_TRY(LaunchClassifyBricks(p.View, g, B, bits, s));
+				End(s);
+			}
+			Begin("list_bricks", s);
+			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
 			End(s);
 			Begin("eval_bricks", s);
 			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s,
@@ -390,6 +416,7 @@ namespace tg
 		}
 		TG_TRY(cudaStreamSynchronize(s));
 		Collect();
+		if (opt.Field) TG_TRY(const_cast<FieldNet*>(opt.Field)->CheckStatus(s));
 		return cudaSuccess;
 	}
 

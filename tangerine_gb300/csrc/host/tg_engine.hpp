@@ -15,6 +15,8 @@
 
 namespace tg
 {
+	class FieldNet;
+
 	// A grow-only device allocation.
 	struct DeviceBuffer
 	{
@@ -52,6 +54,8 @@ namespace tg
 		bool Dense = false;         // evaluate every lattice point (no brick culling)
 		int BrickSize = 7;          // cells per brick edge when culling (1..15)
 		int Lanes = 2;              // lattice points per thread sharing one pass over records
+		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
+		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
 	};
 
 	class Engine

@@ -18,6 +18,7 @@
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
 #include "tg_surface.cuh"
+#include "tg_cull.cuh"
 
 namespace tg
 {
@@ -32,79 +33,8 @@ namespace tg
 			int NBX, NBY, NBZ;      // bricks per axis
 		};
 
-		// Whether the lattice box [i0, i1] x [j0, j1] x [k0, k1] (corner indices) may hold a
-		// sign change of the reference's distances; false only when that is proven.
-		__device__ __forceinline__ bool BoxMayHoldSurface(const DeviceProgram& prog, const GridSpec& g,
-			int i0, int i1, int j0, int j1, int k0, int k1, float* spill, int stride)
-		{
-			const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
-			const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
-			const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
-			const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
-			const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);
-			// Ball through the box's corners, widened for the rounding of the centre.
-			const float r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
-			const float rootClip = __ldg(&prog.Nodes[0].ClipRadius);
-			const float margin = 1e-4f * (1.0f + fabsf(cx) + fabsf(cy) + fabsf(cz) + fabsf(rootClip));
-			// Outside the root cube every brush, and so every clipped program, is positive
-			// (the cube holds the tree's bounds): a ball missing the cube has no surface.
-			const float half = fabsf(rootClip) * 0.57736f;           // span / 2 = radius / sqrt(3), rounded up
-			const float ox = fmaxf(fabsf(cx - __ldg(&prog.Nodes[0].Pivot[0])) - half, 0.0f);
-			const float oy = fmaxf(fabsf(cy - __ldg(&prog.Nodes[0].Pivot[1])) - half, 0.0f);
-			const float oz = fmaxf(fabsf(cz - __ldg(&prog.Nodes[0].Pivot[2])) - half, 0.0f);
-			if (sqrtf(ox * ox + oy * oy + oz * oz) > r + margin) return false;
-			// Deepest cell on the centre's descent path whose clip sphere holds the ball.
-			int path[48];
-			int depth = 0;
-			int at = 0;
-			path[depth++] = 0;
-			for (int guard = 0; guard < 47; ++guard)
-			{
-				const OctNode* n = prog.Nodes + at;
-				const int32_t flags = __ldg(&n->Flags);
-				if (flags & kNodeTerminus) break;
-				const float px = __ldg(&n->Pivot[0]), py = __ldg(&n->Pivot[1]), pz = __ldg(&n->Pivot[2]);
-				const int octant = (cx > px ? 1 : 0) | (cy > py ? 2 : 0) | (cz > pz ? 4 : 0);
-				const int child = __ldg(&n->Child[octant]);
-				if (child < 0)
-				{
-					// The octree dropped this octant because its clip returned null: the parent's
-					// program exceeds the octant sphere's radius at its centre, so (1-Lipschitz) it
-					// stays above the margin inside that sphere shrunk by the margin.  The octant
-					// sphere sits inside the parent's, where the parent's program has the tree's
-					// sign.  (Octants dropped because all their own children clipped away prove
-					// only their cube, without margin, and are not used.)
-					const float clip = __ldg(&n->ClipRadius);
-					if (clip > 0.0f && ((flags >> (8 + octant)) & 1))
-					{
-						const float q = clip * 0.28867513f;               // span / 4 = radius / (2 sqrt 3)
-						const float qx = px + ((octant & 1) ? q : -q), qy = py + ((octant & 2) ? q : -q), qz = pz + ((octant & 4) ? q : -q);
-						const float dx = cx - qx, dy = cy - qy, dz = cz - qz;
-						if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip * 0.4999f) return false;
-					}
-					break;
-				}
-				at = child;
-				path[depth++] = at;
-			}
-			int holder = -1;
-			for (int d = depth - 1; d >= 0; --d)
-			{
-				const OctNode* n = prog.Nodes + path[d];
-				const float clip = __ldg(&n->ClipRadius);
-				if (clip < 0.0f) break;                           // not 1-Lipschitz here or above
-				const float dx = cx - __ldg(&n->Pivot[0]), dy = cy - __ldg(&n->Pivot[1]), dz = cz - __ldg(&n->Pivot[2]);
-				if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip) { holder = path[d]; break; }
-			}
-			if (holder < 0) return true;
-			const float px[1] = { cx }, py[1] = { cy }, pz[1] = { cz };
-			float f[1];
-			RunDistance<1>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill, stride);
-			return !(fabsf(f[0]) > r + margin);
-		}
-
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ list, uint32_t* __restrict__ count)
+			uint32_t* __restrict__ brick_bits)
 		{
 			extern __shared__ float spill[];
 			const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
@@ -119,12 +49,43 @@ namespace tg
 					spill + threadIdx.x, kClassifyThreads);
 			}
 			const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
-			const int lane = threadIdx.x & 31;
-			if (lane == 0 && b < nb) brick_bits[b >> 5] = ballot;
-			uint32_t base = 0;
-			if (lane == 0 && ballot) base = atomicAdd(count, (uint32_t)__popc(ballot));
-			base = __shfl_sync(0xFFFFFFFFu, base, 0);
-			if (active) list[base + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)b;
+			if ((threadIdx.x & 31) == 0 && b < nb) brick_bits[b >> 5] = ballot;
+		}
+
+		// The exact test on a list of candidate bricks; survivors set their bit.
+		__global__ void __launch_bounds__(kClassifyThreads) RefineBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ brick_bits)
+		{
+			extern __shared__ float spill[];
+			const uint32_t n = *count;
+			for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+			{
+				const uint32_t b = __ldg(list + t);
+				const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
+				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
+				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
+				if (BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, g.NX - 1), j0, min(j0 + bg.B, g.NY - 1), k0, min(k0 + bg.B, g.NZ - 1),
+					spill + threadIdx.x, kClassifyThreads))
+					atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
+			}
+		}
+
+		// Bricks whose bit is set, in brick-index order (x fastest): consecutive list entries
+		// are neighbours, so the CTAs evaluating them at the same time share octree cells and
+		// their record streams in cache.
+		__global__ void ListBricksKernel(const uint32_t* __restrict__ bits, int64_t words, const uint32_t* __restrict__ base,
+			uint32_t* __restrict__ list)
+		{
+			const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+			if (w >= words) return;
+			uint32_t m = bits[w];
+			uint32_t at = base[w];
+			while (m)
+			{
+				const int j = __ffs(m) - 1;
+				m &= m - 1u;
+				list[at++] = (uint32_t)(w * 32 + j);
+			}
 		}
 
 		// Lattice points of every listed brick: corners [i0, i0 + B] per axis, clamped to the
@@ -321,18 +282,41 @@ namespace tg
 		return (int64_t)bg.NBX * bg.NBY * bg.NBZ;
 	}
 
-	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, uint32_t* list,
-		uint32_t* count, cudaStream_t stream)
+	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream)
 	{
 		const BrickGrid bg = MakeBrickGrid(g, B);
 		const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
-		cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), stream);
-		if (e != cudaSuccess) return e;
+		if (nb <= 0) return cudaSuccess;
 		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 		const size_t smem = (size_t)depth * kClassifyThreads * sizeof(float);
 		if (smem > 48 * 1024) cudaFuncSetAttribute(ClassifyBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		ClassifyBricksKernel<<<(unsigned)((nb + kClassifyThreads - 1) / kClassifyThreads), kClassifyThreads, smem, stream>>>(
-			prog, g, bg, brick_bits, list, count);
+			prog, g, bg, brick_bits);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchRefineBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		uint32_t* brick_bits, int grid_blocks, cudaStream_t stream)
+	{
+		const BrickGrid bg = MakeBrickGrid(g, B);
+		const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
+		cudaError_t e = cudaMemsetAsync(brick_bits, 0, (size_t)((nb + 31) / 32) * 4, stream);
+		if (e != cudaSuccess || nb <= 0) return e;
+		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+		const size_t smem = (size_t)depth * kClassifyThreads * sizeof(float);
+		if (smem > 48 * 1024) cudaFuncSetAttribute(RefineBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		RefineBricksKernel<<<grid_blocks, kClassifyThreads, smem, stream>>>(prog, g, bg, list, count, brick_bits);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
+		uint32_t* count, cudaStream_t stream)
+	{
+		const int64_t words = (bricks + 31) / 32;
+		if (words <= 0) return cudaMemsetAsync(count, 0, 4, stream);
+		cudaError_t e = LaunchExclusiveScan(brick_bits, words, true, base, count, scratch, stream);
+		if (e != cudaSuccess) return e;
+		ListBricksKernel<<<(unsigned)((words + 255) / 256), 256, 0, stream>>>(brick_bits, words, base, list);
 		return cudaGetLastError();
 	}
 
@@ -371,6 +355,8 @@ namespace tg
 	{
 		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
 		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
+		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
+		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
 		return cudaErrorInvalidValue;
 	}
 

@@ -49,9 +49,15 @@ namespace tg
 	cudaError_t LaunchCellFlags(const float* lattice, const GridSpec& grid, uint32_t* words, cudaStream_t stream);
 
 	// Exact brick culling (tg_cull.cu): bricks of B^3 cells that provably hold no sign
-	// change are skipped.  brick_bits: one bit per brick; list/count: surviving bricks.
+	// change are skipped.  brick_bits: one bit per brick (set: may hold surface).
 	int64_t BrickCount(const GridSpec& g, int B);
-	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, uint32_t* list,
+	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream);
+	// The exact test on listed candidate bricks: clears brick_bits, sets survivors' bits.
+	cudaError_t LaunchRefineBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+		uint32_t* brick_bits, int grid_blocks, cudaStream_t stream);
+	// Set bits as a list in brick-index order (scan + compaction); *count (device) gets the
+	// length.  base: (bricks + 31) / 32 words; scratch: ScanScratchWords of that.
+	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
 		uint32_t* count, cudaStream_t stream);
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
 		float* lattice, int grid_blocks, cudaStream_t stream, int lanes = 4);
@@ -93,4 +99,76 @@ namespace tg
 	// Gradient normal and colour bytes per vertex (SDFOctree::Gradient / GetMaterial).
 	cudaError_t LaunchVertexAttributes(const DeviceProgram& prog, const float* vertices, uint32_t vertex_count,
 		float* normals, uint8_t* colors, cudaStream_t stream);
+}
+
+namespace tg
+{
+	// ---- learned distance bound (tg_field.cu) ----------------------------------------
+	// A multiresolution hash grid (16 levels x 2 features) feeds a 32 -> 64 -> 64 -> 64 -> 1
+	// ReLU network whose three hidden layers run as BF16 x BF16 -> FP32 tcgen05 matrix
+	// multiplies; the output layer is an FP32 dot product.
+	constexpr int kFieldLevels = 16;
+	constexpr int kFieldInputs = 2 * kFieldLevels;
+	constexpr int kFieldHidden = 64;
+
+	struct FieldGrid
+	{
+		float Lo[3];                 // domain box corner
+		float Scale[3];              // 1 / domain extent per axis
+		int Res[kFieldLevels];       // cells per axis at each level
+		uint32_t DenseLevels;        // bit l: level l indexed densely, (Res + 1)^3 <= TableSize
+		uint32_t TableSize;          // entries per level, a power of two
+		float Clamp;                 // the network approximates clamp(d, -Clamp, Clamp)
+	};
+
+	// Offsets (floats) in the network's FP32 parameter vector; weights are [out][in].
+	enum : int
+	{
+		kFieldW1 = 0, kFieldB1 = 2048, kFieldW2 = 2112, kFieldB2 = 6208, kFieldW3 = 6272, kFieldB3 = 10368,
+		kFieldW4 = 10432, kFieldB4 = 10496, kFieldParams = 10497
+	};
+
+	// Device image of the network the kernels stage into shared memory with one bulk copy:
+	// W1, W2, W3 as BF16 tiles in the tensor-core operand layout, then FP32 b1, b2, b3,
+	// W4 (rounded to BF16) and b4.
+	constexpr uint32_t kImageW1 = 0, kImageW2 = 4096, kImageW3 = 12288, kImageTail = 20480, kImageBytes = 21520;
+
+	struct AdamStep
+	{
+		float Rate, Beta1, Beta2, Epsilon;
+		float Correction1, Correction2;    // 1 - beta^t
+	};
+
+	cudaError_t LaunchFieldPack(const float* mlp, uint8_t* image, cudaStream_t stream);
+	// Network output at n points (x, y, z at points + i * stride).  status: set nonzero
+	// after a timed-out wait.
+	cudaError_t LaunchFieldEval(const FieldGrid& grid, const float2* table, const uint8_t* image, const float* points, int64_t n,
+		int stride, float* out, int* status, cudaStream_t stream);
+	// Adds d(loss)/d(parameters) for the mean squared error over n samples (x, y, z, d)
+	// against clamp(d) to table_grad / mlp_grad and the summed squared error to *loss.
+	cudaError_t LaunchFieldTrain(const FieldGrid& grid, const float2* table, const uint8_t* image, const float4* samples, int64_t n,
+		float2* table_grad, float* mlp_grad, float* loss, int* status, cudaStream_t stream);
+	// Adam on n parameters; zeroes the gradient it consumes.
+	cudaError_t LaunchAdam(float* params, float* grads, float* m, float* v, int64_t n, const AdamStep& step, cudaStream_t stream);
+	// Uniform points in [lo, hi) from a counter-based generator: sample i goes to
+	// out[i * stride + offset] with w = 0.
+	cudaError_t LaunchFieldUniform(uint64_t seed, const float* lo, const float* hi, float4* out, int64_t n, int64_t stride,
+		int64_t offset, cudaStream_t stream);
+	// w = the whole tree's distance (SDFNode::Eval) at each sample.
+	cudaError_t LaunchEvalFull(const DeviceProgram& prog, float4* samples, int64_t n, cudaStream_t stream);
+	// Bit i of words: |w_i| < band.
+	cudaError_t LaunchBandFlags(const float4* samples, int64_t n, float band, uint32_t* words, cudaStream_t stream);
+	// Flagged samples in order: the one of rank r goes to out[(first + r) * stride + offset]
+	// while first + r < limit.
+	cudaError_t LaunchBandCompact(const float4* samples, int64_t n, const uint32_t* words, const uint32_t* word_base,
+		float4* out, int64_t first, int64_t limit, int64_t stride, int64_t offset, cudaStream_t stream);
+	// Brick culling with the network: a brick's bit is set unless |net(centre)| exceeds its
+	// ball's radius plus `margin` or it misses the root cube (as LaunchClassifyBricks).
+	cudaError_t LaunchFieldClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, const FieldGrid& grid,
+		const float2* table, const uint8_t* image, float margin, uint32_t* brick_bits, int* status, cudaStream_t stream);
+	// Tensor-core operand-layout check: D = A * B^T through the descriptors the network
+	// kernels use.  mode 0: A 128x64 and B 64x64 read K-major; mode 1: A = a^T and
+	// B = b^T for a 128x128 and b 128x144 read MN-major (K = 128 rows); mode 2: A 128x64
+	// K-major, B = b^T for b 64x64 read MN-major.  Inputs FP32 (rounded to BF16), D 128 x N.
+	cudaError_t LaunchDebugMma(int mode, const float* a, const float* b, float* d, int* status, cudaStream_t stream);
 }

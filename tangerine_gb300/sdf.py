@@ -132,8 +132,9 @@ def _grid(g) -> _lib.Grid:
     return _lib.Grid(g.x0, g.y0, g.z0, g.step, g.sx + 1, g.sy + 1, g.sz + 1)
 
 
-def _flags(attributes=True, dense=False, brick=0, lanes=0) -> int:
-    return (1 if attributes else 0) | (2 if dense else 0) | ((int(brick) & 0xFF) << 8) | ((int(lanes) & 0xF) << 16)
+def _flags(attributes=True, dense=False, brick=0, lanes=0, surrogate_only=False) -> int:
+    return ((1 if attributes else 0) | (2 if dense else 0) | ((int(brick) & 0xFF) << 8) | ((int(lanes) & 0xF) << 16)
+            | ((1 << 20) if surrogate_only else 0))
 
 
 def last_export_stats():
@@ -328,3 +329,121 @@ def profile_read(kernel: str):
     n = C.c_int64()
     load().tg_profile_read(kernel.encode(), C.byref(ms), C.byref(n))
     return ms.value, n.value
+
+
+def surrogate_options(**kw) -> _lib.SurrogateOptions:
+    """tg_surrogate_options with the library defaults, fields overridden by keyword."""
+    o = _lib.SurrogateOptions()
+    load().tg_surrogate_default_options(C.byref(o))
+    for k, v in kw.items():
+        if k in ("domain_min", "domain_max"):
+            getattr(o, k)[:] = [float(x) for x in v]
+        else:
+            setattr(o, k, v)
+    return o
+
+
+class Surrogate:
+    """Learned distance bound of one tree (tg_surrogate_*): hash grid + 3x64 network on the
+    tensor cores, trained by the library's own kernels."""
+
+    def __init__(self, options: _lib.SurrogateOptions | None = None, **kw):
+        if options is None:
+            options = surrogate_options(**kw)
+        self.ptr = C.c_void_p()
+        check(load().tg_surrogate_create(C.byref(options), C.byref(self.ptr)), "tg_surrogate_create")
+        info = self.info()
+        self.table_floats = int(info.table_floats)
+        self.mlp_floats = int(info.mlp_floats)
+
+    def close(self):
+        if self.ptr and self.ptr.value:
+            load().tg_surrogate_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        if _lib._LIB is not None:
+            self.close()
+
+    def info(self) -> _lib.SurrogateInfo:
+        out = _lib.SurrogateInfo()
+        check(load().tg_surrogate_get_info(self.ptr, C.byref(out)), "tg_surrogate_get_info")
+        return out
+
+    def fit(self, program: Program, stream=None) -> _lib.SurrogateInfo:
+        check(load().tg_surrogate_fit(self.ptr, program.ptr, stream), "tg_surrogate_fit")
+        return self.info()
+
+    def params(self):
+        table = np.empty(self.table_floats, np.float32)
+        mlp = np.empty(self.mlp_floats, np.float32)
+        check(load().tg_surrogate_get_params(self.ptr, _lib.as_ptr(table), _lib.as_ptr(mlp)), "tg_surrogate_get_params")
+        return table, mlp
+
+    def set_params(self, table=None, mlp=None):
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        m = None if mlp is None else np.ascontiguousarray(mlp, np.float32)
+        check(load().tg_surrogate_set_params(self.ptr, None if t is None else _lib.as_ptr(t),
+                                             None if m is None else _lib.as_ptr(m)), "tg_surrogate_set_params")
+
+    def eval(self, points, stream=None) -> np.ndarray:
+        p = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+        out = np.empty(p.shape[0], np.float32)
+        check(load().tg_surrogate_eval(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), 0, stream), "tg_surrogate_eval")
+        return out
+
+    def gradients(self, samples):
+        """(table_grad, mlp_grad, summed squared error) of the mean squared error."""
+        s = np.ascontiguousarray(np.asarray(samples, np.float32).reshape(-1, 4))
+        tg_ = np.empty(self.table_floats, np.float32)
+        mg = np.empty(self.mlp_floats, np.float32)
+        loss = C.c_float()
+        check(load().tg_surrogate_gradients(self.ptr, _lib.as_ptr(s), s.shape[0], _lib.as_ptr(tg_), _lib.as_ptr(mg),
+                                            C.byref(loss)), "tg_surrogate_gradients")
+        return tg_, mg, loss.value
+
+    def train(self, samples, steps, stream=None):
+        s = np.ascontiguousarray(np.asarray(samples, np.float32).reshape(-1, 4))
+        check(load().tg_surrogate_train(self.ptr, _lib.as_ptr(s), s.shape[0], int(steps), stream), "tg_surrogate_train")
+
+    def margin(self, radius) -> float:
+        """The margin the culled export uses for bricks whose ball has this radius."""
+        m = C.c_float()
+        check(load().tg_surrogate_margin(self.ptr, float(radius), C.byref(m)), "tg_surrogate_margin")
+        return m.value
+
+    def set_margin(self, margin):
+        check(load().tg_surrogate_set_margin(self.ptr, float(margin)), "tg_surrogate_set_margin")
+
+    def export_mesh(self, program: Program, grid, attributes=True, brick=0, lanes=0, only=False, stream=None) -> Mesh:
+        """only: the network alone decides (no exact test of the bricks it keeps)."""
+        g = _grid(grid)
+        hm = _lib.HostMesh()
+        check(load().tg_export_mesh_surrogate(program.ptr, self.ptr, C.byref(g), _flags(attributes, False, brick, lanes, only),
+                                              C.byref(hm), stream), "tg_export_mesh_surrogate")
+        return _take_mesh(hm)
+
+    def export_mesh_device(self, program: Program, grid, attributes=True, brick=0, lanes=0, only=False,
+                           stream=None) -> _lib.DeviceMesh:
+        g = _grid(grid)
+        dm = _lib.DeviceMesh()
+        check(load().tg_export_mesh_surrogate_device(program.ptr, self.ptr, C.byref(g),
+                                                     _flags(attributes, False, brick, lanes, only), C.byref(dm), stream),
+              "tg_export_mesh_surrogate_device")
+        return dm
+
+
+def debug_mma(mode: int, a, b) -> np.ndarray:
+    """tg_debug_mma: the tensor-core product through the network kernels' operand layouts."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    n = 144 if mode == 1 else 64
+    d = np.zeros((128, n), np.float32)
+    check(load().tg_debug_mma(int(mode), _lib.as_ptr(a), _lib.as_ptr(b), _lib.as_ptr(d)), "tg_debug_mma")
+    return d

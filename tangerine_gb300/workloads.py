@@ -179,3 +179,30 @@ def camera_poses(seed: int, count: int, radius: float = 4.0):
         r = math.sqrt(max(0.0, 1.0 - z * z))
         poses.append((radius * r * math.cos(a), radius * r * math.sin(a), radius * z))
     return np.asarray(poses, dtype=np.float32)
+
+
+def camera_rays(position, width: int, height: int, tan_half: float):
+    """The ray tg_render casts through every pixel of a camera at `position` looking at the
+    origin with +z up, in float32 with the renderer's operation order: origins and
+    unnormalised directions, row-major over pixels."""
+    f32 = np.float32
+
+    def normalize(v):
+        d = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]
+        s = f32(1.0) / np.sqrt(f32(d))
+        return np.array([v[0] * s, v[1] * s, v[2] * s], np.float32)
+
+    def cross(a, b):
+        return np.array([a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]], np.float32)
+
+    pos = np.asarray(position, np.float32)
+    fwd = normalize(np.zeros(3, np.float32) - pos)
+    right = normalize(cross(fwd, np.array([0, 0, 1], np.float32)))
+    up = cross(right, fwd)
+    x = np.arange(width, dtype=np.float32)[None, :].repeat(height, 0)
+    y = np.arange(height, dtype=np.float32)[:, None].repeat(width, 1)
+    aspect = f32(width) / f32(height)
+    u = ((f32(2.0) * (x + f32(0.5)) / f32(width)) - f32(1.0)) * f32(tan_half) * aspect
+    v = (f32(1.0) - f32(2.0) * (y + f32(0.5)) / f32(height)) * f32(tan_half)
+    d = np.stack([(fwd[i] + right[i] * u) + up[i] * v for i in range(3)], -1).astype(np.float32)
+    return np.broadcast_to(pos, d.shape).copy().reshape(-1, 3), d.reshape(-1, 3)

@@ -1,0 +1,127 @@
+"""The learned distance bound on the GPU against the float64 oracle (oracle/surrogate.py):
+tensor-core operand layouts, forward pass, gradients, the Adam step, and a trained
+network culling export bricks without changing the mesh.
+
+Tolerances: the kernels accumulate in FP32 where the oracle uses float64, so a BF16
+rounding of an input or activation can land on the other side of a rounding boundary
+now and then; comparisons bound the worst case loosely and the typical case tightly."""
+
+import numpy as np
+import pytest
+
+from oracle import surrogate as S
+from tangerine_gb300 import sdf
+from tangerine_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _dyadic(rng, shape):
+    """Values exactly representable in BF16 whose products and sums stay exact in FP32."""
+    return rng.integers(-8, 9, shape).astype(np.float32) / 8.0
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_tensor_core_operand_layouts(lib, mode):
+    rng = np.random.default_rng(10 + mode)
+    if mode == 0:
+        a, b = _dyadic(rng, (128, 64)), _dyadic(rng, (64, 64))
+        want = a @ b.T
+    elif mode == 1:
+        a, b = _dyadic(rng, (128, 128)), _dyadic(rng, (128, 144))
+        want = a.T @ b
+    else:
+        a, b = _dyadic(rng, (128, 64)), _dyadic(rng, (64, 64))
+        want = a @ b
+    got = sdf.debug_mma(mode, a, b)
+    np.testing.assert_array_equal(got, want.astype(np.float32))
+
+
+def _net(rng, log2_table=14, **kw):
+    s = sdf.Surrogate(log2_table=log2_table, **kw)
+    info = s.info()
+    table = rng.uniform(-1, 1, s.table_floats).astype(np.float32)
+    _, mlp = s.params()
+    mlp = mlp.copy()
+    mlp[S.B1:S.W2] = rng.uniform(-0.1, 0.1, 64)
+    mlp[S.B2:S.W3] = rng.uniform(-0.1, 0.1, 64)
+    mlp[S.B4] = 0.02
+    s.set_params(table, mlp)
+    return s, S.Grid.from_info(info), table, mlp
+
+
+def test_forward_matches_oracle(lib):
+    rng = np.random.default_rng(1)
+    s, grid, table, mlp = _net(rng)
+    pts = rng.uniform(-2.2, 2.2, (3001, 3)).astype(np.float32)     # partial last tile, points outside the box
+    got = s.eval(pts)
+    want = S.forward(grid, table, mlp, pts)["s"]
+    scale = np.abs(want).max()
+    err = np.abs(got - want)
+    assert err.max() <= 2e-2 * scale, (err.max(), scale)
+    assert np.median(err) <= 1e-4 * scale, (np.median(err), scale)
+    s.close()
+
+
+def test_gradients_match_oracle(lib):
+    rng = np.random.default_rng(2)
+    s, grid, table, mlp = _net(rng)
+    n = 1000
+    smp = np.concatenate([rng.uniform(-2, 2, (n, 3)), rng.uniform(-0.8, 0.8, (n, 1))], 1).astype(np.float32)
+    gt, gm, loss = s.gradients(smp)
+    rt, rm, rloss = S.gradients(grid, table, mlp, smp)
+    assert abs(loss - rloss) <= 1e-3 * rloss
+    for name, lo, hi in (("W1", S.W1, S.B1), ("b1", S.B1, S.W2), ("W2", S.W2, S.B2), ("b2", S.B2, S.W3),
+                         ("W3", S.W3, S.B3), ("b3", S.B3, S.W4), ("W4", S.W4, S.B4), ("b4", S.B4, S.PARAMS)):
+        ref = rm[lo:hi]
+        rel = np.linalg.norm(gm[lo:hi] - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+    rel = np.linalg.norm(gt - rt) / np.linalg.norm(rt)
+    assert rel <= 2e-2, rel
+    # Only the corners the samples touch receive gradient.
+    assert np.array_equal(gt != 0, rt != 0) or np.mean((gt != 0) != (rt != 0)) < 1e-4
+    s.close()
+
+
+def test_adam_step_matches_oracle(lib):
+    rng = np.random.default_rng(4)
+    s, grid, table, mlp = _net(rng, batch=1 << 12, learning_rate=1e-2)
+    n = 2048
+    smp = np.concatenate([rng.uniform(-2, 2, (n, 3)), rng.uniform(-0.5, 0.5, (n, 1))], 1).astype(np.float32)
+    gt, gm, _ = s.gradients(smp)
+    s.train(smp, 1)
+    t1, m1 = s.params()
+    rt, _, _ = S.adam(table, gt, 0, 0, 1, 1e-2)
+    rmlp, _, _ = S.adam(mlp, gm, 0, 0, 1, 1e-2)
+    bad_t = np.abs(t1 - rt) > 1e-6 + 1e-3 * 1e-2
+    bad_m = np.abs(m1 - rmlp) > 1e-6 + 1e-3 * 1e-2
+    assert bad_t.mean() < 1e-3 and bad_m.mean() < 1e-3, (bad_t.mean(), bad_m.mean())
+    s.close()
+
+
+def test_trained_bound_culls_bricks_and_keeps_the_mesh(lib):
+    """What the network gains: most bricks of a 16-primitive tree at 128^3 are skipped on
+    its word, and the mesh is the dense export's, vertex for vertex."""
+    spec = W.random_tree(1, 16, ops=W.OPS_UNIFORM4)
+    grid = W.export_grid(resolution=128)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        s = sdf.Surrogate(samples=1 << 20, steps=400, batch=1 << 16, validation=1 << 18)
+        info = s.fit(prog)
+        assert info.max_error < 0.1 and info.p99_error < info.max_error
+        assert 0.0 < s.margin(0.05) < 0.1
+        dense = prog.export_mesh(grid, dense=True)
+        alone = s.export_mesh(prog, grid, only=True)
+        bricks, kept = sdf.last_export_stats()
+        refined = s.export_mesh(prog, grid, brick=15)
+        _, kept_refined = sdf.last_export_stats()
+        exact = prog.export_mesh(grid, brick=15)
+        bricks15, kept_exact = sdf.last_export_stats()
+        s.close()
+    for m in (alone, refined, exact):
+        np.testing.assert_array_equal(m.vertices, dense.vertices)
+        np.testing.assert_array_equal(m.faces, dense.faces)
+        np.testing.assert_array_equal(m.normals, dense.normals)
+        np.testing.assert_array_equal(m.colors, dense.colors)
+    assert kept < 0.5 * bricks, (kept, bricks)
+    # With the exact test after it, the network can only remove bricks from the exact set.
+    assert kept_refined <= kept_exact, (kept_refined, kept_exact)

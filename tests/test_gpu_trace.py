@@ -6,8 +6,6 @@ Octree-bounded form: different (conservative) steps, so it stops at a different 
 within the hit epsilon of the surface: hit masks must agree on all but grazing rays and
 depths within DEPTH_TOL where both hit."""
 
-import math
-
 import numpy as np
 import pytest
 
@@ -20,35 +18,6 @@ pytestmark = pytest.mark.gpu
 DEPTH_TOL = 2e-3          # octree-bounded vs exact depth, same ray, both hitting
 EPS = 1e-4
 STEPS = 256
-
-
-def f32(x):
-    return np.float32(x)
-
-
-def normalize(v):
-    d = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]
-    s = f32(1.0) / np.sqrt(f32(d))
-    return np.array([v[0] * s, v[1] * s, v[2] * s], np.float32)
-
-
-def cross(a, b):
-    return np.array([a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]], np.float32)
-
-
-def camera_rays(position, width, height, tan_half):
-    """The renderer's ray for every pixel, in float32 with its operation order."""
-    pos = np.asarray(position, np.float32)
-    fwd = normalize(np.zeros(3, np.float32) - pos)
-    right = normalize(cross(fwd, np.array([0, 0, 1], np.float32)))
-    up = cross(right, fwd)
-    x = np.arange(width, dtype=np.float32)[None, :].repeat(height, 0)
-    y = np.arange(height, dtype=np.float32)[:, None].repeat(width, 1)
-    aspect = f32(width) / f32(height)
-    u = ((f32(2.0) * (x + f32(0.5)) / f32(width)) - f32(1.0)) * f32(tan_half) * aspect
-    v = (f32(1.0) - f32(2.0) * (y + f32(0.5)) / f32(height)) * f32(tan_half)
-    d = np.stack([(fwd[i] + right[i] * u) + up[i] * v for i in range(3)], -1).astype(np.float32)
-    return np.broadcast_to(pos, d.shape).copy().reshape(-1, 3), d.reshape(-1, 3)
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -77,7 +46,7 @@ def test_render_exact_and_bounded(lib, port, seed, prims):
     h = port.build(spec)
     try:
         for i, p in enumerate(poses):
-            o, d = camera_rays(p, width, height, tan_half)
+            o, d = W.camera_rays(p, width, height, tan_half)
             hit, travel, pos = port.raymarch(h, o, d, STEPS, EPS, threads=0)
             np.testing.assert_array_equal(d_exact[i].reshape(-1), travel)
             normals = np.zeros((hit.size, 3), np.float32)
