@@ -588,6 +588,110 @@ def render_arm(args, rank, world, local_rank):
     prog.close()
 
 
+def batch_arm(args, rank, world, local_rank):
+    """512 seeded trees (primitives log-uniform in [4, 1024], grids uniform over
+    {64, 128, 192, 256, 384}^3) exported together by one persistent launch replayed from a
+    CUDA graph, per-class brick size and lanes from the autotuner; samples/s and meshes/s."""
+    import concurrent.futures as cf
+    import torch
+    from tangerine_gb300 import build as B
+    B.build()
+    from tangerine_gb300 import sdf
+    from tangerine_gb300 import workloads as W
+    torch.cuda.set_device(local_rank)
+    count = args.batch_models
+    models = W.batch_workload(SEED, count, valid=lambda spec: sdf.has_export_octree(sdf.from_spec(spec)))
+
+    def make(item):
+        seed, prims, res = item
+        return sdf.compile(sdf.from_spec(W.random_tree(seed, prims))), W.export_grid(resolution=res)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 8) as ex:
+        built = list(ex.map(make, models))
+    compile_s = time.perf_counter() - t0
+    progs = [p for p, _ in built]
+    grids = [g for _, g in built]
+    samples = int(sum(g.corners for g in grids))
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    batch = sdf.Batch(progs, grids)
+    t0 = time.perf_counter()
+    batch.autotune(stream=sp)
+    tune_s = time.perf_counter() - t0
+    bricks, lanes = batch.tuning()
+    for _ in range(max(1, args.warmup)):
+        batch.run(stream=sp)
+
+    def timed(fn, steps):
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.zero_()
+            st[i].record(stream)
+            fn()
+            en[i].record(stream)
+        torch.cuda.synchronize()
+        return float(np.sum([a.elapsed_time(b) for a, b in zip(st, en)]))
+
+    with ClockSampler(None) as clocks:
+        ms = timed(lambda: batch.run(stream=sp), args.steps)
+    info = batch.info()
+    # The same models one export call each (the single-model pipeline, same tuning).
+    def sequential():
+        for p, g, b, l in zip(progs, grids, bricks, lanes):
+            p.export_mesh_device(g, brick=int(b), lanes=int(l), stream=sp)
+    seq_ms = timed(sequential, 1)
+    # End to end: the batch run plus every mesh copied to host memory.
+    t0 = time.perf_counter()
+    e2e_steps = 2
+    d2h = 0
+    for _ in range(e2e_steps):
+        batch.run(stream=sp)
+        d2h = 0
+        for m in range(count):
+            mesh = batch.mesh(m, stream=sp)
+            d2h += mesh.vertices.nbytes + mesh.normals.nbytes + mesh.faces.nbytes + mesh.cubes.nbytes + \
+                (mesh.colors.nbytes if mesh.colors is not None else 0)
+    e2e_s = time.perf_counter() - t0
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        big = max(range(count), key=lambda m: models[m][1] * models[m][2] ** 2)
+        cb = cpu_baseline(W.random_tree(models[big][0], models[big][1]), grids[big])
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu["sample"] = f"model {big} ({models[big][1]} primitives, {models[big][2]}^3): " + cpu["sample"]
+    hist = {}
+    for b, l in zip(bricks, lanes):
+        hist[f"{b}x{l}"] = hist.get(f"{b}x{l}", 0) + 1
+    line = {"metric": f"samples/s & meshes/s: {count} trees exported in one persistent launch",
+            "value": samples * args.steps / (ms * 1e-3), "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{count} seeded CSG trees (seed {SEED}; a tree left empty by its set operations is "
+                                   f"replaced by its sequence's next seed), primitives log-uniform in [4, 1024], grids "
+                                   f"uniform over {{64,128,192,256,384}}^3 over [-2,2]^3; exact export with normals + colours; "
+                                   f"one cooperative launch per step replayed from a CUDA graph",
+                       "samples_per_step": samples, "l2": "flushed between steps"},
+            "meshes_per_s": count * args.steps / (ms * 1e-3),
+            "batch": {"bricks": info.bricks, "bricks_evaluated": info.bricks_evaluated, "vertices": info.vertices,
+                      "faces": info.faces, "graph": info.graph, "blocks": info.blocks, "reruns": info.reruns,
+                      "device_gb": info.device_bytes / 1e9, "autotune_seconds": tune_s, "compile_seconds": compile_s,
+                      "tuning_histogram_brick_x_lanes": hist},
+            "sequential_exports": {"ms_per_step": seq_ms, "value": samples / (seq_ms * 1e-3),
+                                   "note": "same models, one tg_export_mesh_device call each"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": samples * e2e_steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(d2h), "call": "tg_batch_run + tg_batch_mesh for every model"},
+            "gpu_launches": args.steps, "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    for p in progs:
+        p.close()
+
+
 def surrogate_arm(args, rank, world, local_rank):
     """The 256-primitive tree on a 1024^3 grid in 32^3 bricks: dense exact, exact-culled and
     surrogate-culled exports (same mesh), samples/s."""
@@ -662,7 +766,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate"],
+    ap.add_argument("--batch-models", type=int, default=512, help="trees in the batch workload")
+    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate", "batch"],
                     help="export: the 512^3 mesh export (the benchmark); render: the sphere-tracing workload; "
                          "surrogate: the 1024^3 export in 32^3 bricks with the learned bound")
     ap.add_argument("--skip-surrogate", action="store_true", help="skip the surrogate-culled leg of the export")
@@ -681,6 +786,8 @@ def main():
         render_arm(args, rank, world, local_rank)
     elif args.workload == "surrogate":
         surrogate_arm(args, rank, world, local_rank)
+    elif args.workload == "batch":
+        batch_arm(args, rank, world, local_rank)
     else:
         our_arm(args, rank, world, local_rank)
 

@@ -291,6 +291,47 @@ TANGERINE_API void tg_profile_reset(void);
  * the compute roofline of the distance interpreter. */
 TANGERINE_API tg_status tg_measure_fp32_peak(double* tflops, void* stream);
 
+/* ---- many trees in one launch ----------------------------------------------------------
+ * No counterpart in the reference (which exports one tree per call on a detached thread).
+ * The programs' exports run together as one persistent cooperative kernel over a global
+ * (model, brick) work queue -- classify, evaluate, surface nets, normals, colours -- replayed
+ * from a CUDA graph.  Each model's mesh equals tg_export_mesh's for its program and lattice.
+ * The programs must outlive the batch. */
+typedef struct tg_batch tg_batch;
+
+typedef struct tg_batch_info
+{
+	int64_t models, samples;                   /* lattice points over all models */
+	int64_t bricks, bricks_evaluated;
+	int64_t vertices, faces;
+	int graph;                                 /* 1: replayed from a CUDA graph; -1: capture refused, launched directly */
+	int blocks;                                /* CTAs of the cooperative launch */
+	int reruns;                                /* runs repeated after growing the output buffers */
+	double autotune_seconds;
+	int64_t device_bytes;
+} tg_batch_info;
+
+/* flags: TG_MESH_ATTRIBUTES.  Brick edge 7 and 2 lattice points per thread for every model
+ * until tg_batch_autotune or tg_batch_set_tuning. */
+TANGERINE_API tg_status tg_batch_create(tg_program* const* programs, const tg_grid* grids, int count, uint32_t flags,
+                                        tg_batch** out);
+TANGERINE_API void tg_batch_free(tg_batch* batch);
+/* Per (lattice extent, program size) class: times single-model exports of one member for
+ * brick edges {4, 7, 11, 15} x lattice points per thread {1, 2, 4} and gives the class the
+ * fastest. */
+TANGERINE_API tg_status tg_batch_autotune(tg_batch* batch, void* stream);
+TANGERINE_API tg_status tg_batch_set_tuning(tg_batch* batch, const int* brick_edges, const int* lanes);
+TANGERINE_API tg_status tg_batch_get_tuning(const tg_batch* batch, int* brick_edges, int* lanes);
+TANGERINE_API tg_status tg_batch_run(tg_batch* batch, void* stream);
+/* Output capacity for the next run (default: an estimate from the lattices); a run that
+ * finds more vertices or faces grows the buffers and runs again (tg_batch_info.reruns). */
+TANGERINE_API tg_status tg_batch_reserve(tg_batch* batch, uint64_t vertices, uint64_t faces);
+TANGERINE_API tg_status tg_batch_get_info(const tg_batch* batch, tg_batch_info* out);
+/* Model `model`'s mesh from the last run, copied to host memory (release with tg_mesh_free),
+ * or left on the device (valid until the next run or tg_batch_free). */
+TANGERINE_API tg_status tg_batch_mesh(tg_batch* batch, int model, tg_mesh* out, void* stream);
+TANGERINE_API tg_status tg_batch_mesh_device(tg_batch* batch, int model, tg_device_mesh* out);
+
 /* ---- learned distance bound ---------------------------------------------------------
  * No counterpart in the reference.  A per-tree network -- a 16-level hash grid (2 features
  * per level) feeding 3 hidden ReLU layers of 64, BF16 weights on the tensor cores with FP32

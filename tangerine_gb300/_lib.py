@@ -61,6 +61,12 @@ class SurrogateInfo(C.Structure):
                 ("dense_levels", C.c_uint32), ("table_floats", C.c_int64), ("mlp_floats", C.c_int64)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("models", C.c_int64), ("samples", C.c_int64), ("bricks", C.c_int64), ("bricks_evaluated", C.c_int64),
+                ("vertices", C.c_int64), ("faces", C.c_int64), ("graph", C.c_int), ("blocks", C.c_int), ("reruns", C.c_int),
+                ("autotune_seconds", C.c_double), ("device_bytes", C.c_int64)]
+
+
 # Every exported symbol with its signature: (restype, argtypes).
 _vp, _f, _i, _i64, _u32 = C.c_void_p, C.c_float, C.c_int, C.c_int64, C.c_uint32
 SIGNATURES = {
@@ -117,6 +123,16 @@ SIGNATURES = {
     "tg_profile_read": (_i, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "tg_profile_reset": (None, []),
     "tg_measure_fp32_peak": (_i, [C.POINTER(C.c_double), _vp]),
+    "tg_batch_create": (_i, [C.POINTER(_vp), C.POINTER(Grid), _i, _u32, C.POINTER(_vp)]),
+    "tg_batch_free": (None, [_vp]),
+    "tg_batch_autotune": (_i, [_vp, _vp]),
+    "tg_batch_set_tuning": (_i, [_vp, _vp, _vp]),
+    "tg_batch_get_tuning": (_i, [_vp, _vp, _vp]),
+    "tg_batch_run": (_i, [_vp, _vp]),
+    "tg_batch_reserve": (_i, [_vp, C.c_uint64, C.c_uint64]),
+    "tg_batch_get_info": (_i, [_vp, C.POINTER(BatchInfo)]),
+    "tg_batch_mesh": (_i, [_vp, _i, C.POINTER(HostMesh), _vp]),
+    "tg_batch_mesh_device": (_i, [_vp, _i, C.POINTER(DeviceMesh)]),
     "tg_surrogate_default_options": (None, [C.POINTER(SurrogateOptions)]),
     "tg_surrogate_create": (_i, [C.POINTER(SurrogateOptions), C.POINTER(_vp)]),
     "tg_surrogate_free": (None, [_vp]),

@@ -14,6 +14,7 @@
 
 #include "tg_engine.hpp"
 #include "tg_surrogate.hpp"
+#include "tg_batch.hpp"
 #include "tg_octree.hpp"
 #include "tg_tree.hpp"
 
@@ -610,6 +611,132 @@ extern "C"
 		cudaError_t e = MeasureFp32Peak(tflops, StreamOf(stream));
 		if (e != cudaSuccess) return CudaFail(e, "measuring FP32 throughput");
 		return TG_OK;
+	}
+
+	// ---- many trees in one launch ---------------------------------------------------------
+
+	TANGERINE_API tg_status tg_batch_create(tg_program* const* programs, const tg_grid* grids, int count, uint32_t flags, tg_batch** out)
+	{
+		if (!out || !programs || !grids || count <= 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		*out = nullptr;
+		std::vector<const Program*> progs((size_t)count);
+		std::vector<GridSpec> specs((size_t)count);
+		for (int m = 0; m < count; ++m)
+		{
+			if (!programs[m]) { SetError("null program in the batch"); return TG_ERR_INVALID; }
+			progs[m] = programs[m];
+			if (!ToGridSpec(&grids[m], specs[m])) return TG_ERR_INVALID;
+		}
+		std::unique_ptr<tg_batch> b(new (std::nothrow) tg_batch(std::move(progs), std::move(specs), (flags & TG_MESH_ATTRIBUTES) != 0));
+		if (!b) { SetError("out of host memory"); return TG_ERR_MEMORY; }
+		*out = b.release();
+		return TG_OK;
+	}
+
+	TANGERINE_API void tg_batch_free(tg_batch* b)
+	{
+		if (!b) return;
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		delete b;
+	}
+
+	TANGERINE_API tg_status tg_batch_autotune(tg_batch* b, void* stream)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = b->Autotune(StreamOf(stream));
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "autotuning the batch");
+	}
+
+	TANGERINE_API tg_status tg_batch_set_tuning(tg_batch* b, const int* bricks, const int* lanes)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		const size_t n = b->Bricks.size();
+		std::vector<int> bv = b->Bricks, lv = b->Lanes;
+		for (size_t m = 0; m < n; ++m)
+		{
+			if (bricks && (bricks[m] < 1 || bricks[m] > 32)) { SetError("brick edge must be 1..32 cells"); return TG_ERR_INVALID; }
+			if (lanes && lanes[m] != 1 && lanes[m] != 2 && lanes[m] != 4) { SetError("lanes must be 1, 2 or 4"); return TG_ERR_INVALID; }
+			if (bricks) bv[m] = bricks[m];
+			if (lanes) lv[m] = lanes[m];
+		}
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		b->SetTuning(bv, lv);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_get_tuning(const tg_batch* b, int* bricks, int* lanes)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		for (size_t m = 0; m < b->Bricks.size(); ++m)
+		{
+			if (bricks) bricks[m] = b->Bricks[m];
+			if (lanes) lanes[m] = b->Lanes[m];
+		}
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_run(tg_batch* b, void* stream)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = b->Run(StreamOf(stream));
+		if (e == cudaErrorLaunchTimeout) return TG_ERR_CUDA;
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "running the batch");
+	}
+
+	TANGERINE_API tg_status tg_batch_reserve(tg_batch* b, uint64_t vertices, uint64_t faces)
+	{
+		if (!b || vertices >= (1ull << 32) || faces >= (1ull << 32)) { SetError("invalid argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		b->Reserve((uint32_t)vertices, (uint32_t)faces);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_get_info(const tg_batch* b, tg_batch_info* out)
+	{
+		if (!b || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		const BatchInfo& i = b->Info;
+		out->models = i.Models;
+		out->samples = i.Samples;
+		out->bricks = i.Bricks;
+		out->bricks_evaluated = i.BricksEvaluated;
+		out->vertices = i.Vertices;
+		out->faces = i.Faces;
+		out->graph = i.Graph;
+		out->blocks = i.Blocks;
+		out->reruns = i.Reruns;
+		out->autotune_seconds = i.AutotuneSeconds;
+		out->device_bytes = i.DeviceBytes;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_mesh_device(tg_batch* b, int model, tg_device_mesh* out)
+	{
+		if (!b || !out || model < 0 || model >= (int)b->Bricks.size()) { SetError("invalid argument"); return TG_ERR_INVALID; }
+		DeviceMesh dm;
+		b->MeshOf(model, dm);
+		out->vertex_count = dm.VertexCount;
+		out->face_count = dm.FaceCount;
+		out->vertices = dm.Vertices;
+		out->normals = dm.Normals;
+		out->colors = dm.Colors;
+		out->faces = dm.Faces;
+		out->cubes = dm.Cubes;
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_mesh(tg_batch* b, int model, tg_mesh* out, void* stream)
+	{
+		if (!b || !out || model < 0 || model >= (int)b->Bricks.size()) { SetError("invalid argument"); return TG_ERR_INVALID; }
+		DeviceMesh dm;
+		b->MeshOf(model, dm);
+		return CopyMeshToHost(dm, out, StreamOf(stream));
 	}
 
 	// ---- learned distance bound ---------------------------------------------------------

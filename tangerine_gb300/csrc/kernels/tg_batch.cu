@@ -1,0 +1,547 @@
+// Many trees exported in one persistent launch.
+//
+// Every model's bricks, cells and vertices live in one global index space: model m owns
+// brick-bit words [BrickWord0, BrickWord0 + BrickWords), cell-bit words from CellWord0,
+// lattice floats from Lattice, and (after the cell scan) vertices from VertexBase[m].  A
+// cooperative grid runs the export's phases over that space -- classify bricks, list the
+// survivors, evaluate them, flag active cells, number the vertices, emit vertices, number
+// and emit faces, gradient normals and colours -- separated by grid-wide barriers, so the
+// work queue of (model, brick) items balances models of very different sizes across the
+// whole GPU.  Per model, the results are exactly the single-model export's: the same
+// kernels' per-item code, vertices in cell order, faces holding the model's own vertex
+// numbers.
+//
+// The grid barrier is a counter and a generation word in global memory, waited on with a
+// time limit: a barrier that runs out sets the status and every block leaves.
+#include <cstdint>
+
+#include "tg_cull.cuh"
+#include "tg_device.cuh"
+#include "tg_kernels.hpp"
+#include "tg_surface.cuh"
+
+namespace tg
+{
+	namespace
+	{
+		constexpr int kThreads = 128;
+		constexpr int kScanItems = 4;
+		constexpr uint64_t kBarrierLimitNs = 5000000000ull;    // 5 s
+		constexpr int kAttribPoints = kThreads / 5;            // 25 vertices x 5 evaluation lanes
+
+		__device__ __forceinline__ uint64_t Now()
+		{
+			uint64_t t;
+			asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+			return t;
+		}
+
+		// Grid-wide barrier of a cooperative launch.  False (for every thread of the block)
+		// when the wait ran out or an earlier one did.
+		__device__ bool GridSync(const BatchState& s)
+		{
+			__shared__ int ok;
+			__syncthreads();
+			if (threadIdx.x == 0)
+			{
+				ok = 1;
+				volatile unsigned* gen = s.Barrier + 1;
+				const unsigned g = *gen;
+				__threadfence();
+				if (atomicAdd(s.Barrier, 1u) == gridDim.x - 1)
+				{
+					atomicExch(s.Barrier, 0u);
+					__threadfence();
+					atomicAdd(s.Barrier + 1, 1u);
+				}
+				else
+				{
+					const uint64_t t0 = Now();
+					while (*gen == g)
+					{
+						if (*(volatile int*)s.Status != 0 || Now() - t0 > kBarrierLimitNs)
+						{
+							atomicCAS(s.Status, 0, 2);
+							ok = 0;
+							break;
+						}
+					}
+				}
+				__threadfence();
+				if (*(volatile int*)s.Status != 0) ok = 0;
+			}
+			__syncthreads();
+			return ok != 0;
+		}
+
+		// Index of the last model whose first item (starts[m]) is <= x.
+		template<typename T>
+		__device__ __forceinline__ int ModelOf(const T* __restrict__ starts, int count, T x)
+		{
+			int lo = 0, hi = count - 1;
+			while (lo < hi)
+			{
+				const int mid = (lo + hi + 1) >> 1;
+				if (__ldg(starts + mid) <= x) lo = mid;
+				else hi = mid - 1;
+			}
+			return lo;
+		}
+
+		// ---- block and grid scans ------------------------------------------------------
+
+		__device__ __forceinline__ uint32_t BlockScan(uint32_t x, uint32_t& total)
+		{
+			__shared__ uint32_t warpSums[kThreads / 32];
+			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+			uint32_t inc = x;
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1)
+			{
+				const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+				if (lane >= o) inc += y;
+			}
+			if (lane == 31) warpSums[warp] = inc;
+			__syncthreads();
+			uint32_t before = 0;
+			total = 0;
+#pragma unroll
+			for (int w = 0; w < kThreads / 32; ++w)
+			{
+				const uint32_t v = warpSums[w];
+				if (w < warp) before += v;
+				total += v;
+			}
+			__syncthreads();
+			return before + inc - x;
+		}
+
+		__device__ __forceinline__ uint32_t Item(const uint32_t* in, int64_t i, int64_t n, bool pop)
+		{
+			if (i >= n) return 0u;
+			const uint32_t x = in[i];
+			return pop ? (uint32_t)__popc(x) : x;
+		}
+
+		// Exclusive prefix sum over n items (popcounts of words, or values) into out; the
+		// total lands in *total.  Three barriers.  `partials` holds gridDim.x + 1 words.
+		__device__ bool GridScan(const BatchState& s, const uint32_t* in, int64_t n, bool pop, uint32_t* out, uint32_t* total)
+		{
+			const int64_t tile = (int64_t)kThreads * kScanItems;
+			int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+			chunk = (chunk + tile - 1) / tile * tile;
+			const int64_t b0 = (int64_t)blockIdx.x * chunk;
+			const int64_t b1 = b0 + chunk < n ? b0 + chunk : n;
+			{
+				uint32_t sum = 0;
+				for (int64_t i = b0 + threadIdx.x; i < b1; i += kThreads) sum += Item(in, i, n, pop);
+				uint32_t t;
+				BlockScan(sum, t);
+				if (threadIdx.x == 0) s.ScanPartials[blockIdx.x] = t;
+			}
+			if (!GridSync(s)) return false;
+			if (blockIdx.x == 0)
+			{
+				uint32_t carry = 0;
+				for (int64_t base = 0; base < gridDim.x; base += kThreads)
+				{
+					const int64_t i = base + threadIdx.x;
+					const uint32_t v = i < gridDim.x ? s.ScanPartials[i] : 0u;
+					uint32_t t;
+					const uint32_t ex = BlockScan(v, t);
+					if (i < gridDim.x) s.ScanPartials[i] = carry + ex;
+					carry += t;
+				}
+				if (threadIdx.x == 0)
+				{
+					s.ScanPartials[gridDim.x] = carry;
+					*total = carry;
+				}
+			}
+			if (!GridSync(s)) return false;
+			uint32_t run = s.ScanPartials[blockIdx.x];
+			for (int64_t base = b0; base < b1; base += tile)
+			{
+				uint32_t v[kScanItems];
+				uint32_t local = 0;
+				const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+				for (int q = 0; q < kScanItems; ++q)
+				{
+					v[q] = first + q < b1 ? Item(in, first + q, n, pop) : 0u;
+					local += v[q];
+				}
+				uint32_t t;
+				uint32_t ex = BlockScan(local, t) + run;
+#pragma unroll
+				for (int q = 0; q < kScanItems; ++q)
+				{
+					if (first + q < b1) out[first + q] = ex;
+					ex += v[q];
+				}
+				run += t;
+			}
+			return GridSync(s);
+		}
+
+		// ---- per-item work ---------------------------------------------------------------
+
+		template<int K>
+		__device__ void EvalBrickK(const BatchModel& m, float* __restrict__ lattice, uint32_t b, float* spill)
+		{
+			const GridSpec& g = m.Grid;
+			const DeviceProgram& prog = m.Prog;
+			constexpr int ZSpan = 2 * K;
+			const int tx = threadIdx.x & 7, ty = (threadIdx.x >> 3) & 7, tz = threadIdx.x >> 6;
+			const int bx = (int)(b % (uint32_t)m.NBX), by = (int)((b / (uint32_t)m.NBX) % (uint32_t)m.NBY);
+			const int bz = (int)(b / ((uint32_t)m.NBX * (uint32_t)m.NBY));
+			const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;
+			const int i1 = min(i0 + m.B, g.NX - 1), j1 = min(j0 + m.B, g.NY - 1), k1 = min(k0 + m.B, g.NZ - 1);
+			for (int oz = 0; oz <= k1 - k0; oz += ZSpan)
+			for (int oy = 0; oy <= j1 - j0; oy += 8)
+			for (int ox = 0; ox <= i1 - i0; ox += 8)
+			{
+				const int ix = i0 + ox + tx, iy = j0 + oy + ty, izb = k0 + oz + tz * K;
+				const bool inPlane = ix <= i1 && iy <= j1;
+				const float x = LatticeCoord(g.X0, min(ix, i1), g.Step);
+				const float y = LatticeCoord(g.Y0, min(iy, j1), g.Step);
+				float px[K], py[K], pz[K], res[K];
+				int cell[K];
+				unsigned todo = 0;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					const int iz = izb + k;
+					px[k] = x;
+					py[k] = y;
+					pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.Step);
+					cell[k] = DescendOctree(prog.Nodes, px[k], py[k], pz[k]);
+					res[k] = 0.0f;
+					if (inPlane && iz <= k1) todo |= 1u << k;
+				}
+				while (todo)
+				{
+					int c = -1;
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+						if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
+					float r[K];
+					RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kThreads);
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+					{
+						if (((todo >> k) & 1u) && cell[k] == c)
+						{
+							res[k] = r[k];
+							todo &= ~(1u << k);
+						}
+					}
+				}
+				if (inPlane)
+				{
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+					{
+						const int iz = izb + k;
+						if (iz <= k1) lattice[((int64_t)iz * g.NY + iy) * g.NX + ix] = res[k];
+					}
+				}
+			}
+		}
+
+		__device__ __forceinline__ Vec3 TetraPoint(Vec3 p, int lane)
+		{
+			const float h = 0.0001f;
+			switch (lane)
+			{
+			case 0: return p + Vec3(h, -h, -h);
+			case 1: return p + Vec3(-h, -h, h);
+			case 2: return p + Vec3(-h, h, -h);
+			case 3: return p + Vec3(h, h, h);
+			default: return p;
+			}
+		}
+
+		__device__ __forceinline__ Vec3 GradientOf(const float* e)
+		{
+			const float h = 0.0001f;
+			const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+			Vec3 g = xyy * e[0];
+			g = g + yyx * e[1];
+			g = g + yxy * e[2];
+			g = g + xxx * e[3];
+			const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+			if (ls == 0.0f)
+			{
+				const float d = e[4];
+				return Normalize(Vec3(e[0] - d, e[2] - d, e[1] - d));
+			}
+			return g / sqrtf(ls);
+		}
+
+		// ---- the persistent kernel ---------------------------------------------------------
+
+		__global__ void __launch_bounds__(kThreads) BatchExportKernel(BatchState s)
+		{
+			extern __shared__ float spill[];
+			const int warpsPerGrid = gridDim.x * (kThreads / 32);
+			const int warp = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+			const int lane = threadIdx.x & 31;
+			const int64_t gthreads = (int64_t)gridDim.x * kThreads;
+			const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+
+			// 1. Classify every brick of every model (a warp per bit word); clear the cell bits.
+			for (int64_t w = warp; w < s.BrickWordsTotal; w += warpsPerGrid)
+			{
+				const int mi = ModelOf(s.BrickWord0, s.Count, w);
+				const BatchModel& m = s.Models[mi];
+				const int64_t local = (w - m.BrickWord0) * 32 + lane;
+				bool active = false;
+				if (local < m.Bricks)
+				{
+					const int bx = (int)(local % m.NBX), by = (int)((local / m.NBX) % m.NBY), bz = (int)(local / ((int64_t)m.NBX * m.NBY));
+					const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;
+					active = BoxMayHoldSurface(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
+						k0, min(k0 + m.B, m.Grid.NZ - 1), spill + threadIdx.x, kThreads);
+				}
+				const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
+				if (lane == 0) s.BrickBits[w] = ballot;
+			}
+			for (int64_t w = gtid; w < s.CellWordsTotal; w += gthreads) s.CellBits[w] = 0u;
+			if (!GridSync(s)) return;
+
+			// 2. Kept bricks as a list in global brick order.
+			if (!GridScan(s, s.BrickBits, s.BrickWordsTotal, true, s.BrickWordBase, s.Counters + 0)) return;
+			for (int64_t w = gtid; w < s.BrickWordsTotal; w += gthreads)
+			{
+				uint32_t bits = s.BrickBits[w];
+				uint32_t at = s.BrickWordBase[w];
+				while (bits)
+				{
+					const int j = __ffs(bits) - 1;
+					bits &= bits - 1u;
+					s.BrickList[at++] = (uint32_t)(w * 32 + j);
+				}
+			}
+			if (!GridSync(s)) return;
+			const uint32_t kept = s.Counters[0];
+
+			// 3. Distances at the lattice points of every kept brick (a CTA per brick).
+			for (uint32_t item = blockIdx.x; item < kept; item += gridDim.x)
+			{
+				const uint32_t gb = s.BrickList[item];
+				const int mi = ModelOf(s.BrickWord0, s.Count, (int64_t)(gb >> 5));
+				const BatchModel& m = s.Models[mi];
+				const uint32_t b = gb - (uint32_t)(m.BrickWord0 * 32);
+				float* lat = s.Lattice + m.Lattice;
+				if (m.Lanes == 1) EvalBrickK<1>(m, lat, b, spill);
+				else if (m.Lanes == 4) EvalBrickK<4>(m, lat, b, spill);
+				else EvalBrickK<2>(m, lat, b, spill);
+			}
+			if (!GridSync(s)) return;
+
+			// 4. Active cells of the kept bricks: bits, and an append list of global cell bits.
+			for (uint32_t item = blockIdx.x; item < kept; item += gridDim.x)
+			{
+				const uint32_t gb = s.BrickList[item];
+				const int mi = ModelOf(s.BrickWord0, s.Count, (int64_t)(gb >> 5));
+				const BatchModel& m = s.Models[mi];
+				const uint32_t b = gb - (uint32_t)(m.BrickWord0 * 32);
+				const CellGeom cg = Geom(m.Grid);
+				const float* lat = s.Lattice + m.Lattice;
+				const int bx = (int)(b % (uint32_t)m.NBX), by = (int)((b / (uint32_t)m.NBX) % (uint32_t)m.NBY);
+				const int bz = (int)(b / ((uint32_t)m.NBX * (uint32_t)m.NBY));
+				const int64_t ci0 = (int64_t)bx * m.B, cj0 = (int64_t)by * m.B, ck0 = (int64_t)bz * m.B;
+				const int nx = (int)min((int64_t)m.B, cg.sx - ci0), ny = (int)min((int64_t)m.B, cg.sy - cj0);
+				const int nz = (int)min((int64_t)m.B, cg.sz - ck0);
+				const int total = nx * ny * nz;
+				for (int r0 = 0; r0 < total; r0 += kThreads)
+				{
+					const int t = r0 + (int)threadIdx.x;
+					bool active = false;
+					int64_t c = 0;
+					if (t < total)
+					{
+						const int64_t i = ci0 + t % nx, j = cj0 + (t / nx) % ny, k = ck0 + t / (nx * ny);
+						float v[8];
+						LoadCorners(lat, cg, i, j, k, v);
+						unsigned pos = 0;
+#pragma unroll
+						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+						active = pos != 0u && pos != 0xFFu;
+						c = i + j * cg.sx + k * cg.sx * cg.sy;
+						if (active) atomicOr(s.CellBits + m.CellWord0 + (c >> 5), 1u << (c & 31));
+					}
+					const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
+					uint32_t base = 0;
+					if (lane == 0 && ballot) base = atomicAdd(s.Counters + 1, (uint32_t)__popc(ballot));
+					base = __shfl_sync(0xFFFFFFFFu, base, 0);
+					const uint32_t at = base + __popc(ballot & ((1u << lane) - 1u));
+					if (active && at < s.CapVertices) s.ActiveCells[at] = (uint64_t)m.CellWord0 * 32u + (uint64_t)c;
+				}
+			}
+			if (!GridSync(s)) return;
+
+			// 5. Vertex numbers: ranks in the global cell bitmask.
+			if (!GridScan(s, s.CellBits, s.CellWordsTotal, true, s.CellWordBase, s.Counters + 2)) return;
+			const uint32_t vertices = s.Counters[2];
+			const bool vertexRoom = vertices <= s.CapVertices;
+			if (!vertexRoom && gtid == 0) atomicOr(s.Counters + 4, 1u);
+
+			// 6. Vertices, cube numbers and face counts; each model's first vertex.
+			for (int64_t mi = gtid; mi <= s.Count; mi += gthreads)
+			{
+				if (mi == s.Count) s.VertexBase[mi] = vertices;
+				else s.VertexBase[mi] = s.CellWords[mi] ? s.CellWordBase[s.Models[mi].CellWord0] : vertices;
+			}
+			if (vertexRoom)
+			{
+				const uint32_t active = s.Counters[1] < s.CapVertices ? s.Counters[1] : s.CapVertices;
+				for (int64_t t = gtid; t < active; t += gthreads)
+				{
+					const uint64_t gc = s.ActiveCells[t];
+					const int m2 = ModelOf(s.CellBit0, s.Count, gc);
+					const BatchModel& m = s.Models[m2];
+					const int64_t c = (int64_t)(gc - (uint64_t)m.CellWord0 * 32u);
+					const CellGeom cg = Geom(m.Grid);
+					const uint32_t* words = s.CellBits + m.CellWord0;
+					const uint32_t* base = s.CellWordBase + m.CellWord0;
+					const uint32_t w = words[c >> 5];
+					const uint32_t vid = base[c >> 5] + __popc(w & ((1u << (c & 31)) - 1u));
+					const int64_t i = c % cg.sx, j = (c / cg.sx) % cg.sy, k = c / (cg.sx * cg.sy);
+					EmitCellVertex(s.Lattice + m.Lattice, m.Grid, cg, words, c, i, j, k, vid, s.Vertices, s.Cubes, s.FaceCounts);
+				}
+			}
+			if (!GridSync(s)) return;
+
+			// 7. Face numbers.
+			if (!GridScan(s, s.FaceCounts, vertexRoom ? vertices : 0, false, s.FaceBase, s.Counters + 3)) return;
+			const uint32_t faces = s.Counters[3];
+			const bool faceRoom = vertexRoom && faces <= s.CapFaces;
+			if (!faceRoom && gtid == 0) atomicOr(s.Counters + 4, 2u);
+			for (int64_t mi = gtid; mi <= s.Count; mi += gthreads)
+			{
+				const uint32_t v = s.VertexBase[mi];
+				s.FaceBaseModel[mi] = (mi == s.Count || v >= vertices || !vertexRoom) ? faces : s.FaceBase[v];
+			}
+
+			// 8. Triangles, numbered within their model.
+			if (faceRoom)
+			{
+				for (int64_t v0 = gtid; v0 < vertices; v0 += gthreads)
+				{
+					const int mi = ModelOf(s.VertexBase, s.Count, (uint32_t)v0);
+					const BatchModel& m = s.Models[mi];
+					const CellGeom cg = Geom(m.Grid);
+					const float* lat = s.Lattice + m.Lattice;
+					const uint32_t* words = s.CellBits + m.CellWord0;
+					const uint32_t* base = s.CellWordBase + m.CellWord0;
+					const uint32_t vb = s.VertexBase[mi];
+					const int64_t c = s.Cubes[v0];
+					const int64_t i = c % cg.sx, j = (c / cg.sx) % cg.sy, k = c / (cg.sx * cg.sy);
+					if (i == 0 || j == 0 || k == 0) continue;
+					const int64_t dy = cg.sx, dz = cg.sx * cg.sy;
+					const int64_t nb[6] = { c - 1, c - 1 - dy, c - dy, c - dy - dz, c - dz, c - 1 - dz };
+					const int quads[3][3] = { {0, 1, 2}, {0, 5, 4}, {2, 3, 4} };
+					const float c0 = Corner(lat, cg, i, j, k);
+					const float sv[3][2] = { { c0, Corner(lat, cg, i, j, k + 1) }, { Corner(lat, cg, i, j + 1, k), c0 },
+						{ c0, Corner(lat, cg, i + 1, j, k) } };
+					uint32_t out = s.FaceBase[v0];
+					const uint32_t self = (uint32_t)v0 - vb;
+					for (int q = 0; q < 3; ++q)
+					{
+						const int64_t a = nb[quads[q][0]], b = nb[quads[q][1]], d = nb[quads[q][2]];
+						if (!(IsActive(words, a) && IsActive(words, b) && IsActive(words, d))) continue;
+						const uint32_t nv[3] = { VertexOf(words, base, a) - vb, VertexOf(words, base, b) - vb, VertexOf(words, base, d) - vb };
+						uint32_t v1, v2, v3;
+						if (sv[q][1] > sv[q][0]) { v1 = nv[0]; v2 = nv[1]; v3 = nv[2]; }
+						else { v1 = nv[2]; v2 = nv[1]; v3 = nv[0]; }
+						uint32_t* f = s.Faces + (int64_t)out * 3;
+						f[0] = self; f[1] = v1; f[2] = v2;
+						f[3] = self; f[4] = v2; f[5] = v3;
+						out += 2;
+					}
+				}
+			}
+
+			// 9. Gradient normals and colours: five evaluation lanes per vertex.
+			if (s.Attributes && vertexRoom)
+			{
+				__shared__ float evals[kThreads];
+				__shared__ int mats[kAttribPoints];
+				const int localPoint = threadIdx.x / 5, elane = threadIdx.x % 5;
+				for (int64_t first = (int64_t)blockIdx.x * kAttribPoints; first < vertices; first += (int64_t)gridDim.x * kAttribPoints)
+				{
+					const int64_t v = first + localPoint;
+					const bool mine = localPoint < kAttribPoints && v < vertices;
+					int mi = 0;
+					if (mine)
+					{
+						mi = ModelOf(s.VertexBase, s.Count, (uint32_t)v);
+						const BatchModel& m = s.Models[mi];
+						const Vec3 p(s.Vertices[v * 3], s.Vertices[v * 3 + 1], s.Vertices[v * 3 + 2]);
+						const int cell = DescendOctree(m.Prog.Nodes, p.x, p.y, p.z);
+						const int pc = __ldg(&m.Prog.Nodes[cell].SurfaceCode);
+						const Vec3 q = TetraPoint(p, elane);
+						const float px[1] = { q.x }, py[1] = { q.y }, pz[1] = { q.z };
+						float e[1];
+						int mat = -1;
+						RunSurfaceBatch<1>(m.Prog.Code, pc, px, py, pz, e, (elane == 4 && m.HasPaint) ? 0 : -1, &mat, spill + threadIdx.x, kThreads);
+						evals[threadIdx.x] = e[0];
+						if (elane == 4) mats[localPoint] = mat;
+					}
+					__syncthreads();
+					if (mine && elane == 0)
+					{
+						const BatchModel& m = s.Models[mi];
+						const Vec3 g = GradientOf(evals + localPoint * 5);
+						s.Normals[v * 3 + 0] = g.x;
+						s.Normals[v * 3 + 1] = g.y;
+						s.Normals[v * 3 + 2] = g.z;
+						if (m.HasPaint)
+						{
+							const int mt = mats[localPoint];
+							const uchar4 c = mt >= 0 ? m.Prog.Colors[mt] : make_uchar4(255, 255, 255, 255);
+							s.Colors[v * 3 + 0] = c.x;
+							s.Colors[v * 3 + 1] = c.y;
+							s.Colors[v * 3 + 2] = c.z;
+						}
+					}
+					__syncthreads();
+				}
+			}
+		}
+	}
+
+	size_t BatchSharedBytes(int max_stack)
+	{
+		const int depth = max_stack > 1 ? max_stack - 1 : 1;
+		return (size_t)depth * 4 * kThreads * sizeof(float);      // K = 4 lanes of distance spill
+	}
+
+	int BatchThreads() { return kThreads; }
+
+	cudaError_t BatchMaxBlocks(int max_stack, int* blocks)
+	{
+		const size_t smem = BatchSharedBytes(max_stack);
+		cudaError_t e = cudaFuncSetAttribute(BatchExportKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		int perSm = 0, dev = 0, sms = 0;
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, BatchExportKernel, kThreads, smem);
+		if (e == cudaSuccess) e = cudaGetDevice(&dev);
+		if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		if (e != cudaSuccess) return e;
+		*blocks = perSm * sms;
+		return cudaSuccess;
+	}
+
+	cudaError_t LaunchBatchExport(const BatchState& s, int blocks, int max_stack, cudaStream_t stream)
+	{
+		const size_t smem = BatchSharedBytes(max_stack);
+		cudaError_t e = cudaFuncSetAttribute(BatchExportKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		BatchState copy = s;
+		void* args[] = { &copy };
+		return cudaLaunchCooperativeKernel((const void*)BatchExportKernel, dim3(blocks), dim3(kThreads), args, smem, stream);
+	}
+}

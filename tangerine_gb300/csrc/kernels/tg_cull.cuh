@@ -3,6 +3,7 @@
 #pragma once
 
 #include "tg_device.cuh"
+#include "tg_kernels.hpp"
 
 namespace tg
 {

@@ -172,3 +172,57 @@ namespace tg
 	// K-major, B = b^T for b 64x64 read MN-major.  Inputs FP32 (rounded to BF16), D 128 x N.
 	cudaError_t LaunchDebugMma(int mode, const float* a, const float* b, float* d, int* status, cudaStream_t stream);
 }
+
+namespace tg
+{
+	// ---- many trees in one persistent launch (tg_batch.cu) ---------------------------
+	struct BatchModel
+	{
+		DeviceProgram Prog;
+		GridSpec Grid;
+		int B, NBX, NBY, NBZ;      // brick edge (cells) and bricks per axis
+		int Lanes, HasPaint;       // lattice points per thread; colours wanted
+		int64_t Bricks;
+		int64_t Lattice;           // first float of the model's lattice in the pool
+		int64_t BrickWord0;        // first word of its brick bits
+		int64_t CellWord0;         // first word of its cell bits
+	};
+
+	struct BatchState
+	{
+		const BatchModel* Models;
+		int Count;
+		int Attributes;
+		const int64_t* BrickWord0;     // per model, ascending
+		const uint64_t* CellBit0;      // per model: CellWord0 * 32
+		const int64_t* CellWords;      // per model
+		int64_t BrickWordsTotal, CellWordsTotal;
+		uint32_t* BrickBits;
+		uint32_t* BrickWordBase;
+		uint32_t* BrickList;
+		uint32_t* CellBits;
+		uint32_t* CellWordBase;
+		uint64_t* ActiveCells;
+		float* Lattice;
+		uint32_t CapVertices, CapFaces;
+		float* Vertices;
+		float* Normals;
+		uint8_t* Colors;
+		uint32_t* Cubes;
+		uint32_t* FaceCounts;
+		uint32_t* FaceBase;
+		uint32_t* Faces;
+		uint32_t* VertexBase;          // per model + 1: first vertex (global numbering)
+		uint32_t* FaceBaseModel;       // per model + 1: first face
+		uint32_t* Counters;            // kept bricks, active cells, vertices, faces, overflow bits
+		uint32_t* ScanPartials;        // blocks + 1
+		unsigned* Barrier;             // arrival count, generation
+		int* Status;                   // nonzero: a barrier wait ran out
+	};
+
+	size_t BatchSharedBytes(int max_stack);
+	int BatchThreads();
+	// Co-resident blocks of the cooperative batch kernel on this device.
+	cudaError_t BatchMaxBlocks(int max_stack, int* blocks);
+	cudaError_t LaunchBatchExport(const BatchState& s, int blocks, int max_stack, cudaStream_t stream);
+}

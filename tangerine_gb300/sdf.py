@@ -111,6 +111,12 @@ def stencil(a: Tree, mask: Tree, rgb, negative=False):
     return Tree(load().MakeStencilOp(a._give(), mask._give(), *map(float, rgb), bool(negative)))
 
 
+def has_export_octree(tree: "Tree") -> bool:
+    """Whether the tree has finite, non-empty bounds (SDFOctree::Create would succeed);
+    host-only, no GPU needed."""
+    return load().tg_debug_octree(tree.handle, None, None, 0, None, 0, None) >= 0
+
+
 def from_spec(spec) -> Tree:
     spec = np.ascontiguousarray(spec, dtype=np.float32)
     return Tree(load().BuildTreeFromSpec(_lib.as_ptr(spec), int(spec.size)))
@@ -447,3 +453,68 @@ def debug_mma(mode: int, a, b) -> np.ndarray:
     d = np.zeros((128, n), np.float32)
     check(load().tg_debug_mma(int(mode), _lib.as_ptr(a), _lib.as_ptr(b), _lib.as_ptr(d)), "tg_debug_mma")
     return d
+
+
+class Batch:
+    """Many programs exported together by one persistent launch (tg_batch_*).  The programs
+    must stay open while the batch lives."""
+
+    def __init__(self, programs, grids, attributes=True):
+        self.programs = list(programs)
+        n = len(self.programs)
+        arr = (C.c_void_p * n)(*[p.ptr.value for p in self.programs])
+        gs = (_lib.Grid * n)(*[_grid(g) for g in grids])
+        self.ptr = C.c_void_p()
+        check(load().tg_batch_create(arr, gs, n, 1 if attributes else 0, C.byref(self.ptr)), "tg_batch_create")
+        self.count = n
+
+    def close(self):
+        if self.ptr and self.ptr.value:
+            load().tg_batch_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        if _lib._LIB is not None:
+            self.close()
+
+    def autotune(self, stream=None):
+        check(load().tg_batch_autotune(self.ptr, stream), "tg_batch_autotune")
+
+    def set_tuning(self, bricks=None, lanes=None):
+        b = None if bricks is None else np.ascontiguousarray(bricks, np.int32)
+        l = None if lanes is None else np.ascontiguousarray(lanes, np.int32)
+        check(load().tg_batch_set_tuning(self.ptr, None if b is None else _lib.as_ptr(b), None if l is None else _lib.as_ptr(l)),
+              "tg_batch_set_tuning")
+
+    def tuning(self):
+        b = np.empty(self.count, np.int32)
+        l = np.empty(self.count, np.int32)
+        check(load().tg_batch_get_tuning(self.ptr, _lib.as_ptr(b), _lib.as_ptr(l)), "tg_batch_get_tuning")
+        return b, l
+
+    def run(self, stream=None):
+        check(load().tg_batch_run(self.ptr, stream), "tg_batch_run")
+
+    def reserve(self, vertices, faces):
+        check(load().tg_batch_reserve(self.ptr, int(vertices), int(faces)), "tg_batch_reserve")
+
+    def info(self) -> _lib.BatchInfo:
+        out = _lib.BatchInfo()
+        check(load().tg_batch_get_info(self.ptr, C.byref(out)), "tg_batch_get_info")
+        return out
+
+    def mesh(self, model: int, stream=None) -> Mesh:
+        hm = _lib.HostMesh()
+        check(load().tg_batch_mesh(self.ptr, int(model), C.byref(hm), stream), "tg_batch_mesh")
+        return _take_mesh(hm)
+
+    def mesh_device(self, model: int) -> _lib.DeviceMesh:
+        dm = _lib.DeviceMesh()
+        check(load().tg_batch_mesh_device(self.ptr, int(model), C.byref(dm)), "tg_batch_mesh_device")
+        return dm

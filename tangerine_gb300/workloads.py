@@ -206,3 +206,30 @@ def camera_rays(position, width: int, height: int, tan_half: float):
     v = (f32(1.0) - f32(2.0) * (y + f32(0.5)) / f32(height)) * f32(tan_half)
     d = np.stack([(fwd[i] + right[i] * u) + up[i] * v for i in range(3)], -1).astype(np.float32)
     return np.broadcast_to(pos, d.shape).copy().reshape(-1, 3), d.reshape(-1, 3)
+
+
+BATCH_RESOLUTIONS = (64, 128, 192, 256, 384)
+
+
+def batch_workload(seed: int, count: int = 512, min_prims: int = 4, max_prims: int = 1024,
+                   resolutions=BATCH_RESOLUTIONS, valid=None):
+    """Independent seeded trees for the batched export: primitive counts log-uniform in
+    [min_prims, max_prims], grid resolution uniform over `resolutions` (cells per axis of
+    [-2, 2]^3).  Returns [(tree seed, primitive count, resolution)].  `valid(spec)`, when
+    given, rejects trees (an intersection or difference can leave nothing); a rejected
+    model takes the next tree seed of its own sequence."""
+    rng = _Words(seed * 7919 + 17)
+    out = []
+    lo, hi = math.log(min_prims), math.log(max_prims)
+    for i in range(count):
+        prims = int(round(math.exp(rng.uniform(lo, hi))))
+        prims = max(min_prims, min(max_prims, prims))
+        res = resolutions[min(len(resolutions) - 1, int(rng.uniform(0.0, float(len(resolutions)))))]
+        tree_seed = seed * 100000 + i
+        if valid is not None:
+            attempt = 0
+            while not valid(random_tree(tree_seed, prims)):
+                attempt += 1
+                tree_seed = seed * 100000 + i + 1000003 * attempt
+        out.append((tree_seed, prims, res))
+    return out

@@ -1,0 +1,79 @@
+"""Many trees in one persistent launch: every model's mesh must equal the single-model
+export of its program and lattice, bit for bit, whatever the per-model tuning."""
+
+import numpy as np
+import pytest
+
+from tangerine_gb300 import sdf
+from tangerine_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+MODELS = [(11, 4, 24), (12, 16, 40), (17, 64, 32), (14, 256, 48), (15, 8, 16), (16, 128, 36)]
+
+
+@pytest.fixture(scope="module")
+def programs(lib):
+    progs, grids = [], []
+    for seed, prims, res in MODELS:
+        ops = W.OPS_UNIFORM4 if prims <= 16 else W.OPS_60_20_10_10
+        progs.append(sdf.compile(sdf.from_spec(W.random_tree(seed, prims, ops=ops))))
+        grids.append(W.export_grid(resolution=res))
+    # An unpainted tree too: the batch must leave its colours out as the export does.
+    progs.append(sdf.compile(sdf.union(sdf.sphere(0.5), sdf.box(0.3, 0.4, 0.2).move(0.4, 0.0, 0.0))))
+    grids.append(W.export_grid(resolution=20))
+    yield progs, grids
+    for p in progs:
+        p.close()
+
+
+def _same(a, b):
+    np.testing.assert_array_equal(a.vertices, b.vertices)
+    np.testing.assert_array_equal(a.faces, b.faces)
+    np.testing.assert_array_equal(a.normals, b.normals)
+    np.testing.assert_array_equal(a.cubes, b.cubes)
+    assert (a.colors is None) == (b.colors is None)
+    if a.colors is not None:
+        np.testing.assert_array_equal(a.colors, b.colors)
+
+
+def test_batch_meshes_equal_single_exports(programs):
+    progs, grids = programs
+    singles = [p.export_mesh(g) for p, g in zip(progs, grids)]
+    with sdf.Batch(progs, grids) as b:
+        b.run()
+        info = b.info()
+        assert info.models == len(progs) and info.reruns == 0
+        for m, ref in enumerate(singles):
+            _same(b.mesh(m), ref)
+        assert info.vertices == sum(len(r.vertices) for r in singles)
+        assert info.faces == sum(len(r.faces) for r in singles)
+        # Replay (from the CUDA graph when capture was accepted) gives the same again.
+        b.run()
+        assert b.info().graph in (1, -1)
+        for m, ref in enumerate(singles):
+            _same(b.mesh(m), ref)
+
+
+def test_batch_mixed_tuning_and_growth(programs):
+    progs, grids = programs
+    singles = [p.export_mesh(g) for p, g in zip(progs, grids)]
+    rng = np.random.default_rng(5)
+    with sdf.Batch(progs, grids) as b:
+        b.set_tuning(rng.choice([1, 3, 4, 7, 11, 15], len(progs)), rng.choice([1, 2, 4], len(progs)))
+        b.reserve(64, 64)                 # far too small: the run grows the outputs and repeats
+        b.run()
+        assert b.info().reruns >= 1
+        for m, ref in enumerate(singles):
+            _same(b.mesh(m), ref)
+
+
+def test_batch_autotune(programs):
+    progs, grids = programs
+    with sdf.Batch(progs[:3], grids[:3]) as b:
+        b.autotune()
+        bricks, lanes = b.tuning()
+        assert set(bricks) <= {4, 7, 11, 15} and set(lanes) <= {1, 2, 4}
+        b.run()
+        for m in range(3):
+            _same(b.mesh(m), progs[m].export_mesh(grids[m]))
