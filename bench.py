@@ -558,7 +558,7 @@ def render_arm(args, rank, world, local_rank):
         port = O.port()
         h = port.build(spec)
         try:
-            stride = 997
+            stride = 41
             o, d = W.camera_rays(poses[0], width, height, cams[0].tan_half_fov)
             idx = np.arange(px)[::stride]
             o, d = np.ascontiguousarray(o[idx]), np.ascontiguousarray(d[idx])
