@@ -544,6 +544,46 @@ def render_arm(args, rank, world, local_rank):
     e1.record(stream)
     torch.cuda.synchronize()
     exact_rays_s = 2 * px / (e0.elapsed_time(e1) * 1e-3)
+    exact_depth = depth[:2 * px].clone()
+    # Network steps with exact final steps, all poses; agreement with the exact tracer on the
+    # first two.
+    network = None
+    if not args.skip_surrogate:
+        sur = sdf.Surrogate()
+        t0 = time.perf_counter()
+        sinfo = sur.fit(prog)
+        fit_s = time.perf_counter() - t0
+
+        def render_net(n, cam_array):
+            _lib.check(lib.tg_render_surrogate(prog.ptr, sur.ptr, cam_array, n, width, height, steps, eps,
+                                               _lib.C.c_void_p(depth.data_ptr()), _lib.C.c_void_p(normals.data_ptr()),
+                                               _lib.C.c_void_p(colors.data_ptr()), 1, _lib.C.c_void_p(sp)), "tg_render_surrogate")
+
+        render_net(2, exact_cams)
+        torch.cuda.synchronize()
+        net_depth = depth[:2 * px]
+        he, hn = torch.isfinite(exact_depth), torch.isfinite(net_depth)
+        both = he & hn
+        agree = float((he == hn).float().mean().item())
+        dd = (exact_depth[both] - net_depth[both]).abs()
+        max_dd = float(dd.max().item()) if bool(both.any()) else 0.0
+        far = int((dd > 2e-3).sum().item())
+        n0, n1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0.record(stream)
+        render_net(poses_n, cams)
+        n1.record(stream)
+        torch.cuda.synchronize()
+        net_ms = n0.elapsed_time(n1)
+        ns, es = sdf.last_render_steps()
+        network = {"rays_per_s": rays / (net_ms * 1e-3), "ms_all_poses": net_ms, "fit_seconds": fit_s,
+                   "held_out_max_error": sinfo.max_error, "step_margin": sinfo.margin,
+                   "network_iterations_per_ray": ns / rays, "exact_steps_per_ray": es / rays,
+                   "vs_exact_only": (rays / (net_ms * 1e-3)) / exact_rays_s,
+                   "hit_agreement_with_exact": agree, "max_depth_difference": max_dd,
+                   "rays_both_hit_depth_over_2e-3": far, "rays_compared": 2 * px,
+                   "note": "network step bounds (tcgen05 network per lockstep iteration) then exact whole-tree steps; "
+                           "every hit is the exact program's"}
+        sur.close()
     # End to end: host buffers, all poses.
     hd = np.empty(rays, np.float32)
     hn = np.empty(rays * 3, np.float32)
@@ -581,6 +621,7 @@ def render_arm(args, rank, world, local_rank):
                                    "1920x1080, 60 deg vertical FOV, 256 steps, epsilon 1e-4, octree-bounded steps",
                        "hit_fraction": hits},
             "exact_rays_per_s": exact_rays_s,
+            "network_steps": network,
             "e2e": {"value": rays / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": rays * 19},
             "cpu_baseline": cpu, "gpu_launches": args.steps}
     if rank == 0:

@@ -415,11 +415,26 @@ TANGERINE_API tg_status tg_export_mesh_surrogate(tg_program* program, tg_surroga
                                                  tg_mesh* out, void* stream);
 TANGERINE_API tg_status tg_export_mesh_surrogate_device(tg_program* program, tg_surrogate* s, const tg_grid* grid,
                                                         uint32_t flags, tg_device_mesh* out, void* stream);
+/* tg_render with network steps: each ray steps by the larger of the root cube's distance
+ * and the network's value less its margin (safety x the largest held-out error) until that
+ * bound falls to the margin, then by SDFNode::RayMarch's exact whole-tree steps; hits are
+ * the exact program's and are shaded with the whole tree's gradient and material.  The
+ * step budget (max_steps) covers both kinds of step. */
+TANGERINE_API tg_status tg_render_surrogate(tg_program* program, tg_surrogate* s, const tg_camera* cameras, int count, int width,
+                                            int height, int max_steps, float epsilon, float* depth, float* normals,
+                                            uint8_t* colors, int out_is_device, void* stream);
+/* Network iterations (per ray, summed) and exact steps of the last tg_render_surrogate. */
+TANGERINE_API tg_status tg_last_render_steps(uint64_t* network_steps, uint64_t* exact_steps);
 /* Check of the tensor-core operand layouts: D = A B^T through the descriptors the network
  * kernels use (mode 0: a 128x64, b 64x64, both K-major, D 128x64; mode 1: D = a^T b for
  * a 128x128, b 128x144, D 128x144; mode 2: D = a b for a 128x64, b 64x64, D 128x64).
  * Host FP32 arrays, inputs rounded to BF16. */
 TANGERINE_API tg_status tg_debug_mma(int mode, const float* a, const float* b, float* d);
+
+/* Check of the GPU's float evaluation of the smooth-blend term against the reference's
+ * double expression on n seeded inputs (x2 signs): counts[0] compared, counts[1] differing
+ * (must be 0), counts[2] sent to the double path. */
+TANGERINE_API tg_status tg_debug_blend_check(uint64_t n, uint64_t seed, uint64_t* counts);
 
 TANGERINE_API const char* tg_last_error(void);
 TANGERINE_API const char* tg_version(void);

@@ -147,7 +147,10 @@ SIGNATURES = {
     "tg_surrogate_margin": (_i, [_vp, _f, C.POINTER(_f)]),
     "tg_export_mesh_surrogate": (_i, [_vp, _vp, C.POINTER(Grid), _u32, C.POINTER(HostMesh), _vp]),
     "tg_export_mesh_surrogate_device": (_i, [_vp, _vp, C.POINTER(Grid), _u32, C.POINTER(DeviceMesh), _vp]),
+    "tg_render_surrogate": (_i, [_vp, _vp, C.POINTER(Camera), _i, _i, _i, _i, _f, _vp, _vp, _vp, _i, _vp]),
+    "tg_last_render_steps": (_i, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tg_debug_mma": (_i, [_i, _vp, _vp, _vp]),
+    "tg_debug_blend_check": (_i, [C.c_uint64, C.c_uint64, _vp]),
     "tg_last_error": (C.c_char_p, []),
     "tg_version": (C.c_char_p, []),
 }

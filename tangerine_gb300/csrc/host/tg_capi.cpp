@@ -429,34 +429,60 @@ extern "C"
 		return TG_OK;
 	}
 
+	namespace
+	{
+		tg_status RenderWith(tg_program* p, tg_surrogate* field, const tg_camera* cameras, int count, int width, int height, int max_steps,
+			float epsilon, uint32_t flags, float* depth, float* normals, uint8_t* colors, int out_is_device, void* stream)
+		{
+			if (!p || !cameras || !depth || !normals) { SetError("null argument"); return TG_ERR_INVALID; }
+			if (count < 0 || width <= 0 || height <= 0 || max_steps < 0) { SetError("invalid image size or step count"); return TG_ERR_INVALID; }
+			std::vector<CameraBasis> basis((size_t)count);
+			for (int c = 0; c < count; ++c)
+			{
+				const tg_camera& cam = cameras[c];
+				const Vec3 pos(cam.position[0], cam.position[1], cam.position[2]);
+				const Vec3 fwd = Normalize(Vec3(cam.target[0], cam.target[1], cam.target[2]) - pos);
+				const Vec3 right = Normalize(Cross(fwd, Vec3(cam.up[0], cam.up[1], cam.up[2])));
+				const Vec3 up = Cross(right, fwd);
+				CameraBasis& b = basis[(size_t)c];
+				b.Position[0] = pos.x; b.Position[1] = pos.y; b.Position[2] = pos.z;
+				b.Forward[0] = fwd.x; b.Forward[1] = fwd.y; b.Forward[2] = fwd.z;
+				b.Right[0] = right.x; b.Right[1] = right.y; b.Right[2] = right.z;
+				b.Up[0] = up.x; b.Up[1] = up.y; b.Up[2] = up.z;
+				b.TanHalfFov = cam.tan_half_fov;
+				b.Aspect = (float)width / (float)height;
+			}
+			Engine& eng = Engine::Get();
+			std::lock_guard<std::mutex> lock(eng.Mutex);
+			cudaError_t e = eng.Render(*p, basis.data(), count, width, height, max_steps, epsilon, (flags & TG_RENDER_EXACT) != 0, depth,
+				normals, p->Host.Header.HasPaint ? colors : nullptr, out_is_device != 0, StreamOf(stream), field);
+			if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the network renderer"); return TG_ERR_CUDA; }
+			if (e != cudaSuccess) return CudaFail(e, "rendering");
+			if (colors && !p->Host.Header.HasPaint && !out_is_device)
+				std::memset(colors, 255, (size_t)width * height * count * 3);
+			return TG_OK;
+		}
+	}
+
 	TANGERINE_API tg_status tg_render(tg_program* p, const tg_camera* cameras, int count, int width, int height, int max_steps,
 		float epsilon, uint32_t flags, float* depth, float* normals, uint8_t* colors, int out_is_device, void* stream)
 	{
-		if (!p || !cameras || !depth || !normals) { SetError("null argument"); return TG_ERR_INVALID; }
-		if (count < 0 || width <= 0 || height <= 0 || max_steps < 0) { SetError("invalid image size or step count"); return TG_ERR_INVALID; }
-		std::vector<CameraBasis> basis((size_t)count);
-		for (int c = 0; c < count; ++c)
-		{
-			const tg_camera& cam = cameras[c];
-			const Vec3 pos(cam.position[0], cam.position[1], cam.position[2]);
-			const Vec3 fwd = Normalize(Vec3(cam.target[0], cam.target[1], cam.target[2]) - pos);
-			const Vec3 right = Normalize(Cross(fwd, Vec3(cam.up[0], cam.up[1], cam.up[2])));
-			const Vec3 up = Cross(right, fwd);
-			CameraBasis& b = basis[(size_t)c];
-			b.Position[0] = pos.x; b.Position[1] = pos.y; b.Position[2] = pos.z;
-			b.Forward[0] = fwd.x; b.Forward[1] = fwd.y; b.Forward[2] = fwd.z;
-			b.Right[0] = right.x; b.Right[1] = right.y; b.Right[2] = right.z;
-			b.Up[0] = up.x; b.Up[1] = up.y; b.Up[2] = up.z;
-			b.TanHalfFov = cam.tan_half_fov;
-			b.Aspect = (float)width / (float)height;
-		}
+		return RenderWith(p, nullptr, cameras, count, width, height, max_steps, epsilon, flags, depth, normals, colors, out_is_device,
+			stream);
+	}
+
+	TANGERINE_API tg_status tg_render_surrogate(tg_program* p, tg_surrogate* net, const tg_camera* cameras, int count, int width,
+		int height, int max_steps, float epsilon, float* depth, float* normals, uint8_t* colors, int out_is_device, void* stream)
+	{
+		if (!net) { SetError("null surrogate"); return TG_ERR_INVALID; }
+		return RenderWith(p, net, cameras, count, width, height, max_steps, epsilon, 0, depth, normals, colors, out_is_device, stream);
+	}
+
+	TANGERINE_API tg_status tg_last_render_steps(uint64_t* network_steps, uint64_t* exact_steps)
+	{
 		Engine& eng = Engine::Get();
-		std::lock_guard<std::mutex> lock(eng.Mutex);
-		cudaError_t e = eng.Render(*p, basis.data(), count, width, height, max_steps, epsilon, (flags & TG_RENDER_EXACT) != 0, depth,
-			normals, p->Host.Header.HasPaint ? colors : nullptr, out_is_device != 0, StreamOf(stream));
-		if (e != cudaSuccess) return CudaFail(e, "rendering");
-		if (colors && !p->Host.Header.HasPaint && !out_is_device)
-			std::memset(colors, 255, (size_t)width * height * count * 3);
+		if (network_steps) *network_steps = eng.LastNetworkSteps;
+		if (exact_steps) *exact_steps = eng.LastExactSteps;
 		return TG_OK;
 	}
 
@@ -1000,6 +1026,24 @@ extern "C"
 		da.Release(); db.Release(); dd.Release(); ds.Release();
 		if (e != cudaSuccess) return CudaFail(e, "tensor-core layout check");
 		if (status) { SetError("a tensor-core wait timed out"); return TG_ERR_CUDA; }
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_debug_blend_check(uint64_t n, uint64_t seed, uint64_t* counts)
+	{
+		if (!counts) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = eng.DefaultStream();
+		DeviceBuffer d;
+		unsigned long long host[3] = { 0, 0, 0 };
+		cudaError_t e = d.Reserve(3 * sizeof(unsigned long long));
+		if (e == cudaSuccess) e = LaunchBlendCheck(n, seed, d.As<unsigned long long>(), st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(host, d.Ptr, sizeof host, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		d.Release();
+		if (e != cudaSuccess) return CudaFail(e, "blend check");
+		for (int i = 0; i < 3; ++i) counts[i] = host[i];
 		return TG_OK;
 	}
 

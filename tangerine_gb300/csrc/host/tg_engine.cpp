@@ -466,7 +466,7 @@ namespace tg
 	}
 
 	cudaError_t Engine::Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
-		bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s)
+		bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s, const FieldNet* field)
 	{
 		const int64_t px = (int64_t)width * height * count;
 		if (px <= 0) return cudaSuccess;
@@ -482,9 +482,26 @@ namespace tg
 			dNormals = dDepth + px;
 			dColors = colors ? reinterpret_cast<uint8_t*>(dNormals + px * 3) : nullptr;
 		}
-		Begin("render", s);
-		TG_TRY(LaunchRender(p.View, Cameras.As<CameraBasis>(), count, width, height, steps, epsilon, exact, dDepth, dNormals, dColors, s));
-		End(s);
+		if (field)
+		{
+			TG_TRY(RenderCounters.Reserve(2 * sizeof(unsigned long long)));
+			TG_TRY(cudaMemsetAsync(RenderCounters.Ptr, 0, 2 * sizeof(unsigned long long), s));
+			// Network steps stop within a few network margins of the surface; exact steps finish.
+			const float margin = field->Info.MarginOverride >= 0.0f ? field->Info.MarginOverride : field->Info.Margin;
+			const float switchAt = margin > epsilon ? margin : epsilon;
+			TG_TRY(RayIn.Reserve((size_t)px * 8));
+			Begin("render_field", s);
+			TG_TRY(LaunchRenderField(p.View, Cameras.As<CameraBasis>(), count, width, height, steps, epsilon, field->Grid,
+				field->TablePtr(), field->ImagePtr(), margin, switchAt, RayIn.As<float>(), RayIn.As<uint32_t>() + px, dDepth, dNormals,
+				dColors, RenderCounters.As<unsigned long long>(), field->StatusPtr(), s));
+			End(s);
+		}
+		else
+		{
+			Begin("render", s);
+			TG_TRY(LaunchRender(p.View, Cameras.As<CameraBasis>(), count, width, height, steps, epsilon, exact, dDepth, dNormals, dColors, s));
+			End(s);
+		}
 		if (!out_is_device)
 		{
 			TG_TRY(cudaMemcpyAsync(depth, dDepth, (size_t)px * 4, cudaMemcpyDeviceToHost, s));
@@ -493,6 +510,14 @@ namespace tg
 		}
 		TG_TRY(cudaStreamSynchronize(s));
 		Collect();
+		if (field)
+		{
+			unsigned long long c[2] = { 0, 0 };
+			TG_TRY(cudaMemcpy(c, RenderCounters.Ptr, sizeof c, cudaMemcpyDeviceToHost));
+			LastNetworkSteps = c[0];
+			LastExactSteps = c[1];
+			TG_TRY(const_cast<FieldNet*>(field)->CheckStatus(s));
+		}
 		return cudaSuccess;
 	}
 }

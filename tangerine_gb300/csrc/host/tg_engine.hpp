@@ -78,7 +78,9 @@ namespace tg
 		cudaError_t RayMarch(const Program& p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
 			uint8_t* hit, float* travel, float* position, cudaStream_t s);
 		cudaError_t Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
-			bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s);
+			bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s, const FieldNet* field = nullptr);
+		// Network iterations and exact steps of the last network-stepped render.
+		uint64_t LastNetworkSteps = 0, LastExactSteps = 0;
 		DeviceBuffer& Lattice() { return LatticeBuf; }
 
 		// Profiling of kernel launches (CUDA events on the launching stream).
@@ -101,7 +103,7 @@ namespace tg
 		cudaStream_t Stream = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
 		DeviceBuffer Points, PointOut, BrickBits, BrickList, ProgramScratch, ActiveCells;
-		DeviceBuffer RayIn, RayOut, Cameras, Image;
+		DeviceBuffer RayIn, RayOut, Cameras, Image, RenderCounters;
 		void* Staging = nullptr;
 		size_t StagingBytes = 0;
 		uint32_t* HostCounts = nullptr;

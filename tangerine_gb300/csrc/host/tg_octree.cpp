@@ -1,6 +1,7 @@
 // Export octree construction and compilation of each octree cell's clipped subtree into
 // the GPU record format (tg_layout.hpp).
 #include "tg_octree.hpp"
+#include "tg_pool.hpp"
 
 #include <atomic>
 #include <chrono>
@@ -23,6 +24,7 @@ namespace tg
 			bool Terminus = false;
 			bool Incomplete = false;
 			bool ClippedAway = false;   // the clip to this cell's sphere returned null
+			bool Expanded = false;      // split into eight children
 			uint32_t NullOctants = 0;   // children whose clip returned null
 			int Leaves = 0;
 			NodeRef Eval;
@@ -34,69 +36,58 @@ namespace tg
 			float Target;
 			bool Coalesce;
 			int MaxDepth;
-			int ParallelDepth;
 		};
-
-		void Populate(TmpCell& c, const BuildParams& bp, int depth);
 
 		// SDFOctree ctor (sdf_evaluator.cpp:1641-1700): the cell's pivot is its min corner
 		// plus half the longest side; its evaluator is the parent's clipped to the sphere
 		// through the cube's corners.
-		std::unique_ptr<TmpCell> MakeCell(const NodeRef& in, AABB bounds, const BuildParams& bp, int depth)
+		void PlaceCell(TmpCell& c, float& span)
 		{
-			auto c = std::make_unique<TmpCell>();
-			c->Bounds = bounds;
-			const Vec3 e = bounds.Max - bounds.Min;
-			const float span = fmaxf(fmaxf(e.x, e.y), e.z);
+			const Vec3 e = c.Bounds.Max - c.Bounds.Min;
+			span = fmaxf(fmaxf(e.x, e.y), e.z);
 			const float half = (float)((double)span * 0.5);
-			c->Pivot = Vec3(half) + bounds.Min;
-			const float radius = (float)((double)Length(Vec3(span)) * 0.5);
-			c->Radius = radius;
-			c->Eval = in->Clip(c->Pivot, radius);
-			c->ClippedAway = !c->Eval;
-			c->Leaves = c->Eval ? c->Eval->LeafCount() : 0;
-			c->Terminus = span <= bp.Target || !c->Eval;
-			if (!c->Terminus)
-			{
-				c->Incomplete = true;
-				if (bp.Coalesce || bp.MaxDepth == -1 || depth < bp.MaxDepth)
-				{
-					Populate(*c, bp, depth);
-				}
-			}
-			return c;
+			c.Pivot = Vec3(half) + c.Bounds.Min;
+			c.Radius = (float)((double)Length(Vec3(span)) * 0.5);
 		}
 
-		// SDFOctree::Populate (sdf_evaluator.cpp:1703-1783): split at the pivot, drop empty
-		// children, shrink the bounds to the live ones, and merge the children back into
-		// this cell when they all ended and share one evaluator, or when few brushes remain.
-		void Populate(TmpCell& c, const BuildParams& bp, int depth)
+		void SetEvaluator(TmpCell& c, NodeRef eval, float span, const BuildParams& bp)
 		{
-			if (!c.Incomplete) return;
-			c.Incomplete = false;
-			AABB childBounds[8];
+			c.Eval = std::move(eval);
+			c.ClippedAway = !c.Eval;
+			c.Leaves = c.Eval ? c.Eval->LeafCount() : 0;
+			c.Terminus = span <= bp.Target || !c.Eval;
+			c.Incomplete = !c.Terminus;
+		}
+
+		void InitCell(TmpCell& c, const NodeRef& in, const BuildParams& bp)
+		{
+			float span;
+			PlaceCell(c, span);
+			SetEvaluator(c, in->Clip(c.Pivot, c.Radius), span, bp);
+		}
+
+		// The eight children of an expanded cell, their clips sharing one walk of its tree.
+		void InitChildren(TmpCell& parent, const BuildParams& bp)
+		{
+			Vec3 pivots[8];
+			float radii[8], spans[8];
 			for (int i = 0; i < 8; ++i)
 			{
-				AABB b = c.Bounds;
-				if (i & 1) b.Min.x = c.Pivot.x; else b.Max.x = c.Pivot.x;
-				if (i & 2) b.Min.y = c.Pivot.y; else b.Max.y = c.Pivot.y;
-				if (i & 4) b.Min.z = c.Pivot.z; else b.Max.z = c.Pivot.z;
-				childBounds[i] = b;
+				PlaceCell(*parent.Kids[i], spans[i]);
+				pivots[i] = parent.Kids[i]->Pivot;
+				radii[i] = parent.Kids[i]->Radius;
 			}
-			if (depth < bp.ParallelDepth)
-			{
-				std::future<std::unique_ptr<TmpCell>> jobs[8];
-				for (int i = 0; i < 8; ++i)
-				{
-					jobs[i] = std::async(std::launch::async, [&, i]() { return MakeCell(c.Eval, childBounds[i], bp, depth + 1); });
-				}
-				for (int i = 0; i < 8; ++i) c.Kids[i] = jobs[i].get();
-			}
-			else
-			{
-				for (int i = 0; i < 8; ++i) c.Kids[i] = MakeCell(c.Eval, childBounds[i], bp, depth + 1);
-			}
+			NodeRef evals[8];
+			parent.Eval->Clip8(pivots, radii, evals);
+			for (int i = 0; i < 8; ++i) SetEvaluator(*parent.Kids[i], std::move(evals[i]), spans[i], bp);
+		}
 
+		// The tail of SDFOctree::Populate (sdf_evaluator.cpp:1703-1783), once the children
+		// exist and are final themselves: drop empty children, shrink the bounds to the live
+		// ones, and merge the children back into this cell when they all ended and share
+		// one evaluator, or when few brushes remain.
+		void FinishCell(TmpCell& c, const BuildParams& bp, int depth)
+		{
 			bool uniform = true, penultimate = true;
 			int live = 0;
 			for (int i = 0; i < 8; ++i)
@@ -132,6 +123,52 @@ namespace tg
 				for (auto& k : c.Kids) k.reset();
 				c.Terminus = true;
 			}
+		}
+
+		// Post-order: children finish before their parent looks at them.
+		void FinishTree(TmpCell& c, const BuildParams& bp, int depth)
+		{
+			if (!c.Expanded) return;
+			for (auto& k : c.Kids) FinishTree(*k, bp, depth + 1);
+			FinishCell(c, bp, depth);
+		}
+
+		// SDFOctree::Populate's recursion, level by level: every cell of a level is clipped
+		// in parallel (the clips are independent), then the cells that go on split into
+		// eight children for the next level.  The merge decisions run afterwards, bottom up;
+		// they depend only on a cell's descendants, so the octree is the one the reference's
+		// depth-first recursion builds.
+		void BuildLevels(TmpCell& top, const BuildParams& bp, int top_depth)
+		{
+			std::vector<TmpCell*> level{ &top };
+			int depth = top_depth;
+			while (!level.empty())
+			{
+				std::vector<TmpCell*> parents;
+				for (TmpCell* c : level)
+				{
+					if (c->Terminus) continue;
+					if (!(bp.Coalesce || bp.MaxDepth == -1 || depth < bp.MaxDepth)) continue;
+					c->Incomplete = false;
+					c->Expanded = true;
+					for (int i = 0; i < 8; ++i)
+					{
+						AABB b = c->Bounds;
+						if (i & 1) b.Min.x = c->Pivot.x; else b.Max.x = c->Pivot.x;
+						if (i & 2) b.Min.y = c->Pivot.y; else b.Max.y = c->Pivot.y;
+						if (i & 4) b.Min.z = c->Pivot.z; else b.Max.z = c->Pivot.z;
+						c->Kids[i] = std::make_unique<TmpCell>();
+						c->Kids[i]->Bounds = b;
+					}
+					parents.push_back(c);
+				}
+				WorkerPool::Get().ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[j], bp); });
+				level.clear();
+				for (TmpCell* c : parents)
+					for (auto& k : c->Kids) level.push_back(k.get());
+				++depth;
+			}
+			FinishTree(top, bp, top_depth);
 		}
 
 		void Flatten(TmpCell& t, std::vector<Octree::Cell>& out)
@@ -174,9 +211,12 @@ namespace tg
 			cube.Max = cube.Max + Vec3(0.0f);
 		}
 		if (cube.Volume() == 0.0f) return false;
-		BuildParams bp{ target, coalesce, max_depth, 2 };
-		std::unique_ptr<TmpCell> top = MakeCell(root, cube, bp, 1);
+		BuildParams bp{ target, coalesce, max_depth };
+		auto top = std::make_unique<TmpCell>();
+		top->Bounds = cube;
+		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
+		BuildLevels(*top, bp, 1);
 		Flatten(*top, Cells);
 		return true;
 	}

@@ -126,9 +126,57 @@ namespace tg
 		return (float)(subtract ? (double)m - q : (double)m + q);
 	}
 
+#if defined(__CUDACC__)
+	// The blend term's double result rounded to float, computed in float where that is
+	// provably the same value (GPU only; the double path stays the reference).
+	//
+	// With a = hh/4 (exact), q = a/k is taken as qh + ql: qh = RN(a/k), the remainder
+	// r = a - qh*k is exact (one fused multiply-add), ql = RN(r/k), so |q - qh - ql| <=
+	// 2^-48 |qh|.  TwoSum gives m -+ qh = s + e exactly; t = RN(e -+ ql); TwoSum gives
+	// s + t = R + w exactly with R = RN(s + t).  The reference's value d = RN53(m -+ RN53(q))
+	// then satisfies |d - (R + w)| <= 2^-46 (|m| + |qh| + |R|) (the two float roundings
+	// above at 2^-48 each, the two double roundings at 2^-53), so when |w| plus that bound
+	// stays below half the gap around R -- a quarter ulp when |R| is a power of two, where
+	// the gap below is half as wide -- RN24(d) = R exactly.  Otherwise, or outside the
+	// ranges where the steps above are exact (tiny or huge operands, non-finite values),
+	// the caller takes the double path.  Failing the test is rare (about 2^-22 (|m| + |q|)
+	// / |R| of the evaluations).
+	__device__ __forceinline__ bool BlendTermFloat(float m, float hh, float k, bool subtract, float& out)
+	{
+		if (!(hh >= 0x1p-100f && hh <= 0x1p100f && k >= 0x1p-100f && k <= 0x1p100f)) return false;
+		const float a = hh * 0.25f;
+		const float qh = __fdiv_rn(a, k);
+		const float aq = fabsf(qh);
+		if (!(aq >= 0x1p-100f && aq <= 0x1p100f)) return false;
+		const float r = __fmaf_rn(-qh, k, a);
+		const float ql = __fdiv_rn(r, k);
+		const float b = subtract ? -qh : qh;
+		const float bl = subtract ? -ql : ql;
+		const float s = __fadd_rn(m, b);
+		const float bp = __fsub_rn(s, m);
+		const float e = __fadd_rn(__fsub_rn(m, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+		const float t = __fadd_rn(e, bl);
+		const float R = __fadd_rn(s, t);
+		const float tp = __fsub_rn(R, s);
+		const float w = __fadd_rn(__fsub_rn(s, __fsub_rn(R, tp)), __fsub_rn(t, tp));
+		const uint32_t bits = __float_as_uint(R) & 0x7FFFFFFFu;
+		if (bits < (25u << 23) || bits >= (0xFFu << 23)) return false;
+		const float ulp = __uint_as_float((bits & 0x7F800000u) - (23u << 23));
+		const float half = (bits & 0x007FFFFFu) ? 0.5f * ulp : 0.25f * ulp;
+		const float bound = 0x1p-46f * __fadd_rn(__fadd_rn(fabsf(m), aq), fabsf(R));
+		if (!(__fadd_rn(fabsf(w), bound) < half)) return false;
+		out = R;
+		return true;
+	}
+#endif
+
 	TG_HD float BlendTerm(float m, float h, float k, bool subtract)
 	{
 		if (h == 0.0f && k > 0.0f) return subtract ? m - 0.0f : m + 0.0f;
+#if defined(__CUDA_ARCH__)
+		float fast;
+		if (BlendTermFloat(m, h * h, k, subtract, fast)) return fast;
+#endif
 		return BlendTermDouble(m, h, k, subtract);
 	}
 

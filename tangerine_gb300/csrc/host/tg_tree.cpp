@@ -5,6 +5,7 @@
 #include <cmath>
 #include <limits>
 #include <unordered_map>
+#include <vector>
 
 namespace tg
 {
@@ -46,14 +47,78 @@ namespace tg
 		// order) in time linear in the tree.
 		struct PointEvaluations
 		{
+			// Open-addressing table keyed by node address; entries of earlier points are
+			// told apart by a per-thread epoch, so no clearing between clips.
+			struct Slot
+			{
+				const Node* Key;
+				float Value;
+				uint32_t Epoch;
+			};
+			static thread_local std::vector<Slot> Table;
+			static thread_local uint32_t Epoch;
 			Vec3 P;
-			std::unordered_map<const Node*, float> Values;
+			uint32_t Used = 0;
+
+			explicit PointEvaluations(Vec3 p) : P(p)
+			{
+				if (Table.empty()) Table.assign(4096, Slot{ nullptr, 0.0f, 0 });
+				if (++Epoch == 0)
+				{
+					for (Slot& s : Table) s.Epoch = 0;
+					Epoch = 1;
+				}
+			}
+
+			static size_t HashOf(const Node* n, size_t mask)
+			{
+				uint64_t x = (uint64_t)(uintptr_t)n;
+				x ^= x >> 33;
+				x *= 0xff51afd7ed558ccdull;
+				x ^= x >> 33;
+				return (size_t)x & mask;
+			}
+
+			bool Find(const Node* n, float& v) const
+			{
+				const size_t mask = Table.size() - 1;
+				for (size_t i = HashOf(n, mask);; i = (i + 1) & mask)
+				{
+					const Slot& s = Table[i];
+					if (s.Epoch != Epoch) return false;
+					if (s.Key == n) { v = s.Value; return true; }
+				}
+			}
+
+			void Insert(const Node* n, float v)
+			{
+				if (2 * (Used + 1) > Table.size()) Grow();
+				const size_t mask = Table.size() - 1;
+				size_t i = HashOf(n, mask);
+				while (Table[i].Epoch == Epoch) i = (i + 1) & mask;
+				Table[i] = Slot{ n, v, Epoch };
+				++Used;
+			}
+
+			void Grow()
+			{
+				std::vector<Slot> old;
+				old.swap(Table);
+				Table.assign(old.size() * 2, Slot{ nullptr, 0.0f, 0 });
+				const size_t mask = Table.size() - 1;
+				for (const Slot& s : old)
+				{
+					if (s.Epoch != Epoch) continue;
+					size_t i = HashOf(s.Key, mask);
+					while (Table[i].Epoch == Epoch) i = (i + 1) & mask;
+					Table[i] = s;
+				}
+			}
 
 			float At(const Node& n)
 			{
-				auto it = Values.find(&n);
-				if (it != Values.end()) return it->second;
 				float v = 0.0f;
+				if (Find(&n, v)) return v;
 				switch (n.Kind)
 				{
 				case NodeKind::Brush: v = BrushDistance(n.Op, n.Params, n.Xf.ApplyInv(P)) * n.Xf.Scalation; break;
@@ -61,15 +126,150 @@ namespace tg
 				case NodeKind::Flate: v = At(*n.Lhs) - n.Threshold; break;
 				case NodeKind::Stencil: v = At(*n.Lhs); break;
 				}
-				Values.emplace(&n, v);
+				Insert(&n, v);
 				return v;
 			}
 		};
 
+		thread_local std::vector<PointEvaluations::Slot> PointEvaluations::Table;
+		thread_local uint32_t PointEvaluations::Epoch = 0;
+
+		// The same evaluations at eight points at once (the eight children of an octree
+		// cell clip their parent's tree at their own pivots): one walk of the tree, one
+		// table lookup per node, one quaternion inverse per brush for all eight points.
+		struct Evaluations8
+		{
+			struct Slot
+			{
+				const Node* Key;
+				uint32_t Index;
+				uint32_t Epoch;
+			};
+			static thread_local std::vector<Slot> Table;
+			static thread_local uint32_t Epoch;
+			Vec3 P[8];
+			std::vector<float> Values;
+			uint32_t Used = 0;
+
+			explicit Evaluations8(const Vec3 (&p)[8])
+			{
+				for (int i = 0; i < 8; ++i) P[i] = p[i];
+				if (Table.empty()) Table.assign(4096, Slot{ nullptr, 0, 0 });
+				if (++Epoch == 0)
+				{
+					for (Slot& s : Table) s.Epoch = 0;
+					Epoch = 1;
+				}
+				Values.reserve(8 * 1024);
+			}
+
+			static size_t HashOf(const Node* n, size_t mask)
+			{
+				uint64_t x = (uint64_t)(uintptr_t)n;
+				x ^= x >> 33;
+				x *= 0xff51afd7ed558ccdull;
+				x ^= x >> 33;
+				return (size_t)x & mask;
+			}
+
+			void Grow()
+			{
+				std::vector<Slot> old;
+				old.swap(Table);
+				Table.assign(old.size() * 2, Slot{ nullptr, 0, 0 });
+				const size_t mask = Table.size() - 1;
+				for (const Slot& s : old)
+				{
+					if (s.Epoch != Epoch) continue;
+					size_t i = HashOf(s.Key, mask);
+					while (Table[i].Epoch == Epoch) i = (i + 1) & mask;
+					Table[i] = s;
+				}
+			}
+
+			// Index (into Values, x8) of the node's eight values, computed on first use.
+			uint32_t Index(const Node& n)
+			{
+				{
+					const size_t mask = Table.size() - 1;
+					for (size_t i = HashOf(&n, mask);; i = (i + 1) & mask)
+					{
+						const Slot& s = Table[i];
+						if (s.Epoch != Epoch) break;
+						if (s.Key == &n) return s.Index;
+					}
+				}
+				float v[8];
+				switch (n.Kind)
+				{
+				case NodeKind::Brush:
+				{
+					// Transform::ApplyInv with the rotation's inverse taken once.
+					const Quat inv = Inverse(n.Xf.Rotation);
+					for (int i = 0; i < 8; ++i)
+					{
+						const Vec3 q = tg::Rotate(inv, P[i] - n.Xf.Translation) / n.Xf.Scalation;
+						v[i] = BrushDistance(n.Op, n.Params, q) * n.Xf.Scalation;
+					}
+					break;
+				}
+				case NodeKind::Set:
+				{
+					const uint32_t li = Index(*n.Lhs);
+					float l[8];
+					for (int i = 0; i < 8; ++i) l[i] = Values[8 * li + i];
+					const uint32_t ri = Index(*n.Rhs);
+					for (int i = 0; i < 8; ++i) v[i] = SetDistance(n.Op, l[i], Values[8 * ri + i], n.Threshold);
+					break;
+				}
+				case NodeKind::Flate:
+				{
+					const uint32_t ci = Index(*n.Lhs);
+					for (int i = 0; i < 8; ++i) v[i] = Values[8 * ci + i] - n.Threshold;
+					break;
+				}
+				case NodeKind::Stencil:
+				{
+					const uint32_t ci = Index(*n.Lhs);
+					for (int i = 0; i < 8; ++i) v[i] = Values[8 * ci + i];
+					break;
+				}
+				}
+				const uint32_t index = (uint32_t)(Values.size() / 8);
+				Values.insert(Values.end(), v, v + 8);
+				if (2 * (Used + 1) > Table.size()) Grow();
+				const size_t mask = Table.size() - 1;
+				size_t i = HashOf(&n, mask);
+				while (Table[i].Epoch == Epoch) i = (i + 1) & mask;
+				Table[i] = Slot{ &n, index, Epoch };
+				++Used;
+				return index;
+			}
+		};
+
+		thread_local std::vector<Evaluations8::Slot> Evaluations8::Table;
+		thread_local uint32_t Evaluations8::Epoch = 0;
+
+		struct LaneOf8
+		{
+			Evaluations8& E;
+			int Lane;
+			float At(const Node& n) { const uint32_t i = E.Index(n); return E.Values[8 * i + Lane]; }
+		};
+
+		// A set node whose clipped operands are its own operands is kept as it is (the
+		// node MakeSet would build from them is the same node).
+		NodeRef RebuildSet(const Node& n, NodeRef l, NodeRef r)
+		{
+			if (l.get() == n.Lhs.get() && r.get() == n.Rhs.get()) return NodeRef::Share(const_cast<Node*>(&n));
+			return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
+		}
+
 		// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
 		// that can matter inside the sphere (p, radius).  Union keeps whichever side is near,
 		// Diff keeps its left side, Inter needs both; blending widens the sphere by k.
-		NodeRef ClipAt(const Node& n, float radius, PointEvaluations& ev)
+		template<typename Ev>
+		NodeRef ClipAt(const Node& n, float radius, Ev& ev)
 		{
 			switch (n.Kind)
 			{
@@ -98,13 +298,13 @@ namespace tg
 					const float wide = radius + n.Threshold;
 					NodeRef l = ClipAt(*n.Lhs, wide, ev);
 					NodeRef r = ClipAt(*n.Rhs, wide, ev);
-					if (l && r) return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
+					if (l && r) return RebuildSet(n, std::move(l), std::move(r));
 					if (!unionFamily && !diffFamily) return NodeRef();
 				}
 				NodeRef l = ClipAt(*n.Lhs, radius, ev);
 				NodeRef r = ClipAt(*n.Rhs, radius, ev);
-				if (l && r) return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
-				if (unionFamily) return l ? l : r;
+				if (l && r) return RebuildSet(n, std::move(l), std::move(r));
+				if (unionFamily) return l ? std::move(l) : std::move(r);
 				if (diffFamily) return l;
 				return NodeRef();
 			}
@@ -115,8 +315,18 @@ namespace tg
 
 	NodeRef Node::Clip(Vec3 p, float radius) const
 	{
-		PointEvaluations ev{ p, {} };
+		PointEvaluations ev(p);
 		return ClipAt(*this, radius, ev);
+	}
+
+	void Node::Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8]) const
+	{
+		Evaluations8 ev(p);
+		for (int i = 0; i < 8; ++i)
+		{
+			LaneOf8 lane{ ev, i };
+			out[i] = ClipAt(*this, radius[i], lane);
+		}
 	}
 
 	AABB Node::Bounds() const { return BoundsImpl(false); }

@@ -73,6 +73,8 @@ namespace tg
 
 		float Eval(Vec3 p) const;
 		NodeRef Clip(Vec3 p, float radius) const;
+		// Clip to eight spheres at once (the same result as eight Clip calls).
+		void Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8]) const;
 		AABB Bounds() const;
 		AABB InnerBounds() const;
 		void Move(Vec3 by);

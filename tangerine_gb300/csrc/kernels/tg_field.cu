@@ -28,6 +28,7 @@
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
 #include "tg_tc.cuh"
+#include "tg_trace.cuh"
 
 namespace tg
 {
@@ -734,6 +735,151 @@ namespace tg
 			Teardown(p, kInferColumns, failed, status);
 		}
 
+		// ---- sphere tracing with network steps ------------------------------------------
+		//
+		// Approach: a CTA marches 128 rays (one per thread) in lockstep; every iteration the
+		// network runs once at all of them (one tensor-core tile).  A ray steps by the larger
+		// of two lower bounds of the whole tree's distance: the distance to the root cube, and
+		// the network's value less `margin` (safety x its largest held-out error).  When that
+		// bound falls to `switch_at` the ray stops and records where (travel, iterations
+		// used); a ray that leaves the root sphere has missed.  Finish (a separate, lighter
+		// kernel with many more resident warps for the divergent part): the reference's exact
+		// steps (SDFNode::RayMarch on the whole tree) from there, so every hit is the exact
+		// program's, shaded with the whole tree's gradient and material.  The step budget is
+		// shared: network iterations plus exact steps never exceed `steps`.
+		__device__ __forceinline__ Vec3 PixelRay(const CameraBasis& cam, int x, int y, int width, int height, Vec3& start)
+		{
+			const float u = ((2.0f * ((float)x + 0.5f) / (float)width) - 1.0f) * cam.TanHalfFov * cam.Aspect;
+			const float v = (1.0f - 2.0f * ((float)y + 0.5f) / (float)height) * cam.TanHalfFov;
+			const Vec3 fwd(cam.Forward[0], cam.Forward[1], cam.Forward[2]);
+			const Vec3 right(cam.Right[0], cam.Right[1], cam.Right[2]);
+			const Vec3 up(cam.Up[0], cam.Up[1], cam.Up[2]);
+			start = Vec3(cam.Position[0], cam.Position[1], cam.Position[2]);
+			return Normalize((fwd + right * u) + up * v);
+		}
+
+		__global__ void __launch_bounds__(kRows) ApproachFieldKernel(DeviceProgram prog, const CameraBasis* __restrict__ cams, int count,
+			int width, int height, int steps, FieldGrid G, const float2* __restrict__ table, const uint8_t* __restrict__ image,
+			float margin, float switch_at, float* __restrict__ travel_out, uint32_t* __restrict__ state_out,
+			unsigned long long* __restrict__ counters, int* status)
+		{
+			extern __shared__ __align__(128) uint8_t smem[];
+			InferSmem& S = *reinterpret_cast<InferSmem*>(smem);
+			const int64_t pixels = (int64_t)width * height;
+			const int64_t total = pixels * count;
+			const int64_t tiles = (total + kRows - 1) / kRows;
+			Pipe p;
+			bool failed = !Setup(&S.TmemSlot, S.Bars, S.Image, image, kInferColumns, p);
+			unsigned long long netSteps = 0;
+			for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+			{
+				if (StageSync(failed)) { failed = true; break; }
+				const int64_t t = tile * kRows + threadIdx.x;
+				const bool valid = t < total;
+				const int64_t tc = valid ? t : total - 1;
+				const int c = (int)(tc / pixels);
+				const int64_t pix = tc % pixels;
+				Vec3 start;
+				const Vec3 dir = PixelRay(cams[c], (int)(pix % width), (int)(pix / width), width, height, start);
+				const float exitTravel = RootSphereExit(prog, start, dir);
+				int mode = (valid && exitTravel >= 0.0f) ? 0 : 2;        // 0 network steps, 1 exact steps next, 2 missed
+				float travel = 0.0f;
+				int used = 0;
+				for (int it = 0; it < steps; ++it)
+				{
+					if (!__syncthreads_or(mode == 0)) break;
+					const Vec3 pos = dir * travel + start;
+					float uu[3];
+					UnitCoords(G, pos.x, pos.y, pos.z, uu);
+					float s;
+					if (!ForwardTile(G, table, S, p, uu, s)) { failed = true; break; }
+					if (mode != 0) continue;
+					++used;
+					const bool inDomain = (pos.x - G.Lo[0]) * G.Scale[0] >= 0.0f && (pos.x - G.Lo[0]) * G.Scale[0] <= 1.0f &&
+						(pos.y - G.Lo[1]) * G.Scale[1] >= 0.0f && (pos.y - G.Lo[1]) * G.Scale[1] <= 1.0f &&
+						(pos.z - G.Lo[2]) * G.Scale[2] >= 0.0f && (pos.z - G.Lo[2]) * G.Scale[2] <= 1.0f;
+					const float bound = fmaxf(RootCubeDistance(prog, pos), inDomain && prog.Lipschitz ? s - margin : 0.0f);
+					if (bound > switch_at)
+					{
+						travel = travel + bound;
+						if (travel > exitTravel) mode = 2;
+					}
+					else mode = 1;
+				}
+				if (failed) break;
+				netSteps += (unsigned long long)used;
+				if (valid)
+				{
+					travel_out[t] = travel;
+					state_out[t] = (uint32_t)used | ((uint32_t)mode << 16);
+				}
+			}
+			if (counters) atomicAdd(counters, netSteps);
+			Teardown(p, kInferColumns, failed, status);
+		}
+
+		constexpr int kFinishThreads = 128;
+
+		__global__ void __launch_bounds__(kFinishThreads) FinishFieldKernel(DeviceProgram prog, const CameraBasis* __restrict__ cams,
+			int count, int width, int height, int steps, float epsilon, const float* __restrict__ travel_in,
+			const uint32_t* __restrict__ state_in, float* __restrict__ depth, float* __restrict__ normals, uint8_t* __restrict__ colors,
+			unsigned long long* __restrict__ counters)
+		{
+			extern __shared__ float spill[];
+			const int64_t pixels = (int64_t)width * height;
+			const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+			const bool valid = t < pixels * count;
+			unsigned exactSteps = 0;
+			if (valid)
+			{
+				const int c = (int)(t / pixels);
+				const int64_t pix = t % pixels;
+				Vec3 start;
+				const Vec3 dir = PixelRay(cams[c], (int)(pix % width), (int)(pix / width), width, height, start);
+				const uint32_t state = state_in[t];
+				const int used = (int)(state & 0xFFFFu), mode = (int)(state >> 16);
+				float travel = travel_in[t];
+				bool hit = false;
+				Vec3 hitPos(0.0f, 0.0f, 0.0f);
+				if (mode == 1)
+				{
+					const float exitTravel = RootSphereExit(prog, start, dir);
+					Vec3 pos = dir * travel + start;
+					for (int i = used; i < steps; ++i)
+					{
+						const float d = TraceSurfaceAt(prog, prog.FullSurfaceCode, pos, false, nullptr, spill + threadIdx.x, kFinishThreads);
+						++exactSteps;
+						if (d <= epsilon) { hit = true; hitPos = pos; break; }
+						travel = travel + d;
+						if (travel > exitTravel) break;
+						pos = dir * travel + start;
+					}
+				}
+				Vec3 n(0.0f, 0.0f, 0.0f);
+				uchar4 col = make_uchar4(0, 0, 0, 0);
+				if (hit)
+				{
+					int mat = -1;
+					n = TraceShade(prog, prog.FullSurfaceCode, hitPos, colors != nullptr, &mat, spill + threadIdx.x, kFinishThreads);
+					col = mat >= 0 ? prog.Colors[mat] : make_uchar4(255, 255, 255, 255);
+				}
+				depth[t] = hit ? travel : INFINITY;
+				normals[t * 3] = n.x;
+				normals[t * 3 + 1] = n.y;
+				normals[t * 3 + 2] = n.z;
+				if (colors)
+				{
+					colors[t * 3] = col.x;
+					colors[t * 3 + 1] = col.y;
+					colors[t * 3 + 2] = col.z;
+				}
+			}
+			// One atomic per warp (blocks are whole warps; every lane gets here).
+			const unsigned w = __reduce_add_sync(0xFFFFFFFFu, exactSteps);
+			if (counters && (threadIdx.x & 31) == 0 && w) atomicAdd(counters + 1, (unsigned long long)w);
+		}
+
+
 		// ---- operand-layout check --------------------------------------------------------
 
 		struct alignas(16) DebugSmem
@@ -914,6 +1060,32 @@ namespace tg
 		const int64_t tiles = (nb + kRows - 1) / kRows;
 		const int blocks = (int)(tiles < (int64_t)SmCount() * 4 ? tiles : (int64_t)SmCount() * 4);
 		FieldClassifyKernel<<<blocks, kRows, sizeof(InferSmem), stream>>>(prog, g, bg, grid, table, image, margin, brick_bits, status);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchRenderField(const DeviceProgram& prog, const CameraBasis* cameras, int count, int width, int height, int steps,
+		float epsilon, const FieldGrid& grid, const float2* table, const uint8_t* image, float margin, float switch_at, float* travel,
+		uint32_t* state, float* depth, float* normals, uint8_t* colors, unsigned long long* counters, int* status, cudaStream_t stream)
+	{
+		const int64_t total = (int64_t)width * height * count;
+		if (total <= 0) return cudaSuccess;
+		cudaError_t e = AllowSmem(ApproachFieldKernel, sizeof(InferSmem));
+		if (e != cudaSuccess) return e;
+		const int64_t tiles = (total + kRows - 1) / kRows;
+		const int blocks = (int)(tiles < (int64_t)SmCount() * 4 ? tiles : (int64_t)SmCount() * 4);
+		ApproachFieldKernel<<<blocks, kRows, sizeof(InferSmem), stream>>>(prog, cameras, count, width, height, steps, grid, table, image,
+			margin, switch_at, travel, state, counters, status);
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+		const int depthStack = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+		const size_t smem = (size_t)depthStack * 2 * kFinishThreads * sizeof(float);
+		if (smem > 48 * 1024)
+		{
+			e = AllowSmem(FinishFieldKernel, smem);
+			if (e != cudaSuccess) return e;
+		}
+		FinishFieldKernel<<<(unsigned)((total + kFinishThreads - 1) / kFinishThreads), kFinishThreads, smem, stream>>>(prog, cameras,
+			count, width, height, steps, epsilon, travel, state, depth, normals, colors, counters);
 		return cudaGetLastError();
 	}
 

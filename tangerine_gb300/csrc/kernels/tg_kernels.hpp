@@ -93,6 +93,10 @@ namespace tg
 	cudaError_t LaunchFaceNormals(const DeviceProgram& prog, const float* vertices, const uint32_t* faces, uint64_t face_count,
 		float* normals, cudaStream_t stream);
 
+	// Self-check of the float blend-term evaluation against the double expression over n
+	// seeded inputs (each both signs of the term): counts = checked, mismatches, fallbacks.
+	cudaError_t LaunchBlendCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream);
+
 	// Achieved FP32 fused-multiply-add throughput of this GPU (TFLOP/s, 2 flops per FMA).
 	cudaError_t MeasureFp32Peak(double* tflops, cudaStream_t stream);
 
@@ -166,6 +170,12 @@ namespace tg
 	// ball's radius plus `margin` or it misses the root cube (as LaunchClassifyBricks).
 	cudaError_t LaunchFieldClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, const FieldGrid& grid,
 		const float2* table, const uint8_t* image, float margin, uint32_t* brick_bits, int* status, cudaStream_t stream);
+	// Sphere tracing with network steps and exact final steps (see tg_field.cu); counters
+	// (optional) accumulate network iterations and exact steps.
+	// travel/state: per-ray scratch (count*width*height each) between the two kernels.
+	cudaError_t LaunchRenderField(const DeviceProgram& prog, const CameraBasis* cameras, int count, int width, int height, int steps,
+		float epsilon, const FieldGrid& grid, const float2* table, const uint8_t* image, float margin, float switch_at, float* travel,
+		uint32_t* state, float* depth, float* normals, uint8_t* colors, unsigned long long* counters, int* status, cudaStream_t stream);
 	// Tensor-core operand-layout check: D = A * B^T through the descriptors the network
 	// kernels use.  mode 0: A 128x64 and B 64x64 read K-major; mode 1: A = a^T and
 	// B = b^T for a 128x128 and b 128x144 read MN-major (K = 128 rows); mode 2: A 128x64

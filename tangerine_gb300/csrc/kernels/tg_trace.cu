@@ -17,6 +17,7 @@
 
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
+#include "tg_trace.cuh"
 
 namespace tg
 {
@@ -24,59 +25,11 @@ namespace tg
 	{
 		constexpr int kTraceThreads = 128;
 
-		__device__ __forceinline__ float SurfaceAt(const DeviceProgram& prog, int pc, Vec3 p, bool material, int* m, float* spill)
-		{
-			const float px[1] = { p.x }, py[1] = { p.y }, pz[1] = { p.z };
-			float e[1];
-			RunSurfaceBatch<1>(prog.Code, pc, px, py, pz, e, material ? 0 : -1, m, spill, kTraceThreads);
-			return e[0];
-		}
-
-		// SDFNode::Gradient (sdf_evaluator.cpp:298-333) and, with colours, GetMaterial.
-		__device__ __forceinline__ Vec3 Shade(const DeviceProgram& prog, int pc, Vec3 p, bool material, int* m, float* spill)
-		{
-			const float h = 0.0001f;
-			const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
-			const float e0 = SurfaceAt(prog, pc, p + xyy, false, nullptr, spill);
-			const float e1 = SurfaceAt(prog, pc, p + yyx, false, nullptr, spill);
-			const float e2 = SurfaceAt(prog, pc, p + yxy, false, nullptr, spill);
-			const float e3 = SurfaceAt(prog, pc, p + xxx, false, nullptr, spill);
-			Vec3 g = xyy * e0;
-			g = g + yyx * e1;
-			g = g + yxy * e2;
-			g = g + xxx * e3;
-			const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
-			if (material) SurfaceAt(prog, pc, p, true, m, spill);
-			if (ls == 0.0f)
-			{
-				const float d = SurfaceAt(prog, pc, p, false, nullptr, spill);
-				return Normalize(Vec3(e0 - d, e2 - d, e1 - d));
-			}
-			return g / sqrtf(ls);
-		}
-
-		struct March
-		{
-			bool Hit;
-			float Travel;
-			Vec3 Position;
-		};
-
 		// SDFNode::RayMarch on the whole tree.
 		__device__ __forceinline__ March MarchExact(const DeviceProgram& prog, Vec3 start, Vec3 dir_in, int iterations, float epsilon,
 			float* spill)
 		{
-			const Vec3 dir = Normalize(dir_in);
-			Vec3 pos = start;
-			float travel = 0.0f;
-			for (int i = 0; i < iterations; ++i)
-			{
-				const float d = SurfaceAt(prog, prog.FullSurfaceCode, pos, false, nullptr, spill);
-				if (d <= epsilon) return { true, travel, pos };
-				travel = travel + d;
-				pos = dir * travel + start;
-			}
-			return { false, INFINITY, pos };
+			return TraceExactFrom(prog, start, Normalize(dir_in), 0.0f, iterations, epsilon, spill, kTraceThreads);
 		}
 
 		__device__ __forceinline__ March MarchBounded(const DeviceProgram& prog, Vec3 start, Vec3 dir_in, int iterations, float epsilon,
@@ -164,7 +117,7 @@ namespace tg
 				const int pc = exact ? prog.FullSurfaceCode
 					: __ldg(&prog.Nodes[DescendOctree(prog.Nodes, m.Position.x, m.Position.y, m.Position.z)].SurfaceCode);
 				int mat = -1;
-				n = Shade(prog, pc, m.Position, colors != nullptr, &mat, my);
+				n = TraceShade(prog, pc, m.Position, colors != nullptr, &mat, my, kTraceThreads);
 				col = mat >= 0 ? prog.Colors[mat] : make_uchar4(255, 255, 255, 255);
 			}
 			normals[t * 3] = n.x;

@@ -427,6 +427,16 @@ class Surrogate:
     def set_margin(self, margin):
         check(load().tg_surrogate_set_margin(self.ptr, float(margin)), "tg_surrogate_set_margin")
 
+    def render(self, program: Program, cams, width, height, steps=256, epsilon=1e-4, stream=None):
+        """(depth, normals, colors) with network steps and exact final steps."""
+        n = len(cams)
+        depth = np.empty((n, height, width), np.float32)
+        normals = np.empty((n, height, width, 3), np.float32)
+        colors = np.empty((n, height, width, 3), np.uint8)
+        check(load().tg_render_surrogate(program.ptr, self.ptr, cams, n, width, height, steps, epsilon, _lib.as_ptr(depth),
+                                         _lib.as_ptr(normals), _lib.as_ptr(colors), 0, stream), "tg_render_surrogate")
+        return depth, normals, colors
+
     def export_mesh(self, program: Program, grid, attributes=True, brick=0, lanes=0, only=False, stream=None) -> Mesh:
         """only: the network alone decides (no exact test of the bricks it keeps)."""
         g = _grid(grid)
@@ -443,6 +453,13 @@ class Surrogate:
                                                      _flags(attributes, False, brick, lanes, only), C.byref(dm), stream),
               "tg_export_mesh_surrogate_device")
         return dm
+
+
+def last_render_steps():
+    """(network iterations, exact steps) of the last network-stepped render."""
+    a, b = C.c_uint64(), C.c_uint64()
+    load().tg_last_render_steps(C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def debug_mma(mode: int, a, b) -> np.ndarray:

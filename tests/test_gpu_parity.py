@@ -247,3 +247,14 @@ def test_edge_cases(lib):
             prog.export_mesh(_lib.Grid(0, 0, 0, -0.1, 4, 4, 4))
     with pytest.raises(_lib.TangerineError):
         sdf.compile(sdf.plane(0, 0, 1))
+
+
+def test_float_blend_term_equals_double(lib):
+    """The GPU's float evaluation of the smooth-blend term returns exactly the reference's
+    double expression rounded to float wherever it does not defer to the double path."""
+    from tangerine_gb300 import _lib
+    counts = np.zeros(3, np.uint64)
+    _lib.check(lib.tg_debug_blend_check(1 << 26, 12345, _lib.as_ptr(counts)), "tg_debug_blend_check")
+    checked, mismatches, fallbacks = (int(c) for c in counts)
+    assert mismatches == 0, counts
+    assert checked > (1 << 26)          # most inputs take the float path

@@ -125,3 +125,26 @@ def test_trained_bound_culls_bricks_and_keeps_the_mesh(lib):
     assert kept < 0.5 * bricks, (kept, bricks)
     # With the exact test after it, the network can only remove bricks from the exact set.
     assert kept_refined <= kept_exact, (kept_refined, kept_exact)
+
+
+def test_network_steps_render_matches_exact(lib):
+    """Sphere tracing with network steps and exact final steps finds the exact tracer's
+    surface: hit masks agree but for grazing rays, depths within 2e-3 where both hit."""
+    spec = W.random_tree(3, 64)
+    poses = W.camera_poses(3, 2, radius=4.0)
+    cams = sdf.cameras(poses, fov_y_degrees=60.0)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        s = sdf.Surrogate(samples=1 << 20, steps=400, batch=1 << 16, validation=1 << 18)
+        s.fit(prog)
+        d_exact, n_exact, c_exact = prog.render(cams, 96, 64, 256, 1e-4, exact=True)
+        d_net, n_net, c_net = s.render(prog, cams, 96, 64, 256, 1e-4)
+        net_steps, exact_steps = sdf.last_render_steps()
+        s.close()
+    hit_e, hit_n = np.isfinite(d_exact), np.isfinite(d_net)
+    assert hit_e.any()
+    assert np.mean(hit_e != hit_n) <= 0.01
+    both = hit_e & hit_n
+    assert np.max(np.abs(d_exact[both] - d_net[both])) <= 2e-3
+    same_colour = np.all(c_exact[both] == c_net[both], axis=-1)
+    assert np.mean(same_colour) >= 0.95
+    assert net_steps > 0 and exact_steps > 0
