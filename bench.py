@@ -163,15 +163,58 @@ def measured_peaks():
     return {}
 
 
-def committed_traffic():
-    """Per-launch DRAM bytes of the interpreter from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "eval_grid_traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except json.JSONDecodeError:
-            return None
+def committed_traffic(kernel: str):
+    """Per-launch DRAM bytes (read + write) of a kernel from the committed ncu summaries:
+    lines `traffic <kernel>: <bytes> bytes per launch`."""
+    import re
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        for line in p.read_text().splitlines():
+            m = re.match(r"^traffic (\w+): (\d+) bytes per launch", line.strip())
+            if m and m.group(1) == kernel:
+                return {"bytes_per_launch": int(m.group(2)), "source": f"profiles/{p.name}"}
     return None
+
+
+def cost_lattice(cells, children, words, grid):
+    """int32 lattice (z, y, x) of the flops of the program SDFOctree::Eval runs at each
+    lattice point: each octree cell's program over its index box, children overriding."""
+    f = np.float32
+    axes = [f(o) + np.arange(n, dtype=np.int64).astype(f) * f(grid.step)
+            for o, n in ((grid.x0, grid.sx + 1), (grid.y0, grid.sy + 1), (grid.z0, grid.sz + 1))]
+    flops_of = [program_flops(words[int(c[11]): int(c[11]) + int(c[12])]) for c in cells]
+    cost = np.zeros((axes[2].size, axes[1].size, axes[0].size), np.int32)
+    stack = [(0, (0, axes[0].size), (0, axes[1].size), (0, axes[2].size))]
+    while stack:
+        node, bx, by, bz = stack.pop()
+        if bx[1] <= bx[0] or by[1] <= by[0] or bz[1] <= bz[0]:
+            continue
+        cost[bz[0]:bz[1], by[0]:by[1], bx[0]:bx[1]] = flops_of[node]
+        if cells[node][9] != 0:
+            continue
+        piv = cells[node][:3]
+        splits = [int(np.searchsorted(axes[a], f(piv[a]), side="right")) for a in range(3)]
+        for octant in range(8):
+            child = int(children[node][octant])
+            if child < 0:
+                continue
+            box = []
+            for a, b in enumerate((bx, by, bz)):
+                lo, hi = (max(b[0], splits[a]), b[1]) if (octant >> a) & 1 else (b[0], min(b[1], splits[a]))
+                box.append((lo, hi))
+            stack.append((child, box[0], box[1], box[2]))
+    return cost
+
+
+def brick_flops(cost, grid, bricks, B):
+    """(flops, lattice points) over the union of the kept bricks' lattice boxes."""
+    nx, ny, nz = grid.sx + 1, grid.sy + 1, grid.sz + 1
+    nbx, nby = (grid.sx + B - 1) // B, (grid.sy + B - 1) // B
+    mask = np.zeros((nz, ny, nx), bool)
+    for b in bricks.tolist():
+        bx, by, bz = b % nbx, (b // nbx) % nby, b // (nbx * nby)
+        i0, j0, k0 = bx * B, by * B, bz * B
+        mask[k0:min(k0 + B, nz - 1) + 1, j0:min(j0 + B, ny - 1) + 1, i0:min(i0 + B, nx - 1) + 1] = True
+    return int(cost[mask].sum(dtype=np.int64)), int(mask.sum())
 
 
 def cpu_baseline(spec, grid, seconds_target=12.0):
@@ -437,24 +480,37 @@ def our_arm(args, rank, world, local_rank):
                "meshes_per_s": world * e2e_steps / e2e_s,
                "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}
 
-    # Roofline of the dominant kernel (the distance interpreter): exact algorithmic flops.
+    # Roofline of the dominant kernel of the timed export (the distance interpreter on the
+    # kept bricks): exact algorithmic flops over the lattice points of those bricks.
     cells, children, words = tree.debug_octree()
     flops, counted = algorithmic_flops(cells, children, words, grid)
     assert counted == samples, (counted, samples)
-    eval_ms = eval_grid_ms
+    prog.export_mesh_device(grid, stream=sp)
+    kept_list, bsize = sdf.last_export_bricks()
+    cost = cost_lattice(cells, children, words, grid)
+    assert int(cost.sum(dtype=np.int64)) == flops
+    brick_fl, brick_points = brick_flops(cost, grid, kept_list, bsize)
+    del cost
+    eval_bricks_ms = kernels["eval_bricks"]["ms_per_step"]
     fp32 = _lib.C.c_double()
     _lib.check(lib.tg_measure_fp32_peak(_lib.C.byref(fp32), sp), "fp32 peak")
-    achieved = flops / (eval_ms * 1e-3) / 1e12
-    traffic = committed_traffic()
+    achieved = brick_fl / (eval_bricks_ms * 1e-3) / 1e12
+    traffic = committed_traffic("EvalBricksKernel")
+    dense_achieved = flops / (eval_grid_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32.value, "unit": "TFLOP/s",
-                "frac": achieved / fp32.value, "traffic": traffic.get("bytes_per_launch") if traffic else None,
-                "kernel": "EvalGridKernel (distance interpreter, every lattice point; timed in the dense export)",
-                "flops_per_launch": flops, "algorithmic_bytes_per_launch": 4 * samples,
+                "frac": achieved / fp32.value, "traffic": traffic["bytes_per_launch"] if traffic else None,
+                "traffic_source": traffic["source"] if traffic else None,
+                "kernel": "EvalBricksKernel (distance interpreter on the kept bricks of the timed export)",
+                "flops_per_launch": brick_fl, "lattice_points_per_launch": brick_points,
+                "algorithmic_bytes_per_launch": 4 * brick_points,
                 "peak_source": "measured in this run: FFMA throughput probe (tg_measure_fp32_peak), of measured",
                 "note": "kernels are built with -fmad=false for bit-exact parity, so every mul and add issues "
                         "separately: half the FFMA flop rate is the arithmetic ceiling",
-                "hbm": {"achieved_gbs": 4 * samples / (eval_ms * 1e-3) / 1e9,
-                        "peak_gbs": measured_peaks().get("hbm_gbs", 6800.0)}}
+                "hbm": {"achieved_gbs": 4 * brick_points / (eval_bricks_ms * 1e-3) / 1e9,
+                        "peak_gbs": measured_peaks().get("hbm_gbs", 6800.0)},
+                "dense_interpreter": {"kernel": "EvalGridKernel (every lattice point, dense export)",
+                                      "flops_per_launch": flops, "ms": eval_grid_ms, "achieved_tflops": dense_achieved,
+                                      "frac": dense_achieved / fp32.value}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:

@@ -275,6 +275,11 @@ TANGERINE_API tg_status tg_write_stl(tg_program* program, const tg_mesh* mesh, c
 /* Bricks in the last culled export on this process's engine and how many were evaluated. */
 TANGERINE_API tg_status tg_last_export_stats(int64_t* bricks, int64_t* active_bricks);
 
+/* The bricks the last culled export evaluated (brick index = bx + nbx * (by + nby * bz),
+ * bricks of brick_size^3 cells from the lattice origin), in index order; returns how many
+ * there were and copies at most `capacity`. */
+TANGERINE_API int64_t tg_last_export_bricks(uint32_t* out, int64_t capacity, int* brick_size);
+
 /* Host wall time of the phases of the last tg_export_tree on this thread: octree build +
  * compile, upload, GPU export, copy back. */
 TANGERINE_API tg_status tg_last_export_timing(double* compile_s, double* upload_s, double* gpu_s, double* copy_s);

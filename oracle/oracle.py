@@ -52,6 +52,19 @@ class Mesh:
         self.seconds = seconds
 
 
+class Drawable:
+    """Sodapop's meshing output: positions, gradient normals (V,3) f32, colours (V,4) f32
+    (material Eval with the normal as view), faces (F,3), and the meshing grid
+    (x, y, z, dx, dy, dz, sx, sy, sz)."""
+
+    def __init__(self, positions, normals, colors, faces, grid):
+        self.positions = positions
+        self.normals = normals
+        self.colors = colors
+        self.faces = faces
+        self.grid = grid
+
+
 class CpuOracle:
     def __init__(self, path: Path, prefix: str):
         self.path = Path(path)
@@ -89,6 +102,9 @@ class CpuOracle:
         self._oct_eval = self._fn("octree_eval", None, [vp, i64, _f32p, i, _f32p])
         self._oct_grad = self._fn("octree_gradient", None, [vp, i64, _f32p, _f32p])
         self._oct_color = self._fn("octree_color", None, [vp, i64, _f32p, _u8p])
+        fpp = C.POINTER(C.POINTER(C.c_float))
+        self._sodapop = self._fn("sodapop", i64, [vp, f, fpp, fpp, fpp, C.POINTER(C.POINTER(C.c_uint64)),
+                                                  C.POINTER(C.c_int64), _f32p])
         self._oct_grid = None
         self._raymarch = None
 
@@ -164,6 +180,26 @@ class CpuOracle:
     def octree(self, h, target=0.25, coalesce=True, max_depth=-1):
         o = self._oct_create(h, target, int(coalesce), max_depth)
         return o or None
+
+    def sodapop(self, h, density=20.0) -> Drawable:
+        """MeshingJob::NaiveSurfaceNets (sodapop.cpp:562-897), serially, without the vertex
+        shuffle; vertices in grid-index order."""
+        P, N, Cl = C.POINTER(C.c_float)(), C.POINTER(C.c_float)(), C.POINTER(C.c_float)()
+        F = C.POINTER(C.c_uint64)()
+        nf = C.c_int64()
+        grid = np.zeros(9, np.float32)
+        nv = self._sodapop(h, float(density), C.byref(P), C.byref(N), C.byref(Cl), C.byref(F), C.byref(nf), grid)
+        if nv < 0:
+            return None
+
+        def take(ptr, n, k, dtype):
+            return np.ctypeslib.as_array(ptr, shape=(max(1, n) * k,))[: n * k].reshape(n, k).astype(dtype).copy()
+
+        d = Drawable(take(P, nv, 3, np.float32), take(N, nv, 3, np.float32), take(Cl, nv, 4, np.float32),
+                     take(F, nf.value, 3, np.uint64), grid)
+        for b in (P, N, Cl, F):
+            self._free_buffer(C.cast(b, C.c_void_p))
+        return d
 
     def octree_free(self, o):
         self._oct_free(o)

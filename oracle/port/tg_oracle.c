@@ -1673,3 +1673,223 @@ void tgo_raymarch(tgo_tree* t, int64_t n, const float* o, const float* d, int it
 	ray_ctx c = { t, o, d, iters, eps, hit, travel, pos };
 	run_parallel(threads, n, 64, ray_one, &c);
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* Sodapop's meshing chain, MeshingJob::NaiveSurfaceNets (sodapop.cpp:562-897), serially.  */
+
+typedef struct { onode** items; int n, cap; } leaf_list;
+
+/* SDFOctree::LinkLeaves (sdf_evaluator.cpp:1912-1947): the terminus cells with an
+ * evaluator. */
+static void collect_leaves(onode* o, leaf_list* out)
+{
+	if (!o) return;
+	if (o->terminus)
+	{
+		if (!o->evaluator) return;
+		if (out->n == out->cap)
+		{
+			out->cap = out->cap ? out->cap * 2 : 256;
+			out->items = (onode**)realloc(out->items, sizeof(onode*) * (size_t)out->cap);
+		}
+		out->items[out->n++] = o;
+		return;
+	}
+	for (int i = 0; i < 8; ++i) collect_leaves(o->children[i], out);
+}
+
+/* SDFOctree::Walk with the incomplete search (sodapop.cpp:108-124), each found cell
+ * populated right away (the cells are disjoint, so the order does not matter). */
+static void populate_incomplete(tgo_octree* T, onode* o)
+{
+	if (!o) return;
+	if (o->terminus || o->incomplete)
+	{
+		if (o->incomplete)
+		{
+			octree_populate(T, o, 0, 3, -1);
+		}
+		return;
+	}
+	for (int i = 0; i < 8; ++i) populate_incomplete(T, o->children[i]);
+}
+
+static inline float sp_implicit(tgo_octree* T, float x, float y, float z)
+{
+	/* glm::clamp(Eval(p, false), -100, 100): min(max(x, lo), hi) with glm's comparisons. */
+	return gclamp(octree_eval_point(T, V3(x, y, z), 0), -100.0f, 100.0f);
+}
+
+/* MaterialPBRBR::Eval(P, N, V) with V = N (material.cpp:33-40): SampleColor x BSDF. */
+static v3 pbrbr(const float* rgb, v3 n)
+{
+	float dd = gmax(dot3(n, normalize3(add3(muls3(n, 0.75f), n))), 0.0f);
+	float D = powf(dd, 2.0f);
+	float F = 1.0f - gmax(dot3(n, n), 0.0f);
+	float bsdf = D + F * 0.25f;
+	return V3(rgb[0] * bsdf, rgb[1] * bsdf, rgb[2] * bsdf);
+}
+
+int64_t tgo_sodapop(tgo_tree* tree, float density, float** positions, float** normals, float** colors, uint64_t** faces,
+	int64_t* face_count, float* grid_out)
+{
+	/* SDFOctree::Create(.25, false, 3), then every incomplete cell populated on its own with
+	 * Populate(false, 3, -1) (sodapop.cpp:565-567): the incomplete cells' ancestors keep the
+	 * bounds they took at depth 3. */
+	tgo_octree* T = tgo_octree_create(tree, 0.25f, 0, 3);
+	if (!T) return -1;
+	populate_incomplete(T, T->root);
+
+	/* NaiveSurfaceNetsScratch (sodapop.cpp:150-177). */
+	const aabb B = T->root->bounds;
+	const v3 ext = sub3(B.max, B.min);
+	const float fl = floorf(density);
+	const v3 spu = gmax3(mul3(ext, V3(fl, fl, fl)), V3(8.0f, 8.0f, 8.0f));
+	int64_t sx = (int64_t)ceilf(spu.x), sy = (int64_t)ceilf(spu.y), sz = (int64_t)ceilf(spu.z);
+	const float dx = ext.x / (float)sx, dy = ext.y / (float)sy, dz = ext.z / (float)sz;
+	const float gx = B.min.x - dx * 2.0f, gy = B.min.y - dy * 2.0f, gz = B.min.z - dz * 2.0f;
+	sx += 3; sy += 3; sz += 3;
+	grid_out[0] = gx; grid_out[1] = gy; grid_out[2] = gz;
+	grid_out[3] = dx; grid_out[4] = dy; grid_out[5] = dz;
+	grid_out[6] = (float)sx; grid_out[7] = (float)sy; grid_out[8] = (float)sz;
+
+	/* Point cache: every grid index inside a leaf's aligned box whose 64-entry bucket
+	 * exists (sodapop.cpp:613-644), in increasing order (std::set per bucket). */
+	const int64_t range = sx * sy * sz;
+	const int64_t bucket = range < 64 ? range : 64;
+	const int64_t limit = ((range + bucket - 1) / bucket) * bucket;
+	uint8_t* cached = (uint8_t*)calloc((size_t)limit, 1);
+	leaf_list leaves = { NULL, 0, 0 };
+	collect_leaves(T->root, &leaves);
+	for (int l = 0; l < leaves.n; ++l)
+	{
+		const onode* o = leaves.items[l];
+		const float amnx = floorf(gmax(0.0f, o->bounds.min.x - gx) / dx);
+		const float amny = floorf(gmax(0.0f, o->bounds.min.y - gy) / dy);
+		const float amnz = floorf(gmax(0.0f, o->bounds.min.z - gz) / dz);
+		const float amxx = ceilf((o->bounds.max.x - gx) / dx);
+		const float amxy = ceilf((o->bounds.max.y - gy) / dy);
+		const float amxz = ceilf((o->bounds.max.z - gz) / dz);
+		for (float z = amnz; z <= amxz; ++z)
+			for (float y = amny; y <= amxy; ++y)
+				for (float x = amnx; x <= amxx; ++x)
+				{
+					const int64_t index = (int64_t)x + (int64_t)y * sx + (int64_t)z * sx * sy;
+					if (index < limit) cached[index] = 1;
+				}
+	}
+	free(leaves.items);
+
+	/* FirstLoopInnerThunk per cached point (surface_nets.cpp:864-974). */
+	const float maxx = gx + (float)sx * dx, maxy = gy + (float)sy * dy, maxz = gz + (float)sz * dz;
+	int64_t* cube_vertex = (int64_t*)malloc(sizeof(int64_t) * (size_t)limit);
+	int64_t nv = 0, capv = 1024;
+	float* V = (float*)malloc(sizeof(float) * 3 * (size_t)capv);
+	int64_t* VC = (int64_t*)malloc(sizeof(int64_t) * (size_t)capv);
+	for (int64_t index = 0; index < limit; ++index)
+	{
+		cube_vertex[index] = -1;
+		if (!cached[index]) continue;
+		const int64_t i = index % sx, j = (index / sx) % sy, k = index / (sx * sy);
+		float v[8];
+		for (int q = 0; q < 8; ++q)
+			v[q] = sp_implicit(T, world(gx, i + CORNER_OFS[q][0], dx), world(gy, j + CORNER_OFS[q][1], dy),
+				world(gz, k + CORNER_OFS[q][2], dz));
+		float sumx = 0.0f, sumy = 0.0f, sumz = 0.0f;
+		int count = 0;
+		for (int e = 0; e < 12; ++e)
+		{
+			const float s1 = v[EDGES[e][0]], s2 = v[EDGES[e][1]];
+			if ((s1 >= 0.0f) == (s2 >= 0.0f)) continue;
+			const int* a = CORNER_OFS[EDGES[e][0]];
+			const int* b = CORNER_OFS[EDGES[e][1]];
+			float p1x = (float)i + (float)a[0], p1y = (float)j + (float)a[1], p1z = (float)k + (float)a[2];
+			float p2x = (float)i + (float)b[0], p2y = (float)j + (float)b[1], p2z = (float)k + (float)b[2];
+			float t = (0.0f - s1) / (s2 - s1);
+			sumx = sumx + (p1x + t * (p2x - p1x));
+			sumy = sumy + (p1y + t * (p2y - p1y));
+			sumz = sumz + (p1z + t * (p2z - p1z));
+			++count;
+		}
+		if (!count) continue;
+		float nf = (float)count;
+		float cx = sumx / nf, cy = sumy / nf, cz = sumz / nf;
+		if (nv == capv)
+		{
+			capv *= 2;
+			V = (float*)realloc(V, sizeof(float) * 3 * (size_t)capv);
+			VC = (int64_t*)realloc(VC, sizeof(int64_t) * (size_t)capv);
+		}
+		V[nv * 3 + 0] = gx + (maxx - gx) * (cx - 0.0f) / ((float)sx - 0.0f);
+		V[nv * 3 + 1] = gy + (maxy - gy) * (cy - 0.0f) / ((float)sy - 0.0f);
+		V[nv * 3 + 2] = gz + (maxz - gz) * (cz - 0.0f) / ((float)sz - 0.0f);
+		VC[nv] = index;
+		cube_vertex[index] = nv++;
+	}
+
+	/* SecondLoopThunk per vertex (surface_nets.cpp:1001-1121). */
+	int64_t nf = 0, capf = 1024;
+	uint64_t* F = (uint64_t*)malloc(sizeof(uint64_t) * 3 * (size_t)capf);
+	for (int64_t n = 0; n < nv; ++n)
+	{
+		const int64_t cell = VC[n];
+		const int64_t i = cell % sx, j = (cell / sx) % sy, k = cell / (sx * sy);
+		if (i == 0 || j == 0 || k == 0) continue;
+		const int64_t nb[6] = { cell - 1, cell - 1 - sx, cell - sx, cell - sx - sx * sy, cell - sx * sy, cell - 1 - sx * sy };
+		const float c0 = sp_implicit(T, world(gx, i, dx), world(gy, j, dy), world(gz, k, dz));
+		const float es[3][2] = {
+			{ c0, sp_implicit(T, world(gx, i, dx), world(gy, j, dy), world(gz, k + 1, dz)) },
+			{ sp_implicit(T, world(gx, i, dx), world(gy, j + 1, dy), world(gz, k, dz)), c0 },
+			{ c0, sp_implicit(T, world(gx, i + 1, dx), world(gy, j, dy), world(gz, k, dz)) } };
+		static const int quad[3][3] = { {0, 1, 2}, {0, 5, 4}, {2, 3, 4} };
+		for (int q = 0; q < 3; ++q)
+		{
+			int64_t w[3];
+			int ok = 1;
+			for (int m = 0; m < 3; ++m)
+			{
+				const int64_t c = nb[quad[q][m]];
+				w[m] = (c >= 0 && c < limit) ? cube_vertex[c] : -1;
+				if (w[m] < 0) ok = 0;
+			}
+			if (!ok) continue;
+			int64_t v1, v2, v3;
+			if (es[q][1] > es[q][0]) { v1 = w[0]; v2 = w[1]; v3 = w[2]; }
+			else { v1 = w[2]; v2 = w[1]; v3 = w[0]; }
+			if (nf + 2 > capf)
+			{
+				capf *= 2;
+				F = (uint64_t*)realloc(F, sizeof(uint64_t) * 3 * (size_t)capf);
+			}
+			uint64_t* f = F + nf * 3;
+			f[0] = (uint64_t)n; f[1] = (uint64_t)v1; f[2] = (uint64_t)v2;
+			f[3] = (uint64_t)n; f[4] = (uint64_t)v2; f[5] = (uint64_t)v3;
+			nf += 2;
+		}
+	}
+
+	/* Gradient normals and material colours (sodapop.cpp:815-872). */
+	float* N = (float*)malloc(sizeof(float) * 3 * (size_t)(nv ? nv : 1));
+	float* C4 = (float*)malloc(sizeof(float) * 4 * (size_t)(nv ? nv : 1));
+	static const float white[3] = { 1.0f, 1.0f, 1.0f };
+	for (int64_t n = 0; n < nv; ++n)
+	{
+		const v3 q = V3(V[n * 3], V[n * 3 + 1], V[n * 3 + 2]);
+		const node* e = octree_select(T, q);
+		const v3 g = node_gradient(e, q);
+		N[n * 3] = g.x; N[n * 3 + 1] = g.y; N[n * 3 + 2] = g.z;
+		const int mat = node_material(e, q);
+		const v3 c = pbrbr(mat >= 0 ? T->tree->materials[mat].rgb : white, g);
+		C4[n * 4] = c.x; C4[n * 4 + 1] = c.y; C4[n * 4 + 2] = c.z; C4[n * 4 + 3] = 1.0f;
+	}
+	free(cached);
+	free(cube_vertex);
+	free(VC);
+	tgo_octree_free(T);
+	*positions = V;
+	*normals = N;
+	*colors = C4;
+	*faces = F;
+	*face_count = nf;
+	return nv;
+}

@@ -75,6 +75,11 @@ void tgo_raymarch(tgo_tree* tree, int64_t n, const float* origins, const float* 
                   uint8_t* hit, float* travel, float* position);
 
 int tgo_hardware_threads(void);
+/* Sodapop's meshing chain (sodapop.cpp:562-897) over the tree, serially: returns the vertex
+ * count (-1 without an octree); positions/normals (3 floats), colours (4 floats), faces (3
+ * indices) are malloc'd (release with tgo_free_buffer); grid_out gets x y z dx dy dz sx sy sz. */
+int64_t tgo_sodapop(tgo_tree* tree, float density, float** positions, float** normals, float** colors, uint64_t** faces,
+	int64_t* face_count, float* grid_out);
 
 #ifdef __cplusplus
 }

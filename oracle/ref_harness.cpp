@@ -27,6 +27,7 @@
 #include "painting_set.h"
 #include "threadpool.h"
 #include <surface_nets.h>
+#include <set>
 
 using namespace glm;
 
@@ -525,6 +526,123 @@ extern "C"
 		*Cubes = CopyOut(C);
 		*Faces = CopyOut(F);
 		*FaceCount = (int64_t)Task.OutputMesh.faces_.size();
+		return (int64_t)VertexCount;
+	}
+
+	// MeshingJob::NaiveSurfaceNets (sodapop.cpp:562-897) replayed serially with the
+	// reference's own classes: the meshing octree (SDFOctree::Create(.25, no coalescing,
+	// depth 3), then every incomplete cell populated without limit, LinkLeaves), the grid of
+	// NaiveSurfaceNetsScratch (sodapop.cpp:150-177), the point cache over the leaves' aligned
+	// boxes, FirstLoopInnerThunk for each cached point in index order (the std::set order of
+	// each bucket, buckets in order), SecondLoopThunk for each map entry, then per vertex
+	// SDFOctree::Gradient and the material's Eval with the normal as the view direction
+	// (sodapop.cpp:815-872).  Left out: ApplyVertexSequence's shuffle, whose input order is
+	// already run-dependent in the app (parallel vertex loop).  Returns the vertex count
+	// (-1 without an octree); grid_out receives x, y, z, dx, dy, dz, sx, sy, sz.
+	int64_t ref_sodapop(void* Handle, float Density, float** Positions, float** Normals, float** Colors, uint64_t** Faces,
+		int64_t* FaceCount, float* GridOut)
+	{
+		SDFNodeShared Root = ((RefTree*)Handle)->Root;
+		SDFOctreeShared Evaluator = SDFOctree::Create(Root, .25, false, 3, 0.0f);
+		if (!Evaluator) return -1;
+		std::vector<SDFOctree*> Incompletes;
+		SDFOctree::CallbackType Search = [&](SDFOctree& Leaf)
+		{
+			if (Leaf.Incomplete) Incompletes.push_back(&Leaf);
+		};
+		Evaluator->Walk(Search);
+		for (SDFOctree* Cell : Incompletes) Cell->Populate(false, 3, -1);
+		Evaluator->LinkLeaves();
+
+		isosurface::AsyncParallelSurfaceNets Ext;
+		isosurface::regular_grid_t& Grid = Ext.Grid;
+		{
+			const float Floored = glm::floor(Density);
+			const glm::vec3 SamplesPerUnit = glm::max(Evaluator->Bounds.Extent() * glm::vec3(Floored), glm::vec3(8.0));
+			Grid.x = Evaluator->Bounds.Min.x;
+			Grid.y = Evaluator->Bounds.Min.y;
+			Grid.z = Evaluator->Bounds.Min.z;
+			Grid.sx = size_t(glm::ceil(SamplesPerUnit.x));
+			Grid.sy = size_t(glm::ceil(SamplesPerUnit.y));
+			Grid.sz = size_t(glm::ceil(SamplesPerUnit.z));
+			Grid.dx = Evaluator->Bounds.Extent().x / static_cast<float>(Grid.sx);
+			Grid.dy = Evaluator->Bounds.Extent().y / static_cast<float>(Grid.sy);
+			Grid.dz = Evaluator->Bounds.Extent().z / static_cast<float>(Grid.sz);
+			Grid.x -= Grid.dx * 2;
+			Grid.y -= Grid.dy * 2;
+			Grid.z -= Grid.dz * 2;
+			Grid.sx += 3;
+			Grid.sy += 3;
+			Grid.sz += 3;
+		}
+		GridOut[0] = Grid.x; GridOut[1] = Grid.y; GridOut[2] = Grid.z;
+		GridOut[3] = Grid.dx; GridOut[4] = Grid.dy; GridOut[5] = Grid.dz;
+		GridOut[6] = (float)Grid.sx; GridOut[7] = (float)Grid.sy; GridOut[8] = (float)Grid.sz;
+		SDFOctree* Raw = Evaluator.get();
+		Ext.ImplicitFunction = [Raw](float X, float Y, float Z) -> float
+		{
+			return glm::clamp(Raw->Eval(glm::vec3(X, Y, Z), false), -100.0f, 100.0f);
+		};
+		Ext.Setup();
+
+		const size_t IndexRange = Grid.sx * Grid.sy * Grid.sz;
+		const size_t BucketSize = std::min(size_t(64), IndexRange);
+		const size_t BucketCount = (IndexRange + BucketSize - 1) / BucketSize;
+		std::set<size_t> Points;
+		{
+			const glm::vec3 Origin(Grid.x, Grid.y, Grid.z);
+			const glm::vec3 Step(Grid.dx, Grid.dy, Grid.dz);
+			for (SDFOctree* Leaf = Evaluator->Next; Leaf; Leaf = (Leaf->Next == Leaf ? nullptr : Leaf->Next))
+			{
+				const glm::vec3 AlignedMin = glm::floor(glm::max(glm::vec3(0.0), Leaf->Bounds.Min - Origin) / Step);
+				const glm::vec3 AlignedMax = glm::ceil((Leaf->Bounds.Max - Origin) / Step);
+				for (float z = AlignedMin.z; z <= AlignedMax.z; ++z)
+					for (float y = AlignedMin.y; y <= AlignedMax.y; ++y)
+						for (float x = AlignedMin.x; x <= AlignedMax.x; ++x)
+						{
+							const size_t Index = size_t(x) + (size_t(y) * Grid.sx) + (size_t(z) * Grid.sx * Grid.sy);
+							if (Index / BucketSize < BucketCount) Points.insert(Index);
+						}
+			}
+		}
+		for (size_t Index : Points)
+		{
+			isosurface::AsyncParallelSurfaceNets::GridPoint P;
+			P.i = Index % Grid.sx;
+			P.j = (Index / Grid.sx) % Grid.sy;
+			P.k = Index / (Grid.sx * Grid.sy);
+			Ext.FirstLoopInnerThunk(Ext, P);
+		}
+		for (auto& Element : Ext.SecondLoopDomain) Ext.SecondLoopThunk(Ext, Element);
+
+		const size_t VertexCount = Ext.OutputMesh.vertices_.size();
+		std::vector<float> P3(VertexCount * 3), N3(VertexCount * 3), C4(VertexCount * 4);
+		for (size_t v = 0; v < VertexCount; ++v)
+		{
+			const glm::vec3 Position(Ext.OutputMesh.vertices_[v].x, Ext.OutputMesh.vertices_[v].y, Ext.OutputMesh.vertices_[v].z);
+			P3[v * 3] = Position.x; P3[v * 3 + 1] = Position.y; P3[v * 3 + 2] = Position.z;
+			const glm::vec3 Normal = Evaluator->Gradient(Position);
+			N3[v * 3] = Normal.x; N3[v * 3 + 1] = Normal.y; N3[v * 3 + 2] = Normal.z;
+			glm::vec3 Sample(0.0f);
+			MaterialShared Material = Evaluator->GetMaterial(Position);
+			if (Material)
+			{
+				ChthonicMaterialInterface* Chthonic = dynamic_cast<ChthonicMaterialInterface*>(Material.get());
+				if (Chthonic) Sample = glm::vec3(Chthonic->Eval(Position, Normal, Normal));
+			}
+			C4[v * 4] = Sample.x; C4[v * 4 + 1] = Sample.y; C4[v * 4 + 2] = Sample.z; C4[v * 4 + 3] = 1.0f;
+		}
+		std::vector<uint64_t> F;
+		F.reserve(Ext.OutputMesh.faces_.size() * 3);
+		for (auto& Face : Ext.OutputMesh.faces_)
+		{
+			F.push_back(Face.v0); F.push_back(Face.v1); F.push_back(Face.v2);
+		}
+		*Positions = CopyOut(P3);
+		*Normals = CopyOut(N3);
+		*Colors = CopyOut(C4);
+		*Faces = CopyOut(F);
+		*FaceCount = (int64_t)Ext.OutputMesh.faces_.size();
 		return (int64_t)VertexCount;
 	}
 

@@ -118,6 +118,7 @@ SIGNATURES = {
     "tg_write_ply": (_i, [C.POINTER(HostMesh), C.c_char_p, _f]),
     "tg_write_stl": (_i, [_vp, C.POINTER(HostMesh), C.c_char_p, _f, _vp]),
     "tg_last_export_stats": (_i, [C.POINTER(_i64), C.POINTER(_i64)]),
+    "tg_last_export_bricks": (_i64, [_vp, _i64, C.POINTER(_i)]),
     "tg_last_export_timing": (_i, [C.POINTER(C.c_double)] * 4),
     "tg_profile_enable": (None, [_i]),
     "tg_profile_read": (_i, [C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),

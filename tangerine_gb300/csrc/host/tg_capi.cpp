@@ -1029,6 +1029,19 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API int64_t tg_last_export_bricks(uint32_t* out, int64_t capacity, int* brick_size)
+	{
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		std::vector<uint32_t> list;
+		int b = 0;
+		if (eng.LastBrickList(list, b) != cudaSuccess) { SetError("reading the brick list"); return -1; }
+		if (brick_size) *brick_size = b;
+		if (out)
+			for (int64_t i = 0; i < capacity && i < (int64_t)list.size(); ++i) out[i] = list[(size_t)i];
+		return (int64_t)list.size();
+	}
+
 	TANGERINE_API tg_status tg_debug_blend_check(uint64_t n, uint64_t seed, uint64_t* counts)
 	{
 		if (!counts) { SetError("null argument"); return TG_ERR_INVALID; }

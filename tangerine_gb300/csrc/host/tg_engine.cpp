@@ -342,6 +342,7 @@ namespace tg
 			Begin("list_bricks", s);
 			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
 			End(s);
+			LastBrickSize = B;
 			Begin("eval_bricks", s);
 			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s,
 				opt.Lanes));
@@ -417,6 +418,15 @@ namespace tg
 		TG_TRY(cudaStreamSynchronize(s));
 		Collect();
 		if (opt.Field) TG_TRY(const_cast<FieldNet*>(opt.Field)->CheckStatus(s));
+		return cudaSuccess;
+	}
+
+	cudaError_t Engine::LastBrickList(std::vector<uint32_t>& out, int& brick_size)
+	{
+		out.resize((size_t)ActiveBricks);
+		brick_size = LastBrickSize;
+		if (ActiveBricks <= 0) return cudaSuccess;
+		TG_TRY(cudaMemcpy(out.data(), BrickList.Ptr, (size_t)ActiveBricks * 4, cudaMemcpyDeviceToHost));
 		return cudaSuccess;
 	}
 

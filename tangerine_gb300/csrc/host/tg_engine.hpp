@@ -72,6 +72,8 @@ namespace tg
 		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
 		cudaError_t Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s);
 		int64_t LastActiveBricks() const { return ActiveBricks; }
+		// The kept bricks of the last culled export (brick index order), copied to host.
+		cudaError_t LastBrickList(std::vector<uint32_t>& out, int& brick_size);
 		int64_t LastBricks() const { return Bricks; }
 		cudaError_t FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
 			uint64_t face_count, float* host_normals, cudaStream_t s);
@@ -109,6 +111,7 @@ namespace tg
 		uint32_t* HostCounts = nullptr;
 		int PersistentBlocks = 0;
 		int64_t ActiveBricks = 0, Bricks = 0;
+		int LastBrickSize = 0;
 	};
 
 	// Pinned host blocks handed out as mesh outputs and taken back by tg_mesh_free, so the

@@ -601,6 +601,32 @@ namespace tg
 			}
 		}
 
+		// The same update four parameters at a time (16-byte loads and stores).
+		__global__ void AdamKernel4(float4* __restrict__ params, float4* __restrict__ grads, float4* __restrict__ m, float4* __restrict__ v,
+			int64_t n4, AdamStep s)
+		{
+			for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x)
+			{
+				const float4 g = grads[i];
+				grads[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				float4 mi = m[i], vi = v[i], p = params[i];
+				float* pg = (float*)&g;
+				float* pm = (float*)&mi;
+				float* pv = (float*)&vi;
+				float* pp = (float*)&p;
+#pragma unroll
+				for (int k = 0; k < 4; ++k)
+				{
+					pm[k] = s.Beta1 * pm[k] + (1.0f - s.Beta1) * pg[k];
+					pv[k] = s.Beta2 * pv[k] + (1.0f - s.Beta2) * (pg[k] * pg[k]);
+					pp[k] -= s.Rate * (pm[k] / s.Correction1) / (sqrtf(pv[k] / s.Correction2) + s.Epsilon);
+				}
+				m[i] = mi;
+				v[i] = vi;
+				params[i] = p;
+			}
+		}
+
 		__global__ void FieldPackKernel(const float* __restrict__ mlp, uint8_t* __restrict__ image)
 		{
 			for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x)
@@ -1012,6 +1038,15 @@ namespace tg
 	cudaError_t LaunchAdam(float* params, float* grads, float* m, float* v, int64_t n, const AdamStep& step, cudaStream_t stream)
 	{
 		if (n <= 0) return cudaSuccess;
+		const bool aligned = ((uintptr_t)params | (uintptr_t)grads | (uintptr_t)m | (uintptr_t)v) % 16 == 0;
+		if (aligned && n % 4 == 0)
+		{
+			const int64_t n4 = n / 4;
+			const int64_t want4 = (n4 + 255) / 256;
+			const int blocks4 = (int)(want4 < (int64_t)SmCount() * 16 ? want4 : (int64_t)SmCount() * 16);
+			AdamKernel4<<<blocks4, 256, 0, stream>>>((float4*)params, (float4*)grads, (float4*)m, (float4*)v, n4, step);
+			return cudaGetLastError();
+		}
 		const int64_t want = (n + 255) / 256;
 		const int blocks = (int)(want < (int64_t)SmCount() * 8 ? want : (int64_t)SmCount() * 8);
 		AdamKernel<<<blocks, 256, 0, stream>>>(params, grads, m, v, n, step);

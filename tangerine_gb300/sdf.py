@@ -150,6 +150,16 @@ def last_export_stats():
     return b.value, a.value
 
 
+def last_export_bricks():
+    """(brick indices evaluated by the last culled export, brick edge in cells)."""
+    b = C.c_int()
+    n = load().tg_last_export_bricks(None, 0, C.byref(b))
+    out = np.empty(max(n, 0), np.uint32)
+    if n > 0:
+        load().tg_last_export_bricks(_lib.as_ptr(out), n, C.byref(b))
+    return out, b.value
+
+
 def last_export_timing():
     """Host seconds of the last tg_export_tree: (compile, upload, gpu, copy)."""
     v = [C.c_double() for _ in range(4)]
