@@ -186,6 +186,15 @@ TANGERINE_API int64_t tg_tree_reference_words(void* tree, uint32_t* out, int64_t
 TANGERINE_API int64_t tg_debug_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
                                       uint32_t* words, int64_t word_capacity, int64_t* word_count);
 
+/* The same dump of Sodapop's meshing octree (see tg_sodapop_mesh). */
+TANGERINE_API int64_t tg_debug_meshing_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
+                                              uint32_t* words, int64_t word_capacity, int64_t* word_count);
+/* Host-only plan of tg_sodapop_mesh: grid gets origin xyz, step xyz, cells xyz, the point
+ * cache's limit and the lattice's z layers (11 floats); boxes the leaves' inclusive integer
+ * point-cache spans (6 per leaf, up to box_capacity leaves); leaves the leaf count. */
+TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* grid, int64_t* boxes, int64_t box_capacity,
+                                              int64_t* leaves);
+
 /* The lattice MeshExportThread builds for (min, max, step): min moves down two steps;
  * ceil((max - min) / step) cells, one more lattice point, per axis (export.cpp:324-337). */
 TANGERINE_API tg_status tg_export_grid(const float model_min[3], const float model_max[3], float step, tg_grid* out);
@@ -232,6 +241,40 @@ TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, const tg_gri
  * normals, colours, copy back to the host (MeshExportThread minus the file write). */
 TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], const float model_max[3], float step,
                                        tg_mesh* out, void* stream);
+
+/* Sodapop's meshing job for one drawable (MeshingJob::NaiveSurfaceNets,
+ * tangerine/sodapop.cpp:562-897), on the GPU:
+ *  - the meshing octree: SDFOctree::Create(.25, false, 3), then every incomplete cell
+ *    populated with Populate(false, 3, -1);
+ *  - a lattice over the root's bounds at floor(density) samples per unit (at least 8 per
+ *    axis), one step per axis, two extra steps below the minimum and three extra cells
+ *    (sodapop.cpp:153-177); Sodapop::Populate uses density 20 plus the caller's push;
+ *  - clamp(octree distance with the non-exact descent, -100, 100) at its points;
+ *  - surface nets over the cells inside the octree leaves' aligned boxes (the point
+ *    cache), vertices in cell-number order;
+ *  - per vertex the gradient normal and the colour MaterialPBRBR gives with V = N (white
+ *    where no material applies), alpha 1.
+ * The reference then permutes the vertices (ApplyVertexSequence) for its renderer; that
+ * order depends on thread timing and is not reproduced.  Results in host memory; release
+ * with tg_drawable_free. */
+typedef struct tg_drawable
+{
+	uint64_t vertex_count;
+	uint64_t face_count;
+	float* positions;           /* 3 per vertex */
+	float* normals;             /* 3 per vertex */
+	float* colors;              /* 4 per vertex (RGBA) */
+	uint32_t* faces;            /* 3 per face */
+	uint32_t* cells;            /* 1 per vertex: x + y*sx + z*sx*sy */
+	float grid_origin[3];       /* lattice point (0, 0, 0) */
+	float grid_step[3];
+	int64_t grid_cells[3];      /* sx, sy, sz */
+	double compile_seconds;     /* meshing octree + programs, on the host */
+	double gpu_seconds;         /* upload, kernels and copies */
+} tg_drawable;
+
+TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream);
+TANGERINE_API void tg_drawable_free(tg_drawable* drawable);
 
 /* SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the whole tree for n rays, on the GPU:
  * the reference's step sequence, so hit flags, travel (+inf on a miss) and end positions

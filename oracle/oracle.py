@@ -96,6 +96,7 @@ class CpuOracle:
         self._clip = self._fn("clip", vp, [vp, f, f, f, f])
         self._equal = self._fn("equal", i, [vp, vp])
         self._oct_create = self._fn("octree_create", vp, [vp, f, i, i])
+        self._mesh_oct_create = self._fn("meshing_octree_create", vp, [vp])
         self._oct_free = self._fn("octree_free", None, [vp])
         self._oct_dump = self._fn("octree_dump", i, [vp, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_int32)),
                                                       C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_int)])
@@ -180,6 +181,11 @@ class CpuOracle:
     def octree(self, h, target=0.25, coalesce=True, max_depth=-1):
         o = self._oct_create(h, target, int(coalesce), max_depth)
         return o or None
+
+    def meshing_octree(self, h):
+        """Sodapop's meshing octree: Create(.25, false, 3), then each incomplete cell
+        populated with Populate(false, 3, -1) (sodapop.cpp:565-569)."""
+        return self._mesh_oct_create(h) or None
 
     def sodapop(self, h, density=20.0) -> Drawable:
         """MeshingJob::NaiveSurfaceNets (sodapop.cpp:562-897), serially, without the vertex

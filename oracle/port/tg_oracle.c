@@ -1271,10 +1271,12 @@ static int dump_node(onode* o, dumpbuf* d)
 	N[9] = o->terminus ? 1.0f : 0.0f;
 	N[10] = o->evaluator ? 1.0f : 0.0f;
 	N[11] = (float)d->n_words;
-	N[12] = (float)o->program.n;
+	/* A cell whose evaluator Populate dropped keeps no program. */
+	const int nwords = o->evaluator ? o->program.n : 0;
+	N[12] = (float)nwords;
 	N[13] = (float)(o->evaluator ? o->stack_size : 0);
 	for (int i = 0; i < 8; ++i) d->children[(size_t)idx * 8 + i] = -1;
-	for (int i = 0; i < o->program.n; ++i)
+	for (int i = 0; i < nwords; ++i)
 	{
 		if (d->n_words == d->cap_words) { d->cap_words = d->cap_words ? d->cap_words * 2 : 1024; d->words = (uint32_t*)realloc(d->words, 4 * (size_t)d->cap_words); }
 		d->words[d->n_words++] = o->program.w[i];
@@ -1728,6 +1730,13 @@ static v3 pbrbr(const float* rgb, v3 n)
 	float F = 1.0f - gmax(dot3(n, n), 0.0f);
 	float bsdf = D + F * 0.25f;
 	return V3(rgb[0] * bsdf, rgb[1] * bsdf, rgb[2] * bsdf);
+}
+
+tgo_octree* tgo_meshing_octree_create(tgo_tree* tree)
+{
+	tgo_octree* T = tgo_octree_create(tree, 0.25f, 0, 3);
+	if (T) populate_incomplete(T, T->root);
+	return T;
 }
 
 int64_t tgo_sodapop(tgo_tree* tree, float density, float** positions, float** normals, float** colors, uint64_t** faces,

@@ -46,6 +46,9 @@ tgo_tree* tgo_clip(tgo_tree* tree, float x, float y, float z, float radius);
 int tgo_equal(tgo_tree* a, tgo_tree* b);
 
 tgo_octree* tgo_octree_create(tgo_tree* tree, float target_size, int coalesce, int max_depth);
+/* Sodapop's meshing octree: create(.25, no coalescing, depth 3), then each incomplete
+ * cell populated without a depth limit (sodapop.cpp:565-569). */
+tgo_octree* tgo_meshing_octree_create(tgo_tree* tree);
 void tgo_octree_free(tgo_octree* octree);
 int tgo_octree_dump(tgo_octree* octree, float** nodes, int32_t** children, uint32_t** words, int* word_count);
 void tgo_octree_eval(tgo_octree* octree, int64_t n, const float* points, int exact, float* out);

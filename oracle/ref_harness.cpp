@@ -373,6 +373,22 @@ extern "C"
 		return new RefOctree{ Octree };
 	}
 
+	// Sodapop's meshing octree (sodapop.cpp:565-569): Create(.25, false, 3), then every
+	// incomplete cell populated with Populate(false, 3, -1).
+	void* ref_meshing_octree_create(void* Handle)
+	{
+		SDFOctreeShared Octree = SDFOctree::Create(((RefTree*)Handle)->Root, .25, false, 3, 0.0f);
+		if (!Octree) return nullptr;
+		std::vector<SDFOctree*> Incompletes;
+		SDFOctree::CallbackType Search = [&](SDFOctree& Leaf)
+		{
+			if (Leaf.Incomplete) Incompletes.push_back(&Leaf);
+		};
+		Octree->Walk(Search);
+		for (SDFOctree* Cell : Incompletes) Cell->Populate(false, 3, -1);
+		return new RefOctree{ Octree };
+	}
+
 	void ref_octree_free(void* Handle)
 	{
 		delete (RefOctree*)Handle;

@@ -67,6 +67,14 @@ class BatchInfo(C.Structure):
                 ("autotune_seconds", C.c_double), ("device_bytes", C.c_int64)]
 
 
+class Drawable(C.Structure):
+    _fields_ = [("vertex_count", C.c_uint64), ("face_count", C.c_uint64),
+                ("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("colors", C.POINTER(C.c_float)), ("faces", C.POINTER(C.c_uint32)),
+                ("cells", C.POINTER(C.c_uint32)), ("grid_origin", C.c_float * 3), ("grid_step", C.c_float * 3),
+                ("grid_cells", C.c_int64 * 3), ("compile_seconds", C.c_double), ("gpu_seconds", C.c_double)]
+
+
 # Every exported symbol with its signature: (restype, argtypes).
 _vp, _f, _i, _i64, _u32 = C.c_void_p, C.c_float, C.c_int, C.c_int64, C.c_uint32
 SIGNATURES = {
@@ -104,6 +112,10 @@ SIGNATURES = {
     "tg_program_get_info": (_i, [_vp, C.POINTER(ProgramInfo)]),
     "tg_tree_reference_words": (_i64, [_vp, _vp, _i64]),
     "tg_debug_octree": (_i64, [_vp, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i64)]),
+    "tg_debug_meshing_octree": (_i64, [_vp, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i64)]),
+    "tg_debug_sodapop_plan": (_i, [_vp, _f, _vp, _vp, _i64, C.POINTER(_i64)]),
+    "tg_sodapop_mesh": (_i, [_vp, _f, C.POINTER(Drawable), _vp]),
+    "tg_drawable_free": (None, [C.POINTER(Drawable)]),
     "tg_export_grid": (_i, [_vp, _vp, _f, C.POINTER(Grid)]),
     "tg_eval_grid": (_i, [_vp, C.POINTER(Grid), _vp, _i, _vp]),
     "tg_eval_points": (_i, [_vp, _vp, _i64, _vp, _vp]),

@@ -135,6 +135,10 @@ namespace
 	}
 
 	void WriteFileError(const char* path) { SetError(std::string("cannot write ") + (path ? path : "(null)")); }
+
+	// An octree's cells in the oracle's dump layout (tg_debug_octree).
+	int64_t DumpOctree(const Octree& o, float* cells, int32_t* children, int64_t cell_capacity, uint32_t* words,
+		int64_t word_capacity, int64_t* word_count);
 }
 
 extern "C"
@@ -255,6 +259,43 @@ extern "C"
 		if (!tree) return -1;
 		Octree o;
 		if (!o.Build(Borrow(tree))) return -1;
+		return DumpOctree(o, cells, children, cell_capacity, words, word_capacity, word_count);
+	}
+
+	TANGERINE_API int64_t tg_debug_meshing_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
+		uint32_t* words, int64_t word_capacity, int64_t* word_count)
+	{
+		if (!tree) return -1;
+		Octree o;
+		if (!o.BuildMeshing(Borrow(tree))) return -1;
+		return DumpOctree(o, cells, children, cell_capacity, words, word_capacity, word_count);
+	}
+
+	TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* grid, int64_t* boxes, int64_t box_capacity,
+		int64_t* leaves)
+	{
+		if (!tree || !grid) { SetError("null argument"); return TG_ERR_INVALID; }
+		CompiledTree t;
+		std::string err;
+		if (!CompileTree(Borrow(tree), t, err, OctreeKind::Meshing)) { SetError(err); return TG_ERR_UNBOUNDED; }
+		SodapopGrid g;
+		std::vector<int64_t> b;
+		if (!SodapopPlan(t, density, g, b, err)) { SetError(err); return TG_ERR_UNSUPPORTED; }
+		grid[0] = g.G[0]; grid[1] = g.G[1]; grid[2] = g.G[2];
+		grid[3] = g.D[0]; grid[4] = g.D[1]; grid[5] = g.D[2];
+		grid[6] = (float)g.SX; grid[7] = (float)g.SY; grid[8] = (float)g.SZ;
+		grid[9] = (float)g.Limit; grid[10] = (float)g.LZ;
+		for (int64_t i = 0; i < (int64_t)b.size() && i < box_capacity * 6 && boxes; ++i) boxes[i] = b[(size_t)i];
+		if (leaves) *leaves = (int64_t)(b.size() / 6);
+		return TG_OK;
+	}
+}
+
+namespace
+{
+	int64_t DumpOctree(const Octree& o, float* cells, int32_t* children, int64_t cell_capacity, uint32_t* words,
+		int64_t word_capacity, int64_t* word_count)
+	{
 		int64_t w = 0;
 		for (size_t i = 0; i < o.Cells.size(); ++i)
 		{
@@ -286,6 +327,10 @@ extern "C"
 		if (word_count) *word_count = w;
 		return (int64_t)o.Cells.size();
 	}
+}
+
+extern "C"
+{
 
 	TANGERINE_API tg_status tg_export_grid(const float lo[3], const float hi[3], float step, tg_grid* out)
 	{
@@ -415,6 +460,92 @@ extern "C"
 		tm.GpuSeconds = secs(t1, t2);
 		tm.CopySeconds = secs(t2, t3);
 		return st;
+	}
+
+	TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream)
+	{
+		if (!out) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::memset(out, 0, sizeof *out);
+		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
+		const auto t0 = std::chrono::steady_clock::now();
+		std::unique_ptr<tg_program> prog(new (std::nothrow) tg_program());
+		if (!prog) { SetError("out of host memory"); return TG_ERR_MEMORY; }
+		std::string err;
+		if (!CompileTree(Borrow(tree), prog->Host, err, OctreeKind::Meshing))
+		{
+			SetError(err);
+			return TG_ERR_UNBOUNDED;
+		}
+		SodapopGrid g;
+		std::vector<int64_t> boxes;
+		if (!SodapopPlan(prog->Host, density, g, boxes, err))
+		{
+			SetError(err);
+			return TG_ERR_UNSUPPORTED;
+		}
+		const auto t1 = std::chrono::steady_clock::now();
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t s = StreamOf(stream);
+		cudaError_t e = eng.UploadScratch(*prog, s);
+		if (e != cudaSuccess) return CudaFail(e, "uploading the program");
+		SodapopMesh m;
+		e = eng.Sodapop(*prog, g, boxes, m, s);
+		if (e != cudaSuccess) return CudaFail(e, "running the meshing job");
+		auto take = [](size_t bytes) -> void*
+		{
+			void* p = HostPool::Get().Take(bytes);
+			return p ? p : std::malloc(bytes);
+		};
+		const size_t v = m.VertexCount ? m.VertexCount : 1, f = m.FaceCount ? m.FaceCount : 1;
+		out->positions = (float*)take(v * 12);
+		out->normals = (float*)take(v * 12);
+		out->colors = (float*)take(v * 16);
+		out->faces = (uint32_t*)take(f * 12);
+		out->cells = (uint32_t*)take(v * 4);
+		if (!out->positions || !out->normals || !out->colors || !out->faces || !out->cells)
+		{
+			tg_drawable_free(out);
+			SetError("out of host memory for the drawable");
+			return TG_ERR_MEMORY;
+		}
+		out->vertex_count = m.VertexCount;
+		out->face_count = m.FaceCount;
+		if (m.VertexCount)
+		{
+			e = cudaMemcpyAsync(out->positions, m.Positions, m.VertexCount * 12, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(out->normals, m.Normals, m.VertexCount * 12, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(out->colors, m.Colors, m.VertexCount * 16, cudaMemcpyDeviceToHost, s);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(out->cells, m.Cells, m.VertexCount * 4, cudaMemcpyDeviceToHost, s);
+		}
+		if (e == cudaSuccess && m.FaceCount) e = cudaMemcpyAsync(out->faces, m.Faces, m.FaceCount * 12, cudaMemcpyDeviceToHost, s);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+		if (e != cudaSuccess)
+		{
+			tg_drawable_free(out);
+			return CudaFail(e, "copying the drawable to the host");
+		}
+		for (int a = 0; a < 3; ++a)
+		{
+			out->grid_origin[a] = g.G[a];
+			out->grid_step[a] = g.D[a];
+		}
+		out->grid_cells[0] = g.SX; out->grid_cells[1] = g.SY; out->grid_cells[2] = g.SZ;
+		const auto t2 = std::chrono::steady_clock::now();
+		out->compile_seconds = std::chrono::duration<double>(t1 - t0).count();
+		out->gpu_seconds = std::chrono::duration<double>(t2 - t1).count();
+		return TG_OK;
+	}
+
+	TANGERINE_API void tg_drawable_free(tg_drawable* d)
+	{
+		if (!d) return;
+		void* blocks[5] = { d->positions, d->normals, d->colors, d->faces, d->cells };
+		for (void* b : blocks)
+		{
+			if (!HostPool::Get().Give(b)) std::free(b);
+		}
+		std::memset(d, 0, sizeof *d);
 	}
 
 	TANGERINE_API tg_status tg_ray_march(tg_program* p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,

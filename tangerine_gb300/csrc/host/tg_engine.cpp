@@ -108,17 +108,19 @@ namespace tg
 	{
 		struct ProgramLayout
 		{
-			size_t NodeBytes, CodeOff, CodeBytes, ColorOff, Total;
+			size_t NodeBytes, CodeOff, CodeBytes, ColorOff, RgbOff, Total;
 		};
 
+		// Nodes, code quads, colour bytes, material RGB: each part 256-byte aligned.
 		ProgramLayout LayoutOf(const Program& p)
 		{
 			ProgramLayout l;
 			l.NodeBytes = p.Host.Nodes.size() * sizeof(OctNode);
-			l.CodeOff = (l.NodeBytes + 255) / 256 * 256;
+			l.CodeOff = AlignUp(l.NodeBytes, 256);
 			l.CodeBytes = p.Host.Code.size() * sizeof(float);
-			l.ColorOff = (l.CodeOff + l.CodeBytes + 255) / 256 * 256;
-			l.Total = l.ColorOff + (p.Host.Colors.size() ? p.Host.Colors.size() : 4);
+			l.ColorOff = AlignUp(l.CodeOff + l.CodeBytes, 256);
+			l.RgbOff = AlignUp(l.ColorOff + (p.Host.Colors.size() ? p.Host.Colors.size() : 4), 256);
+			l.Total = l.RgbOff + (p.Host.MaterialRgb.size() ? p.Host.MaterialRgb.size() * sizeof(float) : 16);
 			return l;
 		}
 
@@ -127,6 +129,8 @@ namespace tg
 			std::memcpy(dst, p.Host.Nodes.data(), l.NodeBytes);
 			std::memcpy(dst + l.CodeOff, p.Host.Code.data(), l.CodeBytes);
 			if (!p.Host.Colors.empty()) std::memcpy(dst + l.ColorOff, p.Host.Colors.data(), p.Host.Colors.size());
+			if (!p.Host.MaterialRgb.empty())
+				std::memcpy(dst + l.RgbOff, p.Host.MaterialRgb.data(), p.Host.MaterialRgb.size() * sizeof(float));
 		}
 
 		void Bind(Program& p, const ProgramLayout& l, void* device)
@@ -135,6 +139,7 @@ namespace tg
 			p.View.Nodes = reinterpret_cast<const OctNode*>(base);
 			p.View.Code = reinterpret_cast<const float4*>(base + l.CodeOff);
 			p.View.Colors = reinterpret_cast<const uchar4*>(base + l.ColorOff);
+			p.View.MaterialRgb = reinterpret_cast<const float4*>(base + l.RgbOff);
 			p.View.MaxStack = p.Host.Header.MaxStack;
 			p.View.FullSurfaceCode = p.Host.Header.FullSurfaceCode;
 			p.View.Lipschitz = p.Host.Header.Lipschitz;
@@ -168,32 +173,19 @@ namespace tg
 		return cudaSuccess;
 	}
 
-	// One allocation: nodes (64-byte records), code quads, colour bytes.
+	// One allocation: nodes (64-byte records), code quads, colour bytes, material RGB.
 	cudaError_t Engine::Upload(Program& p)
 	{
-		const size_t nodeBytes = p.Host.Nodes.size() * sizeof(OctNode);
-		const size_t codeOff = AlignUp(nodeBytes, 256);
-		const size_t codeBytes = p.Host.Code.size() * sizeof(float);
-		const size_t colorOff = AlignUp(codeOff + codeBytes, 256);
-		const size_t colorBytes = p.Host.Colors.size() ? p.Host.Colors.size() : 4;
-		const size_t total = colorOff + colorBytes;
+		const ProgramLayout l = LayoutOf(p);
 		cudaError_t e = cudaGetDevice(&p.DeviceId);
 		if (e != cudaSuccess) return e;
-		e = cudaMalloc(&p.Device, total);
+		e = cudaMalloc(&p.Device, l.Total);
 		if (e != cudaSuccess) { p.Device = nullptr; return e; }
-		std::vector<uint8_t> staging(total, 0);
-		std::memcpy(staging.data(), p.Host.Nodes.data(), nodeBytes);
-		std::memcpy(staging.data() + codeOff, p.Host.Code.data(), codeBytes);
-		if (!p.Host.Colors.empty()) std::memcpy(staging.data() + colorOff, p.Host.Colors.data(), p.Host.Colors.size());
-		e = cudaMemcpy(p.Device, staging.data(), total, cudaMemcpyHostToDevice);
+		std::vector<uint8_t> staging(l.Total, 0);
+		Pack(p, l, staging.data());
+		e = cudaMemcpy(p.Device, staging.data(), l.Total, cudaMemcpyHostToDevice);
 		if (e != cudaSuccess) return e;
-		uint8_t* base = static_cast<uint8_t*>(p.Device);
-		p.View.Nodes = reinterpret_cast<const OctNode*>(base);
-		p.View.Code = reinterpret_cast<const float4*>(base + codeOff);
-		p.View.Colors = reinterpret_cast<const uchar4*>(base + colorOff);
-		p.View.MaxStack = p.Host.Header.MaxStack;
-		p.View.FullSurfaceCode = p.Host.Header.FullSurfaceCode;
-		p.View.Lipschitz = p.Host.Header.Lipschitz;
+		Bind(p, l, p.Device);
 		return cudaSuccess;
 	}
 

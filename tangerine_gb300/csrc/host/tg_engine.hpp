@@ -58,6 +58,26 @@ namespace tg
 		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
 	};
 
+	// Sodapop's meshing job output (device pointers into the engine's buffers, valid until
+	// the next call on the engine).
+	struct SodapopMesh
+	{
+		uint64_t VertexCount = 0;
+		uint64_t FaceCount = 0;
+		float* Positions = nullptr;   // 3 per vertex
+		float* Normals = nullptr;     // 3 per vertex
+		float* Colors = nullptr;      // 4 per vertex
+		uint32_t* Faces = nullptr;    // 3 per face
+		uint32_t* Cells = nullptr;    // cell number per vertex
+		SodapopGrid Grid{};
+	};
+
+	// NaiveSurfaceNetsScratch's lattice (sodapop.cpp:150-177) for a program compiled with
+	// OctreeKind::Meshing at `density` samples per unit, and the integer boxes of its
+	// leaves' point-cache spans (sodapop.cpp:622-644).  False (with a reason) when the
+	// lattice is outside what the kernels index.
+	bool SodapopPlan(const CompiledTree& t, float density, SodapopGrid& g, std::vector<int64_t>& boxes, std::string& error);
+
 	class Engine
 	{
 	public:
@@ -81,6 +101,10 @@ namespace tg
 			uint8_t* hit, float* travel, float* position, cudaStream_t s);
 		cudaError_t Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
 			bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s, const FieldNet* field = nullptr);
+		// Sodapop's meshing job (MeshingJob::NaiveSurfaceNets) for a program compiled with
+		// OctreeKind::Meshing, planned by SodapopPlan.
+		cudaError_t Sodapop(const Program& p, const SodapopGrid& g, const std::vector<int64_t>& boxes, SodapopMesh& out,
+			cudaStream_t s);
 		// Network iterations and exact steps of the last network-stepped render.
 		uint64_t LastNetworkSteps = 0, LastExactSteps = 0;
 		DeviceBuffer& Lattice() { return LatticeBuf; }
@@ -106,6 +130,7 @@ namespace tg
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
 		DeviceBuffer Points, PointOut, BrickBits, BrickList, ProgramScratch, ActiveCells;
 		DeviceBuffer RayIn, RayOut, Cameras, Image, RenderCounters;
+		DeviceBuffer SodaBoxes, SodaCache, SodaColors;
 		void* Staging = nullptr;
 		size_t StagingBytes = 0;
 		uint32_t* HostCounts = nullptr;

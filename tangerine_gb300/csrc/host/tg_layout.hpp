@@ -4,6 +4,7 @@
 //   OctNode  nodes[node_count]      the export octree, depth-first, root first
 //   float4   code[code_quads]       every node's two programs, 16-byte records
 //   uchar4   colors[material_count] resolved material colour bytes
+//   float4   material_rgb[material_count]  each material's stored RGB (alpha 1)
 //
 // Each octree node carries two programs for its clipped subtree:
 //  * the distance program: Tangerine's postfix program (SDFNode::Compile), with each
@@ -36,12 +37,17 @@ namespace tg
 
 	constexpr int kMaxStack = 32;   // deepest postfix stack a program may need
 	constexpr int32_t kNodeTerminus = 1;
+	// The cell has no evaluator: SDFOctree::Populate found all eight children empty after
+	// the cell itself was kept (meshing octree's second stage only).  Its programs are a
+	// lone stop record.
+	constexpr int32_t kNodeNoEvaluator = 2;
 
 	struct OctNode
 	{
 		float Pivot[3];
-		int32_t Flags;              // bit 0: terminus; bits 8..15: octants whose clip returned
-		                            // null (the evaluator exceeds the octant sphere's radius)
+		int32_t Flags;              // bit 0: terminus; bit 1: no evaluator; bits 8..15: octants
+		                            // whose clip returned null (the evaluator exceeds the
+		                            // octant sphere's radius)
 		int32_t Child[8];           // -1: no child there
 		int32_t DistanceCode;       // quad offset of the distance program
 		int32_t SurfaceCode;        // quad offset of the surface program

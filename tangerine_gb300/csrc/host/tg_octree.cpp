@@ -137,10 +137,10 @@ namespace tg
 		// in parallel (the clips are independent), then the cells that go on split into
 		// eight children for the next level.  The merge decisions run afterwards, bottom up;
 		// they depend only on a cell's descendants, so the octree is the one the reference's
-		// depth-first recursion builds.
-		void BuildLevels(TmpCell& top, const BuildParams& bp, int top_depth)
+		// depth-first recursion builds.  `tops` are disjoint subtrees, all at top_depth.
+		void BuildLevels(const std::vector<TmpCell*>& tops, const BuildParams& bp, int top_depth)
 		{
-			std::vector<TmpCell*> level{ &top };
+			std::vector<TmpCell*> level = tops;
 			int depth = top_depth;
 			while (!level.empty())
 			{
@@ -168,7 +168,20 @@ namespace tg
 					for (auto& k : c->Kids) level.push_back(k.get());
 				++depth;
 			}
-			FinishTree(top, bp, top_depth);
+			for (TmpCell* t : tops) FinishTree(*t, bp, top_depth);
+		}
+
+		// SDFOctree::Walk's incomplete search (sodapop.cpp:108-124): cells that were never
+		// split because the depth limit stopped them.
+		void FindIncomplete(TmpCell& c, std::vector<TmpCell*>& out)
+		{
+			if (c.Terminus || c.Incomplete)
+			{
+				if (c.Incomplete) out.push_back(&c);
+				return;
+			}
+			for (auto& k : c.Kids)
+				if (k) FindIncomplete(*k, out);
 		}
 
 		void Flatten(TmpCell& t, std::vector<Octree::Cell>& out)
@@ -216,23 +229,54 @@ namespace tg
 		top->Bounds = cube;
 		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
-		BuildLevels(*top, bp, 1);
+		BuildLevels({ top.get() }, bp, 1);
 		Flatten(*top, Cells);
 		return true;
 	}
 
+	bool Octree::BuildMeshing(const NodeRef& root)
+	{
+		Cells.clear();
+		if (!root || !root->HasFiniteBounds()) return false;
+		AABB cube = root->Bounds().BoundingCube();
+		if (!cube.Degenerate())
+		{
+			cube.Min = cube.Min - Vec3(0.0f);
+			cube.Max = cube.Max + Vec3(0.0f);
+		}
+		if (cube.Volume() == 0.0f) return false;
+		const BuildParams first{ 0.25f, false, 3 };
+		auto top = std::make_unique<TmpCell>();
+		top->Bounds = cube;
+		InitCell(*top, root, first);
+		if (!top->Eval) return false;
+		BuildLevels({ top.get() }, first, 1);
+		// Populate(false, 3, -1) of each incomplete cell: its children start at depth 4 and
+		// split without limit.  The cells are disjoint, so one level-parallel pass serves
+		// them all.
+		std::vector<TmpCell*> incomplete;
+		FindIncomplete(*top, incomplete);
+		const BuildParams second{ 0.25f, false, -1 };
+		BuildLevels(incomplete, second, 3);
+		Flatten(*top, Cells);
+		return true;
+	}
+
+	// The deepest cell on the point's path that has an evaluator: a child whose own search
+	// finds none hands the point back to its parent.
 	int Octree::Descend(Vec3 p) const
 	{
-		int at = 0;
+		int at = 0, found = Cells[0].Evaluator ? 0 : -1;
 		for (;;)
 		{
 			const Cell& c = Cells[at];
-			if (c.Terminus) return at;
+			if (c.Evaluator) found = at;
+			if (c.Terminus) return found;
 			int i = 0;
 			if (p.x > c.Pivot.x) i |= 1;
 			if (p.y > c.Pivot.y) i |= 2;
 			if (p.z > c.Pivot.z) i |= 4;
-			if (c.Children[i] < 0) return at;
+			if (c.Children[i] < 0) return found;
 			at = c.Children[i];
 		}
 	}
@@ -535,23 +579,25 @@ namespace tg
 		return w;
 	}
 
-	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error)
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind)
 	{
 		const auto t0 = std::chrono::steady_clock::now();
 		Octree octree;
-		if (!octree.Build(root))
+		if (!(kind == OctreeKind::Meshing ? octree.BuildMeshing(root) : octree.Build(root)))
 		{
 			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
 			return false;
 		}
 		out = CompiledTree();
 		out.Bounds = root->Bounds();
+		out.OctreeBounds = octree.Cells[0].Bounds;
 		std::unordered_map<const Material*, int> materials;
 		std::vector<const Material*> materialList;
 		CollectMaterials(*root, materials, materialList);
 		out.Code.reserve(1 << 20);
 		Emitter em{ out.Code, materials, Emitter::NextEpoch(), {}, {}, false };
 		int maxStack = 0;
+		int stopQuad = -1;
 		out.Nodes.resize(octree.Cells.size());
 		for (size_t i = 0; i < octree.Cells.size(); ++i)
 		{
@@ -560,6 +606,22 @@ namespace tg
 			n.Pivot[0] = c.Pivot.x; n.Pivot[1] = c.Pivot.y; n.Pivot[2] = c.Pivot.z;
 			n.Flags = (c.Terminus ? kNodeTerminus : 0) | (int32_t)(c.NullOctants << 8);
 			for (int k = 0; k < 8; ++k) n.Child[k] = c.Children[k];
+			if (!c.Evaluator)
+			{
+				// Only the meshing octree's second stage leaves such cells; descents pass
+				// over them, and their programs are one shared stop record.
+				if (stopQuad < 0)
+				{
+					stopQuad = (int)(out.Code.size() / 4);
+					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				}
+				n.Flags |= kNodeNoEvaluator;
+				n.DistanceCode = n.SurfaceCode = stopQuad;
+				n.StackSize = 0;
+				n.ClipRadius = c.ClipRadius;
+				continue;
+			}
+			if (kind == OctreeKind::Meshing && c.Terminus) out.LeafBounds.push_back(c.Bounds);
 			const int dist = (int)(out.Code.size() / 4);
 			em.NonLipschitz = false;
 			em.Distance(*c.Evaluator);
@@ -602,6 +664,12 @@ namespace tg
 				out.Colors[m * 4 + ch] = (uint8_t)v;
 			}
 			out.Colors[m * 4 + 3] = 255;
+		}
+		out.MaterialRgb.resize(materialList.size() * 4);
+		for (size_t m = 0; m < materialList.size(); ++m)
+		{
+			for (int ch = 0; ch < 3; ++ch) out.MaterialRgb[m * 4 + ch] = materialList[m]->Rgb[ch];
+			out.MaterialRgb[m * 4 + 3] = 1.0f;
 		}
 		out.Header.NodeCount = (int32_t)out.Nodes.size();
 		out.Header.CodeQuads = (int32_t)(out.Code.size() / 4);

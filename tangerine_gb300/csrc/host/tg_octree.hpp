@@ -31,6 +31,12 @@ namespace tg
 		// Returns false (and leaves Cells empty) when the tree has infinite or empty
 		// bounds, or clips away entirely, as SDFOctree::Create returns nullptr.
 		bool Build(const NodeRef& root, float target_size = 0.25f, bool coalesce = true, int max_depth = -1);
+		// Sodapop's meshing octree (sodapop.cpp:565-567): SDFOctree::Create(.25, false, 3),
+		// then every cell left incomplete at depth 3 populated on its own with
+		// Populate(false, 3, -1).  The second stage does not revisit the ancestors, so they
+		// keep the bounds they took at depth 3, and a populated cell whose eight children
+		// all clip away stays in place without an evaluator.
+		bool BuildMeshing(const NodeRef& root);
 		int Descend(Vec3 p) const;                 // Descend(Point, Exact=true)
 	};
 
@@ -45,10 +51,17 @@ namespace tg
 		std::vector<OctNode> Nodes;
 		std::vector<float> Code;          // 4 floats per quad
 		std::vector<uint8_t> Colors;      // 4 bytes per material
+		std::vector<float> MaterialRgb;   // 4 floats per material: stored RGB, 1
 		AABB Bounds{};                    // root evaluator bounds
+		AABB OctreeBounds{};              // the octree root cell's bounds
+		std::vector<AABB> LeafBounds;     // terminus cells with an evaluator (meshing octree)
 		double BuildSeconds = 0.0;
 		int64_t DistanceQuadsTotal = 0;
 	};
 
-	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error);
+	enum class OctreeKind { Export, Meshing };
+	// Builds the octree of the given kind (Export: target 0.25 with coalescing, as the
+	// export and the point queries use; Meshing: Octree::BuildMeshing) and compiles every
+	// cell's clipped subtree.
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind = OctreeKind::Export);
 }

@@ -14,6 +14,7 @@ namespace tg
 		const OctNode* Nodes;
 		const float4* Code;
 		const uchar4* Colors;
+		const float4* MaterialRgb;  // stored RGB of each material, alpha 1
 		int MaxStack;
 		int FullSurfaceCode;    // the whole tree's surface program
 		int Lipschitz;          // every brush 1-Lipschitz
@@ -103,6 +104,40 @@ namespace tg
 	// Gradient normal and colour bytes per vertex (SDFOctree::Gradient / GetMaterial).
 	cudaError_t LaunchVertexAttributes(const DeviceProgram& prog, const float* vertices, uint32_t vertex_count,
 		float* normals, uint8_t* colors, cudaStream_t stream);
+}
+
+namespace tg
+{
+	// ---- Sodapop's meshing job (tg_sodapop.cu) ---------------------------------------
+	// NaiveSurfaceNetsScratch's lattice (sodapop.cpp:150-177): cell (i, j, k), i < SX,
+	// j < SY, is number i + j*SX + k*SX*SY and has corners at G + (i..i+1, ...) * D per
+	// axis.  The point cache holds numbers below Limit (a multiple of its 64-entry buckets),
+	// which reaches one layer past SZ; the lattice has (SX+1) x (SY+1) x LZ points.
+	struct SodapopGrid
+	{
+		float G[3];
+		float D[3];
+		int64_t SX, SY, SZ;
+		int64_t Limit;
+		int64_t LZ;
+	};
+
+	// clamp(SDFOctree::Eval(p, Exact = false), -100, 100) at every lattice point (x fastest).
+	cudaError_t LaunchSodapopLattice(const DeviceProgram& prog, const SodapopGrid& g, float* lattice, cudaStream_t stream);
+	// Point cache: cached[n] = 1 for every cell number n < Limit inside one of the leaf
+	// boxes (6 int64 per leaf: x0 x1 y0 y1 z0 z1, inclusive; n = x + y*SX + z*SX*SY).
+	cudaError_t LaunchSodapopCache(const int64_t* boxes, int leaves, const SodapopGrid& g, uint8_t* cached, cudaStream_t stream);
+	// One bit per cell number below Limit: cached and its corners not all of one sign.
+	cudaError_t LaunchSodapopFlags(const float* lattice, const uint8_t* cached, const SodapopGrid& g, uint32_t* words,
+		cudaStream_t stream);
+	// Vertex, cell number and triangle count of every flagged cell, at its rank.
+	cudaError_t LaunchSodapopVertices(const float* lattice, const SodapopGrid& g, const uint32_t* words, const uint32_t* word_base,
+		float* positions, uint32_t* cells, uint32_t* face_counts, cudaStream_t stream);
+	cudaError_t LaunchSodapopFaces(const float* lattice, const SodapopGrid& g, const uint32_t* words, const uint32_t* word_base,
+		const uint32_t* cells, const uint32_t* face_base, uint32_t vertex_count, uint32_t* faces, cudaStream_t stream);
+	// Gradient normal and shaded colour (4 floats) per vertex.
+	cudaError_t LaunchSodapopAttributes(const DeviceProgram& prog, const float* positions, uint32_t vertex_count, float* normals,
+		float* colors, cudaStream_t stream);
 }
 
 namespace tg

@@ -100,4 +100,37 @@ namespace tg
 		}
 		face_counts[vid] = faces;
 	}
+
+	// SDFNode::Gradient's evaluation points (sdf_evaluator.cpp:298-333): the four
+	// tetrahedral offsets for lanes 0..3, the point itself for lane 4.
+	__device__ __forceinline__ Vec3 TetraPoint(Vec3 p, int lane)
+	{
+		const float h = 0.0001f;
+		switch (lane)
+		{
+		case 0: return p + Vec3(h, -h, -h);
+		case 1: return p + Vec3(-h, -h, h);
+		case 2: return p + Vec3(-h, h, -h);
+		case 3: return p + Vec3(h, h, h);
+		default: return p;
+		}
+	}
+
+	// SDFNode::Gradient (sdf_evaluator.cpp:298-333) from the five evaluations.
+	__device__ __forceinline__ Vec3 GradientOf(const float* e)
+	{
+		const float h = 0.0001f;
+		const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+		Vec3 g = xyy * e[0];
+		g = g + yyx * e[1];
+		g = g + yxy * e[2];
+		g = g + xxx * e[3];
+		const float ls = (g.x * g.x + g.y * g.y) + g.z * g.z;
+		if (ls == 0.0f)
+		{
+			const float d = e[4];
+			return Normalize(Vec3(e[0] - d, e[2] - d, e[1] - d));
+		}
+		return g / sqrtf(ls);
+	}
 }

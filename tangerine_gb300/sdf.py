@@ -17,6 +17,20 @@ from . import _lib
 from ._lib import check, load
 
 
+@dataclass
+class SodapopDrawable:
+    """Sodapop's drawable buffers: positions, gradient normals, shaded RGBA colours, triangle
+    indices, each vertex's cell number, and the lattice (origin xyz, step xyz, cells xyz)."""
+    positions: np.ndarray
+    normals: np.ndarray
+    colors: np.ndarray
+    faces: np.ndarray
+    cells: np.ndarray
+    grid: np.ndarray
+    compile_seconds: float = 0.0
+    gpu_seconds: float = 0.0
+
+
 class Tree:
     """A reference-counted CSG tree handle (c_sdf.cpp's `void*` trees)."""
 
@@ -71,18 +85,54 @@ class Tree:
         load().PaintTree(r, g, b, self.handle)
         return self
 
-    def debug_octree(self):
-        """Host-built export octree in the oracle's dump layout: (cells, children, words)."""
+    def debug_octree(self, meshing=False):
+        """Host-built export octree (or Sodapop's meshing octree) in the oracle's dump
+        layout: (cells, children, words)."""
         lib = load()
+        fn = lib.tg_debug_meshing_octree if meshing else lib.tg_debug_octree
         wc = C.c_int64()
-        n = lib.tg_debug_octree(self.handle, None, None, 0, None, 0, C.byref(wc))
+        n = fn(self.handle, None, None, 0, None, 0, C.byref(wc))
         if n < 0:
             return None
         cells = np.zeros((n, 14), np.float32)
         kids = np.zeros((n, 8), np.int32)
         words = np.zeros(max(1, wc.value), np.uint32)
-        lib.tg_debug_octree(self.handle, _lib.as_ptr(cells), _lib.as_ptr(kids), n, _lib.as_ptr(words), wc.value, C.byref(wc))
+        fn(self.handle, _lib.as_ptr(cells), _lib.as_ptr(kids), n, _lib.as_ptr(words), wc.value, C.byref(wc))
         return cells, kids, words[: wc.value]
+
+    def sodapop_plan(self, density=20.0):
+        """Host-side plan of the meshing job: (grid[11], leaf boxes (n, 6) int64)."""
+        lib = load()
+        grid = np.zeros(11, np.float32)
+        n = C.c_int64()
+        check(lib.tg_debug_sodapop_plan(self.handle, float(density), _lib.as_ptr(grid), None, 0, C.byref(n)))
+        boxes = np.zeros((max(1, n.value), 6), np.int64)
+        check(lib.tg_debug_sodapop_plan(self.handle, float(density), _lib.as_ptr(grid), _lib.as_ptr(boxes), n.value, C.byref(n)))
+        return grid, boxes[: n.value]
+
+    def sodapop_mesh(self, density=20.0, stream=None) -> "SodapopDrawable":
+        """Sodapop's meshing job (MeshingJob::NaiveSurfaceNets, sodapop.cpp:562-897) on the
+        GPU; vertices in cell-number order."""
+        lib = load()
+        d = _lib.Drawable()
+        check(lib.tg_sodapop_mesh(self.handle, float(density), C.byref(d), stream))
+        try:
+            nv, nf = int(d.vertex_count), int(d.face_count)
+
+            def take(ptr, n, k, dtype):
+                if n == 0:
+                    return np.zeros((0, k), dtype)
+                return np.ctypeslib.as_array(ptr, shape=(n * k,)).reshape(n, k).astype(dtype, copy=True)
+
+            out = SodapopDrawable(
+                positions=take(d.positions, nv, 3, np.float32), normals=take(d.normals, nv, 3, np.float32),
+                colors=take(d.colors, nv, 4, np.float32), faces=take(d.faces, nf, 3, np.uint32),
+                cells=take(d.cells, nv, 1, np.uint32).reshape(-1),
+                grid=np.array([*d.grid_origin, *d.grid_step, *d.grid_cells], np.float32),
+                compile_seconds=float(d.compile_seconds), gpu_seconds=float(d.gpu_seconds))
+        finally:
+            lib.tg_drawable_free(C.byref(d))
+        return out
 
     def reference_words(self) -> np.ndarray:
         lib = load()

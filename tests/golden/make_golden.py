@@ -4,7 +4,8 @@ Run here, where the reference sources are: it builds oracle/_ref/libtangerine_re
 (``make -C oracle ref``) and records, for a handful of seeded and hand-made CSG trees,
 what the reference computes: program words, the export octree, point distances,
 gradients and colours, naive-surface-nets meshes on small export lattices (with the
-reference's gradient normals and colours per vertex) and RayMarch hits.  The reference
+reference's gradient normals and colours per vertex), RayMarch hits, and Sodapop's meshing
+job (its octree and its drawable at a reduced density).  The reference
 sources do not travel to the GPU host; these fixtures do.
 
     python tests/golden/make_golden.py
@@ -24,6 +25,8 @@ from oracle import oracle as O  # noqa: E402
 from tangerine_gb300 import workloads as W  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
+# Sodapop::Populate meshes at 20 samples per unit; 6 keeps the fixtures small.
+SODAPOP_DENSITY = 6.0
 
 
 def exotic_specs():
@@ -89,6 +92,14 @@ def main():
             rec["mesh_normals"] = R.octree_gradient(o, m.vertices)
             rec["mesh_colors"] = R.octree_color(o, m.vertices)
             R.octree_free(o)
+        mo = R.meshing_octree(h)
+        if mo is not None:
+            nodes, children, words = R.octree_dump(mo)
+            rec.update(meshing_nodes=nodes, meshing_children=children, meshing_words=words)
+            R.octree_free(mo)
+            d = R.sodapop(h, density=SODAPOP_DENSITY)
+            rec.update(soda_density=np.float32(SODAPOP_DENSITY), soda_grid=d.grid, soda_positions=d.positions,
+                       soda_normals=d.normals, soda_colors=d.colors, soda_faces=d.faces.astype(np.uint32))
         R.free(h)
         np.savez_compressed(OUT / f"{name}.npz", **rec)
         print(name, "vertices", rec.get("mesh_vertices", np.zeros((0, 3))).shape[0])

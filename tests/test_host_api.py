@@ -88,3 +88,44 @@ def test_export_lattice_matches_mesh_export_thread(lib):
         assert (g.nx, g.ny, g.nz) == (cells + 1,) * 3
         w = W.export_grid(resolution=res)
         assert (w.sx, w.x0, w.step) == (cells, g.x0, g.step)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_host_meshing_octree_matches_reference(lib, golden, name):
+    """Sodapop's two-stage meshing octree, built by the product's host code."""
+    g = golden[name]
+    dump = sdf.from_spec(g["spec"]).debug_octree(meshing=True)
+    if "meshing_nodes" not in g:
+        assert dump is None
+        return
+    cells, children, words = dump
+    np.testing.assert_array_equal(cells, g["meshing_nodes"])
+    np.testing.assert_array_equal(children, g["meshing_children"])
+    np.testing.assert_array_equal(words, g["meshing_words"])
+
+
+def _point_cache_boxes(nodes, grid):
+    """The reference's aligned leaf boxes (sodapop.cpp:630-633) in float32 arithmetic, for
+    the terminus cells that hold an evaluator, in depth-first order."""
+    f = np.float32
+    origin, step = grid[0:3].astype(f), grid[3:6].astype(f)
+    leaves = nodes[(nodes[:, 9] == 1) & (nodes[:, 10] == 1)]
+    lo = np.floor(np.maximum(f(0), leaves[:, 3:6] - origin) / step)
+    hi = np.ceil((leaves[:, 6:9] - origin) / step)
+    return np.stack([lo[:, 0], hi[:, 0], lo[:, 1], hi[:, 1], lo[:, 2], hi[:, 2]], 1).astype(np.int64)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_sodapop_plan_matches_reference(lib, golden, name):
+    """The meshing lattice and point-cache boxes the product hands its kernels."""
+    g = golden[name]
+    if "meshing_nodes" not in g:
+        pytest.skip("no octree for this tree")
+    grid, boxes = sdf.from_spec(g["spec"]).sodapop_plan(float(g["soda_density"]))
+    np.testing.assert_array_equal(grid[:9], g["soda_grid"])
+    sx, sy, sz = (int(v) for v in g["soda_grid"][6:9])
+    cells = sx * sy * sz
+    bucket = min(64, cells)
+    limit = (cells + bucket - 1) // bucket * bucket
+    assert int(grid[9]) == limit and int(grid[10]) == (limit - 1) // (sx * sy) + 2
+    np.testing.assert_array_equal(boxes, _point_cache_boxes(g["meshing_nodes"], g["soda_grid"]))

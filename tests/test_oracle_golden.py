@@ -75,3 +75,31 @@ def test_planted_mistake_is_caught(port, golden):
         assert not np.array_equal(port.compile(h), g["words"])
     finally:
         port.free(h)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_sodapop_meshing_job(port, golden, name):
+    """Sodapop's meshing octree and drawable (MeshingJob::NaiveSurfaceNets) against the
+    reference's serial replay: vertices, normals and colours in cell order, faces as a set
+    (the reference's face order follows its own vertex traversal)."""
+    g = golden[name]
+    if "meshing_nodes" not in g:
+        pytest.skip("no octree for this tree")
+    h = port.build(g["spec"])
+    try:
+        mo = port.meshing_octree(h)
+        try:
+            nodes, children, words = port.octree_dump(mo)
+        finally:
+            port.octree_free(mo)
+        np.testing.assert_array_equal(nodes, g["meshing_nodes"])
+        np.testing.assert_array_equal(children, g["meshing_children"])
+        np.testing.assert_array_equal(words, g["meshing_words"])
+        d = port.sodapop(h, density=float(g["soda_density"]))
+        np.testing.assert_array_equal(d.grid, g["soda_grid"])
+        np.testing.assert_array_equal(d.positions, g["soda_positions"])
+        np.testing.assert_array_equal(d.normals, g["soda_normals"])
+        np.testing.assert_array_equal(d.colors, g["soda_colors"])
+        np.testing.assert_array_equal(sorted_faces(d.faces), sorted_faces(g["soda_faces"]))
+    finally:
+        port.free(h)
