@@ -276,6 +276,46 @@ typedef struct tg_drawable
 TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream);
 TANGERINE_API void tg_drawable_free(tg_drawable* drawable);
 
+/* PointCloudExportThread (export.cpp:384-480) on the GPU: the centres of the voxels of the
+ * ceil((max - min) / step) lattice from model_min whose octree distance is below the
+ * half-voxel diagonal, moved by refine_iterations steps of -distance along the gradient,
+ * clamped to the voxel and kept only when they stay within the diagonal; with
+ * TG_MESH_ATTRIBUTES, gradient normals and colour bytes as WritePLY(Octree, ...) takes them.
+ * The reference's threads push points in a run-dependent order; here they come in voxel
+ * order.  Results as a tg_mesh without faces (cubes = each point's voxel number, x
+ * fastest); release with tg_mesh_free. */
+TANGERINE_API tg_status tg_export_point_cloud(tg_program* program, const float model_min[3], const float model_max[3],
+                                              const float step[3], int refine_iterations, uint32_t flags, tg_mesh* out,
+                                              void* stream);
+
+/* VoxExport's voxels (magica.cpp:27-72) on the GPU: the ivec3(ceil(max - min) * grid_size)
+ * lattice over the tree bounds, a voxel kept when |SDFNode::Eval| at its centre
+ * mix(min, max, (i + .5) / size) is at most the half-voxel radius; colour index
+ * abs(color_index) % 255 + 1.  Voxels in voxel order (x fastest). */
+typedef struct tg_voxels
+{
+	uint64_t count;
+	int32_t* voxels;            /* 4 per voxel: x, y, z, colour index */
+	int32_t size[3];
+	float radius;
+} tg_voxels;
+
+TANGERINE_API tg_status tg_export_voxels(tg_program* program, float grid_size, int color_index, tg_voxels* out, void* stream);
+TANGERINE_API void tg_voxels_free(tg_voxels* voxels);
+/* The MagicaVoxel file VoxWriter writes for these voxels added in order (version 150, one
+ * model per 126-voxel cube, a transform per cube, no palette). */
+TANGERINE_API tg_status tg_write_vox(const tg_voxels* voxels, const char* path);
+/* ExportMagicaVoxel (magica.cpp:79-83, shipped disabled): voxelise the tree and write the
+ * file, synchronously. */
+TANGERINE_API void ExportMagicaVoxel(void* Handle, float GridSize, int ColorIndex, const char* Path);
+/* MeshExport (export.h:37, export.cpp:566-580) synchronously: Format 0 = STL, 1 = PLY, as
+ * ExportFormat; ExportPointCloud selects the point-cloud export (PLY only, as the reference
+ * writes nothing else for it).  Vertices are multiplied by Scale when written.  The mesh
+ * export takes one step for all axes here (TG_ERR_UNSUPPORTED otherwise); RefineIterations
+ * applies to point clouds only, as in the reference. */
+TANGERINE_API tg_status MeshExport(void* Handle, const char* Path, const float ModelMin[3], const float ModelMax[3],
+                                   const float Step[3], int RefineIterations, int Format, bool ExportPointCloud, float Scale);
+
 /* SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the whole tree for n rays, on the GPU:
  * the reference's step sequence, so hit flags, travel (+inf on a miss) and end positions
  * match it bit for bit.  Host arrays, 3 floats per origin / direction / position. */

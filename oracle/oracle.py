@@ -65,6 +65,10 @@ class Drawable:
         self.grid = grid
 
 
+def _vec3(v):
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float32), (3,)))
+
+
 class CpuOracle:
     def __init__(self, path: Path, prefix: str):
         self.path = Path(path)
@@ -108,6 +112,7 @@ class CpuOracle:
                                                   C.POINTER(C.c_int64), _f32p])
         self._oct_grid = None
         self._raymarch = None
+        self._i32pp = C.POINTER(C.POINTER(C.c_int32))
 
     # -- trees ----------------------------------------------------------------------
     def build(self, spec) -> int:
@@ -253,6 +258,8 @@ class PortOracle(CpuOracle):
         self._attrs = self._fn("vertex_attributes", None, [vp, i64, _f32p, i, _f32p, C.c_void_p])
         self._oct_paint = self._fn("octree_has_paint", i, [vp])
         self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
+        self._cloud = self._fn("point_cloud", i64, [vp, _f32p, _f32p, _f32p, i, C.POINTER(C.POINTER(C.c_float)), self._i32pp])
+        self._vox = self._fn("vox", i64, [vp, f, i, C.POINTER(C.c_int32), C.POINTER(C.c_float), self._i32pp])
         self._hw = self._fn("hardware_threads", i, [])
 
     def hardware_threads(self):
@@ -317,6 +324,28 @@ class PortOracle(CpuOracle):
         return hit.astype(bool), travel, pos
 
 
+    def point_cloud(self, o, lo, hi, step, refine):
+        """PointCloudExportThread's points in cell order (export.cpp:384-480): (points, cells)."""
+        P = C.POINTER(C.c_float)()
+        I = C.POINTER(C.c_int32)()
+        n = self._cloud(o, _vec3(lo), _vec3(hi), _vec3(step), int(refine), C.byref(P), C.byref(I))
+        pts = np.ctypeslib.as_array(P, shape=(max(1, n) * 3,))[: n * 3].reshape(n, 3).copy()
+        cells = np.ctypeslib.as_array(I, shape=(max(1, n),))[:n].copy()
+        for b in (P, I):
+            self._free_buffer(C.cast(b, C.c_void_p))
+        return pts, cells
+
+    def vox(self, h, grid_size, color_index=0):
+        """VoxExport's voxels in cell order (magica.cpp:27-69): ((n, 4) x y z colour, size, radius)."""
+        V = C.POINTER(C.c_int32)()
+        size = (C.c_int32 * 3)()
+        radius = C.c_float()
+        n = self._vox(h, float(grid_size), int(color_index), size, C.byref(radius), C.byref(V))
+        vox = np.ctypeslib.as_array(V, shape=(max(1, n) * 4,))[: n * 4].reshape(n, 4).copy()
+        self._free_buffer(C.cast(V, C.c_void_p))
+        return vox, tuple(size), float(radius.value)
+
+
 class ReferenceOracle(CpuOracle):
     def __init__(self, path: Path = REF_SO):
         super().__init__(path, "ref_")
@@ -326,6 +355,11 @@ class ReferenceOracle(CpuOracle):
                                                   C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_uint64)),
                                                   C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(C.c_int64), C.POINTER(C.c_double)])
         self._export_file = self._fn("mesh_export_file", None, [vp, f, f, f, f, f, f, f, i, C.c_char_p])
+        self._cloud_file = self._fn("point_cloud_file", None, [vp, _f32p, _f32p, _f32p, i, f, C.c_char_p])
+        self._vox_file = self._fn("vox_file", None, [vp, f, i, C.c_char_p])
+        self._vox_write = self._fn("vox_write", None, [C.POINTER(C.c_int32), i64, C.POINTER(C.c_int32), C.c_char_p])
+        self._vox_serial = self._fn("vox_serial", i64, [vp, f, i, C.c_char_p, self._i32pp, C.POINTER(C.c_int32),
+                                                        C.POINTER(C.c_float)])
         self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
 
     def octree_grid(self, o, grid):
@@ -352,6 +386,31 @@ class ReferenceOracle(CpuOracle):
     def export_file(self, h, lo, hi, step, path, fmt="ply"):
         self._export_file(h, *[float(v) for v in lo], *[float(v) for v in hi], float(step),
                           1 if fmt == "ply" else 0, str(path).encode())
+
+    def point_cloud_file(self, h, lo, hi, step, refine, path, scale=1.0):
+        """PointCloudExportThread writing its PLY (threaded: rows in run-dependent order)."""
+        self._cloud_file(h, _vec3(lo), _vec3(hi), _vec3(step), int(refine), float(scale), str(path).encode())
+
+    def vox_file(self, h, grid_size, color_index, path):
+        """VoxExport as shipped (threaded)."""
+        self._vox_file(h, float(grid_size), int(color_index), str(path).encode())
+
+    def vox_write(self, voxels, size, path):
+        """VoxWriter fed (x, y, z, colour) rows in order, saved to path."""
+        v = np.ascontiguousarray(np.asarray(voxels, np.int32).reshape(-1, 4))
+        sz = (C.c_int32 * 3)(*[int(x) for x in size])
+        self._vox_write(v.ctypes.data_as(C.POINTER(C.c_int32)), v.shape[0], sz, str(path).encode())
+
+    def vox_serial(self, h, grid_size, color_index=0, path=None):
+        """VoxExport run serially in cell order through VoxWriter: ((n, 4) voxels, size, radius)."""
+        V = C.POINTER(C.c_int32)()
+        size = (C.c_int32 * 3)()
+        radius = C.c_float()
+        n = self._vox_serial(h, float(grid_size), int(color_index), (str(path) if path else "").encode(), C.byref(V), size,
+                             C.byref(radius))
+        vox = np.ctypeslib.as_array(V, shape=(max(1, n) * 4,))[: n * 4].reshape(n, 4).copy()
+        self._free_buffer(C.cast(V, C.c_void_p))
+        return vox, tuple(size), float(radius.value)
 
     def raymarch(self, h, origins, dirs, iterations=100, epsilon=1e-3, threads=0):
         o = self._pts(origins)
@@ -395,3 +454,43 @@ def read_ply(path):
     fdt = np.dtype([("k", "u1"), ("i", "<u4", 3)])
     faces = np.frombuffer(data, dtype=fdt, count=nf, offset=off)
     return header, vert["p"].copy(), vert["n"].copy(), (vert["c"].copy() if color else None), faces["i"].astype(np.uint64)
+
+
+def read_vox(path):
+    """Parses a MagicaVoxel file as VoxWriter writes it (voxwriter/VoxWriter.cpp): version,
+    the models' (size, (n, 4) uint8 voxels x y z colour) in file order, and each shape
+    transform's "_t" translation in scene order."""
+    data = Path(path).read_bytes()
+    assert data[:4] == b"VOX "
+    version = int.from_bytes(data[4:8], "little")
+    assert data[8:12] == b"MAIN"
+    pos = 20
+    models, translations = [], []
+    size = None
+    while pos < len(data):
+        cid = data[pos:pos + 4]
+        content = int.from_bytes(data[pos + 4:pos + 8], "little")
+        body = data[pos + 12:pos + 12 + content]
+        if cid == b"SIZE":
+            size = tuple(int.from_bytes(body[i:i + 4], "little", signed=True) for i in (0, 4, 8))
+        elif cid == b"XYZI":
+            n = int.from_bytes(body[:4], "little")
+            models.append((size, np.frombuffer(body[4:4 + 4 * n], np.uint8).reshape(n, 4).copy()))
+        elif cid == b"nTRN":
+            q = 4
+            nattr = int.from_bytes(body[q:q + 4], "little"); q += 4
+            for _ in range(2 * nattr):
+                q += 4 + int.from_bytes(body[q:q + 4], "little")
+            q += 16
+            nframes = int.from_bytes(body[q - 4:q], "little")
+            for _ in range(nframes):
+                nkeys = int.from_bytes(body[q:q + 4], "little"); q += 4
+                kv = []
+                for _ in range(2 * nkeys):
+                    ln = int.from_bytes(body[q:q + 4], "little")
+                    kv.append(body[q + 4:q + 4 + ln].decode()); q += 4 + ln
+                d = dict(zip(kv[::2], kv[1::2]))
+                if "_t" in d:
+                    translations.append(tuple(int(v) for v in d["_t"].split()))
+        pos += 12 + content
+    return version, models, translations

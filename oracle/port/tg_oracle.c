@@ -1902,3 +1902,111 @@ int64_t tgo_sodapop(tgo_tree* tree, float density, float** positions, float** no
 	*face_count = nf;
 	return nv;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* PointCloudExportThread (export.cpp:384-480), serially in cell order.                   */
+int64_t tgo_point_cloud(tgo_octree* T, const float* lo, const float* hi, const float* step, int refine,
+	float** points, int32_t** cells)
+{
+	/* Half = Step / vec3(2.0); Diagonal = length(Half) */
+	const v3 Step = V3(step[0], step[1], step[2]);
+	const v3 Half = V3(Step.x / 2.0f, Step.y / 2.0f, Step.z / 2.0f);
+	const float diag = len3(Half);
+	const v3 Start = V3(lo[0], lo[1], lo[2]);
+	/* ivec3(ceil((Stop - Start) / Step)) */
+	const int ix = (int)ceilf((hi[0] - Start.x) / Step.x);
+	const int iy = (int)ceilf((hi[1] - Start.y) / Step.y);
+	const int iz = (int)ceilf((hi[2] - Start.z) / Step.z);
+	const int slice = ix * iy;
+	const int total = ix * iy * iz;
+	int64_t n = 0, cap = 1024;
+	float* P = (float*)malloc(sizeof(float) * 3 * (size_t)cap);
+	int32_t* I = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+	for (int i = 0; i < total; ++i)
+	{
+		const float Z = (float)(i / slice) * Step.z + Start.z;
+		const float Y = (float)((i % slice) / ix) * Step.y + Start.y;
+		const float X = (float)(i % ix) * Step.x + Start.x;
+		const v3 c = add3(V3(X, Y, Z), Half);
+		const float d = octree_eval_point(T, c, 1);
+		if (!(fabsf(d) < diag)) continue;
+		if (n == cap)
+		{
+			cap *= 2;
+			P = (float*)realloc(P, sizeof(float) * 3 * (size_t)cap);
+			I = (int32_t*)realloc(I, sizeof(int32_t) * (size_t)cap);
+		}
+		P[n * 3] = c.x; P[n * 3 + 1] = c.y; P[n * 3 + 2] = c.z;
+		I[n++] = i;
+	}
+	for (int64_t k = 0; k < n && refine > 0; ++k)
+	{
+		const v3 V = V3(P[k * 3], P[k * 3 + 1], P[k * 3 + 2]);
+		const v3 low = sub3(V, Half), high = add3(V, Half);
+		v3 cur = V;
+		for (int r = 0; r < refine; ++r)
+		{
+			const v3 dir = node_gradient(octree_select(T, cur), cur);
+			/* Octree->Eval(Cursor) * -1.0 in double, stored to float: the exact negation. */
+			const float dist = (float)((double)octree_eval_point(T, cur, 1) * -1.0);
+			cur = add3(cur, muls3(dir, dist));
+		}
+		/* glm::clamp(x, lo, hi) = min(max(x, lo), hi) per component */
+		cur = gmin3(gmax3(cur, low), high);
+		if (len3(sub3(V, cur)) <= diag)
+		{
+			P[k * 3] = cur.x; P[k * 3 + 1] = cur.y; P[k * 3 + 2] = cur.z;
+		}
+	}
+	*points = P;
+	*cells = I;
+	return n;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* VoxExport's voxel test (magica.cpp:27-69), serially in cell order: the voxels whose     */
+/* centre's full-tree distance is within the half-voxel radius.                            */
+static v3 glm_mix3(v3 x, v3 y, v3 a)
+{
+	/* glm::mix(x, y, a) for vectors: x * (1 - a) + y * a */
+	const v3 one_minus = V3(1.0f - a.x, 1.0f - a.y, 1.0f - a.z);
+	return add3(mul3(x, one_minus), mul3(y, a));
+}
+
+int64_t tgo_vox(tgo_tree* tree, float grid_size, int color_index, int32_t* size_out, float* radius_out, int32_t** voxels)
+{
+	const aabb B = node_bounds(tree->root, 0);
+	/* ivec3(glm::ceil(Max - Min) * GridSize) */
+	const int sx = (int)(ceilf(B.max.x - B.min.x) * grid_size);
+	const int sy = (int)(ceilf(B.max.y - B.min.y) * grid_size);
+	const int sz = (int)(ceilf(B.max.z - B.min.z) * grid_size);
+	const v3 fs = V3((float)sx, (float)sy, (float)sz);
+	const v3 a0 = V3(0.5f / fs.x, 0.5f / fs.y, 0.5f / fs.z);
+	/* glm::distance(Min, mix(Min, Max, Alpha)) = length(mix - Min) */
+	const float radius = len3(sub3(glm_mix3(B.min, B.max, a0), B.min));
+	const int slice = sx * sy;
+	const int total = sx * sy * sz;
+	const int color = abs(color_index) % 255 + 1;
+	int64_t n = 0, cap = 1024;
+	int32_t* out = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)cap);
+	for (int i = 0; i < total; ++i)
+	{
+		const int z = i / slice, y = (i % slice) / sx, x = i % sx;
+		/* vec3(x + .5, ...) converts the double sums to float */
+		const v3 alpha = V3((float)((double)x + .5) / fs.x, (float)((double)y + .5) / fs.y, (float)((double)z + .5) / fs.z);
+		const v3 p = glm_mix3(B.min, B.max, alpha);
+		const float d = node_eval(tree->root, p);
+		if (!(fabsf(d) <= radius)) continue;
+		if (n == cap)
+		{
+			cap *= 2;
+			out = (int32_t*)realloc(out, sizeof(int32_t) * 4 * (size_t)cap);
+		}
+		out[n * 4] = x; out[n * 4 + 1] = y; out[n * 4 + 2] = z; out[n * 4 + 3] = color;
+		++n;
+	}
+	size_out[0] = sx; size_out[1] = sy; size_out[2] = sz;
+	*radius_out = radius;
+	*voxels = out;
+	return n;
+}

@@ -84,6 +84,16 @@ int tgo_hardware_threads(void);
 int64_t tgo_sodapop(tgo_tree* tree, float density, float** positions, float** normals, float** colors, uint64_t** faces,
 	int64_t* face_count, float* grid_out);
 
+/* PointCloudExportThread (export.cpp:384-480) in cell order: cell centres of the
+ * ceil((max - min) / step) lattice with |octree distance| < |step / 2|, refined by
+ * `refine` gradient steps and kept within their voxel.  points: 3 floats per point, cells:
+ * the lattice cell number (malloc'd).  Returns the point count. */
+int64_t tgo_point_cloud(tgo_octree* octree, const float* min3, const float* max3, const float* step3, int refine,
+                        float** points, int32_t** cells);
+/* VoxExport's voxel test (magica.cpp:27-69) in cell order: voxels gets x, y, z, colour index
+ * per voxel (malloc'd); size_out the lattice, radius_out the half-voxel radius. */
+int64_t tgo_vox(tgo_tree* tree, float grid_size, int color_index, int32_t* size_out, float* radius_out, int32_t** voxels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,8 @@
 #include "sdf_evaluator.h"
 #include "material.h"
 #include "export.h"
+#include "magica.h"
+#include <VoxWriter.h>
 #include "painting_set.h"
 #include "threadpool.h"
 #include <surface_nets.h>
@@ -43,6 +45,7 @@ extern std::atomic_int GenerationProgress;
 extern std::atomic_int RefinementProgress;
 extern std::atomic_int WriteProgress;
 void MeshExportThread(SDFNodeShared Evaluator, vec3 ModelMin, vec3 ModelMax, vec3 Step, int RefineIterations, std::string Path, ExportFormat Format, float Scale);
+void PointCloudExportThread(SDFNodeShared Evaluator, vec3 ModelMin, vec3 ModelMax, vec3 Step, int RefineIterations, std::string Path, ExportFormat Format, float Scale);
 
 namespace
 {
@@ -674,6 +677,80 @@ extern "C"
 		WriteProgress.store(0);
 		MeshExportThread(((RefTree*)Handle)->Root, vec3(MinX, MinY, MinZ), vec3(MaxX, MaxY, MaxZ), vec3(Step), 0,
 			std::string(Path), Format == 0 ? ExportFormat::STL : ExportFormat::PLY, 1.0f);
+	}
+
+	// The reference's point-cloud export (export.cpp:384-480) writing a PLY file.  Its
+	// threads push points in a run-dependent order; every row is a function of its cell.
+	void ref_point_cloud_file(void* Handle, const float* Min, const float* Max, const float* Step, int RefineIterations,
+		float Scale, const char* Path)
+	{
+		ExportActive.store(true);
+		ExportState.store(1);
+		GenerationProgress.store(0);
+		RefinementProgress.store(0);
+		WriteProgress.store(0);
+		PointCloudExportThread(((RefTree*)Handle)->Root, vec3(Min[0], Min[1], Min[2]), vec3(Max[0], Max[1], Max[2]),
+			vec3(Step[0], Step[1], Step[2]), RefineIterations, std::string(Path), ExportFormat::PLY, Scale);
+	}
+
+	// The reference's MagicaVoxel export (magica.cpp:27-72) as shipped: threads add voxels in a
+	// run-dependent order, which moves cubes and one translation in the file.
+	void ref_vox_file(void* Handle, float GridSize, int ColorIndex, const char* Path)
+	{
+		std::string P(Path);
+		VoxExport(((RefTree*)Handle)->Root, P, GridSize, ColorIndex);
+	}
+
+	// VoxExport's loop (magica.cpp:29-69) run serially in cell order, through the same
+	// VoxWriter, so the file bytes are deterministic.  Returns the voxel count; Voxels gets
+	// x, y, z, colour index per voxel (malloc'd) and Size the lattice.
+	int64_t ref_vox_serial(void* Handle, float GridSize, int ColorIndex, const char* Path, int32_t** Voxels, int32_t* SizeOut,
+		float* RadiusOut)
+	{
+		SDFNodeShared Evaluator = ((RefTree*)Handle)->Root;
+		AABB Bounds = Evaluator->Bounds();
+		glm::ivec3 Size = glm::ivec3(glm::ceil(Bounds.Max - Bounds.Min) * GridSize);
+		float Radius;
+		{
+			glm::vec3 Alpha = glm::vec3(.5, .5, .5) / glm::vec3(Size);
+			Radius = glm::distance(Bounds.Min, glm::mix(Bounds.Min, Bounds.Max, Alpha));
+		}
+		const int Slice = Size.x * Size.y;
+		const int TotalCells = Size.x * Size.y * Size.z;
+		vox::VoxWriter Writer(Size.x, Size.y, Size.z);
+		std::vector<int32_t> Out;
+		for (int i = 0; i < TotalCells; ++i)
+		{
+			int z = i / Slice;
+			int y = (i % Slice) / Size.x;
+			int x = i % Size.x;
+			glm::vec3 Alpha = glm::vec3(x + .5, y + .5, z + .5) / glm::vec3(Size);
+			glm::vec3 Point = glm::mix(Bounds.Min, Bounds.Max, Alpha);
+			float Dist = Evaluator->Eval(Point);
+			if (std::abs(Dist) <= Radius)
+			{
+				const int Color = abs(ColorIndex) % 255 + 1;
+				Writer.AddVoxel(x, y, z, Color);
+				Out.push_back(x); Out.push_back(y); Out.push_back(z); Out.push_back(Color);
+			}
+		}
+		if (Path && Path[0]) Writer.SaveToFile(std::string(Path));
+		*Voxels = CopyOut(Out);
+		SizeOut[0] = Size.x; SizeOut[1] = Size.y; SizeOut[2] = Size.z;
+		*RadiusOut = Radius;
+		return (int64_t)(Out.size() / 4);
+	}
+
+	// VoxWriter given voxels (x, y, z, colour) in order, for checking a writer on volumes
+	// larger than one 126-voxel cube.
+	void ref_vox_write(const int32_t* Voxels, int64_t Count, const int32_t* Size, const char* Path)
+	{
+		vox::VoxWriter Writer(Size[0], Size[1], Size[2]);
+		for (int64_t v = 0; v < Count; ++v)
+		{
+			Writer.AddVoxel(Voxels[v * 4], Voxels[v * 4 + 1], Voxels[v * 4 + 2], (uint8_t)Voxels[v * 4 + 3]);
+		}
+		Writer.SaveToFile(std::string(Path));
 	}
 
 	// SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the full tree.

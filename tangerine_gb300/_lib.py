@@ -75,6 +75,10 @@ class Drawable(C.Structure):
                 ("grid_cells", C.c_int64 * 3), ("compile_seconds", C.c_double), ("gpu_seconds", C.c_double)]
 
 
+class Voxels(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("voxels", C.POINTER(C.c_int32)), ("size", C.c_int32 * 3), ("radius", C.c_float)]
+
+
 # Every exported symbol with its signature: (restype, argtypes).
 _vp, _f, _i, _i64, _u32 = C.c_void_p, C.c_float, C.c_int, C.c_int64, C.c_uint32
 SIGNATURES = {
@@ -115,6 +119,12 @@ SIGNATURES = {
     "tg_debug_meshing_octree": (_i64, [_vp, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i64)]),
     "tg_debug_sodapop_plan": (_i, [_vp, _f, _vp, _vp, _i64, C.POINTER(_i64)]),
     "tg_sodapop_mesh": (_i, [_vp, _f, C.POINTER(Drawable), _vp]),
+    "tg_export_point_cloud": (_i, [_vp, _vp, _vp, _vp, _i, _u32, C.POINTER(HostMesh), _vp]),
+    "tg_export_voxels": (_i, [_vp, _f, _i, C.POINTER(Voxels), _vp]),
+    "tg_voxels_free": (None, [C.POINTER(Voxels)]),
+    "tg_write_vox": (_i, [C.POINTER(Voxels), C.c_char_p]),
+    "ExportMagicaVoxel": (None, [_vp, _f, _i, C.c_char_p]),
+    "MeshExport": (_i, [_vp, C.c_char_p, _vp, _vp, _vp, _i, _i, C.c_bool, _f]),
     "tg_drawable_free": (None, [C.POINTER(Drawable)]),
     "tg_export_grid": (_i, [_vp, _vp, _f, C.POINTER(Grid)]),
     "tg_eval_grid": (_i, [_vp, C.POINTER(Grid), _vp, _i, _vp]),

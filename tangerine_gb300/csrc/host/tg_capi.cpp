@@ -462,6 +462,125 @@ extern "C"
 		return st;
 	}
 
+	TANGERINE_API tg_status tg_export_point_cloud(tg_program* p, const float lo[3], const float hi[3], const float step[3],
+		int refine_iterations, uint32_t flags, tg_mesh* out, void* stream)
+	{
+		if (!p || !lo || !hi || !step || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::memset(out, 0, sizeof *out);
+		if (refine_iterations < 0) { SetError("negative refinement count"); return TG_ERR_INVALID; }
+		CloudSpec cs;
+		std::string err;
+		if (!CloudPlan(lo, hi, step, cs, err)) { SetError(err); return TG_ERR_UNSUPPORTED; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t s = StreamOf(stream);
+		DeviceMesh dm;
+		cudaError_t e = eng.PointCloud(*p, cs, refine_iterations, (flags & TG_MESH_ATTRIBUTES) != 0, dm, s);
+		if (e != cudaSuccess) return CudaFail(e, "exporting the point cloud");
+		return CopyMeshToHost(dm, out, s);
+	}
+
+	TANGERINE_API tg_status tg_export_voxels(tg_program* p, float grid_size, int color_index, tg_voxels* out, void* stream)
+	{
+		if (!p || !out) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::memset(out, 0, sizeof *out);
+		VoxSpec vs;
+		std::string err;
+		if (!VoxPlan(p->Host.Bounds, grid_size, vs, err)) { SetError(err); return TG_ERR_UNSUPPORTED; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		std::vector<uint32_t> cells;
+		cudaError_t e = eng.Voxels(*p, vs, cells, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "voxelising the tree");
+		out->voxels = (int32_t*)std::malloc(sizeof(int32_t) * 4 * (cells.empty() ? 1 : cells.size()));
+		if (!out->voxels) { SetError("out of host memory for the voxels"); return TG_ERR_MEMORY; }
+		// int z = i / Slice, y = (i % Slice) / Size.x, x = i % Size.x; abs(ColorIndex) % 255 + 1
+		const int32_t slice = vs.SX * vs.SY;
+		const int32_t color = std::abs(color_index) % 255 + 1;
+		for (size_t v = 0; v < cells.size(); ++v)
+		{
+			const int32_t i = (int32_t)cells[v];
+			out->voxels[v * 4 + 0] = i % vs.SX;
+			out->voxels[v * 4 + 1] = (i % slice) / vs.SX;
+			out->voxels[v * 4 + 2] = i / slice;
+			out->voxels[v * 4 + 3] = color;
+		}
+		out->count = cells.size();
+		out->size[0] = vs.SX; out->size[1] = vs.SY; out->size[2] = vs.SZ;
+		out->radius = vs.Radius;
+		return TG_OK;
+	}
+
+	TANGERINE_API void tg_voxels_free(tg_voxels* v)
+	{
+		if (!v) return;
+		std::free(v->voxels);
+		std::memset(v, 0, sizeof *v);
+	}
+
+	TANGERINE_API tg_status tg_write_vox(const tg_voxels* v, const char* path)
+	{
+		if (!v || !path || (v->count && !v->voxels)) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (!WriteVoxFile(path, v->size, v->voxels, (size_t)v->count)) { WriteFileError(path); return TG_ERR_IO; }
+		return TG_OK;
+	}
+
+	TANGERINE_API void ExportMagicaVoxel(void* h, float grid_size, int color_index, const char* path)
+	{
+		if (!h || !path) { SetError("invalid export arguments"); return; }
+		tg_program* prog = nullptr;
+		if (tg_compile(h, &prog) != TG_OK) return;
+		tg_voxels v;
+		if (tg_export_voxels(prog, grid_size, color_index, &v, nullptr) == TG_OK)
+		{
+			tg_write_vox(&v, path);
+			tg_voxels_free(&v);
+		}
+		tg_program_free(prog);
+	}
+
+	TANGERINE_API tg_status MeshExport(void* h, const char* path, const float lo[3], const float hi[3], const float step[3],
+		int refine_iterations, int format, bool point_cloud, float scale)
+	{
+		if (!h || !path || !lo || !hi || !step) { SetError("invalid export arguments"); return TG_ERR_INVALID; }
+		if (format != 0 && format != 1)
+		{
+			SetError("MeshExport writes STL (0) or PLY (1); MagicaVoxel files come from ExportMagicaVoxel");
+			return TG_ERR_UNSUPPORTED;
+		}
+		if (point_cloud && format != 1)
+		{
+			SetError("the point-cloud export writes PLY only");
+			return TG_ERR_UNSUPPORTED;
+		}
+		if (!point_cloud && !(step[0] == step[1] && step[1] == step[2]))
+		{
+			SetError("the mesh export takes one step for all three axes");
+			return TG_ERR_UNSUPPORTED;
+		}
+		tg_program* prog = nullptr;
+		tg_status st = tg_compile(h, &prog);
+		if (st != TG_OK) return st;
+		tg_mesh m;
+		if (point_cloud)
+		{
+			st = tg_export_point_cloud(prog, lo, hi, step, refine_iterations, TG_MESH_ATTRIBUTES, &m, nullptr);
+		}
+		else
+		{
+			tg_grid g;
+			st = tg_export_grid(lo, hi, step[0], &g);
+			if (st == TG_OK) st = tg_export_mesh(prog, &g, TG_MESH_ATTRIBUTES, &m, nullptr);
+		}
+		if (st == TG_OK)
+		{
+			st = format == 1 ? tg_write_ply(&m, path, scale) : tg_write_stl(prog, &m, path, scale, nullptr);
+			tg_mesh_free(&m);
+		}
+		tg_program_free(prog);
+		return st;
+	}
+
 	TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream)
 	{
 		if (!out) { SetError("null argument"); return TG_ERR_INVALID; }

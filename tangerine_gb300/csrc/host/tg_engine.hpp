@@ -78,6 +78,15 @@ namespace tg
 	// lattice is outside what the kernels index.
 	bool SodapopPlan(const CompiledTree& t, float density, SodapopGrid& g, std::vector<int64_t>& boxes, std::string& error);
 
+	// PointCloudExportThread's lattice (export.cpp:384-400) for (min, max, step); false
+	// when it is empty or beyond the reference's int cell numbers.
+	bool CloudPlan(const float lo[3], const float hi[3], const float step[3], CloudSpec& s, std::string& error);
+	// VoxExport's lattice and radius (magica.cpp:29-40) over `bounds` at grid_size.
+	bool VoxPlan(const AABB& bounds, float grid_size, VoxSpec& s, std::string& error);
+	// VoxWriter::SaveToFile (voxwriter/VoxWriter.cpp:560-660) for voxels (x, y, z, colour
+	// index) added in the given order to a writer whose cube limits are `size`.
+	bool WriteVoxFile(const std::string& path, const int32_t size[3], const int32_t* xyzc, size_t count);
+
 	class Engine
 	{
 	public:
@@ -105,6 +114,12 @@ namespace tg
 		// OctreeKind::Meshing, planned by SodapopPlan.
 		cudaError_t Sodapop(const Program& p, const SodapopGrid& g, const std::vector<int64_t>& boxes, SodapopMesh& out,
 			cudaStream_t s);
+		// PointCloudExportThread on the GPU: the kept voxel centres (cell order), refined,
+		// with gradient normals and colours when `attributes`; Cubes holds each point's
+		// voxel number, Faces nothing.
+		cudaError_t PointCloud(const Program& p, const CloudSpec& s, int refine, bool attributes, DeviceMesh& out, cudaStream_t st);
+		// VoxExport's voxel test on the GPU: the kept voxel numbers in order, to the host.
+		cudaError_t Voxels(const Program& p, const VoxSpec& s, std::vector<uint32_t>& cells, cudaStream_t st);
 		// Network iterations and exact steps of the last network-stepped render.
 		uint64_t LastNetworkSteps = 0, LastExactSteps = 0;
 		DeviceBuffer& Lattice() { return LatticeBuf; }

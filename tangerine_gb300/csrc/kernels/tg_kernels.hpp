@@ -142,6 +142,38 @@ namespace tg
 
 namespace tg
 {
+	// ---- point-cloud and MagicaVoxel exports (tg_exports.cu) --------------------------
+	// PointCloudExportThread's lattice (export.cpp:384-400): IX*IY*IZ voxels from Start at
+	// Step per axis (IX = ceil((max - min) / step) per axis), centres offset by Half.
+	struct CloudSpec
+	{
+		float Start[3];
+		float Step[3];
+		float Half[3];          // Step / 2
+		float Diagonal;         // length(Half)
+		int32_t IX, IY, IZ;
+		int64_t Total;          // IX * IY * IZ (< 2^31, the reference's int)
+	};
+	// VoxExport's lattice (magica.cpp:29-40): SX*SY*SZ voxels over the tree bounds.
+	struct VoxSpec
+	{
+		float Min[3], Max[3];
+		int32_t SX, SY, SZ;
+		float Radius;
+		int64_t Total;
+	};
+
+	// One bit per voxel (cell number order): |octree distance at the centre| < Diagonal.
+	cudaError_t LaunchCloudFlags(const DeviceProgram& prog, const CloudSpec& s, uint32_t* words, cudaStream_t stream);
+	// Refined point of each listed cell (*count of them, at most `capacity`).
+	cudaError_t LaunchCloudRefine(const DeviceProgram& prog, const CloudSpec& s, const uint32_t* cells, const uint32_t* count,
+		uint32_t capacity, int iterations, float* points, cudaStream_t stream);
+	// One bit per voxel: |full-tree distance at the centre| <= Radius.
+	cudaError_t LaunchVoxFlags(const DeviceProgram& prog, const VoxSpec& s, uint32_t* words, cudaStream_t stream);
+}
+
+namespace tg
+{
 	// ---- learned distance bound (tg_field.cu) ----------------------------------------
 	// A multiresolution hash grid (16 levels x 2 features) feeds a 32 -> 64 -> 64 -> 64 -> 1
 	// ReLU network whose three hidden layers run as BF16 x BF16 -> FP32 tcgen05 matrix

@@ -292,6 +292,45 @@ class Program:
               "tg_export_mesh_device")
         return dm
 
+    def export_point_cloud(self, lo, hi, step, refine=5, attributes=True, stream=None) -> Mesh:
+        """PointCloudExportThread on the GPU: points in voxel order (cubes = voxel numbers)."""
+        v3 = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float32), (3,)))
+        lo, hi, step = v3(lo), v3(hi), v3(step)
+        hm = _lib.HostMesh()
+        check(load().tg_export_point_cloud(self.ptr, _lib.as_ptr(lo), _lib.as_ptr(hi), _lib.as_ptr(step), int(refine),
+                                           _flags(attributes, False, 0, 0), C.byref(hm), stream), "tg_export_point_cloud")
+        return _take_mesh(hm)
+
+    def export_voxels(self, grid_size, color_index=0, stream=None):
+        """VoxExport's voxels on the GPU: ((n, 4) int32 x y z colour, size, radius)."""
+        lib = load()
+        v = _lib.Voxels()
+        check(lib.tg_export_voxels(self.ptr, float(grid_size), int(color_index), C.byref(v), stream), "tg_export_voxels")
+        try:
+            n = int(v.count)
+            vox = (np.ctypeslib.as_array(v.voxels, shape=(n * 4,)).reshape(n, 4).copy() if n else np.zeros((0, 4), np.int32))
+            return vox, tuple(v.size), float(v.radius)
+        finally:
+            lib.tg_voxels_free(C.byref(v))
+
+
+def write_vox(voxels, size, path):
+    """The MagicaVoxel file VoxWriter writes for these voxels (x, y, z, colour) in order."""
+    vox = np.ascontiguousarray(np.asarray(voxels, np.int32).reshape(-1, 4))
+    v = _lib.Voxels()
+    v.count = vox.shape[0]
+    v.voxels = vox.ctypes.data_as(C.POINTER(C.c_int32))
+    v.size[:] = [int(s) for s in size]
+    check(load().tg_write_vox(C.byref(v), str(path).encode()), "tg_write_vox")
+
+
+def mesh_export(tree: "Tree", path, lo, hi, step, refine=5, fmt="ply", point_cloud=False, scale=1.0):
+    """MeshExport (export.h:37), synchronously."""
+    v3 = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float32), (3,)))
+    lo, hi, step = v3(lo), v3(hi), v3(step)
+    check(load().MeshExport(tree.handle, str(path).encode(), _lib.as_ptr(lo), _lib.as_ptr(hi), _lib.as_ptr(step), int(refine),
+                            {"stl": 0, "ply": 1, "vox": 2}[fmt], bool(point_cloud), float(scale)), "MeshExport")
+
 
 def _program_ray_march(self, origins, dirs, iterations=100, epsilon=1e-3, stream=None):
     """SDFNode::RayMarch on the GPU: (hit, travel, position) per ray."""

@@ -41,3 +41,13 @@ def golden():
 def sorted_faces(faces):
     f = np.ascontiguousarray(np.asarray(faces, dtype=np.uint64).reshape(-1, 3))
     return np.sort(f.view([("a", "<u8"), ("b", "<u8"), ("c", "<u8")]).ravel())
+
+
+def canonical_rows(points, normals, colors):
+    """Point-cloud rows (position, normal, colour bits) sorted: the reference's threads write
+    them in a run-dependent order, every row a function of its voxel alone."""
+    cols = [np.ascontiguousarray(points, np.float32).view(np.uint32), np.ascontiguousarray(normals, np.float32).view(np.uint32)]
+    if colors is not None:
+        cols.append(np.asarray(colors).astype(np.uint32))
+    a = np.concatenate(cols, 1)
+    return a[np.lexsort(a.T[::-1])]

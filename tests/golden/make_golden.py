@@ -27,6 +27,10 @@ from tangerine_gb300 import workloads as W  # noqa: E402
 OUT = Path(__file__).resolve().parent
 # Sodapop::Populate meshes at 20 samples per unit; 6 keeps the fixtures small.
 SODAPOP_DENSITY = 6.0
+# PointCloudExportThread at 0.1-unit voxels with the app's 5 refinement steps; VoxExport at
+# 8 voxels per unit with colour index 3.
+CLOUD_STEP, CLOUD_REFINE = 0.1, 5
+VOX_GRID, VOX_COLOR = 8.0, 3
 
 
 def exotic_specs():
@@ -55,6 +59,45 @@ def cases():
     for name, spec in exotic_specs().items():
         out[name] = (np.asarray(spec, np.float32), 40)
     return out
+
+
+def canonical_rows(points, normals, colors):
+    """Point-cloud rows sorted by their bits: the reference's threads write them in a
+    run-dependent order."""
+    cols = [points.view(np.uint32), normals.view(np.uint32)]
+    if colors is not None:
+        cols.append(colors.astype(np.uint32))
+    a = np.concatenate(cols, 1)
+    return a[np.lexsort(a.T[::-1])]
+
+
+def voxel_cubes(path):
+    """The multiset of (model size, sorted voxel records) of a .vox file: independent of
+    the order in which a writer was given the voxels."""
+    _, models, _ = O.read_vox(path)
+    keys = []
+    for size, vox in models:
+        v = vox[np.lexsort(vox.T[::-1])]
+        keys.append((size, v.tobytes()))
+    return sorted(keys)
+
+
+def add_point_cloud_and_voxels(R, h, b, rec):
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        R.point_cloud_file(h, b[:3], b[3:], CLOUD_STEP, CLOUD_REFINE, f"{d}/cloud.ply")
+        _, p, n, c, _ = O.read_ply(f"{d}/cloud.ply")
+        rec["cloud_rows"] = canonical_rows(p, n, c)
+        rec["cloud_has_color"] = np.int32(c is not None)
+        vox, size, radius = R.vox_serial(h, VOX_GRID, VOX_COLOR, f"{d}/serial.vox")
+        R.vox_file(h, VOX_GRID, VOX_COLOR, f"{d}/threaded.vox")
+        # The shipped, threaded VoxExport must hold the same cubes of voxels as the serial
+        # replay (its cube order and one translation follow the threads' timing).
+        assert voxel_cubes(f"{d}/serial.vox") == voxel_cubes(f"{d}/threaded.vox")
+        rec["vox_voxels"] = vox
+        rec["vox_size"] = np.array(size, np.int32)
+        rec["vox_radius"] = np.float32(radius)
+        rec["vox_file"] = np.frombuffer(Path(f"{d}/serial.vox").read_bytes(), np.uint8)
 
 
 def main():
@@ -92,6 +135,8 @@ def main():
             rec["mesh_normals"] = R.octree_gradient(o, m.vertices)
             rec["mesh_colors"] = R.octree_color(o, m.vertices)
             R.octree_free(o)
+        if R.has_finite_bounds(h):
+            add_point_cloud_and_voxels(R, h, R.bounds(h), rec)
         mo = R.meshing_octree(h)
         if mo is not None:
             nodes, children, words = R.octree_dump(mo)

@@ -1,0 +1,118 @@
+"""The point-cloud export (PointCloudExportThread) and the MagicaVoxel export (VoxExport) on
+the GPU, through the C ABI, against the reference fixtures and the CPU oracle.
+
+Everything is bit-exact: kept voxels, refined points, normals, colour bytes, voxel lists and
+the .vox file bytes."""
+
+import numpy as np
+import pytest
+
+from conftest import canonical_rows, golden_names
+from oracle import oracle as O
+from tangerine_gb300 import _lib, sdf
+from tangerine_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+CLOUD_STEP, CLOUD_REFINE, VOX_GRID, VOX_COLOR = 0.1, 5, 8.0, 3
+
+
+def bounds_of(prog):
+    """The tree's bounds (SDFNode::Bounds) as the program holds them."""
+    i = prog.info()
+    return np.array(i.bounds_min[:], np.float32), np.array(i.bounds_max[:], np.float32)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_point_cloud_matches_reference(lib, golden, name):
+    g = golden[name]
+    if "cloud_rows" not in g:
+        pytest.skip("unbounded tree")
+    t = sdf.from_spec(g["spec"])
+    with sdf.compile(t) as prog:
+        lo, hi = bounds_of(prog)
+        m = prog.export_point_cloud(lo, hi, CLOUD_STEP, CLOUD_REFINE)
+    assert m.faces.shape[0] == 0
+    assert np.all(np.diff(m.cubes.astype(np.int64)) > 0)
+    assert (m.colors is not None) == bool(g["cloud_has_color"])
+    np.testing.assert_array_equal(canonical_rows(m.vertices, m.normals, m.colors), g["cloud_rows"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_voxels_match_reference(lib, golden, name, tmp_path):
+    g = golden[name]
+    if "vox_voxels" not in g:
+        pytest.skip("unbounded tree")
+    t = sdf.from_spec(g["spec"])
+    with sdf.compile(t) as prog:
+        vox, size, radius = prog.export_voxels(VOX_GRID, VOX_COLOR)
+    np.testing.assert_array_equal(vox, g["vox_voxels"])
+    assert size == tuple(g["vox_size"]) and np.float32(radius) == g["vox_radius"]
+    # ExportMagicaVoxel end to end: the file VoxWriter writes for the cell-order voxels.
+    path = tmp_path / "model.vox"
+    lib.ExportMagicaVoxel(t.handle, VOX_GRID, VOX_COLOR, str(path).encode())
+    assert path.read_bytes() == g["vox_file"].tobytes()
+
+
+@pytest.mark.parametrize("seed,prims,step,refine", [(2, 64, 0.03, 3), (8, 256, 0.05, 5), (5, 16, (0.04, 0.07, 0.05), 0)])
+def test_point_cloud_matches_oracle(lib, port, seed, prims, step, refine):
+    """Finer voxels, a per-axis step, and no refinement, in voxel order against the oracle."""
+    spec = W.random_tree(seed, prims)
+    h = port.build(spec)
+    try:
+        b = port.bounds(h)
+        o = port.octree(h)
+        try:
+            pts, cells = port.point_cloud(o, b[:3], b[3:], step, refine)
+            normals, colors = port.vertex_attributes(o, pts)
+        finally:
+            port.octree_free(o)
+    finally:
+        port.free(h)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        m = prog.export_point_cloud(b[:3], b[3:], step, refine)
+    assert pts.shape[0] > 500
+    np.testing.assert_array_equal(m.cubes, cells.astype(np.uint32))
+    np.testing.assert_array_equal(m.vertices, pts)
+    np.testing.assert_array_equal(m.normals, normals)
+    np.testing.assert_array_equal(m.colors, colors)
+
+
+@pytest.mark.parametrize("seed,prims,grid,color", [(6, 256, 12.0, -300), (1, 16, 30.0, 254)])
+def test_voxels_match_oracle(lib, port, seed, prims, grid, color):
+    spec = W.random_tree(seed, prims)
+    h = port.build(spec)
+    try:
+        want, size, radius = port.vox(h, grid, color)
+    finally:
+        port.free(h)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        vox, gsize, gradius = prog.export_voxels(grid, color)
+    assert want.shape[0] > 100
+    np.testing.assert_array_equal(vox, want)
+    assert gsize == size and np.float32(gradius) == np.float32(radius)
+
+
+def test_mesh_export_entry(lib, golden, tmp_path):
+    """MeshExport: the point cloud written as PLY (scaled), the mesh as PLY and STL, and the
+    formats the reference writes nothing for."""
+    g = golden["cfg1_seed1"]
+    t = sdf.from_spec(g["spec"])
+    with sdf.compile(t) as prog:
+        lo, hi = bounds_of(prog)
+    sdf.mesh_export(t, tmp_path / "cloud.ply", lo, hi, CLOUD_STEP, CLOUD_REFINE, "ply", point_cloud=True, scale=2.0)
+    _, p, n, c, f = O.read_ply(tmp_path / "cloud.ply")
+    assert f.shape[0] == 0
+    rows = canonical_rows(p, n, c)
+    want = g["cloud_rows"].copy()
+    want[:, :3] = (want[:, :3].view(np.float32) * np.float32(2.0)).view(np.uint32)
+    np.testing.assert_array_equal(rows, canonical_rows(want[:, :3].view(np.float32), want[:, 3:6].view(np.float32),
+                                                       want[:, 6:9] if want.shape[1] > 6 else None))
+    sdf.mesh_export(t, tmp_path / "mesh.ply", lo, hi, 0.05, 0, "ply")
+    _, mp, mn, mc, mf = O.read_ply(tmp_path / "mesh.ply")
+    assert mp.shape[0] > 100 and mf.shape[0] > 100
+    sdf.mesh_export(t, tmp_path / "mesh.stl", lo, hi, 0.05, 0, "stl")
+    assert (tmp_path / "mesh.stl").stat().st_size == 84 + 50 * mf.shape[0]
+    for fmt, cloud, step in (("vox", False, 0.05), ("stl", True, 0.05), ("ply", False, (0.05, 0.06, 0.05))):
+        with pytest.raises(_lib.TangerineError):
+            sdf.mesh_export(t, tmp_path / "x", lo, hi, step, 0, fmt, point_cloud=cloud)

@@ -5,7 +5,7 @@ Everything here is bit-exact: the oracle keeps the reference's float operation o
 import numpy as np
 import pytest
 
-from conftest import golden_names, sorted_faces
+from conftest import canonical_rows, golden_names, sorted_faces
 from tangerine_gb300 import workloads as W
 
 
@@ -101,5 +101,34 @@ def test_sodapop_meshing_job(port, golden, name):
         np.testing.assert_array_equal(d.normals, g["soda_normals"])
         np.testing.assert_array_equal(d.colors, g["soda_colors"])
         np.testing.assert_array_equal(sorted_faces(d.faces), sorted_faces(g["soda_faces"]))
+    finally:
+        port.free(h)
+
+
+CLOUD_STEP, CLOUD_REFINE, VOX_GRID, VOX_COLOR = 0.1, 5, 8.0, 3
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_point_cloud_and_voxels(port, golden, name):
+    """PointCloudExportThread (with the refinement and WritePLY's attributes) and VoxExport's
+    voxel test against the reference."""
+    g = golden[name]
+    if "cloud_rows" not in g:
+        pytest.skip("unbounded tree")
+    h = port.build(g["spec"])
+    try:
+        b = port.bounds(h)
+        o = port.octree(h)
+        try:
+            pts, cells = port.point_cloud(o, b[:3], b[3:], CLOUD_STEP, CLOUD_REFINE)
+            normals, colors = port.vertex_attributes(o, pts)
+        finally:
+            port.octree_free(o)
+        assert np.all(np.diff(cells) > 0)
+        assert (colors is not None) == bool(g["cloud_has_color"])
+        np.testing.assert_array_equal(canonical_rows(pts, normals, colors), g["cloud_rows"])
+        vox, size, radius = port.vox(h, VOX_GRID, VOX_COLOR)
+        np.testing.assert_array_equal(vox, g["vox_voxels"])
+        assert size == tuple(g["vox_size"]) and np.float32(radius) == g["vox_radius"]
     finally:
         port.free(h)
