@@ -323,6 +323,21 @@ TANGERINE_API tg_status tg_ray_march(tg_program* program, const float* origins, 
                                      int max_iterations, float epsilon, uint8_t* hit, float* travel, float* position,
                                      void* stream);
 
+/* The app's other ray casts, batched: mode 0 is tg_ray_march; mode 1 is Lua's magnet cast
+ * (lua_sdf.cpp:410-437), whose `dirs` are target points: the direction is
+ * normalize(target - origin); mode 2 is SDFModel::RayMarch (sdf_model.cpp:261-266), mouse
+ * picking on a placed model: frame = the model's rotation quaternion (w, x, y, z),
+ * translation (x, y, z) and scale; the ray goes into the model's frame and marches 1000
+ * iterations at epsilon 0.001, whatever `iterations` and `epsilon` say, as the reference
+ * ignores its own arguments there.  Positions are in the frame the march ran in. */
+TANGERINE_API tg_status tg_ray_query(tg_program* program, int mode, const float frame[8], const float* origins, const float* dirs,
+                                     int64_t n, int iterations, float epsilon, uint8_t* hit, float* travel, float* position,
+                                     void* stream);
+/* SDFNode::Eval / SDFNode::Gradient on the whole tree at n points, on the GPU: Lua's eval
+ * and gradient (lua_sdf.cpp:386-405) and EvalTree, batched.  out: 1 / 3 floats per point. */
+TANGERINE_API tg_status tg_eval_tree_points(tg_program* program, const float* points, int64_t n, float* out, void* stream);
+TANGERINE_API tg_status tg_gradient_tree_points(tg_program* program, const float* points, int64_t n, float* out, void* stream);
+
 /* Pinhole camera looking from `position` at `target`; `up` fixes the roll; tan_half_fov is
  * tan(vertical field of view / 2).  Pixel (x, y) of a W x H image looks along
  * forward + right*u + up'*v, u = (2(x+0.5)/W - 1) * tan_half_fov * W/H,

@@ -113,6 +113,7 @@ class CpuOracle:
         self._oct_grid = None
         self._raymarch = None
         self._i32pp = C.POINTER(C.POINTER(C.c_int32))
+        self._ray_query = self._fn("ray_query", None, [vp, i, _f32p, i64, _f32p, _f32p, i, f, _u8p, _f32p, _f32p])
 
     # -- trees ----------------------------------------------------------------------
     def build(self, spec) -> int:
@@ -181,6 +182,19 @@ class CpuOracle:
 
     def equal(self, a, b):
         return bool(self._equal(a, b))
+
+    def ray_query(self, h, mode, origins, dirs, frame=None, iterations=100, epsilon=1e-3):
+        """mode 1: Lua's magnet cast (dirs are targets); mode 2: SDFModel::RayMarch in the
+        model frame (quat w x y z, translation xyz, scale)."""
+        o = self._pts(origins)
+        d = self._pts(dirs)
+        n = o.shape[0]
+        fr = np.ascontiguousarray(np.zeros(8, np.float32) if frame is None else np.asarray(frame, np.float32))
+        hit = np.empty(n, np.uint8)
+        travel = np.empty(n, np.float32)
+        pos = np.empty((n, 3), np.float32)
+        self._ray_query(h, int(mode), fr, n, o, d, int(iterations), float(epsilon), hit, travel, pos)
+        return hit, travel, pos
 
     # -- octree ---------------------------------------------------------------------
     def octree(self, h, target=0.25, coalesce=True, max_depth=-1):

@@ -1669,6 +1669,39 @@ static void ray_one(void* cv, int64_t r)
 	c->pos[r * 3] = pos.x; c->pos[r * 3 + 1] = pos.y; c->pos[r * 3 + 2] = pos.z;
 }
 
+/* Lua's magnet cast (mode 1: dir = normalize(target - origin)) and SDFModel::RayMarch (mode
+ * 2: the ray taken into the model frame {quat w x y z, translation, scale}, 1000 iterations,
+ * epsilon 0.001), serially (lua_sdf.cpp:410-437, sdf_model.cpp:261-266). */
+void tgo_ray_query(tgo_tree* t, int mode, const float* frame, int64_t n, const float* o, const float* d, int iters, float eps,
+                   uint8_t* hit, float* travel, float* pos)
+{
+	xform X = xf_identity();
+	if (mode == 2)
+	{
+		X.rot.w = frame[0]; X.rot.x = frame[1]; X.rot.y = frame[2]; X.rot.z = frame[3];
+		X.trans = V3(frame[4], frame[5], frame[6]);
+		X.scale = frame[7];
+	}
+	for (int64_t r = 0; r < n; ++r)
+	{
+		v3 origin = V3(o[r * 3], o[r * 3 + 1], o[r * 3 + 2]);
+		v3 dir = V3(d[r * 3], d[r * 3 + 1], d[r * 3 + 2]);
+		int it = iters;
+		float e = eps;
+		if (mode == 1) dir = normalize3(sub3(dir, origin));
+		else
+		{
+			origin = xf_apply_inv(&X, origin);
+			dir = qrot(qinv(X.rot), dir);
+			it = 1000;
+			e = 0.001f;
+		}
+		float rd[3] = { dir.x, dir.y, dir.z }, ro[3] = { origin.x, origin.y, origin.z };
+		ray_ctx c = { t, ro, rd, it, e, hit + r, travel + r, pos + r * 3 };
+		ray_one(&c, 0);
+	}
+}
+
 void tgo_raymarch(tgo_tree* t, int64_t n, const float* o, const float* d, int iters, float eps, int threads,
                   uint8_t* hit, float* travel, float* pos)
 {

@@ -77,6 +77,10 @@ void tgo_raymarch(tgo_tree* tree, int64_t n, const float* origins, const float* 
                   int max_iterations, float epsilon, int threads,
                   uint8_t* hit, float* travel, float* position);
 
+/* Lua's magnet cast (mode 1) and SDFModel::RayMarch in a model frame (mode 2: frame = quat
+ * w x y z, translation xyz, scale), serially. */
+void tgo_ray_query(tgo_tree* tree, int mode, const float* frame, int64_t n, const float* origins, const float* dirs,
+                   int iterations, float epsilon, uint8_t* hit, float* travel, float* position);
 int tgo_hardware_threads(void);
 /* Sodapop's meshing chain (sodapop.cpp:562-897) over the tree, serially: returns the vertex
  * count (-1 without an octree); positions/normals (3 floats), colours (4 floats), faces (3

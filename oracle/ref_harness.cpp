@@ -24,6 +24,7 @@
 #include "sdf_evaluator.h"
 #include "material.h"
 #include "export.h"
+#include "transform.h"
 #include "magica.h"
 #include <VoxWriter.h>
 #include "painting_set.h"
@@ -751,6 +752,46 @@ extern "C"
 			Writer.AddVoxel(Voxels[v * 4], Voxels[v * 4 + 1], Voxels[v * 4 + 2], (uint8_t)Voxels[v * 4 + 3]);
 		}
 		Writer.SaveToFile(std::string(Path));
+	}
+
+	// The two framed ray casts of the app, serially: Mode 1 is Lua's magnet cast
+	// (lua_sdf.cpp:410-417: Direction = normalize(Target - Origin), 100 iterations, 0.001 by
+	// default); Mode 2 is SDFModel::RayMarch (sdf_model.cpp:261-266: the ray taken into the
+	// model's frame, Transform{Rotation = quat(Q[0..3] as w x y z), Translation = T,
+	// Scalation = S}, then 1000 iterations at the default epsilon).
+	void ref_ray_query(void* Handle, int Mode, const float* Frame, int64_t Count, const float* Origins, const float* Dirs,
+		int MaxIterations, float Epsilon, uint8_t* Hit, float* Travel, float* Position)
+	{
+		SDFNodeShared Root = ((RefTree*)Handle)->Root;
+		Transform LocalToWorld;
+		if (Mode == 2)
+		{
+			LocalToWorld.Rotation = glm::quat(Frame[0], Frame[1], Frame[2], Frame[3]);
+			LocalToWorld.Translation = vec3(Frame[4], Frame[5], Frame[6]);
+			LocalToWorld.Scalation = Frame[7];
+		}
+		for (int64_t r = 0; r < Count; ++r)
+		{
+			vec3 Origin(Origins[r * 3], Origins[r * 3 + 1], Origins[r * 3 + 2]);
+			vec3 Direction(Dirs[r * 3], Dirs[r * 3 + 1], Dirs[r * 3 + 2]);
+			RayHit H;
+			if (Mode == 1)
+			{
+				Direction = glm::normalize(Direction - Origin);
+				H = Root->RayMarch(Origin, Direction, MaxIterations, Epsilon);
+			}
+			else
+			{
+				vec3 RelativeOrigin = LocalToWorld.ApplyInv(Origin);
+				vec3 RelativeRayDir = glm::rotate(glm::inverse(LocalToWorld.Rotation), Direction);
+				H = Root->RayMarch(RelativeOrigin, RelativeRayDir, 1000);
+			}
+			Hit[r] = H.Hit ? 1 : 0;
+			Travel[r] = H.Travel;
+			Position[r * 3 + 0] = H.Position.x;
+			Position[r * 3 + 1] = H.Position.y;
+			Position[r * 3 + 2] = H.Position.z;
+		}
 	}
 
 	// SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the full tree.

@@ -125,6 +125,9 @@ SIGNATURES = {
     "tg_write_vox": (_i, [C.POINTER(Voxels), C.c_char_p]),
     "ExportMagicaVoxel": (None, [_vp, _f, _i, C.c_char_p]),
     "MeshExport": (_i, [_vp, C.c_char_p, _vp, _vp, _vp, _i, _i, C.c_bool, _f]),
+    "tg_ray_query": (_i, [_vp, _i, _vp, _vp, _vp, _i64, _i, _f, _vp, _vp, _vp, _vp]),
+    "tg_eval_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
+    "tg_gradient_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "tg_drawable_free": (None, [C.POINTER(Drawable)]),
     "tg_export_grid": (_i, [_vp, _vp, _f, C.POINTER(Grid)]),
     "tg_eval_grid": (_i, [_vp, C.POINTER(Grid), _vp, _i, _vp]),

@@ -667,6 +667,52 @@ extern "C"
 		std::memset(d, 0, sizeof *d);
 	}
 
+	TANGERINE_API tg_status tg_ray_query(tg_program* p, int mode, const float frame[8], const float* origins, const float* dirs, int64_t n,
+		int iterations, float epsilon, uint8_t* hit, float* travel, float* position, void* stream)
+	{
+		if (!p || (n > 0 && (!origins || !dirs || !hit || !travel || !position))) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (mode < 0 || mode > 2 || (mode == 2 && !frame)) { SetError("ray mode is 0, 1 or 2 (2 needs a frame)"); return TG_ERR_INVALID; }
+		if (iterations < 0) { SetError("negative iteration count"); return TG_ERR_INVALID; }
+		RayFrame f{};
+		f.Mode = mode;
+		f.Rotation[0] = 1.0f;
+		f.Scale = 1.0f;
+		if (mode == 2)
+		{
+			for (int k = 0; k < 4; ++k) f.Rotation[k] = frame[k];
+			for (int k = 0; k < 3; ++k) f.Translation[k] = frame[4 + k];
+			f.Scale = frame[7];
+			// SDFModel::RayMarch passes 1000 iterations and RayMarch's default epsilon.
+			iterations = 1000;
+			epsilon = 0.001f;
+		}
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.RayMarch(*p, origins, dirs, n, iterations, epsilon, hit, travel, position, StreamOf(stream), &f);
+		if (e != cudaSuccess) return CudaFail(e, "casting rays");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_eval_tree_points(tg_program* p, const float* points, int64_t n, float* out, void* stream)
+	{
+		if (!p || (n > 0 && (!points || !out))) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.PointQuery(*p, points, n, false, out, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "evaluating the tree");
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_gradient_tree_points(tg_program* p, const float* points, int64_t n, float* out, void* stream)
+	{
+		if (!p || (n > 0 && (!points || !out))) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		cudaError_t e = eng.PointQuery(*p, points, n, true, out, StreamOf(stream));
+		if (e != cudaSuccess) return CudaFail(e, "taking gradients");
+		return TG_OK;
+	}
+
 	TANGERINE_API tg_status tg_ray_march(tg_program* p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
 		uint8_t* hit, float* travel, float* position, void* stream)
 	{

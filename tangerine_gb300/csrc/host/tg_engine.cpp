@@ -443,7 +443,7 @@ namespace tg
 	}
 
 	cudaError_t Engine::RayMarch(const Program& p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
-		uint8_t* hit, float* travel, float* position, cudaStream_t s)
+		uint8_t* hit, float* travel, float* position, cudaStream_t s, const RayFrame* frame)
 	{
 		if (n <= 0) return cudaSuccess;
 		const size_t in = (size_t)n * 12;
@@ -457,11 +457,28 @@ namespace tg
 		TG_TRY(cudaMemcpyAsync(dOrig, origins, in, cudaMemcpyHostToDevice, s));
 		TG_TRY(cudaMemcpyAsync(dDir, dirs, in, cudaMemcpyHostToDevice, s));
 		Begin("ray_march", s);
-		TG_TRY(LaunchRayMarch(p.View, dOrig, dDir, n, iterations, epsilon, dHit, dTravel, dPos, s));
+		if (frame && frame->Mode != 0) TG_TRY(LaunchRayQuery(p.View, *frame, dOrig, dDir, n, iterations, epsilon, dHit, dTravel, dPos, s));
+		else TG_TRY(LaunchRayMarch(p.View, dOrig, dDir, n, iterations, epsilon, dHit, dTravel, dPos, s));
 		End(s);
 		TG_TRY(cudaMemcpyAsync(hit, dHit, (size_t)n, cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaMemcpyAsync(travel, dTravel, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaMemcpyAsync(position, dPos, in, cudaMemcpyDeviceToHost, s));
+		TG_TRY(cudaStreamSynchronize(s));
+		Collect();
+		return cudaSuccess;
+	}
+
+	cudaError_t Engine::PointQuery(const Program& p, const float* points, int64_t n, bool gradient, float* out, cudaStream_t s)
+	{
+		if (n <= 0) return cudaSuccess;
+		const size_t in = (size_t)n * 12, outBytes = (size_t)n * (gradient ? 12 : 4);
+		TG_TRY(RayIn.Reserve(in));
+		TG_TRY(RayOut.Reserve(outBytes));
+		TG_TRY(cudaMemcpyAsync(RayIn.Ptr, points, in, cudaMemcpyHostToDevice, s));
+		Begin(gradient ? "tree_gradient" : "tree_eval", s);
+		TG_TRY(LaunchPointQuery(p.View, RayIn.As<float>(), n, gradient, RayOut.As<float>(), s));
+		End(s);
+		TG_TRY(cudaMemcpyAsync(out, RayOut.Ptr, outBytes, cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaStreamSynchronize(s));
 		Collect();
 		return cudaSuccess;

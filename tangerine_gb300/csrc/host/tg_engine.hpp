@@ -107,7 +107,10 @@ namespace tg
 		cudaError_t FaceNormals(const Program& p, const float* host_vertices, uint64_t vertex_count, const uint32_t* host_faces,
 			uint64_t face_count, float* host_normals, cudaStream_t s);
 		cudaError_t RayMarch(const Program& p, const float* origins, const float* dirs, int64_t n, int iterations, float epsilon,
-			uint8_t* hit, float* travel, float* position, cudaStream_t s);
+			uint8_t* hit, float* travel, float* position, cudaStream_t s, const RayFrame* frame = nullptr);
+		// SDFNode::Eval (gradient = false, 1 float per point) or SDFNode::Gradient (3) on the
+		// whole tree at host points.
+		cudaError_t PointQuery(const Program& p, const float* points, int64_t n, bool gradient, float* out, cudaStream_t s);
 		cudaError_t Render(const Program& p, const CameraBasis* cams, int count, int width, int height, int steps, float epsilon,
 			bool exact, float* depth, float* normals, uint8_t* colors, bool out_is_device, cudaStream_t s, const FieldNet* field = nullptr);
 		// Sodapop's meshing job (MeshingJob::NaiveSurfaceNets) for a program compiled with

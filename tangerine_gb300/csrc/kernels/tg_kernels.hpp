@@ -38,6 +38,21 @@ namespace tg
 
 	// Depth (travel, +inf on a miss), gradient normal and colour per pixel for `count`
 	// cameras.  exact: the reference's full-tree steps; otherwise octree-bounded steps.
+	// Ray frames of the app's casts: 0 plain SDFNode::RayMarch, 1 Lua's magnet cast (the
+	// direction operand is a target), 2 SDFModel::RayMarch in a model frame.
+	struct RayFrame
+	{
+		int Mode;
+		float Rotation[4];      // w x y z
+		float Translation[3];
+		float Scale;
+	};
+	cudaError_t LaunchRayQuery(const DeviceProgram& prog, const RayFrame& frame, const float* origins, const float* dirs, int64_t n,
+		int max_iterations, float epsilon, uint8_t* hit, float* travel, float* position, cudaStream_t stream);
+	// SDFNode::Eval (1 float per point) or SDFNode::Gradient (3) on the whole tree.
+	cudaError_t LaunchPointQuery(const DeviceProgram& prog, const float* points, int64_t n, bool gradient, float* out,
+		cudaStream_t stream);
+
 	cudaError_t LaunchRender(const DeviceProgram& prog, const CameraBasis* cameras, int count, int width, int height,
 		int max_steps, float epsilon, bool exact, float* depth, float* normals, uint8_t* colors, cudaStream_t stream);
 

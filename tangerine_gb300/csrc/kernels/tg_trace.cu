@@ -88,6 +88,60 @@ namespace tg
 			position[r * 3 + 2] = m.Position.z;
 		}
 
+		// The app's framed casts: mode 1 is Lua's magnet cast (lua_sdf.cpp:410-417, the
+		// direction is normalize(target - origin)); mode 2 is SDFModel::RayMarch
+		// (sdf_model.cpp:261-266): origin = Transform::ApplyInv (rotate by the inverse
+		// rotation after removing the translation, then divide by the scale), direction
+		// rotated by the inverse rotation.
+		__global__ void __launch_bounds__(kTraceThreads) RayQueryKernel(DeviceProgram prog, RayFrame f, const float* __restrict__ origins,
+			const float* __restrict__ dirs, int64_t n, int iterations, float epsilon, uint8_t* __restrict__ hit,
+			float* __restrict__ travel, float* __restrict__ position)
+		{
+			extern __shared__ float spill[];
+			const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+			if (r >= n) return;
+			Vec3 o(origins[r * 3], origins[r * 3 + 1], origins[r * 3 + 2]);
+			Vec3 d(dirs[r * 3], dirs[r * 3 + 1], dirs[r * 3 + 2]);
+			if (f.Mode == 1)
+			{
+				d = Normalize(d - o);
+			}
+			else if (f.Mode == 2)
+			{
+				const Quat qi = Inverse(Quat{ f.Rotation[0], f.Rotation[1], f.Rotation[2], f.Rotation[3] });
+				o = Rotate(qi, o - Vec3(f.Translation[0], f.Translation[1], f.Translation[2])) / f.Scale;
+				d = Rotate(qi, d);
+			}
+			const March m = MarchExact(prog, o, d, iterations, epsilon, spill + threadIdx.x);
+			hit[r] = m.Hit ? 1 : 0;
+			travel[r] = m.Travel;
+			position[r * 3] = m.Position.x;
+			position[r * 3 + 1] = m.Position.y;
+			position[r * 3 + 2] = m.Position.z;
+		}
+
+		// SDFNode::Eval (gradient = false) or SDFNode::Gradient on the whole tree per point,
+		// as Lua's eval / gradient and EvalTree compute them (lua_sdf.cpp:386-405).
+		__global__ void __launch_bounds__(kTraceThreads) PointQueryKernel(DeviceProgram prog, const float* __restrict__ points, int64_t n,
+			bool gradient, float* __restrict__ out)
+		{
+			extern __shared__ float spill[];
+			const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+			if (t >= n) return;
+			const Vec3 p(points[t * 3], points[t * 3 + 1], points[t * 3 + 2]);
+			if (gradient)
+			{
+				const Vec3 g = TraceShade(prog, prog.FullSurfaceCode, p, false, nullptr, spill + threadIdx.x, kTraceThreads);
+				out[t * 3] = g.x;
+				out[t * 3 + 1] = g.y;
+				out[t * 3 + 2] = g.z;
+			}
+			else
+			{
+				out[t] = TraceSurfaceAt(prog, prog.FullSurfaceCode, p, false, nullptr, spill + threadIdx.x, kTraceThreads);
+			}
+		}
+
 		__global__ void __launch_bounds__(kTraceThreads) RenderKernel(DeviceProgram prog, const CameraBasis* __restrict__ cams,
 			int count, int width, int height, int steps, float epsilon, bool exact, float* __restrict__ depth,
 			float* __restrict__ normals, uint8_t* __restrict__ colors)
@@ -146,6 +200,36 @@ namespace tg
 		if (smem > 48 * 1024) cudaFuncSetAttribute(RayMarchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		RayMarchKernel<<<(unsigned)((n + kTraceThreads - 1) / kTraceThreads), kTraceThreads, smem, stream>>>(
 			prog, origins, dirs, n, max_iterations, epsilon, hit, travel, position);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchRayQuery(const DeviceProgram& prog, const RayFrame& frame, const float* origins, const float* dirs, int64_t n,
+		int max_iterations, float epsilon, uint8_t* hit, float* travel, float* position, cudaStream_t stream)
+	{
+		if (n <= 0) return cudaSuccess;
+		const size_t smem = TraceSpillBytes(prog);
+		if (smem > 48 * 1024)
+		{
+			cudaError_t e = cudaFuncSetAttribute(RayQueryKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		RayQueryKernel<<<(unsigned)((n + kTraceThreads - 1) / kTraceThreads), kTraceThreads, smem, stream>>>(
+			prog, frame, origins, dirs, n, max_iterations, epsilon, hit, travel, position);
+		return cudaGetLastError();
+	}
+
+	cudaError_t LaunchPointQuery(const DeviceProgram& prog, const float* points, int64_t n, bool gradient, float* out,
+		cudaStream_t stream)
+	{
+		if (n <= 0) return cudaSuccess;
+		const size_t smem = TraceSpillBytes(prog);
+		if (smem > 48 * 1024)
+		{
+			cudaError_t e = cudaFuncSetAttribute(PointQueryKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		PointQueryKernel<<<(unsigned)((n + kTraceThreads - 1) / kTraceThreads), kTraceThreads, smem, stream>>>(
+			prog, points, n, gradient, out);
 		return cudaGetLastError();
 	}
 

@@ -345,6 +345,37 @@ def _program_ray_march(self, origins, dirs, iterations=100, epsilon=1e-3, stream
     return hit.astype(bool), travel, pos
 
 
+def _program_ray_query(self, mode, origins, dirs, frame=None, iterations=100, epsilon=1e-3, stream=None):
+    """mode 1: Lua's magnet cast (dirs are targets); mode 2: SDFModel::RayMarch in the model
+    frame (quat w x y z, translation xyz, scale)."""
+    o = np.ascontiguousarray(np.asarray(origins, np.float32).reshape(-1, 3))
+    d = np.ascontiguousarray(np.asarray(dirs, np.float32).reshape(-1, 3))
+    fr = np.ascontiguousarray(np.zeros(8, np.float32) if frame is None else np.asarray(frame, np.float32).reshape(8))
+    n = o.shape[0]
+    hit = np.empty(n, np.uint8)
+    travel = np.empty(n, np.float32)
+    pos = np.empty((n, 3), np.float32)
+    check(load().tg_ray_query(self.ptr, int(mode), _lib.as_ptr(fr), _lib.as_ptr(o), _lib.as_ptr(d), n, iterations, epsilon,
+                              _lib.as_ptr(hit), _lib.as_ptr(travel), _lib.as_ptr(pos), stream), "tg_ray_query")
+    return hit.astype(bool), travel, pos
+
+
+def _program_eval_tree(self, points, stream=None):
+    """SDFNode::Eval on the whole tree per point (Lua's eval), on the GPU."""
+    p = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+    out = np.empty(p.shape[0], np.float32)
+    check(load().tg_eval_tree_points(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), stream), "tg_eval_tree_points")
+    return out
+
+
+def _program_gradient_tree(self, points, stream=None):
+    """SDFNode::Gradient on the whole tree per point (Lua's gradient), on the GPU."""
+    p = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
+    out = np.empty((p.shape[0], 3), np.float32)
+    check(load().tg_gradient_tree_points(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), stream), "tg_gradient_tree_points")
+    return out
+
+
 def cameras(positions, target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_y_degrees=60.0):
     """tg_camera array looking at `target` from each position."""
     import math
@@ -370,6 +401,9 @@ def _program_render(self, cams, width, height, steps=256, epsilon=1e-4, exact=Fa
 
 
 Program.ray_march = _program_ray_march
+Program.ray_query = _program_ray_query
+Program.eval_tree = _program_eval_tree
+Program.gradient_tree = _program_gradient_tree
 Program.render = _program_render
 
 

@@ -30,6 +30,9 @@ SODAPOP_DENSITY = 6.0
 # PointCloudExportThread at 0.1-unit voxels with the app's 5 refinement steps; VoxExport at
 # 8 voxels per unit with colour index 3.
 CLOUD_STEP, CLOUD_REFINE = 0.1, 5
+# A model placement for picking: rotation (w, x, y, z) 35 degrees about y, translation, scale.
+_q = W.axis_quaternion(1, 35)
+PICK_FRAME = np.array([_q[3], _q[0], _q[1], _q[2], 0.3, -0.2, 0.15, 1.25], np.float32)
 VOX_GRID, VOX_COLOR = 8.0, 3
 
 
@@ -108,6 +111,7 @@ def main():
     points = rng.uniform(-2.0, 2.0, (2048, 3)).astype(np.float32)
     ray_o = W.camera_poses(77, 256, radius=4.0)
     ray_d = (rng.uniform(-0.3, 0.3, (256, 3)) - ray_o / 4.0).astype(np.float32)
+    magnet_targets = rng.uniform(-0.6, 0.6, (256, 3)).astype(np.float32)
     for name, (spec, res) in cases().items():
         h = R.build(spec)
         rec = {"spec": spec, "points": points, "resolution": np.int32(res)}
@@ -121,6 +125,12 @@ def main():
         rec["color"] = R.color(h, points[:512])
         hit, travel, pos = R.raymarch(h, ray_o, ray_d, iterations=256, epsilon=1e-4, threads=1)
         rec.update(ray_origins=ray_o, ray_dirs=ray_d, ray_hit=hit, ray_travel=travel, ray_position=pos)
+        # Lua's magnet cast toward targets near the origin, and SDFModel::RayMarch on the tree
+        # placed with a rotation, translation and scale.
+        hit, travel, pos = R.ray_query(h, 1, ray_o, magnet_targets, iterations=100, epsilon=1e-3)
+        rec.update(magnet_targets=magnet_targets, magnet_hit=hit, magnet_travel=travel, magnet_position=pos)
+        hit, travel, pos = R.ray_query(h, 2, ray_o, ray_d, frame=PICK_FRAME)
+        rec.update(pick_frame=PICK_FRAME, pick_hit=hit, pick_travel=travel, pick_position=pos)
         o = R.octree(h)
         if o is not None:
             nodes, children, words = R.octree_dump(o)

@@ -132,3 +132,21 @@ def test_point_cloud_and_voxels(port, golden, name):
         assert size == tuple(g["vox_size"]) and np.float32(radius) == g["vox_radius"]
     finally:
         port.free(h)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_framed_ray_casts(port, golden, name):
+    """Lua's magnet cast and SDFModel::RayMarch (mouse picking on a placed model)."""
+    g = golden[name]
+    h = port.build(g["spec"])
+    try:
+        hit, travel, pos = port.ray_query(h, 1, g["ray_origins"], g["magnet_targets"], iterations=100, epsilon=1e-3)
+        np.testing.assert_array_equal(hit, g["magnet_hit"])
+        np.testing.assert_array_equal(travel, g["magnet_travel"])
+        np.testing.assert_array_equal(pos, g["magnet_position"])
+        hit, travel, pos = port.ray_query(h, 2, g["ray_origins"], g["ray_dirs"], frame=g["pick_frame"])
+        np.testing.assert_array_equal(hit, g["pick_hit"])
+        np.testing.assert_array_equal(travel, g["pick_travel"])
+        np.testing.assert_array_equal(pos, g["pick_position"])
+    finally:
+        port.free(h)
