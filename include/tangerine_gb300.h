@@ -275,6 +275,14 @@ typedef struct tg_drawable
 
 TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream);
 TANGERINE_API void tg_drawable_free(tg_drawable* drawable);
+/* MeshExport(Path, UseBaseColor = true, Format, Scale) (export.cpp:495-563): the drawables of
+ * placed models written as one STL (format 0) or PLY (1) file.  frames: 8 floats per
+ * drawable, the model's LocalToWorld (rotation w x y z, translation, scale), or NULL for
+ * none; positions go through its matrix and are multiplied by scale, normals are written as
+ * they are, colours as bytes 0xFF * c, faces offset by the vertices before.  The STL facet
+ * normal is the normalised sum of its corners' normals. */
+TANGERINE_API tg_status tg_write_drawables(const tg_drawable* drawables, const float* frames, int count, const char* path,
+                                           int format, float scale);
 
 /* PointCloudExportThread (export.cpp:384-480) on the GPU: the centres of the voxels of the
  * ceil((max - min) / step) lattice from model_min whose octree distance is below the

@@ -372,6 +372,8 @@ class ReferenceOracle(CpuOracle):
         self._cloud_file = self._fn("point_cloud_file", None, [vp, _f32p, _f32p, _f32p, i, f, C.c_char_p])
         self._vox_file = self._fn("vox_file", None, [vp, f, i, C.c_char_p])
         self._vox_write = self._fn("vox_write", None, [C.POINTER(C.c_int32), i64, C.POINTER(C.c_int32), C.c_char_p])
+        self._write_drawables = self._fn("write_drawables", None, [i, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                                   C.c_void_p, C.c_void_p, i, f, C.c_char_p])
         self._vox_serial = self._fn("vox_serial", i64, [vp, f, i, C.c_char_p, self._i32pp, C.POINTER(C.c_int32),
                                                         C.POINTER(C.c_float)])
         self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
@@ -408,6 +410,20 @@ class ReferenceOracle(CpuOracle):
     def vox_file(self, h, grid_size, color_index, path):
         """VoxExport as shipped (threaded)."""
         self._vox_file(h, float(grid_size), int(color_index), str(path).encode())
+
+    def write_drawables(self, drawables, frames, path, fmt="ply", scale=1.0):
+        """MeshExport(Path, UseBaseColor=True, ...) over (positions, normals, colors rgba,
+        faces) tuples placed by frames (8 floats each), through the reference's writers."""
+        vc = np.array([len(d[0]) for d in drawables], np.int64)
+        ic = np.array([d[3].size for d in drawables], np.int64)
+        P = np.ascontiguousarray(np.concatenate([d[0] for d in drawables]).astype(np.float32))
+        N = np.ascontiguousarray(np.concatenate([d[1] for d in drawables]).astype(np.float32))
+        Cl = np.ascontiguousarray(np.concatenate([d[2] for d in drawables]).astype(np.float32))
+        I = np.ascontiguousarray(np.concatenate([d[3].reshape(-1) for d in drawables]).astype(np.uint32))
+        Fr = np.ascontiguousarray(np.asarray(frames, np.float32).reshape(-1, 8))
+        ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._write_drawables(len(drawables), ptr(vc), ptr(ic), ptr(P), ptr(N), ptr(Cl), ptr(I), ptr(Fr),
+                              0 if fmt == "stl" else 1, float(scale), str(path).encode())
 
     def vox_write(self, voxels, size, path):
         """VoxWriter fed (x, y, z, colour) rows in order, saved to path."""

@@ -46,6 +46,8 @@ extern std::atomic_int GenerationProgress;
 extern std::atomic_int RefinementProgress;
 extern std::atomic_int WriteProgress;
 void MeshExportThread(SDFNodeShared Evaluator, vec3 ModelMin, vec3 ModelMax, vec3 Step, int RefineIterations, std::string Path, ExportFormat Format, float Scale);
+void WritePLY(std::string Path, std::vector<vec3>& Vertices, std::vector<uint8_t>& Colors, std::vector<glm::vec3>& Normals, std::vector<ivec3>& Triangles);
+void WriteSTL(std::string Path, std::vector<vec3>& Vertices, std::vector<glm::vec3>& Normals, std::vector<ivec3>& Triangles);
 void PointCloudExportThread(SDFNodeShared Evaluator, vec3 ModelMin, vec3 ModelMax, vec3 Step, int RefineIterations, std::string Path, ExportFormat Format, float Scale);
 
 namespace
@@ -792,6 +794,49 @@ extern "C"
 			Position[r * 3 + 1] = H.Position.y;
 			Position[r * 3 + 2] = H.Position.z;
 		}
+	}
+
+	// MeshExport(Path, UseBaseColor = true, ...)'s gather (export.cpp:495-548) over drawables
+	// given as arrays (positions xyz, normals xyz, colours rgba, indices, per drawable), with
+	// each model's LocalToWorld from a Transform {quat w x y z, translation, scale}, then the
+	// reference's own writers.
+	void ref_write_drawables(int Count, const int64_t* VertexCounts, const int64_t* IndexCounts, const float* Positions,
+		const float* Normals, const float* Colors, const uint32_t* Indices, const float* Frames, int Format, float Scale,
+		const char* Path)
+	{
+		std::vector<vec3> Vertices;
+		std::vector<vec3> OutNormals;
+		std::vector<uint8_t> OutColors;
+		std::vector<ivec3> Triangles;
+		size_t Offset = 0, IndexBase = 0;
+		for (int d = 0; d < Count; ++d)
+		{
+			Transform LocalToWorldT;
+			LocalToWorldT.Rotation = glm::quat(Frames[d * 8], Frames[d * 8 + 1], Frames[d * 8 + 2], Frames[d * 8 + 3]);
+			LocalToWorldT.Translation = vec3(Frames[d * 8 + 4], Frames[d * 8 + 5], Frames[d * 8 + 6]);
+			LocalToWorldT.Scalation = Frames[d * 8 + 7];
+			glm::mat4 LocalToWorld = LocalToWorldT.ToMatrix();
+			for (int64_t i = 0; i < VertexCounts[d]; ++i)
+			{
+				const size_t v = Offset + (size_t)i;
+				const glm::vec4 Position(Positions[v * 3], Positions[v * 3 + 1], Positions[v * 3 + 2], 1.0);
+				Vertices.push_back((LocalToWorld * Position).xyz() * glm::vec3(Scale));
+				OutNormals.push_back(vec3(Normals[v * 3], Normals[v * 3 + 1], Normals[v * 3 + 2]));
+				const glm::vec4 Color(Colors[v * 4], Colors[v * 4 + 1], Colors[v * 4 + 2], Colors[v * 4 + 3]);
+				OutColors.push_back(0xFF * Color.r);
+				OutColors.push_back(0xFF * Color.g);
+				OutColors.push_back(0xFF * Color.b);
+			}
+			for (int64_t i = 0; i < IndexCounts[d]; i += 3)
+			{
+				const uint32_t* I = Indices + IndexBase + i;
+				Triangles.emplace_back(Offset + I[0], Offset + I[1], Offset + I[2]);
+			}
+			Offset += (size_t)VertexCounts[d];
+			IndexBase += (size_t)IndexCounts[d];
+		}
+		if (Format == 0) WriteSTL(std::string(Path), Vertices, OutNormals, Triangles);
+		else WritePLY(std::string(Path), Vertices, OutColors, OutNormals, Triangles);
 	}
 
 	// SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the full tree.

@@ -129,6 +129,7 @@ SIGNATURES = {
     "tg_eval_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "tg_gradient_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "tg_drawable_free": (None, [C.POINTER(Drawable)]),
+    "tg_write_drawables": (_i, [_vp, _vp, _i, C.c_char_p, _i, _f]),
     "tg_export_grid": (_i, [_vp, _vp, _f, C.POINTER(Grid)]),
     "tg_eval_grid": (_i, [_vp, C.POINTER(Grid), _vp, _i, _vp]),
     "tg_eval_points": (_i, [_vp, _vp, _i64, _vp, _vp]),

@@ -875,6 +875,93 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API tg_status tg_write_drawables(const tg_drawable* drawables, const float* frames, int count, const char* path,
+		int format, float scale)
+	{
+		if ((count > 0 && !drawables) || !path || count < 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (format != 0 && format != 1) { SetError("format is 0 (STL) or 1 (PLY)"); return TG_ERR_INVALID; }
+		// The gather of MeshExport(Path, UseBaseColor, ...) (export.cpp:495-548): positions
+		// through the model's LocalToWorld matrix times Scale, normals as they are, colour
+		// bytes 0xFF * c, indices offset by the vertices before.
+		uint64_t nv = 0, nf = 0;
+		for (int d = 0; d < count; ++d) { nv += drawables[d].vertex_count; nf += drawables[d].face_count; }
+		std::vector<float> V((size_t)nv * 3), N((size_t)nv * 3);
+		std::vector<uint8_t> Cb((size_t)nv * 3);
+		std::vector<uint32_t> F((size_t)nf * 3);
+		uint64_t vo = 0, fo = 0;
+		for (int d = 0; d < count; ++d)
+		{
+			const tg_drawable& dr = drawables[d];
+			Transform t;
+			if (frames)
+			{
+				const float* fr = frames + (size_t)d * 8;
+				t.Rotation = Quat{ fr[0], fr[1], fr[2], fr[3] };
+				t.Translation = Vec3(fr[4], fr[5], fr[6]);
+				t.Scalation = fr[7];
+			}
+			const Mat4 M = t.ToMatrix();
+			for (uint64_t i = 0; i < dr.vertex_count; ++i)
+			{
+				const float x = dr.positions[i * 3], y = dr.positions[i * 3 + 1], z = dr.positions[i * 3 + 2];
+				// (M * vec4(p, 1)).xyz = (m0*x + m1*y) + (m2*z + m3*1), then * vec3(Scale)
+				for (int r = 0; r < 3; ++r)
+				{
+					const float w = (M.at(0, r) * x + M.at(1, r) * y) + (M.at(2, r) * z + M.at(3, r) * 1.0f);
+					V[(size_t)(vo + i) * 3 + r] = w * scale;
+					N[(size_t)(vo + i) * 3 + r] = dr.normals[i * 3 + r];
+					// float -> integer -> low byte, as the x86 conversion into a uint8_t vector does
+					Cb[(size_t)(vo + i) * 3 + r] = (uint8_t)(int32_t)(255.0f * dr.colors[i * 4 + r]);
+				}
+			}
+			for (uint64_t f = 0; f < dr.face_count * 3; ++f) F[(size_t)(fo * 3 + f)] = (uint32_t)(vo + dr.faces[f]);
+			vo += dr.vertex_count;
+			fo += dr.face_count;
+		}
+		if (format == 1)
+		{
+			tg_mesh m{};
+			m.vertex_count = nv;
+			m.face_count = nf;
+			m.vertices = V.data();
+			m.normals = N.data();
+			m.colors = Cb.data();
+			m.faces = F.data();
+			return tg_write_ply(&m, path, 1.0f);
+		}
+		// WriteSTL(Path, Vertices, Normals, Triangles) (export.cpp:60-108): each facet's normal
+		// is normalize(N[a] + N[b] + N[c]); no padding follows (84 + 50n is a multiple of 4
+		// whenever the reference's 84 + 100n is).
+		FILE* out = std::fopen(path, "wb");
+		if (!out) { WriteFileError(path); return TG_ERR_IO; }
+		char header[80];
+		std::memset(header, 0, sizeof header);
+		const char* title = "STL generated by TangerineCSG";
+		std::memcpy(header, title, std::strlen(title));
+		bool ok = std::fwrite(header, 1, 80, out) == 80;
+		const uint32_t tris = (uint32_t)nf;
+		ok = ok && std::fwrite(&tris, 4, 1, out) == 1;
+		uint8_t rec[50];
+		for (uint64_t t = 0; ok && t < nf; ++t)
+		{
+			const uint32_t a = F[t * 3], b = F[t * 3 + 1], c = F[t * 3 + 2];
+			Vec3 n(N[(size_t)a * 3], N[(size_t)a * 3 + 1], N[(size_t)a * 3 + 2]);
+			n = n + Vec3(N[(size_t)b * 3], N[(size_t)b * 3 + 1], N[(size_t)b * 3 + 2]);
+			n = n + Vec3(N[(size_t)c * 3], N[(size_t)c * 3 + 1], N[(size_t)c * 3 + 2]);
+			n = Normalize(n);
+			const float nn[3] = { n.x, n.y, n.z };
+			std::memcpy(rec, nn, 12);
+			std::memcpy(rec + 12, &V[(size_t)a * 3], 12);
+			std::memcpy(rec + 24, &V[(size_t)b * 3], 12);
+			std::memcpy(rec + 36, &V[(size_t)c * 3], 12);
+			rec[48] = 0; rec[49] = 0;
+			ok = std::fwrite(rec, 1, 50, out) == 50;
+		}
+		ok = (std::fclose(out) == 0) && ok;
+		if (!ok) { WriteFileError(path); return TG_ERR_IO; }
+		return TG_OK;
+	}
+
 	// ExportCommon (export.cpp:595-607): the tree's bounds at a 1/GridSize step.
 	static void ExportToFile(void* h, float grid_size, const char* path, bool ply)
 	{

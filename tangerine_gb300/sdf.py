@@ -314,6 +314,28 @@ class Program:
             lib.tg_voxels_free(C.byref(v))
 
 
+def write_drawables(drawables, path, frames=None, fmt="ply", scale=1.0):
+    """MeshExport(Path, UseBaseColor=True, ...) over Sodapop drawables placed by frames
+    (8 floats each: rotation w x y z, translation xyz, scale)."""
+    keep = []
+    arr = (_lib.Drawable * max(1, len(drawables)))()
+    for i, d in enumerate(drawables):
+        p = np.ascontiguousarray(d.positions, np.float32)
+        n = np.ascontiguousarray(d.normals, np.float32)
+        c = np.ascontiguousarray(d.colors, np.float32)
+        f = np.ascontiguousarray(d.faces, np.uint32)
+        keep += [p, n, c, f]
+        arr[i].vertex_count = p.shape[0]
+        arr[i].face_count = f.shape[0]
+        arr[i].positions = p.ctypes.data_as(C.POINTER(C.c_float))
+        arr[i].normals = n.ctypes.data_as(C.POINTER(C.c_float))
+        arr[i].colors = c.ctypes.data_as(C.POINTER(C.c_float))
+        arr[i].faces = f.ctypes.data_as(C.POINTER(C.c_uint32))
+    fr = None if frames is None else np.ascontiguousarray(np.asarray(frames, np.float32).reshape(-1, 8))
+    check(load().tg_write_drawables(arr, None if fr is None else _lib.as_ptr(fr), len(drawables), str(path).encode(),
+                                    0 if fmt == "stl" else 1, float(scale)), "tg_write_drawables")
+
+
 def write_vox(voxels, size, path):
     """The MagicaVoxel file VoxWriter writes for these voxels (x, y, z, colour) in order."""
     vox = np.ascontiguousarray(np.asarray(voxels, np.int32).reshape(-1, 4))

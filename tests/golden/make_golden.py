@@ -160,5 +160,21 @@ def main():
         print(name, "vertices", rec.get("mesh_vertices", np.zeros((0, 3))).shape[0])
 
 
+def drawables_fixture(R):
+    """Two Sodapop drawables from the fixtures, placed by two frames, written by the
+    reference's MeshExport(Path, UseBaseColor=True, ...) gather and writers."""
+    import tempfile
+    recs = [np.load(OUT / f"{n}.npz") for n in ("cfg1_seed1", "stencil_align")]   # tree fixtures written above
+    drawables = [(r["soda_positions"], r["soda_normals"], r["soda_colors"], r["soda_faces"]) for r in recs]
+    frames = np.stack([PICK_FRAME, np.array([1, 0, 0, 0, -1.5, 2.0, 0.25, 0.5], np.float32)])
+    out = {"frames": frames, "scale": np.float32(1.5)}
+    with tempfile.TemporaryDirectory() as d:
+        for fmt in ("ply", "stl"):
+            R.write_drawables(drawables, frames, f"{d}/out.{fmt}", fmt=fmt, scale=1.5)
+            out[f"{fmt}_bytes"] = np.frombuffer(Path(f"{d}/out.{fmt}").read_bytes(), np.uint8)
+    np.savez_compressed(OUT / "writer_drawables.npz", **out)
+
+
 if __name__ == "__main__":
     main()
+    drawables_fixture(O.reference())

@@ -165,3 +165,18 @@ def test_vox_writer_splits_large_volumes(lib, tmp_path):
         R.vox_write(v, size, tmp_path / f"ref_{name}.vox")
         sdf.write_vox(v, size, tmp_path / f"own_{name}.vox")
         assert (tmp_path / f"own_{name}.vox").read_bytes() == (tmp_path / f"ref_{name}.vox").read_bytes(), name
+
+
+def test_drawable_writer_matches_reference(lib, golden, tmp_path):
+    """MeshExport(Path, UseBaseColor, ...) over two placed Sodapop drawables: the product's
+    PLY and STL bytes against the reference's gather and writers."""
+    from conftest import GOLDEN
+    w = np.load(GOLDEN / "writer_drawables.npz")
+    drawables = []
+    for name in ("cfg1_seed1", "stencil_align"):
+        g = golden[name]
+        drawables.append(sdf.SodapopDrawable(g["soda_positions"], g["soda_normals"], g["soda_colors"],
+                                             g["soda_faces"].astype(np.uint32), np.zeros(0, np.uint32), g["soda_grid"]))
+    for fmt in ("ply", "stl"):
+        sdf.write_drawables(drawables, tmp_path / f"out.{fmt}", frames=w["frames"], fmt=fmt, scale=float(w["scale"]))
+        assert (tmp_path / f"out.{fmt}").read_bytes() == w[f"{fmt}_bytes"].tobytes(), fmt
