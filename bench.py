@@ -473,9 +473,12 @@ def our_arm(args, rank, world, local_rank):
         prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
         d2h = nv * (12 + 12 + 4 + (3 if has_colors else 0)) + nf * 12
         phases = sdf.last_export_timing()
+        oct_s, comp_s = _lib.C.c_double(), _lib.C.c_double()
+        lib.tg_debug_compile_seconds(tree.handle, 0, _lib.C.byref(oct_s), _lib.C.byref(comp_s))
         e2e = {"value": world * samples * e2e_steps / e2e_s, "unit": "samples/s",
                "last_call_phases_s": {"octree_compile": phases[0], "upload": phases[1], "gpu_export": phases[2],
                                       "copy_to_host": phases[3]},
+               "host_compile_split_s": {"octree": oct_s.value, "programs": comp_s.value - oct_s.value},
                "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
                "meshes_per_s": world * e2e_steps / e2e_s,
                "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}
@@ -854,6 +857,108 @@ def surrogate_arm(args, rank, world, local_rank):
     prog.close()
 
 
+def exports_arm(args, rank, world, local_rank):
+    """The exports beside the mesh export on the 256-primitive tree: Sodapop's meshing job
+    at its density 20, the point-cloud export at 0.01-unit voxels with 5 refinement steps,
+    and the MagicaVoxel export at 64 voxels per unit; each against the C restatement."""
+    import torch
+    from tangerine_gb300 import build as B
+    B.build()
+    from tangerine_gb300 import sdf
+    from tangerine_gb300 import workloads as W
+    torch.cuda.set_device(local_rank)
+    spec = W.random_tree(SEED, PRIMS)
+    tree = sdf.from_spec(spec)
+    prog = sdf.compile(tree)
+    info = prog.info()
+    lo = np.array(info.bounds_min[:], np.float32)
+    hi = np.array(info.bounds_max[:], np.float32)
+    density, cloud_step, refine, vox_grid = 20.0, 0.01, 5, 64.0
+    kernels = {"soda": ("soda_lattice", "soda_cache", "soda_flags", "scan", "soda_vertices", "soda_faces", "soda_attributes"),
+               "cloud": ("cloud_flags", "list_cells", "cloud_refine", "attributes"),
+               "vox": ("vox_flags", "list_cells")}
+
+    def timed(fn, names):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        sdf.profile_reset()
+        sdf.profile_enable(True)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            out = fn()
+        wall = (time.perf_counter() - t) / args.steps
+        sdf.profile_enable(False)
+        kms = {k: sdf.profile_read(k)[0] / args.steps for k in names}
+        return out, wall, kms
+
+    with ClockSampler(None) as clocks:
+        d, soda_wall, soda_k = timed(lambda: tree.sodapop_mesh(density), kernels["soda"])
+        cloud, cloud_wall, cloud_k = timed(lambda: prog.export_point_cloud(lo, hi, cloud_step, refine), kernels["cloud"])
+        vox, vox_wall, vox_k = timed(lambda: prog.export_voxels(vox_grid, 1), kernels["vox"])
+    soda_cells = int(np.prod(d.grid[6:9].astype(np.int64)))
+    n_cloud = int(np.prod(np.ceil((hi - lo) / np.float32(cloud_step)).astype(np.int64)))
+    vsize = vox[1]
+    n_vox = int(vsize[0]) * int(vsize[1]) * int(vsize[2])
+    cloud_gpu_ms = sum(cloud_k.values())
+    vox_gpu_ms = sum(vox_k.values())
+    soda_gpu_ms = sum(soda_k.values())
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        from oracle import oracle as O
+        port = O.port()
+        h = port.build(spec)
+        try:
+            t = time.perf_counter()
+            port.sodapop(h, density)
+            soda_cpu = time.perf_counter() - t
+            # Middle z-slabs of the same lattices (8 voxel layers each), one core.
+            mid = np.float32(0.5) * (lo[2] + hi[2])
+            slab_lo = np.array([lo[0], lo[1], mid], np.float32)
+            slab_hi = np.array([hi[0], hi[1], mid + np.float32(8 * cloud_step)], np.float32)
+            o = port.octree(h)
+            t = time.perf_counter()
+            pts, _ = port.point_cloud(o, slab_lo, slab_hi, cloud_step, refine)
+            port.vertex_attributes(o, pts, threads=1)
+            cloud_cpu = time.perf_counter() - t
+            port.octree_free(o)
+            slab_voxels = int(np.prod(np.ceil((slab_hi - slab_lo) / np.float32(cloud_step)).astype(np.int64)))
+            t = time.perf_counter()
+            vox_small, vs_small, _ = port.vox(h, 8.0, 1)
+            vox_cpu = time.perf_counter() - t
+            cpu = {"sodapop_meshes_per_s": 1.0 / soda_cpu,
+                   "point_cloud_voxels_per_s": slab_voxels / cloud_cpu,
+                   "vox_voxels_per_s": int(np.prod(vs_small)) / vox_cpu,
+                   "cores": 1, "kind": "port",
+                   "sample": f"C restatement, one core: the whole Sodapop job ({soda_cpu:.2f} s); the point cloud on "
+                             f"an 8-layer middle z-slab ({slab_voxels} voxels, {cloud_cpu:.2f} s); VoxExport's test at "
+                             f"8 voxels per unit ({int(np.prod(vs_small))} voxels, {vox_cpu:.2f} s; full-tree eval per "
+                             f"voxel, the same per-voxel work as at 64)"}
+        finally:
+            port.free(h)
+    line = {"metric": "voxels/s: point-cloud export (with Sodapop meshing and MagicaVoxel export beside it)",
+            "value": world * n_cloud / cloud_wall, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": cloud_wall * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"seeded {PRIMS}-primitive tree (seed {SEED}): point cloud at {cloud_step}-unit voxels "
+                                   f"over the tree bounds ({n_cloud} voxels), {refine} refinement steps, normals + colours; "
+                                   f"Sodapop meshing at density {density:g}; MagicaVoxel at {vox_grid:g} voxels per unit",
+                       "l2": "inputs resident; results copied to host every step"},
+            "point_cloud": {"voxels": n_cloud, "points": int(cloud.vertices.shape[0]), "ms_per_call": cloud_wall * 1e3,
+                            "gpu_kernel_ms": cloud_k, "voxels_per_s_gpu": n_cloud / (cloud_gpu_ms * 1e-3)},
+            "sodapop": {"cells": soda_cells, "vertices": int(d.positions.shape[0]), "faces": int(d.faces.shape[0]),
+                        "ms_per_call": soda_wall * 1e3, "meshes_per_s": 1.0 / soda_wall,
+                        "host_octree_and_compile_ms": d.compile_seconds * 1e3, "gpu_kernel_ms": soda_k,
+                        "gpu_kernels_total_ms": soda_gpu_ms},
+            "vox": {"voxels": n_vox, "kept": int(vox[0].shape[0]), "ms_per_call": vox_wall * 1e3, "gpu_kernel_ms": vox_k,
+                    "voxels_per_s": n_vox / vox_wall, "voxels_per_s_gpu": n_vox / (vox_gpu_ms * 1e-3)},
+            "e2e": {"value": world * n_cloud / cloud_wall, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(cloud.vertices.shape[0]) * 31},
+            "cpu_baseline": cpu, "gpu_launches": 7, "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    prog.close()
+
+
 def main():
     global RES, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -864,9 +969,10 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--batch-models", type=int, default=512, help="trees in the batch workload")
-    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate", "batch"],
+    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate", "batch", "exports"],
                     help="export: the 512^3 mesh export (the benchmark); render: the sphere-tracing workload; "
-                         "surrogate: the 1024^3 export in 32^3 bricks with the learned bound")
+                         "surrogate: the 1024^3 export in 32^3 bricks with the learned bound; batch: 512 trees in one "
+                         "launch; exports: Sodapop meshing, point cloud and MagicaVoxel")
     ap.add_argument("--skip-surrogate", action="store_true", help="skip the surrogate-culled leg of the export")
     ap.add_argument("--resolution", type=int, default=RES,
                     help="grid resolution (512 is the benchmark; smaller values are profiling cases)")
@@ -885,6 +991,8 @@ def main():
         surrogate_arm(args, rank, world, local_rank)
     elif args.workload == "batch":
         batch_arm(args, rank, world, local_rank)
+    elif args.workload == "exports":
+        exports_arm(args, rank, world, local_rank)
     else:
         our_arm(args, rank, world, local_rank)
 

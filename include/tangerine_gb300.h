@@ -189,6 +189,9 @@ TANGERINE_API int64_t tg_debug_octree(void* tree, float* cells, int32_t* childre
 /* The same dump of Sodapop's meshing octree (see tg_sodapop_mesh). */
 TANGERINE_API int64_t tg_debug_meshing_octree(void* tree, float* cells, int32_t* children, int64_t cell_capacity,
                                               uint32_t* words, int64_t word_capacity, int64_t* word_count);
+/* Host-only: builds and compiles the export (or meshing) octree without uploading it and
+ * reports the seconds spent in the octree and in all of the compile. */
+TANGERINE_API tg_status tg_debug_compile_seconds(void* tree, int meshing, double* octree_seconds, double* total_seconds);
 /* Host-only plan of tg_sodapop_mesh: grid gets origin xyz, step xyz, cells xyz, the point
  * cache's limit and the lattice's z layers (11 floats); boxes the leaves' inclusive integer
  * point-cache spans (6 per leaf, up to box_capacity leaves); leaves the leaf count. */

@@ -271,6 +271,17 @@ extern "C"
 		return DumpOctree(o, cells, children, cell_capacity, words, word_capacity, word_count);
 	}
 
+	TANGERINE_API tg_status tg_debug_compile_seconds(void* tree, int meshing, double* octree_seconds, double* total_seconds)
+	{
+		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
+		CompiledTree t;
+		std::string err;
+		if (!CompileTree(Borrow(tree), t, err, meshing ? OctreeKind::Meshing : OctreeKind::Export)) { SetError(err); return TG_ERR_UNBOUNDED; }
+		if (octree_seconds) *octree_seconds = t.OctreeSeconds;
+		if (total_seconds) *total_seconds = t.BuildSeconds;
+		return TG_OK;
+	}
+
 	TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* grid, int64_t* boxes, int64_t box_capacity,
 		int64_t* leaves)
 	{

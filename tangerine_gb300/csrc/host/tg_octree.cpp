@@ -588,7 +588,9 @@ namespace tg
 			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
 			return false;
 		}
+		const auto t1 = std::chrono::steady_clock::now();
 		out = CompiledTree();
+		out.OctreeSeconds = std::chrono::duration<double>(t1 - t0).count();
 		out.Bounds = root->Bounds();
 		out.OctreeBounds = octree.Cells[0].Bounds;
 		std::unordered_map<const Material*, int> materials;
@@ -598,6 +600,9 @@ namespace tg
 		Emitter em{ out.Code, materials, Emitter::NextEpoch(), {}, {}, false };
 		int maxStack = 0;
 		int stopQuad = -1;
+		struct EmittedPrograms { int Distance, Surface, Stack; bool NonLipschitz; };
+		std::unordered_map<const Node*, EmittedPrograms> emitted;
+		emitted.reserve(octree.Cells.size());
 		out.Nodes.resize(octree.Cells.size());
 		for (size_t i = 0; i < octree.Cells.size(); ++i)
 		{
@@ -622,6 +627,19 @@ namespace tg
 				continue;
 			}
 			if (kind == OctreeKind::Meshing && c.Terminus) out.LeafBounds.push_back(c.Bounds);
+			// Cells whose clip left the parent's subtree untouched share its node (RebuildSet),
+			// so their programs are the same records: emit them once.
+			auto found = emitted.find(c.Evaluator.get());
+			if (found != emitted.end())
+			{
+				const EmittedPrograms& e = found->second;
+				n.DistanceCode = e.Distance;
+				n.SurfaceCode = e.Surface;
+				n.StackSize = e.Stack;
+				n.ClipRadius = e.NonLipschitz ? -c.ClipRadius : c.ClipRadius;
+				out.DistanceQuadsTotal += e.Surface - e.Distance;
+				continue;
+			}
 			const int dist = (int)(out.Code.size() / 4);
 			em.NonLipschitz = false;
 			em.Distance(*c.Evaluator);
@@ -637,6 +655,7 @@ namespace tg
 			n.StackSize = d1 > d2 ? d1 : d2;
 			if (n.StackSize > maxStack) maxStack = n.StackSize;
 			out.DistanceQuadsTotal += surf - dist;
+			emitted.emplace(c.Evaluator.get(), EmittedPrograms{ dist, surf, n.StackSize, em.NonLipschitz });
 		}
 		// The whole tree's surface program, for SDFNode::RayMarch / Eval on the full tree.
 		const int full = (int)(out.Code.size() / 4);

@@ -56,6 +56,7 @@ namespace tg
 		AABB OctreeBounds{};              // the octree root cell's bounds
 		std::vector<AABB> LeafBounds;     // terminus cells with an evaluator (meshing octree)
 		double BuildSeconds = 0.0;
+		double OctreeSeconds = 0.0;       // of which the octree (clips, merges)
 		int64_t DistanceQuadsTotal = 0;
 	};
 

@@ -108,6 +108,13 @@ namespace tg
 				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
 				const int i1 = min(i0 + bg.B, g.NX - 1), j1 = min(j0 + bg.B, g.NY - 1), k1 = min(k0 + bg.B, g.NZ - 1);
+				// The brick's points mostly share one octree cell: descend once with the
+				// brick's box (lattice coordinates are monotone in the index), then per point
+				// only below where the box straddles a pivot.
+				bool shared;
+				const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.Step), LatticeCoord(g.X0, i1, g.Step),
+					LatticeCoord(g.Y0, j0, g.Step), LatticeCoord(g.Y0, j1, g.Step), LatticeCoord(g.Z0, k0, g.Step),
+					LatticeCoord(g.Z0, k1, g.Step), shared);
 				for (int oz = 0; oz < C; oz += ZSpan)
 				for (int oy = 0; oy < C; oy += 8)
 				for (int ox = 0; ox < C; ox += 8)
@@ -126,7 +133,7 @@ namespace tg
 						px[k] = x;
 						py[k] = y;
 						pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.Step);
-						cell[k] = DescendOctree(prog.Nodes, px[k], py[k], pz[k]);
+						cell[k] = shared ? top : DescendOctreeFrom(prog.Nodes, top, px[k], py[k], pz[k]);
 						res[k] = 0.0f;
 						if (inPlane && iz <= k1) todo |= 1u << k;
 					}

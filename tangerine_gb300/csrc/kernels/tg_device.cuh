@@ -37,6 +37,46 @@ namespace tg
 		return at;
 	}
 
+	// DescendOctree continued from cell `at` (an ancestor of the point's cell).
+	__device__ __forceinline__ int DescendOctreeFrom(const OctNode* __restrict__ nodes, int at, float x, float y, float z)
+	{
+		for (int guard = 0; guard < 64; ++guard)
+		{
+			const float4 a = __ldg(reinterpret_cast<const float4*>(nodes + at));
+			if (__float_as_int(a.w) & kNodeTerminus) break;
+			const int octant = (x > a.x ? 1 : 0) | (y > a.y ? 2 : 0) | (z > a.z ? 4 : 0);
+			const int child = __ldg(&nodes[at].Child[octant]);
+			if (child < 0) break;
+			at = child;
+		}
+		return at;
+	}
+
+	// The descent of a whole box of points [x0, x1] x [y0, y1] x [z0, z1] as far as they all
+	// take the same octant: returns the cell reached, and `shared` = every point of the box
+	// descends to exactly that cell (DescendOctree's `p > pivot` rule holds for the whole box
+	// when its lower corner is above the pivot, and fails for it when its upper corner is not).
+	__device__ __forceinline__ int DescendBox(const OctNode* __restrict__ nodes, float x0, float x1, float y0, float y1, float z0,
+		float z1, bool& shared)
+	{
+		int at = 0;
+		shared = false;
+		for (int guard = 0; guard < 64; ++guard)
+		{
+			const float4 a = __ldg(reinterpret_cast<const float4*>(nodes + at));
+			if (__float_as_int(a.w) & kNodeTerminus) { shared = true; break; }
+			const bool hx = x0 > a.x, lx = !(x1 > a.x);
+			const bool hy = y0 > a.y, ly = !(y1 > a.y);
+			const bool hz = z0 > a.z, lz = !(z1 > a.z);
+			if (!((hx || lx) && (hy || ly) && (hz || lz))) break;
+			const int octant = (hx ? 1 : 0) | (hy ? 2 : 0) | (hz ? 4 : 0);
+			const int child = __ldg(&nodes[at].Child[octant]);
+			if (child < 0) { shared = true; break; }
+			at = child;
+		}
+		return at;
+	}
+
 	__device__ __forceinline__ float4 LoadQuad(const float4* __restrict__ code, int q)
 	{
 		return __ldg(code + q);
