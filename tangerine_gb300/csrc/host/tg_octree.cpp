@@ -3,6 +3,7 @@
 #include "tg_octree.hpp"
 #include "tg_pool.hpp"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -80,6 +81,16 @@ namespace tg
 			NodeRef evals[8];
 			parent.Eval->Clip8(pivots, radii, evals);
 			for (int i = 0; i < 8; ++i) SetEvaluator(*parent.Kids[i], std::move(evals[i]), spans[i], bp);
+		}
+
+		// One child of an expanded cell on its own (Clip to its sphere): the same evaluator
+		// InitChildren gives it, for levels with too few cells to keep the workers busy.
+		void InitChild(TmpCell& parent, int i, const BuildParams& bp)
+		{
+			TmpCell& kid = *parent.Kids[i];
+			float span;
+			PlaceCell(kid, span);
+			SetEvaluator(kid, parent.Eval->Clip(kid.Pivot, kid.Radius), span, bp);
 		}
 
 		// The tail of SDFOctree::Populate (sdf_evaluator.cpp:1703-1783), once the children
@@ -162,7 +173,11 @@ namespace tg
 					}
 					parents.push_back(c);
 				}
-				WorkerPool::Get().ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[j], bp); });
+				WorkerPool& pool = WorkerPool::Get();
+				if ((int)parents.size() <= pool.Workers())
+					pool.ParallelFor((int)parents.size() * 8, [&](int j) { InitChild(*parents[j / 8], j % 8, bp); });
+				else
+					pool.ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[j], bp); });
 				level.clear();
 				for (TmpCell* c : parents)
 					for (auto& k : c->Kids) level.push_back(k.get());
@@ -184,6 +199,15 @@ namespace tg
 				if (k) FindIncomplete(*k, out);
 		}
 
+		size_t CountCells(const TmpCell& t)
+		{
+			size_t n = 1;
+			if (!t.Terminus)
+				for (const auto& k : t.Kids)
+					if (k) n += CountCells(*k);
+			return n;
+		}
+
 		void Flatten(TmpCell& t, std::vector<Octree::Cell>& out)
 		{
 			const int index = (int)out.size();
@@ -197,7 +221,7 @@ namespace tg
 				c.Terminus = t.Terminus;
 				c.Incomplete = t.Incomplete;
 				c.EvaluatorLeaves = t.Leaves;
-				c.Evaluator = t.Eval;
+				c.Evaluator = std::move(t.Eval);   // the build is done with it
 			}
 			if (t.Terminus) return;
 			for (int i = 0; i < 8; ++i)
@@ -230,6 +254,7 @@ namespace tg
 		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
 		BuildLevels({ top.get() }, bp, 1);
+		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
 		return true;
 	}
@@ -258,6 +283,7 @@ namespace tg
 		FindIncomplete(*top, incomplete);
 		const BuildParams second{ 0.25f, false, -1 };
 		BuildLevels(incomplete, second, 3);
+		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
 		return true;
 	}
@@ -333,39 +359,98 @@ namespace tg
 			}
 		}
 
+		// Facts the emitter caches per node: the slot of a brush's records and whether a
+		// subtree has paint.  Open addressing on the node's address; one table per emitter,
+		// so emitters on different threads share nothing.
+		class NodeFacts
+		{
+		public:
+			struct Entry
+			{
+				const Node* Key;
+				int32_t Record;     // -1: not built
+				int8_t Paint;       // -1: not known
+			};
+			NodeFacts() { Slots.assign(1024, Entry{ nullptr, -1, -1 }); }
+			// The entry of n, or null (no insertion).
+			const Entry* Find(const Node* n) const
+			{
+				const size_t mask = Slots.size() - 1;
+				for (size_t i = Hash(n) & mask;; i = (i + 1) & mask)
+				{
+					const Entry& e = Slots[i];
+					if (e.Key == n) return &e;
+					if (!e.Key) return nullptr;
+				}
+			}
+			// The entry of n, created if absent; valid until the next call.
+			Entry& At(const Node* n)
+			{
+				if ((Size + 1) * 2 > Slots.size()) Grow();
+				const size_t mask = Slots.size() - 1;
+				size_t i = Hash(n) & mask;
+				for (;;)
+				{
+					Entry& e = Slots[i];
+					if (e.Key == n) return e;
+					if (!e.Key)
+					{
+						e = Entry{ n, -1, -1 };
+						++Size;
+						return e;
+					}
+					i = (i + 1) & mask;
+				}
+			}
+
+		private:
+			static size_t Hash(const Node* n)
+			{
+				uint64_t x = (uint64_t)(uintptr_t)n;
+				x ^= x >> 33;
+				x *= 0xff51afd7ed558ccdULL;
+				x ^= x >> 33;
+				return (size_t)x;
+			}
+			void Grow()
+			{
+				std::vector<Entry> old;
+				old.swap(Slots);
+				Slots.assign(old.size() * 2, Entry{ nullptr, -1, -1 });
+				Size = 0;
+				for (const Entry& e : old)
+				{
+					if (!e.Key) continue;
+					Entry& n = At(e.Key);
+					n.Record = e.Record;
+					n.Paint = e.Paint;
+				}
+			}
+			std::vector<Entry> Slots;
+			size_t Size = 0;
+		};
+
 		// Emits record programs.  Clipped trees share their brush nodes with the full tree,
 		// so one brush appears in many cells' programs: its records (an inverse matrix is
-		// ~200 flops to build) and every subtree's paint flag are computed once per compile.
+		// ~200 flops to build) and every subtree's paint flag are computed once per emitter.
+		// A brush's two records, as spans of a record arena.
+		struct RecordSpans
+		{
+			int DistanceAt, DistanceFloats, SurfaceAt, SurfaceFloats;
+		};
+
 		struct Emitter
 		{
 			std::vector<float>& Code;
 			const std::unordered_map<const Material*, int>& Materials;
-			uint32_t Epoch;
-			std::vector<std::vector<float>> DistanceRecords;
-			std::vector<std::vector<float>> SurfaceRecords;
+			std::vector<float> Arena;                    // this emitter's own brush records
+			std::vector<RecordSpans> Spans;
+			const Emitter* Shared = nullptr;             // records built before the parallel emission
 			bool NonLipschitz = false;
+			NodeFacts Facts;
 
-			static uint32_t NextEpoch()
-			{
-				static std::atomic<uint32_t> counter{ 0 };
-				uint32_t e = counter.fetch_add(1) + 1;
-				return e == 0 ? counter.fetch_add(1) + 1 : e;
-			}
-
-			// Slot of this node in the per-compile caches (created on first use).
-			void Touch(const Node& n)
-			{
-				if (n.CacheEpoch == Epoch) return;
-				n.CacheEpoch = Epoch;
-				n.CacheRecord = -1;
-				switch (n.Kind)
-				{
-				case NodeKind::Brush: n.CachePaint = n.Mat != nullptr; break;
-				case NodeKind::Set: n.CachePaint = HasPaint(*n.Lhs) || HasPaint(*n.Rhs); break;
-				case NodeKind::Flate: n.CachePaint = HasPaint(*n.Lhs); break;
-				case NodeKind::Stencil: n.CachePaint = true; break;
-				}
-			}
+			Emitter(std::vector<float>& code, const std::unordered_map<const Material*, int>& materials, const Emitter* shared = nullptr)
+				: Code(code), Materials(materials), Shared(shared) {}
 
 			void Quad(uint32_t head, float a, float b, float c)
 			{
@@ -390,15 +475,50 @@ namespace tg
 			}
 			bool HasPaint(const Node& n)
 			{
-				Touch(n);
-				return n.CachePaint;
+				{
+					const NodeFacts::Entry& e = Facts.At(&n);
+					if (e.Paint >= 0) return e.Paint != 0;
+				}
+				bool paint = false;
+				switch (n.Kind)
+				{
+				case NodeKind::Brush: paint = n.Mat != nullptr; break;
+				case NodeKind::Set: paint = HasPaint(*n.Lhs) || HasPaint(*n.Rhs); break;
+				case NodeKind::Flate: paint = HasPaint(*n.Lhs); break;
+				case NodeKind::Stencil: paint = true; break;
+				}
+				Facts.At(&n).Paint = paint ? 1 : 0;
+				return paint;
 			}
 
-			// Records of one brush: [distance quads, surface quads], built once per compile.
+			// Records of one brush: [distance quads, surface quads], built once per emitter
+			// (or taken from the shared emitter's arena).
+			void AppendRecords(const Node& n, bool surface)
+			{
+				const float* arena;
+				const RecordSpans* sp;
+				const NodeFacts::Entry* shared = Shared ? Shared->Facts.Find(&n) : nullptr;
+				if (shared && shared->Record >= 0)
+				{
+					arena = Shared->Arena.data();
+					sp = &Shared->Spans[(size_t)shared->Record];
+				}
+				else
+				{
+					const int r = Records(n);
+					arena = Arena.data();
+					sp = &Spans[(size_t)r];
+				}
+				const float* from = arena + (surface ? sp->SurfaceAt : sp->DistanceAt);
+				Code.insert(Code.end(), from, from + (surface ? sp->SurfaceFloats : sp->DistanceFloats));
+			}
+
 			int Records(const Node& n)
 			{
-				Touch(n);
-				if (n.CacheRecord >= 0) return n.CacheRecord;
+				{
+					const NodeFacts::Entry& e = Facts.At(&n);
+					if (e.Record >= 0) return e.Record;
+				}
 				std::vector<float> dist, surf;
 				const Transform& t = n.Xf;
 				const bool rot = !t.Rotation.IsIdentity();
@@ -425,12 +545,30 @@ namespace tg
 				Quad4(surf, qi.w, qi.x, qi.y, qi.z);
 				Quad4(surf, t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
 				Quad(surf, (uint32_t)MaterialIndex(n.Mat.get()), 0.0f, 0.0f, 0.0f);
-				n.CacheRecord = (int32_t)DistanceRecords.size();
-				DistanceRecords.push_back(std::move(dist));
-				SurfaceRecords.push_back(std::move(surf));
-				return n.CacheRecord;
+				const int32_t slot = (int32_t)Spans.size();
+				RecordSpans sp;
+				sp.DistanceAt = (int)Arena.size();
+				sp.DistanceFloats = (int)dist.size();
+				Arena.insert(Arena.end(), dist.begin(), dist.end());
+				sp.SurfaceAt = (int)Arena.size();
+				sp.SurfaceFloats = (int)surf.size();
+				Arena.insert(Arena.end(), surf.begin(), surf.end());
+				Spans.push_back(sp);
+				Facts.At(&n).Record = slot;
+				return slot;
 			}
-			void Append(const std::vector<float>& rec) { Code.insert(Code.end(), rec.begin(), rec.end()); }
+
+			// Builds the records of every brush under n (the full tree, before emission).
+			void BuildAllRecords(const Node& n)
+			{
+				switch (n.Kind)
+				{
+				case NodeKind::Brush: Records(n); break;
+				case NodeKind::Set: BuildAllRecords(*n.Lhs); BuildAllRecords(*n.Rhs); break;
+				case NodeKind::Flate: BuildAllRecords(*n.Lhs); break;
+				case NodeKind::Stencil: BuildAllRecords(*n.Lhs); BuildAllRecords(*n.Mask); break;
+				}
+			}
 
 			// Distance program: Tangerine's postfix program with each brush's transform,
 			// primitive and field scale fused into one record.
@@ -440,7 +578,7 @@ namespace tg
 				{
 				case NodeKind::Brush:
 					if (n.Op == OpEllipsoid) NonLipschitz = true;
-					Append(DistanceRecords[Records(n)]);
+					AppendRecords(n, false);
 					break;
 				case NodeKind::Set:
 					Distance(*n.Lhs);
@@ -463,7 +601,7 @@ namespace tg
 				switch (n.Kind)
 				{
 				case NodeKind::Brush:
-					Append(SurfaceRecords[Records(n)]);
+					AppendRecords(n, true);
 					break;
 				case NodeKind::Set:
 				{
@@ -596,13 +734,82 @@ namespace tg
 		std::unordered_map<const Material*, int> materials;
 		std::vector<const Material*> materialList;
 		CollectMaterials(*root, materials, materialList);
-		out.Code.reserve(1 << 20);
-		Emitter em{ out.Code, materials, Emitter::NextEpoch(), {}, {}, false };
-		int maxStack = 0;
-		int stopQuad = -1;
+		// Each distinct evaluator's two programs are emitted once (cells whose clip left the
+		// parent's subtree untouched share its node, RebuildSet), in parallel over chunks of
+		// the distinct evaluators, each chunk into its own buffer with its own emitter; the
+		// buffers are then laid end to end in chunk order, so the layout does not depend on
+		// the threads' timing.
 		struct EmittedPrograms { int Distance, Surface, Stack; bool NonLipschitz; };
-		std::unordered_map<const Node*, EmittedPrograms> emitted;
-		emitted.reserve(octree.Cells.size());
+		std::vector<const Node*> distinct;
+		std::vector<int> programOf(octree.Cells.size(), -1);
+		{
+			std::unordered_map<const Node*, int> index;
+			index.reserve(octree.Cells.size());
+			for (size_t i = 0; i < octree.Cells.size(); ++i)
+			{
+				const Node* e = octree.Cells[i].Evaluator.get();
+				if (!e) continue;
+				auto ins = index.emplace(e, (int)distinct.size());
+				if (ins.second) distinct.push_back(e);
+				programOf[i] = ins.first->second;
+			}
+		}
+		// Every brush of the full tree (clipped trees share them) gets its records once, up
+		// front; the emitters only copy spans of them.
+		std::vector<float> unused;
+		Emitter shared(unused, materials);
+		shared.BuildAllRecords(*root);
+		// The last item is the whole tree's surface program, for SDFNode::RayMarch / Eval.
+		const size_t items = distinct.size() + 1;
+		const int chunkCount = (int)std::min<size_t>(items, (size_t)WorkerPool::Get().Workers() * 4 + 4);
+		std::vector<std::vector<float>> chunkCode((size_t)chunkCount);
+		std::vector<EmittedPrograms> programs(items);
+		auto chunkBegin = [&](int ch) { return (size_t)((uint64_t)items * (uint64_t)ch / (uint64_t)chunkCount); };
+		WorkerPool::Get().ParallelFor(chunkCount, [&](int ch)
+		{
+			std::vector<float>& code = chunkCode[(size_t)ch];
+			code.reserve(1 << 14);
+			Emitter em(code, materials, &shared);
+			for (size_t u = chunkBegin(ch); u < chunkBegin(ch + 1); ++u)
+			{
+				if (u == distinct.size())
+				{
+					const int surf = (int)(code.size() / 4);
+					em.Surface(*root);
+					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+					programs[u] = EmittedPrograms{ surf, surf, SurfaceDepth(code.data(), surf), false };
+					continue;
+				}
+				const int dist = (int)(code.size() / 4);
+				em.NonLipschitz = false;
+				em.Distance(*distinct[u]);
+				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				const int surf = (int)(code.size() / 4);
+				em.Surface(*distinct[u]);
+				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				const int d1 = ProgramDepth(code.data(), dist);
+				const int d2 = SurfaceDepth(code.data(), surf);
+				programs[u] = EmittedPrograms{ dist, surf, d1 > d2 ? d1 : d2, em.NonLipschitz };
+			}
+		});
+		size_t total = 4;
+		for (const auto& c : chunkCode) total += c.size();
+		out.Code.reserve(total + 4096);
+		// One stop record first: the programs of cells without an evaluator.
+		out.Code.push_back(BitsFloat(OpStop));
+		out.Code.push_back(0.0f); out.Code.push_back(0.0f); out.Code.push_back(0.0f);
+		const int stopQuad = 0;
+		for (int ch = 0; ch < chunkCount; ++ch)
+		{
+			const int base = (int)(out.Code.size() / 4);
+			for (size_t u = chunkBegin(ch); u < chunkBegin(ch + 1); ++u)
+			{
+				programs[u].Distance += base;
+				programs[u].Surface += base;
+			}
+			out.Code.insert(out.Code.end(), chunkCode[(size_t)ch].begin(), chunkCode[(size_t)ch].end());
+		}
+		int maxStack = 0;
 		out.Nodes.resize(octree.Cells.size());
 		for (size_t i = 0; i < octree.Cells.size(); ++i)
 		{
@@ -614,12 +821,7 @@ namespace tg
 			if (!c.Evaluator)
 			{
 				// Only the meshing octree's second stage leaves such cells; descents pass
-				// over them, and their programs are one shared stop record.
-				if (stopQuad < 0)
-				{
-					stopQuad = (int)(out.Code.size() / 4);
-					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-				}
+				// over them.
 				n.Flags |= kNodeNoEvaluator;
 				n.DistanceCode = n.SurfaceCode = stopQuad;
 				n.StackSize = 0;
@@ -627,45 +829,16 @@ namespace tg
 				continue;
 			}
 			if (kind == OctreeKind::Meshing && c.Terminus) out.LeafBounds.push_back(c.Bounds);
-			// Cells whose clip left the parent's subtree untouched share its node (RebuildSet),
-			// so their programs are the same records: emit them once.
-			auto found = emitted.find(c.Evaluator.get());
-			if (found != emitted.end())
-			{
-				const EmittedPrograms& e = found->second;
-				n.DistanceCode = e.Distance;
-				n.SurfaceCode = e.Surface;
-				n.StackSize = e.Stack;
-				n.ClipRadius = e.NonLipschitz ? -c.ClipRadius : c.ClipRadius;
-				out.DistanceQuadsTotal += e.Surface - e.Distance;
-				continue;
-			}
-			const int dist = (int)(out.Code.size() / 4);
-			em.NonLipschitz = false;
-			em.Distance(*c.Evaluator);
-			n.ClipRadius = em.NonLipschitz ? -c.ClipRadius : c.ClipRadius;
-			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-			const int surf = (int)(out.Code.size() / 4);
-			em.Surface(*c.Evaluator);
-			em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-			n.DistanceCode = dist;
-			n.SurfaceCode = surf;
-			const int d1 = ProgramDepth(out.Code.data(), dist);
-			const int d2 = SurfaceDepth(out.Code.data(), surf);
-			n.StackSize = d1 > d2 ? d1 : d2;
+			const EmittedPrograms& e = programs[(size_t)programOf[i]];
+			n.DistanceCode = e.Distance;
+			n.SurfaceCode = e.Surface;
+			n.StackSize = e.Stack;
+			n.ClipRadius = e.NonLipschitz ? -c.ClipRadius : c.ClipRadius;
 			if (n.StackSize > maxStack) maxStack = n.StackSize;
-			out.DistanceQuadsTotal += surf - dist;
-			emitted.emplace(c.Evaluator.get(), EmittedPrograms{ dist, surf, n.StackSize, em.NonLipschitz });
+			out.DistanceQuadsTotal += e.Surface - e.Distance;
 		}
-		// The whole tree's surface program, for SDFNode::RayMarch / Eval on the full tree.
-		const int full = (int)(out.Code.size() / 4);
-		em.NonLipschitz = false;
-		em.Surface(*root);
-		em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-		{
-			const int d = SurfaceDepth(out.Code.data(), full);
-			if (d > maxStack) maxStack = d;
-		}
+		const int full = programs[distinct.size()].Surface;
+		if (programs[distinct.size()].Stack > maxStack) maxStack = programs[distinct.size()].Stack;
 		out.Header.FullSurfaceCode = full;
 		out.Header.Lipschitz = HasNonLipschitzBrush(*root) ? 0 : 1;
 		if (maxStack > kMaxStack)

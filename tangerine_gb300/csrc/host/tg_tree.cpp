@@ -257,75 +257,96 @@ namespace tg
 			float At(const Node& n) { const uint32_t i = E.Index(n); return E.Values[8 * i + Lane]; }
 		};
 
+		// The clip works on plain pointers: an untouched subtree is the input node itself, and
+		// only rebuilt nodes are allocated, kept alive in `keep` until the caller holds the
+		// result.  Reference counts (atomics on nodes that every thread's clips share) are
+		// touched only for rebuilt nodes' operands and the final result.
+		struct ClipScratch
+		{
+			std::vector<NodeRef> Keep;
+			const Node* Hold(NodeRef n)
+			{
+				const Node* raw = n.get();
+				Keep.push_back(std::move(n));
+				return raw;
+			}
+		};
+
+		inline NodeRef Own(const Node* n) { return NodeRef::Share(const_cast<Node*>(n)); }
+
 		// A set node whose clipped operands are its own operands is kept as it is (the
 		// node MakeSet would build from them is the same node).
-		NodeRef RebuildSet(const Node& n, NodeRef l, NodeRef r)
+		const Node* RebuildSet(const Node& n, const Node* l, const Node* r, ClipScratch& cs)
 		{
-			if (l.get() == n.Lhs.get() && r.get() == n.Rhs.get()) return NodeRef::Share(const_cast<Node*>(&n));
-			return SDF::MakeSet(n.Op, std::move(l), std::move(r), n.Threshold);
+			if (l == n.Lhs.get() && r == n.Rhs.get()) return &n;
+			return cs.Hold(SDF::MakeSet(n.Op, Own(l), Own(r), n.Threshold));
 		}
 
 		// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
 		// that can matter inside the sphere (p, radius).  Union keeps whichever side is near,
 		// Diff keeps its left side, Inter needs both; blending widens the sphere by k.
 		template<typename Ev>
-		NodeRef ClipAt(const Node& n, float radius, Ev& ev)
+		const Node* ClipAt(const Node& n, float radius, Ev& ev, ClipScratch& cs)
 		{
 			switch (n.Kind)
 			{
 			case NodeKind::Brush:
-				return ev.At(n) <= radius ? NodeRef::Share(const_cast<Node*>(&n)) : NodeRef();
+				return ev.At(n) <= radius ? &n : nullptr;
 			case NodeKind::Stencil:
 			{
-				NodeRef child = ClipAt(*n.Lhs, radius, ev);
-				if (!child) return NodeRef();
-				return SDF::Stencil(std::move(child), n.Mask, n.Mat, n.Negative);
+				const Node* child = ClipAt(*n.Lhs, radius, ev, cs);
+				if (!child) return nullptr;
+				return cs.Hold(SDF::Stencil(Own(child), n.Mask, n.Mat, n.Negative));
 			}
 			case NodeKind::Flate:
 			{
-				if (!(ev.At(n) <= radius)) return NodeRef();
-				NodeRef child = ClipAt(*n.Lhs, radius + n.Threshold, ev);
-				if (!child) return NodeRef();
-				return SDF::Flate(std::move(child), n.Threshold);
+				if (!(ev.At(n) <= radius)) return nullptr;
+				const Node* child = ClipAt(*n.Lhs, radius + n.Threshold, ev, cs);
+				if (!child) return nullptr;
+				return cs.Hold(SDF::Flate(Own(child), n.Threshold));
 			}
 			case NodeKind::Set:
 			{
-				if (!(ev.At(n) <= radius)) return NodeRef();
+				if (!(ev.At(n) <= radius)) return nullptr;
 				const bool unionFamily = (n.Op == OpUnion || n.Op == OpBlendUnion);
 				const bool diffFamily = (n.Op == OpDiff || n.Op == OpBlendDiff);
 				if (IsBlendOp(n.Op))
 				{
 					const float wide = radius + n.Threshold;
-					NodeRef l = ClipAt(*n.Lhs, wide, ev);
-					NodeRef r = ClipAt(*n.Rhs, wide, ev);
-					if (l && r) return RebuildSet(n, std::move(l), std::move(r));
-					if (!unionFamily && !diffFamily) return NodeRef();
+					const Node* l = ClipAt(*n.Lhs, wide, ev, cs);
+					const Node* r = ClipAt(*n.Rhs, wide, ev, cs);
+					if (l && r) return RebuildSet(n, l, r, cs);
+					if (!unionFamily && !diffFamily) return nullptr;
 				}
-				NodeRef l = ClipAt(*n.Lhs, radius, ev);
-				NodeRef r = ClipAt(*n.Rhs, radius, ev);
-				if (l && r) return RebuildSet(n, std::move(l), std::move(r));
-				if (unionFamily) return l ? std::move(l) : std::move(r);
+				const Node* l = ClipAt(*n.Lhs, radius, ev, cs);
+				const Node* r = ClipAt(*n.Rhs, radius, ev, cs);
+				if (l && r) return RebuildSet(n, l, r, cs);
+				if (unionFamily) return l ? l : r;
 				if (diffFamily) return l;
-				return NodeRef();
+				return nullptr;
 			}
 			}
-			return NodeRef();
+			return nullptr;
 		}
 	}
 
 	NodeRef Node::Clip(Vec3 p, float radius) const
 	{
 		PointEvaluations ev(p);
-		return ClipAt(*this, radius, ev);
+		ClipScratch cs;
+		const Node* r = ClipAt(*this, radius, ev, cs);
+		return r ? Own(r) : NodeRef();
 	}
 
 	void Node::Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8]) const
 	{
 		Evaluations8 ev(p);
+		ClipScratch cs;
 		for (int i = 0; i < 8; ++i)
 		{
 			LaneOf8 lane{ ev, i };
-			out[i] = ClipAt(*this, radius[i], lane);
+			const Node* r = ClipAt(*this, radius[i], lane, cs);
+			out[i] = r ? Own(r) : NodeRef();
 		}
 	}
 

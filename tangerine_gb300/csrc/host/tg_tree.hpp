@@ -65,12 +65,6 @@ namespace tg
 		float Threshold = 0.0f;
 		bool Negative = false;
 
-		// Per-compile caches of the program emitter (valid while CacheEpoch matches the
-		// emitter's epoch; emission runs under the engine lock, one compile at a time).
-		mutable uint32_t CacheEpoch = 0;
-		mutable int32_t CacheRecord = -1;
-		mutable bool CachePaint = false;
-
 		float Eval(Vec3 p) const;
 		NodeRef Clip(Vec3 p, float radius) const;
 		// Clip to eight spheres at once (the same result as eight Clip calls).
