@@ -756,6 +756,35 @@ def batch_arm(args, rank, world, local_rank):
             d2h += mesh.vertices.nbytes + mesh.normals.nbytes + mesh.faces.nbytes + mesh.cubes.nbytes + \
                 (mesh.colors.nbytes if mesh.colors is not None else 0)
     e2e_s = time.perf_counter() - t0
+    # The surrogate form: a learned bound per large model culls its bricks inside the same
+    # graph, the kept bricks also take the exact test; every mesh must stay the exact one.
+    surrogate = None
+    if not args.skip_surrogate:
+        large = [m for m in range(count) if models[m][1] >= 256 and models[m][2] >= 256]
+        exact_meshes = {m: batch.mesh(m, stream=sp) for m in large}
+        t0 = time.perf_counter()
+        nets = [None] * count
+        for m in large:
+            nets[m] = sdf.Surrogate(samples=1 << 20, steps=600, batch=1 << 16, validation=1 << 18)
+            nets[m].fit(progs[m])
+        fit_s = time.perf_counter() - t0
+        batch.set_surrogates(nets, only=False)
+        for _ in range(max(1, args.warmup)):
+            batch.run(stream=sp)
+        sur_ms = timed(lambda: batch.run(stream=sp), args.steps)
+        sinfo = batch.info()
+        same = all(np.array_equal(batch.mesh(m, stream=sp).vertices, exact_meshes[m].vertices) and
+                   np.array_equal(batch.mesh(m, stream=sp).faces, exact_meshes[m].faces) for m in large)
+        surrogate = {"value": samples * args.steps / (sur_ms * 1e-3), "ms_per_step": sur_ms / args.steps,
+                     "vs_exact_batch": ms / sur_ms, "models_with_network": len(large), "fit_seconds_total": fit_s,
+                     "bricks_evaluated": sinfo.bricks_evaluated, "same_meshes_as_exact": bool(same),
+                     "note": "a 16-level hash grid + 3x64 BF16 network per model with >= 256 primitives on a >= 256^3 grid "
+                             "(600 Adam steps each), network bits written before the persistent launch, kept bricks "
+                             "re-tested exactly"}
+        batch.set_surrogates([None] * count)
+        for n in nets:
+            if n is not None:
+                n.close()
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         big = max(range(count), key=lambda m: models[m][1] * models[m][2] ** 2)
@@ -781,6 +810,7 @@ def batch_arm(args, rank, world, local_rank):
                       "tuning_histogram_brick_x_lanes": hist},
             "sequential_exports": {"ms_per_step": seq_ms, "value": samples / (seq_ms * 1e-3),
                                    "note": "same models, one tg_export_mesh_device call each"},
+            "surrogate_form": surrogate,
             "cpu_baseline": cpu,
             "e2e": {"value": samples * e2e_steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(d2h), "call": "tg_batch_run + tg_batch_mesh for every model"},

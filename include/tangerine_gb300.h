@@ -529,6 +529,13 @@ TANGERINE_API tg_status tg_export_mesh_surrogate(tg_program* program, tg_surroga
                                                  tg_mesh* out, void* stream);
 TANGERINE_API tg_status tg_export_mesh_surrogate_device(tg_program* program, tg_surrogate* s, const tg_grid* grid,
                                                         uint32_t flags, tg_device_mesh* out, void* stream);
+
+/* The batch's surrogate form: model m's bricks are culled by nets[m] (a fitted
+ * tg_surrogate; NULL keeps the exact test for that model) before the launch, inside the same
+ * CUDA graph; the bricks a network keeps then take the exact test too, unless flags has
+ * TG_MESH_SURROGATE_ONLY.  Either way each model's mesh is the exact export's (the networks'
+ * margins are conservative).  The networks must outlive the batch's runs. */
+TANGERINE_API tg_status tg_batch_set_surrogates(tg_batch* batch, tg_surrogate* const* nets, int count, uint32_t flags);
 /* tg_render with network steps: each ray steps by the larger of the root cube's distance
  * and the network's value less its margin (safety x the largest held-out error) until that
  * bound falls to the margin, then by SDFNode::RayMarch's exact whole-tree steps; hits are

@@ -156,6 +156,7 @@ SIGNATURES = {
     "tg_batch_autotune": (_i, [_vp, _vp]),
     "tg_batch_set_tuning": (_i, [_vp, _vp, _vp]),
     "tg_batch_get_tuning": (_i, [_vp, _vp, _vp]),
+    "tg_batch_set_surrogates": (_i, [_vp, _vp, _i, _u32]),
     "tg_batch_run": (_i, [_vp, _vp]),
     "tg_batch_reserve": (_i, [_vp, C.c_uint64, C.c_uint64]),
     "tg_batch_get_info": (_i, [_vp, C.POINTER(BatchInfo)]),

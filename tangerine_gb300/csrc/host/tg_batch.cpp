@@ -1,4 +1,5 @@
 #include "tg_batch.hpp"
+#include "tg_surrogate.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -57,6 +58,15 @@ namespace tg
 		DropGraph();
 	}
 
+	void Batch::SetFields(const std::vector<const FieldNet*>& fields, bool refine)
+	{
+		Fields = fields;
+		Fields.resize(Programs.size(), nullptr);
+		FieldRefine = refine;
+		Planned = false;
+		DropGraph();
+	}
+
 	cudaError_t Batch::Plan(cudaStream_t s)
 	{
 		const int n = (int)Programs.size();
@@ -84,6 +94,7 @@ namespace tg
 			bm.Lattice = lat;
 			bm.BrickWord0 = bw0[m] = bword;
 			bm.CellWord0 = cword;
+			bm.Cull = (m < (int)Fields.size() && Fields[m]) ? (FieldRefine ? 2 : 1) : 0;
 			const int64_t sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
 			cw[m] = (sx * sy * sz + 31) / 32;
 			cb0[m] = (uint64_t)cword * 32u;
@@ -95,6 +106,7 @@ namespace tg
 			capV += 10.0 * (double)std::max({ sx * sy, sy * sz, sx * sz }) + 4096.0;
 			MaxStack = std::max(MaxStack, bm.Prog.MaxStack);
 		}
+		BrickWordHost = bw0;
 		if ((double)bword * 32.0 >= 4294967296.0) { SetError("batch too large: more than 2^32 bricks"); return cudaErrorInvalidValue; }
 		CapVertices = ReqVertices ? ReqVertices : (uint32_t)std::min(capV, 4.0e9 / 2.5);
 		CapFaces = ReqFaces ? ReqFaces : (uint32_t)std::min(2.5 * (double)CapVertices, 4.0e9);
@@ -181,6 +193,17 @@ namespace tg
 			TG_TRY(cudaMemsetAsync(Counters.Ptr, 0, 8 * 4, s));
 			TG_TRY(cudaMemsetAsync(Barrier.Ptr, 0, 8, s));
 			TG_TRY(cudaMemsetAsync(Status.Ptr, 0, 4, s));
+			// Models with a learned bound: its brick bits first, into the model's words.
+			for (size_t m = 0; m < Fields.size() && m < Programs.size(); ++m)
+			{
+				const FieldNet* f = Fields[m];
+				if (!f) continue;
+				const GridSpec& g = Grids[m];
+				const int B = Bricks[m];
+				const float radius = 0.8660254f * (float)B * g.Step;
+				TG_TRY(LaunchFieldClassifyBricks(Programs[m]->View, g, B, f->Grid, f->TablePtr(), f->ImagePtr(), f->MarginFor(radius),
+					BrickBits.As<uint32_t>() + BrickWordHost[m], f->StatusPtr(), s));
+			}
 			return LaunchBatchExport(State, Blocks, MaxStack, s);
 		};
 		if (!GraphExec && !Info.Graph)
@@ -230,6 +253,8 @@ namespace tg
 				SetError("the batch kernel's grid barrier timed out");
 				return cudaErrorLaunchTimeout;
 			}
+			for (const FieldNet* f : Fields)
+				if (f) TG_TRY(const_cast<FieldNet*>(f)->CheckStatus(s));
 			const uint32_t overflow = HostCounters[4];
 			if (!overflow) break;
 			// Outputs did not fit: grow to the counts this run found and run again.

@@ -32,6 +32,10 @@ namespace tg
 		// class for every candidate (brick edge, lanes) and gives each class its fastest.
 		cudaError_t Autotune(cudaStream_t s);
 		cudaError_t Run(cudaStream_t s);
+		// Learned distance bounds per model (null: exact test), which cull the model's bricks
+		// before the launch; with `refine` the bricks a bound keeps also take the exact test.
+		// The nets must outlive the batch's runs.  Invalidates the plan.
+		void SetFields(const std::vector<const FieldNet*>& fields, bool refine);
 		// Output capacities (vertices, faces) for the next run; a run that finds more grows
 		// them and runs again.
 		void Reserve(uint32_t vertices, uint32_t faces);
@@ -50,6 +54,8 @@ namespace tg
 
 		std::vector<const Program*> Programs;
 		std::vector<GridSpec> Grids;
+		std::vector<const FieldNet*> Fields;
+		bool FieldRefine = true;
 		bool Attributes;
 		bool Planned = false;
 		int MaxStack = 1, Blocks = 0;
@@ -60,6 +66,7 @@ namespace tg
 			ActiveCells, Lattice, Vertices, Normals, Colors, Cubes, FaceCounts, FaceBase, Faces, VertexBase, FaceBaseModel,
 			Counters, ScanPartials, Barrier, Status;
 		std::vector<uint32_t> HostVertexBase, HostFaceBase;
+		std::vector<int64_t> BrickWordHost;        // per model: first word of its brick bits
 		std::vector<int> HasPaint;
 		uint32_t* HostCounters = nullptr;
 		cudaGraph_t Graph = nullptr;

@@ -1088,6 +1088,15 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API tg_status tg_batch_set_surrogates(tg_batch* b, tg_surrogate* const* nets, int count, uint32_t flags)
+	{
+		if (!b || (count > 0 && !nets) || count < 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		std::vector<const FieldNet*> fields((size_t)count);
+		for (int m = 0; m < count; ++m) fields[(size_t)m] = nets[m];
+		b->SetFields(fields, (flags & TG_MESH_SURROGATE_ONLY) == 0);
+		return TG_OK;
+	}
+
 	TANGERINE_API tg_status tg_batch_get_tuning(const tg_batch* b, int* bricks, int* lanes)
 	{
 		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }

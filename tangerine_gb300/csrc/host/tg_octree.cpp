@@ -254,6 +254,9 @@ namespace tg
 		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
 		BuildLevels({ top.get() }, bp, 1);
+		// SDFOctree::Create returns nullptr when the root lost its evaluator while
+		// populating (every octant clipped away).
+		if (!top->Eval) return false;
 		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
 		return true;
@@ -276,6 +279,7 @@ namespace tg
 		InitCell(*top, root, first);
 		if (!top->Eval) return false;
 		BuildLevels({ top.get() }, first, 1);
+		if (!top->Eval) return false;
 		// Populate(false, 3, -1) of each incomplete cell: its children start at depth 4 and
 		// split without limit.  The cells are disjoint, so one level-parallel pass serves
 		// them all.

@@ -261,13 +261,20 @@ namespace tg
 			const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
 
 			// 1. Classify every brick of every model (a warp per bit word); clear the cell bits.
+			//    Models culled by a learned bound arrive with their bits set by it: those keep
+			//    them (Cull 1) or put the kept bricks through the exact test (Cull 2).
 			for (int64_t w = warp; w < s.BrickWordsTotal; w += warpsPerGrid)
 			{
 				const int mi = ModelOf(s.BrickWord0, s.Count, w);
 				const BatchModel& m = s.Models[mi];
 				const int64_t local = (w - m.BrickWord0) * 32 + lane;
 				bool active = false;
-				if (local < m.Bricks)
+				const bool candidate = m.Cull == 0 || ((s.BrickBits[w] >> lane) & 1u);
+				if (local < m.Bricks && candidate && m.Cull == 1)
+				{
+					active = true;
+				}
+				else if (local < m.Bricks && candidate)
 				{
 					const int bx = (int)(local % m.NBX), by = (int)((local / m.NBX) % m.NBY), bz = (int)(local / ((int64_t)m.NBX * m.NBY));
 					const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;

@@ -278,6 +278,9 @@ namespace tg
 		int64_t Lattice;           // first float of the model's lattice in the pool
 		int64_t BrickWord0;        // first word of its brick bits
 		int64_t CellWord0;         // first word of its cell bits
+		int Cull;                  // bricks kept by: 0 the exact test; 1 the model's learned bound
+		                           // (its bits written before the launch); 2 the bound, then
+		                           // the exact test on the bricks it keeps
 	};
 
 	struct BatchState

@@ -670,6 +670,13 @@ class Batch:
         check(load().tg_batch_get_tuning(self.ptr, _lib.as_ptr(b), _lib.as_ptr(l)), "tg_batch_get_tuning")
         return b, l
 
+    def set_surrogates(self, nets, only=False):
+        """Cull model m's bricks with nets[m] (a fitted Surrogate or None for the exact test);
+        with only=False the bricks a network keeps also take the exact test."""
+        arr = (C.c_void_p * max(1, len(nets)))(*[(n.ptr.value if n is not None else None) for n in nets])
+        self._nets = list(nets)       # the networks must outlive the runs
+        check(load().tg_batch_set_surrogates(self.ptr, arr, len(nets), (1 << 20) if only else 0), "tg_batch_set_surrogates")
+
     def run(self, stream=None):
         check(load().tg_batch_run(self.ptr, stream), "tg_batch_run")
 

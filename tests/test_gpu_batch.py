@@ -77,3 +77,41 @@ def test_batch_autotune(programs):
         b.run()
         for m in range(3):
             _same(b.mesh(m), progs[m].export_mesh(grids[m]))
+
+
+def test_batch_surrogate_form_same_meshes(programs):
+    """Learned bounds culling some models' bricks inside the batch (with and without the exact
+    test of the kept bricks, a model without a network in between): every mesh is still the
+    exact export's."""
+    progs, grids = programs
+    singles = [p.export_mesh(g) for p, g in zip(progs, grids)]
+    nets = []
+    for m, p in enumerate(progs):
+        if m in (1, 3, 5):
+            s = sdf.Surrogate(samples=1 << 20, steps=400, batch=1 << 16, validation=1 << 18)
+            s.fit(p)
+            nets.append(s)
+        else:
+            nets.append(None)
+    try:
+        with sdf.Batch(progs, grids) as b:
+            b.set_tuning(bricks=[7, 4, 7, 5, 3, 7, 2])
+            refined_bricks = None
+            for only in (False, True):
+                b.set_surrogates(nets, only=only)
+                b.run()
+                info = b.info()
+                for m, ref in enumerate(singles):
+                    _same(b.mesh(m), ref)
+                if not only:
+                    refined_bricks = info.bricks_evaluated
+            b.set_surrogates([None] * len(progs))
+            b.run()
+            # The exact test alone keeps at least what the network and the exact test keep.
+            assert b.info().bricks_evaluated >= refined_bricks
+            for m, ref in enumerate(singles):
+                _same(b.mesh(m), ref)
+    finally:
+        for s in nets:
+            if s is not None:
+                s.close()

@@ -180,3 +180,26 @@ def test_drawable_writer_matches_reference(lib, golden, tmp_path):
     for fmt in ("ply", "stl"):
         sdf.write_drawables(drawables, tmp_path / f"out.{fmt}", frames=w["frames"], fmt=fmt, scale=float(w["scale"]))
         assert (tmp_path / f"out.{fmt}").read_bytes() == w[f"{fmt}_bytes"].tobytes(), fmt
+
+
+def test_tree_whose_octants_all_clip_away_has_no_octree(lib, port):
+    """A tree whose root cube's eight octants all clip away leaves the root without an
+    evaluator: SDFOctree::Create returns nullptr, and so does the host build."""
+    spec = W.random_tree(100010, 8)
+    h = port.build(spec)
+    try:
+        assert port.octree(h) is None
+        # Sodapop's depth-limited first stage keeps the root's evaluator.
+        mo = port.meshing_octree(h)
+        want = port.octree_dump(mo)
+        port.octree_free(mo)
+    finally:
+        port.free(h)
+    t = sdf.from_spec(spec)
+    assert t.finite() and not sdf.has_export_octree(t)
+    assert t.debug_octree() is None
+    got = t.debug_octree(meshing=True)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+    a, b = C.c_double(), C.c_double()
+    assert lib.tg_debug_compile_seconds(t.handle, 0, C.byref(a), C.byref(b)) == 2   # TG_ERR_UNBOUNDED
