@@ -33,23 +33,30 @@ namespace tg
 			int NBX, NBY, NBZ;      // bricks per axis
 		};
 
+		// A CTA takes a tile of 8 x 4 x 4 bricks and each warp an 8 x 4 patch of it: the
+		// bricks of a warp are neighbours in space, so they mostly run the same holder
+		// program (a warp along a row of 32 bricks spans several octree cells and diverges).
+		// Kept bricks set their bit with atomicOr into the zeroed bit words.
+		constexpr int kTileX = 8, kTileY = 4, kTileZ = kClassifyThreads / (kTileX * kTileY);
+
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			uint32_t* __restrict__ brick_bits)
 		{
 			extern __shared__ float spill[];
-			const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
-			const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-			bool active = false;
-			if (b < nb)
+			const int tilesX = (bg.NBX + kTileX - 1) / kTileX, tilesY = (bg.NBY + kTileY - 1) / kTileY;
+			const int tile = (int)blockIdx.x;
+			const int bx = (tile % tilesX) * kTileX + (int)(threadIdx.x % kTileX);
+			const int by = ((tile / tilesX) % tilesY) * kTileY + (int)((threadIdx.x / kTileX) % kTileY);
+			const int bz = (tile / (tilesX * tilesY)) * kTileZ + (int)(threadIdx.x / (kTileX * kTileY));
+			if (bx >= bg.NBX || by >= bg.NBY || bz >= bg.NBZ) return;
+			const int sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
+			const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
+			if (BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, sx), j0, min(j0 + bg.B, sy), k0, min(k0 + bg.B, sz), spill + threadIdx.x,
+				kClassifyThreads))
 			{
-				const int bx = (int)(b % bg.NBX), by = (int)((b / bg.NBX) % bg.NBY), bz = (int)(b / ((int64_t)bg.NBX * bg.NBY));
-				const int sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
-				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
-				active = BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, sx), j0, min(j0 + bg.B, sy), k0, min(k0 + bg.B, sz),
-					spill + threadIdx.x, kClassifyThreads);
+				const int64_t b = bx + (int64_t)bg.NBX * (by + (int64_t)bg.NBY * bz);
+				atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
 			}
-			const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
-			if ((threadIdx.x & 31) == 0 && b < nb) brick_bits[b >> 5] = ballot;
 		}
 
 		// The exact test on a list of candidate bricks; survivors set their bit.
@@ -297,8 +304,10 @@ namespace tg
 		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 		const size_t smem = (size_t)depth * kClassifyThreads * sizeof(float);
 		if (smem > 48 * 1024) cudaFuncSetAttribute(ClassifyBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		ClassifyBricksKernel<<<(unsigned)((nb + kClassifyThreads - 1) / kClassifyThreads), kClassifyThreads, smem, stream>>>(
-			prog, g, bg, brick_bits);
+		cudaError_t e = cudaMemsetAsync(brick_bits, 0, (size_t)((nb + 31) / 32) * 4, stream);
+		if (e != cudaSuccess) return e;
+		const int64_t tiles = (int64_t)((bg.NBX + kTileX - 1) / kTileX) * ((bg.NBY + kTileY - 1) / kTileY) * ((bg.NBZ + kTileZ - 1) / kTileZ);
+		ClassifyBricksKernel<<<(unsigned)tiles, kClassifyThreads, smem, stream>>>(prog, g, bg, brick_bits);
 		return cudaGetLastError();
 	}
 
