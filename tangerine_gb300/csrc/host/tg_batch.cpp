@@ -71,7 +71,8 @@ namespace tg
 	{
 		const int n = (int)Programs.size();
 		std::vector<BatchModel> models((size_t)n);
-		std::vector<int64_t> bw0((size_t)n), cw((size_t)n);
+		std::vector<int64_t> bw0((size_t)n), cw((size_t)n), t0((size_t)n);
+		int64_t tiles = 0;
 		std::vector<uint64_t> cb0((size_t)n);
 		HasPaint.assign((size_t)n, 0);
 		int64_t bword = 0, cword = 0, lat = 0, bricks = 0, samples = 0;
@@ -95,6 +96,8 @@ namespace tg
 			bm.BrickWord0 = bw0[m] = bword;
 			bm.CellWord0 = cword;
 			bm.Cull = (m < (int)Fields.size() && Fields[m]) ? (FieldRefine ? 2 : 1) : 0;
+			t0[m] = tiles;
+			tiles += (int64_t)((bm.NBX + 7) / 8) * ((bm.NBY + 3) / 4) * bm.NBZ;
 			const int64_t sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
 			cw[m] = (sx * sy * sz + 31) / 32;
 			cb0[m] = (uint64_t)cword * 32u;
@@ -118,6 +121,7 @@ namespace tg
 		TG_TRY(BrickWord0.Reserve(8 * (size_t)n));
 		TG_TRY(CellBit0.Reserve(8 * (size_t)n));
 		TG_TRY(CellWords.Reserve(8 * (size_t)n));
+		TG_TRY(Tile0.Reserve(8 * (size_t)n));
 		TG_TRY(BrickBits.Reserve(4 * (size_t)bword));
 		TG_TRY(BrickWordBase.Reserve(4 * (size_t)bword));
 		TG_TRY(BrickList.Reserve(4 * (size_t)bword * 32));
@@ -137,6 +141,7 @@ namespace tg
 		TG_TRY(cudaMemcpyAsync(BrickWord0.Ptr, bw0.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s));
 		TG_TRY(cudaMemcpyAsync(CellBit0.Ptr, cb0.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s));
 		TG_TRY(cudaMemcpyAsync(CellWords.Ptr, cw.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+		TG_TRY(cudaMemcpyAsync(Tile0.Ptr, t0.data(), 8 * (size_t)n, cudaMemcpyHostToDevice, s));
 		TG_TRY(cudaStreamSynchronize(s));
 
 		State = BatchState{};
@@ -147,6 +152,8 @@ namespace tg
 		State.CellBit0 = CellBit0.As<uint64_t>();
 		State.CellWords = CellWords.As<int64_t>();
 		State.BrickWordsTotal = bword;
+		State.Tile0 = Tile0.As<int64_t>();
+		State.TilesTotal = tiles;
 		State.CellWordsTotal = cword;
 		State.BrickBits = BrickBits.As<uint32_t>();
 		State.BrickWordBase = BrickWordBase.As<uint32_t>();

@@ -260,16 +260,46 @@ namespace tg
 			const int64_t gthreads = (int64_t)gridDim.x * kThreads;
 			const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
 
-			// 1. Classify every brick of every model (a warp per bit word); clear the cell bits.
-			//    Models culled by a learned bound arrive with their bits set by it: those keep
-			//    them (Cull 1) or put the kept bricks through the exact test (Cull 2).
+			// 1. Classify every brick of every model; clear the cell bits.  Exact models go by
+			//    8 x 4 patches of neighbouring bricks (a warp each, bits set with atomicOr into
+			//    words zeroed first), which keeps a warp on one holder program.  Models culled
+			//    by a learned bound arrive with their bits set by it (a warp per bit word):
+			//    those keep them (Cull 1) or put the kept bricks through the exact test (Cull 2).
+			for (int64_t w = gtid; w < s.BrickWordsTotal; w += gthreads)
+			{
+				if (s.Models[ModelOf(s.BrickWord0, s.Count, w)].Cull == 0) s.BrickBits[w] = 0u;
+			}
+			for (int64_t w = gtid; w < s.CellWordsTotal; w += gthreads) s.CellBits[w] = 0u;
+			if (!GridSync(s)) return;
+			for (int64_t t = warp; t < s.TilesTotal; t += warpsPerGrid)
+			{
+				const int mi = ModelOf(s.Tile0, s.Count, t);
+				const BatchModel& m = s.Models[mi];
+				if (m.Cull != 0) continue;
+				const int64_t local = t - __ldg(s.Tile0 + mi);
+				const int tilesX = (m.NBX + 7) / 8, tilesY = (m.NBY + 3) / 4;
+				const int bx = (int)(local % tilesX) * 8 + (lane & 7);
+				const int by = (int)((local / tilesX) % tilesY) * 4 + (lane >> 3);
+				const int bz = (int)(local / ((int64_t)tilesX * tilesY));
+				if (bx < m.NBX && by < m.NBY)
+				{
+					const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;
+					if (BoxMayHoldSurface(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
+						k0, min(k0 + m.B, m.Grid.NZ - 1), spill + threadIdx.x, kThreads))
+					{
+						const int64_t b = bx + (int64_t)m.NBX * (by + (int64_t)m.NBY * bz);
+						atomicOr(s.BrickBits + m.BrickWord0 + (b >> 5), 1u << (b & 31));
+					}
+				}
+			}
 			for (int64_t w = warp; w < s.BrickWordsTotal; w += warpsPerGrid)
 			{
 				const int mi = ModelOf(s.BrickWord0, s.Count, w);
 				const BatchModel& m = s.Models[mi];
+				if (m.Cull == 0) continue;
 				const int64_t local = (w - m.BrickWord0) * 32 + lane;
 				bool active = false;
-				const bool candidate = m.Cull == 0 || ((s.BrickBits[w] >> lane) & 1u);
+				const bool candidate = ((s.BrickBits[w] >> lane) & 1u) != 0;
 				if (local < m.Bricks && candidate && m.Cull == 1)
 				{
 					active = true;
@@ -284,7 +314,6 @@ namespace tg
 				const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
 				if (lane == 0) s.BrickBits[w] = ballot;
 			}
-			for (int64_t w = gtid; w < s.CellWordsTotal; w += gthreads) s.CellBits[w] = 0u;
 			if (!GridSync(s)) return;
 
 			// 2. Kept bricks as a list in global brick order.

@@ -289,6 +289,8 @@ namespace tg
 		int Count;
 		int Attributes;
 		const int64_t* BrickWord0;     // per model, ascending
+		const int64_t* Tile0;          // per model, ascending: first 8 x 4 brick patch of its classification
+		int64_t TilesTotal;
 		const uint64_t* CellBit0;      // per model: CellWord0 * 32
 		const int64_t* CellWords;      // per model
 		int64_t BrickWordsTotal, CellWordsTotal;
