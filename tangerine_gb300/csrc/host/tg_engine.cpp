@@ -296,7 +296,8 @@ namespace tg
 		{
 			const int B = opt.BrickSize;
 			const int64_t nb = BrickCount(g, B);
-			TG_TRY(BrickBits.Reserve((size_t)((nb + 31) / 32) * 4));
+			const int64_t brickWords = (nb + 31) / 32;
+			TG_TRY(BrickBits.Reserve((size_t)brickWords * 4 * (opt.Field && opt.Refine ? 2 : 1)));
 			TG_TRY(BrickList.Reserve((size_t)nb * 4));
 			if (!PersistentBlocks)
 			{
@@ -317,12 +318,13 @@ namespace tg
 				End(s);
 				if (opt.Refine)
 				{
-					Begin("list_bricks", s);
-					TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
-					End(s);
+					// The exact test on the bricks the network kept, in the classifier's
+					// spatial tiles; survivors go to the second half of the bit buffer.
+					uint32_t* kept = bits + brickWords;
 					Begin("refine_bricks", s);
-					TG_TRY(LaunchRefineBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, bits, PersistentBlocks, s));
+					TG_TRY(LaunchClassifyBricks(p.View, g, B, kept, s, bits));
 					End(s);
+					bits = kept;
 				}
 			}
 			else

@@ -40,7 +40,7 @@ namespace tg
 		constexpr int kTileX = 8, kTileY = 4, kTileZ = kClassifyThreads / (kTileX * kTileY);
 
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			uint32_t* __restrict__ brick_bits)
+			const uint32_t* __restrict__ candidates, uint32_t* __restrict__ brick_bits)
 		{
 			extern __shared__ float spill[];
 			const int tilesX = (bg.NBX + kTileX - 1) / kTileX, tilesY = (bg.NBY + kTileY - 1) / kTileY;
@@ -49,31 +49,14 @@ namespace tg
 			const int by = ((tile / tilesX) % tilesY) * kTileY + (int)((threadIdx.x / kTileX) % kTileY);
 			const int bz = (tile / (tilesX * tilesY)) * kTileZ + (int)(threadIdx.x / (kTileX * kTileY));
 			if (bx >= bg.NBX || by >= bg.NBY || bz >= bg.NBZ) return;
+			const int64_t b = bx + (int64_t)bg.NBX * (by + (int64_t)bg.NBY * bz);
+			if (candidates && !((__ldg(candidates + (b >> 5)) >> (b & 31)) & 1u)) return;
 			const int sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
 			const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
 			if (BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, sx), j0, min(j0 + bg.B, sy), k0, min(k0 + bg.B, sz), spill + threadIdx.x,
 				kClassifyThreads))
 			{
-				const int64_t b = bx + (int64_t)bg.NBX * (by + (int64_t)bg.NBY * bz);
 				atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
-			}
-		}
-
-		// The exact test on a list of candidate bricks; survivors set their bit.
-		__global__ void __launch_bounds__(kClassifyThreads) RefineBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ brick_bits)
-		{
-			extern __shared__ float spill[];
-			const uint32_t n = *count;
-			for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-			{
-				const uint32_t b = __ldg(list + t);
-				const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
-				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
-				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
-				if (BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, g.NX - 1), j0, min(j0 + bg.B, g.NY - 1), k0, min(k0 + bg.B, g.NZ - 1),
-					spill + threadIdx.x, kClassifyThreads))
-					atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
 			}
 		}
 
@@ -296,7 +279,8 @@ namespace tg
 		return (int64_t)bg.NBX * bg.NBY * bg.NBZ;
 	}
 
-	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream)
+	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream,
+		const uint32_t* candidates)
 	{
 		const BrickGrid bg = MakeBrickGrid(g, B);
 		const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
@@ -307,21 +291,7 @@ namespace tg
 		cudaError_t e = cudaMemsetAsync(brick_bits, 0, (size_t)((nb + 31) / 32) * 4, stream);
 		if (e != cudaSuccess) return e;
 		const int64_t tiles = (int64_t)((bg.NBX + kTileX - 1) / kTileX) * ((bg.NBY + kTileY - 1) / kTileY) * ((bg.NBZ + kTileZ - 1) / kTileZ);
-		ClassifyBricksKernel<<<(unsigned)tiles, kClassifyThreads, smem, stream>>>(prog, g, bg, brick_bits);
-		return cudaGetLastError();
-	}
-
-	cudaError_t LaunchRefineBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* brick_bits, int grid_blocks, cudaStream_t stream)
-	{
-		const BrickGrid bg = MakeBrickGrid(g, B);
-		const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
-		cudaError_t e = cudaMemsetAsync(brick_bits, 0, (size_t)((nb + 31) / 32) * 4, stream);
-		if (e != cudaSuccess || nb <= 0) return e;
-		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-		const size_t smem = (size_t)depth * kClassifyThreads * sizeof(float);
-		if (smem > 48 * 1024) cudaFuncSetAttribute(RefineBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		RefineBricksKernel<<<grid_blocks, kClassifyThreads, smem, stream>>>(prog, g, bg, list, count, brick_bits);
+		ClassifyBricksKernel<<<(unsigned)tiles, kClassifyThreads, smem, stream>>>(prog, g, bg, candidates, brick_bits);
 		return cudaGetLastError();
 	}
 

@@ -67,10 +67,10 @@ namespace tg
 	// Exact brick culling (tg_cull.cu): bricks of B^3 cells that provably hold no sign
 	// change are skipped.  brick_bits: one bit per brick (set: may hold surface).
 	int64_t BrickCount(const GridSpec& g, int B);
-	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream);
-	// The exact test on listed candidate bricks: clears brick_bits, sets survivors' bits.
-	cudaError_t LaunchRefineBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* brick_bits, int grid_blocks, cudaStream_t stream);
+	// With `candidates` (bits of another classification, e.g. the learned bound's), only
+	// bricks set there are tested; the rest stay clear.
+	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream,
+		const uint32_t* candidates = nullptr);
 	// Set bits as a list in brick-index order (scan + compaction); *count (device) gets the
 	// length.  base: (bricks + 31) / 32 words; scratch: ScanScratchWords of that.
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
