@@ -353,14 +353,11 @@ def our_arm(args, rank, world, local_rank):
     from tangerine_gb300 import workloads as W
 
     torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from tangerine_gb300.replicas import Replicas
+    group = Replicas(world, rank)
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        group.barrier()
 
     spec = W.random_tree(SEED, PRIMS)
     grid = W.export_grid(resolution=RES)
@@ -406,10 +403,7 @@ def our_arm(args, rank, world, local_rank):
     bricks, active_bricks = sdf.last_export_stats()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(np.sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = group.max(total_ms)
     kernels = {}
     for name in ("classify_bricks", "list_bricks", "eval_bricks", "cell_flags", "scan", "cell_vertices", "faces", "attributes"):
         ms, n = sdf.profile_read(name)
@@ -466,10 +460,7 @@ def our_arm(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
         e2e_s = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = group.max(e2e_s)
         prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
         d2h = nv * (12 + 12 + 4 + (3 if has_colors else 0)) + nf * 12
         phases = sdf.last_export_timing()
@@ -547,8 +538,7 @@ def our_arm(args, rank, world, local_rank):
         }
         print(json.dumps(line), flush=True)
     prog.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    group.close()
 
 
 def render_arm(args, rank, world, local_rank):
