@@ -64,6 +64,30 @@ namespace
 		g.nz = (int64_t)std::ceil(ext.z) + 1;
 	}
 
+	// An export run with ExportOptions::Host: its host blocks become the tg_mesh.
+	tg_status TakeHostMesh(cudaError_t e, HostMeshOut& h, tg_mesh* out, const char* what)
+	{
+		std::memset(out, 0, sizeof *out);
+		if (e != cudaSuccess)
+		{
+			FreeHostMesh(h);
+			return CudaFail(e, what);
+		}
+		if (h.OutOfMemory)
+		{
+			SetError("out of host memory for the mesh");
+			return TG_ERR_MEMORY;
+		}
+		out->vertex_count = h.VertexCount;
+		out->face_count = h.FaceCount;
+		out->vertices = h.Vertices;
+		out->normals = h.Normals;
+		out->colors = h.Colors;
+		out->faces = h.Faces;
+		out->cubes = h.Cubes;
+		return TG_OK;
+	}
+
 	tg_status CopyMeshToHost(const DeviceMesh& dm, tg_mesh* out, cudaStream_t s)
 	{
 		std::memset(out, 0, sizeof *out);
@@ -414,9 +438,11 @@ extern "C"
 		const cudaStream_t s = StreamOf(stream);
 		DeviceMesh dm;
 		if (((flags >> 8) & 0xFFu) > 32) { SetError("brick size must be 1..32 cells"); return TG_ERR_INVALID; }
-		cudaError_t e = eng.Export(*p, gs, OptionsOf(flags), dm, s);
-		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
-		return CopyMeshToHost(dm, out, s);
+		ExportOptions opt = OptionsOf(flags);
+		HostMeshOut host;
+		opt.Host = &host;
+		const cudaError_t e = eng.Export(*p, gs, opt, dm, s);
+		return TakeHostMesh(e, host, out, "exporting the mesh");
 	}
 
 	TANGERINE_API void tg_mesh_free(tg_mesh* m)
@@ -461,10 +487,12 @@ extern "C"
 		if (ue != cudaSuccess) return CudaFail(ue, "uploading the program");
 		const auto t1 = clock();
 		DeviceMesh dm;
-		cudaError_t e = eng.Export(*prog, gs, OptionsOf(TG_MESH_ATTRIBUTES), dm, s);
-		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
+		ExportOptions opt = OptionsOf(TG_MESH_ATTRIBUTES);
+		HostMeshOut host;
+		opt.Host = &host;
+		const cudaError_t e = eng.Export(*prog, gs, opt, dm, s);
 		const auto t2 = clock();
-		st = CopyMeshToHost(dm, out, s);
+		st = TakeHostMesh(e, host, out, "exporting the mesh");
 		const auto t3 = clock();
 		tm.CompileSeconds = prog->Host.BuildSeconds;
 		tm.UploadSeconds = secs(t0, t1) - prog->Host.BuildSeconds;
@@ -1397,10 +1425,17 @@ extern "C"
 		opt.Field = sur;
 		opt.Refine = (flags & TG_MESH_SURROGATE_ONLY) == 0;
 		DeviceMesh dm;
+		HostMeshOut host;
+		opt.Host = &host;
 		cudaError_t e = eng.Export(*p, gs, opt, dm, s);
-		if (e == cudaErrorLaunchTimeout) { SetError("a tensor-core wait timed out in the surrogate kernels"); return TG_ERR_CUDA; }
-		if (e != cudaSuccess) return CudaFail(e, "exporting the mesh");
-		return CopyMeshToHost(dm, out, s);
+		if (e == cudaErrorLaunchTimeout)
+		{
+			FreeHostMesh(host);
+			std::memset(out, 0, sizeof *out);
+			SetError("a tensor-core wait timed out in the surrogate kernels");
+			return TG_ERR_CUDA;
+		}
+		return TakeHostMesh(e, host, out, "exporting the mesh");
 	}
 
 	TANGERINE_API tg_status tg_debug_mma(int mode, const float* a, const float* b, float* d)

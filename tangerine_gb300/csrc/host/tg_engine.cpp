@@ -2,6 +2,7 @@
 #include "tg_engine.hpp"
 #include "tg_surrogate.hpp"
 
+#include <cstdlib>
 #include <cstring>
 
 namespace tg
@@ -394,6 +395,48 @@ namespace tg
 		out.Vertices = Vertices.As<float>();
 		out.Cubes = Cubes.As<uint32_t>();
 		out.Faces = Faces.As<uint32_t>();
+		HostMeshOut* host = opt.Host;
+		bool early = false;
+		if (host)
+		{
+			// Host blocks now that the counts are known; vertices, cubes and faces travel on
+			// the copy stream while the attribute pass runs.
+			*host = HostMeshOut();
+			host->VertexCount = vcount;
+			host->FaceCount = fcount;
+			const size_t v = vcount ? vcount : 1, f = fcount ? fcount : 1;
+			auto take = [](size_t bytes) -> void*
+			{
+				void* b = HostPool::Get().Take(bytes);
+				return b ? b : std::malloc(bytes);
+			};
+			host->Vertices = (float*)take(v * 12);
+			host->Normals = (float*)take(v * 12);
+			host->Faces = (uint32_t*)take(f * 12);
+			host->Cubes = (uint32_t*)take(v * 4);
+			if (opt.Attributes && p.Host.Header.HasPaint) host->Colors = (uint8_t*)take(v * 3);
+			if (!host->Vertices || !host->Normals || !host->Faces || !host->Cubes ||
+				(opt.Attributes && p.Host.Header.HasPaint && !host->Colors))
+			{
+				FreeHostMesh(*host);
+				host->OutOfMemory = true;
+				host = nullptr;
+			}
+			else
+			{
+				if (!CopyStream) TG_TRY(cudaStreamCreateWithFlags(&CopyStream, cudaStreamNonBlocking));
+				if (!MeshReady) TG_TRY(cudaEventCreateWithFlags(&MeshReady, cudaEventDisableTiming));
+				TG_TRY(cudaEventRecord(MeshReady, s));
+				TG_TRY(cudaStreamWaitEvent(CopyStream, MeshReady, 0));
+				if (vcount)
+				{
+					TG_TRY(cudaMemcpyAsync(host->Vertices, Vertices.Ptr, (size_t)vcount * 12, cudaMemcpyDeviceToHost, CopyStream));
+					TG_TRY(cudaMemcpyAsync(host->Cubes, Cubes.Ptr, (size_t)vcount * 4, cudaMemcpyDeviceToHost, CopyStream));
+				}
+				if (fcount) TG_TRY(cudaMemcpyAsync(host->Faces, Faces.Ptr, (size_t)fcount * 12, cudaMemcpyDeviceToHost, CopyStream));
+				early = true;
+			}
+		}
 		if (opt.Attributes)
 		{
 			TG_TRY(Normals.Reserve((size_t)vcount * 12));
@@ -408,11 +451,31 @@ namespace tg
 			End(s);
 			out.Normals = Normals.As<float>();
 			out.Colors = colors;
+			if (early && vcount)
+			{
+				TG_TRY(cudaMemcpyAsync(host->Normals, Normals.Ptr, (size_t)vcount * 12, cudaMemcpyDeviceToHost, s));
+				if (colors) TG_TRY(cudaMemcpyAsync(host->Colors, colors, (size_t)vcount * 3, cudaMemcpyDeviceToHost, s));
+			}
+		}
+		else if (early)
+		{
+			std::memset(host->Normals, 0, (size_t)(vcount ? vcount : 1) * 12);
 		}
 		TG_TRY(cudaStreamSynchronize(s));
+		if (early) TG_TRY(cudaStreamSynchronize(CopyStream));
 		Collect();
 		if (opt.Field) TG_TRY(const_cast<FieldNet*>(opt.Field)->CheckStatus(s));
 		return cudaSuccess;
+	}
+
+	void FreeHostMesh(HostMeshOut& m)
+	{
+		void* blocks[5] = { m.Vertices, m.Normals, m.Colors, m.Faces, m.Cubes };
+		for (void* b : blocks)
+		{
+			if (b && !HostPool::Get().Give(b)) std::free(b);
+		}
+		m = HostMeshOut();
 	}
 
 	cudaError_t Engine::LastBrickList(std::vector<uint32_t>& out, int& brick_size)

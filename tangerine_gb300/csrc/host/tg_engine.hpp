@@ -48,6 +48,21 @@ namespace tg
 		uint32_t* Cubes = nullptr;
 	};
 
+	// Host blocks an export fills itself (allocated from the pinned pool once the counts are
+	// known): the vertices, cubes and faces are copied on a second stream while the normals
+	// and colours are still being computed.
+	struct HostMeshOut
+	{
+		uint64_t VertexCount = 0, FaceCount = 0;
+		float* Vertices = nullptr;
+		float* Normals = nullptr;
+		uint8_t* Colors = nullptr;
+		uint32_t* Faces = nullptr;
+		uint32_t* Cubes = nullptr;
+		bool OutOfMemory = false;
+	};
+	void FreeHostMesh(HostMeshOut& m);
+
 	struct ExportOptions
 	{
 		bool Attributes = true;     // gradient normals and colours
@@ -56,6 +71,7 @@ namespace tg
 		int Lanes = 2;              // lattice points per thread sharing one pass over records
 		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
 		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
+		HostMeshOut* Host = nullptr;        // also copy the mesh to host memory (see HostMeshOut)
 	};
 
 	// Sodapop's meshing job output (device pointers into the engine's buffers, valid until
@@ -145,6 +161,8 @@ namespace tg
 		std::vector<Total> Totals;
 
 		cudaStream_t Stream = nullptr;
+		cudaStream_t CopyStream = nullptr;          // early device-to-host copies of an export
+		cudaEvent_t MeshReady = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
 		DeviceBuffer Points, PointOut, BrickBits, BrickList, ProgramScratch, ActiveCells;
 		DeviceBuffer RayIn, RayOut, Cameras, Image, RenderCounters;
