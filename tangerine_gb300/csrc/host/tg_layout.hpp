@@ -26,6 +26,8 @@ namespace tg
 		RecLhsPaint = 1u << 11,     // surface set op: left operand has paint
 		RecRhsPaint = 1u << 12,     // surface set op: right operand has paint
 		RecNegative = 1u << 13,     // surface stencil: override applies inside the mask
+		RecThenSet = 1u << 14,      // distance brush: the next record is the set operator whose
+		                            // right operand this brush is (applied in the same step)
 	};
 
 	// Extra opcodes used only by surface programs.

@@ -514,8 +514,10 @@ namespace tg
 					sp = &Spans[(size_t)r];
 				}
 				const float* from = arena + (surface ? sp->SurfaceAt : sp->DistanceAt);
+				if (!surface) LastBrushAt = Code.size();
 				Code.insert(Code.end(), from, from + (surface ? sp->SurfaceFloats : sp->DistanceFloats));
 			}
+			size_t LastBrushAt = 0;     // float index of the last distance brush record's head
 
 			int Records(const Node& n)
 			{
@@ -587,6 +589,10 @@ namespace tg
 				case NodeKind::Set:
 					Distance(*n.Lhs);
 					Distance(*n.Rhs);
+					// A brush right operand (the usual case: the tree leans left) is combined
+					// with the left operand in the brush's own step, without a stack push.
+					if (n.Rhs->Kind == NodeKind::Brush)
+						Code[LastBrushAt] = BitsFloat(FloatBits(Code[LastBrushAt]) | RecThenSet);
 					Quad(n.Op, IsBlendOp(n.Op) ? n.Threshold : 0.0f, 0.0f, 0.0f);
 					break;
 				case NodeKind::Flate:

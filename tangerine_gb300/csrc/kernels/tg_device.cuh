@@ -101,12 +101,21 @@ namespace tg
 			const uint32_t op = head & 0xFFu;
 			if (op >= OpSphere && op <= OpPlane)
 			{
-				if (depth > 0)
-				{
+				// RecThenSet: the set operator after this brush takes the current accumulator as
+				// its left operand, so nothing is pushed (same operations, same order).
+				const bool thenSet = (head & RecThenSet) != 0;
+				float left[K];
 #pragma unroll
-					for (int k = 0; k < K; ++k) spill[((depth - 1) * K + k) * stride] = acc[k];
+				for (int k = 0; k < K; ++k) left[k] = acc[k];
+				if (!thenSet)
+				{
+					if (depth > 0)
+					{
+#pragma unroll
+						for (int k = 0; k < K; ++k) spill[((depth - 1) * K + k) * stride] = acc[k];
+					}
+					++depth;
 				}
-				++depth;
 				float qx[K], qy[K], qz[K];
 				if (head & RecMatrix)
 				{
@@ -161,6 +170,13 @@ namespace tg
 					const float4 S = LoadQuad(code, pc++);
 #pragma unroll
 					for (int k = 0; k < K; ++k) acc[k] = acc[k] * S.x;
+				}
+				if (thenSet)
+				{
+					const float4 T = LoadQuad(code, pc++);
+					const uint32_t setOp = __float_as_uint(T.x) & 0xFFu;
+#pragma unroll
+					for (int k = 0; k < K; ++k) acc[k] = SetDistance(setOp, left[k], acc[k], T.y);
 				}
 			}
 			else if (op >= OpUnion && op <= OpBlendDiff)
