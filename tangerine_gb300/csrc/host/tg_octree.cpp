@@ -514,10 +514,11 @@ namespace tg
 					sp = &Spans[(size_t)r];
 				}
 				const float* from = arena + (surface ? sp->SurfaceAt : sp->DistanceAt);
-				if (!surface) LastBrushAt = Code.size();
+				(surface ? LastSurfaceBrushAt : LastBrushAt) = Code.size();
 				Code.insert(Code.end(), from, from + (surface ? sp->SurfaceFloats : sp->DistanceFloats));
 			}
-			size_t LastBrushAt = 0;     // float index of the last distance brush record's head
+			size_t LastBrushAt = 0;         // float index of the last distance brush record's head
+			size_t LastSurfaceBrushAt = 0;  // and of the last surface brush record's
 
 			int Records(const Node& n)
 			{
@@ -620,6 +621,8 @@ namespace tg
 					uint32_t flags = 0;
 					if (HasPaint(*n.Lhs)) flags |= RecLhsPaint;
 					if (HasPaint(*n.Rhs)) flags |= RecRhsPaint;
+					if (n.Rhs->Kind == NodeKind::Brush)
+						Code[LastSurfaceBrushAt] = BitsFloat(FloatBits(Code[LastSurfaceBrushAt]) | RecThenSet);
 					Quad(n.Op | flags, n.Threshold, 0.0f, 0.0f);
 					break;
 				}

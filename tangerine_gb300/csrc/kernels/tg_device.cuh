@@ -302,15 +302,56 @@ namespace tg
 			const float4 h = LoadQuad(code, pc++);
 			const uint32_t head = __float_as_uint(h.x);
 			const uint32_t op = head & 0xFFu;
+			// SetNode::Eval and SetNode::GetMaterial (sdf_evaluator.cpp:774-780, 957-1012) on the
+			// left operands l[] (material ml) and the accumulator (the right operands).
+			auto applySet = [&](uint32_t setHead, float k0, const float (&l)[K], int ml)
+			{
+				const uint32_t setOp = setHead & 0xFFu;
+				float lm = 0.0f, rm = 0.0f, dm = 0.0f;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					const float d = SetDistance(setOp, l[k], acc[k], k0);
+					if (k == mat_lane) { lm = l[k]; rm = acc[k]; dm = d; }
+					acc[k] = d;
+				}
+				if (withMaterial)
+				{
+					const int mr = macc;
+					if (setOp == OpDiff || setOp == OpBlendDiff) macc = ml;
+					else
+					{
+						const bool blend = (setOp == OpBlendUnion || setOp == OpBlendInter);
+						const bool takeLeft = blend ? (fabsf(lm - dm) <= fabsf(rm - dm)) : (dm == lm);
+						if (setOp == OpUnion || setOp == OpBlendUnion) macc = takeLeft ? ml : mr;
+						else
+						{
+							const bool lv = (setHead & RecLhsPaint) != 0, rv = (setHead & RecRhsPaint) != 0;
+							if (lv && rv) macc = takeLeft ? ml : mr;
+							else macc = lv ? ml : mr;
+						}
+					}
+				}
+			};
 			if (op >= OpSphere && op <= OpPlane)
 			{
-				if (depth > 0)
-				{
+				// RecThenSet: the set operator after this brush takes the current accumulator
+				// (and material) as its left operand, so nothing is pushed.
+				const bool thenSet = (head & RecThenSet) != 0;
+				float left[K];
 #pragma unroll
-					for (int k = 0; k < K; ++k) slot(depth - 1, k) = acc[k];
-					slot(depth - 1, K) = __int_as_float(macc);
+				for (int k = 0; k < K; ++k) left[k] = acc[k];
+				const int leftMaterial = macc;
+				if (!thenSet)
+				{
+					if (depth > 0)
+					{
+#pragma unroll
+						for (int k = 0; k < K; ++k) slot(depth - 1, k) = acc[k];
+						slot(depth - 1, K) = __int_as_float(macc);
+					}
+					++depth;
 				}
-				++depth;
 				const float4 Q = LoadQuad(code, pc);
 				const float4 T = LoadQuad(code, pc + 1);
 				const float4 M = LoadQuad(code, pc + 2);
@@ -326,38 +367,19 @@ namespace tg
 					acc[k] = BrushDistance(op, prm, local) * T.w;
 				}
 				macc = __float_as_int(M.x);
+				if (thenSet)
+				{
+					const float4 S = LoadQuad(code, pc++);
+					applySet(__float_as_uint(S.x), S.y, left, leftMaterial);
+				}
 			}
 			else if (op >= OpUnion && op <= OpBlendDiff)
 			{
 				--depth;
-				float lm = 0.0f, rm = 0.0f, dm = 0.0f;
+				float l[K];
 #pragma unroll
-				for (int k = 0; k < K; ++k)
-				{
-					const float l = slot(depth - 1, k);
-					const float d = SetDistance(op, l, acc[k], h.y);
-					if (k == mat_lane) { lm = l; rm = acc[k]; dm = d; }
-					acc[k] = d;
-				}
-				if (withMaterial)
-				{
-					// SetNode::GetMaterial (sdf_evaluator.cpp:957-1012).
-					const int ml = __float_as_int(slot(depth - 1, K));
-					const int mr = macc;
-					if (op == OpDiff || op == OpBlendDiff) macc = ml;
-					else
-					{
-						const bool blend = (op == OpBlendUnion || op == OpBlendInter);
-						const bool takeLeft = blend ? (fabsf(lm - dm) <= fabsf(rm - dm)) : (dm == lm);
-						if (op == OpUnion || op == OpBlendUnion) macc = takeLeft ? ml : mr;
-						else
-						{
-							const bool lv = (head & RecLhsPaint) != 0, rv = (head & RecRhsPaint) != 0;
-							if (lv && rv) macc = takeLeft ? ml : mr;
-							else macc = lv ? ml : mr;
-						}
-					}
-				}
+				for (int k = 0; k < K; ++k) l[k] = slot(depth - 1, k);
+				applySet(head, h.y, l, withMaterial ? __float_as_int(slot(depth - 1, K)) : -1);
 			}
 			else if (op == OpFlate)
 			{
