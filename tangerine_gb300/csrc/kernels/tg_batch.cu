@@ -226,7 +226,7 @@ namespace tg
 					for (int k = 0; k < K; ++k)
 						if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
 					float r[K];
-					RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kThreads);
+					RunDistance<K, false>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kThreads);
 #pragma unroll
 					for (int k = 0; k < K; ++k)
 					{
@@ -284,7 +284,7 @@ namespace tg
 				if (bx < m.NBX && by < m.NBY)
 				{
 					const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;
-					if (BoxMayHoldSurface(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
+					if (BoxMayHoldSurface<false>(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
 						k0, min(k0 + m.B, m.Grid.NZ - 1), spill + threadIdx.x, kThreads))
 					{
 						const int64_t b = bx + (int64_t)m.NBX * (by + (int64_t)m.NBY * bz);
@@ -308,7 +308,7 @@ namespace tg
 				{
 					const int bx = (int)(local % m.NBX), by = (int)((local / m.NBX) % m.NBY), bz = (int)(local / ((int64_t)m.NBX * m.NBY));
 					const int i0 = bx * m.B, j0 = by * m.B, k0 = bz * m.B;
-					active = BoxMayHoldSurface(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
+					active = BoxMayHoldSurface<false>(m.Prog, m.Grid, i0, min(i0 + m.B, m.Grid.NX - 1), j0, min(j0 + m.B, m.Grid.NY - 1),
 						k0, min(k0 + m.B, m.Grid.NZ - 1), spill + threadIdx.x, kThreads);
 				}
 				const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
@@ -492,7 +492,7 @@ namespace tg
 						const float px[1] = { q.x }, py[1] = { q.y }, pz[1] = { q.z };
 						float e[1];
 						int mat = -1;
-						RunSurfaceBatch<1>(m.Prog.Code, pc, px, py, pz, e, (elane == 4 && m.HasPaint) ? 0 : -1, &mat, spill + threadIdx.x, kThreads);
+						RunSurfaceBatch<1, false>(m.Prog.Code, pc, px, py, pz, e, (elane == 4 && m.HasPaint) ? 0 : -1, &mat, spill + threadIdx.x, kThreads);
 						evals[threadIdx.x] = e[0];
 						if (elane == 4) mats[localPoint] = mat;
 					}

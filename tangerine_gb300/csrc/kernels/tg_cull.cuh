@@ -9,6 +9,7 @@ namespace tg
 {
 	// Whether the lattice box [i0, i1] x [j0, j1] x [k0, k1] (corner indices) may hold a
 	// sign change of the reference's distances; false only when that is proven.
+	template<bool FuseSet = true>
 	__device__ __forceinline__ bool BoxMayHoldSurface(const DeviceProgram& prog, const GridSpec& g,
 		int i0, int i1, int j0, int j1, int k0, int k1, float* spill, int stride)
 	{
@@ -74,7 +75,7 @@ namespace tg
 		if (holder < 0) return true;
 		const float px[1] = { cx }, py[1] = { cy }, pz[1] = { cz };
 		float f[1];
-		RunDistance<1>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill, stride);
+		RunDistance<1, FuseSet>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill, stride);
 		return !(fabsf(f[0]) > r + margin);
 	}
 }

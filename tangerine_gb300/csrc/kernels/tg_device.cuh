@@ -85,7 +85,9 @@ namespace tg
 	// Runs a distance program for K points at once (one record stream, K accumulators).
 	// `spill` is this thread's column of the operand stack in shared memory: entry
 	// (depth, lane) lives at spill[(depth * K + lane) * stride].
-	template<int K>
+	// FuseSet = false ignores RecThenSet (the set record is then taken as its own step, with
+	// the same result) for kernels whose register budget cannot hold the fused step.
+	template<int K, bool FuseSet = true>
 	__device__ __forceinline__ void RunDistance(const float4* __restrict__ code, int pc,
 		const float (&px)[K], const float (&py)[K], const float (&pz)[K], float (&out)[K],
 		float* spill, int stride)
@@ -103,7 +105,7 @@ namespace tg
 			{
 				// RecThenSet: the set operator after this brush takes the current accumulator as
 				// its left operand, so nothing is pushed (same operations, same order).
-				const bool thenSet = (head & RecThenSet) != 0;
+				const bool thenSet = FuseSet && (head & RecThenSet) != 0;
 				float left[K];
 #pragma unroll
 				for (int k = 0; k < K; ++k) left[k] = acc[k];
@@ -285,7 +287,7 @@ namespace tg
 	// to *material_out.  Operands below the top of the stack spill to shared memory:
 	// distance (depth, lane) at spill[(depth * (K + 1) + lane) * stride] and the material
 	// lane's material index at spill[(depth * (K + 1) + K) * stride].
-	template<int K>
+	template<int K, bool FuseSet = true>
 	__device__ __forceinline__ void RunSurfaceBatch(const float4* __restrict__ code, int pc,
 		const float (&px)[K], const float (&py)[K], const float (&pz)[K], float (&out)[K],
 		int mat_lane, int* material_out, float* spill, int stride)
@@ -337,7 +339,7 @@ namespace tg
 			{
 				// RecThenSet: the set operator after this brush takes the current accumulator
 				// (and material) as its left operand, so nothing is pushed.
-				const bool thenSet = (head & RecThenSet) != 0;
+				const bool thenSet = FuseSet && (head & RecThenSet) != 0;
 				float left[K];
 #pragma unroll
 				for (int k = 0; k < K; ++k) left[k] = acc[k];
