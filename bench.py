@@ -297,7 +297,7 @@ def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_
     """Trains the network on the program, then times the culled export with it deciding
     which bricks to skip: alone, and with the exact test on the bricks it keeps."""
     import torch
-    from tangerine_gb300 import sdf
+    from tangerine_gb300 import _lib, sdf
     sur = sdf.Surrogate()
     info = sur.fit(prog)
     exact_mesh = prog.export_mesh(grid, brick=brick)
@@ -330,15 +330,30 @@ def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_
     best_mode = max(out["modes"], key=lambda k: out["modes"][k]["value"])
     out["value"] = out["modes"][best_mode]["value"]
     out["unit"] = "samples/s"
-    # End to end through the C ABI: tg_export_mesh_surrogate, mesh copied to host memory.
+    # End to end through the C ABI: tg_export_mesh_surrogate fills a tg_mesh in host memory,
+    # which the caller releases with tg_mesh_free.
     only = best_mode == "network alone"
-    reps = 3
+    lib = _lib.load()
+    g = sdf._grid(grid)
+    flags = sdf._flags(True, False, brick, 0, only)
+
+    def c_export():
+        hm = _lib.HostMesh()
+        _lib.check(lib.tg_export_mesh_surrogate(prog.ptr, sur.ptr, _lib.C.byref(g), flags, _lib.C.byref(hm),
+                                                _lib.C.c_void_p(sp)), "tg_export_mesh_surrogate")
+        nv, nf = int(hm.vertex_count), int(hm.face_count)
+        nbytes = nv * (12 + 12 + 4 + (3 if hm.colors else 0)) + nf * 12
+        lib.tg_mesh_free(_lib.C.byref(hm))
+        return nbytes
+
+    reps = max(3, min(args.steps, 10))
+    c_export()     # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
-        m = sur.export_mesh(prog, grid, brick=brick, only=only, stream=sp)
+        d2h = c_export()
+    torch.cuda.synchronize()
     secs = time.perf_counter() - t0
-    d2h = m.vertices.nbytes + m.normals.nbytes + m.faces.nbytes + m.cubes.nbytes + (m.colors.nbytes if m.colors is not None else 0)
     out["e2e"] = {"value": world * samples * reps / secs, "unit": "samples/s", "h2d_bytes_per_step": 0,
                   "d2h_bytes_per_step": int(d2h), "call": f"tg_export_mesh_surrogate ({best_mode}), host mesh out"}
     sur.close()

@@ -1,6 +1,7 @@
 #include "tg_pool.hpp"
 
 #include <algorithm>
+#include <chrono>
 
 namespace tg
 {
@@ -21,20 +22,29 @@ namespace tg
 	{
 		{
 			std::lock_guard<std::mutex> lock(M);
-			Stop = true;
+			Stop.store(true);
 		}
 		Wake.notify_all();
 		for (auto& t : Threads) t.join();
 	}
 
-	void WorkerPool::Drain()
+	void WorkerPool::Drain(Job& job)
 	{
+		int done = 0;
 		for (;;)
 		{
-			const int i = Next.fetch_add(1, std::memory_order_relaxed);
-			if (i >= Count) return;
-			(*Body)(i);
+			const int i = job.Next.fetch_add(1, std::memory_order_relaxed);
+			if (i >= job.Count) break;
+			(*job.Body)(i);
+			++done;
 		}
+		if (done) job.Finished.fetch_add(done, std::memory_order_acq_rel);
+	}
+
+	namespace
+	{
+		// How long a worker polls for the next loop before it sleeps.
+		constexpr auto kPollFor = std::chrono::microseconds(300);
 	}
 
 	void WorkerPool::Run()
@@ -42,17 +52,23 @@ namespace tg
 		uint64_t seen = 0;
 		for (;;)
 		{
+			if (Generation.load(std::memory_order_acquire) == seen)
+			{
+				const auto until = std::chrono::steady_clock::now() + kPollFor;
+				for (int n = 1; Generation.load(std::memory_order_acquire) == seen && !Stop.load(std::memory_order_relaxed); ++n)
+				{
+					if ((n & 255) == 0 && std::chrono::steady_clock::now() > until) break;
+				}
+			}
+			std::shared_ptr<Job> job;
 			{
 				std::unique_lock<std::mutex> lock(M);
-				Wake.wait(lock, [&]() { return Stop || Generation != seen; });
-				if (Stop) return;
-				seen = Generation;
+				Wake.wait(lock, [&]() { return Stop.load() || Generation.load() != seen; });
+				if (Stop.load()) return;
+				seen = Generation.load();
+				job = Current;
 			}
-			Drain();
-			{
-				std::lock_guard<std::mutex> lock(M);
-				if (--Active == 0) Done.notify_all();
-			}
+			if (job) Drain(*job);
 		}
 	}
 
@@ -65,18 +81,20 @@ namespace tg
 			for (int i = 0; i < count; ++i) body(i);
 			return;
 		}
+		auto job = std::make_shared<Job>();
+		job->Body = &body;
+		job->Count = count;
 		{
 			std::lock_guard<std::mutex> lock(M);
-			Body = &body;
-			Count = count;
-			Next.store(0, std::memory_order_relaxed);
-			Active = (int)Threads.size();
-			++Generation;
+			Current = job;
+			Generation.fetch_add(1, std::memory_order_release);
 		}
 		Wake.notify_all();
-		Drain();
-		std::unique_lock<std::mutex> lock(M);
-		Done.wait(lock, [&]() { return Active == 0; });
-		Body = nullptr;
+		Drain(*job);
+		// The indices other threads claimed: once they are done nothing calls `body` again
+		// (a late worker finds Next past Count).
+		while (job->Finished.load(std::memory_order_acquire) != count) std::this_thread::yield();
+		std::lock_guard<std::mutex> lock(M);
+		if (Current == job) Current.reset();
 	}
 }

@@ -1,12 +1,20 @@
 // A process-wide pool of worker threads for the host side of compilation (the export
-// octree's clips).  Threads are created once; ParallelFor hands out loop indices through
-// one atomic counter and the calling thread works too.  One loop runs on the pool at a
-// time: a caller that finds it busy runs its loop alone.
+// octree's clips, the program emission).  Threads are created once; ParallelFor hands out
+// loop indices through one atomic counter and the calling thread works too.  One loop runs
+// on the pool at a time: a caller that finds it busy runs its loop alone.
+//
+// A compile runs several loops back to back (one per octree level, then the programs), so
+// waking threads must not sit on the critical path.  The caller waits for the indices to
+// be done, not for every worker to have woken: each loop is a shared job object, and a
+// worker that wakes after its loop ended finds the job's counter exhausted and touches
+// nothing of the caller's.  A worker that finishes a loop polls for the next one for a
+// short while before it sleeps.
 #pragma once
 
 #include <atomic>
 #include <condition_variable>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -22,19 +30,24 @@ namespace tg
 		~WorkerPool();
 
 	private:
+		struct Job
+		{
+			const std::function<void(int)>* Body = nullptr;
+			int Count = 0;
+			std::atomic<int> Next{ 0 };
+			std::atomic<int> Finished{ 0 };
+		};
+
 		WorkerPool();
 		void Run();
-		void Drain();
+		static void Drain(Job& job);
 
 		std::vector<std::thread> Threads;
 		std::mutex Busy;                    // held by the thread whose loop is running
-		std::mutex M;
-		std::condition_variable Wake, Done;
-		const std::function<void(int)>* Body = nullptr;
-		std::atomic<int> Next{ 0 };
-		int Count = 0;
-		int Active = 0;
-		uint64_t Generation = 0;
-		bool Stop = false;
+		std::mutex M;                       // guards Current and sleeping on Wake
+		std::condition_variable Wake;
+		std::shared_ptr<Job> Current;
+		std::atomic<uint64_t> Generation{ 0 };
+		std::atomic<bool> Stop{ false };
 	};
 }

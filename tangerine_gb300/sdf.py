@@ -217,21 +217,37 @@ def last_export_timing():
     return tuple(x.value for x in v)
 
 
+class _HostBlocks:
+    """Owns the host blocks of one tg_mesh (pinned memory the library reuses): they go back
+    to the library with tg_mesh_free once no array views them."""
+
+    def __init__(self, hm: _lib.HostMesh):
+        self.hm = hm
+
+    def __del__(self):
+        try:
+            load().tg_mesh_free(C.byref(self.hm))
+        except Exception:   # interpreter shutdown
+            pass
+
+
 def _take_mesh(hm: _lib.HostMesh) -> Mesh:
+    """The mesh's arrays view the library's host blocks without a copy."""
     v, f = int(hm.vertex_count), int(hm.face_count)
+    owner = _HostBlocks(hm)
 
-    def arr(ptr, n, dtype):
-        if n == 0:
+    def arr(ptr, n, ctype, dtype):
+        if n == 0 or not ptr:
             return np.zeros(0, dtype)
-        return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+        buf = (ctype * n).from_address(C.addressof(ptr.contents))
+        buf._owner = owner
+        return np.frombuffer(buf, dtype)
 
-    m = Mesh(arr(hm.vertices, v * 3, np.float32).reshape(v, 3),
-             arr(hm.normals, v * 3, np.float32).reshape(v, 3),
-             arr(hm.colors, v * 3, np.uint8).reshape(v, 3) if hm.colors else None,
-             arr(hm.faces, f * 3, np.uint32).reshape(f, 3),
-             arr(hm.cubes, v, np.uint32))
-    load().tg_mesh_free(C.byref(hm))
-    return m
+    return Mesh(arr(hm.vertices, v * 3, C.c_float, np.float32).reshape(v, 3),
+                arr(hm.normals, v * 3, C.c_float, np.float32).reshape(v, 3),
+                arr(hm.colors, v * 3, C.c_uint8, np.uint8).reshape(v, 3) if hm.colors else None,
+                arr(hm.faces, f * 3, C.c_uint32, np.uint32).reshape(f, 3),
+                arr(hm.cubes, v, C.c_uint32, np.uint32))
 
 
 class Program:
