@@ -29,7 +29,25 @@ namespace tg
 			uint32_t NullOctants = 0;   // children whose clip returned null
 			int Leaves = 0;
 			NodeRef Eval;
-			std::unique_ptr<TmpCell> Kids[8];
+			TmpCell* Kids[8] = { nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
+		};
+
+		// The build's cells, a block per level.  A cell dropped from the tree is only
+		// unlinked: its clipped tree is released with the blocks, on the background thread,
+		// after the build (the live cells' trees borrow only from live ancestors).
+		struct CellArena
+		{
+			std::vector<std::unique_ptr<TmpCell[]>> Blocks;
+			TmpCell* Take(size_t n)
+			{
+				Blocks.emplace_back(new TmpCell[n]);
+				return Blocks.back().get();
+			}
+			void ReleaseLater()
+			{
+				auto held = std::make_shared<std::vector<std::unique_ptr<TmpCell[]>>>(std::move(Blocks));
+				WorkerPool::Get().Later([held]() { held->clear(); });
+			}
 		};
 
 		struct BuildParams
@@ -64,7 +82,7 @@ namespace tg
 		{
 			float span;
 			PlaceCell(c, span);
-			SetEvaluator(c, in->Clip(c.Pivot, c.Radius), span, bp);
+			SetEvaluator(c, in->Clip(c.Pivot, c.Radius, true), span, bp);
 		}
 
 		// The eight children of an expanded cell, their clips sharing one walk of its tree.
@@ -79,7 +97,7 @@ namespace tg
 				radii[i] = parent.Kids[i]->Radius;
 			}
 			NodeRef evals[8];
-			parent.Eval->Clip8(pivots, radii, evals);
+			parent.Eval->Clip8(pivots, radii, evals, true);
 			for (int i = 0; i < 8; ++i) SetEvaluator(*parent.Kids[i], std::move(evals[i]), spans[i], bp);
 		}
 
@@ -90,7 +108,7 @@ namespace tg
 			TmpCell& kid = *parent.Kids[i];
 			float span;
 			PlaceCell(kid, span);
-			SetEvaluator(kid, parent.Eval->Clip(kid.Pivot, kid.Radius), span, bp);
+			SetEvaluator(kid, parent.Eval->Clip(kid.Pivot, kid.Radius, true), span, bp);
 		}
 
 		// The tail of SDFOctree::Populate (sdf_evaluator.cpp:1703-1783), once the children
@@ -106,7 +124,7 @@ namespace tg
 				if (!c.Kids[i]->Eval)
 				{
 					if (c.Kids[i]->ClippedAway) c.NullOctants |= 1u << i;
-					c.Kids[i].reset();
+					c.Kids[i] = nullptr;
 					continue;
 				}
 				uniform = uniform && c.Eval->Equals(*c.Kids[i]->Eval);
@@ -131,27 +149,20 @@ namespace tg
 			const int limit = depth > 3 ? depth : 3;
 			if (bp.Coalesce && ((penultimate && uniform) || c.Leaves <= limit))
 			{
-				for (auto& k : c.Kids) k.reset();
+				for (auto& k : c.Kids) k = nullptr;
 				c.Terminus = true;
 			}
 		}
 
-		// Post-order: children finish before their parent looks at them.
-		void FinishTree(TmpCell& c, const BuildParams& bp, int depth)
-		{
-			if (!c.Expanded) return;
-			for (auto& k : c.Kids) FinishTree(*k, bp, depth + 1);
-			FinishCell(c, bp, depth);
-		}
-
 		// SDFOctree::Populate's recursion, level by level: every cell of a level is clipped
 		// in parallel (the clips are independent), then the cells that go on split into
-		// eight children for the next level.  The merge decisions run afterwards, bottom up;
-		// they depend only on a cell's descendants, so the octree is the one the reference's
-		// depth-first recursion builds.  `tops` are disjoint subtrees, all at top_depth.
-		void BuildLevels(const std::vector<TmpCell*>& tops, const BuildParams& bp, int top_depth)
+		// eight children for the next level.  The merge decisions run afterwards, bottom up
+		// a level at a time; they depend only on a cell's descendants, so the octree is the one the reference's depth-first recursion
+		// builds.  `tops` are disjoint subtrees, all at top_depth.
+		void BuildLevels(const std::vector<TmpCell*>& tops, const BuildParams& bp, int top_depth, CellArena& arena)
 		{
 			std::vector<TmpCell*> level = tops;
+			std::vector<std::vector<TmpCell*>> expanded;   // per depth from top_depth
 			int depth = top_depth;
 			while (!level.empty())
 			{
@@ -162,16 +173,22 @@ namespace tg
 					if (!(bp.Coalesce || bp.MaxDepth == -1 || depth < bp.MaxDepth)) continue;
 					c->Incomplete = false;
 					c->Expanded = true;
+					parents.push_back(c);
+				}
+				if (parents.empty()) break;
+				TmpCell* kids = arena.Take(parents.size() * 8);
+				for (size_t p = 0; p < parents.size(); ++p)
+				{
+					TmpCell* c = parents[p];
 					for (int i = 0; i < 8; ++i)
 					{
 						AABB b = c->Bounds;
 						if (i & 1) b.Min.x = c->Pivot.x; else b.Max.x = c->Pivot.x;
 						if (i & 2) b.Min.y = c->Pivot.y; else b.Max.y = c->Pivot.y;
 						if (i & 4) b.Min.z = c->Pivot.z; else b.Max.z = c->Pivot.z;
-						c->Kids[i] = std::make_unique<TmpCell>();
+						c->Kids[i] = kids + p * 8 + i;
 						c->Kids[i]->Bounds = b;
 					}
-					parents.push_back(c);
 				}
 				WorkerPool& pool = WorkerPool::Get();
 				if ((int)parents.size() <= pool.Workers())
@@ -180,10 +197,12 @@ namespace tg
 					pool.ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[j], bp); });
 				level.clear();
 				for (TmpCell* c : parents)
-					for (auto& k : c->Kids) level.push_back(k.get());
+					for (TmpCell* k : c->Kids) level.push_back(k);
+				expanded.push_back(std::move(parents));
 				++depth;
 			}
-			for (TmpCell* t : tops) FinishTree(*t, bp, top_depth);
+			for (size_t d = expanded.size(); d-- > 0;)
+				for (TmpCell* c : expanded[d]) FinishCell(*c, bp, top_depth + (int)d);
 		}
 
 		// SDFOctree::Walk's incomplete search (sodapop.cpp:108-124): cells that were never
@@ -195,7 +214,7 @@ namespace tg
 				if (c.Incomplete) out.push_back(&c);
 				return;
 			}
-			for (auto& k : c.Kids)
+			for (TmpCell* k : c.Kids)
 				if (k) FindIncomplete(*k, out);
 		}
 
@@ -203,7 +222,7 @@ namespace tg
 		{
 			size_t n = 1;
 			if (!t.Terminus)
-				for (const auto& k : t.Kids)
+				for (const TmpCell* k : t.Kids)
 					if (k) n += CountCells(*k);
 			return n;
 		}
@@ -249,16 +268,22 @@ namespace tg
 		}
 		if (cube.Volume() == 0.0f) return false;
 		BuildParams bp{ target, coalesce, max_depth };
-		auto top = std::make_unique<TmpCell>();
+		CellArena arena;
+		TmpCell* top = arena.Take(1);
 		top->Bounds = cube;
 		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
-		BuildLevels({ top.get() }, bp, 1);
+		BuildLevels({ top }, bp, 1, arena);
 		// SDFOctree::Create returns nullptr when the root lost its evaluator while
 		// populating (every octant clipped away).
-		if (!top->Eval) return false;
+		if (!top->Eval)
+		{
+			arena.ReleaseLater();
+			return false;
+		}
 		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
+		arena.ReleaseLater();
 		return true;
 	}
 
@@ -274,21 +299,27 @@ namespace tg
 		}
 		if (cube.Volume() == 0.0f) return false;
 		const BuildParams first{ 0.25f, false, 3 };
-		auto top = std::make_unique<TmpCell>();
+		CellArena arena;
+		TmpCell* top = arena.Take(1);
 		top->Bounds = cube;
 		InitCell(*top, root, first);
 		if (!top->Eval) return false;
-		BuildLevels({ top.get() }, first, 1);
-		if (!top->Eval) return false;
+		BuildLevels({ top }, first, 1, arena);
+		if (!top->Eval)
+		{
+			arena.ReleaseLater();
+			return false;
+		}
 		// Populate(false, 3, -1) of each incomplete cell: its children start at depth 4 and
 		// split without limit.  The cells are disjoint, so one level-parallel pass serves
 		// them all.
 		std::vector<TmpCell*> incomplete;
 		FindIncomplete(*top, incomplete);
 		const BuildParams second{ 0.25f, false, -1 };
-		BuildLevels(incomplete, second, 3);
+		BuildLevels(incomplete, second, 3, arena);
 		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
+		arena.ReleaseLater();
 		return true;
 	}
 
@@ -883,8 +914,10 @@ namespace tg
 		out.Header.MaxStack = maxStack;
 		out.BuildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 		// Releasing thousands of clipped subtrees takes about a millisecond; the caller does
-		// not need to wait for it (node reference counts are atomic).
-		std::thread([cells = std::move(octree.Cells)]() mutable { cells.clear(); }).detach();
+		// not need to wait for it (it touches only the nodes the clips made: the rest are
+		// borrowed, and counts are atomic).
+		auto cells = std::make_shared<std::vector<Octree::Cell>>(std::move(octree.Cells));
+		WorkerPool::Get().Later([cells]() { cells->clear(); });
 		return true;
 	}
 }

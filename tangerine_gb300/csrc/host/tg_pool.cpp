@@ -26,6 +26,37 @@ namespace tg
 		}
 		Wake.notify_all();
 		for (auto& t : Threads) t.join();
+		{
+			std::lock_guard<std::mutex> lock(LaterMutex);
+			LaterStop = true;
+		}
+		LaterWake.notify_all();
+		if (Background.joinable()) Background.join();
+	}
+
+	void WorkerPool::Later(std::function<void()> task)
+	{
+		std::lock_guard<std::mutex> lock(LaterMutex);
+		LaterTasks.push_back(std::move(task));
+		if (!Background.joinable())
+		{
+			Background = std::thread([this]()
+			{
+				std::vector<std::function<void()>> run;
+				for (;;)
+				{
+					{
+						std::unique_lock<std::mutex> lk(LaterMutex);
+						LaterWake.wait(lk, [&]() { return LaterStop || !LaterTasks.empty(); });
+						if (LaterTasks.empty()) return;   // stopping with nothing left
+						run.swap(LaterTasks);
+					}
+					for (auto& t : run) t();
+					run.clear();
+				}
+			});
+		}
+		LaterWake.notify_one();
 	}
 
 	void WorkerPool::Drain(Job& job)

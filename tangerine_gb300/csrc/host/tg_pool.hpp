@@ -27,6 +27,9 @@ namespace tg
 		static WorkerPool& Get();
 		void ParallelFor(int count, const std::function<void(int)>& body);
 		int Workers() const { return (int)Threads.size(); }
+		// Runs `task` later on a background thread of its own, in submission order (used to
+		// release large temporary structures without making the caller wait).
+		void Later(std::function<void()> task);
 		~WorkerPool();
 
 	private:
@@ -49,5 +52,11 @@ namespace tg
 		std::shared_ptr<Job> Current;
 		std::atomic<uint64_t> Generation{ 0 };
 		std::atomic<bool> Stop{ false };
+
+		std::thread Background;             // started by the first Later call
+		std::mutex LaterMutex;
+		std::condition_variable LaterWake;
+		std::vector<std::function<void()>> LaterTasks;
+		bool LaterStop = false;
 	};
 }

@@ -11,18 +11,33 @@ namespace tg
 {
 	NodeRef::NodeRef(const NodeRef& o) : P(o.P)
 	{
-		if (P) P->Refs.fetch_add(1, std::memory_order_relaxed);
+		if (P && !Borrowed()) get()->Refs.fetch_add(1, std::memory_order_relaxed);
 	}
 
 	NodeRef::~NodeRef()
 	{
-		if (P && P->Refs.fetch_sub(1, std::memory_order_acq_rel) == 1) delete P;
+		if (P && !Borrowed() && get()->Refs.fetch_sub(1, std::memory_order_acq_rel) == 1) delete get();
+	}
+
+	Node* NodeRef::release()
+	{
+		Node* r = get();
+		if (Borrowed() && r) r->Refs.fetch_add(1, std::memory_order_relaxed);
+		P = 0;
+		return r;
 	}
 
 	NodeRef NodeRef::Share(Node* n)
 	{
 		if (n) n->Refs.fetch_add(1, std::memory_order_relaxed);
 		return NodeRef(n);
+	}
+
+	NodeRef NodeRef::Borrow(const Node* n)
+	{
+		NodeRef r;
+		if (n) r.P = reinterpret_cast<uintptr_t>(n) | kBorrowed;
+		return r;
 	}
 
 	// Virtual Eval (sdf_evaluator.cpp:463-466, 598-601, 774-780, 1059-1062): brushes map
@@ -260,26 +275,46 @@ namespace tg
 		// The clip works on plain pointers: an untouched subtree is the input node itself, and
 		// only rebuilt nodes are allocated, kept alive in `keep` until the caller holds the
 		// result.  Reference counts (atomics on nodes that every thread's clips share) are
-		// touched only for rebuilt nodes' operands and the final result.
+		// touched only for rebuilt nodes' operands and the final result, and not at all for
+		// the input tree's nodes when the result borrows them.
+		std::atomic<uint32_t> gClipCalls{ 0 };
+
 		struct ClipScratch
 		{
 			std::vector<NodeRef> Keep;
+			bool BorrowInputs = false;
+			uint32_t Mark = 0;
+			explicit ClipScratch(bool borrow) : BorrowInputs(borrow)
+			{
+				if (borrow)
+				{
+					do Mark = gClipCalls.fetch_add(1, std::memory_order_relaxed) + 1;
+					while (Mark == 0);
+				}
+			}
 			const Node* Hold(NodeRef n)
 			{
+				n->ClipMark = Mark;
 				const Node* raw = n.get();
 				Keep.push_back(std::move(n));
 				return raw;
 			}
+			// A reference to a node of the clip's result: counted for the nodes this clip
+			// made (Keep lets go of them), borrowed for the input's nodes when the caller
+			// asked for that.  A mark left by another clip only makes a reference counted.
+			NodeRef Ref(const Node* n) const
+			{
+				if (BorrowInputs && n->ClipMark != Mark) return NodeRef::Borrow(n);
+				return NodeRef::Share(const_cast<Node*>(n));
+			}
 		};
-
-		inline NodeRef Own(const Node* n) { return NodeRef::Share(const_cast<Node*>(n)); }
 
 		// A set node whose clipped operands are its own operands is kept as it is (the
 		// node MakeSet would build from them is the same node).
 		const Node* RebuildSet(const Node& n, const Node* l, const Node* r, ClipScratch& cs)
 		{
 			if (l == n.Lhs.get() && r == n.Rhs.get()) return &n;
-			return cs.Hold(SDF::MakeSet(n.Op, Own(l), Own(r), n.Threshold));
+			return cs.Hold(SDF::MakeSet(n.Op, cs.Ref(l), cs.Ref(r), n.Threshold));
 		}
 
 		// Clip (sdf_evaluator.cpp:468-478, 603-615, 782-850, 1064-1075): the part of the tree
@@ -296,14 +331,14 @@ namespace tg
 			{
 				const Node* child = ClipAt(*n.Lhs, radius, ev, cs);
 				if (!child) return nullptr;
-				return cs.Hold(SDF::Stencil(Own(child), n.Mask, n.Mat, n.Negative));
+				return cs.Hold(SDF::Stencil(cs.Ref(child), cs.BorrowInputs ? NodeRef::Borrow(n.Mask.get()) : n.Mask, n.Mat, n.Negative));
 			}
 			case NodeKind::Flate:
 			{
 				if (!(ev.At(n) <= radius)) return nullptr;
 				const Node* child = ClipAt(*n.Lhs, radius + n.Threshold, ev, cs);
 				if (!child) return nullptr;
-				return cs.Hold(SDF::Flate(Own(child), n.Threshold));
+				return cs.Hold(SDF::Flate(cs.Ref(child), n.Threshold));
 			}
 			case NodeKind::Set:
 			{
@@ -330,23 +365,23 @@ namespace tg
 		}
 	}
 
-	NodeRef Node::Clip(Vec3 p, float radius) const
+	NodeRef Node::Clip(Vec3 p, float radius, bool borrow) const
 	{
 		PointEvaluations ev(p);
-		ClipScratch cs;
+		ClipScratch cs(borrow);
 		const Node* r = ClipAt(*this, radius, ev, cs);
-		return r ? Own(r) : NodeRef();
+		return r ? cs.Ref(r) : NodeRef();
 	}
 
-	void Node::Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8]) const
+	void Node::Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8], bool borrow) const
 	{
 		Evaluations8 ev(p);
-		ClipScratch cs;
+		ClipScratch cs(borrow);
 		for (int i = 0; i < 8; ++i)
 		{
 			LaneOf8 lane{ ev, i };
 			const Node* r = ClipAt(*this, radius[i], lane, cs);
-			out[i] = r ? Own(r) : NodeRef();
+			out[i] = r ? cs.Ref(r) : NodeRef();
 		}
 	}
 

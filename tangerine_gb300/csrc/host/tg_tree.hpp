@@ -26,29 +26,38 @@ namespace tg
 
 	struct Node;
 
-	// Intrusive reference: the C ABI hands these out as plain pointers.
+	// Intrusive reference: the C ABI hands these out as plain pointers.  A reference may
+	// also be borrowed (tagged in the pointer's low bit): it counts nothing and keeps
+	// nothing alive.  The octree's clipped trees borrow the nodes of the tree they were
+	// clipped from, which outlives them, so that threads clipping in parallel do not all
+	// write the shared nodes' counters.
 	class NodeRef
 	{
 	public:
 		NodeRef() = default;
-		explicit NodeRef(Node* adopt) : P(adopt) {}
+		explicit NodeRef(Node* adopt) : P(reinterpret_cast<uintptr_t>(adopt)) {}
 		NodeRef(const NodeRef& o);
-		NodeRef(NodeRef&& o) noexcept : P(o.P) { o.P = nullptr; }
+		NodeRef(NodeRef&& o) noexcept : P(o.P) { o.P = 0; }
 		NodeRef& operator=(NodeRef o) { std::swap(P, o.P); return *this; }
 		~NodeRef();
-		Node* get() const { return P; }
-		Node* operator->() const { return P; }
-		Node& operator*() const { return *P; }
-		explicit operator bool() const { return P != nullptr; }
-		Node* release() { Node* r = P; P = nullptr; return r; }
+		Node* get() const { return reinterpret_cast<Node*>(P & ~kBorrowed); }
+		Node* operator->() const { return get(); }
+		Node& operator*() const { return *get(); }
+		explicit operator bool() const { return P != 0; }
+		bool Borrowed() const { return (P & kBorrowed) != 0; }
+		// A counted pointer for the caller (a borrowed reference takes a count first).
+		Node* release();
 		static NodeRef Share(Node* n);
+		static NodeRef Borrow(const Node* n);
 	private:
-		Node* P = nullptr;
+		static constexpr uintptr_t kBorrowed = 1;
+		uintptr_t P = 0;
 	};
 
 	struct Node
 	{
 		std::atomic<int> Refs{ 1 };
+		uint32_t ClipMark = 0;   // the clip call that made this node (0: not made by a clip)
 		NodeKind Kind = NodeKind::Brush;
 		uint32_t Op = OpStop;
 		int StackSize = 1;
@@ -66,9 +75,11 @@ namespace tg
 		bool Negative = false;
 
 		float Eval(Vec3 p) const;
-		NodeRef Clip(Vec3 p, float radius) const;
+		// `borrow`: the result borrows the nodes it keeps from this tree (only the nodes the
+		// clip rebuilt are counted), so it must not outlive this tree.
+		NodeRef Clip(Vec3 p, float radius, bool borrow = false) const;
 		// Clip to eight spheres at once (the same result as eight Clip calls).
-		void Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8]) const;
+		void Clip8(const Vec3 (&p)[8], const float (&radius)[8], NodeRef (&out)[8], bool borrow = false) const;
 		AABB Bounds() const;
 		AABB InnerBounds() const;
 		void Move(Vec3 by);
