@@ -118,7 +118,7 @@ namespace tg
 			ProgramLayout l;
 			l.NodeBytes = p.Host.Nodes.size() * sizeof(OctNode);
 			l.CodeOff = AlignUp(l.NodeBytes, 256);
-			l.CodeBytes = p.Host.Code.size() * sizeof(float);
+			l.CodeBytes = p.Host.CodeFloats * sizeof(float);
 			l.ColorOff = AlignUp(l.CodeOff + l.CodeBytes, 256);
 			l.RgbOff = AlignUp(l.ColorOff + (p.Host.Colors.size() ? p.Host.Colors.size() : 4), 256);
 			l.Total = l.RgbOff + (p.Host.MaterialRgb.size() ? p.Host.MaterialRgb.size() * sizeof(float) : 16);
@@ -128,7 +128,7 @@ namespace tg
 		void Pack(const Program& p, const ProgramLayout& l, uint8_t* dst)
 		{
 			std::memcpy(dst, p.Host.Nodes.data(), l.NodeBytes);
-			std::memcpy(dst + l.CodeOff, p.Host.Code.data(), l.CodeBytes);
+			p.Host.CopyCode(reinterpret_cast<float*>(dst + l.CodeOff));
 			if (!p.Host.Colors.empty()) std::memcpy(dst + l.ColorOff, p.Host.Colors.data(), p.Host.Colors.size());
 			if (!p.Host.MaterialRgb.empty())
 				std::memcpy(dst + l.RgbOff, p.Host.MaterialRgb.data(), p.Host.MaterialRgb.size() * sizeof(float));

@@ -761,6 +761,15 @@ namespace tg
 		return w;
 	}
 
+	void CompiledTree::CopyCode(float* dst) const
+	{
+		for (const auto& c : CodeChunks)
+		{
+			std::memcpy(dst, c.data(), c.size() * sizeof(float));
+			dst += c.size();
+		}
+	}
+
 	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind)
 	{
 		const auto t0 = std::chrono::steady_clock::now();
@@ -787,15 +796,22 @@ namespace tg
 		std::vector<const Node*> distinct;
 		std::vector<int> programOf(octree.Cells.size(), -1);
 		{
-			std::unordered_map<const Node*, int> index;
-			index.reserve(octree.Cells.size());
+			// Open addressing on the node address, first appearance order.
+			size_t cap = 64;
+			while (cap < octree.Cells.size() * 2) cap <<= 1;
+			std::vector<std::pair<const Node*, int>> index(cap, { nullptr, -1 });
 			for (size_t i = 0; i < octree.Cells.size(); ++i)
 			{
 				const Node* e = octree.Cells[i].Evaluator.get();
 				if (!e) continue;
-				auto ins = index.emplace(e, (int)distinct.size());
-				if (ins.second) distinct.push_back(e);
-				programOf[i] = ins.first->second;
+				size_t h = (size_t)(((uint64_t)(uintptr_t)e >> 4) * 0x9E3779B97F4A7C15ull >> 20) & (cap - 1);
+				while (index[h].first && index[h].first != e) h = (h + 1) & (cap - 1);
+				if (!index[h].first)
+				{
+					index[h] = { e, (int)distinct.size() };
+					distinct.push_back(e);
+				}
+				programOf[i] = index[h].second;
 			}
 		}
 		// Every brush of the full tree (clipped trees share them) gets its records once, up
@@ -836,22 +852,22 @@ namespace tg
 				programs[u] = EmittedPrograms{ dist, surf, d1 > d2 ? d1 : d2, em.NonLipschitz };
 			}
 		});
-		size_t total = 4;
-		for (const auto& c : chunkCode) total += c.size();
-		out.Code.reserve(total + 4096);
-		// One stop record first: the programs of cells without an evaluator.
-		out.Code.push_back(BitsFloat(OpStop));
-		out.Code.push_back(0.0f); out.Code.push_back(0.0f); out.Code.push_back(0.0f);
+		// One stop record first (the programs of cells without an evaluator), then the
+		// chunks in order; they are not copied together here (the upload packs them).
+		out.CodeChunks.reserve((size_t)chunkCount + 1);
+		out.CodeChunks.push_back({ BitsFloat(OpStop), 0.0f, 0.0f, 0.0f });
+		out.CodeFloats = 4;
 		const int stopQuad = 0;
 		for (int ch = 0; ch < chunkCount; ++ch)
 		{
-			const int base = (int)(out.Code.size() / 4);
+			const int base = (int)(out.CodeFloats / 4);
 			for (size_t u = chunkBegin(ch); u < chunkBegin(ch + 1); ++u)
 			{
 				programs[u].Distance += base;
 				programs[u].Surface += base;
 			}
-			out.Code.insert(out.Code.end(), chunkCode[(size_t)ch].begin(), chunkCode[(size_t)ch].end());
+			out.CodeFloats += chunkCode[(size_t)ch].size();
+			out.CodeChunks.push_back(std::move(chunkCode[(size_t)ch]));
 		}
 		int maxStack = 0;
 		out.Nodes.resize(octree.Cells.size());
@@ -908,7 +924,7 @@ namespace tg
 			out.MaterialRgb[m * 4 + 3] = 1.0f;
 		}
 		out.Header.NodeCount = (int32_t)out.Nodes.size();
-		out.Header.CodeQuads = (int32_t)(out.Code.size() / 4);
+		out.Header.CodeQuads = (int32_t)(out.CodeFloats / 4);
 		out.Header.MaterialCount = (int32_t)materialList.size();
 		out.Header.HasPaint = octree.Cells[0].Evaluator->HasPaint() ? 1 : 0;
 		out.Header.MaxStack = maxStack;

@@ -49,7 +49,11 @@ namespace tg
 	{
 		ProgramHeader Header{};
 		std::vector<OctNode> Nodes;
-		std::vector<float> Code;          // 4 floats per quad
+		// The record quads (4 floats each) in the pieces the emitters wrote them in; laid
+		// end to end they are the program image (CopyCode).
+		std::vector<std::vector<float>> CodeChunks;
+		size_t CodeFloats = 0;
+		void CopyCode(float* dst) const;
 		std::vector<uint8_t> Colors;      // 4 bytes per material
 		std::vector<float> MaterialRgb;   // 4 floats per material: stored RGB, 1
 		AABB Bounds{};                    // root evaluator bounds
