@@ -86,57 +86,87 @@ namespace tg
 			}
 		}
 
-		// Normals and colours: five threads per point (the four tetrahedral offsets of
-		// SDFNode::Gradient and the point itself, which also follows GetMaterial), each a
-		// single pass over the point's surface program; lane 0 combines them.  One lane per
-		// evaluation keeps the interpreter's code small enough for the instruction cache.
+		// Face normals (the STL writer): five threads per point (the four tetrahedral offsets
+		// of SDFNode::Gradient and the point itself), each a single pass over the point's
+		// surface program; lane 0 combines them.  One lane per evaluation keeps the
+		// interpreter's code small enough for the instruction cache.
 		constexpr int kPointsPerBlock = 32;
 		constexpr int kAttribThreads = kPointsPerBlock * 5;
 
 		// One evaluation lane: distance at TetraPoint(p, lane); lane 4 with `material` also
-		// returns the material index.
-		__device__ __forceinline__ float EvaluationLane(const DeviceProgram& prog, Vec3 p, int lane, bool material, int* m, float* spill)
+		// returns the material index.  `stride`: the block's thread count (spill layout).
+		__device__ __forceinline__ float EvaluationLane(const DeviceProgram& prog, Vec3 p, int lane, bool material, int* m, float* spill,
+			int stride = kAttribThreads)
 		{
 			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
 			const int pc = __ldg(&prog.Nodes[cell].SurfaceCode);
 			const Vec3 q = TetraPoint(p, lane);
 			const float px[1] = { q.x }, py[1] = { q.y }, pz[1] = { q.z };
 			float e[1];
-			RunSurfaceBatch<1>(prog.Code, pc, px, py, pz, e, (lane == 4 && material) ? 0 : -1, m, spill, kAttribThreads);
+			RunSurfaceBatch<1>(prog.Code, pc, px, py, pz, e, (lane == 4 && material) ? 0 : -1, m, spill, stride);
 			return e[0];
 		}
 
-		__global__ void __launch_bounds__(kAttribThreads) VertexAttributesKernel(DeviceProgram prog, const float* __restrict__ vertices,
-			uint32_t n, float* __restrict__ normals, uint8_t* __restrict__ colors)
+		// Normals alone: four threads per vertex, one per tetrahedral offset, all running the
+		// same code; lane 0 combines them and evaluates the vertex itself only when the four
+		// cancel (SDFNode::Gradient's fallback).  The colours are a separate pass, so no lane
+		// takes the material path while the others wait.
+		constexpr int kNormalThreads = 128;
+		constexpr int kNormalPoints = kNormalThreads / 4;
+
+		__global__ void __launch_bounds__(kNormalThreads) VertexNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
+			uint32_t n, float* __restrict__ normals)
 		{
 			extern __shared__ float spill[];
-			__shared__ float evals[kAttribThreads];
-			__shared__ int mats[kPointsPerBlock];
-			const int local = threadIdx.x / 5, lane = threadIdx.x % 5;
-			const uint32_t v = blockIdx.x * kPointsPerBlock + local;
+			const int local = threadIdx.x >> 2, lane = threadIdx.x & 3;
+			const uint32_t v = blockIdx.x * kNormalPoints + local;
+			Vec3 p(0.0f, 0.0f, 0.0f);
+			float mine = 0.0f;
 			if (v < n)
 			{
-				const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
-				int m = -1;
-				evals[threadIdx.x] = EvaluationLane(prog, p, lane, colors != nullptr, &m, spill + threadIdx.x);
-				if (lane == 4) mats[local] = m;
+				p = Vec3(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
+				mine = EvaluationLane(prog, p, lane, false, nullptr, spill + threadIdx.x, kNormalThreads);
 			}
-			__syncthreads();
+			// The four lanes of a vertex are neighbours in one warp.
+			float e[5];
+			e[0] = __shfl_sync(0xFFFFFFFFu, mine, (threadIdx.x & 31) & ~3);
+			e[1] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 1);
+			e[2] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 2);
+			e[3] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 3);
 			if (v < n && lane == 0)
 			{
-				const Vec3 g = GradientOf(evals + local * 5);
-				normals[(int64_t)v * 3 + 0] = g.x;
-				normals[(int64_t)v * 3 + 1] = g.y;
-				normals[(int64_t)v * 3 + 2] = g.z;
-				if (colors)
-				{
-					const int m = mats[local];
-					const uchar4 c = m >= 0 ? prog.Colors[m] : make_uchar4(255, 255, 255, 255);
-					colors[(int64_t)v * 3 + 0] = c.x;
-					colors[(int64_t)v * 3 + 1] = c.y;
-					colors[(int64_t)v * 3 + 2] = c.z;
-				}
+				e[4] = 0.0f;
+				const float h = 0.0001f;
+				const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+				Vec3 g = xyy * e[0];
+				g = g + yyx * e[1];
+				g = g + yxy * e[2];
+				g = g + xxx * e[3];
+				if ((g.x * g.x + g.y * g.y) + g.z * g.z == 0.0f)
+					e[4] = EvaluationLane(prog, p, 4, false, nullptr, spill + threadIdx.x, kNormalThreads);
+				const Vec3 r = GradientOf(e);
+				normals[(int64_t)v * 3 + 0] = r.x;
+				normals[(int64_t)v * 3 + 1] = r.y;
+				normals[(int64_t)v * 3 + 2] = r.z;
 			}
+		}
+
+		// Colours: GetMaterial's walk at each vertex, one thread per vertex.
+		constexpr int kColorThreads = 128;
+
+		__global__ void __launch_bounds__(kColorThreads) VertexColorsKernel(DeviceProgram prog, const float* __restrict__ vertices,
+			uint32_t n, uint8_t* __restrict__ colors)
+		{
+			extern __shared__ float spill[];
+			const uint32_t v = blockIdx.x * kColorThreads + threadIdx.x;
+			if (v >= n) return;
+			const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
+			int m = -1;
+			EvaluationLane(prog, p, 4, true, &m, spill + threadIdx.x, kColorThreads);
+			const uchar4 c = m >= 0 ? prog.Colors[m] : make_uchar4(255, 255, 255, 255);
+			colors[(int64_t)v * 3 + 0] = c.x;
+			colors[(int64_t)v * 3 + 1] = c.y;
+			colors[(int64_t)v * 3 + 2] = c.z;
 		}
 
 		// WriteSTL(Octree, ...) (export.cpp:140-148): the gradient at (a + b + c) / 3.
@@ -350,10 +380,14 @@ namespace tg
 		float* normals, uint8_t* colors, cudaStream_t stream)
 	{
 		if (vertex_count == 0) return cudaSuccess;
-		const size_t smem = SurfaceSpillBytes(prog, kAttribThreads);
-		if (smem > 40 * 1024) cudaFuncSetAttribute(VertexAttributesKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		VertexAttributesKernel<<<Blocks(vertex_count, kPointsPerBlock), kAttribThreads, smem, stream>>>(prog, vertices, vertex_count,
-			normals, colors);
+		const size_t smem = SurfaceSpillBytes(prog, kNormalThreads);
+		if (smem > 40 * 1024) cudaFuncSetAttribute(VertexNormalsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		VertexNormalsKernel<<<Blocks(vertex_count, kNormalPoints), kNormalThreads, smem, stream>>>(prog, vertices, vertex_count, normals);
+		cudaError_t e = cudaGetLastError();
+		if (e != cudaSuccess || !colors) return e;
+		const size_t csmem = SurfaceSpillBytes(prog, kColorThreads);
+		if (csmem > 40 * 1024) cudaFuncSetAttribute(VertexColorsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
+		VertexColorsKernel<<<Blocks(vertex_count, kColorThreads), kColorThreads, csmem, stream>>>(prog, vertices, vertex_count, colors);
 		return cudaGetLastError();
 	}
 }
