@@ -250,6 +250,85 @@ namespace tg
 			}
 		}
 
+		// The same pass for bricks of at most 7^3 cells: the CTA first stages the brick's
+		// lattice box (at most 8^3 points, coalesced rows) in shared memory, so each cell
+		// reads its eight corners there instead of issuing eight scattered global loads, and
+		// the brick's active cells take their slots in `cells` with one atomic per brick.
+		constexpr int kTiledBox = 8;
+		constexpr int kTiledThreads = 128;
+		constexpr int kTiledRounds = 3;   // 7^3 = 343 cells <= 3 x 128
+
+		__global__ void __launch_bounds__(kTiledThreads) CellFlagsTiledKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words,
+			uint32_t* __restrict__ cells, uint32_t* __restrict__ cell_count)
+		{
+			__shared__ float box[kTiledBox * kTiledBox * kTiledBox];
+			__shared__ uint32_t warpBase[kTiledThreads / 32];
+			const CellGeom cg = Geom(g);
+			const uint32_t n = *count;
+			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
+			{
+				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
+				__syncthreads();   // the previous brick is done with the box and the bases
+				for (int t = (int)threadIdx.x; t < kTiledBox * kTiledBox * kTiledBox; t += kTiledThreads)
+				{
+					const int x = t & 7, y = (t >> 3) & 7, z = t >> 6;
+					if (x <= bc.nx && y <= bc.ny && z <= bc.nz)
+						box[t] = __ldg(lat + ((bc.k0 + z) * cg.ny + bc.j0 + y) * cg.nx + bc.i0 + x);
+				}
+				__syncthreads();
+				const int total = bc.nx * bc.ny * bc.nz;
+				unsigned ballots[kTiledRounds];
+				uint32_t cellOf[kTiledRounds];
+				uint32_t mine = 0;
+#pragma unroll
+				for (int r = 0; r < kTiledRounds; ++r)
+				{
+					const int t = r * kTiledThreads + (int)threadIdx.x;
+					bool active = false;
+					cellOf[r] = 0;
+					if (t < total)
+					{
+						const int x = t % bc.nx, y = (t / bc.nx) % bc.ny, z = t / (bc.nx * bc.ny);
+						const float* b = box + (z * kTiledBox + y) * kTiledBox + x;
+						constexpr int dy = kTiledBox, dz = kTiledBox * kTiledBox;
+						const float v[8] = { b[0], b[1], b[dy + 1], b[dy], b[dz], b[dz + 1], b[dz + dy + 1], b[dz + dy] };
+						unsigned pos = 0;
+#pragma unroll
+						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+						active = pos != 0u && pos != 0xFFu;
+						const int64_t c = (bc.i0 + x) + (bc.j0 + y) * cg.sx + (bc.k0 + z) * cg.sx * cg.sy;
+						cellOf[r] = (uint32_t)c;
+						if (active) atomicOr(words + (c >> 5), 1u << (c & 31));
+					}
+					ballots[r] = __ballot_sync(0xFFFFFFFFu, active);
+					mine += (uint32_t)__popc(ballots[r]);
+				}
+				if (lane == 0) warpBase[warp] = mine;
+				__syncthreads();
+				if (threadIdx.x == 0)
+				{
+					uint32_t sum = 0;
+					uint32_t counts[kTiledThreads / 32];
+#pragma unroll
+					for (int w = 0; w < kTiledThreads / 32; ++w) { counts[w] = warpBase[w]; sum += counts[w]; }
+					uint32_t at = sum ? atomicAdd(cell_count, sum) : 0u;
+#pragma unroll
+					for (int w = 0; w < kTiledThreads / 32; ++w) { warpBase[w] = at; at += counts[w]; }
+				}
+				__syncthreads();
+				uint32_t at = warpBase[warp];
+				const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+				for (int r = 0; r < kTiledRounds; ++r)
+				{
+					if ((ballots[r] >> lane) & 1u) cells[at + __popc(ballots[r] & below)] = cellOf[r];
+					at += (uint32_t)__popc(ballots[r]);
+				}
+			}
+		}
+
 		// One thread per active cell of the list: its vertex number is its rank in the
 		// bitmask, so the output is in cell order whatever the list order.
 		__global__ void __launch_bounds__(128) CellVerticesListedKernel(const float* __restrict__ lat, GridSpec g,
@@ -363,7 +442,11 @@ namespace tg
 		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((total + 31) / 32) * 4, stream);
 		if (e == cudaSuccess) e = cudaMemsetAsync(cell_count, 0, sizeof(uint32_t), stream);
 		if (e != cudaSuccess) return e;
-		CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
+		if (B + 1 <= kTiledBox)
+			CellFlagsTiledKernel<<<grid_blocks * 2, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells,
+				cell_count);
+		else
+			CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
 		return cudaGetLastError();
 	}
 
