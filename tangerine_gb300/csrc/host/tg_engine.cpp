@@ -300,12 +300,11 @@ namespace tg
 			const int64_t brickWords = (nb + 31) / 32;
 			TG_TRY(BrickBits.Reserve((size_t)brickWords * 4 * (opt.Field && opt.Refine ? 2 : 1)));
 			TG_TRY(BrickList.Reserve((size_t)nb * 4));
-			if (!PersistentBlocks)
+			if (!SmCount)
 			{
-				int dev = 0, sms = 0;
+				int dev = 0;
 				TG_TRY(cudaGetDevice(&dev));
-				TG_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-				PersistentBlocks = sms * 8;
+				TG_TRY(cudaDeviceGetAttribute(&SmCount, cudaDevAttrMultiProcessorCount, dev));
 			}
 			uint32_t* brickCount = Counts.As<uint32_t>() + 2;
 			uint32_t* bits = BrickBits.As<uint32_t>();
@@ -339,14 +338,14 @@ namespace tg
 			End(s);
 			LastBrickSize = B;
 			Begin("eval_bricks", s);
-			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), PersistentBlocks, s,
+			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), SmCount, s,
 				opt.Lanes));
 			End(s);
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.
 			TG_TRY(ActiveCells.Reserve((size_t)(nb * (int64_t)B * B * B < cells ? nb * (int64_t)B * B * B : cells) * 4));
 			Begin("cell_flags", s);
 			TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
-				ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, PersistentBlocks, s));
+				ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, SmCount, s));
 			End(s);
 			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 8, cudaMemcpyDeviceToHost, s));
 			Bricks = nb;

@@ -170,7 +170,7 @@ namespace tg
 		void* Staging = nullptr;
 		size_t StagingBytes = 0;
 		uint32_t* HostCounts = nullptr;
-		int PersistentBlocks = 0;
+		int SmCount = 0;
 		int64_t ActiveBricks = 0, Bricks = 0;
 		int LastBrickSize = 0;
 	};

@@ -26,6 +26,12 @@ namespace tg
 	{
 		constexpr int kClassifyThreads = 128;
 		constexpr int kBrickThreads = 128;     // 8 x 8 columns x 2 z-groups of 4 points
+		// Resident CTAs per SM the brick evaluation is compiled for.  For 7^3-cell bricks
+		// (48 registers a thread) the 512^3 export measured 0.65 ms at 8 (64 registers),
+		// 0.58 at 9, 0.56 at 10, 0.66 at 12 (spills); larger bricks keep 8.
+		template<int C> constexpr int EvalBricksCtasPerSm() { return C == 8 ? 10 : 8; }
+		constexpr int kCellPassCtasPerSm = 16;
+		constexpr int kListedCtasPerSm = 8;
 
 		struct BrickGrid
 		{
@@ -84,7 +90,7 @@ namespace tg
 		// A CTA is 8 x 8 columns x (128 / 64) z-groups; each thread runs K z-consecutive
 		// points, so one pass covers an 8 x 8 x 2K chunk of the brick's lattice box.
 		template<int C, int K>
-		__global__ void __launch_bounds__(kBrickThreads) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
+		__global__ void __launch_bounds__(kBrickThreads, EvalBricksCtasPerSm<C>()) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice)
 		{
 			extern __shared__ float spill[];
@@ -389,7 +395,7 @@ namespace tg
 	{
 		template<int C, int K>
 		cudaError_t LaunchEvalBricksCK(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int grid_blocks, cudaStream_t stream)
+			float* lattice, int sms, cudaStream_t stream)
 		{
 			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 			const size_t smem = (size_t)depth * K * kBrickThreads * sizeof(float);
@@ -398,30 +404,30 @@ namespace tg
 				cudaError_t e = cudaFuncSetAttribute(EvalBricksKernel<C, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 				if (e != cudaSuccess) return e;
 			}
-			EvalBricksKernel<C, K><<<grid_blocks, kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list, count, lattice);
+			EvalBricksKernel<C, K><<<sms * EvalBricksCtasPerSm<C>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list, count, lattice);
 			return cudaGetLastError();
 		}
 
 		template<int C>
 		cudaError_t LaunchEvalBricksC(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int grid_blocks, cudaStream_t stream, int lanes)
+			float* lattice, int sms, cudaStream_t stream, int lanes)
 		{
 			switch (lanes)
 			{
-			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, grid_blocks, stream);
-			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, grid_blocks, stream);
-			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, grid_blocks, stream);
+			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, sms, stream);
+			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, sms, stream);
+			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, sms, stream);
 			}
 		}
 	}
 
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int grid_blocks, cudaStream_t stream, int lanes)
+		float* lattice, int sms, cudaStream_t stream, int lanes)
 	{
-		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
-		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
-		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
-		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, grid_blocks, stream, lanes);
+		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, sms, stream, lanes);
+		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, sms, stream, lanes);
+		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, sms, stream, lanes);
+		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, sms, stream, lanes);
 		return cudaErrorInvalidValue;
 	}
 
@@ -436,17 +442,17 @@ namespace tg
 	}
 
 	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int grid_blocks, cudaStream_t stream)
+		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int sms, cudaStream_t stream)
 	{
 		const int64_t total = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
 		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((total + 31) / 32) * 4, stream);
 		if (e == cudaSuccess) e = cudaMemsetAsync(cell_count, 0, sizeof(uint32_t), stream);
 		if (e != cudaSuccess) return e;
 		if (B + 1 <= kTiledBox)
-			CellFlagsTiledKernel<<<grid_blocks * 2, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells,
+			CellFlagsTiledKernel<<<sms * kCellPassCtasPerSm, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells,
 				cell_count);
 		else
-			CellFlagsListedKernel<<<grid_blocks, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
+			CellFlagsListedKernel<<<sms * kListedCtasPerSm, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
 		return cudaGetLastError();
 	}
 

@@ -75,14 +75,15 @@ namespace tg
 	// length.  base: (bricks + 31) / 32 words; scratch: ScanScratchWords of that.
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
 		uint32_t* count, cudaStream_t stream);
+	// The brick kernels below run persistent grids sized from the SM count (`sms`).
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int grid_blocks, cudaStream_t stream, int lanes = 4);
+		float* lattice, int sms, cudaStream_t stream, int lanes = 4);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
 		cudaStream_t stream);
 	// Cell pass over the cells of listed bricks only: clears and fills the bitmask and
 	// lists the active cells (`cells` holds up to the lattice's cell count).
 	cudaError_t LaunchCellFlagsListed(const float* lattice, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int grid_blocks, cudaStream_t stream);
+		uint32_t* words, uint32_t* cells, uint32_t* cell_count, int sms, cudaStream_t stream);
 	// Vertex pass over the listed active cells (one thread each).
 	cudaError_t LaunchCellVerticesListed(const float* lattice, const GridSpec& g, const uint32_t* cells, uint32_t cell_count,
 		const uint32_t* words, const uint32_t* word_base, float* vertices, uint32_t* cubes, uint32_t* face_counts, cudaStream_t stream);
