@@ -7,40 +7,63 @@
 
 namespace tg
 {
-	// Whether the lattice box [i0, i1] x [j0, j1] x [k0, k1] (corner indices) may hold a
-	// sign change of the reference's distances; false only when that is proven.
-	template<bool FuseSet = true>
-	__device__ __forceinline__ bool BoxMayHoldSurface(const DeviceProgram& prog, const GridSpec& g,
-		int i0, int i1, int j0, int j1, int k0, int k1, float* spill, int stride)
+	// The ball the exact test works with: the lattice box's bounding ball and the margin
+	// that covers the rounding of its centre and of the programs.
+	struct BoxBall
+	{
+		float cx, cy, cz, r, margin;
+	};
+
+	__device__ __forceinline__ BoxBall BallOfBox(const DeviceProgram& prog, const GridSpec& g, int i0, int i1, int j0, int j1, int k0, int k1)
 	{
 		const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
 		const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
 		const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
-		const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
+		BoxBall b;
+		b.cx = 0.5f * (x0 + x1); b.cy = 0.5f * (y0 + y1); b.cz = 0.5f * (z0 + z1);
 		const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);
 		// Ball through the box's corners, widened for the rounding of the centre.
-		const float r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
+		b.r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
 		const float rootClip = __ldg(&prog.Nodes[0].ClipRadius);
-		const float margin = 1e-4f * (1.0f + fabsf(cx) + fabsf(cy) + fabsf(cz) + fabsf(rootClip));
+		b.margin = 1e-4f * (1.0f + fabsf(b.cx) + fabsf(b.cy) + fabsf(b.cz) + fabsf(rootClip));
+		return b;
+	}
+
+	constexpr int kBoxEmpty = -2;       // proven to hold no surface without a program
+	constexpr int kBoxUndecided = -1;   // may hold surface: no cell's program can decide
+
+	// The part of the exact test that needs no program: the root cube and dropped-octant
+	// tests, then the deepest cell on the centre's descent path whose clip sphere holds
+	// the ball (with no cell at or below it that is not 1-Lipschitz).  Returns that cell,
+	// kBoxEmpty or kBoxUndecided.
+	__device__ __forceinline__ int BoxHolder(const DeviceProgram& prog, const BoxBall& b)
+	{
+		const float rootClip = __ldg(&prog.Nodes[0].ClipRadius);
 		// Outside the root cube every brush, and so every clipped program, is positive
 		// (the cube holds the tree's bounds): a ball missing the cube has no surface.
 		const float half = fabsf(rootClip) * 0.57736f;           // span / 2 = radius / sqrt(3), rounded up
-		const float ox = fmaxf(fabsf(cx - __ldg(&prog.Nodes[0].Pivot[0])) - half, 0.0f);
-		const float oy = fmaxf(fabsf(cy - __ldg(&prog.Nodes[0].Pivot[1])) - half, 0.0f);
-		const float oz = fmaxf(fabsf(cz - __ldg(&prog.Nodes[0].Pivot[2])) - half, 0.0f);
-		if (sqrtf(ox * ox + oy * oy + oz * oz) > r + margin) return false;
-		// Deepest cell on the centre's descent path whose clip sphere holds the ball.
-		int path[48];
-		int depth = 0;
+		const float ox = fmaxf(fabsf(b.cx - __ldg(&prog.Nodes[0].Pivot[0])) - half, 0.0f);
+		const float oy = fmaxf(fabsf(b.cy - __ldg(&prog.Nodes[0].Pivot[1])) - half, 0.0f);
+		const float oz = fmaxf(fabsf(b.cz - __ldg(&prog.Nodes[0].Pivot[2])) - half, 0.0f);
+		if (sqrtf(ox * ox + oy * oy + oz * oz) > b.r + b.margin) return kBoxEmpty;
+		// Walking down, the holder is the deepest cell so far that holds the ball; a cell
+		// that is not 1-Lipschitz voids the holders above it.
+		int holder = kBoxUndecided;
 		int at = 0;
-		path[depth++] = 0;
-		for (int guard = 0; guard < 47; ++guard)
+		for (int guard = 0; guard < 48; ++guard)
 		{
 			const OctNode* n = prog.Nodes + at;
 			const int32_t flags = __ldg(&n->Flags);
-			if (flags & kNodeTerminus) break;
 			const float px = __ldg(&n->Pivot[0]), py = __ldg(&n->Pivot[1]), pz = __ldg(&n->Pivot[2]);
-			const int octant = (cx > px ? 1 : 0) | (cy > py ? 2 : 0) | (cz > pz ? 4 : 0);
+			const float clip = __ldg(&n->ClipRadius);
+			if (clip < 0.0f) holder = kBoxUndecided;
+			else
+			{
+				const float dx = b.cx - px, dy = b.cy - py, dz = b.cz - pz;
+				if (sqrtf(dx * dx + dy * dy + dz * dz) + b.r + b.margin <= clip) holder = at;
+			}
+			if (flags & kNodeTerminus) break;
+			const int octant = (b.cx > px ? 1 : 0) | (b.cy > py ? 2 : 0) | (b.cz > pz ? 4 : 0);
 			const int child = __ldg(&n->Child[octant]);
 			if (child < 0)
 			{
@@ -50,32 +73,41 @@ namespace tg
 				// sphere sits inside the parent's, where the parent's program has the tree's
 				// sign.  (Octants dropped because all their own children clipped away prove
 				// only their cube, without margin, and are not used.)
-				const float clip = __ldg(&n->ClipRadius);
 				if (clip > 0.0f && ((flags >> (8 + octant)) & 1))
 				{
 					const float q = clip * 0.28867513f;               // span / 4 = radius / (2 sqrt 3)
 					const float qx = px + ((octant & 1) ? q : -q), qy = py + ((octant & 2) ? q : -q), qz = pz + ((octant & 4) ? q : -q);
-					const float dx = cx - qx, dy = cy - qy, dz = cz - qz;
-					if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip * 0.4999f) return false;
+					const float dx = b.cx - qx, dy = b.cy - qy, dz = b.cz - qz;
+					if (sqrtf(dx * dx + dy * dy + dz * dz) + b.r + b.margin <= clip * 0.4999f) return kBoxEmpty;
 				}
 				break;
 			}
 			at = child;
-			path[depth++] = at;
 		}
-		int holder = -1;
-		for (int d = depth - 1; d >= 0; --d)
-		{
-			const OctNode* n = prog.Nodes + path[d];
-			const float clip = __ldg(&n->ClipRadius);
-			if (clip < 0.0f) break;                           // not 1-Lipschitz here or above
-			const float dx = cx - __ldg(&n->Pivot[0]), dy = cy - __ldg(&n->Pivot[1]), dz = cz - __ldg(&n->Pivot[2]);
-			if (sqrtf(dx * dx + dy * dy + dz * dz) + r + margin <= clip) { holder = path[d]; break; }
-		}
-		if (holder < 0) return true;
-		const float px[1] = { cx }, py[1] = { cy }, pz[1] = { cz };
+		return holder;
+	}
+
+	// The holder cell's program at the ball's centre decides: |f| > r + margin proves no
+	// sign change inside the ball.
+	template<bool FuseSet = true>
+	__device__ __forceinline__ bool HolderMayHoldSurface(const DeviceProgram& prog, int holder, const BoxBall& b, float* spill, int stride)
+	{
+		const float px[1] = { b.cx }, py[1] = { b.cy }, pz[1] = { b.cz };
 		float f[1];
 		RunDistance<1, FuseSet>(prog.Code, __ldg(&prog.Nodes[holder].DistanceCode), px, py, pz, f, spill, stride);
-		return !(fabsf(f[0]) > r + margin);
+		return !(fabsf(f[0]) > b.r + b.margin);
+	}
+
+	// Whether the lattice box [i0, i1] x [j0, j1] x [k0, k1] (corner indices) may hold a
+	// sign change of the reference's distances; false only when that is proven.
+	template<bool FuseSet = true>
+	__device__ __forceinline__ bool BoxMayHoldSurface(const DeviceProgram& prog, const GridSpec& g,
+		int i0, int i1, int j0, int j1, int k0, int k1, float* spill, int stride)
+	{
+		const BoxBall b = BallOfBox(prog, g, i0, i1, j0, j1, k0, k1);
+		const int holder = BoxHolder(prog, b);
+		if (holder == kBoxEmpty) return false;
+		if (holder == kBoxUndecided) return true;
+		return HolderMayHoldSurface<FuseSet>(prog, holder, b, spill, stride);
 	}
 }
