@@ -264,6 +264,9 @@ namespace tg
 		constexpr int kTiledThreads = 128;
 		constexpr int kTiledRounds = 3;   // 7^3 = 343 cells <= 3 x 128
 
+		// BT: the brick edge in cells when known at compile time (the cell coordinates then
+		// come from constant divisions, edge bricks masking their missing cells), or 0.
+		template<int BT>
 		__global__ void __launch_bounds__(kTiledThreads) CellFlagsTiledKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words,
 			uint32_t* __restrict__ cells, uint32_t* __restrict__ cell_count)
@@ -284,7 +287,10 @@ namespace tg
 						box[t] = __ldg(lat + ((bc.k0 + z) * cg.ny + bc.j0 + y) * cg.nx + bc.i0 + x);
 				}
 				__syncthreads();
-				const int total = bc.nx * bc.ny * bc.nz;
+				const int ex = BT ? BT : bc.nx, ey = BT ? BT : bc.ny;
+				const int total = BT ? BT * BT * BT : bc.nx * bc.ny * bc.nz;
+				const int64_t sxy = cg.sx * cg.sy;
+				const int64_t c0 = bc.i0 + bc.j0 * cg.sx + bc.k0 * sxy;
 				unsigned ballots[kTiledRounds];
 				uint32_t cellOf[kTiledRounds];
 				uint32_t mine = 0;
@@ -294,9 +300,9 @@ namespace tg
 					const int t = r * kTiledThreads + (int)threadIdx.x;
 					bool active = false;
 					cellOf[r] = 0;
-					if (t < total)
+					const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+					if (t < total && x < bc.nx && y < bc.ny && z < bc.nz)
 					{
-						const int x = t % bc.nx, y = (t / bc.nx) % bc.ny, z = t / (bc.nx * bc.ny);
 						const float* b = box + (z * kTiledBox + y) * kTiledBox + x;
 						constexpr int dy = kTiledBox, dz = kTiledBox * kTiledBox;
 						const float v[8] = { b[0], b[1], b[dy + 1], b[dy], b[dz], b[dz + 1], b[dz + dy + 1], b[dz + dy] };
@@ -304,7 +310,7 @@ namespace tg
 #pragma unroll
 						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
 						active = pos != 0u && pos != 0xFFu;
-						const int64_t c = (bc.i0 + x) + (bc.j0 + y) * cg.sx + (bc.k0 + z) * cg.sx * cg.sy;
+						const int64_t c = c0 + x + y * cg.sx + z * sxy;
 						cellOf[r] = (uint32_t)c;
 						if (active) atomicOr(words + (c >> 5), 1u << (c & 31));
 					}
@@ -448,9 +454,12 @@ namespace tg
 		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((total + 31) / 32) * 4, stream);
 		if (e == cudaSuccess) e = cudaMemsetAsync(cell_count, 0, sizeof(uint32_t), stream);
 		if (e != cudaSuccess) return e;
-		if (B + 1 <= kTiledBox)
-			CellFlagsTiledKernel<<<sms * kCellPassCtasPerSm, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells,
-				cell_count);
+		if (B == kTiledBox - 1)
+			CellFlagsTiledKernel<kTiledBox - 1><<<sms * kCellPassCtasPerSm, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list,
+				count, words, cells, cell_count);
+		else if (B + 1 <= kTiledBox)
+			CellFlagsTiledKernel<0><<<sms * kCellPassCtasPerSm, kTiledThreads, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count,
+				words, cells, cell_count);
 		else
 			CellFlagsListedKernel<<<sms * kListedCtasPerSm, 128, 0, stream>>>(lattice, g, MakeBrickGrid(g, B), list, count, words, cells, cell_count);
 		return cudaGetLastError();
