@@ -98,8 +98,9 @@ namespace tg
 		TG_TRY(WordBase.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4 + 4));
+		TG_TRY(BrickBits.Reserve(VoxelBrickWords(s.IX, s.IY, s.IZ) * 4));
 		Begin("cloud_flags", st);
-		TG_TRY(LaunchCloudFlags(p.View, s, Words.As<uint32_t>(), st));
+		TG_TRY(LaunchCloudFlags(p.View, s, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), st));
 		End(st);
 		// The kept voxels' numbers in increasing order (bitmask -> scan -> list).
 		TG_TRY(Cubes.Reserve((size_t)(words ? words : 1) * 32 * 4));
@@ -147,8 +148,9 @@ namespace tg
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4 + 4));
 		TG_TRY(Cubes.Reserve((size_t)(words ? words : 1) * 32 * 4));
+		TG_TRY(BrickBits.Reserve(VoxelBrickWords(s.SX, s.SY, s.SZ) * 4));
 		Begin("vox_flags", st);
-		TG_TRY(LaunchVoxFlags(p.View, s, Words.As<uint32_t>(), st));
+		TG_TRY(LaunchVoxFlags(p.View, s, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), st));
 		End(st);
 		Begin("list_cells", st);
 		TG_TRY(LaunchListBricks(Words.As<uint32_t>(), s.Total, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), Cubes.As<uint32_t>(),

@@ -37,12 +37,96 @@ namespace tg
 			return r[0];
 		}
 
+		// Voxel bricks: 8^3 voxels whose tests are decided together when a bound proves that
+		// none of them can pass.  The distance functions are 1-Lipschitz (or the test is not
+		// made), so |f(c)| > r + threshold + margin at the centre c of the ball (radius r)
+		// through the brick's voxel centres means |f| > threshold at every one of them; the
+		// margin covers the rounding of f at c and at the voxel (as in the export's bricks).
+		constexpr int kVoxelBrick = 8;
+
+		struct VoxelBricks
+		{
+			int NX, NY, NZ;     // bricks per axis
+		};
+
+		__device__ __forceinline__ void BrickRange(int b, const VoxelBricks& vb, int sx, int sy, int sz, int (&lo)[3], int (&hi)[3])
+		{
+			const int bx = b % vb.NX, by = (b / vb.NX) % vb.NY, bz = b / (vb.NX * vb.NY);
+			lo[0] = bx * kVoxelBrick; hi[0] = min(lo[0] + kVoxelBrick - 1, sx - 1);
+			lo[1] = by * kVoxelBrick; hi[1] = min(lo[1] + kVoxelBrick - 1, sy - 1);
+			lo[2] = bz * kVoxelBrick; hi[2] = min(lo[2] + kVoxelBrick - 1, sz - 1);
+		}
+
+		__device__ __forceinline__ int BrickOfVoxel(int x, int y, int z, const VoxelBricks& vb)
+		{
+			return x / kVoxelBrick + vb.NX * (y / kVoxelBrick + vb.NY * (z / kVoxelBrick));
+		}
+
+		// The ball through the box [lo, hi] of voxel centres, and the margin for rounding.
+		__device__ __forceinline__ void BallOf(const float (&lo)[3], const float (&hi)[3], float (&c)[3], float& r, float& margin,
+			float scale)
+		{
+			float e2 = 0.0f;
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+			{
+				c[a] = 0.5f * (lo[a] + hi[a]);
+				const float e = 0.5f * (hi[a] - lo[a]);
+				e2 += e * e;
+			}
+			r = sqrtf(e2) * 1.0001f + 1e-6f;
+			margin = 1e-4f * (1.0f + fabsf(c[0]) + fabsf(c[1]) + fabsf(c[2]) + scale);
+		}
+
+		// One thread per brick of the point cloud's voxels: when the bricks' voxel centres
+		// all descend to one octree cell, that cell's program at the ball's centre decides.
+		__global__ void __launch_bounds__(128) CloudBricksKernel(DeviceProgram prog, CloudSpec s, VoxelBricks vb,
+			uint32_t* __restrict__ brick_bits)
+		{
+			extern __shared__ float spill[];
+			const int b = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+			if (b >= vb.NX * vb.NY * vb.NZ) return;
+			int lo[3], hi[3];
+			BrickRange(b, vb, s.IX, s.IY, s.IZ, lo, hi);
+			// Voxel centres float(i) * step + start + half: monotone in i.
+			float clo[3], chi[3];
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+			{
+				clo[a] = ((float)lo[a] * s.Step[a] + s.Start[a]) + s.Half[a];
+				chi[a] = ((float)hi[a] * s.Step[a] + s.Start[a]) + s.Half[a];
+			}
+			bool keep = true;
+			bool shared;
+			const int cell = DescendBox(prog.Nodes, clo[0], chi[0], clo[1], chi[1], clo[2], chi[2], shared);
+			const float clip = __ldg(&prog.Nodes[cell].ClipRadius);
+			if (shared && clip >= 0.0f && !(__ldg(&prog.Nodes[cell].Flags) & kNodeNoEvaluator))
+			{
+				float c[3], r, margin;
+				BallOf(clo, chi, c, r, margin, fabsf(__ldg(&prog.Nodes[0].ClipRadius)));
+				const float px[1] = { c[0] }, py[1] = { c[1] }, pz[1] = { c[2] };
+				float f[1];
+				RunDistance<1>(prog.Code, __ldg(&prog.Nodes[cell].DistanceCode), px, py, pz, f, spill + threadIdx.x, 128);
+				keep = !(fabsf(f[0]) > r + s.Diagonal + margin);
+			}
+			if (keep) atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
+		}
+
 		// abs(Octree->Eval(Cursor)) < Diagonal per voxel centre (export.cpp:404-423).
-		__global__ void __launch_bounds__(128) CloudFlagsKernel(DeviceProgram prog, CloudSpec s, uint32_t* __restrict__ words)
+		__global__ void __launch_bounds__(128) CloudFlagsKernel(DeviceProgram prog, CloudSpec s, VoxelBricks vb,
+			const uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ words)
 		{
 			const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
 			bool keep = false;
+			bool live = false;
 			if (t < s.Total)
+			{
+				const int i = (int)t;
+				const int slice = s.IX * s.IY;
+				const int b = BrickOfVoxel(i % s.IX, (i % slice) / s.IX, i / slice, vb);
+				live = (__ldg(brick_bits + (b >> 5)) >> (b & 31)) & 1u;
+			}
+			if (live)
 			{
 				const float d = OctreeDistance(prog, CloudCentre(s, (int)t));
 				keep = fabsf(d) < s.Diagonal;
@@ -124,25 +208,72 @@ namespace tg
 			return x * (1.0f - a) + y * a;
 		}
 
+		// VoxExport's voxel centre on one axis: mix(Min, Max, (x + .5) / Size), where
+		// vec3(x + .5, ...) converts the double sums to float.
+		__device__ __forceinline__ float VoxCentre(float lo, float hi, int x, int size)
+		{
+			return Mix(lo, hi, (float)((double)x + 0.5) / (float)size);
+		}
+
+		// One thread per brick of VoxExport's voxels: the whole tree's program at the centre
+		// of the ball through the brick's voxel centres decides (a tree with a brush that is
+		// not 1-Lipschitz keeps every brick).  mix() rounds each centre separately, so the
+		// box is widened by a relative 1e-6 of its coordinates.
+		__global__ void __launch_bounds__(128) VoxBricksKernel(DeviceProgram prog, VoxSpec s, VoxelBricks vb,
+			uint32_t* __restrict__ brick_bits)
+		{
+			extern __shared__ float spill[];
+			const int b = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+			if (b >= vb.NX * vb.NY * vb.NZ) return;
+			bool keep = true;
+			if (prog.Lipschitz)
+			{
+				int lo[3], hi[3];
+				BrickRange(b, vb, s.SX, s.SY, s.SZ, lo, hi);
+				const int size[3] = { s.SX, s.SY, s.SZ };
+				float clo[3], chi[3];
+#pragma unroll
+				for (int a = 0; a < 3; ++a)
+				{
+					const float u = VoxCentre(s.Min[a], s.Max[a], lo[a], size[a]);
+					const float v = VoxCentre(s.Min[a], s.Max[a], hi[a], size[a]);
+					const float slack = 1e-6f * (fabsf(u) + fabsf(v) + fabsf(s.Min[a]) + fabsf(s.Max[a]));
+					clo[a] = fminf(u, v) - slack;
+					chi[a] = fmaxf(u, v) + slack;
+				}
+				float c[3], r, margin;
+				BallOf(clo, chi, c, r, margin, fabsf(__ldg(&prog.Nodes[0].ClipRadius)));
+				const float px[1] = { c[0] }, py[1] = { c[1] }, pz[1] = { c[2] };
+				float f[1];
+				RunSurfaceBatch<1>(prog.Code, prog.FullSurfaceCode, px, py, pz, f, -1, nullptr, spill + threadIdx.x, 128);
+				keep = !(fabsf(f[0]) > r + s.Radius + margin);
+			}
+			if (keep) atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
+		}
+
 		// VoxExport's test (magica.cpp:52-64): the voxel centre mix(Min, Max, (x + .5) / Size)
 		// on the whole tree (SDFNode::Eval), kept when |d| <= Radius.
-		__global__ void __launch_bounds__(128) VoxFlagsKernel(DeviceProgram prog, VoxSpec s, uint32_t* __restrict__ words)
+		__global__ void __launch_bounds__(128) VoxFlagsKernel(DeviceProgram prog, VoxSpec s, VoxelBricks vb,
+			const uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ words)
 		{
 			extern __shared__ float spill[];
 			const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
 			bool keep = false;
+			int x = 0, y = 0, z = 0;
+			bool live = false;
 			if (t < s.Total)
 			{
 				const int i = (int)t;
 				const int slice = s.SX * s.SY;
-				const int z = i / slice, y = (i % slice) / s.SX, x = i % s.SX;
-				// vec3(x + .5, ...) converts the double sums to float.
-				const float ax = (float)((double)x + 0.5) / (float)s.SX;
-				const float ay = (float)((double)y + 0.5) / (float)s.SY;
-				const float az = (float)((double)z + 0.5) / (float)s.SZ;
-				const float px[1] = { Mix(s.Min[0], s.Max[0], ax) };
-				const float py[1] = { Mix(s.Min[1], s.Max[1], ay) };
-				const float pz[1] = { Mix(s.Min[2], s.Max[2], az) };
+				z = i / slice; y = (i % slice) / s.SX; x = i % s.SX;
+				const int b = BrickOfVoxel(x, y, z, vb);
+				live = (__ldg(brick_bits + (b >> 5)) >> (b & 31)) & 1u;
+			}
+			if (live)
+			{
+				const float px[1] = { VoxCentre(s.Min[0], s.Max[0], x, s.SX) };
+				const float py[1] = { VoxCentre(s.Min[1], s.Max[1], y, s.SY) };
+				const float pz[1] = { VoxCentre(s.Min[2], s.Max[2], z, s.SZ) };
 				float r[1];
 				RunSurfaceBatch<1>(prog.Code, prog.FullSurfaceCode, px, py, pz, r, -1, nullptr, spill + threadIdx.x, 128);
 				keep = fabsf(r[0]) <= s.Radius;
@@ -152,10 +283,43 @@ namespace tg
 		}
 	}
 
-	cudaError_t LaunchCloudFlags(const DeviceProgram& prog, const CloudSpec& s, uint32_t* words, cudaStream_t stream)
+	namespace
+	{
+		VoxelBricks BricksOf(int sx, int sy, int sz)
+		{
+			return { (sx + kVoxelBrick - 1) / kVoxelBrick, (sy + kVoxelBrick - 1) / kVoxelBrick, (sz + kVoxelBrick - 1) / kVoxelBrick };
+		}
+
+		size_t DistanceSpillBytes(const DeviceProgram& prog, int threads)
+		{
+			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+			return (size_t)depth * 2 * threads * sizeof(float);
+		}
+	}
+
+	size_t VoxelBrickWords(int sx, int sy, int sz)
+	{
+		const VoxelBricks vb = BricksOf(sx, sy, sz);
+		return ((size_t)vb.NX * vb.NY * vb.NZ + 31) / 32;
+	}
+
+	cudaError_t LaunchCloudFlags(const DeviceProgram& prog, const CloudSpec& s, uint32_t* brick_bits, uint32_t* words, cudaStream_t stream)
 	{
 		if (s.Total <= 0) return cudaSuccess;
-		CloudFlagsKernel<<<Blocks(s.Total, 128), 128, 0, stream>>>(prog, s, words);
+		const VoxelBricks vb = BricksOf(s.IX, s.IY, s.IZ);
+		const int nb = vb.NX * vb.NY * vb.NZ;
+		cudaError_t e = cudaMemsetAsync(brick_bits, 0, VoxelBrickWords(s.IX, s.IY, s.IZ) * 4, stream);
+		if (e != cudaSuccess) return e;
+		const size_t smem = DistanceSpillBytes(prog, 128);
+		if (smem > 48 * 1024)
+		{
+			e = cudaFuncSetAttribute(CloudBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		CloudBricksKernel<<<Blocks(nb, 128), 128, smem, stream>>>(prog, s, vb, brick_bits);
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+		CloudFlagsKernel<<<Blocks(s.Total, 128), 128, 0, stream>>>(prog, s, vb, brick_bits, words);
 		return cudaGetLastError();
 	}
 
@@ -167,17 +331,24 @@ namespace tg
 		return cudaGetLastError();
 	}
 
-	cudaError_t LaunchVoxFlags(const DeviceProgram& prog, const VoxSpec& s, uint32_t* words, cudaStream_t stream)
+	cudaError_t LaunchVoxFlags(const DeviceProgram& prog, const VoxSpec& s, uint32_t* brick_bits, uint32_t* words, cudaStream_t stream)
 	{
 		if (s.Total <= 0) return cudaSuccess;
-		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-		const size_t smem = (size_t)depth * 2 * 128 * sizeof(float);
+		const VoxelBricks vb = BricksOf(s.SX, s.SY, s.SZ);
+		const int nb = vb.NX * vb.NY * vb.NZ;
+		cudaError_t e = cudaMemsetAsync(brick_bits, 0, VoxelBrickWords(s.SX, s.SY, s.SZ) * 4, stream);
+		if (e != cudaSuccess) return e;
+		const size_t smem = DistanceSpillBytes(prog, 128);
 		if (smem > 48 * 1024)
 		{
-			cudaError_t e = cudaFuncSetAttribute(VoxFlagsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			e = cudaFuncSetAttribute(VoxFlagsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e == cudaSuccess) e = cudaFuncSetAttribute(VoxBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			if (e != cudaSuccess) return e;
 		}
-		VoxFlagsKernel<<<Blocks(s.Total, 128), 128, smem, stream>>>(prog, s, words);
+		VoxBricksKernel<<<Blocks(nb, 128), 128, smem, stream>>>(prog, s, vb, brick_bits);
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+		VoxFlagsKernel<<<Blocks(s.Total, 128), 128, smem, stream>>>(prog, s, vb, brick_bits, words);
 		return cudaGetLastError();
 	}
 }

@@ -179,13 +179,16 @@ namespace tg
 		int64_t Total;
 	};
 
+	// Both voxel tests first decide 8^3-voxel bricks with one bound each (bits in
+	// `brick_bits`, VoxelBrickWords of scratch), then test the voxels of the rest.
+	size_t VoxelBrickWords(int sx, int sy, int sz);
 	// One bit per voxel (cell number order): |octree distance at the centre| < Diagonal.
-	cudaError_t LaunchCloudFlags(const DeviceProgram& prog, const CloudSpec& s, uint32_t* words, cudaStream_t stream);
+	cudaError_t LaunchCloudFlags(const DeviceProgram& prog, const CloudSpec& s, uint32_t* brick_bits, uint32_t* words, cudaStream_t stream);
 	// Refined point of each listed cell (*count of them, at most `capacity`).
 	cudaError_t LaunchCloudRefine(const DeviceProgram& prog, const CloudSpec& s, const uint32_t* cells, const uint32_t* count,
 		uint32_t capacity, int iterations, float* points, cudaStream_t stream);
 	// One bit per voxel: |full-tree distance at the centre| <= Radius.
-	cudaError_t LaunchVoxFlags(const DeviceProgram& prog, const VoxSpec& s, uint32_t* words, cudaStream_t stream);
+	cudaError_t LaunchVoxFlags(const DeviceProgram& prog, const VoxSpec& s, uint32_t* brick_bits, uint32_t* words, cudaStream_t stream);
 }
 
 namespace tg
