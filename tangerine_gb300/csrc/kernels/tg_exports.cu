@@ -27,13 +27,14 @@ namespace tg
 			return Vec3(X, Y, Z) + Vec3(s.Half[0], s.Half[1], s.Half[2]);
 		}
 
-		__device__ __forceinline__ float OctreeDistance(const DeviceProgram& prog, Vec3 p)
+		// `spill`: this thread's column of the operand stack in shared memory (stride
+		// `stride`), as the interpreters lay it out.
+		__device__ __forceinline__ float OctreeDistance(const DeviceProgram& prog, Vec3 p, float* spill, int stride)
 		{
-			float spill[kMaxStack];
 			const float px[1] = { p.x }, py[1] = { p.y }, pz[1] = { p.z };
 			float r[1];
 			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
-			RunDistance<1>(prog.Code, __ldg(&prog.Nodes[cell].DistanceCode), px, py, pz, r, spill, 1);
+			RunDistance<1>(prog.Code, __ldg(&prog.Nodes[cell].DistanceCode), px, py, pz, r, spill, stride);
 			return r[0];
 		}
 
@@ -116,6 +117,7 @@ namespace tg
 		__global__ void __launch_bounds__(128) CloudFlagsKernel(DeviceProgram prog, CloudSpec s, VoxelBricks vb,
 			const uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ words)
 		{
+			extern __shared__ float spill[];
 			const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
 			bool keep = false;
 			bool live = false;
@@ -128,7 +130,7 @@ namespace tg
 			}
 			if (live)
 			{
-				const float d = OctreeDistance(prog, CloudCentre(s, (int)t));
+				const float d = OctreeDistance(prog, CloudCentre(s, (int)t), spill + threadIdx.x, 128);
 				keep = fabsf(d) < s.Diagonal;
 			}
 			const unsigned ballot = __ballot_sync(0xFFFFFFFFu, keep);
@@ -138,7 +140,7 @@ namespace tg
 		// SDFOctree::Gradient (the selected cell's SDFNode::Gradient, sdf_evaluator.cpp:298-333)
 		// at p: the four tetrahedral evaluations share one pass over the cell's surface
 		// program; the evaluation at p itself is needed only when they cancel.
-		__device__ __forceinline__ Vec3 OctreeGradient(const DeviceProgram& prog, Vec3 p, float* spill)
+		__device__ __forceinline__ Vec3 OctreeGradient(const DeviceProgram& prog, Vec3 p, float* spill, int stride)
 		{
 			const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
 			const int pc = __ldg(&prog.Nodes[cell].SurfaceCode);
@@ -151,7 +153,7 @@ namespace tg
 			}
 			float e[5];
 			float r4[4];
-			RunSurfaceBatch<4>(prog.Code, pc, px, py, pz, r4, -1, nullptr, spill, 1);
+			RunSurfaceBatch<4>(prog.Code, pc, px, py, pz, r4, -1, nullptr, spill, stride);
 #pragma unroll
 			for (int k = 0; k < 4; ++k) e[k] = r4[k];
 			e[4] = 0.0f;
@@ -165,7 +167,7 @@ namespace tg
 			{
 				const float qx[1] = { p.x }, qy[1] = { p.y }, qz[1] = { p.z };
 				float r1[1];
-				RunSurfaceBatch<1>(prog.Code, pc, qx, qy, qz, r1, -1, nullptr, spill, 1);
+				RunSurfaceBatch<1>(prog.Code, pc, qx, qy, qz, r1, -1, nullptr, spill, stride);
 				e[4] = r1[0];
 			}
 			return GradientOf(e);
@@ -176,6 +178,7 @@ namespace tg
 		__global__ void __launch_bounds__(128) CloudRefineKernel(DeviceProgram prog, CloudSpec s, const uint32_t* __restrict__ cells,
 			const uint32_t* __restrict__ count, int iterations, float* __restrict__ points)
 		{
+			extern __shared__ float spill[];
 			const uint32_t n = __ldg(count);
 			const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
 			if (v >= n) return;
@@ -184,13 +187,12 @@ namespace tg
 			Vec3 cursor = vertex;
 			if (iterations > 0)
 			{
-				float spill[kMaxStack * 5];
 				const Vec3 low = vertex - half, high = vertex + half;
 				for (int r = 0; r < iterations; ++r)
 				{
-					const Vec3 dir = OctreeGradient(prog, cursor, spill);
+					const Vec3 dir = OctreeGradient(prog, cursor, spill + threadIdx.x, 128);
 					// Octree->Eval(Cursor) * -1.0 rounds back to float exactly: a negation.
-					const float dist = -OctreeDistance(prog, cursor);
+					const float dist = -OctreeDistance(prog, cursor, spill + threadIdx.x, 128);
 					cursor = cursor + dir * dist;
 				}
 				cursor = TernaryMin(TernaryMax(cursor, low), high);
@@ -314,12 +316,13 @@ namespace tg
 		if (smem > 48 * 1024)
 		{
 			e = cudaFuncSetAttribute(CloudBricksKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e == cudaSuccess) e = cudaFuncSetAttribute(CloudFlagsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 			if (e != cudaSuccess) return e;
 		}
 		CloudBricksKernel<<<Blocks(nb, 128), 128, smem, stream>>>(prog, s, vb, brick_bits);
 		e = cudaGetLastError();
 		if (e != cudaSuccess) return e;
-		CloudFlagsKernel<<<Blocks(s.Total, 128), 128, 0, stream>>>(prog, s, vb, brick_bits, words);
+		CloudFlagsKernel<<<Blocks(s.Total, 128), 128, smem, stream>>>(prog, s, vb, brick_bits, words);
 		return cudaGetLastError();
 	}
 
@@ -327,7 +330,16 @@ namespace tg
 		uint32_t capacity, int iterations, float* points, cudaStream_t stream)
 	{
 		if (capacity == 0) return cudaSuccess;
-		CloudRefineKernel<<<Blocks(capacity, 128), 128, 0, stream>>>(prog, s, cells, count, iterations, points);
+		// The gradient's four-point surface pass: four distances and a material slot per
+		// depth (RunSurfaceBatch<4>'s layout), enough for the distance pass too.
+		const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+		const size_t smem = (size_t)depth * 5 * 128 * sizeof(float);
+		if (smem > 48 * 1024)
+		{
+			const cudaError_t e = cudaFuncSetAttribute(CloudRefineKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if (e != cudaSuccess) return e;
+		}
+		CloudRefineKernel<<<Blocks(capacity, 128), 128, smem, stream>>>(prog, s, cells, count, iterations, points);
 		return cudaGetLastError();
 	}
 
