@@ -116,3 +116,29 @@ def test_mesh_export_entry(lib, golden, tmp_path):
     for fmt, cloud, step in (("vox", False, 0.05), ("stl", True, 0.05), ("ply", False, (0.05, 0.06, 0.05))):
         with pytest.raises(_lib.TangerineError):
             sdf.mesh_export(t, tmp_path / "x", lo, hi, step, 0, fmt, point_cloud=cloud)
+
+
+def test_exports_of_a_tree_that_is_not_lipschitz(lib, port):
+    """An ellipsoid brush (its distance estimate is not 1-Lipschitz): the voxel bricks cannot
+    be rejected by a bound, so every voxel is tested, with the same voxels as the oracle."""
+    spec = np.array([W.ELLIPSOID, 0.5, 0.3, 0.2, W.ROTATE, 0.2, 0.3, 0.1, 0.927, W.PAINT, 1.0, 0.2, 0.1,
+                     W.SPHERE, 0.4, W.MOVE, 0.6, 0.1, 0.0, W.PAINT, 0.1, 0.9, 0.2, W.BLEND_UNION, 0.1], np.float32)
+    h = port.build(spec)
+    try:
+        want, size, radius = port.vox(h, 40.0, 7)
+        b = port.bounds(h)
+        o = port.octree(h)
+        try:
+            pts, cells = port.point_cloud(o, b[:3], b[3:], 0.02, 2)
+        finally:
+            port.octree_free(o)
+    finally:
+        port.free(h)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        vox, gsize, gradius = prog.export_voxels(40.0, 7)
+        m = prog.export_point_cloud(b[:3], b[3:], 0.02, 2)
+    assert want.shape[0] > 100 and pts.shape[0] > 100
+    np.testing.assert_array_equal(vox, want)
+    assert gsize == size
+    np.testing.assert_array_equal(m.cubes, cells.astype(np.uint32))
+    np.testing.assert_array_equal(m.vertices, pts)

@@ -203,3 +203,25 @@ def test_tree_whose_octants_all_clip_away_has_no_octree(lib, port):
         np.testing.assert_array_equal(a, b)
     a, b = C.c_double(), C.c_double()
     assert lib.tg_debug_compile_seconds(t.handle, 0, C.byref(a), C.byref(b)) == 2   # TG_ERR_UNBOUNDED
+
+
+def test_compiles_release_their_clipped_trees_whatever_the_order(lib):
+    """The octree's clipped trees borrow the nodes of the tree they were clipped from and
+    are released on a background thread after the compile: freeing the tree at once,
+    compiling trees back to back, and clipping a tree that is then freed all leave every
+    result intact (the host compile only: no device here)."""
+    a, b = C.c_double(), C.c_double()
+    for seed in range(12):
+        spec = W.random_tree(seed, 64 if seed % 2 else 16)
+        t = sdf.from_spec(spec)
+        want = t.eval(0.1, 0.2, 0.3)
+        for _ in range(3):
+            assert lib.tg_debug_compile_seconds(t.handle, seed % 2, C.byref(a), C.byref(b)) == 0
+        near = t.clip((0.1, 0.2, 0.3), 0.5)
+        dump = t.debug_octree()
+        del t                                    # the caller's tree goes first
+        if near is not None:
+            assert near.eval(0.1, 0.2, 0.3) == want   # an owned clip outlives its source
+        again = sdf.from_spec(spec).debug_octree()
+        for x, y in zip(dump, again):
+            np.testing.assert_array_equal(x, y)
