@@ -27,7 +27,6 @@ namespace tg
 		constexpr int kThreads = 128;
 		constexpr int kScanItems = 4;
 		constexpr uint64_t kBarrierLimitNs = 5000000000ull;    // 5 s
-		constexpr int kAttribPoints = kThreads / 5;            // 25 vertices x 5 evaluation lanes
 
 		__device__ __forceinline__ uint64_t Now()
 		{
@@ -347,43 +346,107 @@ namespace tg
 			if (!GridSync(s)) return;
 
 			// 4. Active cells of the kept bricks: bits, and an append list of global cell bits.
-			for (uint32_t item = blockIdx.x; item < kept; item += gridDim.x)
+			//    Bricks of at most 7^3 cells (every brick size the tuner picks) stage their
+			//    lattice box in shared memory and append their cells with one atomic.
 			{
-				const uint32_t gb = s.BrickList[item];
-				const int mi = ModelOf(s.BrickWord0, s.Count, (int64_t)(gb >> 5));
-				const BatchModel& m = s.Models[mi];
-				const uint32_t b = gb - (uint32_t)(m.BrickWord0 * 32);
-				const CellGeom cg = Geom(m.Grid);
-				const float* lat = s.Lattice + m.Lattice;
-				const int bx = (int)(b % (uint32_t)m.NBX), by = (int)((b / (uint32_t)m.NBX) % (uint32_t)m.NBY);
-				const int bz = (int)(b / ((uint32_t)m.NBX * (uint32_t)m.NBY));
-				const int64_t ci0 = (int64_t)bx * m.B, cj0 = (int64_t)by * m.B, ck0 = (int64_t)bz * m.B;
-				const int nx = (int)min((int64_t)m.B, cg.sx - ci0), ny = (int)min((int64_t)m.B, cg.sy - cj0);
-				const int nz = (int)min((int64_t)m.B, cg.sz - ck0);
-				const int total = nx * ny * nz;
-				for (int r0 = 0; r0 < total; r0 += kThreads)
+				__shared__ float box[8 * 8 * 8];
+				__shared__ uint32_t warpBase[kThreads / 32];
+				for (uint32_t item = blockIdx.x; item < kept; item += gridDim.x)
 				{
-					const int t = r0 + (int)threadIdx.x;
-					bool active = false;
-					int64_t c = 0;
-					if (t < total)
+					const uint32_t gb = s.BrickList[item];
+					const int mi = ModelOf(s.BrickWord0, s.Count, (int64_t)(gb >> 5));
+					const BatchModel& m = s.Models[mi];
+					const uint32_t b = gb - (uint32_t)(m.BrickWord0 * 32);
+					const CellGeom cg = Geom(m.Grid);
+					const float* lat = s.Lattice + m.Lattice;
+					const int bx = (int)(b % (uint32_t)m.NBX), by = (int)((b / (uint32_t)m.NBX) % (uint32_t)m.NBY);
+					const int bz = (int)(b / ((uint32_t)m.NBX * (uint32_t)m.NBY));
+					const int64_t ci0 = (int64_t)bx * m.B, cj0 = (int64_t)by * m.B, ck0 = (int64_t)bz * m.B;
+					const int nx = (int)min((int64_t)m.B, cg.sx - ci0), ny = (int)min((int64_t)m.B, cg.sy - cj0);
+					const int nz = (int)min((int64_t)m.B, cg.sz - ck0);
+					const int total = nx * ny * nz;
+					if (m.B <= 7)
 					{
-						const int64_t i = ci0 + t % nx, j = cj0 + (t / nx) % ny, k = ck0 + t / (nx * ny);
-						float v[8];
-						LoadCorners(lat, cg, i, j, k, v);
-						unsigned pos = 0;
+						__syncthreads();   // the previous brick is done with the box and the bases
+						for (int t = (int)threadIdx.x; t < 512; t += kThreads)
+						{
+							const int x = t & 7, y = (t >> 3) & 7, z = t >> 6;
+							if (x <= nx && y <= ny && z <= nz) box[t] = __ldg(lat + ((ck0 + z) * cg.ny + cj0 + y) * cg.nx + ci0 + x);
+						}
+						__syncthreads();
+						constexpr int kRounds = 3;   // 7^3 = 343 cells <= 3 x 128
+						unsigned ballots[kRounds];
+						uint64_t cellOf[kRounds];
+						uint32_t count = 0;
 #pragma unroll
-						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
-						active = pos != 0u && pos != 0xFFu;
-						c = i + j * cg.sx + k * cg.sx * cg.sy;
-						if (active) atomicOr(s.CellBits + m.CellWord0 + (c >> 5), 1u << (c & 31));
+						for (int r = 0; r < kRounds; ++r)
+						{
+							const int t = r * kThreads + (int)threadIdx.x;
+							bool active = false;
+							cellOf[r] = 0;
+							if (t < total)
+							{
+								const int x = t % nx, y = (t / nx) % ny, z = t / (nx * ny);
+								const float* q = box + (z * 8 + y) * 8 + x;
+								const float v[8] = { q[0], q[1], q[9], q[8], q[64], q[65], q[73], q[72] };
+								unsigned pos = 0;
+#pragma unroll
+								for (int k = 0; k < 8; ++k) pos |= (v[k] >= 0.0f ? 1u : 0u) << k;
+								active = pos != 0u && pos != 0xFFu;
+								const int64_t c = (ci0 + x) + (cj0 + y) * cg.sx + (ck0 + z) * cg.sx * cg.sy;
+								if (active) atomicOr(s.CellBits + m.CellWord0 + (c >> 5), 1u << (c & 31));
+								cellOf[r] = (uint64_t)m.CellWord0 * 32u + (uint64_t)c;
+							}
+							ballots[r] = __ballot_sync(0xFFFFFFFFu, active);
+							count += (uint32_t)__popc(ballots[r]);
+						}
+						if (lane == 0) warpBase[threadIdx.x >> 5] = count;
+						__syncthreads();
+						if (threadIdx.x == 0)
+						{
+							uint32_t counts[kThreads / 32], sum = 0;
+#pragma unroll
+							for (int w = 0; w < kThreads / 32; ++w) { counts[w] = warpBase[w]; sum += counts[w]; }
+							uint32_t at = sum ? atomicAdd(s.Counters + 1, sum) : 0u;
+#pragma unroll
+							for (int w = 0; w < kThreads / 32; ++w) { warpBase[w] = at; at += counts[w]; }
+						}
+						__syncthreads();
+						uint32_t at = warpBase[threadIdx.x >> 5];
+						const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+						for (int r = 0; r < kRounds; ++r)
+						{
+							const uint32_t slot = at + (uint32_t)__popc(ballots[r] & below);
+							if (((ballots[r] >> lane) & 1u) && slot < s.CapVertices) s.ActiveCells[slot] = cellOf[r];
+							at += (uint32_t)__popc(ballots[r]);
+						}
+						continue;
 					}
-					const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
-					uint32_t base = 0;
-					if (lane == 0 && ballot) base = atomicAdd(s.Counters + 1, (uint32_t)__popc(ballot));
-					base = __shfl_sync(0xFFFFFFFFu, base, 0);
-					const uint32_t at = base + __popc(ballot & ((1u << lane) - 1u));
-					if (active && at < s.CapVertices) s.ActiveCells[at] = (uint64_t)m.CellWord0 * 32u + (uint64_t)c;
+					for (int r0 = 0; r0 < total; r0 += kThreads)
+					{
+						const int t = r0 + (int)threadIdx.x;
+						bool active = false;
+						int64_t c = 0;
+						if (t < total)
+						{
+							const int64_t i = ci0 + t % nx, j = cj0 + (t / nx) % ny, k = ck0 + t / (nx * ny);
+							float v[8];
+							LoadCorners(lat, cg, i, j, k, v);
+							unsigned pos = 0;
+#pragma unroll
+							for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+							active = pos != 0u && pos != 0xFFu;
+							c = i + j * cg.sx + k * cg.sx * cg.sy;
+							if (active) atomicOr(s.CellBits + m.CellWord0 + (c >> 5), 1u << (c & 31));
+						}
+						const unsigned ballot = __ballot_sync(0xFFFFFFFFu, active);
+						uint32_t base = 0;
+						if (lane == 0 && ballot) base = atomicAdd(s.Counters + 1, (uint32_t)__popc(ballot));
+						base = __shfl_sync(0xFFFFFFFFu, base, 0);
+						const uint32_t at = base + __popc(ballot & ((1u << lane) - 1u));
+						if (active && at < s.CapVertices) s.ActiveCells[at] = (uint64_t)m.CellWord0 * 32u + (uint64_t)c;
+					}
 				}
 			}
 			if (!GridSync(s)) return;
@@ -470,50 +533,76 @@ namespace tg
 				}
 			}
 
-			// 9. Gradient normals and colours: five evaluation lanes per vertex.
+			// 9. Gradient normals (four lanes per vertex, one tetrahedral offset each, all
+			//    running the same code; the vertex itself only when the four cancel), then
+			//    colours (one thread per vertex of a painted model, GetMaterial's walk).
 			if (s.Attributes && vertexRoom)
 			{
-				__shared__ float evals[kThreads];
-				__shared__ int mats[kAttribPoints];
-				const int localPoint = threadIdx.x / 5, elane = threadIdx.x % 5;
-				for (int64_t first = (int64_t)blockIdx.x * kAttribPoints; first < vertices; first += (int64_t)gridDim.x * kAttribPoints)
+				constexpr int kNormalPoints = kThreads / 4;
+				const int localPoint = threadIdx.x >> 2, elane = threadIdx.x & 3;
+				const int groupFirst = (lane & ~3);
+				for (int64_t first = (int64_t)blockIdx.x * kNormalPoints; first < vertices; first += (int64_t)gridDim.x * kNormalPoints)
 				{
 					const int64_t v = first + localPoint;
-					const bool mine = localPoint < kAttribPoints && v < vertices;
-					int mi = 0;
+					const bool mine = v < vertices;
+					float e = 0.0f;
+					int mi = 0, pc = 0;
+					Vec3 p(0.0f, 0.0f, 0.0f);
 					if (mine)
 					{
 						mi = ModelOf(s.VertexBase, s.Count, (uint32_t)v);
 						const BatchModel& m = s.Models[mi];
-						const Vec3 p(s.Vertices[v * 3], s.Vertices[v * 3 + 1], s.Vertices[v * 3 + 2]);
+						p = Vec3(s.Vertices[v * 3], s.Vertices[v * 3 + 1], s.Vertices[v * 3 + 2]);
 						const int cell = DescendOctree(m.Prog.Nodes, p.x, p.y, p.z);
-						const int pc = __ldg(&m.Prog.Nodes[cell].SurfaceCode);
+						pc = __ldg(&m.Prog.Nodes[cell].SurfaceCode);
 						const Vec3 q = TetraPoint(p, elane);
 						const float px[1] = { q.x }, py[1] = { q.y }, pz[1] = { q.z };
-						float e[1];
-						int mat = -1;
-						RunSurfaceBatch<1, false>(m.Prog.Code, pc, px, py, pz, e, (elane == 4 && m.HasPaint) ? 0 : -1, &mat, spill + threadIdx.x, kThreads);
-						evals[threadIdx.x] = e[0];
-						if (elane == 4) mats[localPoint] = mat;
+						float r[1];
+						RunSurfaceBatch<1, false>(m.Prog.Code, pc, px, py, pz, r, -1, nullptr, spill + threadIdx.x, kThreads);
+						e = r[0];
 					}
-					__syncthreads();
+					float ev[5];
+#pragma unroll
+					for (int j = 0; j < 4; ++j) ev[j] = __shfl_sync(0xFFFFFFFFu, e, groupFirst + j);
 					if (mine && elane == 0)
 					{
 						const BatchModel& m = s.Models[mi];
-						const Vec3 g = GradientOf(evals + localPoint * 5);
-						s.Normals[v * 3 + 0] = g.x;
-						s.Normals[v * 3 + 1] = g.y;
-						s.Normals[v * 3 + 2] = g.z;
-						if (m.HasPaint)
+						ev[4] = 0.0f;
+						const float h = 0.0001f;
+						const Vec3 xyy(h, -h, -h), yyx(-h, -h, h), yxy(-h, h, -h), xxx(h, h, h);
+						Vec3 g = xyy * ev[0];
+						g = g + yyx * ev[1];
+						g = g + yxy * ev[2];
+						g = g + xxx * ev[3];
+						if ((g.x * g.x + g.y * g.y) + g.z * g.z == 0.0f)
 						{
-							const int mt = mats[localPoint];
-							const uchar4 c = mt >= 0 ? m.Prog.Colors[mt] : make_uchar4(255, 255, 255, 255);
-							s.Colors[v * 3 + 0] = c.x;
-							s.Colors[v * 3 + 1] = c.y;
-							s.Colors[v * 3 + 2] = c.z;
+							const float qx[1] = { p.x }, qy[1] = { p.y }, qz[1] = { p.z };
+							float r[1];
+							RunSurfaceBatch<1, false>(m.Prog.Code, pc, qx, qy, qz, r, -1, nullptr, spill + threadIdx.x, kThreads);
+							ev[4] = r[0];
 						}
+						const Vec3 n = GradientOf(ev);
+						s.Normals[v * 3 + 0] = n.x;
+						s.Normals[v * 3 + 1] = n.y;
+						s.Normals[v * 3 + 2] = n.z;
 					}
-					__syncthreads();
+				}
+				for (int64_t v = gtid; v < vertices; v += gthreads)
+				{
+					const int mi = ModelOf(s.VertexBase, s.Count, (uint32_t)v);
+					const BatchModel& m = s.Models[mi];
+					if (!m.HasPaint) continue;
+					const Vec3 p(s.Vertices[v * 3], s.Vertices[v * 3 + 1], s.Vertices[v * 3 + 2]);
+					const int cell = DescendOctree(m.Prog.Nodes, p.x, p.y, p.z);
+					const int pc = __ldg(&m.Prog.Nodes[cell].SurfaceCode);
+					const float px[1] = { p.x }, py[1] = { p.y }, pz[1] = { p.z };
+					float r[1];
+					int mt = -1;
+					RunSurfaceBatch<1, false>(m.Prog.Code, pc, px, py, pz, r, 0, &mt, spill + threadIdx.x, kThreads);
+					const uchar4 c = mt >= 0 ? m.Prog.Colors[mt] : make_uchar4(255, 255, 255, 255);
+					s.Colors[v * 3 + 0] = c.x;
+					s.Colors[v * 3 + 1] = c.y;
+					s.Colors[v * 3 + 2] = c.z;
 				}
 			}
 		}
