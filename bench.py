@@ -380,7 +380,11 @@ def our_arm(args, rank, world, local_rank):
     tree = sdf.from_spec(spec)
     prog = sdf.compile(tree)
     info = prog.info()
-    stream = torch.cuda.current_stream()
+    # One non-default stream for everything: the L2 flush, the CUDA events and the
+    # library's work (a null stream would send the library to its own stream, where the
+    # flush and the events would not be ordered with the work they bracket).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     lib = _lib.load()
 
@@ -572,7 +576,11 @@ def render_arm(args, rank, world, local_rank):
     poses = W.camera_poses(5, poses_n, radius=4.0)
     cams = sdf.cameras(poses, fov_y_degrees=60.0)
     lib = _lib.load()
-    stream = torch.cuda.current_stream()
+    # One non-default stream for everything: the L2 flush, the CUDA events and the
+    # library's work (a null stream would send the library to its own stream, where the
+    # flush and the events would not be ordered with the work they bracket).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     px = width * height
     depth = torch.empty(poses_n * px, dtype=torch.float32, device="cuda")
@@ -718,7 +726,11 @@ def batch_arm(args, rank, world, local_rank):
     progs = [p for p, _ in built]
     grids = [g for _, g in built]
     samples = int(sum(g.corners for g in grids))
-    stream = torch.cuda.current_stream()
+    # One non-default stream for everything: the L2 flush, the CUDA events and the
+    # library's work (a null stream would send the library to its own stream, where the
+    # flush and the events would not be ordered with the work they bracket).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     batch = sdf.Batch(progs, grids)
@@ -841,7 +853,11 @@ def surrogate_arm(args, rank, world, local_rank):
     grid = W.export_grid(resolution=res)
     samples = grid.corners
     prog = sdf.compile(sdf.from_spec(spec))
-    stream = torch.cuda.current_stream()
+    # One non-default stream for everything: the L2 flush, the CUDA events and the
+    # library's work (a null stream would send the library to its own stream, where the
+    # flush and the events would not be ordered with the work they bracket).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
