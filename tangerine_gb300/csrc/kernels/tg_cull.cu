@@ -26,10 +26,11 @@ namespace tg
 	{
 		constexpr int kClassifyThreads = 128;
 		constexpr int kBrickThreads = 128;     // 8 x 8 columns x 2 z-groups of 4 points
-		// Resident CTAs per SM the brick evaluation is compiled for.  For 7^3-cell bricks
-		// (48 registers a thread) the 512^3 export measured 0.65 ms at 8 (64 registers),
-		// 0.58 at 9, 0.56 at 10, 0.66 at 12 (spills); larger bricks keep 8.
-		template<int C> constexpr int EvalBricksCtasPerSm() { return C == 8 ? 10 : 8; }
+		// Resident CTAs per SM the brick evaluation is compiled for (48 registers a thread).
+		// 7^3-cell bricks, 512^3 export: 0.65 ms at 8 (64 registers), 0.58 at 9, 0.56 at 10,
+		// 0.66 at 12 (spills).  32^3-cell bricks, 1024^3 export: 56.1 -> 63.3 G samples/s
+		// (network-culled) from 8 to 10.
+		template<int C> constexpr int EvalBricksCtasPerSm() { return 10; }
 		constexpr int kCellPassCtasPerSm = 16;
 		constexpr int kListedCtasPerSm = 8;
 
