@@ -763,11 +763,14 @@ namespace tg
 
 	void CompiledTree::CopyCode(float* dst) const
 	{
-		for (const auto& c : CodeChunks)
-		{
-			std::memcpy(dst, c.data(), c.size() * sizeof(float));
-			dst += c.size();
-		}
+		// The chunks to their offsets on the worker pool when there is enough to copy (a
+		// 256-primitive tree's program image is about 2.5 MB).
+		std::vector<size_t> at(CodeChunks.size());
+		size_t off = 0;
+		for (size_t i = 0; i < CodeChunks.size(); ++i) { at[i] = off; off += CodeChunks[i].size(); }
+		auto copy = [&](int i) { std::memcpy(dst + at[(size_t)i], CodeChunks[(size_t)i].data(), CodeChunks[(size_t)i].size() * sizeof(float)); };
+		if (off * sizeof(float) >= ((size_t)1 << 20)) WorkerPool::Get().ParallelFor((int)CodeChunks.size(), copy);
+		else for (size_t i = 0; i < CodeChunks.size(); ++i) copy((int)i);
 	}
 
 	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind)
