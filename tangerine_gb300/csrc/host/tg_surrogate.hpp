@@ -1,6 +1,6 @@
 // Learned distance bound of one tree: a hash-grid network (kernels in tg_field.cu) trained
 // on distances the exact whole-tree program produces, then used to skip export bricks.
-// The exact program stays the judge: every kept brick is evaluated exactly, and the
+// The exact program has the last word: every kept brick is evaluated exactly, and the
 // network's error on held-out samples sets the safety margin of every skip.
 #pragma once
 
