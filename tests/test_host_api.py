@@ -225,3 +225,21 @@ def test_compiles_release_their_clipped_trees_whatever_the_order(lib):
         again = sdf.from_spec(spec).debug_octree()
         for x, y in zip(dump, again):
             np.testing.assert_array_equal(x, y)
+
+
+def test_process_exits_cleanly_with_releases_pending(lib):
+    """Compiles hand their octrees to a background release thread; a process that exits
+    right after compiling must still exit at once and cleanly (the pool joins its threads
+    after running what is queued)."""
+    import subprocess
+    import sys
+    code = ("import ctypes as C, sys; sys.path.insert(0, %r)\n"
+            "from tangerine_gb300 import _lib, sdf, workloads as W\n"
+            "lib = _lib.load(); a, b = C.c_double(), C.c_double()\n"
+            "for s in range(8):\n"
+            "    t = sdf.from_spec(W.random_tree(s, 128))\n"
+            "    assert lib.tg_debug_compile_seconds(t.handle, 0, C.byref(a), C.byref(b)) == 0\n"
+            "print('ok')\n") % str(ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().endswith("ok")
