@@ -151,6 +151,35 @@ def test_full_size_export_properties(lib, port):
         port.free(h)
 
 
+def test_full_size_mesh_matches_oracle(lib, port):
+    """The headline export in full: 256-primitive tree (seed 1) on the 512^3 export grid
+    (515^3 lattice points).  Every lattice distance, every vertex (in the reference's serial
+    order), cube index, face, normal and colour byte of the GPU's culled export against the
+    oracle's surface nets (FirstLoopInnerThunk / SecondLoopThunk, surface_nets.cpp:864-1121)
+    and its per-vertex Gradient + GetMaterial (export.cpp:283-317) on all host cores."""
+    spec = W.random_tree(1, 256)
+    grid = W.export_grid(resolution=512)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        m = prog.export_mesh(grid)
+        lat = prog.eval_grid(grid)
+    h = port.build(spec)
+    o = port.octree(h)
+    try:
+        np.testing.assert_array_equal(lat, port.octree_grid(o, grid))
+        del lat
+        want = port.surface_nets(o, grid)
+        assert want.vertices.shape[0] > 1000000
+        np.testing.assert_array_equal(m.vertices, want.vertices)
+        np.testing.assert_array_equal(m.cubes.astype(np.uint64), want.cubes)
+        np.testing.assert_array_equal(sorted_faces(m.faces), sorted_faces(want.faces))
+        normals, colors = port.vertex_attributes(o, want.vertices)
+        np.testing.assert_array_equal(m.normals, normals)
+        np.testing.assert_array_equal(m.colors, colors)
+    finally:
+        port.octree_free(o)
+        port.free(h)
+
+
 @pytest.mark.parametrize("brick", [1, 4, 7, 15])
 def test_culled_export_equals_dense_export(lib, brick):
     """Brick culling skips only bricks that provably hold no surface: same mesh, bit for bit."""

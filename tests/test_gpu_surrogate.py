@@ -2,9 +2,16 @@
 tensor-core operand layouts, forward pass, gradients, the Adam step, and a trained
 network culling export bricks without changing the mesh.
 
-Tolerances: the kernels accumulate in FP32 where the oracle uses float64, so a BF16
-rounding of an input or activation can land on the other side of a rounding boundary
-now and then; comparisons bound the worst case loosely and the typical case tightly."""
+Tolerances.  The oracle rounds to BF16 at exactly the places the kernels do (inputs,
+hidden activations, the backward pass's dZ, every weight) and accumulates in float64 where
+the tensor cores accumulate in FP32.  The two sums of one product therefore differ by a
+few FP32 ulps, which is what the typical error shows (median 1-2e-8, p99 about 1e-7 of the
+output scale, measured on a GB300).  Now and then such a difference straddles a BF16
+rounding boundary of the next layer's input, and that activation then moves by one BF16
+ulp (2^-8 relative): about 1 output in 10^4 is off by up to 2e-3 of the scale.  The bounds
+below are those figures with room to spare: the bulk is held to FP32 accuracy, and only
+the rare BF16 flips may reach the max bound.  Gradient sums add many such products, so
+their relative error stays near 3e-5 (bound 2e-4)."""
 
 import numpy as np
 import pytest
@@ -57,9 +64,11 @@ def test_forward_matches_oracle(lib):
     got = s.eval(pts)
     want = S.forward(grid, table, mlp, pts)["s"]
     scale = np.abs(want).max()
-    err = np.abs(got - want)
-    assert err.max() <= 2e-2 * scale, (err.max(), scale)
-    assert np.median(err) <= 1e-4 * scale, (np.median(err), scale)
+    err = np.abs(got - want) / scale
+    assert np.median(err) <= 1e-7, np.median(err)
+    assert np.quantile(err, 0.99) <= 1e-6, np.quantile(err, 0.99)
+    assert np.mean(err > 1e-5) <= 2e-3, np.mean(err > 1e-5)      # BF16 flips only
+    assert err.max() <= 5e-3, err.max()
     s.close()
 
 
@@ -70,14 +79,14 @@ def test_gradients_match_oracle(lib):
     smp = np.concatenate([rng.uniform(-2, 2, (n, 3)), rng.uniform(-0.8, 0.8, (n, 1))], 1).astype(np.float32)
     gt, gm, loss = s.gradients(smp)
     rt, rm, rloss = S.gradients(grid, table, mlp, smp)
-    assert abs(loss - rloss) <= 1e-3 * rloss
+    assert abs(loss - rloss) <= 1e-5 * rloss
     for name, lo, hi in (("W1", S.W1, S.B1), ("b1", S.B1, S.W2), ("W2", S.W2, S.B2), ("b2", S.B2, S.W3),
                          ("W3", S.W3, S.B3), ("b3", S.B3, S.W4), ("W4", S.W4, S.B4), ("b4", S.B4, S.PARAMS)):
         ref = rm[lo:hi]
         rel = np.linalg.norm(gm[lo:hi] - ref) / max(np.linalg.norm(ref), 1e-30)
-        assert rel <= 2e-2, (name, rel)
+        assert rel <= 2e-4, (name, rel)
     rel = np.linalg.norm(gt - rt) / np.linalg.norm(rt)
-    assert rel <= 2e-2, rel
+    assert rel <= 2e-4, rel
     # Only the corners the samples touch receive gradient.
     assert np.array_equal(gt != 0, rt != 0) or np.mean((gt != 0) != (rt != 0)) < 1e-4
     s.close()
@@ -123,8 +132,9 @@ def test_trained_bound_culls_bricks_and_keeps_the_mesh(lib):
         np.testing.assert_array_equal(m.normals, dense.normals)
         np.testing.assert_array_equal(m.colors, dense.colors)
     assert kept < 0.5 * bricks, (kept, bricks)
-    # With the exact test after it, the network can only remove bricks from the exact set.
-    assert kept_refined <= kept_exact, (kept_refined, kept_exact)
+    # With the exact test after it, the network can only remove bricks from the exact set,
+    # and it must remove some: that is its gain over the exact test alone.
+    assert kept_refined < kept_exact, (kept_refined, kept_exact)
 
 
 def test_network_steps_render_matches_exact(lib):
@@ -148,3 +158,46 @@ def test_network_steps_render_matches_exact(lib):
     same_colour = np.all(c_exact[both] == c_net[both], axis=-1)
     assert np.mean(same_colour) >= 0.95
     assert net_steps > 0 and exact_steps > 0
+
+
+def test_surrogate_export_1024_matches_dense_and_oracle(lib, port):
+    """The surrogate-culled workload: the 256-primitive tree (seed 1) on the 1024^3 export
+    grid in 32^3 bricks, network + exact test.  The mesh equals the dense GPU export bit
+    for bit (zero topology differences, Hausdorff 0); sampled vertices are recomputed from
+    the oracle's corner distances, and their normals and colours taken from the oracle."""
+    from test_gpu_parity import CORNERS, lattice_points, vertices_from_corners
+    spec = W.random_tree(1, 256)
+    grid = W.export_grid(resolution=1024)
+    rng = np.random.RandomState(3)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        with sdf.Surrogate() as s:
+            info = s.fit(prog)
+            assert info.max_error < 0.1
+            culled = s.export_mesh(prog, grid, brick=32)
+            bricks, kept = sdf.last_export_stats()
+        exact = prog.export_mesh(grid, brick=32)
+        _, kept_exact = sdf.last_export_stats()
+        dense = prog.export_mesh(grid, dense=True)
+    assert kept < kept_exact < bricks, (kept, kept_exact, bricks)
+    for a, b in ((culled.vertices, dense.vertices), (culled.cubes, dense.cubes), (culled.faces, dense.faces),
+                 (culled.normals, dense.normals), (culled.colors, dense.colors), (exact.vertices, dense.vertices),
+                 (exact.faces, dense.faces)):
+        np.testing.assert_array_equal(a, b)
+    h = port.build(spec)
+    o = port.octree(h)
+    try:
+        V = culled.vertices.shape[0]
+        sample = rng.choice(V, 20000, replace=False)
+        c = culled.cubes.astype(np.int64)[sample]
+        i, j, k = c % grid.sx, (c // grid.sx) % grid.sy, c // (grid.sx * grid.sy)
+        corner_vals = np.stack([port.octree_eval(o, lattice_points(grid, i + dx, j + dy, k + dz))
+                                for dx, dy, dz in CORNERS], 1)
+        pos = corner_vals >= 0
+        assert np.all(pos.any(1) & ~pos.all(1))
+        np.testing.assert_array_equal(culled.vertices[sample], vertices_from_corners(grid, i, j, k, corner_vals))
+        normals, colors = port.vertex_attributes(o, culled.vertices[sample])
+        np.testing.assert_array_equal(culled.normals[sample], normals)
+        np.testing.assert_array_equal(culled.colors[sample], colors)
+    finally:
+        port.octree_free(o)
+        port.free(h)
