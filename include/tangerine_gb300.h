@@ -107,16 +107,20 @@ enum
 	TG_ERR_MEMORY = 4,       /* host or device allocation failed */
 	TG_ERR_IO = 5,           /* file could not be written */
 	TG_ERR_UNSUPPORTED = 6,  /* input outside what the kernels handle */
+	TG_ERR_CANCELLED = 7,    /* stopped by CancelExport(true) or tg_batch_cancel */
+	TG_ERR_BUSY = 8,         /* an asynchronous export is still running */
 };
 
 typedef struct tg_program tg_program;
 
-/* Lattice of sample points x0 + i*step (i < nx), likewise y, z; x varies fastest. */
+/* Lattice of sample points x0 + i*step (i < nx), y0 + j*step_y, z0 + k*step_z; x varies
+ * fastest.  step_y / step_z of 0 mean `step` (one step for every axis). */
 typedef struct tg_grid
 {
 	float x0, y0, z0;
 	float step;
 	int64_t nx, ny, nz;
+	float step_y, step_z;
 } tg_grid;
 
 typedef struct tg_program_info
@@ -201,6 +205,9 @@ TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* 
 /* The lattice MeshExportThread builds for (min, max, step): min moves down two steps;
  * ceil((max - min) / step) cells, one more lattice point, per axis (export.cpp:324-337). */
 TANGERINE_API tg_status tg_export_grid(const float model_min[3], const float model_max[3], float step, tg_grid* out);
+/* The same with a step per axis, as MeshExportThread's vec3 Step. */
+TANGERINE_API tg_status tg_export_grid_axes(const float model_min[3], const float model_max[3], const float step[3],
+                                            tg_grid* out);
 
 /* SDFOctree::Eval(p, Exact = true) at every lattice point.  `out` holds nx*ny*nz floats,
  * host memory, or device memory when out_is_device is nonzero. */
@@ -221,20 +228,31 @@ TANGERINE_API void tg_mesh_free(tg_mesh* mesh);
  * cannot absorb cudaMalloc's device-wide synchronisation).  No counterpart in the
  * reference: Tangerine's export runs on the CPU and allocates freely.
  *
- * Same kernels and the same results as tg_export_mesh, but nothing is allocated: the
- * outputs are the caller's device buffers (vertices and normals 3 floats per vertex,
+ * The results equal tg_export_mesh's bit for bit, but this path always runs the dense
+ * kernels: every lattice point is evaluated, as the reference does, with no brick culling
+ * (at 128^3 that is several times the culled export's device time).  Nothing is allocated:
+ * the outputs are the caller's device buffers (vertices and normals 3 floats per vertex,
  * colors 3 bytes per vertex, faces 3 uint32 per face, cubes 1 uint32 per vertex) and the
  * scratch (lattice, active-cell bitmask, prefix sums) lives in one fixed 64 MiB device
- * array inside the library -- about a 240^3 lattice at most.  Larger inputs fail with
- * TG_ERR_UNSUPPORTED; too small an output capacity fails with TG_ERR_INVALID after
- * counts[0] (vertices) / counts[1] (faces) report the size needed.  `normals` may be NULL
- * without TG_MESH_ATTRIBUTES, `colors` when the tree has no paint.
- *  - Every GPU that loads the library holds the 64 MiB array until the process exits.
- *  - The first call on a device looks up the array's address (cudaGetSymbolAddress with
- *    that device current); make that first call before any stream capture.
+ * array inside the library -- about a 240^3 lattice at most.
+ *  - flags: TG_MESH_ATTRIBUTES (normals and colours) and TG_MESH_DENSE (a no-op here); any
+ *    other bit fails with TG_ERR_UNSUPPORTED.  `normals` may be NULL without
+ *    TG_MESH_ATTRIBUTES, `colors` when the tree has no paint.
+ *  - Larger lattices fail with TG_ERR_UNSUPPORTED.  Too small a vertex capacity fails with
+ *    TG_ERR_INVALID and counts[0] = the vertices needed (counts[1] stays 0: the face count
+ *    is known only once the vertices fit); too small a face capacity fails with
+ *    TG_ERR_INVALID and counts[1] = the faces needed.
+ *  - The array is part of a CUDA module that loads lazily: a device reserves the 64 MiB
+ *    the first time this function runs on it, and holds them until the process exits.
+ *    Calling it with every pointer NULL only does that set-up on the current device
+ *    (looks up the array's address with cudaGetSymbolAddress and caches it).  Make that
+ *    first call before giving the rest of device memory to a pool, and before any stream
+ *    capture.  cudaDeviceReset is not supported while the library is in use (the cached
+ *    address would be stale).
  *  - All calls share the array, which keeps the last call's contents.  Calls that overlap
  *    on the GPU (several threads or streams at once) race on it: serialise them.
- *  - stream NULL is the default stream. */
+ *  - stream NULL is the legacy default stream here (the other entry points take NULL as
+ *    the library's own stream). */
 TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, const tg_grid* grid, uint32_t flags,
                                                float* vertices, float* normals, uint8_t* colors, uint32_t* faces,
                                                uint32_t* cubes, uint64_t vertex_capacity, uint64_t face_capacity,
@@ -319,13 +337,43 @@ TANGERINE_API tg_status tg_write_vox(const tg_voxels* voxels, const char* path);
 /* ExportMagicaVoxel (magica.cpp:79-83, shipped disabled): voxelise the tree and write the
  * file, synchronously. */
 TANGERINE_API void ExportMagicaVoxel(void* Handle, float GridSize, int ColorIndex, const char* Path);
-/* MeshExport (export.h:37, export.cpp:566-580) synchronously: Format 0 = STL, 1 = PLY, as
+/* MeshExport (export.h:37, export.cpp:566-580): starts the export on a detached host
+ * thread and returns at once, as the reference does.  Format 0 = STL, 1 = PLY, as
  * ExportFormat; ExportPointCloud selects the point-cloud export (PLY only, as the reference
- * writes nothing else for it).  Vertices are multiplied by Scale when written.  The mesh
- * export takes one step for all axes here (TG_ERR_UNSUPPORTED otherwise); RefineIterations
- * applies to point clouds only, as in the reference. */
+ * writes nothing else for it).  Vertices are multiplied by Scale when written.  Step is
+ * per axis; RefineIterations applies to point clouds only, as in the reference.
+ * Arguments are checked before the thread starts (a bad format returns TG_ERR_UNSUPPORTED
+ * and starts nothing); one export runs at a time (TG_ERR_BUSY while one is running).  The
+ * job's own outcome comes from tg_export_result; its progress from GetExportProgress. */
 TANGERINE_API tg_status MeshExport(void* Handle, const char* Path, const float ModelMin[3], const float ModelMax[3],
                                    const float Step[3], int RefineIterations, int Format, bool ExportPointCloud, float Scale);
+
+/* ExportProgress (export.h:27-34), as GetExportProgress (export.cpp:483-492) fills it.
+ * Stage: 0 idle or finished, 1 generation (octree, lattice and surface nets, or the
+ * point cloud's voxel search), 2 refinement (point clouds), 3 vertex attributes and the
+ * file write.  Each fraction runs from 0 to 1 over its stage; the GPU finishes a stage in
+ * milliseconds, so they advance by whole phases (the reference counts single cells). */
+typedef struct ExportProgress
+{
+	int Stage;
+	float Generation;
+	float Refinement;
+	float Secondary;
+	float Write;
+} ExportProgress;
+
+TANGERINE_API ExportProgress GetExportProgress(void);
+/* CancelExport (export.cpp:582-592).  Halt = true stops the running export at its next
+ * phase boundary: no file is written (a partly written file is removed) and the job ends
+ * with TG_ERR_CANCELLED.  The reference instead goes on to write whatever part of the mesh
+ * it had.  Halt = false is the reference's "good enough": it ends the current stage early
+ * -- for a point cloud, the refinement is skipped when pressed before or during it; a mesh
+ * export has no partial stage result and goes on. */
+TANGERINE_API void CancelExport(bool Halt);
+/* Outcome of the last MeshExport job: with wait != 0, blocks until it has finished; with
+ * wait == 0, TG_ERR_BUSY while it runs.  TG_OK when no job ran.  On failure the job's
+ * message becomes this thread's tg_last_error. */
+TANGERINE_API tg_status tg_export_result(int wait);
 
 /* SDFNode::RayMarch (sdf_evaluator.cpp:336-353) on the whole tree for n rays, on the GPU:
  * the reference's step sequence, so hit flags, travel (+inf on a miss) and end positions
@@ -437,6 +485,19 @@ TANGERINE_API tg_status tg_batch_autotune(tg_batch* batch, void* stream);
 TANGERINE_API tg_status tg_batch_set_tuning(tg_batch* batch, const int* brick_edges, const int* lanes);
 TANGERINE_API tg_status tg_batch_get_tuning(const tg_batch* batch, int* brick_edges, int* lanes);
 TANGERINE_API tg_status tg_batch_run(tg_batch* batch, void* stream);
+/* Cancels a batch run from any thread (cancel = 1), as CancelExport(true) does for the
+ * single export: the persistent kernel reads a host-mapped flag at each of its grid
+ * barriers, every block leaves after the first barrier that sees it, and tg_batch_run
+ * returns TG_ERR_CANCELLED (the outputs are incomplete) and clears the flag.  A cancel that
+ * comes after the running batch's last barrier cancels the next run instead; cancel = 0
+ * withdraws it. */
+TANGERINE_API tg_status tg_batch_cancel(tg_batch* batch, int cancel);
+/* Test hook for the persistent kernel's grid barrier: its wait limit (limit_ns; 0 = the
+ * default 5 s, else 1 ms..60 s) and one block (late_block; -1 = none) that starts late_ns
+ * late (at most 2 s).  With a late start longer than the limit, the other blocks' first
+ * wait runs out: every block leaves and tg_batch_run returns TG_ERR_CUDA ("timed out"),
+ * the GPU context stays usable, and the next run (knobs back at 0, -1, 0) is whole. */
+TANGERINE_API tg_status tg_batch_debug_barrier(tg_batch* batch, uint64_t limit_ns, int late_block, uint64_t late_ns);
 /* Output capacity for the next run (default: an estimate from the lattices); a run that
  * finds more vertices or faces grows the buffers and runs again (tg_batch_info.reruns). */
 TANGERINE_API tg_status tg_batch_reserve(tg_batch* batch, uint64_t vertices, uint64_t faces);

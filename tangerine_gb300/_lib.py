@@ -20,7 +20,7 @@ class RayHit(C.Structure):
 
 class Grid(C.Structure):
     _fields_ = [("x0", C.c_float), ("y0", C.c_float), ("z0", C.c_float), ("step", C.c_float),
-                ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64)]
+                ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64), ("step_y", C.c_float), ("step_z", C.c_float)]
 
 
 class Camera(C.Structure):
@@ -75,6 +75,11 @@ class Drawable(C.Structure):
                 ("grid_cells", C.c_int64 * 3), ("compile_seconds", C.c_double), ("gpu_seconds", C.c_double)]
 
 
+class ExportProgress(C.Structure):
+    _fields_ = [("Stage", C.c_int), ("Generation", C.c_float), ("Refinement", C.c_float), ("Secondary", C.c_float),
+                ("Write", C.c_float)]
+
+
 class Voxels(C.Structure):
     _fields_ = [("count", C.c_uint64), ("voxels", C.POINTER(C.c_int32)), ("size", C.c_int32 * 3), ("radius", C.c_float)]
 
@@ -126,6 +131,12 @@ SIGNATURES = {
     "tg_write_vox": (_i, [C.POINTER(Voxels), C.c_char_p]),
     "ExportMagicaVoxel": (None, [_vp, _f, _i, C.c_char_p]),
     "MeshExport": (_i, [_vp, C.c_char_p, _vp, _vp, _vp, _i, _i, C.c_bool, _f]),
+    "GetExportProgress": (ExportProgress, []),
+    "CancelExport": (None, [C.c_bool]),
+    "tg_export_result": (_i, [_i]),
+    "tg_debug_export_pause": (None, [_i]),
+    "tg_debug_export_paused": (_i, [_i]),
+    "tg_export_grid_axes": (_i, [_vp, _vp, _vp, C.POINTER(Grid)]),
     "tg_ray_query": (_i, [_vp, _i, _vp, _vp, _vp, _i64, _i, _f, _vp, _vp, _vp, _vp]),
     "tg_eval_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
     "tg_gradient_tree_points": (_i, [_vp, _vp, _i64, _vp, _vp]),
@@ -158,6 +169,8 @@ SIGNATURES = {
     "tg_batch_get_tuning": (_i, [_vp, _vp, _vp]),
     "tg_batch_set_surrogates": (_i, [_vp, _vp, _i, _u32]),
     "tg_batch_run": (_i, [_vp, _vp]),
+    "tg_batch_cancel": (_i, [_vp, _i]),
+    "tg_batch_debug_barrier": (_i, [_vp, C.c_uint64, _i, C.c_uint64]),
     "tg_batch_reserve": (_i, [_vp, C.c_uint64, C.c_uint64]),
     "tg_batch_get_info": (_i, [_vp, C.POINTER(BatchInfo)]),
     "tg_batch_mesh": (_i, [_vp, _i, C.POINTER(HostMesh), _vp]),

@@ -41,10 +41,46 @@ namespace tg
 		DropGraph();
 		for (DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &CellBits,
 			&CellWordBase, &ActiveCells, &Lattice, &Vertices, &Normals, &Colors, &Cubes, &FaceCounts, &FaceBase, &Faces,
-			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status })
+			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status, &Knobs })
 			b->Release();
 		if (HostCounters) cudaFreeHost(HostCounters);
 		HostCounters = nullptr;
+		std::lock_guard<std::mutex> l(CancelMutex);
+		if (CancelHost) cudaFreeHost(CancelHost);
+		CancelHost = CancelDevice = nullptr;
+	}
+
+	bool Batch::SetCancel(bool cancel)
+	{
+		std::lock_guard<std::mutex> l(CancelMutex);
+		if (!CancelHost)
+		{
+			int dev = 0;
+			if (cudaGetDevice(&dev) != cudaSuccess || dev != DeviceId) { cudaGetLastError(); return false; }
+			if (cudaHostAlloc((void**)&CancelHost, sizeof(int), cudaHostAllocMapped) != cudaSuccess)
+			{
+				cudaGetLastError();
+				CancelHost = nullptr;
+				return false;
+			}
+			*CancelHost = 0;
+			if (cudaHostGetDevicePointer((void**)&CancelDevice, CancelHost, 0) != cudaSuccess)
+			{
+				cudaGetLastError();
+				cudaFreeHost(CancelHost);
+				CancelHost = CancelDevice = nullptr;
+				return false;
+			}
+		}
+		*(volatile int*)CancelHost = cancel ? 1 : 0;
+		return true;
+	}
+
+	void Batch::SetBarrierKnobs(uint64_t limit_ns, int late_block, uint64_t late_ns)
+	{
+		KnobHost[0] = limit_ns;
+		KnobHost[1] = late_block >= 0 ? (uint64_t)late_block + 1 : 0;
+		KnobHost[2] = late_ns;
 	}
 
 	void Batch::SetTuning(const std::vector<int>& bricks, const std::vector<int>& lanes)
@@ -133,6 +169,8 @@ namespace tg
 		TG_TRY(Counters.Reserve(8 * 4));
 		TG_TRY(Barrier.Reserve(8));
 		TG_TRY(Status.Reserve(4));
+		TG_TRY(Knobs.Reserve(4 * sizeof(uint64_t)));
+		if (!CancelHost && !SetCancel(false)) { SetError("cannot map the batch's cancel flag"); return cudaErrorMemoryAllocation; }
 		if (!HostCounters) TG_TRY(cudaMallocHost(&HostCounters, 8 * sizeof(uint32_t)));
 		TG_TRY(BatchMaxBlocks(MaxStack, &Blocks));
 		if (Blocks <= 0) { SetError("the batch kernel does not fit on this device"); return cudaErrorInvalidConfiguration; }
@@ -167,6 +205,8 @@ namespace tg
 		State.ScanPartials = ScanPartials.As<uint32_t>();
 		State.Barrier = Barrier.As<unsigned>();
 		State.Status = Status.As<int>();
+		State.Cancel = CancelDevice;
+		State.Knobs = Knobs.As<uint64_t>();
 		Planned = true;
 		return cudaSuccess;
 	}
@@ -207,7 +247,7 @@ namespace tg
 				if (!f) continue;
 				const GridSpec& g = Grids[m];
 				const int B = Bricks[m];
-				const float radius = 0.8660254f * (float)B * g.Step;
+				const float radius = 0.8660254f * (float)B * std::max(g.DX, std::max(g.DY, g.DZ));
 				TG_TRY(LaunchFieldClassifyBricks(Programs[m]->View, g, B, f->Grid, f->TablePtr(), f->ImagePtr(), f->MarginFor(radius),
 					BrickBits.As<uint32_t>() + BrickWordHost[m], f->StatusPtr(), s));
 			}
@@ -249,14 +289,23 @@ namespace tg
 		if (!Planned) TG_TRY(Plan(s));
 		const int n = (int)Programs.size();
 		Info.Reruns = 0;
+		LastStatus = 0;
 		for (int attempt = 0; attempt < 3; ++attempt)
 		{
+			TG_TRY(cudaMemcpyAsync(Knobs.Ptr, KnobHost, sizeof KnobHost, cudaMemcpyHostToDevice, s));
 			TG_TRY(Launch(s));
 			TG_TRY(cudaMemcpyAsync(HostCounters, Counters.Ptr, 5 * 4, cudaMemcpyDeviceToHost, s));
 			TG_TRY(cudaMemcpyAsync(HostCounters + 5, Status.Ptr, 4, cudaMemcpyDeviceToHost, s));
 			TG_TRY(cudaStreamSynchronize(s));
 			if (HostCounters[5] != 0)
 			{
+				LastStatus = (int)HostCounters[5];
+				if (LastStatus == 3)
+				{
+					SetCancel(false);
+					SetError("the batch run was cancelled");
+					return cudaSuccess;
+				}
 				SetError("the batch kernel's grid barrier timed out");
 				return cudaErrorLaunchTimeout;
 			}
@@ -285,7 +334,7 @@ namespace tg
 		int64_t bytes = 0;
 		for (const DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &CellBits,
 			&CellWordBase, &ActiveCells, &Lattice, &Vertices, &Normals, &Colors, &Cubes, &FaceCounts, &FaceBase, &Faces,
-			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status })
+			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status, &Knobs })
 			bytes += (int64_t)b->Bytes;
 		Info.DeviceBytes = bytes;
 		return cudaSuccess;

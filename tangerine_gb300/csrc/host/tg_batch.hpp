@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -42,6 +43,13 @@ namespace tg
 		// Model m's slice of the outputs (device pointers; faces hold the model's own
 		// vertex numbers).  Valid until the next Run.
 		void MeshOf(int m, DeviceMesh& out) const;
+		// Sets (or withdraws) the cancel flag the running kernel polls at its grid barriers;
+		// callable from any thread.  False when the flag could not be allocated.
+		bool SetCancel(bool cancel);
+		// Grid-barrier test hook: time limit (0: default) and one block started late.
+		void SetBarrierKnobs(uint64_t limit_ns, int late_block, uint64_t late_ns);
+		// Outcome of the last Run's kernel: 0, 2 (a barrier wait ran out) or 3 (cancelled).
+		int LastStatus = 0;
 
 		std::vector<int> Bricks, Lanes;
 		BatchInfo Info;
@@ -64,7 +72,10 @@ namespace tg
 		BatchState State{};
 		DeviceBuffer Models, BrickWord0, Tile0, CellBit0, CellWords, BrickBits, BrickWordBase, BrickList, CellBits, CellWordBase,
 			ActiveCells, Lattice, Vertices, Normals, Colors, Cubes, FaceCounts, FaceBase, Faces, VertexBase, FaceBaseModel,
-			Counters, ScanPartials, Barrier, Status;
+			Counters, ScanPartials, Barrier, Status, Knobs;
+		int* CancelHost = nullptr;                 // host-mapped page-locked flag
+		int* CancelDevice = nullptr;               // its device address
+		uint64_t KnobHost[4] = {};
 		std::vector<uint32_t> HostVertexBase, HostFaceBase;
 		std::vector<int64_t> BrickWordHost;        // per model: first word of its brick bits
 		std::vector<int> HasPaint;
@@ -72,6 +83,7 @@ namespace tg
 		cudaGraph_t Graph = nullptr;
 		cudaGraphExec_t GraphExec = nullptr;
 		int DeviceId = 0;
+		std::mutex CancelMutex;
 	};
 }
 

@@ -2,7 +2,9 @@
 // reference-counted trees, and the GPU-native tg_* entry points.
 #include "../../../include/tangerine_gb300.h"
 
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -10,6 +12,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tg_engine.hpp"
@@ -37,7 +40,10 @@ namespace
 
 	bool ToGridSpec(const tg_grid* g, GridSpec& out)
 	{
-		if (!g || g->nx < 2 || g->ny < 2 || g->nz < 2 || !(g->step > 0.0f))
+		const float dy = g && g->step_y != 0.0f ? g->step_y : (g ? g->step : 0.0f);
+		const float dz = g && g->step_z != 0.0f ? g->step_z : (g ? g->step : 0.0f);
+		if (!g || g->nx < 2 || g->ny < 2 || g->nz < 2 || !(g->step > 0.0f) || !(dy > 0.0f) || !(dz > 0.0f) ||
+			!std::isfinite(g->step) || !std::isfinite(dy) || !std::isfinite(dz))
 		{
 			SetError("a lattice needs at least 2 points per axis and a positive step");
 			return false;
@@ -48,17 +54,21 @@ namespace
 			SetError("lattice too large: cube indices must fit in 32 bits");
 			return false;
 		}
-		out = GridSpec{ g->x0, g->y0, g->z0, g->step, (int)g->nx, (int)g->ny, (int)g->nz };
+		out = GridSpec{ g->x0, g->y0, g->z0, g->step, dy, dz, (int)g->nx, (int)g->ny, (int)g->nz };
 		return true;
 	}
 
-	// MeshExportThread's lattice (export.cpp:324-337).
-	void ExportLattice(Vec3 lo, Vec3 hi, float step, tg_grid& g)
+	// MeshExportThread's lattice (export.cpp:324-337): ModelMin -= Step * 2, then
+	// ceil((ModelMax - ModelMin) / Step) cells per axis.
+	void ExportLattice(Vec3 lo, Vec3 hi, Vec3 step, tg_grid& g)
 	{
-		lo = lo - Vec3(step) * Vec3(2.0f);
-		const Vec3 ext = (hi - lo) / step;
+		lo = lo - step * Vec3(2.0f);
+		const Vec3 span = hi - lo;
+		const Vec3 ext(span.x / step.x, span.y / step.y, span.z / step.z);
 		g.x0 = lo.x; g.y0 = lo.y; g.z0 = lo.z;
-		g.step = step;
+		g.step = step.x;
+		g.step_y = step.y;
+		g.step_z = step.z;
 		g.nx = (int64_t)std::ceil(ext.x) + 1;
 		g.ny = (int64_t)std::ceil(ext.y) + 1;
 		g.nz = (int64_t)std::ceil(ext.z) + 1;
@@ -159,6 +169,164 @@ namespace
 	}
 
 	void WriteFileError(const char* path) { SetError(std::string("cannot write ") + (path ? path : "(null)")); }
+
+	// The asynchronous export behind MeshExport: one job at a time on a detached thread,
+	// with the reference's progress words and flags (export.cpp:48-57) -- Active is
+	// ExportActive, Stage ExportState -- and the job's outcome for tg_export_result.  Never
+	// destroyed, so a job still running at process exit touches no destroyed state.
+	struct ExportJob
+	{
+		std::mutex M;
+		std::condition_variable CV;
+		bool Running = false;
+		tg_status Result = TG_OK;
+		std::string Error;
+		std::atomic<bool> Active{ false };
+		std::atomic<int> Stage{ 0 };
+		std::atomic<float> Generation{ 0.0f }, Refinement{ 0.0f }, Secondary{ 0.0f }, Write{ 0.0f };
+		int PauseAt = 0;            // test hook (tg_debug_export_pause)
+		bool Paused = false;
+	};
+
+	ExportJob& Job()
+	{
+		static ExportJob* j = new ExportJob();
+		return *j;
+	}
+
+	struct ExportArgs
+	{
+		NodeRef Tree;
+		std::string Path;
+		float Lo[3], Hi[3], Step[3];
+		int Refine = 0, Format = 1;
+		bool PointCloud = false;
+		float Scale = 1.0f;
+	};
+
+	// The test hook's wait at the start of `stage`.
+	void PauseAt(ExportJob& j, int stage)
+	{
+		std::unique_lock<std::mutex> l(j.M);
+		if (j.PauseAt != stage) return;
+		j.Paused = true;
+		j.CV.notify_all();
+		j.CV.wait_for(l, std::chrono::seconds(30), [&]() { return j.PauseAt != stage || !j.Active.load(); });
+		j.Paused = false;
+	}
+
+	// MeshExportThread / PointCloudExportThread (export.cpp:320-480) on the GPU: stage 1
+	// builds the octree, compiles and runs the export (or the voxel search), stage 2 the
+	// point cloud's refinement, stage 3 writes the file; stage 0 when done.  Halting stops at
+	// the next phase boundary and writes no file.
+	void RunExportJob(ExportArgs a)
+	{
+		ExportJob& j = Job();
+		tg_status st = TG_OK;
+		std::string err;
+		bool cancelled = false;
+		tg_mesh m;
+		std::memset(&m, 0, sizeof m);
+		bool haveMesh = false;
+		std::unique_ptr<tg_program> prog;
+		PauseAt(j, 1);
+		if (!j.Active.load()) cancelled = true;
+		else if ((st = CompileInto(a.Tree.get(), prog)) != TG_OK) err = LastError();
+		if (st == TG_OK && !cancelled)
+		{
+			Engine& eng = Engine::Get();
+			ExportOptions control = OptionsOf(TG_MESH_ATTRIBUTES);
+			control.Active = &j.Active;
+			control.Cancelled = &cancelled;
+			control.Stage = &j.Stage;
+			control.Progress = &j.Generation;
+			if (a.PointCloud)
+			{
+				CloudSpec cs;
+				if (!CloudPlan(a.Lo, a.Hi, a.Step, cs, err)) st = TG_ERR_UNSUPPORTED;
+				else
+				{
+					std::lock_guard<std::mutex> lock(eng.Mutex);
+					const cudaStream_t s = eng.DefaultStream();
+					DeviceMesh dm;
+					const cudaError_t e = eng.PointCloud(*prog, cs, a.Refine, true, dm, s, &control);
+					if (e != cudaSuccess) { st = CudaFail(e, "exporting the point cloud"); err = LastError(); }
+					else if (!cancelled)
+					{
+						j.Refinement.store(1.0f);
+						st = CopyMeshToHost(dm, &m, s);
+						if (st == TG_OK) haveMesh = true;
+						else err = LastError();
+					}
+				}
+			}
+			else
+			{
+				tg_grid g;
+				GridSpec gs;
+				if (tg_export_grid_axes(a.Lo, a.Hi, a.Step, &g) != TG_OK || !ToGridSpec(&g, gs))
+				{
+					st = TG_ERR_INVALID;
+					err = LastError();
+				}
+				else
+				{
+					HostMeshOut host;
+					control.Host = &host;
+					DeviceMesh dm;
+					cudaError_t e;
+					{
+						std::lock_guard<std::mutex> lock(eng.Mutex);
+						e = eng.Export(*prog, gs, control, dm, eng.DefaultStream());
+					}
+					if (cancelled && e == cudaSuccess) FreeHostMesh(host);
+					else
+					{
+						st = TakeHostMesh(e, host, &m, "exporting the mesh");
+						if (st == TG_OK) haveMesh = true;
+						else err = LastError();
+					}
+				}
+			}
+		}
+		if (st == TG_OK && !cancelled)
+		{
+			// ExportState.store(2), then (3): normals and colours came with the mesh.
+			if (!a.PointCloud) j.Stage.store(2);
+			j.Stage.store(3);
+			j.Secondary.store(1.0f);
+			PauseAt(j, 3);
+			if (!j.Active.load()) cancelled = true;
+		}
+		if (st == TG_OK && !cancelled)
+		{
+			st = a.Format == 1 ? tg_write_ply(&m, a.Path.c_str(), a.Scale) : tg_write_stl(prog.get(), &m, a.Path.c_str(), a.Scale, nullptr);
+			if (st != TG_OK) err = LastError();
+			else if (!j.Active.load())
+			{
+				cancelled = true;
+				std::remove(a.Path.c_str());
+			}
+			else j.Write.store(1.0f);
+		}
+		if (haveMesh) tg_mesh_free(&m);
+		prog.reset();
+		a.Tree = NodeRef();
+		if (cancelled && st == TG_OK)
+		{
+			st = TG_ERR_CANCELLED;
+			err = "the export was halted (CancelExport(true))";
+		}
+		{
+			std::lock_guard<std::mutex> l(j.M);
+			j.Result = st;
+			j.Error = err;
+			j.Running = false;
+			j.Paused = false;
+			j.Stage.store(0);
+		}
+		j.CV.notify_all();
+	}
 
 	// An octree's cells in the oracle's dump layout (tg_debug_octree).
 	int64_t DumpOctree(const Octree& o, float* cells, int32_t* children, int64_t cell_capacity, uint32_t* words,
@@ -370,7 +538,18 @@ extern "C"
 	TANGERINE_API tg_status tg_export_grid(const float lo[3], const float hi[3], float step, tg_grid* out)
 	{
 		if (!lo || !hi || !out || !(step > 0.0f)) { SetError("invalid export bounds"); return TG_ERR_INVALID; }
-		ExportLattice(Vec3(lo[0], lo[1], lo[2]), Vec3(hi[0], hi[1], hi[2]), step, *out);
+		ExportLattice(Vec3(lo[0], lo[1], lo[2]), Vec3(hi[0], hi[1], hi[2]), Vec3(step), *out);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_export_grid_axes(const float lo[3], const float hi[3], const float step[3], tg_grid* out)
+	{
+		if (!lo || !hi || !out || !step || !(step[0] > 0.0f) || !(step[1] > 0.0f) || !(step[2] > 0.0f))
+		{
+			SetError("invalid export bounds");
+			return TG_ERR_INVALID;
+		}
+		ExportLattice(Vec3(lo[0], lo[1], lo[2]), Vec3(hi[0], hi[1], hi[2]), Vec3(step[0], step[1], step[2]), *out);
 		return TG_OK;
 	}
 
@@ -592,32 +771,105 @@ extern "C"
 			SetError("the point-cloud export writes PLY only");
 			return TG_ERR_UNSUPPORTED;
 		}
-		if (!point_cloud && !(step[0] == step[1] && step[1] == step[2]))
+		if (!(step[0] > 0.0f) || !(step[1] > 0.0f) || !(step[2] > 0.0f))
 		{
-			SetError("the mesh export takes one step for all three axes");
-			return TG_ERR_UNSUPPORTED;
+			SetError("the export step must be positive on every axis");
+			return TG_ERR_INVALID;
 		}
-		tg_program* prog = nullptr;
-		tg_status st = tg_compile(h, &prog);
-		if (st != TG_OK) return st;
-		tg_mesh m;
-		if (point_cloud)
+		ExportJob& j = Job();
 		{
-			st = tg_export_point_cloud(prog, lo, hi, step, refine_iterations, TG_MESH_ATTRIBUTES, &m, nullptr);
+			std::lock_guard<std::mutex> l(j.M);
+			if (j.Running) { SetError("an export is already running (tg_export_result waits for it)"); return TG_ERR_BUSY; }
+			// MeshExport (export.cpp:566-580): active, every progress word reset, stage 1.
+			j.Running = true;
+			j.Result = TG_OK;
+			j.Error.clear();
+			j.Active.store(true);
+			j.Stage.store(0);
+			j.Generation.store(0.0f);
+			j.Refinement.store(0.0f);
+			j.Secondary.store(0.0f);
+			j.Write.store(0.0f);
+			j.Stage.store(1);
 		}
-		else
+		ExportArgs args;
+		args.Tree = Borrow(h);              // the job holds its own reference to the tree
+		args.Path = path;
+		for (int a = 0; a < 3; ++a) { args.Lo[a] = lo[a]; args.Hi[a] = hi[a]; args.Step[a] = step[a]; }
+		args.Refine = refine_iterations;
+		args.Format = format;
+		args.PointCloud = point_cloud;
+		args.Scale = scale;
+		try
 		{
-			tg_grid g;
-			st = tg_export_grid(lo, hi, step[0], &g);
-			if (st == TG_OK) st = tg_export_mesh(prog, &g, TG_MESH_ATTRIBUTES, &m, nullptr);
+			std::thread(RunExportJob, std::move(args)).detach();
 		}
-		if (st == TG_OK)
+		catch (...)
 		{
-			st = format == 1 ? tg_write_ply(&m, path, scale) : tg_write_stl(prog, &m, path, scale, nullptr);
-			tg_mesh_free(&m);
+			{
+				std::lock_guard<std::mutex> l(j.M);
+				j.Running = false;
+				j.Stage.store(0);
+			}
+			j.CV.notify_all();
+			SetError("cannot start the export thread");
+			return TG_ERR_MEMORY;
 		}
-		tg_program_free(prog);
-		return st;
+		return TG_OK;
+	}
+
+	TANGERINE_API ExportProgress GetExportProgress(void)
+	{
+		ExportJob& j = Job();
+		ExportProgress p;
+		p.Stage = j.Stage.load();
+		p.Generation = j.Generation.load();
+		p.Refinement = j.Refinement.load();
+		p.Secondary = j.Secondary.load();
+		p.Write = j.Write.load();
+		return p;
+	}
+
+	TANGERINE_API void CancelExport(bool halt)
+	{
+		ExportJob& j = Job();
+		{
+			std::lock_guard<std::mutex> l(j.M);
+			if (halt) j.Active.store(false);
+			else j.Stage.fetch_add(1);
+		}
+		j.CV.notify_all();
+	}
+
+	TANGERINE_API tg_status tg_export_result(int wait)
+	{
+		ExportJob& j = Job();
+		std::unique_lock<std::mutex> l(j.M);
+		if (wait) j.CV.wait(l, [&]() { return !j.Running; });
+		else if (j.Running) { SetError("the export is still running"); return TG_ERR_BUSY; }
+		if (j.Result != TG_OK) SetError(j.Error);
+		return j.Result;
+	}
+
+	// Test hook: the next asynchronous export waits at the start of `stage` (1: before the
+	// compile, 3: before the file write) until this is called with another stage or the export
+	// is halted; the wait gives up after 30 s.  0 disarms.
+	TANGERINE_API void tg_debug_export_pause(int stage)
+	{
+		ExportJob& j = Job();
+		{
+			std::lock_guard<std::mutex> l(j.M);
+			j.PauseAt = stage;
+		}
+		j.CV.notify_all();
+	}
+
+	// 1 once the export waits at the armed stage (within timeout_ms), else 0.
+	TANGERINE_API int tg_debug_export_paused(int timeout_ms)
+	{
+		ExportJob& j = Job();
+		std::unique_lock<std::mutex> l(j.M);
+		return j.CV.wait_for(l, std::chrono::milliseconds(timeout_ms), [&]() { return j.Paused; }) ? 1 : 0;
 	}
 
 	TANGERINE_API tg_status tg_sodapop_mesh(void* tree, float density, tg_drawable* out, void* stream)
@@ -1143,7 +1395,29 @@ extern "C"
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		cudaError_t e = b->Run(StreamOf(stream));
 		if (e == cudaErrorLaunchTimeout) return TG_ERR_CUDA;
+		if (e == cudaSuccess && b->LastStatus == 3) return TG_ERR_CANCELLED;
 		return e == cudaSuccess ? TG_OK : CudaFail(e, "running the batch");
+	}
+
+	TANGERINE_API tg_status tg_batch_cancel(tg_batch* b, int cancel)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (!b->SetCancel(cancel != 0)) { SetError("cannot map the batch's cancel flag (wrong device current?)"); return TG_ERR_CUDA; }
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_batch_debug_barrier(tg_batch* b, uint64_t limit_ns, int late_block, uint64_t late_ns)
+	{
+		if (!b) { SetError("null argument"); return TG_ERR_INVALID; }
+		if (late_ns > 2000000000ull || limit_ns > 60000000000ull || (limit_ns && limit_ns < 1000000ull))
+		{
+			SetError("barrier limit must be 0 or 1 ms..60 s, the late start at most 2 s");
+			return TG_ERR_INVALID;
+		}
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		b->SetBarrierKnobs(limit_ns, late_block, late_ns);
+		return TG_OK;
 	}
 
 	TANGERINE_API tg_status tg_batch_reserve(tg_batch* b, uint64_t vertices, uint64_t faces)

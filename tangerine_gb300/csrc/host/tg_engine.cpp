@@ -272,6 +272,17 @@ namespace tg
 	cudaError_t Engine::Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s)
 	{
 		out = DeviceMesh();
+		// Asynchronous exports stop at a synchronisation point once cancelled.
+		auto stopped = [&](float done) -> bool
+		{
+			if (opt.Progress) opt.Progress->store(done);
+			if (opt.Active && !opt.Active->load())
+			{
+				if (opt.Cancelled) *opt.Cancelled = true;
+				return true;
+			}
+			return false;
+		};
 		const int64_t lattice = (int64_t)g.NX * g.NY * g.NZ;
 		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
 		const int64_t words = (cells + 31) / 32;
@@ -311,7 +322,7 @@ namespace tg
 			if (opt.Field)
 			{
 				// Ball radius of a whole brick: half its diagonal.
-				const float radius = 0.8660254f * (float)B * g.Step;
+				const float radius = 0.8660254f * (float)B * std::max(g.DX, std::max(g.DY, g.DZ));
 				Begin("classify_field", s);
 				TG_TRY(LaunchFieldClassifyBricks(p.View, g, B, opt.Field->Grid, opt.Field->TablePtr(), opt.Field->ImagePtr(),
 					opt.Field->MarginFor(radius), bits, opt.Field->StatusPtr(), s));
@@ -357,6 +368,7 @@ namespace tg
 		TG_TRY(cudaStreamSynchronize(s));
 		const uint32_t vcount = HostCounts[0];
 		if (!opt.Dense) ActiveBricks = HostCounts[2];
+		if (stopped(0.6f)) return cudaSuccess;
 
 		TG_TRY(Vertices.Reserve((size_t)vcount * 12));
 		TG_TRY(Cubes.Reserve((size_t)vcount * 4));
@@ -382,6 +394,7 @@ namespace tg
 		TG_TRY(cudaMemcpyAsync(HostCounts + 1, Counts.As<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaStreamSynchronize(s));
 		const uint32_t fcount = HostCounts[1];
+		if (stopped(0.8f)) return cudaSuccess;
 
 		TG_TRY(Faces.Reserve((size_t)fcount * 12));
 		Begin("faces", s);
@@ -464,6 +477,7 @@ namespace tg
 		if (early) TG_TRY(cudaStreamSynchronize(CopyStream));
 		Collect();
 		if (opt.Field) TG_TRY(const_cast<FieldNet*>(opt.Field)->CheckStatus(s));
+		if (opt.Progress) opt.Progress->store(1.0f);
 		return cudaSuccess;
 	}
 

@@ -2,6 +2,7 @@
 // optional per-kernel profiler.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -72,6 +73,16 @@ namespace tg
 		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
 		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
 		HostMeshOut* Host = nullptr;        // also copy the mesh to host memory (see HostMeshOut)
+		// Host-side control of an asynchronous export (MeshExport): when *Active turns false
+		// the export stops at its next synchronisation point, sets *Cancelled and returns an
+		// empty mesh; *Progress receives the share of its phases done (0..1).
+		const std::atomic<bool>* Active = nullptr;
+		bool* Cancelled = nullptr;
+		std::atomic<float>* Progress = nullptr;
+		// The asynchronous export's stage word (ExportProgress::Stage): the point-cloud
+		// export stores 2 when its voxel search ends and skips the refinement when the word
+		// has moved past 2 by then (CancelExport(false) during the refinement stage).
+		std::atomic<int>* Stage = nullptr;
 	};
 
 	// Sodapop's meshing job output (device pointers into the engine's buffers, valid until
@@ -136,7 +147,8 @@ namespace tg
 		// PointCloudExportThread on the GPU: the kept voxel centres (cell order), refined,
 		// with gradient normals and colours when `attributes`; Cubes holds each point's
 		// voxel number, Faces nothing.
-		cudaError_t PointCloud(const Program& p, const CloudSpec& s, int refine, bool attributes, DeviceMesh& out, cudaStream_t st);
+		cudaError_t PointCloud(const Program& p, const CloudSpec& s, int refine, bool attributes, DeviceMesh& out, cudaStream_t st,
+			const ExportOptions* control = nullptr);
 		// VoxExport's voxel test on the GPU: the kept voxel numbers in order, to the host.
 		cudaError_t Voxels(const Program& p, const VoxSpec& s, std::vector<uint32_t>& cells, cudaStream_t st);
 		// Network iterations and exact steps of the last network-stepped render.

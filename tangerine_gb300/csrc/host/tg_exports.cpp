@@ -89,7 +89,8 @@ namespace tg
 		return true;
 	}
 
-	cudaError_t Engine::PointCloud(const Program& p, const CloudSpec& s, int refine, bool attributes, DeviceMesh& out, cudaStream_t st)
+	cudaError_t Engine::PointCloud(const Program& p, const CloudSpec& s, int refine, bool attributes, DeviceMesh& out, cudaStream_t st,
+		const ExportOptions* control)
 	{
 		out = DeviceMesh();
 		const int64_t words = (s.Total + 31) / 32;
@@ -111,6 +112,19 @@ namespace tg
 		TG_TRY(cudaMemcpyAsync(HostCounts, Counts.Ptr, 4, cudaMemcpyDeviceToHost, st));
 		TG_TRY(cudaStreamSynchronize(st));
 		const uint32_t n = HostCounts[0];
+		if (control)
+		{
+			// End of the voxel search (PointCloudExportThread's ExportState.store(2)).
+			if (control->Progress) control->Progress->store(1.0f);
+			if (control->Stage) control->Stage->store(2);
+			if (control->Active && !control->Active->load())
+			{
+				if (control->Cancelled) *control->Cancelled = true;
+				Collect();
+				return cudaSuccess;
+			}
+			if (control->Stage && control->Stage->load() > 2) refine = 0;
+		}
 		TG_TRY(Vertices.Reserve((size_t)n * 12 + 12));
 		Begin("cloud_refine", st);
 		TG_TRY(LaunchCloudRefine(p.View, s, Cubes.As<uint32_t>(), Counts.As<uint32_t>(), n, refine, Vertices.As<float>(), st));

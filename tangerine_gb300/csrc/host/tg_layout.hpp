@@ -59,11 +59,11 @@ namespace tg
 	};
 	static_assert(sizeof(OctNode) == 64, "OctNode is one 64-byte line");
 
-	// Export lattice: point (i, j, k) sits at (X0 + i*Step, Y0 + j*Step, Z0 + k*Step).
+	// Export lattice: point (i, j, k) sits at (X0 + i*DX, Y0 + j*DY, Z0 + k*DZ).
 	struct GridSpec
 	{
 		float X0, Y0, Z0;
-		float Step;
+		float DX, DY, DZ;       // step per axis
 		int NX, NY, NZ;         // lattice points per axis; cells are one fewer
 	};
 

@@ -12,7 +12,9 @@
 // numbers.
 //
 // The grid barrier is a counter and a generation word in global memory, waited on with a
-// time limit: a barrier that runs out sets the status and every block leaves.
+// time limit: a barrier that runs out sets the status and every block leaves.  The last
+// block to arrive at a barrier also reads the host's cancel flag; when it is set, every
+// block leaves after that barrier.
 #include <cstdint>
 
 #include "tg_cull.cuh"
@@ -36,7 +38,7 @@ namespace tg
 		}
 
 		// Grid-wide barrier of a cooperative launch.  False (for every thread of the block)
-		// when the wait ran out or an earlier one did.
+		// when the wait ran out, the run was cancelled, or an earlier barrier failed.
 		__device__ bool GridSync(const BatchState& s)
 		{
 			__shared__ int ok;
@@ -49,16 +51,20 @@ namespace tg
 				__threadfence();
 				if (atomicAdd(s.Barrier, 1u) == gridDim.x - 1)
 				{
+					// Every block has arrived: the cancel decision is taken once, here, and
+					// published with the status before the release.
+					if (s.Cancel && *s.Cancel != 0) atomicCAS(s.Status, 0, 3);
 					atomicExch(s.Barrier, 0u);
 					__threadfence();
 					atomicAdd(s.Barrier + 1, 1u);
 				}
 				else
 				{
+					const uint64_t limit = (s.Knobs && s.Knobs[0]) ? s.Knobs[0] : kBarrierLimitNs;
 					const uint64_t t0 = Now();
 					while (*gen == g)
 					{
-						if (*(volatile int*)s.Status != 0 || Now() - t0 > kBarrierLimitNs)
+						if (*(volatile int*)s.Status != 0 || Now() - t0 > limit)
 						{
 							atomicCAS(s.Status, 0, 2);
 							ok = 0;
@@ -202,8 +208,8 @@ namespace tg
 			{
 				const int ix = i0 + ox + tx, iy = j0 + oy + ty, izb = k0 + oz + tz * K;
 				const bool inPlane = ix <= i1 && iy <= j1;
-				const float x = LatticeCoord(g.X0, min(ix, i1), g.Step);
-				const float y = LatticeCoord(g.Y0, min(iy, j1), g.Step);
+				const float x = LatticeCoord(g.X0, min(ix, i1), g.DX);
+				const float y = LatticeCoord(g.Y0, min(iy, j1), g.DY);
 				float px[K], py[K], pz[K], res[K];
 				int cell[K];
 				unsigned todo = 0;
@@ -213,7 +219,7 @@ namespace tg
 					const int iz = izb + k;
 					px[k] = x;
 					py[k] = y;
-					pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.Step);
+					pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.DZ);
 					cell[k] = DescendOctree(prog.Nodes, px[k], py[k], pz[k]);
 					res[k] = 0.0f;
 					if (inPlane && iz <= k1) todo |= 1u << k;
@@ -261,6 +267,15 @@ namespace tg
 			const int lane = threadIdx.x & 31;
 			const int64_t gthreads = (int64_t)gridDim.x * kThreads;
 			const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+
+			// Test hook (tg_batch_debug_barrier): one block starts late, by at most 2 s, so the
+			// other blocks' first barrier wait can be made to run out.
+			if (s.Knobs && s.Knobs[1] == (uint64_t)blockIdx.x + 1 && threadIdx.x == 0)
+			{
+				const uint64_t delay = s.Knobs[2] < 2000000000ull ? s.Knobs[2] : 2000000000ull;
+				const uint64_t t0 = Now();
+				while (Now() - t0 < delay) __nanosleep(1000);
+			}
 
 			// 1. Classify every brick of every model; clear the cell bits.  Exact models go by
 			//    8 x 4 patches of neighbouring bricks (a warp each, bits set with atomicOr into

@@ -109,17 +109,17 @@ namespace tg
 				// brick's box (lattice coordinates are monotone in the index), then per point
 				// only below where the box straddles a pivot.
 				bool shared;
-				const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.Step), LatticeCoord(g.X0, i1, g.Step),
-					LatticeCoord(g.Y0, j0, g.Step), LatticeCoord(g.Y0, j1, g.Step), LatticeCoord(g.Z0, k0, g.Step),
-					LatticeCoord(g.Z0, k1, g.Step), shared);
+				const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.DX), LatticeCoord(g.X0, i1, g.DX),
+					LatticeCoord(g.Y0, j0, g.DY), LatticeCoord(g.Y0, j1, g.DY), LatticeCoord(g.Z0, k0, g.DZ),
+					LatticeCoord(g.Z0, k1, g.DZ), shared);
 				for (int oz = 0; oz < C; oz += ZSpan)
 				for (int oy = 0; oy < C; oy += 8)
 				for (int ox = 0; ox < C; ox += 8)
 				{
 					const int ix = i0 + ox + tx, iy = j0 + oy + ty, izb = k0 + oz + tz * K;
 					const bool inPlane = ix <= i1 && iy <= j1;
-					const float x = LatticeCoord(g.X0, min(ix, i1), g.Step);
-					const float y = LatticeCoord(g.Y0, min(iy, j1), g.Step);
+					const float x = LatticeCoord(g.X0, min(ix, i1), g.DX);
+					const float y = LatticeCoord(g.Y0, min(iy, j1), g.DY);
 					float px[K], py[K], pz[K], res[K];
 					int cell[K];
 					unsigned todo = 0;
@@ -129,7 +129,7 @@ namespace tg
 						const int iz = izb + k;
 						px[k] = x;
 						py[k] = y;
-						pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.Step);
+						pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.DZ);
 						cell[k] = shared ? top : DescendOctreeFrom(prog.Nodes, top, px[k], py[k], pz[k]);
 						res[k] = 0.0f;
 						if (inPlane && iz <= k1) todo |= 1u << k;

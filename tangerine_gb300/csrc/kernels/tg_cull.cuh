@@ -16,9 +16,9 @@ namespace tg
 
 	__device__ __forceinline__ BoxBall BallOfBox(const DeviceProgram& prog, const GridSpec& g, int i0, int i1, int j0, int j1, int k0, int k1)
 	{
-		const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
-		const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
-		const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
+		const float x0 = LatticeCoord(g.X0, i0, g.DX), x1 = LatticeCoord(g.X0, i1, g.DX);
+		const float y0 = LatticeCoord(g.Y0, j0, g.DY), y1 = LatticeCoord(g.Y0, j1, g.DY);
+		const float z0 = LatticeCoord(g.Z0, k0, g.DZ), z1 = LatticeCoord(g.Z0, k1, g.DZ);
 		BoxBall b;
 		b.cx = 0.5f * (x0 + x1); b.cy = 0.5f * (y0 + y1); b.cz = 0.5f * (z0 + z1);
 		const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);

@@ -27,8 +27,8 @@ namespace tg
 			const int iy = blockIdx.y * kTileY + ty;
 			const int iz0 = blockIdx.z * K;
 			const bool inPlane = ix < g.NX && iy < g.NY;
-			const float x = LatticeCoord(g.X0, ix < g.NX ? ix : g.NX - 1, g.Step);
-			const float y = LatticeCoord(g.Y0, iy < g.NY ? iy : g.NY - 1, g.Step);
+			const float x = LatticeCoord(g.X0, ix < g.NX ? ix : g.NX - 1, g.DX);
+			const float y = LatticeCoord(g.Y0, iy < g.NY ? iy : g.NY - 1, g.DY);
 
 			float px[K], py[K], pz[K], res[K];
 			int cell[K];
@@ -39,7 +39,7 @@ namespace tg
 				const int iz = iz0 + k;
 				px[k] = x;
 				py[k] = y;
-				pz[k] = LatticeCoord(g.Z0, iz < g.NZ ? iz : g.NZ - 1, g.Step);
+				pz[k] = LatticeCoord(g.Z0, iz < g.NZ ? iz : g.NZ - 1, g.DZ);
 				cell[k] = DescendOctree(prog.Nodes, px[k], py[k], pz[k]);
 				res[k] = 0.0f;
 				if (inPlane && iz < g.NZ) todo |= 1u << k;

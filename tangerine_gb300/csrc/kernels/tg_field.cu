@@ -737,9 +737,9 @@ namespace tg
 				const int bx = (int)(bc % bg.NBX), by = (int)((bc / bg.NBX) % bg.NBY), bz = (int)(bc / ((int64_t)bg.NBX * bg.NBY));
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
 				const int i1 = min(i0 + bg.B, g.NX - 1), j1 = min(j0 + bg.B, g.NY - 1), k1 = min(k0 + bg.B, g.NZ - 1);
-				const float x0 = LatticeCoord(g.X0, i0, g.Step), x1 = LatticeCoord(g.X0, i1, g.Step);
-				const float y0 = LatticeCoord(g.Y0, j0, g.Step), y1 = LatticeCoord(g.Y0, j1, g.Step);
-				const float z0 = LatticeCoord(g.Z0, k0, g.Step), z1 = LatticeCoord(g.Z0, k1, g.Step);
+				const float x0 = LatticeCoord(g.X0, i0, g.DX), x1 = LatticeCoord(g.X0, i1, g.DX);
+				const float y0 = LatticeCoord(g.Y0, j0, g.DY), y1 = LatticeCoord(g.Y0, j1, g.DY);
+				const float z0 = LatticeCoord(g.Z0, k0, g.DZ), z1 = LatticeCoord(g.Z0, k1, g.DZ);
 				const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
 				const float ex = 0.5f * (x1 - x0), ey = 0.5f * (y1 - y0), ez = 0.5f * (z1 - z0);
 				const float r = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;

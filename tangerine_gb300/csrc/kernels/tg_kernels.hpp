@@ -318,7 +318,9 @@ namespace tg
 		uint32_t* Counters;            // kept bricks, active cells, vertices, faces, overflow bits
 		uint32_t* ScanPartials;        // blocks + 1
 		unsigned* Barrier;             // arrival count, generation
-		int* Status;                   // nonzero: a barrier wait ran out
+		int* Status;                   // 2: a barrier wait ran out; 3: cancelled
+		const volatile int* Cancel;    // host-mapped flag polled at every grid barrier (null: none)
+		const uint64_t* Knobs;         // barrier limit in ns (0: default), late block + 1, its delay in ns
 	};
 
 	size_t BatchSharedBytes(int max_stack);

@@ -3,16 +3,23 @@
 // Some callers cannot call cudaMalloc once they are running: a host application that
 // hands all device memory to its own pool at start-up, or meshing code on a latency-bound
 // thread where cudaMalloc/cudaFree's implicit device-wide synchronisation is not
-// acceptable.  This entry point runs the same kernels as tg_export_mesh, but the export's
-// scratch memory -- the lattice of distances, the active-cell bitmask, its prefix sums,
-// the per-vertex triangle counts and the scan block sums -- lives in one file-scope
-// device array of fixed size (kNoAllocScratchBytes, 64 MiB), and the caller passes the
-// output buffers.  The library never allocates on this path.
+// acceptable.  This entry point runs the dense export kernels (every lattice point
+// evaluated, as the reference does -- not tg_export_mesh's default brick-culled path; the
+// mesh is the same bit for bit), with the export's scratch memory -- the lattice of
+// distances, the active-cell bitmask, its prefix sums, the per-vertex triangle counts and
+// the scan block sums -- in one file-scope device array of fixed size
+// (kNoAllocScratchBytes, 64 MiB), and output buffers the caller passes.  The library never
+// allocates on this path.
 //
-// * Every GPU that loads the library holds the 64 MiB array until the process exits.
-// * The array's device address is looked up with cudaGetSymbolAddress the first time the
-//   entry point runs on a device (with that device current); make that first call before
-//   any stream capture.
+// * The array belongs to this file's CUDA module.  CUDA loads modules lazily (the default
+//   since CUDA 12.2), so a device reserves the 64 MiB the first time this entry point
+//   runs on it -- at the set-up call (program and grid NULL) or the first export -- and
+//   holds them until the process exits.  A caller that later gives the rest of device
+//   memory to its own pool makes that first call before it does.
+// * The array's device address is looked up with cudaGetSymbolAddress by that first call
+//   on a device (with that device current) and cached; make that first call before any
+//   stream capture.  cudaDeviceReset invalidates the cached address: it is not supported
+//   while the library is in use.
 // * All calls share the array and it keeps the last call's contents.  The pipeline writes
 //   every scratch word before reading it; the vertex/face totals are cleared each call.
 //   Calls that overlap on the GPU (from several host threads or streams) race on the
@@ -73,18 +80,35 @@ extern "C" TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, c
 	float* vertices, float* normals, uint8_t* colors, uint32_t* faces, uint32_t* cubes,
 	uint64_t vertex_capacity, uint64_t face_capacity, uint64_t* counts, void* stream)
 {
+	if (!program && !grid && !vertices && !normals && !colors && !faces && !cubes && !counts)
+	{
+		// Set-up only: reserve the scratch array on the current device and cache its address.
+		int device = 0;
+		cudaError_t e = cudaGetDevice(&device);
+		if (e != cudaSuccess) return CudaFail(e, "tg_export_mesh_noalloc: cudaGetDevice");
+		void* base = nullptr;
+		e = ScratchAddress(device, &base);
+		if (e != cudaSuccess) return CudaFail(e, "tg_export_mesh_noalloc: cudaGetSymbolAddress");
+		return TG_OK;
+	}
 	if (!program || !grid || !vertices || !faces || !cubes || !counts)
 		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: null argument");
+	counts[0] = counts[1] = 0;
+	if (flags & ~(uint32_t)(TG_MESH_ATTRIBUTES | TG_MESH_DENSE))
+		return Fail(TG_ERR_UNSUPPORTED, "tg_export_mesh_noalloc: only TG_MESH_ATTRIBUTES and TG_MESH_DENSE apply "
+			"(this path always evaluates every lattice point; brick and lane settings do not exist here)");
 	const bool attributes = (flags & TG_MESH_ATTRIBUTES) != 0;
 	if (attributes && !normals)
 		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: normals buffer required with TG_MESH_ATTRIBUTES");
 	if (attributes && program->Host.Header.HasPaint && !colors)
 		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: colors buffer required: the tree has paint");
-	if (grid->nx < 2 || grid->ny < 2 || grid->nz < 2 || !(grid->step > 0.0f) ||
+	const float dy = grid->step_y != 0.0f ? grid->step_y : grid->step;
+	const float dz = grid->step_z != 0.0f ? grid->step_z : grid->step;
+	if (grid->nx < 2 || grid->ny < 2 || grid->nz < 2 || !(grid->step > 0.0f) || !(dy > 0.0f) || !(dz > 0.0f) ||
 		grid->nx > (1 << 20) || grid->ny > (1 << 20) || grid->nz > (1 << 20))
-		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: a lattice needs 2..2^20 points per axis and a positive step");
+		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: a lattice needs 2..2^20 points per axis and positive steps");
 
-	const GridSpec g{ grid->x0, grid->y0, grid->z0, grid->step, (int)grid->nx, (int)grid->ny, (int)grid->nz };
+	const GridSpec g{ grid->x0, grid->y0, grid->z0, grid->step, dy, dz, (int)grid->nx, (int)grid->ny, (int)grid->nz };
 	const int64_t lattice = grid->nx * grid->ny * grid->nz;
 	const int64_t cells = (grid->nx - 1) * (grid->ny - 1) * (grid->nz - 1);
 	const int64_t words = (cells + 31) / 32;
@@ -139,7 +163,8 @@ extern "C" TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, c
 	if (host[0] > vertex_capacity)
 	{
 		return Fail(TG_ERR_INVALID, "tg_export_mesh_noalloc: " + std::to_string(host[0]) +
-			" vertices exceed the vertex capacity (counts[0] holds the size needed)");
+			" vertices exceed the vertex capacity (counts[0] holds the size needed; counts[1] is known only "
+			"once the vertices fit)");
 	}
 
 	e = LaunchCellVertices(lat, g, wordBits, wordBase, vertices, cubes, faceCounts, cells, s);

@@ -81,7 +81,7 @@ namespace tg
 		const float n = (float)count;
 		const float cx = sx / n, cy = sy / n, cz = sz / n;
 		const float fsx = (float)cg.sx, fsy = (float)cg.sy, fsz = (float)cg.sz;
-		const float maxx = g.X0 + fsx * g.Step, maxy = g.Y0 + fsy * g.Step, maxz = g.Z0 + fsz * g.Step;
+		const float maxx = g.X0 + fsx * g.DX, maxy = g.Y0 + fsy * g.DY, maxz = g.Z0 + fsz * g.DZ;
 		vertices[(int64_t)vid * 3 + 0] = g.X0 + (maxx - g.X0) * (cx - 0.0f) / (fsx - 0.0f);
 		vertices[(int64_t)vid * 3 + 1] = g.Y0 + (maxy - g.Y0) * (cy - 0.0f) / (fsy - 0.0f);
 		vertices[(int64_t)vid * 3 + 2] = g.Z0 + (maxz - g.Z0) * (cz - 0.0f) / (fsz - 0.0f);

@@ -185,7 +185,8 @@ def _grid(g) -> _lib.Grid:
     if isinstance(g, _lib.Grid):
         return g
     # workloads.ExportGrid: cells -> lattice points
-    return _lib.Grid(g.x0, g.y0, g.z0, g.step, g.sx + 1, g.sy + 1, g.sz + 1)
+    return _lib.Grid(g.x0, g.y0, g.z0, g.step, g.sx + 1, g.sy + 1, g.sz + 1, getattr(g, "step_y", 0.0),
+                     getattr(g, "step_z", 0.0))
 
 
 def _flags(attributes=True, dense=False, brick=0, lanes=0, surrogate_only=False) -> int:
@@ -362,12 +363,30 @@ def write_vox(voxels, size, path):
     check(load().tg_write_vox(C.byref(v), str(path).encode()), "tg_write_vox")
 
 
-def mesh_export(tree: "Tree", path, lo, hi, step, refine=5, fmt="ply", point_cloud=False, scale=1.0):
-    """MeshExport (export.h:37), synchronously."""
+def mesh_export(tree: "Tree", path, lo, hi, step, refine=5, fmt="ply", point_cloud=False, scale=1.0, wait=True):
+    """MeshExport (export.h:37): starts the export on the library's export thread; with
+    wait (default) returns once the file is written (raising if the job failed)."""
     v3 = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float32), (3,)))
     lo, hi, step = v3(lo), v3(hi), v3(step)
     check(load().MeshExport(tree.handle, str(path).encode(), _lib.as_ptr(lo), _lib.as_ptr(hi), _lib.as_ptr(step), int(refine),
                             {"stl": 0, "ply": 1, "vox": 2}[fmt], bool(point_cloud), float(scale)), "MeshExport")
+    if wait:
+        check(load().tg_export_result(1), "MeshExport job")
+
+
+def export_progress():
+    """GetExportProgress: (stage, generation, refinement, secondary, write)."""
+    p = load().GetExportProgress()
+    return p.Stage, p.Generation, p.Refinement, p.Secondary, p.Write
+
+
+def cancel_export(halt: bool):
+    load().CancelExport(bool(halt))
+
+
+def export_result(wait=True) -> int:
+    """The last MeshExport job's status (tg_export_result)."""
+    return int(load().tg_export_result(1 if wait else 0))
 
 
 def _program_ray_march(self, origins, dirs, iterations=100, epsilon=1e-3, stream=None):
@@ -463,6 +482,15 @@ def export_grid(lo, hi, step) -> _lib.Grid:
     hi = np.asarray(hi, np.float32)
     g = _lib.Grid()
     check(load().tg_export_grid(_lib.as_ptr(lo), _lib.as_ptr(hi), float(step), C.byref(g)), "tg_export_grid")
+    return g
+
+
+def export_grid_axes(lo, hi, steps) -> _lib.Grid:
+    """tg_export_grid_axes: MeshExportThread's lattice with a step per axis."""
+    v3 = lambda v: np.ascontiguousarray(np.asarray(v, np.float32).reshape(3))
+    lo, hi, st = v3(lo), v3(hi), v3(steps)
+    g = _lib.Grid()
+    check(load().tg_export_grid_axes(_lib.as_ptr(lo), _lib.as_ptr(hi), _lib.as_ptr(st), C.byref(g)), "tg_export_grid_axes")
     return g
 
 

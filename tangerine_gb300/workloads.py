@@ -148,6 +148,12 @@ class ExportGrid:
     sx: int
     sy: int
     sz: int
+    step_y: float = 0.0          # 0: same as step (MeshExport's vec3 Step may differ per axis)
+    step_z: float = 0.0
+
+    @property
+    def steps(self) -> tuple[float, float, float]:
+        return (self.step, self.step_y or self.step, self.step_z or self.step)
 
     @property
     def corners(self) -> int:
@@ -159,14 +165,19 @@ class ExportGrid:
 
 
 def export_grid(lo=(-2.0, -2.0, -2.0), hi=(2.0, 2.0, 2.0), step: float | None = None,
-                resolution: int | None = None) -> ExportGrid:
+                resolution: int | None = None, steps=None) -> ExportGrid:
+    """`steps`: one step per axis instead of `step` (MeshExport's vec3 Step)."""
     f32 = np.float32
-    if step is None:
-        step = float(f32(f32(hi[0]) - f32(lo[0])) / f32(resolution))
-    s = f32(step)
-    mins = [f32(f32(v) - f32(s * f32(2.0))) for v in lo]
-    extent = [int(math.ceil(float(f32(f32(f32(h) - m) / s)))) for h, m in zip(hi, mins)]
-    return ExportGrid(float(mins[0]), float(mins[1]), float(mins[2]), float(s), *extent)
+    if steps is None:
+        if step is None:
+            step = float(f32(f32(hi[0]) - f32(lo[0])) / f32(resolution))
+        steps = (step, step, step)
+    st = [f32(v) for v in steps]
+    mins = [f32(f32(v) - f32(s * f32(2.0))) for v, s in zip(lo, st)]
+    extent = [int(math.ceil(float(f32(f32(f32(h) - m) / s)))) for h, m, s in zip(hi, mins, st)]
+    if st[0] == st[1] == st[2]:
+        return ExportGrid(float(mins[0]), float(mins[1]), float(mins[2]), float(st[0]), *extent)
+    return ExportGrid(float(mins[0]), float(mins[1]), float(mins[2]), float(st[0]), *extent, float(st[1]), float(st[2]))
 
 
 def camera_poses(seed: int, count: int, radius: float = 4.0):

@@ -115,3 +115,32 @@ def test_batch_surrogate_form_same_meshes(programs):
         for s in nets:
             if s is not None:
                 s.close()
+
+
+def test_batch_cancel_and_barrier_time_limit(lib, programs):
+    """Failure paths of the persistent kernel, made on purpose with no GPU fault: a cancel
+    flag set on the host ends the run at its first grid barrier (TG_ERR_CANCELLED, every
+    block gone); a block started 300 ms late makes the other blocks' 20 ms barrier wait run
+    out (TG_ERR_CUDA, "timed out", every block gone).  After each, the context is usable
+    and the next run gives the same meshes as before."""
+    progs, grids = programs
+    singles = [p.export_mesh(g) for p, g in zip(progs, grids)]
+    with sdf.Batch(progs, grids) as b:
+        b.run()
+        assert lib.tg_batch_cancel(b.ptr, 1) == 0
+        assert lib.tg_batch_run(b.ptr, None) == 7
+        assert b"cancelled" in lib.tg_last_error()
+        b.run()                                    # the flag was cleared by the cancelled run
+        for m, ref in enumerate(singles):
+            _same(b.mesh(m), ref)
+        assert lib.tg_batch_cancel(b.ptr, 1) == 0
+        assert lib.tg_batch_cancel(b.ptr, 0) == 0  # withdrawn before the run
+        b.run()
+        assert lib.tg_batch_debug_barrier(b.ptr, 20_000_000, 0, 300_000_000) == 0
+        assert lib.tg_batch_run(b.ptr, None) == 3
+        assert b"timed out" in lib.tg_last_error()
+        assert lib.tg_batch_debug_barrier(b.ptr, 0, -1, 0) == 0
+        b.run()
+        for m, ref in enumerate(singles):
+            _same(b.mesh(m), ref)
+        assert lib.tg_batch_debug_barrier(b.ptr, 0, 0, 3_000_000_000) != 0     # late start above 2 s refused

@@ -7,7 +7,7 @@ the .vox file bytes."""
 import numpy as np
 import pytest
 
-from conftest import canonical_rows, golden_names
+from conftest import canonical_rows, golden_names, sorted_faces
 from oracle import oracle as O
 from tangerine_gb300 import _lib, sdf
 from tangerine_gb300 import workloads as W
@@ -113,9 +113,80 @@ def test_mesh_export_entry(lib, golden, tmp_path):
     assert mp.shape[0] > 100 and mf.shape[0] > 100
     sdf.mesh_export(t, tmp_path / "mesh.stl", lo, hi, 0.05, 0, "stl")
     assert (tmp_path / "mesh.stl").stat().st_size == 84 + 50 * mf.shape[0]
-    for fmt, cloud, step in (("vox", False, 0.05), ("stl", True, 0.05), ("ply", False, (0.05, 0.06, 0.05))):
+    for fmt, cloud, step in (("vox", False, 0.05), ("stl", True, 0.05), ("ply", False, (0.05, -0.06, 0.05))):
         with pytest.raises(_lib.TangerineError):
             sdf.mesh_export(t, tmp_path / "x", lo, hi, step, 0, fmt, point_cloud=cloud)
+
+
+def test_async_mesh_export_progress_halt_and_rerun(lib, tmp_path):
+    """MeshExport returns at once and writes the same bytes as the synchronous calls; while
+    it waits before its write, GetExportProgress reports stage 3 with the generation and
+    attribute stages complete; a halt there writes no file and ends the job with
+    TG_ERR_CANCELLED; the next export runs to the end."""
+    t = sdf.from_spec(W.random_tree(1, 16, ops=W.OPS_UNIFORM4))
+    lo, hi, step = (-2.0, -2.0, -2.0), (2.0, 2.0, 2.0), 4.0 / 128
+    with sdf.compile(t) as prog:
+        sdf.write_ply(prog.export_mesh(sdf.export_grid(lo, hi, step)), tmp_path / "want.ply")
+    want = (tmp_path / "want.ply").read_bytes()
+    lib.tg_debug_export_pause(3)
+    try:
+        sdf.mesh_export(t, tmp_path / "a.ply", lo, hi, step, 0, "ply", wait=False)
+        assert lib.tg_debug_export_paused(60000) == 1
+        assert sdf.export_progress() == (3, 1.0, 0.0, 1.0, 0.0)
+        assert not (tmp_path / "a.ply").exists()
+        lib.tg_debug_export_pause(0)
+        assert sdf.export_result() == 0
+        assert sdf.export_progress() == (0, 1.0, 0.0, 1.0, 1.0)
+        assert (tmp_path / "a.ply").read_bytes() == want
+        lib.tg_debug_export_pause(3)
+        sdf.mesh_export(t, tmp_path / "b.ply", lo, hi, step, 0, "ply", wait=False)
+        assert lib.tg_debug_export_paused(60000) == 1
+        sdf.cancel_export(True)
+        assert sdf.export_result() == 7
+        assert not (tmp_path / "b.ply").exists()
+    finally:
+        lib.tg_debug_export_pause(0)
+    sdf.mesh_export(t, tmp_path / "c.ply", lo, hi, step, 0, "ply")
+    assert (tmp_path / "c.ply").read_bytes() == want
+
+
+def test_mesh_export_per_axis_step(lib, port, tmp_path):
+    """MeshExportThread's vec3 Step: a different step per axis (z with the most cells, so
+    the reference's loop order is the plain one), against the oracle's lattice, surface nets
+    and attributes; the culled export equals the dense one; MeshExport writes that mesh."""
+    spec = W.random_tree(5, 16, ops=W.OPS_UNIFORM4)
+    steps = (0.04, 0.05, 0.03)
+    grid = W.export_grid(steps=steps)
+    g = sdf.export_grid_axes((-2, -2, -2), (2, 2, 2), steps)
+    assert (g.nx, g.ny, g.nz) == (grid.sx + 1, grid.sy + 1, grid.sz + 1)
+    assert (g.step, g.step_y, g.step_z) == tuple(float(np.float32(s)) for s in steps)
+    t = sdf.from_spec(spec)
+    with sdf.compile(t) as prog:
+        lat = prog.eval_grid(grid)
+        m = prog.export_mesh(grid)
+        dense = prog.export_mesh(grid, dense=True)
+    h = port.build(spec)
+    o = port.octree(h)
+    try:
+        np.testing.assert_array_equal(lat, port.octree_grid(o, grid))
+        want = port.surface_nets(o, grid)
+        assert want.vertices.shape[0] > 1000
+        np.testing.assert_array_equal(m.vertices, want.vertices)
+        np.testing.assert_array_equal(m.cubes.astype(np.uint64), want.cubes)
+        np.testing.assert_array_equal(sorted_faces(m.faces), sorted_faces(want.faces))
+        normals, colors = port.vertex_attributes(o, want.vertices)
+        np.testing.assert_array_equal(m.normals, normals)
+        np.testing.assert_array_equal(m.colors, colors)
+    finally:
+        port.octree_free(o)
+        port.free(h)
+    for a, b in ((m.vertices, dense.vertices), (m.faces, dense.faces), (m.normals, dense.normals), (m.colors, dense.colors)):
+        np.testing.assert_array_equal(a, b)
+    sdf.mesh_export(t, tmp_path / "axes.ply", (-2, -2, -2), (2, 2, 2), steps, 0, "ply")
+    _, p, n, c, f = O.read_ply(tmp_path / "axes.ply")
+    np.testing.assert_array_equal(p, m.vertices)
+    np.testing.assert_array_equal(n, m.normals)
+    np.testing.assert_array_equal(sorted_faces(f), sorted_faces(m.faces))
 
 
 def test_exports_of_a_tree_that_is_not_lipschitz(lib, port):
