@@ -617,6 +617,11 @@ TANGERINE_API tg_status tg_debug_mma(int mode, const float* a, const float* b, f
  * double expression on n seeded inputs (x2 signs): counts[0] compared, counts[1] differing
  * (must be 0), counts[2] sent to the double path. */
 TANGERINE_API tg_status tg_debug_blend_check(uint64_t n, uint64_t seed, uint64_t* counts);
+/* Check of the paired FP32 arithmetic the distance interpreters use (FADD2 / FMUL2, two
+ * points per instruction) against the scalar formulas on n seeded inputs: counts[0] inputs,
+ * counts[1..9] lanes differing in bits (all must be 0) for: one add, one multiply, a product
+ * then a sum, sphere, box, torus, cylinder, plane, the affine transform. */
+TANGERINE_API tg_status tg_debug_pair_check(uint64_t n, uint64_t seed, uint64_t* counts);
 
 TANGERINE_API const char* tg_last_error(void);
 TANGERINE_API const char* tg_version(void);

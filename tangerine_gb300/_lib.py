@@ -193,6 +193,7 @@ SIGNATURES = {
     "tg_last_render_steps": (_i, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tg_debug_mma": (_i, [_i, _vp, _vp, _vp]),
     "tg_debug_blend_check": (_i, [C.c_uint64, C.c_uint64, _vp]),
+    "tg_debug_pair_check": (_i, [C.c_uint64, C.c_uint64, _vp]),
     "tg_last_error": (C.c_char_p, []),
     "tg_version": (C.c_char_p, []),
 }

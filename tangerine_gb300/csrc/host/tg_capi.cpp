@@ -1772,6 +1772,24 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API tg_status tg_debug_pair_check(uint64_t n, uint64_t seed, uint64_t* counts)
+	{
+		if (!counts) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaStream_t st = eng.DefaultStream();
+		DeviceBuffer d;
+		unsigned long long host[10] = {};
+		cudaError_t e = d.Reserve(sizeof host);
+		if (e == cudaSuccess) e = LaunchPairCheck(n, seed, d.As<unsigned long long>(), st);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(host, d.Ptr, sizeof host, cudaMemcpyDeviceToHost, st);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+		d.Release();
+		if (e != cudaSuccess) return CudaFail(e, "paired arithmetic check");
+		for (int i = 0; i < 10; ++i) counts[i] = host[i];
+		return TG_OK;
+	}
+
 	TANGERINE_API const char* tg_last_error(void) { return LastError().c_str(); }
 	TANGERINE_API const char* tg_version(void) { return "tangerine_gb300 0.1 (sm_103a)"; }
 }

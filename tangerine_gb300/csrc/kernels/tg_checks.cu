@@ -1,11 +1,16 @@
-// Device self-check of the float evaluation of the smooth-blend term
-// (BlendTermFloat in tg_sdfmath.hpp) against the reference's double expression, over
-// seeded inputs: realistic operand ranges, values where m and the blend term cancel (the
-// blended surface), operands at scattered exponents, and arbitrary finite bit patterns.
+// Device self-checks:
+// * the float evaluation of the smooth-blend term (BlendTermFloat in tg_sdfmath.hpp)
+//   against the reference's double expression, over seeded inputs: realistic operand
+//   ranges, values where m and the blend term cancel (the blended surface), operands at
+//   scattered exponents, and arbitrary finite bit patterns;
+// * the paired FP32 arithmetic of tg_pair.cuh against the scalar formulas, lane by lane:
+//   single adds and multiplies on arbitrary finite bit patterns, a product followed by a
+//   sum, the brush formulas and the affine transform on realistic points.
 #include <cstdint>
 
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
+#include "tg_pair.cuh"
 
 namespace tg
 {
@@ -80,6 +85,75 @@ namespace tg
 			atomicAdd(counts + 1, mismatches);
 			atomicAdd(counts + 2, fallbacks);
 		}
+	}
+
+	namespace
+	{
+		__device__ __forceinline__ bool SameBits(float a, float b)
+		{
+			return __float_as_uint(a) == __float_as_uint(b) || (isnan(a) && isnan(b));
+		}
+
+		constexpr int kPairChecks = 9;
+
+		__global__ void PairCheckKernel(uint64_t n, uint64_t seed, unsigned long long* counts)
+		{
+			unsigned long long bad[kPairChecks] = {};
+			unsigned long long seen = 0;
+			const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+			const PairUnits un = LoadPairUnits();
+			for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+			{
+				uint64_t z = Mix(seed ^ (i * 0xD1B54A32D192ED03ull));
+				uint32_t u[12];
+				for (int j = 0; j < 12; j += 2) { z = Mix(z); u[j] = (uint32_t)z; u[j + 1] = (uint32_t)(z >> 32); }
+				++seen;
+				// 0, 1: one add, one multiply on any finite bit patterns (subnormals included).
+				const float a0 = Finite(u[0], 1.0f), a1 = Finite(u[1], -2.0f), b0 = Finite(u[2], 0.5f), b1 = Finite(u[3], 3.0f);
+				const float2 s2 = Add2(make_float2(a0, a1), make_float2(b0, b1), un);
+				if (!SameBits(s2.x, a0 + b0) || !SameBits(s2.y, a1 + b1)) ++bad[0];
+				const float2 m2 = Mul2(make_float2(a0, a1), make_float2(b0, b1), un);
+				if (!SameBits(m2.x, a0 * b0) || !SameBits(m2.y, a1 * b1)) ++bad[1];
+				// 2: a product then a sum (never fused into one rounding).
+				const float c0 = (Unit(u[4]) - 0.5f) * 4.0f, c1 = (Unit(u[5]) - 0.5f) * 4.0f;
+				const float d0 = (Unit(u[6]) - 0.5f) * 4.0f, d1 = (Unit(u[7]) - 0.5f) * 4.0f;
+				const float e0 = (Unit(u[8]) - 0.5f), e1 = (Unit(u[9]) - 0.5f);
+				const float2 f2 = Add2(Mul2(make_float2(c0, c1), make_float2(d0, d1), un), make_float2(e0, e1), un);
+				if (!SameBits(f2.x, c0 * d0 + e0) || !SameBits(f2.y, c1 * d1 + e1)) ++bad[2];
+				// 3..7: brushes at points of [-2, 2]^3 with parameters in [0.1, 0.5].
+				const float2 x = make_float2(c0, d0), y = make_float2(c1, d1), zz = make_float2(2.0f * e0 + 0.5f * e1, 4.0f * e1);
+				const float p0 = 0.1f + 0.4f * Unit(u[10]), p1 = 0.1f + 0.4f * Unit(u[11]), p2 = 0.1f + 0.4f * Unit(u[4] ^ u[11]);
+				const Vec3 q0(x.x, y.x, zz.x), q1(x.y, y.y, zz.y);
+				float2 r = SdSphere2(x, y, zz, p0, un);
+				if (!SameBits(r.x, SdSphere(q0, p0)) || !SameBits(r.y, SdSphere(q1, p0))) ++bad[3];
+				r = SdBox2(x, y, zz, p0, p1, p2, un);
+				if (!SameBits(r.x, SdBox(q0, Vec3(p0, p1, p2))) || !SameBits(r.y, SdBox(q1, Vec3(p0, p1, p2)))) ++bad[4];
+				r = SdTorus2(x, y, zz, p0, p1 * 0.5f, un);
+				if (!SameBits(r.x, SdTorus(q0, p0, p1 * 0.5f)) || !SameBits(r.y, SdTorus(q1, p0, p1 * 0.5f))) ++bad[5];
+				r = SdCylinder2(x, y, zz, p0, p1, un);
+				if (!SameBits(r.x, SdCylinder(q0, p0, p1)) || !SameBits(r.y, SdCylinder(q1, p0, p1))) ++bad[6];
+				// 8: the affine transform (M * vec4(p, 1)).x = (m0*x + m1*y) + (m2*z + m3).
+				const float4 M = make_float4(p0 - 0.3f, p1 - 0.3f, p2 - 0.3f, e0);
+				const float2 t = AffineRow2(M, x, y, zz, un);
+				if (!SameBits(t.x, (M.x * q0.x + M.y * q0.y) + (M.z * q0.z + M.w)) ||
+					!SameBits(t.y, (M.x * q1.x + M.y * q1.y) + (M.z * q1.z + M.w))) ++bad[8];
+				r = SdPlane2(x, y, zz, p0, p1, p2, un);
+				if (!SameBits(r.x, SdPlane(q0, Vec3(p0, p1, p2))) || !SameBits(r.y, SdPlane(q1, Vec3(p0, p1, p2)))) ++bad[7];
+			}
+			atomicAdd(counts, seen);
+			for (int c = 0; c < kPairChecks; ++c) atomicAdd(counts + 1 + c, bad[c]);
+		}
+	}
+
+	cudaError_t LaunchPairCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream)
+	{
+		int dev = 0, sms = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		cudaError_t e = cudaMemsetAsync(counts, 0, (1 + kPairChecks) * sizeof(unsigned long long), stream);
+		if (e != cudaSuccess) return e;
+		PairCheckKernel<<<sms * 4, 256, 0, stream>>>(n, seed, counts);
+		return cudaGetLastError();
 	}
 
 	cudaError_t LaunchBlendCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream)

@@ -19,6 +19,7 @@
 #include "tg_kernels.hpp"
 #include "tg_surface.cuh"
 #include "tg_cull.cuh"
+#include "tg_pair.cuh"
 
 namespace tg
 {
@@ -141,7 +142,17 @@ namespace tg
 						for (int k = 0; k < K; ++k)
 							if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
 						float r[K];
-						RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kBrickThreads);
+						if constexpr (K % 2 == 0)
+						{
+							// Points in pairs through the paired FP32 instructions (tg_pair.cuh).
+							const float4* code = prog.Code;
+							RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
+								spill + 2 * threadIdx.x, kBrickThreads);
+						}
+						else
+						{
+							RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kBrickThreads);
+						}
 #pragma unroll
 						for (int k = 0; k < K; ++k)
 						{

@@ -223,11 +223,16 @@ namespace tg
 				const float4 T = LoadQuad(code, pc + 1);
 				const float4 M = LoadQuad(code, pc + 2);
 				pc += 3;
-				// BrushFn(ApplyInv(p)) * s, ApplyInv(p) = rotate(inverse(q), p - t) / s
+				// BrushFn(ApplyInv(p)) * s, ApplyInv(p) = rotate(inverse(q), p - t) / s.  An
+				// unscaled brush (s = 1, the common case) skips the divide and the multiply:
+				// x / 1 and x * 1 are x exactly.
 				const Quat qi{ Q.x, Q.y, Q.z, Q.w };
-				const Vec3 local = Rotate(qi, p - Vec3(T.x, T.y, T.z)) / T.w;
+				Vec3 local = Rotate(qi, p - Vec3(T.x, T.y, T.z));
+				if (T.w != 1.0f) local = local / T.w;
 				const float prm[3] = { h.y, h.z, h.w };
-				dst[depth] = BrushDistance(op, prm, local) * T.w;
+				float d = BrushDistance(op, prm, local);
+				if (T.w != 1.0f) d = d * T.w;
+				dst[depth] = d;
 				mat[depth] = __float_as_int(M.x);
 				++depth;
 			}
@@ -361,12 +366,16 @@ namespace tg
 				const Quat qi{ Q.x, Q.y, Q.z, Q.w };
 				const Vec3 t(T.x, T.y, T.z);
 				const float prm[3] = { h.y, h.z, h.w };
+				const bool scaled = T.w != 1.0f;    // x / 1 and x * 1 are x exactly
 #pragma unroll
 				for (int k = 0; k < K; ++k)
 				{
 					// BrushFn(ApplyInv(p)) * s with ApplyInv(p) = rotate(inverse(q), p - t) / s
-					const Vec3 local = Rotate(qi, Vec3(px[k], py[k], pz[k]) - t) / T.w;
-					acc[k] = BrushDistance(op, prm, local) * T.w;
+					Vec3 local = Rotate(qi, Vec3(px[k], py[k], pz[k]) - t);
+					if (scaled) local = local / T.w;
+					float d = BrushDistance(op, prm, local);
+					if (scaled) d = d * T.w;
+					acc[k] = d;
 				}
 				macc = __float_as_int(M.x);
 				if (thenSet)

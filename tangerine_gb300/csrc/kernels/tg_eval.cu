@@ -8,6 +8,7 @@
 // a thread-interleaved layout (no bank conflicts).
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
+#include "tg_pair.cuh"
 
 namespace tg
 {
@@ -53,7 +54,17 @@ namespace tg
 				for (int k = 0; k < K; ++k)
 					if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
 				float r[K];
-				RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kThreads);
+				if constexpr (K % 2 == 0)
+				{
+					// Points in pairs through the paired FP32 instructions (tg_pair.cuh).
+					const float4* code = prog.Code;
+					RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
+						spill + 2 * threadIdx.x, kThreads);
+				}
+				else
+				{
+					RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kThreads);
+				}
 #pragma unroll
 				for (int k = 0; k < K; ++k)
 				{

@@ -113,6 +113,8 @@ namespace tg
 	// Self-check of the float blend-term evaluation against the double expression over n
 	// seeded inputs (each both signs of the term): counts = checked, mismatches, fallbacks.
 	cudaError_t LaunchBlendCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream);
+	// counts[0] = points checked, counts[1..9] = mismatches per check (tg_checks.cu).
+	cudaError_t LaunchPairCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream);
 
 	// Achieved FP32 fused-multiply-add throughput of this GPU (TFLOP/s, 2 flops per FMA).
 	cudaError_t MeasureFp32Peak(double* tflops, cudaStream_t stream);

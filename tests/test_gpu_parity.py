@@ -287,3 +287,16 @@ def test_float_blend_term_equals_double(lib):
     checked, mismatches, fallbacks = (int(c) for c in counts)
     assert mismatches == 0, counts
     assert checked > (1 << 26)          # most inputs take the float path
+
+
+def test_paired_arithmetic_equals_scalar(lib):
+    """The interpreters evaluate two points per FADD2 / FMUL2 instruction; every lane must
+    equal the scalar float32 operation bit for bit: single adds and multiplies on arbitrary
+    finite bit patterns (subnormals included), a product then a sum (never fused), and the
+    brush formulas and affine transform on realistic points."""
+    counts = np.zeros(10, np.uint64)
+    _lib.check(lib.tg_debug_pair_check(1 << 22, 777, _lib.as_ptr(counts)), "tg_debug_pair_check")
+    names = ["add", "mul", "mul+add", "sphere", "box", "torus", "cylinder", "plane", "affine"]
+    assert int(counts[0]) == 1 << 22
+    bad = {n: int(c) for n, c in zip(names, counts[1:]) if c}
+    assert not bad, f"lanes differing from the scalar operations: {bad}"
