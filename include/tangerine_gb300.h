@@ -88,6 +88,20 @@ TANGERINE_API void ScaleTree(void* Handle, float Scale);
 /* Replays a tree spec: the postfix construction word stream tangerine_gb300.workloads
  * writes (op codes there).  NULL on a malformed spec (tg_last_error explains). */
 TANGERINE_API void* BuildTreeFromSpec(const float* Spec, int Count);
+/* The spec that rebuilds this tree exactly (BuildTreeFromSpec): brushes with their whole
+ * transforms and materials, operators in their stored order.  Returns the word count
+ * (-1: null handle) and copies at most `capacity` words. */
+TANGERINE_API int64_t tg_tree_spec(void* Handle, float* Out, int64_t Capacity);
+/* Used by the Lua tangerine.sdf surface (tangerine/lua_sdf.cpp), which never mutates a tree
+ * in place: SDFNode::Copy (a new handle); paint_over (ApplyMaterial with Force); and
+ * SDF::RotateX/Y/Z (degrees, through sinf / cosf as the reference). */
+TANGERINE_API void* CopyTree(void* Handle);
+/* SDFNode::Gradient on the host (Lua's gradient, lua_sdf.cpp:398-405): 3 floats to Out. */
+TANGERINE_API void GradientTree(void* Handle, float X, float Y, float Z, float* Out);
+TANGERINE_API void PaintOverTree(float Red, float Green, float Blue, void* Handle);
+TANGERINE_API void RotateTreeX(void* Handle, float Degrees);
+TANGERINE_API void RotateTreeY(void* Handle, float Degrees);
+TANGERINE_API void RotateTreeZ(void* Handle, float Degrees);
 
 /* Export the tree's bounds at 1/GridSize spacing to a file, synchronously
  * (ExportCommon + MeshExportThread, tangerine/export.cpp:320-381, 595-621).

@@ -22,7 +22,7 @@ enum
 {
 	SPEC_SPHERE = 1, SPEC_ELLIPSOID, SPEC_BOX, SPEC_TORUS, SPEC_CYLINDER, SPEC_PLANE, SPEC_CONE, SPEC_CONINDER,
 	SPEC_UNION, SPEC_DIFF, SPEC_INTER, SPEC_BUNION, SPEC_BDIFF, SPEC_BINTER, SPEC_FLATE,
-	SPEC_MOVE, SPEC_ROTATE, SPEC_SCALE, SPEC_PAINT, SPEC_ALIGN, SPEC_STENCIL,
+	SPEC_MOVE, SPEC_ROTATE, SPEC_SCALE, SPEC_PAINT, SPEC_ALIGN, SPEC_STENCIL, SPEC_TRANSFORM,
 };
 
 /* Interpreter op codes: OpcodeT, sdf_evaluator.h:83-107. */
@@ -949,6 +949,7 @@ static int spec_arity(int op)
 	case SPEC_MOVE: case SPEC_PAINT: case SPEC_ALIGN: return 3;
 	case SPEC_ROTATE: case SPEC_STENCIL: return 4;
 	case SPEC_SCALE: return 1;
+	case SPEC_TRANSFORM: return 8;
 	default: return -1;
 	}
 }
@@ -1021,6 +1022,14 @@ tgo_tree* tgo_build(const float* spec, int count)
 			node_move(stack[sp - 1], mul3(mixed, V3(-1.0f, -1.0f, -1.0f)));
 			break;
 		}
+		case SPEC_TRANSFORM:
+			/* a brush's whole transform as it is: rotation (w x y z), translation, scale */
+			if (sp < 1 || stack[sp - 1]->kind != K_BRUSH) { ok = 0; break; }
+			stack[sp - 1]->xf.rot.w = P[0]; stack[sp - 1]->xf.rot.x = P[1];
+			stack[sp - 1]->xf.rot.y = P[2]; stack[sp - 1]->xf.rot.z = P[3];
+			stack[sp - 1]->xf.trans = V3(P[4], P[5], P[6]);
+			stack[sp - 1]->xf.scale = P[7];
+			break;
 		case SPEC_STENCIL:
 		{
 			if (sp < 2) { ok = 0; break; }

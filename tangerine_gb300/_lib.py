@@ -114,6 +114,13 @@ SIGNATURES = {
     "MakeStencilOp": (_vp, [_vp, _vp, _f, _f, _f, C.c_bool]),
     "ScaleTree": (None, [_vp, _f]),
     "BuildTreeFromSpec": (_vp, [_vp, _i]),
+    "tg_tree_spec": (_i64, [_vp, _vp, _i64]),
+    "CopyTree": (_vp, [_vp]),
+    "GradientTree": (None, [_vp, _f, _f, _f, _vp]),
+    "PaintOverTree": (None, [_f, _f, _f, _vp]),
+    "RotateTreeX": (None, [_vp, _f]),
+    "RotateTreeY": (None, [_vp, _f]),
+    "RotateTreeZ": (None, [_vp, _f]),
     "ExportSTL": (None, [_vp, _f, _i, C.c_char_p]),
     "ExportPLY": (None, [_vp, _f, _i, C.c_char_p]),
     "tg_compile": (_i, [_vp, C.POINTER(_vp)]),

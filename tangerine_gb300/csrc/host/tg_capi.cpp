@@ -375,6 +375,33 @@ extern "C"
 		AsNode(h)->ApplyMaterial(m, false);
 	}
 
+	TANGERINE_API void PaintOverTree(float r, float g, float b, void* h)
+	{
+		auto m = std::make_shared<Material>();
+		m->Rgb[0] = r; m->Rgb[1] = g; m->Rgb[2] = b;
+		AsNode(h)->ApplyMaterial(m, true);
+	}
+
+	TANGERINE_API void* CopyTree(void* h) { return h ? Hand(tg::CopyTree(*AsNode(h))) : nullptr; }
+	TANGERINE_API void GradientTree(void* h, float x, float y, float z, float* out)
+	{
+		const Vec3 g = AsNode(h)->Gradient(Vec3(x, y, z));
+		out[0] = g.x; out[1] = g.y; out[2] = g.z;
+	}
+	TANGERINE_API void RotateTreeX(void* h, float degrees) { SDF::RotateX(*AsNode(h), degrees); }
+	TANGERINE_API void RotateTreeY(void* h, float degrees) { SDF::RotateY(*AsNode(h), degrees); }
+	TANGERINE_API void RotateTreeZ(void* h, float degrees) { SDF::RotateZ(*AsNode(h), degrees); }
+
+	TANGERINE_API int64_t tg_tree_spec(void* h, float* out, int64_t capacity)
+	{
+		if (!h) { SetError("null tree handle"); return -1; }
+		std::vector<float> spec;
+		tg::WriteSpec(*AsNode(h), spec);
+		if (out)
+			for (int64_t i = 0; i < capacity && i < (int64_t)spec.size(); ++i) out[i] = spec[(size_t)i];
+		return (int64_t)spec.size();
+	}
+
 	TANGERINE_API void* MakeSphereBrush(float r) { return Hand(SDF::Sphere(r)); }
 	TANGERINE_API void* MakeEllipsoidBrush(float x, float y, float z) { return Hand(SDF::Ellipsoid(x, y, z)); }
 	TANGERINE_API void* MakeBoxBrush(float x, float y, float z) { return Hand(SDF::Box(x, y, z)); }

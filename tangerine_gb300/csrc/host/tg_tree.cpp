@@ -597,12 +597,13 @@ namespace tg
 
 	namespace
 	{
-		NodeRef MakeBrush(uint32_t op, const float* params, AABB box)
+		NodeRef MakeBrush(uint32_t op, const float* params, AABB box, float a0 = 0.0f, float a1 = 0.0f, float a2 = 0.0f)
 		{
 			Node* n = new Node();
 			n->Kind = NodeKind::Brush;
 			n->Op = op;
 			for (int i = 0; i < BrushParamCount(op); ++i) n->Params[i] = params[i];
+			n->Args[0] = a0; n->Args[1] = a1; n->Args[2] = a2;
 			n->BrushBox = box;
 			n->StackSize = 1;
 			return NodeRef(n);
@@ -613,19 +614,19 @@ namespace tg
 
 	namespace SDF
 	{
-		NodeRef Sphere(float r) { const float p[1] = { r }; return MakeBrush(OpSphere, p, Symmetric(Vec3(r))); }
-		NodeRef Ellipsoid(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpEllipsoid, p, Symmetric(Vec3(x, y, z))); }
-		NodeRef Box(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpBox, p, Symmetric(Vec3(x, y, z))); }
+		NodeRef Sphere(float r) { const float p[1] = { r }; return MakeBrush(OpSphere, p, Symmetric(Vec3(r)), r); }
+		NodeRef Ellipsoid(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpEllipsoid, p, Symmetric(Vec3(x, y, z)), x, y, z); }
+		NodeRef Box(float x, float y, float z) { const float p[3] = { x, y, z }; return MakeBrush(OpBox, p, Symmetric(Vec3(x, y, z)), x, y, z); }
 		NodeRef Torus(float major, float minor)
 		{
 			const float p[2] = { major, minor };
 			const float r = major + minor;
-			return MakeBrush(OpTorus, p, Symmetric(Vec3(r, r, minor)));
+			return MakeBrush(OpTorus, p, Symmetric(Vec3(r, r, minor)), major, minor);
 		}
 		NodeRef Cylinder(float radius, float extent)
 		{
 			const float p[2] = { radius, extent };
-			return MakeBrush(OpCylinder, p, Symmetric(Vec3(radius, radius, extent)));
+			return MakeBrush(OpCylinder, p, Symmetric(Vec3(radius, radius, extent)), radius, extent);
 		}
 		// Unit normal; infinite bounds, halved when the normal is an axis (sdf_evaluator.cpp:1260-1294).
 		NodeRef Plane(float nx, float ny, float nz)
@@ -640,19 +641,19 @@ namespace tg
 			else if (n.y == 1.0f) b.Max.y = 0.0f;
 			else if (n.z == -1.0f) b.Min.z = 0.0f;
 			else if (n.z == 1.0f) b.Max.z = 0.0f;
-			return MakeBrush(OpPlane, p, b);
+			return MakeBrush(OpPlane, p, b, nx, ny, nz);
 		}
 		NodeRef Cone(float radius, float height)
 		{
 			const float p[2] = { radius / height, height };
-			return MakeBrush(OpCone, p, Symmetric(Vec3(radius, radius, (float)((double)height * 0.5))));
+			return MakeBrush(OpCone, p, Symmetric(Vec3(radius, radius, (float)((double)height * 0.5))), radius, height);
 		}
 		NodeRef Coninder(float rl, float rh, float height)
 		{
 			const float half = (float)((double)height * 0.5);
 			const float p[3] = { rl, rh, half };
 			const float mr = fmaxf(rl, rh);
-			return MakeBrush(OpConinder, p, Symmetric(Vec3(mr, mr, half)));
+			return MakeBrush(OpConinder, p, Symmetric(Vec3(mr, mr, half)), rl, rh, height);
 		}
 
 		// Non-Diff operators put the operand with the deeper stack on the left
@@ -729,7 +730,7 @@ namespace tg
 		{
 			SpecSphere = 1, SpecEllipsoid, SpecBox, SpecTorus, SpecCylinder, SpecPlane, SpecCone, SpecConinder,
 			SpecUnion, SpecDiff, SpecInter, SpecBlendUnion, SpecBlendDiff, SpecBlendInter, SpecFlate,
-			SpecMove, SpecRotate, SpecScale, SpecPaint, SpecAlign, SpecStencil,
+			SpecMove, SpecRotate, SpecScale, SpecPaint, SpecAlign, SpecStencil, SpecTransform,
 		};
 
 		int SpecArity(int op)
@@ -744,6 +745,7 @@ namespace tg
 			case SpecMove: case SpecPaint: case SpecAlign: return 3;
 			case SpecRotate: case SpecStencil: return 4;
 			case SpecScale: return 1;
+			case SpecTransform: return 8;
 			default: return -1;
 			}
 		}
@@ -795,6 +797,16 @@ namespace tg
 				break;
 			}
 			case SpecAlign: SDF::Align(*stack.back(), Vec3(P[0], P[1], P[2])); break;
+			case SpecTransform:
+			{
+				// A brush's whole transform, set as it is: rotation (w x y z), translation, scale.
+				Node& n = *stack.back();
+				if (n.Kind != NodeKind::Brush) return fail("tree spec transform on a node that is not a brush");
+				n.Xf.Rotation = Quat{ P[0], P[1], P[2], P[3] };
+				n.Xf.Translation = Vec3(P[4], P[5], P[6]);
+				n.Xf.Scalation = P[7];
+				break;
+			}
 			case SpecStencil:
 			{
 				NodeRef mask = std::move(stack.back()); stack.pop_back();
@@ -808,5 +820,72 @@ namespace tg
 		}
 		if (stack.size() != 1) return fail("tree spec does not reduce to one tree");
 		return std::move(stack.back());
+	}
+
+	void WriteSpec(const Node& n, std::vector<float>& out)
+	{
+		switch (n.Kind)
+		{
+		case NodeKind::Brush:
+		{
+			static const std::pair<uint32_t, int> brush[] = { { OpSphere, SpecSphere }, { OpEllipsoid, SpecEllipsoid },
+				{ OpBox, SpecBox }, { OpTorus, SpecTorus }, { OpCylinder, SpecCylinder }, { OpPlane, SpecPlane },
+				{ OpCone, SpecCone }, { OpConinder, SpecConinder } };
+			int op = 0;
+			for (const auto& b : brush) if (b.first == n.Op) op = b.second;
+			out.push_back((float)op);
+			for (int i = 0; i < SpecArity(op); ++i) out.push_back(n.Args[i]);
+			const Transform& x = n.Xf;
+			out.insert(out.end(), { (float)SpecTransform, x.Rotation.w, x.Rotation.x, x.Rotation.y, x.Rotation.z,
+				x.Translation.x, x.Translation.y, x.Translation.z, x.Scalation });
+			if (n.Mat) out.insert(out.end(), { (float)SpecPaint, n.Mat->Rgb[0], n.Mat->Rgb[1], n.Mat->Rgb[2] });
+			break;
+		}
+		case NodeKind::Set:
+		{
+			WriteSpec(*n.Lhs, out);
+			WriteSpec(*n.Rhs, out);
+			static const std::pair<uint32_t, int> set[] = { { OpUnion, SpecUnion }, { OpDiff, SpecDiff }, { OpInter, SpecInter },
+				{ OpBlendUnion, SpecBlendUnion }, { OpBlendDiff, SpecBlendDiff }, { OpBlendInter, SpecBlendInter } };
+			int op = 0;
+			for (const auto& b : set) if (b.first == n.Op) op = b.second;
+			out.push_back((float)op);
+			if (op >= SpecBlendUnion) out.push_back(n.Threshold);
+			break;
+		}
+		case NodeKind::Flate:
+			WriteSpec(*n.Lhs, out);
+			out.insert(out.end(), { (float)SpecFlate, n.Threshold });
+			break;
+		case NodeKind::Stencil:
+			WriteSpec(*n.Lhs, out);
+			WriteSpec(*n.Mask, out);
+			out.insert(out.end(), { (float)SpecStencil, n.Negative ? 1.0f : 0.0f, n.Mat ? n.Mat->Rgb[0] : 1.0f,
+				n.Mat ? n.Mat->Rgb[1] : 1.0f, n.Mat ? n.Mat->Rgb[2] : 1.0f });
+			break;
+		}
+	}
+
+	NodeRef CopyTree(const Node& n)
+	{
+		switch (n.Kind)
+		{
+		case NodeKind::Brush:
+		{
+			Node* c = new Node();
+			c->Kind = NodeKind::Brush;
+			c->Op = n.Op;
+			c->StackSize = n.StackSize;
+			for (int i = 0; i < 3; ++i) { c->Params[i] = n.Params[i]; c->Args[i] = n.Args[i]; }
+			c->BrushBox = n.BrushBox;
+			c->Xf = n.Xf;
+			c->Mat = n.Mat;
+			return NodeRef(c);
+		}
+		case NodeKind::Set: return SDF::MakeSet(n.Op, CopyTree(*n.Lhs), CopyTree(*n.Rhs), n.Threshold);
+		case NodeKind::Flate: return SDF::Flate(CopyTree(*n.Lhs), n.Threshold);
+		case NodeKind::Stencil: return SDF::Stencil(CopyTree(*n.Lhs), CopyTree(*n.Mask), n.Mat, n.Negative);
+		}
+		return NodeRef();
 	}
 }

@@ -64,6 +64,7 @@ namespace tg
 
 		// Brush
 		float Params[3] = { 0.0f, 0.0f, 0.0f };
+		float Args[3] = { 0.0f, 0.0f, 0.0f };   // the constructor's arguments (tree specs replay them)
 		AABB BrushBox{};
 		Transform Xf;
 		MaterialRef Mat;
@@ -133,4 +134,11 @@ namespace tg
 	// Builds a tree from a postfix tree spec (the word stream tangerine_gb300.workloads
 	// writes).  Returns an empty ref and fills `error` on a malformed spec.
 	NodeRef BuildFromSpec(const float* spec, int count, const char** error);
+	// The spec that rebuilds this tree exactly: each brush with its whole transform (the
+	// transform op) and material, set operators in their stored operand order (already
+	// left-leaning, so the replay keeps it), flates and stencils.
+	void WriteSpec(const Node& tree, std::vector<float>& out);
+	// SDFNode::Copy (sdf_evaluator.cpp:480-483, 617-620, 852-855, 1077-1080): a new tree of
+	// new nodes with the same parameters, transforms and materials.
+	NodeRef CopyTree(const Node& tree);
 }

@@ -23,12 +23,12 @@ import numpy as np
 # Spec op codes (shared with oracle/ref_harness.cpp and oracle/port/tg_oracle.c).
 SPHERE, ELLIPSOID, BOX, TORUS, CYLINDER, PLANE, CONE, CONINDER = range(1, 9)
 UNION, DIFF, INTER, BLEND_UNION, BLEND_DIFF, BLEND_INTER, FLATE = range(9, 16)
-MOVE, ROTATE, SCALE, PAINT, ALIGN, STENCIL = range(16, 22)
+MOVE, ROTATE, SCALE, PAINT, ALIGN, STENCIL, TRANSFORM = range(16, 23)
 
 ARITY = {
     SPHERE: 1, ELLIPSOID: 3, BOX: 3, TORUS: 2, CYLINDER: 2, PLANE: 3, CONE: 2, CONINDER: 3,
     UNION: 0, DIFF: 0, INTER: 0, BLEND_UNION: 1, BLEND_DIFF: 1, BLEND_INTER: 1, FLATE: 1,
-    MOVE: 3, ROTATE: 4, SCALE: 1, PAINT: 3, ALIGN: 3, STENCIL: 4,
+    MOVE: 3, ROTATE: 4, SCALE: 1, PAINT: 3, ALIGN: 3, STENCIL: 4, TRANSFORM: 8,
 }
 
 

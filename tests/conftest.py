@@ -30,8 +30,9 @@ def lib():
 
 
 def golden_names():
-    """The per-tree fixtures (writer_*.npz hold file-writer cases instead)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("writer_"))
+    """The per-tree fixtures (writer_*.npz hold file-writer cases, lua_*.npz the trees of
+    the reference's Lua model scripts)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("writer_", "lua_")))
 
 
 @pytest.fixture(scope="session")

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import golden_names, sorted_faces
+from conftest import GOLDEN, golden_names, sorted_faces
 from oracle import oracle as O
 from tangerine_gb300 import _lib, sdf
 from tangerine_gb300 import workloads as W
@@ -300,3 +300,38 @@ def test_paired_arithmetic_equals_scalar(lib):
     assert int(counts[0]) == 1 << 22
     bad = {n: int(c) for n, c in zip(names, counts[1:]) if c}
     assert not bad, f"lanes differing from the scalar operations: {bad}"
+
+
+LUA_MODELS = sorted(np.load(GOLDEN / "lua_models.npz").files)
+
+
+@pytest.mark.parametrize("name", LUA_MODELS)
+def test_lua_model_export_matches_oracle(lib, port, name):
+    """Tangerine's own model scripts (models/*.lua), built by the Lua surface and stored as
+    tree specs: the GPU lattice and mesh (vertices, cubes, faces, normals, colours) against
+    the oracle's, on a cube lattice of 96 cells around the model."""
+    spec = np.load(GOLDEN / "lua_models.npz")[name]
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        info = prog.info()
+        half = float(np.max(np.abs(np.concatenate([info.bounds_min[:], info.bounds_max[:]])))) * 1.05
+        grid = W.export_grid(lo=(-half,) * 3, hi=(half,) * 3, resolution=96)
+        lat = prog.eval_grid(grid)
+        m = prog.export_mesh(grid)
+    h = port.build(spec)
+    o = port.octree(h)
+    try:
+        np.testing.assert_array_equal(lat, port.octree_grid(o, grid))
+        want = port.surface_nets(o, grid)
+        assert want.vertices.shape[0] > 100
+        np.testing.assert_array_equal(m.vertices, want.vertices)
+        np.testing.assert_array_equal(m.cubes.astype(np.uint64), want.cubes)
+        np.testing.assert_array_equal(sorted_faces(m.faces), sorted_faces(want.faces))
+        normals, colors = port.vertex_attributes(o, want.vertices)
+        np.testing.assert_array_equal(m.normals, normals)
+        if colors is None:
+            assert m.colors is None
+        else:
+            np.testing.assert_array_equal(m.colors, colors)
+    finally:
+        port.octree_free(o)
+        port.free(h)
