@@ -10,10 +10,14 @@ mesh in host memory out, octree build and all host<->device copies inside the ti
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-`--impl reference` times Tangerine's CPU algorithm on the host cores instead: the
-reference built from its sources where those exist, otherwise the C restatement in
-oracle/port run in the reference's cost mode (8 corner evaluations per cell, 6 per face
-check), on a bounded z-slab of the same workload.
+`--impl reference` times Tangerine's CPU export of the same workload on the host cores
+instead: its own code (the AsyncParallelSurfaceNets thunks on its Pool() threadpool, then
+per-vertex Gradient + GetMaterial) where the reference library built from its sources loads,
+otherwise -- on the GPU host, which has neither the sources nor a way to run x86 builds --
+the C restatement in oracle/port run in the reference's cost mode (8 corner evaluations per
+cell, 6 per face check).  Its K timed steps are K z-slabs that together make one complete
+export; `kind` in the line says which code ran.  `--workload cpu-compare` (x86 host with the
+reference sources) times both CPU codes on the same whole export.
 """
 
 from __future__ import annotations
@@ -39,6 +43,11 @@ RES = 512
 WORKLOAD = (f"exact export (bricks without surface skipped, same mesh): seeded {PRIMS}-primitive CSG tree (seed {SEED}; 60% union, 20% diff, 10% inter, "
             f"10% smooth-union; depth <= 12), FP32 on a {RES}^3 grid over [-2,2]^3 "
             f"({RES + 3}^3 lattice samples), surface nets + gradient normals + material colours")
+# The config both arms print (the GPU arm and `--impl reference`).
+CONFIG = {"workload": WORKLOAD, "samples_per_mesh": (RES + 3) ** 3,
+          "l2": "GPU arm: L2 flushed between steps (512 MB write outside the per-step events); per-step working set "
+                "0.55 GB lattice > L2",
+          "parallelism": "GPU arm: one GPU (replicas for N > 1); reference arm: all host cores of rank 0"}
 
 # FP32 operations per program op (mul/add/sub/div/sqrt/min/max/abs = 1 each), from the
 # formulas in tangerine/sdf_evaluator.cpp:165-295 and the interpreter's transforms.
@@ -217,66 +226,160 @@ def brick_flops(cost, grid, bricks, B):
     return int(cost[mask].sum(dtype=np.int64)), int(mask.sum())
 
 
-def cpu_baseline(spec, grid, seconds_target=12.0):
-    """Tangerine's CPU export cost on a z-slab of the workload, all host cores."""
+def cpu_checker(prefer_reference=True):
+    """(library, kind): Tangerine's own CPU code built from its sources (oracle/_ref) where
+    it loads -- the x86 container that holds the sources -- else the C restatement in
+    oracle/port, which builds on any host (the GPU host has no reference sources, and x86
+    binaries do not run on its Arm cores)."""
     from oracle import oracle as O
+    if prefer_reference:
+        try:
+            ref = O.reference() if O.REF_SO.exists() else None
+            if ref is not None:
+                return ref, "reference"
+        except OSError:
+            pass
+    return O.port(), "port"
+
+
+def slab_bounds(sz: int, parts: int):
+    """`parts` contiguous z-ranges of cells [k0, k1) that partition the lattice's sz cells."""
+    edges = [round(i * sz / parts) for i in range(parts + 1)]
+    return [(edges[i], edges[i + 1]) for i in range(parts) if edges[i + 1] > edges[i]]
+
+
+def cpu_export_slab(cpu, kind, o, grid, k0, k1, threads):
+    """Tangerine's CPU export of cells with k0 <= k < k1 (all x, y) on all host threads:
+    the surface-nets cell and face passes as the reference runs them (8 corner evaluations
+    per cell, 6 per face check, through SDFOctree::Eval) and per-vertex Gradient +
+    GetMaterial.  Returns (seconds, lattice samples the slab owns, vertices)."""
     from tangerine_gb300 import workloads as W
-    port = O.port()
-    threads = port.hardware_threads()
-    h = port.build(spec)
-    o = port.octree(h)
+    z0 = float(np.float32(grid.z0) + np.float32(k0) * np.float32(grid.step))
+    g = W.ExportGrid(grid.x0, grid.y0, z0, grid.step, grid.sx, grid.sy, k1 - k0)
+    t = time.perf_counter()
+    if kind == "reference":
+        m = cpu.surface_nets(o, g, threads=0)
+        cpu.vertex_attributes(o, m.vertices, threads=0)
+    else:
+        m = cpu.surface_nets(o, g, threads=threads, faithful=True)
+        cpu.vertex_attributes(o, m.vertices, threads=threads)
+    dt = time.perf_counter() - t
+    owned = (grid.sx + 1) * (grid.sy + 1) * ((k1 - k0) + (1 if k1 == grid.sz else 0))
+    return dt, owned, m.vertices.shape[0]
+
+
+def cpu_full_export(spec, grid, parts=20, prefer_reference=True, max_seconds=None):
+    """The whole export on the host cores, slab after slab: every one of the lattice's
+    samples is owned by exactly one slab.  The face pass skips each slab's first cell layer
+    (its neighbours below lie in the slab before), about 1/26 of the face checks at 20
+    slabs: the CPU side is timed slightly in its favour.  With max_seconds, slabs spread
+    over the whole z range (bit-reversed order) run until that much time is spent, and the
+    rate is that of the slabs run (labelled in `sample`)."""
+    cpu, kind = cpu_checker(prefer_reference)
+    threads = cpu.hardware_threads()
+    h = cpu.build(spec)
+    o = cpu.octree(h)
     try:
-        slab = 4
-        done_samples, secs = 0, 0.0
-        kmid = grid.sz // 2
-        while secs < seconds_target and slab <= grid.sz:
-            z0 = float(np.float32(grid.z0) + np.float32(kmid - slab // 2) * np.float32(grid.step))
-            g = W.ExportGrid(grid.x0, grid.y0, z0, grid.step, grid.sx, grid.sy, slab)
-            t = time.perf_counter()
-            m = port.surface_nets(o, g, threads=threads, faithful=True)
-            port.vertex_attributes(o, m.vertices, threads=threads)
-            dt = time.perf_counter() - t
-            done_samples += (grid.sx + 1) * (grid.sy + 1) * (slab + 1)
+        slabs = slab_bounds(grid.sz, parts)
+        bits = max(1, (len(slabs) - 1).bit_length())
+        order = sorted(range(len(slabs)), key=lambda i: int(format(i, f"0{bits}b")[::-1], 2))
+        secs, samples, done = 0.0, 0, 0
+        for i in order:
+            k0, k1 = slabs[i]
+            dt, owned, _ = cpu_export_slab(cpu, kind, o, grid, k0, k1, threads)
             secs += dt
-            slab *= 2
-        return {"value": done_samples / secs, "unit": "samples/s", "cores": threads, "kind": "port",
-                "sample": f"z-slabs of the same {grid.sx - 2}^3 export ({done_samples} lattice samples, {secs:.1f} s): "
-                          f"C restatement of the reference export, 8 corner evaluations per cell and 6 per "
-                          f"face check as the reference makes, then per-vertex gradient + colour",
-                "seconds": secs}
+            samples += owned
+            done += 1
+            if max_seconds is not None and secs >= max_seconds:
+                break
+        whole = done == len(slabs)
+        what = (f"the whole {grid.sx - 2}^3 export ({samples} lattice samples) in {parts} z-slabs" if whole else
+                f"{done} of {len(slabs)} z-slabs spread over the {grid.sx - 2}^3 export ({samples} lattice samples)")
+        return {"value": samples / secs, "unit": "samples/s", "cores": threads, "kind": kind, "seconds": secs,
+                "sample": f"{what}, {secs:.1f} s: " + CPU_KIND_TEXT[kind]}
     finally:
-        port.octree_free(o)
-        port.free(h)
+        cpu.octree_free(o)
+        cpu.free(h)
+
+
+CPU_KIND_TEXT = {
+    "reference": "Tangerine's own AsyncParallelSurfaceNets thunks on its Pool() threadpool over the SDFOctree "
+                 "(surface_nets.cpp:864-1121, threadpool.cpp:27-40), then per-vertex Gradient + GetMaterial on Pool(), "
+                 "built from the reference sources",
+    "port": "C restatement of the reference export on all host threads (8 corner evaluations per cell and 6 per face "
+            "check as the reference's thunks make, then per-vertex gradient + colour); the reference itself cannot run "
+            "on this host (its sources are not here, and x86 builds do not run on Arm)",
+}
+
+
+def cpu_baseline(spec, grid, max_seconds=30.0):
+    """The cpu_baseline object: the export on the host cores -- whole at 512^3 (about 10 s
+    on 16 Grace cores), spread slabs for about max_seconds on larger lattices."""
+    return cpu_full_export(spec, grid, parts=max(20, grid.sz // 26), max_seconds=max_seconds)
 
 
 def reference_arm(args, rank):
+    """`--impl reference`: Tangerine's CPU export of the same workload.  The K timed steps
+    are the K z-slabs of one partition of the lattice, so together they are one complete
+    export, measured slab by slab (nothing extrapolated); the W warm-up steps run slabs of
+    a W-way partition first.  value = the lattice's samples / the K steps' summed time."""
     if rank != 0:
         return
     from tangerine_gb300 import workloads as W
     spec = W.random_tree(SEED, PRIMS)
     grid = W.export_grid(resolution=RES)
-    for _ in range(args.warmup):
-        cpu_baseline(spec, grid, seconds_target=0.5)
-    vals = []
-    t0 = time.perf_counter()
-    cb = None
-    for _ in range(args.steps):
-        cb = cpu_baseline(spec, grid, seconds_target=max(1.0, 60.0 / max(1, args.steps)))
-        vals.append(cb["value"])
-    wall = time.perf_counter() - t0
-    value = float(np.mean(vals))
-    samples = grid.corners
+    cpu, kind = cpu_checker(not args.port)
+    threads = cpu.hardware_threads()
+    h = cpu.build(spec)
+    o = cpu.octree(h)
+    try:
+        for k0, k1 in slab_bounds(grid.sz, max(args.warmup, 1))[: max(args.warmup, 1)]:
+            cpu_export_slab(cpu, kind, o, grid, k0, min(k1, k0 + 8), threads)
+        t0 = time.perf_counter()
+        step_s, samples, vertices = [], 0, 0
+        for k0, k1 in slab_bounds(grid.sz, args.steps):
+            dt, owned, nv = cpu_export_slab(cpu, kind, o, grid, k0, k1, threads)
+            step_s.append(dt)
+            samples += owned
+            vertices += nv
+        wall = time.perf_counter() - t0
+    finally:
+        cpu.octree_free(o)
+        cpu.free(h)
+    assert samples == grid.corners, (samples, grid.corners)
+    total = float(np.sum(step_s))
+    value = samples / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * samples / value,
+        "steps": len(step_s), "warmup": args.warmup, "ms_per_step": 1e3 * total / len(step_s),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "samples_per_mesh": samples},
-        "meshes_per_s": value / samples,
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "config": CONFIG,
+        "meshes_per_s": 1.0 / total,
+        "vertices": vertices,
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": kind,
+                         "sample": f"one whole {RES}^3 export ({samples} lattice samples) as {len(step_s)} z-slab steps, "
+                                   f"{total:.1f} s: " + CPU_KIND_TEXT[kind]},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_compare(args):
+    """x86 leg (where the reference sources are present): the reference's own CPU export
+    and the C restatement over the same whole 512^3 export on the same host threads."""
+    from tangerine_gb300 import workloads as W
+    spec = W.random_tree(SEED, PRIMS)
+    grid = W.export_grid(resolution=args.compare_res)
+    ref = cpu_full_export(spec, grid, parts=args.steps, prefer_reference=True)
+    if ref["kind"] != "reference":
+        print(json.dumps({"workload": "cpu-compare", "unavailable": "the reference library (oracle/_ref) is not built here"}))
+        return
+    port = cpu_full_export(spec, grid, parts=args.steps, prefer_reference=False)
+    print(json.dumps({"workload": "cpu-compare", "resolution": args.compare_res, "threads": ref["cores"],
+                      "reference_samples_per_s": ref["value"], "port_samples_per_s": port["value"],
+                      "port_over_reference": port["value"] / ref["value"],
+                      "reference_seconds": ref["seconds"], "port_seconds": port["seconds"]}), flush=True)
 
 
 def mesh_difference(a, b):
@@ -293,13 +396,14 @@ def mesh_difference(a, b):
     return False, float(max(d1, d2))
 
 
-def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_ms, world, brick=0):
-    """Trains the network on the program, then times the culled export with it deciding
-    which bricks to skip: alone, and with the exact test on the bricks it keeps."""
+def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_ms, world, brick=0, fitted=None):
+    """Trains the network on the program (unless `fitted` is one already trained on it),
+    then times the culled export with it deciding which bricks to skip: alone, and with the
+    exact test on the bricks it keeps."""
     import torch
     from tangerine_gb300 import _lib, sdf
-    sur = sdf.Surrogate()
-    info = sur.fit(prog)
+    sur = fitted or sdf.Surrogate()
+    info = sur.fit(prog) if fitted is None else sur.info()
     exact_mesh = prog.export_mesh(grid, brick=brick)
     out = {"train_seconds": info.train_seconds, "data_seconds": info.data_seconds, "samples": int(info.samples),
            "steps": int(info.steps), "max_error": info.max_error, "p99_error": info.p99_error,
@@ -356,8 +460,48 @@ def surrogate_leg(prog, grid, samples, args, stream, sp, flush, exact_ms, dense_
     secs = time.perf_counter() - t0
     out["e2e"] = {"value": world * samples * reps / secs, "unit": "samples/s", "h2d_bytes_per_step": 0,
                   "d2h_bytes_per_step": int(d2h), "call": f"tg_export_mesh_surrogate ({best_mode}), host mesh out"}
-    sur.close()
+    if fitted is None:
+        sur.close()
     return out
+
+
+def surrogate_1024_leg(prog, args, stream, sp, flush, world):
+    """The surrogate-culled workload inside the default line: the same tree on the 1024^3
+    grid in 32^3 bricks -- dense, exact-culled and network-culled (network + exact test, and
+    the network alone), same mesh required; one network trained on the tree."""
+    import torch
+    from tangerine_gb300 import sdf
+    from tangerine_gb300 import workloads as W
+    grid = W.export_grid(resolution=1024)
+    samples = grid.corners
+    steps = max(2, min(args.steps, 5))
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.zero_()
+            st[i].record(stream)
+            fn()
+            en[i].record(stream)
+        torch.cuda.synchronize()
+        return float(np.sum([a.elapsed_time(b) for a, b in zip(st, en)]))
+
+    dense_ms = timed(lambda: prog.export_mesh_device(grid, dense=True, stream=sp))
+    exact_ms = timed(lambda: prog.export_mesh_device(grid, brick=32, stream=sp))
+    _, exact_kept = sdf.last_export_stats()
+    sub = argparse.Namespace(steps=steps, warmup=2)
+    sur = surrogate_leg(prog, grid, samples, sub, stream, sp, flush, exact_ms, dense_ms, world, brick=32)
+    sur["workload"] = (f"the same tree on a 1024^3 grid over [-2,2]^3 ({samples} lattice samples) in 32^3-cell bricks; "
+                       f"network: 16-level hash grid + 3x64 BF16 layers trained on 2^22 exact samples")
+    sur["exact_culled"] = {"value": world * samples * steps / (exact_ms * 1e-3), "ms_per_step": exact_ms / steps,
+                           "bricks_evaluated": exact_kept}
+    sur["dense"] = {"value": world * samples * steps / (dense_ms * 1e-3), "ms_per_step": dense_ms / steps}
+    sur["steps"] = steps
+    return sur
 
 
 def our_arm(args, rank, world, local_rank):
@@ -454,6 +598,7 @@ def our_arm(args, rank, world, local_rank):
     # skip (alone, or followed by the exact test); same mesh required.
     surrogate = None if args.skip_surrogate else surrogate_leg(prog, grid, samples, args, stream, sp, flush, total_ms, dense_ms,
                                                                 world)
+    surrogate_1024 = None if args.skip_surrogate else surrogate_1024_leg(prog, args, stream, sp, flush, world)
 
     # End to end through the C ABI: tree handle in, host mesh out, every step.
     e2e_steps = 0 if args.skip_e2e else max(3, min(args.steps, 10))
@@ -535,15 +680,13 @@ def our_arm(args, rank, world, local_rank):
             "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "samples_per_mesh": samples, "vertices": vertex_count,
-                       "faces": face_count, "octree_cells": info.octree_cells,
-                       "l2": "flushed between steps (512 MB write outside the per-step events); "
-                             "per-step working set 0.55 GB lattice > L2",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": CONFIG,
+            "mesh": {"vertices": vertex_count, "faces": face_count, "octree_cells": info.octree_cells},
             "meshes_per_s": world * args.steps / (total_ms * 1e-3),
             "bricks": {"size_cells": 7, "total": bricks, "evaluated": active_bricks,
                        "evaluated_fraction": active_bricks / max(1, bricks)},
             "surrogate_culled": surrogate,
+            "surrogate_culled_1024": surrogate_1024,
             "dense_export": {"value": world * samples * args.steps / (dense_ms * 1e-3), "unit": "samples/s",
                              "ms_per_step": dense_ms / args.steps, "eval_grid_ms": eval_grid_ms,
                              "note": "every lattice point evaluated (the reference's work); identical mesh"},
@@ -1011,7 +1154,7 @@ def exports_arm(args, rank, world, local_rank):
 
 
 def main():
-    global RES, WORKLOAD
+    global RES, WORKLOAD, CONFIG
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -1020,10 +1163,15 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--batch-models", type=int, default=512, help="trees in the batch workload")
-    ap.add_argument("--workload", default="export", choices=["export", "render", "surrogate", "batch", "exports"],
+    ap.add_argument("--port", action="store_true", help="reference arm: time the C restatement even where the "
+                                                        "reference library loads")
+    ap.add_argument("--compare-res", type=int, default=512, help="cpu-compare: grid resolution")
+    ap.add_argument("--workload", default="export",
+                    choices=["export", "render", "surrogate", "batch", "exports", "cpu-compare"],
                     help="export: the 512^3 mesh export (the benchmark); render: the sphere-tracing workload; "
                          "surrogate: the 1024^3 export in 32^3 bricks with the learned bound; batch: 512 trees in one "
-                         "launch; exports: Sodapop meshing, point cloud and MagicaVoxel")
+                         "launch; exports: Sodapop meshing, point cloud and MagicaVoxel; cpu-compare: the reference's "
+                         "CPU export against the C restatement (x86 host with the reference sources)")
     ap.add_argument("--skip-surrogate", action="store_true", help="skip the surrogate-culled leg of the export")
     ap.add_argument("--resolution", type=int, default=RES,
                     help="grid resolution (512 is the benchmark; smaller values are profiling cases)")
@@ -1031,10 +1179,13 @@ def main():
     if args.resolution != RES:
         WORKLOAD = WORKLOAD.replace(f"{RES}^3", f"{args.resolution}^3").replace(f"({RES + 3}^3", f"({args.resolution + 3}^3")
         RES = args.resolution
+        CONFIG = dict(CONFIG, workload=WORKLOAD, samples_per_mesh=(RES + 3) ** 3)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.workload == "cpu-compare":
+        cpu_compare(args)
+    elif args.impl == "reference":
         reference_arm(args, rank)
     elif args.workload == "render":
         render_arm(args, rank, world, local_rank)

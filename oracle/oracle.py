@@ -65,6 +65,12 @@ class Drawable:
         self.grid = grid
 
 
+def _steps(grid):
+    """Per-axis steps of an export grid (one step for all axes unless it has step_y/z)."""
+    s = grid.step
+    return s, (getattr(grid, "step_y", 0.0) or s), (getattr(grid, "step_z", 0.0) or s)
+
+
 def _vec3(v):
     return np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float32), (3,)))
 
@@ -282,7 +288,7 @@ class PortOracle(CpuOracle):
     def octree_grid(self, o, grid, threads=0):
         nx, ny, nz = grid.sx + 1, grid.sy + 1, grid.sz + 1
         out = np.empty(nx * ny * nz, np.float32)
-        self._oct_grid(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, nx, ny, nz, threads, out)
+        self._oct_grid(o, grid.x0, grid.y0, grid.z0, *_steps(grid), nx, ny, nz, threads, out)
         return out.reshape(nz, ny, nx)
 
     def surface_nets(self, o, grid, threads=0, faithful=False) -> Mesh:
@@ -291,7 +297,7 @@ class PortOracle(CpuOracle):
         F = C.POINTER(C.c_uint64)()
         nf = C.c_int64()
         secs = C.c_double()
-        nv = self._sn(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, grid.sx, grid.sy, grid.sz,
+        nv = self._sn(o, grid.x0, grid.y0, grid.z0, *_steps(grid), grid.sx, grid.sy, grid.sz,
                       threads, int(faithful), C.byref(V), C.byref(Cb), C.byref(F), C.byref(nf), C.byref(secs))
         if nv < 0:
             raise ValueError("grid with a strictly longest axis is not restated")
@@ -377,12 +383,27 @@ class ReferenceOracle(CpuOracle):
         self._vox_serial = self._fn("vox_serial", i64, [vp, f, i, C.c_char_p, self._i32pp, C.POINTER(C.c_int32),
                                                         C.POINTER(C.c_float)])
         self._raymarch = self._fn("raymarch", None, [vp, i64, _f32p, _f32p, i, f, i, _u8p, _f32p, _f32p])
+        self._attrs = self._fn("vertex_attributes", None, [vp, i64, _f32p, i, _f32p, C.c_void_p])
+        self._oct_paint = self._fn("octree_has_paint", i, [vp])
+        self._hw = self._fn("hardware_threads", i, [])
 
     def octree_grid(self, o, grid):
         nx, ny, nz = grid.sx + 1, grid.sy + 1, grid.sz + 1
         out = np.empty(nx * ny * nz, np.float32)
-        self._oct_grid(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, nx, ny, nz, out)
+        self._oct_grid(o, grid.x0, grid.y0, grid.z0, *_steps(grid), nx, ny, nz, out)
         return out.reshape(nz, ny, nx)
+
+    def hardware_threads(self):
+        return self._hw()
+
+    def vertex_attributes(self, o, vertices, threads=0):
+        """WritePLY(Octree, ...)'s per-vertex Gradient + GetMaterial colour bytes on Pool()
+        (threads=0) or that many threads."""
+        v = self._pts(vertices)
+        normals = np.empty_like(v)
+        colors = np.empty(v.shape, np.uint8) if self._oct_paint(o) else None
+        self._attrs(o, v.shape[0], v, threads, normals, colors.ctypes.data_as(C.c_void_p) if colors is not None else None)
+        return normals, colors
 
     def surface_nets(self, o, grid, threads=1) -> Mesh:
         V = C.POINTER(C.c_float)()
@@ -390,7 +411,7 @@ class ReferenceOracle(CpuOracle):
         F = C.POINTER(C.c_uint64)()
         nf = C.c_int64()
         secs = C.c_double()
-        nv = self._sn(o, grid.x0, grid.y0, grid.z0, grid.step, grid.step, grid.step, grid.sx, grid.sy, grid.sz,
+        nv = self._sn(o, grid.x0, grid.y0, grid.z0, *_steps(grid), grid.sx, grid.sy, grid.sz,
                       threads, C.byref(V), C.byref(Cb), C.byref(F), C.byref(nf), C.byref(secs))
         verts = np.ctypeslib.as_array(V, shape=(max(1, nv) * 3,))[: nv * 3].reshape(nv, 3).copy()
         cubes = np.ctypeslib.as_array(Cb, shape=(max(1, nv),))[:nv].copy()

@@ -466,6 +466,45 @@ extern "C"
 		}
 	}
 
+	// Octree->Evaluator->HasPaint(): WritePLY(Octree, ...) writes colours (export.cpp:285).
+	int ref_octree_has_paint(void* Handle)
+	{
+		return ((RefOctree*)Handle)->Octree->Evaluator->HasPaint() ? 1 : 0;
+	}
+
+	// WritePLY(Octree, ...)'s per-vertex attribute loop (export.cpp:283-317: Gradient, then
+	// GetMaterial -> SampleColor -> 0xFF * c when the tree has paint) over Pool() threads
+	// (Threads <= 0) or `Threads` threads, vertices handed out in order.  Colors may be null.
+	void ref_vertex_attributes(void* Handle, int64_t Count, const float* Points, int Threads, float* Normals, uint8_t* Colors)
+	{
+		SDFOctreeShared Octree = ((RefOctree*)Handle)->Octree;
+		std::atomic<int64_t> Next(0);
+		auto Thunk = [&]()
+		{
+			for (int64_t i = Next.fetch_add(256); i < Count; i = Next.fetch_add(256))
+			{
+				const int64_t End = std::min<int64_t>(Count, i + 256);
+				for (int64_t v = i; v < End; ++v)
+				{
+					const vec3 P(Points[v * 3 + 0], Points[v * 3 + 1], Points[v * 3 + 2]);
+					const vec3 G = Octree->Gradient(P);
+					Normals[v * 3 + 0] = G.x; Normals[v * 3 + 1] = G.y; Normals[v * 3 + 2] = G.z;
+					if (Colors) ColorBytes(Octree->GetMaterial(P), Colors + v * 3);
+				}
+			}
+		};
+		if (Threads <= 0)
+		{
+			Pool(Thunk);
+		}
+		else
+		{
+			std::vector<std::thread> Workers;
+			for (int t = 0; t < Threads; ++t) Workers.emplace_back(Thunk);
+			for (auto& W : Workers) W.join();
+		}
+	}
+
 	// Runs Tangerine's naive surface nets (the AsyncParallelSurfaceNets thunks that
 	// par_surface_nets drives, surface_nets.cpp:1148-1205) over the export octree, with
 	// the z-slices and then the active-cell map entries spread over Pool() threads.
