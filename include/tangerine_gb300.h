@@ -599,6 +599,9 @@ TANGERINE_API tg_status tg_surrogate_set_margin(tg_surrogate* s, float margin);
 enum
 {
 	TG_MESH_SURROGATE_ONLY = 1u << 20,
+	/* Brick evaluation: a brick inside one octree cell copies that cell's distance program
+	   into shared memory (one bulk copy) and reads its records there (same results). */
+	TG_MESH_STAGED = 1u << 21,
 };
 TANGERINE_API tg_status tg_export_mesh_surrogate(tg_program* program, tg_surrogate* s, const tg_grid* grid, uint32_t flags,
                                                  tg_mesh* out, void* stream);

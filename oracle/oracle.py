@@ -20,7 +20,21 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_SO = HERE / "_build" / "libtg_oracle.so"
 REF_SO = HERE / "_ref" / "libtangerine_ref.so"
-REFERENCE_SOURCES = Path(os.environ.get("TANGERINE_REFERENCE", "/root/reference"))
+
+
+def _reference_sources() -> Path:
+    """Where Tangerine's sources are: TANGERINE_REFERENCE, else the build recipe's REF
+    (oracle/Makefile, the one place that names this machine's copy)."""
+    env = os.environ.get("TANGERINE_REFERENCE")
+    if env:
+        return Path(env)
+    for line in (HERE / "Makefile").read_text().splitlines():
+        if line.startswith("REF ?="):
+            return Path(line.split("?=", 1)[1].strip())
+    return HERE / "_ref" / "no-reference"
+
+
+REFERENCE_SOURCES = _reference_sources()
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")

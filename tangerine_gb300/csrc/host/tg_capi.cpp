@@ -149,6 +149,7 @@ namespace
 		const int lanes = (int)((flags >> 16) & 0xFu);
 		// Default: 2 points per thread for the culled export, 4 for the dense one (measured).
 		o.Lanes = (lanes == 1 || lanes == 2 || lanes == 4) ? lanes : (o.Dense ? 4 : 2);
+		o.Staged = (flags & TG_MESH_STAGED) != 0;
 		return o;
 	}
 

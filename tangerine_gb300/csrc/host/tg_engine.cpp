@@ -286,12 +286,12 @@ namespace tg
 		const int64_t lattice = (int64_t)g.NX * g.NY * g.NZ;
 		const int64_t cells = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
 		const int64_t words = (cells + 31) / 32;
-		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 4 * sizeof(uint32_t)));
+		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 8 * sizeof(uint32_t)));
 
 		TG_TRY(LatticeBuf.Reserve((size_t)lattice * sizeof(float)));
 		TG_TRY(Words.Reserve((size_t)words * 4));
 		TG_TRY(WordBase.Reserve((size_t)words * 4));
-		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
+		TG_TRY(Counts.Reserve(8 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4));
 
 		if (opt.Dense)
@@ -349,8 +349,10 @@ namespace tg
 			End(s);
 			LastBrickSize = B;
 			Begin("eval_bricks", s);
+			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);
+			TG_TRY(cudaMemsetAsync(evalStatus, 0, sizeof(int), s));
 			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), SmCount, s,
-				opt.Lanes));
+				opt.Lanes, opt.Staged, evalStatus));
 			End(s);
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.
 			TG_TRY(ActiveCells.Reserve((size_t)(nb * (int64_t)B * B * B < cells ? nb * (int64_t)B * B * B : cells) * 4));
@@ -358,7 +360,7 @@ namespace tg
 			TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
 				ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, SmCount, s));
 			End(s);
-			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 8, cudaMemcpyDeviceToHost, s));
+			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 12, cudaMemcpyDeviceToHost, s));
 			Bricks = nb;
 		}
 		Begin("scan", s);
@@ -368,6 +370,11 @@ namespace tg
 		TG_TRY(cudaStreamSynchronize(s));
 		const uint32_t vcount = HostCounts[0];
 		if (!opt.Dense) ActiveBricks = HostCounts[2];
+		if (!opt.Dense && HostCounts[4] != 0)
+		{
+			SetError("brick evaluation: a program copy to shared memory did not complete in time");
+			return cudaErrorLaunchTimeout;
+		}
 		if (stopped(0.6f)) return cudaSuccess;
 
 		TG_TRY(Vertices.Reserve((size_t)vcount * 12));

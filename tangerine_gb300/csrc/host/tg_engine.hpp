@@ -70,6 +70,7 @@ namespace tg
 		bool Dense = false;         // evaluate every lattice point (no brick culling)
 		int BrickSize = 7;          // cells per brick edge when culling (1..15)
 		int Lanes = 2;              // lattice points per thread sharing one pass over records
+		bool Staged = false;        // brick evaluation reads single-cell bricks' programs from shared memory
 		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
 		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
 		HostMeshOut* Host = nullptr;        // also copy the mesh to host memory (see HostMeshOut)

@@ -94,7 +94,7 @@ namespace tg
 	{
 		out = DeviceMesh();
 		const int64_t words = (s.Total + 31) / 32;
-		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 4 * sizeof(uint32_t)));
+		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 8 * sizeof(uint32_t)));
 		TG_TRY(Words.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(WordBase.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
@@ -156,7 +156,7 @@ namespace tg
 	{
 		cells.clear();
 		const int64_t words = (s.Total + 31) / 32;
-		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 4 * sizeof(uint32_t)));
+		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 8 * sizeof(uint32_t)));
 		TG_TRY(Words.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(WordBase.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));

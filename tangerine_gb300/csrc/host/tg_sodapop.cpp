@@ -89,7 +89,7 @@ namespace tg
 		const int64_t lattice = (g.SX + 1) * (g.SY + 1) * g.LZ;
 		const int64_t words = (g.Limit + 31) / 32;
 		const int leaves = (int)(boxes.size() / 6);
-		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 4 * sizeof(uint32_t)));
+		if (!HostCounts) TG_TRY(cudaMallocHost(&HostCounts, 8 * sizeof(uint32_t)));
 		TG_TRY(LatticeBuf.Reserve((size_t)lattice * sizeof(float)));
 		TG_TRY(Words.Reserve((size_t)words * 4));
 		TG_TRY(WordBase.Reserve((size_t)words * 4));

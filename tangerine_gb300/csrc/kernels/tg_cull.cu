@@ -20,6 +20,7 @@
 #include "tg_surface.cuh"
 #include "tg_cull.cuh"
 #include "tg_pair.cuh"
+#include "tg_tc.cuh"
 
 namespace tg
 {
@@ -91,11 +92,25 @@ namespace tg
 		// four z-consecutive points through one pass over their octree cell's records.
 		// A CTA is 8 x 8 columns x (128 / 64) z-groups; each thread runs K z-consecutive
 		// points, so one pass covers an 8 x 8 x 2K chunk of the brick's lattice box.
-		template<int C, int K>
+		// Stage = true: a brick whose points all descend to one octree cell (the common case)
+		// first copies that cell's distance program into shared memory with one bulk copy
+		// (cp.async.bulk, completion on an mbarrier, bounded wait), and every point of the
+		// brick reads its records there; other bricks read them from global memory.  Both go
+		// through one generic-address load, so the interpreter is compiled once.
+		template<int C, int K, bool Stage>
 		__global__ void __launch_bounds__(kBrickThreads, EvalBricksCtasPerSm<C>()) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice)
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice, int spill_floats,
+			int stage_quads, int* __restrict__ status)
 		{
-			extern __shared__ float spill[];
+			extern __shared__ __align__(16) float spill[];
+			__shared__ uint64_t staged_bar;
+			float4* staged = reinterpret_cast<float4*>(spill + spill_floats);
+			uint32_t phase = 0;
+			if (Stage)
+			{
+				if (threadIdx.x == 0) tc::BarInit(&staged_bar, 1);
+				__syncthreads();
+			}
 			constexpr int ZSpan = 2 * K;
 			const uint32_t n = *count;
 			const int tx = threadIdx.x & 7, ty = (threadIdx.x >> 3) & 7, tz = threadIdx.x >> 6;
@@ -113,6 +128,29 @@ namespace tg
 				const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.DX), LatticeCoord(g.X0, i1, g.DX),
 					LatticeCoord(g.Y0, j0, g.DY), LatticeCoord(g.Y0, j1, g.DY), LatticeCoord(g.Z0, k0, g.DZ),
 					LatticeCoord(g.Z0, k1, g.DZ), shared);
+				// Record reads go through `code` (generic address): the staged copy, offset so that
+				// the program's own record numbers index it, or the program's global records.
+				const float4* code = prog.Code;
+				if (Stage && shared)
+				{
+					const int dc = __ldg(&prog.Nodes[top].DistanceCode);
+					const int len = __ldg(&prog.Nodes[top].SurfaceCode) - dc;
+					if (len > 0 && len <= stage_quads)
+					{
+						__syncthreads();   // every thread is done with the previous brick's copy
+						if (threadIdx.x == 0) tc::BulkLoad(staged, prog.Code + dc, (uint32_t)len * 16u, &staged_bar);
+						if (!tc::BarWait(&staged_bar, phase))
+						{
+							// The copy did not complete in time: report it, wait (bounded) for the
+							// copy still in flight, and leave.
+							atomicExch(status, 1);
+							tc::BarWait(&staged_bar, phase);
+							return;
+						}
+						phase ^= 1u;
+						code = staged - dc;
+					}
+				}
 				for (int oz = 0; oz < C; oz += ZSpan)
 				for (int oy = 0; oy < C; oy += 8)
 				for (int ox = 0; ox < C; ox += 8)
@@ -145,9 +183,16 @@ namespace tg
 						if constexpr (K % 2 == 0)
 						{
 							// Points in pairs through the paired FP32 instructions (tg_pair.cuh).
-							const float4* code = prog.Code;
-							RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
-								spill + 2 * threadIdx.x, kBrickThreads);
+							if (Stage)
+							{
+								RunDistancePaired<K>([&](int q) { return code[q]; }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
+									spill + 2 * threadIdx.x, kBrickThreads);
+							}
+							else
+							{
+								RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px,
+									py, pz, r, spill + 2 * threadIdx.x, kBrickThreads);
+							}
 						}
 						else
 						{
@@ -411,41 +456,57 @@ namespace tg
 
 	namespace
 	{
-		template<int C, int K>
-		cudaError_t LaunchEvalBricksCK(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int sms, cudaStream_t stream)
+		// Shared memory of a CTA at the compiled occupancy, with a little left for the
+		// mbarrier and the runtime's reserve; the staged program gets what the spill leaves.
+		constexpr size_t kStageBudget = 20 * 1024;
+
+		template<int C, int K, bool Stage>
+		cudaError_t LaunchEvalBricksCKS(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+			float* lattice, int sms, cudaStream_t stream, int* status)
 		{
 			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
-			const size_t smem = (size_t)depth * K * kBrickThreads * sizeof(float);
+			const size_t spill = (size_t)depth * K * kBrickThreads * sizeof(float);
+			int stageQuads = 0;
+			if (Stage && spill + 16 * 64 <= kStageBudget) stageQuads = (int)((kStageBudget - spill) / 16);
+			const size_t smem = spill + (size_t)stageQuads * 16;
 			if (smem > 48 * 1024)
 			{
-				cudaError_t e = cudaFuncSetAttribute(EvalBricksKernel<C, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+				cudaError_t e = cudaFuncSetAttribute(EvalBricksKernel<C, K, Stage>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 				if (e != cudaSuccess) return e;
 			}
-			EvalBricksKernel<C, K><<<sms * EvalBricksCtasPerSm<C>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list, count, lattice);
+			EvalBricksKernel<C, K, Stage><<<sms * EvalBricksCtasPerSm<C>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list,
+				count, lattice, (int)(spill / sizeof(float)), stageQuads, status);
 			return cudaGetLastError();
+		}
+
+		template<int C, int K>
+		cudaError_t LaunchEvalBricksCK(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
+			float* lattice, int sms, cudaStream_t stream, bool staged, int* status)
+		{
+			if (staged) return LaunchEvalBricksCKS<C, K, true>(prog, g, B, list, count, lattice, sms, stream, status);
+			return LaunchEvalBricksCKS<C, K, false>(prog, g, B, list, count, lattice, sms, stream, status);
 		}
 
 		template<int C>
 		cudaError_t LaunchEvalBricksC(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int sms, cudaStream_t stream, int lanes)
+			float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
 		{
 			switch (lanes)
 			{
-			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, sms, stream);
-			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, sms, stream);
-			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, sms, stream);
+			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, sms, stream, staged, status);
+			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, sms, stream, staged, status);
+			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, sms, stream, staged, status);
 			}
 		}
 	}
 
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int sms, cudaStream_t stream, int lanes)
+		float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
 	{
-		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, sms, stream, lanes);
-		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, sms, stream, lanes);
-		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, sms, stream, lanes);
-		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, sms, stream, lanes);
+		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
 		return cudaErrorInvalidValue;
 	}
 

@@ -9,6 +9,7 @@
 #include "tg_device.cuh"
 #include "tg_kernels.hpp"
 #include "tg_surface.cuh"
+#include "tg_pair.cuh"
 
 namespace tg
 {
@@ -107,32 +108,42 @@ namespace tg
 			return e[0];
 		}
 
-		// Normals alone: four threads per vertex, one per tetrahedral offset, all running the
-		// same code; lane 0 combines them and evaluates the vertex itself only when the four
-		// cancel (SDFNode::Gradient's fallback).  The colours are a separate pass, so no lane
-		// takes the material path while the others wait.
+		// Normals alone: two threads per vertex, each evaluating two of the four tetrahedral
+		// points as one pair (tg_pair.cuh), all running the same code; lane 0 combines them and
+		// evaluates the vertex itself only when the four cancel (SDFNode::Gradient's
+		// fallback).  The colours are a separate pass, so no lane takes the material path
+		// while the others wait.
 		constexpr int kNormalThreads = 128;
-		constexpr int kNormalPoints = kNormalThreads / 4;
+		constexpr int kNormalPoints = kNormalThreads / 2;
 
 		__global__ void __launch_bounds__(kNormalThreads) VertexNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
 			uint32_t n, float* __restrict__ normals)
 		{
 			extern __shared__ float spill[];
-			const int local = threadIdx.x >> 2, lane = threadIdx.x & 3;
+			const int local = threadIdx.x >> 1, lane = threadIdx.x & 1;
 			const uint32_t v = blockIdx.x * kNormalPoints + local;
 			Vec3 p(0.0f, 0.0f, 0.0f);
-			float mine = 0.0f;
+			float2 mine = make_float2(0.0f, 0.0f);
+			int pc = 0;
+			const float4* code = prog.Code;
+			auto load = [&](int q) { return __ldg(code + q); };
+			float2* spill2 = reinterpret_cast<float2*>(spill) + threadIdx.x;
 			if (v < n)
 			{
 				p = Vec3(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
-				mine = EvaluationLane(prog, p, lane, false, nullptr, spill + threadIdx.x, kNormalThreads);
+				const int cell = DescendOctree(prog.Nodes, p.x, p.y, p.z);
+				pc = __ldg(&prog.Nodes[cell].SurfaceCode);
+				const Vec3 a = TetraPoint(p, 2 * lane), b = TetraPoint(p, 2 * lane + 1);
+				mine = RunSurfacePair(load, pc, make_float2(a.x, b.x), make_float2(a.y, b.y), make_float2(a.z, b.z), spill2,
+					kNormalThreads);
 			}
-			// The four lanes of a vertex are neighbours in one warp.
+			// The two lanes of a vertex are neighbours in one warp.
+			const int first = (threadIdx.x & 31) & ~1;
 			float e[5];
-			e[0] = __shfl_sync(0xFFFFFFFFu, mine, (threadIdx.x & 31) & ~3);
-			e[1] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 1);
-			e[2] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 2);
-			e[3] = __shfl_sync(0xFFFFFFFFu, mine, ((threadIdx.x & 31) & ~3) + 3);
+			e[0] = __shfl_sync(0xFFFFFFFFu, mine.x, first);
+			e[1] = __shfl_sync(0xFFFFFFFFu, mine.y, first);
+			e[2] = __shfl_sync(0xFFFFFFFFu, mine.x, first + 1);
+			e[3] = __shfl_sync(0xFFFFFFFFu, mine.y, first + 1);
 			if (v < n && lane == 0)
 			{
 				e[4] = 0.0f;
@@ -143,7 +154,11 @@ namespace tg
 				g = g + yxy * e[2];
 				g = g + xxx * e[3];
 				if ((g.x * g.x + g.y * g.y) + g.z * g.z == 0.0f)
-					e[4] = EvaluationLane(prog, p, 4, false, nullptr, spill + threadIdx.x, kNormalThreads);
+				{
+					// The vertex itself, in the same spill layout (both lanes of the pair at p).
+					e[4] = RunSurfacePair(load, pc, make_float2(p.x, p.x), make_float2(p.y, p.y), make_float2(p.z, p.z), spill2,
+						kNormalThreads).x;
+				}
 				const Vec3 r = GradientOf(e);
 				normals[(int64_t)v * 3 + 0] = r.x;
 				normals[(int64_t)v * 3 + 1] = r.y;

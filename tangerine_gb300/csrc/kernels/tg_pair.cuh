@@ -250,4 +250,94 @@ namespace tg
 #pragma unroll
 		for (int j = 0; j < NP; ++j) { out[2 * j] = r[j].x; out[2 * j + 1] = r[j].y; }
 	}
+
+	// Cross(a, b) of tg_math.hpp for a uniform a and a pair b:
+	// { a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y }.
+	__device__ __forceinline__ void CrossPair(float ax, float ay, float az, float2 bx, float2 by, float2 bz,
+		float2& cx, float2& cy, float2& cz, const PairUnits& u)
+	{
+		cx = Sub2(Mul2(Pair(ay), bz, u), Mul2(by, Pair(az), u), u);
+		cy = Sub2(Mul2(Pair(az), bx, u), Mul2(bz, Pair(ax), u), u);
+		cz = Sub2(Mul2(Pair(ax), by, u), Mul2(bx, Pair(ay), u), u);
+	}
+
+	// SDFNode::Eval through a surface program (RunSurfaceBatch in tg_device.cuh without the
+	// material walk) for one pair of points: every brush rotates the point by its inverse
+	// quaternion, q * v = v + ((cross(q.xyz, v) * w) + cross(q.xyz, cross(q.xyz, v))) * 2,
+	// after subtracting its translation, divides by its scale (skipped at scale 1: x / 1 is
+	// x), and multiplies the brush distance by the scale.  `spill`: entry `depth` at
+	// spill[depth * stride] (a float2).
+	template<typename Load>
+	__device__ __forceinline__ float2 RunSurfacePair(Load load, int pc, float2 px, float2 py, float2 pz, float2* spill, int stride)
+	{
+		const PairUnits u = LoadPairUnits();
+		float2 acc = make_float2(0.0f, 0.0f);
+		int depth = 0;
+		for (int guard = 0; guard < (1 << 24); ++guard)
+		{
+			const float4 h = load(pc++);
+			const uint32_t head = __float_as_uint(h.x);
+			const uint32_t op = head & 0xFFu;
+			if (op >= OpSphere && op <= OpPlane)
+			{
+				const bool thenSet = (head & RecThenSet) != 0;
+				const float2 left = acc;
+				if (!thenSet)
+				{
+					if (depth > 0) spill[(depth - 1) * stride] = acc;
+					++depth;
+				}
+				const float4 Q = load(pc);
+				const float4 T = load(pc + 1);
+				pc += 3;
+				const float2 vx = Sub2(px, Pair(T.x), u), vy = Sub2(py, Pair(T.y), u), vz = Sub2(pz, Pair(T.z), u);
+				// The quad holds the inverse quaternion as (w, x, y, z).
+				float2 ux, uy, uz, wx, wy, wz;
+				CrossPair(Q.y, Q.z, Q.w, vx, vy, vz, ux, uy, uz, u);
+				CrossPair(Q.y, Q.z, Q.w, ux, uy, uz, wx, wy, wz, u);
+				float2 lx = Add2(vx, Mul2(Add2(Mul2(ux, Pair(Q.x), u), wx, u), Pair(2.0f), u), u);
+				float2 ly = Add2(vy, Mul2(Add2(Mul2(uy, Pair(Q.x), u), wy, u), Pair(2.0f), u), u);
+				float2 lz = Add2(vz, Mul2(Add2(Mul2(uz, Pair(Q.x), u), wz, u), Pair(2.0f), u), u);
+				const bool scaled = T.w != 1.0f;
+				if (scaled)
+				{
+					lx = make_float2(lx.x / T.w, lx.y / T.w);
+					ly = make_float2(ly.x / T.w, ly.y / T.w);
+					lz = make_float2(lz.x / T.w, lz.y / T.w);
+				}
+				const float prm[3] = { h.y, h.z, h.w };
+				float2 d = BrushDistance2(op, prm, lx, ly, lz, u);
+				if (scaled) d = Mul2(d, Pair(T.w), u);
+				acc = d;
+				if (thenSet)
+				{
+					const float4 S = load(pc++);
+					acc = SetDistance2(__float_as_uint(S.x) & 0xFFu, left, acc, S.y);
+				}
+			}
+			else if (op >= OpUnion && op <= OpBlendDiff)
+			{
+				--depth;
+				acc = SetDistance2(op, spill[(depth - 1) * stride], acc, h.y);
+			}
+			else if (op == OpFlate)
+			{
+				acc = Sub2(acc, Pair(h.y), u);
+			}
+			else if (op == OpMaskBegin)
+			{
+				pc += (int)__float_as_uint(h.y);
+			}
+			else if (op == OpStencilEnd)
+			{
+				--depth;
+				acc = spill[(depth - 1) * stride];
+			}
+			else
+			{
+				break;   // OpStop
+			}
+		}
+		return acc;
+	}
 }

@@ -189,9 +189,9 @@ def _grid(g) -> _lib.Grid:
                      getattr(g, "step_z", 0.0))
 
 
-def _flags(attributes=True, dense=False, brick=0, lanes=0, surrogate_only=False) -> int:
+def _flags(attributes=True, dense=False, brick=0, lanes=0, surrogate_only=False, staged=False) -> int:
     return ((1 if attributes else 0) | (2 if dense else 0) | ((int(brick) & 0xFF) << 8) | ((int(lanes) & 0xF) << 16)
-            | ((1 << 20) if surrogate_only else 0))
+            | ((1 << 20) if surrogate_only else 0) | ((1 << 21) if staged else 0))
 
 
 def last_export_stats():
@@ -295,17 +295,18 @@ class Program:
         check(load().tg_eval_points(self.ptr, _lib.as_ptr(p), p.shape[0], _lib.as_ptr(out), stream), "tg_eval_points")
         return out
 
-    def export_mesh(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None) -> Mesh:
+    def export_mesh(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None, staged=False) -> Mesh:
         g = _grid(grid)
         hm = _lib.HostMesh()
-        check(load().tg_export_mesh(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes), C.byref(hm), stream),
+        check(load().tg_export_mesh(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes, staged=staged), C.byref(hm),
+                                    stream),
               "tg_export_mesh")
         return _take_mesh(hm)
 
-    def export_mesh_device(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None) -> _lib.DeviceMesh:
+    def export_mesh_device(self, grid, attributes=True, dense=False, brick=0, lanes=0, stream=None, staged=False) -> _lib.DeviceMesh:
         g = _grid(grid)
         dm = _lib.DeviceMesh()
-        check(load().tg_export_mesh_device(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes), C.byref(dm), stream),
+        check(load().tg_export_mesh_device(self.ptr, C.byref(g), _flags(attributes, dense, brick, lanes, staged=staged), C.byref(dm), stream),
               "tg_export_mesh_device")
         return dm
 

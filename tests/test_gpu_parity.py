@@ -203,10 +203,13 @@ def test_culled_export_full_size(lib):
         dense = prog.export_mesh(grid, dense=True)
         culled = prog.export_mesh(grid)
         bricks, active = sdf.last_export_stats()
+        staged = prog.export_mesh(grid, staged=True)
+        staged4 = prog.export_mesh(grid, staged=True, lanes=4, brick=15)
     assert active < bricks // 3
-    for a, b in ((dense.vertices, culled.vertices), (dense.faces, culled.faces), (dense.normals, culled.normals),
-                 (dense.colors, culled.colors)):
-        np.testing.assert_array_equal(a, b)
+    for m in (culled, staged, staged4):
+        for a, b in ((dense.vertices, m.vertices), (dense.faces, m.faces), (dense.normals, m.normals),
+                     (dense.colors, m.colors)):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_export_tree_matches_program_export(lib):
