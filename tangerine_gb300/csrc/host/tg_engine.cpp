@@ -349,8 +349,8 @@ namespace tg
 			End(s);
 			LastBrickSize = B;
 			Begin("eval_bricks", s);
-			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);
-			TG_TRY(cudaMemsetAsync(evalStatus, 0, sizeof(int), s));
+			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);      // status and work counter
+			TG_TRY(cudaMemsetAsync(evalStatus, 0, 2 * sizeof(int), s));
 			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), SmCount, s,
 				opt.Lanes, opt.Staged, evalStatus));
 			End(s);

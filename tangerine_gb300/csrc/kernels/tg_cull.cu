@@ -87,36 +87,47 @@ namespace tg
 			}
 		}
 
+		constexpr int kBrickWarps = kBrickThreads / 32;
+
 		// Lattice points of every listed brick: corners [i0, i0 + B] per axis, clamped to the
-		// lattice.  A CTA takes bricks from the list with a grid stride; each thread runs
-		// four z-consecutive points through one pass over their octree cell's records.
-		// A CTA is 8 x 8 columns x (128 / 64) z-groups; each thread runs K z-consecutive
-		// points, so one pass covers an 8 x 8 x 2K chunk of the brick's lattice box.
-		// Stage = true: a brick whose points all descend to one octree cell (the common case)
-		// first copies that cell's distance program into shared memory with one bulk copy
-		// (cp.async.bulk, completion on an mbarrier, bounded wait), and every point of the
-		// brick reads its records there; other bricks read them from global memory.  Both go
-		// through one generic-address load, so the interpreter is compiled once.
+		// lattice.  A brick's box is covered in 8 x 8 column blocks x 2 z-groups: a brick has
+		// four slices, slice s holding rows 4 (s & 1) .. 4 (s & 1) + 3 of each 8 x 8 block and
+		// z-group s >> 1; a lane runs K z-consecutive points of its column through one pass
+		// over their octree cell's records, so one pass of a slice covers an 8 x 4 x K box.
+		// A warp draws (brick, slice) items from a counter and goes on to its next item when it
+		// is done: a brick's cost follows its cell programs' lengths, and a fixed stride over
+		// the list left some SMs working for 1.3 times the mean.  The four slices of a brick
+		// are consecutive items, so they mostly run at the same time and share the records in
+		// L1.
+		// Stage = true: a warp whose brick's points all descend to one octree cell (the common
+		// case) first copies that cell's distance program into its own shared memory with one
+		// bulk copy (cp.async.bulk, completion on the warp's mbarrier, bounded wait) and reads
+		// the records there; other bricks read them from global memory.  Both go through one
+		// generic-address load, so the interpreter is compiled once.
 		template<int C, int K, bool Stage>
 		__global__ void __launch_bounds__(kBrickThreads, EvalBricksCtasPerSm<C>()) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice, int spill_floats,
-			int stage_quads, int* __restrict__ status)
+			int stage_quads, int* __restrict__ status, uint32_t* __restrict__ next)
 		{
 			extern __shared__ __align__(16) float spill[];
-			__shared__ uint64_t staged_bar;
-			float4* staged = reinterpret_cast<float4*>(spill + spill_floats);
+			__shared__ uint64_t staged_bar[kBrickWarps];
+			const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+			float4* staged = reinterpret_cast<float4*>(spill + spill_floats) + warp * stage_quads;
 			uint32_t phase = 0;
-			if (Stage)
-			{
-				if (threadIdx.x == 0) tc::BarInit(&staged_bar, 1);
-				__syncthreads();
-			}
+			if (Stage && lane == 0) tc::BarInit(&staged_bar[warp], 1);
+			__syncwarp();
 			constexpr int ZSpan = 2 * K;
-			const uint32_t n = *count;
-			const int tx = threadIdx.x & 7, ty = (threadIdx.x >> 3) & 7, tz = threadIdx.x >> 6;
-			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
+			// Items: a lattice that fits the device has fewer than 2^30 bricks.
+			const uint32_t items = *count * (uint32_t)kBrickWarps;
+			for (;;)
 			{
-				const uint32_t b = __ldg(list + item);
+				uint32_t item = 0;
+				if (lane == 0) item = atomicAdd(next, 1u);
+				item = __shfl_sync(0xffffffffu, item, 0);
+				if (item >= items) break;
+				const int slice = (int)(item % kBrickWarps);
+				const int tx = lane & 7, ty = (lane >> 3) + 4 * (slice & 1), tz = slice >> 1;
+				const uint32_t b = __ldg(list + item / kBrickWarps);
 				const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
 				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
@@ -137,14 +148,13 @@ namespace tg
 					const int len = __ldg(&prog.Nodes[top].SurfaceCode) - dc;
 					if (len > 0 && len <= stage_quads)
 					{
-						__syncthreads();   // every thread is done with the previous brick's copy
-						if (threadIdx.x == 0) tc::BulkLoad(staged, prog.Code + dc, (uint32_t)len * 16u, &staged_bar);
-						if (!tc::BarWait(&staged_bar, phase))
+						if (lane == 0) tc::BulkLoad(staged, prog.Code + dc, (uint32_t)len * 16u, &staged_bar[warp]);
+						if (!tc::BarWait(&staged_bar[warp], phase))
 						{
 							// The copy did not complete in time: report it, wait (bounded) for the
 							// copy still in flight, and leave.
 							atomicExch(status, 1);
-							tc::BarWait(&staged_bar, phase);
+							tc::BarWait(&staged_bar[warp], phase);
 							return;
 						}
 						phase ^= 1u;
@@ -218,6 +228,7 @@ namespace tg
 						}
 					}
 				}
+				__syncwarp();   // every lane is done with this item's staged copy
 			}
 		}
 
@@ -457,7 +468,7 @@ namespace tg
 	namespace
 	{
 		// Shared memory of a CTA at the compiled occupancy, with a little left for the
-		// mbarrier and the runtime's reserve; the staged program gets what the spill leaves.
+		// runtime's reserve; the warps' staged programs get what the spill leaves.
 		constexpr size_t kStageBudget = 20 * 1024;
 
 		template<int C, int K, bool Stage>
@@ -467,15 +478,15 @@ namespace tg
 			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 			const size_t spill = (size_t)depth * K * kBrickThreads * sizeof(float);
 			int stageQuads = 0;
-			if (Stage && spill + 16 * 64 <= kStageBudget) stageQuads = (int)((kStageBudget - spill) / 16);
-			const size_t smem = spill + (size_t)stageQuads * 16;
+			if (Stage && spill + kBrickWarps * 16 * 16 <= kStageBudget) stageQuads = (int)((kStageBudget - spill) / (16 * kBrickWarps));
+			const size_t smem = spill + (size_t)kBrickWarps * stageQuads * 16;
 			if (smem > 48 * 1024)
 			{
 				cudaError_t e = cudaFuncSetAttribute(EvalBricksKernel<C, K, Stage>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 				if (e != cudaSuccess) return e;
 			}
 			EvalBricksKernel<C, K, Stage><<<sms * EvalBricksCtasPerSm<C>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list,
-				count, lattice, (int)(spill / sizeof(float)), stageQuads, status);
+				count, lattice, (int)(spill / sizeof(float)), stageQuads, status, reinterpret_cast<uint32_t*>(status) + 1);
 			return cudaGetLastError();
 		}
 

@@ -76,8 +76,10 @@ namespace tg
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
 		uint32_t* count, cudaStream_t stream);
 	// The brick kernels below run persistent grids sized from the SM count (`sms`).
+	// Brick evaluation.  status[0..1], zeroed by the caller: status[0] becomes nonzero if a
+	// staged program copy does not complete in time; status[1] is the warps' work counter.
 	// staged: bricks inside one octree cell read their program from a shared-memory copy made
-	// by one bulk copy; *status becomes nonzero if such a copy does not complete in time.
+	// by one bulk copy.
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
 		float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
