@@ -465,8 +465,12 @@ namespace tg
 				TG_TRY(Colors.Reserve((size_t)vcount * 3));
 				colors = Colors.As<uint8_t>();
 			}
+			// The culled export visits the vertices in its active-cell list's order (cells
+			// grouped by brick, so a warp's vertices mostly share one surface program).
+			VertexOrder order;
+			if (!opt.Dense) order = { ActiveCells.As<uint32_t>(), Words.As<uint32_t>(), WordBase.As<uint32_t>() };
 			Begin("attributes", s);
-			TG_TRY(LaunchVertexAttributes(p.View, Vertices.As<float>(), vcount, Normals.As<float>(), colors, s));
+			TG_TRY(LaunchVertexAttributes(p.View, Vertices.As<float>(), vcount, Normals.As<float>(), colors, s, order));
 			End(s);
 			out.Normals = Normals.As<float>();
 			out.Colors = colors;

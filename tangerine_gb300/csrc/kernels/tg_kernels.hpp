@@ -123,9 +123,21 @@ namespace tg
 	// Achieved FP32 fused-multiply-add throughput of this GPU (TFLOP/s, 2 flops per FMA).
 	cudaError_t MeasureFp32Peak(double* tflops, cudaStream_t stream);
 
+	// The order the attribute passes visit the vertices in.  Cells == nullptr: vertex order.
+	// Otherwise the active-cell list of the culled export (its cells grouped by brick): entry t
+	// is the vertex of cell Cells[t], numbered as the cell passes number it (rank of the
+	// cell's bit in Words, plus Base of its word).  Neighbouring cells mostly run one surface
+	// program, so a warp visiting them in list order runs one program.
+	struct VertexOrder
+	{
+		const uint32_t* Cells = nullptr;
+		const uint32_t* Words = nullptr;
+		const uint32_t* Base = nullptr;
+	};
+
 	// Gradient normal and colour bytes per vertex (SDFOctree::Gradient / GetMaterial).
 	cudaError_t LaunchVertexAttributes(const DeviceProgram& prog, const float* vertices, uint32_t vertex_count,
-		float* normals, uint8_t* colors, cudaStream_t stream);
+		float* normals, uint8_t* colors, cudaStream_t stream, VertexOrder order = VertexOrder());
 }
 
 namespace tg

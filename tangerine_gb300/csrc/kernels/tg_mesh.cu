@@ -116,12 +116,22 @@ namespace tg
 		constexpr int kNormalThreads = 128;
 		constexpr int kNormalPoints = kNormalThreads / 2;
 
+		// The vertex the attribute passes visit at position t (VertexOrder in tg_kernels.hpp).
+		__device__ __forceinline__ uint32_t VertexAt(const VertexOrder& o, uint32_t t)
+		{
+			if (!o.Cells) return t;
+			const uint32_t c = __ldg(o.Cells + t);
+			const uint32_t w = __ldg(o.Words + (c >> 5));
+			return __ldg(o.Base + (c >> 5)) + __popc(w & ((1u << (c & 31)) - 1u));
+		}
+
 		__global__ void __launch_bounds__(kNormalThreads) VertexNormalsKernel(DeviceProgram prog, const float* __restrict__ vertices,
-			uint32_t n, float* __restrict__ normals)
+			uint32_t n, float* __restrict__ normals, VertexOrder order)
 		{
 			extern __shared__ float spill[];
 			const int local = threadIdx.x >> 1, lane = threadIdx.x & 1;
-			const uint32_t v = blockIdx.x * kNormalPoints + local;
+			const uint32_t t = blockIdx.x * kNormalPoints + local;
+			const uint32_t v = t < n ? VertexAt(order, t) : n;
 			Vec3 p(0.0f, 0.0f, 0.0f);
 			float2 mine = make_float2(0.0f, 0.0f);
 			int pc = 0;
@@ -170,11 +180,12 @@ namespace tg
 		constexpr int kColorThreads = 128;
 
 		__global__ void __launch_bounds__(kColorThreads) VertexColorsKernel(DeviceProgram prog, const float* __restrict__ vertices,
-			uint32_t n, uint8_t* __restrict__ colors)
+			uint32_t n, uint8_t* __restrict__ colors, VertexOrder order)
 		{
 			extern __shared__ float spill[];
-			const uint32_t v = blockIdx.x * kColorThreads + threadIdx.x;
-			if (v >= n) return;
+			const uint32_t t = blockIdx.x * kColorThreads + threadIdx.x;
+			if (t >= n) return;
+			const uint32_t v = VertexAt(order, t);
 			const Vec3 p(vertices[(int64_t)v * 3], vertices[(int64_t)v * 3 + 1], vertices[(int64_t)v * 3 + 2]);
 			int m = -1;
 			EvaluationLane(prog, p, 4, true, &m, spill + threadIdx.x, kColorThreads);
@@ -392,17 +403,19 @@ namespace tg
 	}
 
 	cudaError_t LaunchVertexAttributes(const DeviceProgram& prog, const float* vertices, uint32_t vertex_count,
-		float* normals, uint8_t* colors, cudaStream_t stream)
+		float* normals, uint8_t* colors, cudaStream_t stream, VertexOrder order)
 	{
 		if (vertex_count == 0) return cudaSuccess;
 		const size_t smem = SurfaceSpillBytes(prog, kNormalThreads);
 		if (smem > 40 * 1024) cudaFuncSetAttribute(VertexNormalsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		VertexNormalsKernel<<<Blocks(vertex_count, kNormalPoints), kNormalThreads, smem, stream>>>(prog, vertices, vertex_count, normals);
+		VertexNormalsKernel<<<Blocks(vertex_count, kNormalPoints), kNormalThreads, smem, stream>>>(prog, vertices, vertex_count, normals,
+			order);
 		cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess || !colors) return e;
 		const size_t csmem = SurfaceSpillBytes(prog, kColorThreads);
 		if (csmem > 40 * 1024) cudaFuncSetAttribute(VertexColorsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
-		VertexColorsKernel<<<Blocks(vertex_count, kColorThreads), kColorThreads, csmem, stream>>>(prog, vertices, vertex_count, colors);
+		VertexColorsKernel<<<Blocks(vertex_count, kColorThreads), kColorThreads, csmem, stream>>>(prog, vertices, vertex_count, colors,
+			order);
 		return cudaGetLastError();
 	}
 }
