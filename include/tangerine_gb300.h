@@ -512,6 +512,14 @@ TANGERINE_API tg_status tg_batch_cancel(tg_batch* batch, int cancel);
  * wait runs out: every block leaves and tg_batch_run returns TG_ERR_CUDA ("timed out"),
  * the GPU context stays usable, and the next run (knobs back at 0, -1, 0) is whole. */
 TANGERINE_API tg_status tg_batch_debug_barrier(tg_batch* batch, uint64_t limit_ns, int late_block, uint64_t late_ns);
+/* Test hook for two bounded mbarrier waits.  which = 0: the staged-program copy of the
+ * brick evaluation (TG_MESH_STAGED); which = 1: the network-image copy at the start of the
+ * surrogate kernels.  With limit_ns > 0 (at most 1 s) the wait is made on an mbarrier that
+ * nothing arrives at, so it runs out after limit_ns: the kernel records the failure, waits
+ * (bounded) for its own copy in flight, frees its tensor memory and returns, and the call
+ * returns an error ("did not complete in time" / "timed out").  limit_ns = 0 restores the
+ * normal waits. */
+TANGERINE_API tg_status tg_debug_wait_test(int which, uint64_t limit_ns);
 /* Output capacity for the next run (default: an estimate from the lattices); a run that
  * finds more vertices or faces grows the buffers and runs again (tg_batch_info.reruns). */
 TANGERINE_API tg_status tg_batch_reserve(tg_batch* batch, uint64_t vertices, uint64_t faces);

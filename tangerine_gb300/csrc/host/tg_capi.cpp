@@ -78,6 +78,13 @@ namespace
 	tg_status TakeHostMesh(cudaError_t e, HostMeshOut& h, tg_mesh* out, const char* what)
 	{
 		std::memset(out, 0, sizeof *out);
+		if (e == cudaErrorLaunchTimeout)
+		{
+			// A bounded device wait ran out; the engine said which.
+			FreeHostMesh(h);
+			SetError(std::string(what) + ": " + LastError());
+			return TG_ERR_CUDA;
+		}
 		if (e != cudaSuccess)
 		{
 			FreeHostMesh(h);
@@ -1445,6 +1452,20 @@ extern "C"
 		Engine& eng = Engine::Get();
 		std::lock_guard<std::mutex> lock(eng.Mutex);
 		b->SetBarrierKnobs(limit_ns, late_block, late_ns);
+		return TG_OK;
+	}
+
+	TANGERINE_API tg_status tg_debug_wait_test(int which, uint64_t limit_ns)
+	{
+		if ((which != 0 && which != 1) || limit_ns > 1000000000ull)
+		{
+			SetError("wait test: which is 0 (staged program copy) or 1 (network image), the limit at most 1 s");
+			return TG_ERR_INVALID;
+		}
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		const cudaError_t e = which == 0 ? SetStageWaitTest(limit_ns) : SetSetupWaitTest(limit_ns);
+		if (e != cudaSuccess) return CudaFail(e, "setting a wait test hook");
 		return TG_OK;
 	}
 

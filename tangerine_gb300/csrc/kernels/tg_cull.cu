@@ -89,6 +89,11 @@ namespace tg
 
 		constexpr int kBrickWarps = kBrickThreads / 32;
 
+		// Test hook of the staged-copy wait (SetStageWaitTest): nonzero, a staging warp first
+		// waits this long on an mbarrier that nothing arrives at, so the wait runs out as a
+		// copy that never completes would.
+		__device__ unsigned long long g_stage_wait_test_ns = 0;
+
 		// Lattice points of every listed brick: corners [i0, i0 + B] per axis, clamped to the
 		// lattice.  A brick's box is covered in 8 x 8 column blocks x 2 z-groups: a brick has
 		// four slices, slice s holding rows 4 (s & 1) .. 4 (s & 1) + 3 of each 8 x 8 block and
@@ -110,11 +115,15 @@ namespace tg
 			int stage_quads, int* __restrict__ status, uint32_t* __restrict__ next)
 		{
 			extern __shared__ __align__(16) float spill[];
-			__shared__ uint64_t staged_bar[kBrickWarps];
+			__shared__ uint64_t staged_bar[kBrickWarps], idle_bar[kBrickWarps];
 			const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
 			float4* staged = reinterpret_cast<float4*>(spill + spill_floats) + warp * stage_quads;
 			uint32_t phase = 0;
-			if (Stage && lane == 0) tc::BarInit(&staged_bar[warp], 1);
+			if (Stage && lane == 0)
+			{
+				tc::BarInit(&staged_bar[warp], 1);
+				tc::BarInit(&idle_bar[warp], 1);
+			}
 			__syncwarp();
 			constexpr int ZSpan = 2 * K;
 			// Items: a lattice that fits the device has fewer than 2^30 bricks.
@@ -149,7 +158,9 @@ namespace tg
 					if (len > 0 && len <= stage_quads)
 					{
 						if (lane == 0) tc::BulkLoad(staged, prog.Code + dc, (uint32_t)len * 16u, &staged_bar[warp]);
-						if (!tc::BarWait(&staged_bar[warp], phase))
+						const uint64_t testLimit = g_stage_wait_test_ns;
+						const bool ok = testLimit ? tc::BarWaitFor(&idle_bar[warp], 0, testLimit) : tc::BarWait(&staged_bar[warp], phase);
+						if (!ok)
 						{
 							// The copy did not complete in time: report it, wait (bounded) for the
 							// copy still in flight, and leave.
@@ -509,6 +520,12 @@ namespace tg
 			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, sms, stream, staged, status);
 			}
 		}
+	}
+
+	cudaError_t SetStageWaitTest(uint64_t limit_ns)
+	{
+		const unsigned long long v = limit_ns;
+		return cudaMemcpyToSymbol(g_stage_wait_test_ns, &v, sizeof(v));
 	}
 
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,

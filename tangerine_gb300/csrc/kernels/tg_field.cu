@@ -227,8 +227,14 @@ namespace tg
 			}
 		}
 
+		// Test hook of the network-image wait (SetSetupWaitTest): nonzero, every thread first
+		// waits this long on an mbarrier that nothing arrives at (bars[2]), so Setup fails as
+		// if the image copy had not completed.
+		__device__ unsigned long long g_setup_wait_test_ns = 0;
+
 		// Shared setup: tensor memory (warp 0), barriers (thread 0), the network image by one
-		// bulk copy.  Returns false if the copy's wait ran out.
+		// bulk copy.  Returns false if the copy's wait ran out; the copy has then landed (a
+		// second bounded wait) before the caller tears the CTA down.
 		__device__ __forceinline__ bool Setup(uint32_t* tmem_slot, uint64_t* bars, void* image_dst, const uint8_t* image,
 			uint32_t columns, Pipe& p)
 		{
@@ -237,6 +243,7 @@ namespace tg
 			{
 				tc::BarInit(&bars[0], 1);
 				tc::BarInit(&bars[1], 1);
+				tc::BarInit(&bars[2], 1);
 			}
 			tc::FenceBeforeSync();
 			__syncthreads();
@@ -245,7 +252,11 @@ namespace tg
 			p.Bar = &bars[1];
 			p.Phase = 0;
 			if (threadIdx.x == 0) tc::BulkLoad(image_dst, image, kImageBytes, &bars[0]);
-			return tc::BarWait(&bars[0], 0);
+			const uint64_t testLimit = g_setup_wait_test_ns;
+			const bool ok = testLimit ? tc::BarWaitFor(&bars[2], 0, testLimit) : tc::BarWait(&bars[0], 0);
+			if (ok) return true;
+			tc::BarWait(&bars[0], 0);
+			return false;
 		}
 
 		__device__ __forceinline__ void Teardown(const Pipe& p, uint32_t columns, bool failed, int* status)
@@ -267,7 +278,7 @@ namespace tg
 			uint8_t X[kRows * 32 * 2];          // inputs, 128 x 32
 			uint8_t H[kRows * 64 * 2];          // activations, 128 x 64 (H1, then H2)
 			uint8_t Image[kImageBytes];
-			uint64_t Bars[2];
+			uint64_t Bars[3];
 			uint32_t TmemSlot;
 		};
 		constexpr uint32_t kInferColumns = 64;
@@ -355,7 +366,7 @@ namespace tg
 			uint8_t X[kRows * kXCols * 2];
 			uint8_t Image[kImageBytes];
 			float Out[68];                      // sums of dW4 (64) and db4, then the squared error
-			uint64_t Bars[2];
+			uint64_t Bars[3];
 			uint32_t TmemSlot;
 			uint8_t Guard[8192];
 		};
@@ -1060,6 +1071,12 @@ namespace tg
 		UniformKernel<<<Blocks(n, 256), 256, 0, stream>>>(seed, make_float3(lo[0], lo[1], lo[2]),
 			make_float3(hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]), out, n, stride, offset);
 		return cudaGetLastError();
+	}
+
+	cudaError_t SetSetupWaitTest(uint64_t limit_ns)
+	{
+		const unsigned long long v = limit_ns;
+		return cudaMemcpyToSymbol(g_setup_wait_test_ns, &v, sizeof(v));
 	}
 
 	cudaError_t LaunchEvalFull(const DeviceProgram& prog, float4* samples, int64_t n, cudaStream_t stream)

@@ -120,6 +120,13 @@ namespace tg
 	// counts[0] = points checked, counts[1..9] = mismatches per check (tg_checks.cu).
 	cudaError_t LaunchPairCheck(uint64_t n, uint64_t seed, unsigned long long* counts, cudaStream_t stream);
 
+	// Test hooks of two bounded mbarrier waits (0 restores them): the staged-program copy of
+	// the brick evaluation (tg_cull.cu) and the network-image copy of the field kernels
+	// (tg_field.cu).  Nonzero, the wait is made on an mbarrier that nothing arrives at, with
+	// this limit, so it runs out and the kernel takes its failure path.
+	cudaError_t SetStageWaitTest(uint64_t limit_ns);
+	cudaError_t SetSetupWaitTest(uint64_t limit_ns);
+
 	// Achieved FP32 fused-multiply-add throughput of this GPU (TFLOP/s, 2 flops per FMA).
 	cudaError_t MeasureFp32Peak(double* tflops, cudaStream_t stream);
 

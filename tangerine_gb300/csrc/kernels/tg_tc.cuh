@@ -139,14 +139,20 @@ namespace tg
 			return ok != 0;
 		}
 
-		// Waits for the phase with this parity to complete; false after the time limit.
-		__device__ __forceinline__ bool BarWait(uint64_t* bar, uint32_t parity)
+		// Waits for the phase with this parity to complete; false after `limit_ns`.
+		__device__ __forceinline__ bool BarWaitFor(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
 		{
 			if (BarTryWait(bar, parity)) return true;
 			const uint64_t t0 = GlobalTimer();
 			while (!BarTryWait(bar, parity))
-				if (GlobalTimer() - t0 > kWaitLimitNs) return false;
+				if (GlobalTimer() - t0 > limit_ns) return false;
 			return true;
+		}
+
+		// BarWaitFor with the library's limit.
+		__device__ __forceinline__ bool BarWait(uint64_t* bar, uint32_t parity)
+		{
+			return BarWaitFor(bar, parity, kWaitLimitNs);
 		}
 
 		// Bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned) from global

@@ -213,3 +213,25 @@ def test_exports_of_a_tree_that_is_not_lipschitz(lib, port):
     assert gsize == size
     np.testing.assert_array_equal(m.cubes, cells.astype(np.uint32))
     np.testing.assert_array_equal(m.vertices, pts)
+
+
+def test_staged_copy_wait_runs_out_and_recovers(lib):
+    """The bounded wait for a brick's staged program copy (TG_MESH_STAGED), made to run out
+    on purpose with no GPU fault: with the test hook a staging warp waits 1 ms on an
+    mbarrier that nothing arrives at, records the failure, waits for its own copy and
+    leaves; the export fails with "did not complete in time".  With the hook off the staged
+    export equals the unstaged one bit for bit."""
+    spec = W.random_tree(3, 64)
+    grid = W.export_grid(resolution=96)
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        want = prog.export_mesh(grid)
+        try:
+            assert lib.tg_debug_wait_test(0, 1_000_000) == 0
+            with pytest.raises(_lib.TangerineError, match="did not complete in time"):
+                prog.export_mesh(grid, staged=True)
+        finally:
+            assert lib.tg_debug_wait_test(0, 0) == 0
+        got = prog.export_mesh(grid, staged=True)
+        np.testing.assert_array_equal(got.vertices, want.vertices)
+        np.testing.assert_array_equal(got.faces, want.faces)
+        np.testing.assert_array_equal(got.normals, want.normals)

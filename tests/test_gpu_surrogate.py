@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from oracle import surrogate as S
-from tangerine_gb300 import sdf
+from tangerine_gb300 import _lib, sdf
 from tangerine_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -203,3 +203,25 @@ def test_surrogate_export_1024_matches_dense_and_oracle(lib, port):
     finally:
         port.octree_free(o)
         port.free(h)
+
+
+def test_network_image_wait_runs_out_and_recovers(lib):
+    """The bounded mbarrier wait at the start of the network kernels, made to run out on
+    purpose with no GPU fault: with the test hook the wait is made on an mbarrier that
+    nothing arrives at (2 ms), every CTA records the failure, waits for its image copy,
+    frees its tensor memory and leaves; the call fails with "timed out".  With the hook off
+    the same call gives the same values as before."""
+    rng = np.random.default_rng(5)
+    s, _, _, _ = _net(rng)
+    pts = rng.uniform(-2.0, 2.0, (1000, 3)).astype(np.float32)
+    want = s.eval(pts)
+    try:
+        assert lib.tg_debug_wait_test(1, 2_000_000) == 0
+        with pytest.raises(_lib.TangerineError, match="timed out"):
+            s.eval(pts)
+    finally:
+        assert lib.tg_debug_wait_test(1, 0) == 0
+    np.testing.assert_array_equal(s.eval(pts), want)
+    assert lib.tg_debug_wait_test(1, 2_000_000_000) != 0      # above 1 s: refused
+    assert lib.tg_debug_wait_test(2, 0) != 0                  # no such wait
+    s.close()
