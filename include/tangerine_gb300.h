@@ -551,7 +551,7 @@ typedef struct tg_surrogate_options
 	int64_t samples;            /* training samples, half uniform, half |d| < band (2^22) */
 	float band;                 /* (0.05) */
 	int64_t batch;              /* samples per Adam step (2^18) */
-	int steps;                  /* Adam steps (2000) */
+	int steps;                  /* Adam steps (1000) */
 	float learning_rate;        /* (1e-2, decaying to 1e-3 over the second half) */
 	int64_t validation;         /* held-out samples, same mix (2^20) */
 	float safety;               /* margin = safety x max held-out error (2) */

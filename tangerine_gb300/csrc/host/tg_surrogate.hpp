@@ -24,7 +24,7 @@ namespace tg
 		int64_t Samples = int64_t(1) << 22;     // training set: half uniform, half |d| < Band
 		float Band = 0.05f;
 		int64_t Batch = int64_t(1) << 18;
-		int Steps = 2000;
+		int Steps = 1000;
 		float Rate = 1e-2f;             // Adam step; decays to 1/10 over the last half
 		float Beta1 = 0.9f, Beta2 = 0.99f, Epsilon = 1e-15f;
 		int64_t Validation = int64_t(1) << 20;  // held-out samples, same mix
