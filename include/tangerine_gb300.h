@@ -584,6 +584,15 @@ TANGERINE_API tg_status tg_surrogate_get_info(const tg_surrogate* s, tg_surrogat
 /* Parameters as FP32 host arrays (table: level-major, entry-major, 2 features). */
 TANGERINE_API tg_status tg_surrogate_get_params(tg_surrogate* s, float* table, float* mlp);
 TANGERINE_API tg_status tg_surrogate_set_params(tg_surrogate* s, const float* table, const float* mlp);
+/* Checkpoint and resume: the parameters with both Adam moments and the step count, the
+ * info and the held-out error record behind the margins.  tg_surrogate_save with out ==
+ * NULL returns the checkpoint's size in bytes; with a buffer of at least that capacity it
+ * writes the checkpoint and returns its size; -1 on error.  tg_surrogate_load restores one
+ * into a surrogate created with the same grid options (table size, resolutions, domain,
+ * clamp; TG_ERR_INVALID otherwise or for a damaged checkpoint): tg_surrogate_train then
+ * continues the same Adam schedule, and the margins are the saved ones. */
+TANGERINE_API int64_t tg_surrogate_save(tg_surrogate* s, void* out, int64_t capacity);
+TANGERINE_API tg_status tg_surrogate_load(tg_surrogate* s, const void* data, int64_t size);
 /* Network output at n points (3 floats each); host arrays, or device when io_is_device. */
 TANGERINE_API tg_status tg_surrogate_eval(tg_surrogate* s, const float* points, int64_t n, float* out, int io_is_device,
                                           void* stream);

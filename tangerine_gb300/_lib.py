@@ -179,6 +179,8 @@ SIGNATURES = {
     "tg_batch_cancel": (_i, [_vp, _i]),
     "tg_batch_debug_barrier": (_i, [_vp, C.c_uint64, _i, C.c_uint64]),
     "tg_debug_wait_test": (_i, [_i, C.c_uint64]),
+    "tg_surrogate_save": (_i64, [_vp, _vp, _i64]),
+    "tg_surrogate_load": (_i, [_vp, _vp, _i64]),
     "tg_batch_reserve": (_i, [_vp, C.c_uint64, C.c_uint64]),
     "tg_batch_get_info": (_i, [_vp, C.POINTER(BatchInfo)]),
     "tg_batch_mesh": (_i, [_vp, _i, C.POINTER(HostMesh), _vp]),

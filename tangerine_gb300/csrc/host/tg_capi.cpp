@@ -1635,6 +1635,33 @@ extern "C"
 		return e == cudaSuccess ? TG_OK : CudaFail(e, "writing surrogate parameters");
 	}
 
+	TANGERINE_API int64_t tg_surrogate_save(tg_surrogate* s, void* out, int64_t capacity)
+	{
+		if (!s || capacity < 0) { SetError("null argument"); return -1; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		std::vector<uint8_t> bytes;
+		const cudaError_t e = s->Save(bytes, eng.DefaultStream());
+		if (e != cudaSuccess) { CudaFail(e, "saving the surrogate"); return -1; }
+		if (out)
+		{
+			if (capacity < (int64_t)bytes.size()) { SetError("checkpoint buffer too small"); return -1; }
+			std::memcpy(out, bytes.data(), bytes.size());
+		}
+		return (int64_t)bytes.size();
+	}
+
+	TANGERINE_API tg_status tg_surrogate_load(tg_surrogate* s, const void* data, int64_t size)
+	{
+		if (!s || !data || size <= 0) { SetError("null argument"); return TG_ERR_INVALID; }
+		Engine& eng = Engine::Get();
+		std::lock_guard<std::mutex> lock(eng.Mutex);
+		std::string why;
+		const cudaError_t e = s->Load(static_cast<const uint8_t*>(data), (size_t)size, why, eng.DefaultStream());
+		if (e == cudaErrorInvalidValue && !why.empty()) { SetError(why); return TG_ERR_INVALID; }
+		return e == cudaSuccess ? TG_OK : CudaFail(e, "loading the surrogate");
+	}
+
 	TANGERINE_API tg_status tg_surrogate_eval(tg_surrogate* s, const float* points, int64_t n, float* out, int io_is_device, void* stream)
 	{
 		if (!s || (n > 0 && (!points || !out)) || n < 0) { SetError("null argument"); return TG_ERR_INVALID; }

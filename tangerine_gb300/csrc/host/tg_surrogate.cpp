@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #define TG_TRY(expr) do { cudaError_t _e = (expr); if (_e != cudaSuccess) return _e; } while (0)
@@ -113,6 +114,126 @@ namespace tg
 	{
 		if (host_table) TG_TRY(cudaMemcpyAsync(host_table, Table.Ptr, (size_t)TableFloats * sizeof(float), cudaMemcpyDeviceToHost, s));
 		if (host_mlp) TG_TRY(cudaMemcpyAsync(host_mlp, Mlp.Ptr, (size_t)kFieldParams * sizeof(float), cudaMemcpyDeviceToHost, s));
+		return cudaStreamSynchronize(s);
+	}
+
+	// Checkpoint bytes, little-endian, in this order: the magic "TGFIELD1"; int32 Log2Table,
+	// BaseRes, MaxRes; float Lo[3], Hi[3], Clamp; int64 table floats; int32 network floats;
+	// int32 steps taken; the info (float MaxError, P99Error, MeanError, Margin, FinalLoss,
+	// MarginOverride; double DataSeconds, TrainSeconds; int64 Samples; int32 Steps); int64
+	// held-out count; then float arrays: table, its first and second moments, network, its
+	// two moments, the held-out |clamp(d)| and prefix maxima.
+	namespace
+	{
+		constexpr char kCheckpointMagic[8] = { 'T', 'G', 'F', 'I', 'E', 'L', 'D', '1' };
+
+		struct Writer
+		{
+			std::vector<uint8_t>& Out;
+			template<typename T> void Put(const T& v)
+			{
+				const uint8_t* b = reinterpret_cast<const uint8_t*>(&v);
+				Out.insert(Out.end(), b, b + sizeof(T));
+			}
+		};
+
+		struct Reader
+		{
+			const uint8_t* At;
+			const uint8_t* End;
+			template<typename T> bool Get(T& v)
+			{
+				if ((size_t)(End - At) < sizeof(T)) return false;
+				std::memcpy(&v, At, sizeof(T));
+				At += sizeof(T);
+				return true;
+			}
+		};
+	}
+
+	cudaError_t FieldNet::Save(std::vector<uint8_t>& out, cudaStream_t s)
+	{
+		out.clear();
+		Writer w{ out };
+		for (char c : kCheckpointMagic) w.Put(c);
+		w.Put((int32_t)Opt.Log2Table); w.Put((int32_t)Opt.BaseRes); w.Put((int32_t)Opt.MaxRes);
+		for (int i = 0; i < 3; ++i) w.Put(Opt.Lo[i]);
+		for (int i = 0; i < 3; ++i) w.Put(Opt.Hi[i]);
+		w.Put(Opt.Clamp);
+		w.Put((int64_t)TableFloats); w.Put((int32_t)kFieldParams);
+		w.Put((int32_t)Steps);
+		w.Put(Info.MaxError); w.Put(Info.P99Error); w.Put(Info.MeanError); w.Put(Info.Margin); w.Put(Info.FinalLoss);
+		w.Put(Info.MarginOverride); w.Put(Info.DataSeconds); w.Put(Info.TrainSeconds); w.Put((int64_t)Info.Samples);
+		w.Put((int32_t)Info.Steps);
+		const int64_t held = (int64_t)HeldAbsTarget.size();
+		w.Put(held);
+		const size_t head = out.size();
+		const size_t tb = (size_t)TableFloats * 4, mb = (size_t)kFieldParams * 4, hb = (size_t)held * 4;
+		out.resize(head + 3 * tb + 3 * mb + 2 * hb);
+		uint8_t* p = out.data() + head;
+		const DeviceBuffer* tables[3] = { &Table, &TableM, &TableV };
+		for (const DeviceBuffer* b : tables) { TG_TRY(cudaMemcpyAsync(p, b->Ptr, tb, cudaMemcpyDeviceToHost, s)); p += tb; }
+		const DeviceBuffer* nets[3] = { &Mlp, &MlpM, &MlpV };
+		for (const DeviceBuffer* b : nets) { TG_TRY(cudaMemcpyAsync(p, b->Ptr, mb, cudaMemcpyDeviceToHost, s)); p += mb; }
+		if (held)
+		{
+			std::memcpy(p, HeldAbsTarget.data(), hb);
+			std::memcpy(p + hb, HeldPrefixMax.data(), hb);
+		}
+		return cudaStreamSynchronize(s);
+	}
+
+	cudaError_t FieldNet::Load(const uint8_t* data, size_t size, std::string& error, cudaStream_t s)
+	{
+		Reader r{ data, data + size };
+		char magic[8];
+		for (char& c : magic)
+			if (!r.Get(c)) { error = "checkpoint too short"; return cudaErrorInvalidValue; }
+		if (std::memcmp(magic, kCheckpointMagic, 8) != 0) { error = "not a surrogate checkpoint"; return cudaErrorInvalidValue; }
+		int32_t log2Table = 0, baseRes = 0, maxRes = 0, mlpFloats = 0, steps = 0, infoSteps = 0;
+		float lo[3], hi[3], clamp = 0.0f;
+		int64_t tableFloats = 0, samples = 0, held = 0;
+		FieldInfo info;
+		bool ok = r.Get(log2Table) && r.Get(baseRes) && r.Get(maxRes);
+		for (int i = 0; i < 3; ++i) ok = ok && r.Get(lo[i]);
+		for (int i = 0; i < 3; ++i) ok = ok && r.Get(hi[i]);
+		ok = ok && r.Get(clamp) && r.Get(tableFloats) && r.Get(mlpFloats) && r.Get(steps);
+		ok = ok && r.Get(info.MaxError) && r.Get(info.P99Error) && r.Get(info.MeanError) && r.Get(info.Margin) && r.Get(info.FinalLoss)
+			&& r.Get(info.MarginOverride) && r.Get(info.DataSeconds) && r.Get(info.TrainSeconds) && r.Get(samples) && r.Get(infoSteps)
+			&& r.Get(held);
+		if (!ok) { error = "checkpoint too short"; return cudaErrorInvalidValue; }
+		bool same = log2Table == Opt.Log2Table && baseRes == Opt.BaseRes && maxRes == Opt.MaxRes && clamp == Opt.Clamp;
+		for (int i = 0; i < 3; ++i) same = same && lo[i] == Opt.Lo[i] && hi[i] == Opt.Hi[i];
+		if (!same || tableFloats != TableFloats || mlpFloats != kFieldParams)
+		{
+			error = "checkpoint of a surrogate with other grid options";
+			return cudaErrorInvalidValue;
+		}
+		const size_t tb = (size_t)TableFloats * 4, mb = (size_t)kFieldParams * 4;
+		if (held < 0 || steps < 0 || (size_t)(r.End - r.At) != 3 * tb + 3 * mb + 2 * (size_t)held * 4)
+		{
+			error = "checkpoint size does not match its header";
+			return cudaErrorInvalidValue;
+		}
+		const uint8_t* p = r.At;
+		DeviceBuffer* tables[3] = { &Table, &TableM, &TableV };
+		for (DeviceBuffer* b : tables) { TG_TRY(cudaMemcpyAsync(b->Ptr, p, tb, cudaMemcpyHostToDevice, s)); p += tb; }
+		DeviceBuffer* nets[3] = { &Mlp, &MlpM, &MlpV };
+		for (DeviceBuffer* b : nets) { TG_TRY(cudaMemcpyAsync(b->Ptr, p, mb, cudaMemcpyHostToDevice, s)); p += mb; }
+		TG_TRY(cudaMemsetAsync(TableGrad.Ptr, 0, tb, s));
+		TG_TRY(cudaMemsetAsync(MlpGrad.Ptr, 0, mb, s));
+		TG_TRY(LaunchFieldPack(Mlp.As<float>(), Image.As<uint8_t>(), s));
+		HeldAbsTarget.resize((size_t)held);
+		HeldPrefixMax.resize((size_t)held);
+		if (held)
+		{
+			std::memcpy(HeldAbsTarget.data(), p, (size_t)held * 4);
+			std::memcpy(HeldPrefixMax.data(), p + (size_t)held * 4, (size_t)held * 4);
+		}
+		Steps = steps;
+		info.Samples = samples;
+		info.Steps = infoSteps;
+		Info = info;
 		return cudaStreamSynchronize(s);
 	}
 

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -56,6 +57,11 @@ namespace tg
 		cudaError_t Init(cudaStream_t s);
 		cudaError_t SetParams(const float* host_table, const float* host_mlp, cudaStream_t s);
 		cudaError_t GetParams(float* host_table, float* host_mlp, cudaStream_t s);
+		// Checkpoint: the grid options, the step count, the info and held-out error record,
+		// the parameters and both Adam moments (byte layout in tg_surrogate.cpp).  Load
+		// requires the same grid options; training then resumes where it stopped.
+		cudaError_t Save(std::vector<uint8_t>& out, cudaStream_t s);
+		cudaError_t Load(const uint8_t* data, size_t size, std::string& error, cudaStream_t s);
 		// Gradients of the mean squared error over n device samples (x, y, z, d), to host.
 		cudaError_t Gradients(const float4* samples, int64_t n, float* host_table_grad, float* host_mlp_grad, float* host_loss,
 			cudaStream_t s);

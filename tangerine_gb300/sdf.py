@@ -598,6 +598,20 @@ class Surrogate:
         check(load().tg_surrogate_set_params(self.ptr, None if t is None else _lib.as_ptr(t),
                                              None if m is None else _lib.as_ptr(m)), "tg_surrogate_set_params")
 
+    def save(self) -> bytes:
+        """Checkpoint: parameters, Adam moments, step count, info and held-out record."""
+        n = load().tg_surrogate_save(self.ptr, None, 0)
+        if n < 0:
+            raise _lib.TangerineError(load().tg_last_error().decode())
+        buf = C.create_string_buffer(int(n))
+        if load().tg_surrogate_save(self.ptr, buf, n) != n:
+            raise _lib.TangerineError(load().tg_last_error().decode())
+        return buf.raw
+
+    def restore(self, data: bytes):
+        """Restores a checkpoint (save()) of a surrogate with the same grid options."""
+        check(load().tg_surrogate_load(self.ptr, data, len(data)), "tg_surrogate_load")
+
     def eval(self, points, stream=None) -> np.ndarray:
         p = np.ascontiguousarray(np.asarray(points, np.float32).reshape(-1, 3))
         out = np.empty(p.shape[0], np.float32)

@@ -225,3 +225,47 @@ def test_network_image_wait_runs_out_and_recovers(lib):
     assert lib.tg_debug_wait_test(1, 2_000_000_000) != 0      # above 1 s: refused
     assert lib.tg_debug_wait_test(2, 0) != 0                  # no such wait
     s.close()
+
+
+def test_checkpoint_resumes_training(lib):
+    """A checkpoint holds the parameters, both Adam moments and the step count: a fresh
+    surrogate restored from it holds the saved parameters bit for bit, and training both
+    on from there gives the same parameters (up to the order of the float atomics in the
+    gradient sums) -- with the step count lost, Adam's bias correction would differ at
+    once.  Checkpoints of other grid options and damaged ones are refused."""
+    rng = np.random.default_rng(6)
+    s, _, _, _ = _net(rng, batch=1 << 12, learning_rate=1e-2)
+    n = 4096
+    smp = np.concatenate([rng.uniform(-2, 2, (n, 3)), rng.uniform(-0.5, 0.5, (n, 1))], 1).astype(np.float32)
+    s.train(smp, 3)
+    ck = s.save()
+    t0, m0 = s.params()
+    s.train(smp, 2)
+    t1, m1 = s.params()
+    r = sdf.Surrogate(log2_table=14, batch=1 << 12, learning_rate=1e-2)
+    r.restore(ck)
+    rt, rm = r.params()
+    np.testing.assert_array_equal(rt, t0)
+    np.testing.assert_array_equal(rm, m0)
+    assert r.save() == ck
+    r.train(smp, 2)
+    t2, m2 = r.params()
+    # Entries whose gradient sums to about zero take a full Adam step of either sign
+    # (m / sqrt(v) with epsilon 1e-15), so a different summation order can move a few of
+    # them by up to 2 x the rate: compare the fraction that moved, as the Adam test does.
+    assert np.mean(np.abs(t2 - t1) > 1e-5) < 1e-3
+    assert np.mean(np.abs(m2 - m1) > 1e-5) < 1e-3
+    s2 = sdf.Surrogate(log2_table=14, batch=1 << 12, learning_rate=1e-2)
+    s2.set_params(t0, m0)                      # parameters alone: moments and step count lost
+    s2.train(smp, 2)
+    t3, _ = s2.params()
+    assert np.mean(np.abs(t3 - t1) > 1e-5) > 0.01
+    other = sdf.Surrogate(log2_table=13)
+    with pytest.raises(_lib.TangerineError, match="other grid options"):
+        other.restore(ck)
+    with pytest.raises(_lib.TangerineError, match="size"):
+        r.restore(ck[:-4])
+    with pytest.raises(_lib.TangerineError, match="not a surrogate checkpoint"):
+        r.restore(b"x" * len(ck))
+    for x in (s, r, s2, other):
+        x.close()
