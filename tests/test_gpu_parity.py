@@ -338,3 +338,22 @@ def test_lua_model_export_matches_oracle(lib, port, name):
     finally:
         port.octree_free(o)
         port.free(h)
+
+
+@pytest.mark.parametrize("lanes,staged", [(1, False), (2, False), (4, False), (2, True), (4, True)])
+def test_culled_export_on_ragged_grids(lib, lanes, staged):
+    """Lattices whose sides are not multiples of the brick edge and differ per axis, with
+    per-axis steps: every brick size, lane count and staging gives the dense export's mesh
+    bit for bit (the last bricks of each axis are cut by the lattice end)."""
+    spec = W.random_tree(9, 64, ops=W.OPS_60_20_10_10)
+    grids = [_lib.Grid(-1.9, -1.7, -2.0, 0.061, 53, 37, 61),
+             _lib.Grid(-2.0, -1.5, -1.2, 0.05, 71, 44, 30, 0.07, 0.09)]
+    with sdf.compile(sdf.from_spec(spec)) as prog:
+        for grid in grids:
+            dense = prog.export_mesh(grid, dense=True)
+            assert dense.vertices.shape[0] > 0
+            for brick in (3, 7, 10, 32):
+                culled = prog.export_mesh(grid, brick=brick, lanes=lanes, staged=staged)
+                for a, b in ((dense.vertices, culled.vertices), (dense.faces, culled.faces),
+                             (dense.normals, culled.normals), (dense.colors, culled.colors), (dense.cubes, culled.cubes)):
+                    np.testing.assert_array_equal(a, b)
