@@ -311,6 +311,10 @@ namespace tg
 			const int64_t brickWords = (nb + 31) / 32;
 			TG_TRY(BrickBits.Reserve((size_t)brickWords * 4 * (opt.Field && opt.Refine ? 2 : 1)));
 			TG_TRY(BrickList.Reserve((size_t)nb * 4));
+			TG_TRY(BrickTops.Reserve((size_t)nb * 4));
+			// The exact classifier stores each kept brick's descent for the evaluation; the
+			// network alone leaves the evaluation to descend.
+			const uint32_t* tops = (!opt.Field || opt.Refine) ? BrickTops.As<uint32_t>() : nullptr;
 			if (!SmCount)
 			{
 				int dev = 0;
@@ -333,7 +337,7 @@ namespace tg
 					// spatial tiles; survivors go to the second half of the bit buffer.
 					uint32_t* kept = bits + brickWords;
 					Begin("refine_bricks", s);
-					TG_TRY(LaunchClassifyBricks(p.View, g, B, kept, s, bits));
+					TG_TRY(LaunchClassifyBricks(p.View, g, B, kept, s, bits, BrickTops.As<uint32_t>()));
 					End(s);
 					bits = kept;
 				}
@@ -341,7 +345,7 @@ namespace tg
 			else
 			{
 				Begin("classify_bricks", s);
-				TG_TRY(LaunchClassifyBricks(p.View, g, B, bits, s));
+				TG_TRY(LaunchClassifyBricks(p.View, g, B, bits, s, nullptr, BrickTops.As<uint32_t>()));
 				End(s);
 			}
 			Begin("list_bricks", s);
@@ -351,7 +355,7 @@ namespace tg
 			Begin("eval_bricks", s);
 			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);      // status and work counter
 			TG_TRY(cudaMemsetAsync(evalStatus, 0, 2 * sizeof(int), s));
-			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, LatticeBuf.As<float>(), SmCount, s,
+			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, tops, LatticeBuf.As<float>(), SmCount, s,
 				opt.Lanes, opt.Staged, evalStatus));
 			End(s);
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.

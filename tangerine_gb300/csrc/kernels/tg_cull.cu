@@ -48,8 +48,20 @@ namespace tg
 		// Kept bricks set their bit with atomicOr into the zeroed bit words.
 		constexpr int kTileX = 8, kTileY = 4, kTileZ = kClassifyThreads / (kTileX * kTileY);
 
+		// A kept brick's descent for the evaluation (DescendBox over its corner box): the cell
+		// reached in the low 31 bits, bit 31 set when every point of the box descends to it.
+		__device__ __forceinline__ uint32_t BrickTop(const DeviceProgram& prog, const GridSpec& g, int i0, int i1, int j0, int j1, int k0,
+			int k1)
+		{
+			bool shared;
+			const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.DX), LatticeCoord(g.X0, i1, g.DX),
+				LatticeCoord(g.Y0, j0, g.DY), LatticeCoord(g.Y0, j1, g.DY), LatticeCoord(g.Z0, k0, g.DZ),
+				LatticeCoord(g.Z0, k1, g.DZ), shared);
+			return (uint32_t)top | (shared ? 0x80000000u : 0u);
+		}
+
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ candidates, uint32_t* __restrict__ brick_bits)
+			const uint32_t* __restrict__ candidates, uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ brick_tops)
 		{
 			extern __shared__ float spill[];
 			const int tilesX = (bg.NBX + kTileX - 1) / kTileX, tilesY = (bg.NBY + kTileY - 1) / kTileY;
@@ -62,10 +74,11 @@ namespace tg
 			if (candidates && !((__ldg(candidates + (b >> 5)) >> (b & 31)) & 1u)) return;
 			const int sx = g.NX - 1, sy = g.NY - 1, sz = g.NZ - 1;
 			const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
-			if (BoxMayHoldSurface(prog, g, i0, min(i0 + bg.B, sx), j0, min(j0 + bg.B, sy), k0, min(k0 + bg.B, sz), spill + threadIdx.x,
-				kClassifyThreads))
+			const int i1 = min(i0 + bg.B, sx), j1 = min(j0 + bg.B, sy), k1 = min(k0 + bg.B, sz);
+			if (BoxMayHoldSurface(prog, g, i0, i1, j0, j1, k0, k1, spill + threadIdx.x, kClassifyThreads))
 			{
 				atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
+				if (brick_tops) brick_tops[b] = BrickTop(prog, g, i0, i1, j0, j1, k0, k1);
 			}
 		}
 
@@ -111,8 +124,8 @@ namespace tg
 		// generic-address load, so the interpreter is compiled once.
 		template<int C, int K, bool Stage>
 		__global__ void __launch_bounds__(kBrickThreads, EvalBricksCtasPerSm<C>()) EvalBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
-			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, float* __restrict__ lattice, int spill_floats,
-			int stage_quads, int* __restrict__ status, uint32_t* __restrict__ next)
+			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, const uint32_t* __restrict__ tops,
+			float* __restrict__ lattice, int spill_floats, int stage_quads, int* __restrict__ status, uint32_t* __restrict__ next)
 		{
 			extern __shared__ __align__(16) float spill[];
 			__shared__ uint64_t staged_bar[kBrickWarps], idle_bar[kBrickWarps];
@@ -141,13 +154,12 @@ namespace tg
 				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
 				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
 				const int i1 = min(i0 + bg.B, g.NX - 1), j1 = min(j0 + bg.B, g.NY - 1), k1 = min(k0 + bg.B, g.NZ - 1);
-				// The brick's points mostly share one octree cell: descend once with the
-				// brick's box (lattice coordinates are monotone in the index), then per point
-				// only below where the box straddles a pivot.
-				bool shared;
-				const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.DX), LatticeCoord(g.X0, i1, g.DX),
-					LatticeCoord(g.Y0, j0, g.DY), LatticeCoord(g.Y0, j1, g.DY), LatticeCoord(g.Z0, k0, g.DZ),
-					LatticeCoord(g.Z0, k1, g.DZ), shared);
+				// The brick's points mostly share one octree cell: the descent with the brick's
+				// box (lattice coordinates are monotone in the index; the classifier's, when it
+				// stored one), then per point only below where the box straddles a pivot.
+				const uint32_t packed = tops ? __ldg(tops + b) : BrickTop(prog, g, i0, i1, j0, j1, k0, k1);
+				const int top = (int)(packed & 0x7FFFFFFFu);
+				const bool shared = (packed >> 31) != 0u;
 				// Record reads go through `code` (generic address): the staged copy, offset so that
 				// the program's own record numbers index it, or the program's global records.
 				const float4* code = prog.Code;
@@ -450,7 +462,7 @@ namespace tg
 	}
 
 	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream,
-		const uint32_t* candidates)
+		const uint32_t* candidates, uint32_t* brick_tops)
 	{
 		const BrickGrid bg = MakeBrickGrid(g, B);
 		const int64_t nb = (int64_t)bg.NBX * bg.NBY * bg.NBZ;
@@ -461,7 +473,7 @@ namespace tg
 		cudaError_t e = cudaMemsetAsync(brick_bits, 0, (size_t)((nb + 31) / 32) * 4, stream);
 		if (e != cudaSuccess) return e;
 		const int64_t tiles = (int64_t)((bg.NBX + kTileX - 1) / kTileX) * ((bg.NBY + kTileY - 1) / kTileY) * ((bg.NBZ + kTileZ - 1) / kTileZ);
-		ClassifyBricksKernel<<<(unsigned)tiles, kClassifyThreads, smem, stream>>>(prog, g, bg, candidates, brick_bits);
+		ClassifyBricksKernel<<<(unsigned)tiles, kClassifyThreads, smem, stream>>>(prog, g, bg, candidates, brick_bits, brick_tops);
 		return cudaGetLastError();
 	}
 
@@ -484,7 +496,7 @@ namespace tg
 
 		template<int C, int K, bool Stage>
 		cudaError_t LaunchEvalBricksCKS(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int sms, cudaStream_t stream, int* status)
+			const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, int* status)
 		{
 			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
 			const size_t spill = (size_t)depth * K * kBrickThreads * sizeof(float);
@@ -497,27 +509,27 @@ namespace tg
 				if (e != cudaSuccess) return e;
 			}
 			EvalBricksKernel<C, K, Stage><<<sms * EvalBricksCtasPerSm<C>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, B), list,
-				count, lattice, (int)(spill / sizeof(float)), stageQuads, status, reinterpret_cast<uint32_t*>(status) + 1);
+				count, tops, lattice, (int)(spill / sizeof(float)), stageQuads, status, reinterpret_cast<uint32_t*>(status) + 1);
 			return cudaGetLastError();
 		}
 
 		template<int C, int K>
 		cudaError_t LaunchEvalBricksCK(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int sms, cudaStream_t stream, bool staged, int* status)
+			const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, bool staged, int* status)
 		{
-			if (staged) return LaunchEvalBricksCKS<C, K, true>(prog, g, B, list, count, lattice, sms, stream, status);
-			return LaunchEvalBricksCKS<C, K, false>(prog, g, B, list, count, lattice, sms, stream, status);
+			if (staged) return LaunchEvalBricksCKS<C, K, true>(prog, g, B, list, count, tops, lattice, sms, stream, status);
+			return LaunchEvalBricksCKS<C, K, false>(prog, g, B, list, count, tops, lattice, sms, stream, status);
 		}
 
 		template<int C>
 		cudaError_t LaunchEvalBricksC(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-			float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
+			const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
 		{
 			switch (lanes)
 			{
-			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, lattice, sms, stream, staged, status);
-			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, lattice, sms, stream, staged, status);
-			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, lattice, sms, stream, staged, status);
+			case 1: return LaunchEvalBricksCK<C, 1>(prog, g, B, list, count, tops, lattice, sms, stream, staged, status);
+			case 2: return LaunchEvalBricksCK<C, 2>(prog, g, B, list, count, tops, lattice, sms, stream, staged, status);
+			default: return LaunchEvalBricksCK<C, 4>(prog, g, B, list, count, tops, lattice, sms, stream, staged, status);
 			}
 		}
 	}
@@ -529,12 +541,12 @@ namespace tg
 	}
 
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
+		const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status)
 	{
-		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
-		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
-		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
-		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 8) return LaunchEvalBricksC<8>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 16) return LaunchEvalBricksC<16>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
+		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
 		return cudaErrorInvalidValue;
 	}
 

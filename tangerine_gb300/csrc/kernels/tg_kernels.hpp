@@ -69,8 +69,10 @@ namespace tg
 	int64_t BrickCount(const GridSpec& g, int B);
 	// With `candidates` (bits of another classification, e.g. the learned bound's), only
 	// bricks set there are tested; the rest stay clear.
+	// brick_tops (optional, one word per brick): each kept brick's octree descent for the
+	// evaluation (cell | shared << 31), which LaunchEvalBricks then reads instead of descending.
 	cudaError_t LaunchClassifyBricks(const DeviceProgram& prog, const GridSpec& g, int B, uint32_t* brick_bits, cudaStream_t stream,
-		const uint32_t* candidates = nullptr);
+		const uint32_t* candidates = nullptr, uint32_t* brick_tops = nullptr);
 	// Set bits as a list in brick-index order (scan + compaction); *count (device) gets the
 	// length.  base: (bricks + 31) / 32 words; scratch: ScanScratchWords of that.
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
@@ -80,8 +82,9 @@ namespace tg
 	// staged program copy does not complete in time; status[1] is the warps' work counter.
 	// staged: bricks inside one octree cell read their program from a shared-memory copy made
 	// by one bulk copy.
+	// tops: the classifier's brick_tops for every listed brick, or nullptr (the kernel descends).
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
-		float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status);
+		const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
 		cudaStream_t stream);
 	// Cell pass over the cells of listed bricks only: clears and fills the bitmask and
