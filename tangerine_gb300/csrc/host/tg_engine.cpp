@@ -352,18 +352,30 @@ namespace tg
 			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
 			End(s);
 			LastBrickSize = B;
-			Begin("eval_bricks", s);
-			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);      // status and work counter
-			TG_TRY(cudaMemsetAsync(evalStatus, 0, 2 * sizeof(int), s));
-			TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, tops, LatticeBuf.As<float>(), SmCount, s,
-				opt.Lanes, opt.Staged, evalStatus));
-			End(s);
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.
 			TG_TRY(ActiveCells.Reserve((size_t)(nb * (int64_t)B * B * B < cells ? nb * (int64_t)B * B * B : cells) * 4));
-			Begin("cell_flags", s);
-			TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
-				ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, SmCount, s));
-			End(s);
+			int* evalStatus = reinterpret_cast<int*>(Counts.As<uint32_t>() + 4);      // status and work counter
+			TG_TRY(cudaMemsetAsync(evalStatus, 0, 2 * sizeof(int), s));
+			if (B == 7 && !opt.Staged)
+			{
+				// The cell pass runs inside the brick evaluation, on each brick's values in
+				// shared memory.
+				Begin("eval_bricks", s);
+				TG_TRY(LaunchEvalBricksCells(p.View, g, BrickList.As<uint32_t>(), brickCount, tops, LatticeBuf.As<float>(),
+					Words.As<uint32_t>(), ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, SmCount, s, opt.Lanes, evalStatus));
+				End(s);
+			}
+			else
+			{
+				Begin("eval_bricks", s);
+				TG_TRY(LaunchEvalBricks(p.View, g, B, BrickList.As<uint32_t>(), brickCount, tops, LatticeBuf.As<float>(), SmCount, s,
+					opt.Lanes, opt.Staged, evalStatus));
+				End(s);
+				Begin("cell_flags", s);
+				TG_TRY(LaunchCellFlagsListed(LatticeBuf.As<float>(), g, B, BrickList.As<uint32_t>(), brickCount, Words.As<uint32_t>(),
+					ActiveCells.As<uint32_t>(), Counts.As<uint32_t>() + 3, SmCount, s));
+				End(s);
+			}
 			TG_TRY(cudaMemcpyAsync(HostCounts + 2, brickCount, 12, cudaMemcpyDeviceToHost, s));
 			Bricks = nb;
 		}

@@ -107,6 +107,91 @@ namespace tg
 		// copy that never completes would.
 		__device__ unsigned long long g_stage_wait_test_ns = 0;
 
+		// One slice of a brick (see EvalBricksKernel): lane `lane` runs its column's K
+		// z-consecutive points of every 8 x 8 x 2K block of the brick's box, through one pass
+		// over their octree cell's records per distinct cell.  `code`: the records (read with
+		// __ldg, or with generic loads when Generic: a staged copy).  Box: the values also go
+		// to `box`, the brick's C^3 corner box in shared memory (x fastest), for the cell pass
+		// folded into EvalBricksCellsKernel.
+		template<int C, int K, bool Generic, bool Box>
+		__device__ __forceinline__ void EvalSlice(const DeviceProgram& prog, const GridSpec& g, int i0, int i1, int j0, int j1, int k0,
+			int k1, int top, bool shared, int slice, int lane, const float4* code, float* __restrict__ lattice, float* spill, float* box)
+		{
+			constexpr int ZSpan = 2 * K;
+			const int tx = lane & 7, ty = (lane >> 3) + 4 * (slice & 1), tz = slice >> 1;
+			for (int oz = 0; oz < C; oz += ZSpan)
+			for (int oy = 0; oy < C; oy += 8)
+			for (int ox = 0; ox < C; ox += 8)
+			{
+				const int ix = i0 + ox + tx, iy = j0 + oy + ty, izb = k0 + oz + tz * K;
+				const bool inPlane = ix <= i1 && iy <= j1;
+				const float x = LatticeCoord(g.X0, min(ix, i1), g.DX);
+				const float y = LatticeCoord(g.Y0, min(iy, j1), g.DY);
+				float px[K], py[K], pz[K], res[K];
+				int cell[K];
+				unsigned todo = 0;
+#pragma unroll
+				for (int k = 0; k < K; ++k)
+				{
+					const int iz = izb + k;
+					px[k] = x;
+					py[k] = y;
+					pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.DZ);
+					cell[k] = shared ? top : DescendOctreeFrom(prog.Nodes, top, px[k], py[k], pz[k]);
+					res[k] = 0.0f;
+					if (inPlane && iz <= k1) todo |= 1u << k;
+				}
+				while (todo)
+				{
+					int c = -1;
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+						if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
+					float r[K];
+					if constexpr (K % 2 == 0)
+					{
+						// Points in pairs through the paired FP32 instructions (tg_pair.cuh).
+						if (Generic)
+						{
+							RunDistancePaired<K>([&](int q) { return code[q]; }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
+								spill + 2 * threadIdx.x, kBrickThreads);
+						}
+						else
+						{
+							RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px,
+								py, pz, r, spill + 2 * threadIdx.x, kBrickThreads);
+						}
+					}
+					else
+					{
+						RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kBrickThreads);
+					}
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+					{
+						if (((todo >> k) & 1u) && cell[k] == c)
+						{
+							res[k] = r[k];
+							todo &= ~(1u << k);
+						}
+					}
+				}
+				if (inPlane)
+				{
+#pragma unroll
+					for (int k = 0; k < K; ++k)
+					{
+						const int iz = izb + k;
+						if (iz <= k1)
+						{
+							lattice[((int64_t)iz * g.NY + iy) * g.NX + ix] = res[k];
+							if (Box) box[((oz + tz * K + k) * C + (oy + ty)) * C + (ox + tx)] = res[k];
+						}
+					}
+				}
+			}
+		}
+
 		// Lattice points of every listed brick: corners [i0, i0 + B] per axis, clamped to the
 		// lattice.  A brick's box is covered in 8 x 8 column blocks x 2 z-groups: a brick has
 		// four slices, slice s holding rows 4 (s & 1) .. 4 (s & 1) + 3 of each 8 x 8 block and
@@ -138,7 +223,6 @@ namespace tg
 				tc::BarInit(&idle_bar[warp], 1);
 			}
 			__syncwarp();
-			constexpr int ZSpan = 2 * K;
 			// Items: a lattice that fits the device has fewer than 2^30 bricks.
 			const uint32_t items = *count * (uint32_t)kBrickWarps;
 			for (;;)
@@ -148,7 +232,6 @@ namespace tg
 				item = __shfl_sync(0xffffffffu, item, 0);
 				if (item >= items) break;
 				const int slice = (int)(item % kBrickWarps);
-				const int tx = lane & 7, ty = (lane >> 3) + 4 * (slice & 1), tz = slice >> 1;
 				const uint32_t b = __ldg(list + item / kBrickWarps);
 				const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
 				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
@@ -184,73 +267,7 @@ namespace tg
 						code = staged - dc;
 					}
 				}
-				for (int oz = 0; oz < C; oz += ZSpan)
-				for (int oy = 0; oy < C; oy += 8)
-				for (int ox = 0; ox < C; ox += 8)
-				{
-					const int ix = i0 + ox + tx, iy = j0 + oy + ty, izb = k0 + oz + tz * K;
-					const bool inPlane = ix <= i1 && iy <= j1;
-					const float x = LatticeCoord(g.X0, min(ix, i1), g.DX);
-					const float y = LatticeCoord(g.Y0, min(iy, j1), g.DY);
-					float px[K], py[K], pz[K], res[K];
-					int cell[K];
-					unsigned todo = 0;
-#pragma unroll
-					for (int k = 0; k < K; ++k)
-					{
-						const int iz = izb + k;
-						px[k] = x;
-						py[k] = y;
-						pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.DZ);
-						cell[k] = shared ? top : DescendOctreeFrom(prog.Nodes, top, px[k], py[k], pz[k]);
-						res[k] = 0.0f;
-						if (inPlane && iz <= k1) todo |= 1u << k;
-					}
-					while (todo)
-					{
-						int c = -1;
-#pragma unroll
-						for (int k = 0; k < K; ++k)
-							if (c < 0 && ((todo >> k) & 1u)) c = cell[k];
-						float r[K];
-						if constexpr (K % 2 == 0)
-						{
-							// Points in pairs through the paired FP32 instructions (tg_pair.cuh).
-							if (Stage)
-							{
-								RunDistancePaired<K>([&](int q) { return code[q]; }, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r,
-									spill + 2 * threadIdx.x, kBrickThreads);
-							}
-							else
-							{
-								RunDistancePaired<K>([&](int q) { return __ldg(code + q); }, __ldg(&prog.Nodes[c].DistanceCode), px,
-									py, pz, r, spill + 2 * threadIdx.x, kBrickThreads);
-							}
-						}
-						else
-						{
-							RunDistance<K>(prog.Code, __ldg(&prog.Nodes[c].DistanceCode), px, py, pz, r, spill + threadIdx.x, kBrickThreads);
-						}
-#pragma unroll
-						for (int k = 0; k < K; ++k)
-						{
-							if (((todo >> k) & 1u) && cell[k] == c)
-							{
-								res[k] = r[k];
-								todo &= ~(1u << k);
-							}
-						}
-					}
-					if (inPlane)
-					{
-#pragma unroll
-						for (int k = 0; k < K; ++k)
-						{
-							const int iz = izb + k;
-							if (iz <= k1) lattice[((int64_t)iz * g.NY + iy) * g.NX + ix] = res[k];
-						}
-					}
-				}
+				EvalSlice<C, K, Stage, false>(prog, g, i0, i1, j0, j1, k0, k1, top, shared, slice, lane, code, lattice, spill, nullptr);
 				__syncwarp();   // every lane is done with this item's staged copy
 			}
 		}
@@ -357,6 +374,68 @@ namespace tg
 
 		// BT: the brick edge in cells when known at compile time (the cell coordinates then
 		// come from constant divisions, edge bricks masking their missing cells), or 0.
+		// The cell pass of one kept brick from its corner box in shared memory (kTiledBox^3,
+		// x fastest): every cell with corners of both signs sets its bit in `words` and is
+		// appended to `cells` (one atomic per brick).  Called by the whole CTA (it
+		// synchronises); `warpBase` is shared scratch, one word per warp.
+		template<int BT>
+		__device__ __forceinline__ void BrickCellFlags(const float* box, const BrickCells& bc, const CellGeom& cg, uint32_t* __restrict__ words,
+			uint32_t* __restrict__ cells, uint32_t* __restrict__ cell_count, uint32_t* warpBase)
+		{
+			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+			const int ex = BT ? BT : bc.nx, ey = BT ? BT : bc.ny;
+			const int total = BT ? BT * BT * BT : bc.nx * bc.ny * bc.nz;
+			const int64_t sxy = cg.sx * cg.sy;
+			const int64_t c0 = bc.i0 + bc.j0 * cg.sx + bc.k0 * sxy;
+			unsigned ballots[kTiledRounds];
+			uint32_t cellOf[kTiledRounds];
+			uint32_t mine = 0;
+#pragma unroll
+			for (int r = 0; r < kTiledRounds; ++r)
+			{
+				const int t = r * kTiledThreads + (int)threadIdx.x;
+				bool active = false;
+				cellOf[r] = 0;
+				const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+				if (t < total && x < bc.nx && y < bc.ny && z < bc.nz)
+				{
+					const float* b = box + (z * kTiledBox + y) * kTiledBox + x;
+					constexpr int dy = kTiledBox, dz = kTiledBox * kTiledBox;
+					const float v[8] = { b[0], b[1], b[dy + 1], b[dy], b[dz], b[dz + 1], b[dz + dy + 1], b[dz + dy] };
+					unsigned pos = 0;
+#pragma unroll
+					for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
+					active = pos != 0u && pos != 0xFFu;
+					const int64_t c = c0 + x + y * cg.sx + z * sxy;
+					cellOf[r] = (uint32_t)c;
+					if (active) atomicOr(words + (c >> 5), 1u << (c & 31));
+				}
+				ballots[r] = __ballot_sync(0xFFFFFFFFu, active);
+				mine += (uint32_t)__popc(ballots[r]);
+			}
+			if (lane == 0) warpBase[warp] = mine;
+			__syncthreads();
+			if (threadIdx.x == 0)
+			{
+				uint32_t sum = 0;
+				uint32_t counts[kTiledThreads / 32];
+#pragma unroll
+				for (int w = 0; w < kTiledThreads / 32; ++w) { counts[w] = warpBase[w]; sum += counts[w]; }
+				uint32_t at = sum ? atomicAdd(cell_count, sum) : 0u;
+#pragma unroll
+				for (int w = 0; w < kTiledThreads / 32; ++w) { warpBase[w] = at; at += counts[w]; }
+			}
+			__syncthreads();
+			uint32_t at = warpBase[warp];
+			const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+			for (int r = 0; r < kTiledRounds; ++r)
+			{
+				if ((ballots[r] >> lane) & 1u) cells[at + __popc(ballots[r] & below)] = cellOf[r];
+				at += (uint32_t)__popc(ballots[r]);
+			}
+		}
+
 		template<int BT>
 		__global__ void __launch_bounds__(kTiledThreads) CellFlagsTiledKernel(const float* __restrict__ lat, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, uint32_t* __restrict__ words,
@@ -366,7 +445,6 @@ namespace tg
 			__shared__ uint32_t warpBase[kTiledThreads / 32];
 			const CellGeom cg = Geom(g);
 			const uint32_t n = *count;
-			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 			for (uint32_t item = blockIdx.x; item < n; item += gridDim.x)
 			{
 				const BrickCells bc = CellsOf(__ldg(list + item), bg, cg);
@@ -378,57 +456,46 @@ namespace tg
 						box[t] = __ldg(lat + ((bc.k0 + z) * cg.ny + bc.j0 + y) * cg.nx + bc.i0 + x);
 				}
 				__syncthreads();
-				const int ex = BT ? BT : bc.nx, ey = BT ? BT : bc.ny;
-				const int total = BT ? BT * BT * BT : bc.nx * bc.ny * bc.nz;
-				const int64_t sxy = cg.sx * cg.sy;
-				const int64_t c0 = bc.i0 + bc.j0 * cg.sx + bc.k0 * sxy;
-				unsigned ballots[kTiledRounds];
-				uint32_t cellOf[kTiledRounds];
-				uint32_t mine = 0;
-#pragma unroll
-				for (int r = 0; r < kTiledRounds; ++r)
-				{
-					const int t = r * kTiledThreads + (int)threadIdx.x;
-					bool active = false;
-					cellOf[r] = 0;
-					const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
-					if (t < total && x < bc.nx && y < bc.ny && z < bc.nz)
-					{
-						const float* b = box + (z * kTiledBox + y) * kTiledBox + x;
-						constexpr int dy = kTiledBox, dz = kTiledBox * kTiledBox;
-						const float v[8] = { b[0], b[1], b[dy + 1], b[dy], b[dz], b[dz + 1], b[dz + dy + 1], b[dz + dy] };
-						unsigned pos = 0;
-#pragma unroll
-						for (int q = 0; q < 8; ++q) pos |= (v[q] >= 0.0f ? 1u : 0u) << q;
-						active = pos != 0u && pos != 0xFFu;
-						const int64_t c = c0 + x + y * cg.sx + z * sxy;
-						cellOf[r] = (uint32_t)c;
-						if (active) atomicOr(words + (c >> 5), 1u << (c & 31));
-					}
-					ballots[r] = __ballot_sync(0xFFFFFFFFu, active);
-					mine += (uint32_t)__popc(ballots[r]);
-				}
-				if (lane == 0) warpBase[warp] = mine;
+				BrickCellFlags<BT>(box, bc, cg, words, cells, cell_count, warpBase);
+			}
+		}
+
+		// The brick evaluation with the cell pass folded in (7^3-cell bricks, programs read
+		// from global memory): a CTA draws a brick from a counter, each warp evaluates one of
+		// its four slices (EvalSlice) into the lattice and into the brick's 8^3 corner box in
+		// shared memory, and the CTA then flags and lists the brick's active cells from that
+		// box (BrickCellFlags) -- the separate cell pass read the boxes back from memory.
+		template<int K>
+		__global__ void __launch_bounds__(kBrickThreads, EvalBricksCtasPerSm<8>()) EvalBricksCellsKernel(DeviceProgram prog, GridSpec g,
+			BrickGrid bg, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count, const uint32_t* __restrict__ tops,
+			float* __restrict__ lattice, uint32_t* __restrict__ words, uint32_t* __restrict__ cells, uint32_t* __restrict__ cell_count,
+			uint32_t* __restrict__ next)
+		{
+			extern __shared__ __align__(16) float spill[];
+			__shared__ float box[kTiledBox * kTiledBox * kTiledBox];
+			__shared__ uint32_t warpBase[kBrickWarps];
+			__shared__ uint32_t itemSlot;
+			static_assert(kBrickWarps == kTiledThreads / 32, "the cell pass takes the CTA's warps");
+			const CellGeom cg = Geom(g);
+			const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+			const uint32_t n = *count;
+			for (;;)
+			{
+				if (threadIdx.x == 0) itemSlot = atomicAdd(next, 1u);
+				__syncthreads();   // also: the previous brick is done with the box and the bases
+				const uint32_t item = itemSlot;
 				__syncthreads();
-				if (threadIdx.x == 0)
-				{
-					uint32_t sum = 0;
-					uint32_t counts[kTiledThreads / 32];
-#pragma unroll
-					for (int w = 0; w < kTiledThreads / 32; ++w) { counts[w] = warpBase[w]; sum += counts[w]; }
-					uint32_t at = sum ? atomicAdd(cell_count, sum) : 0u;
-#pragma unroll
-					for (int w = 0; w < kTiledThreads / 32; ++w) { warpBase[w] = at; at += counts[w]; }
-				}
+				if (item >= n) break;
+				const uint32_t b = __ldg(list + item);
+				const int bx = (int)(b % (uint32_t)bg.NBX), by = (int)((b / (uint32_t)bg.NBX) % (uint32_t)bg.NBY);
+				const int bz = (int)(b / ((uint32_t)bg.NBX * (uint32_t)bg.NBY));
+				const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
+				const int i1 = min(i0 + bg.B, g.NX - 1), j1 = min(j0 + bg.B, g.NY - 1), k1 = min(k0 + bg.B, g.NZ - 1);
+				const uint32_t packed = tops ? __ldg(tops + b) : BrickTop(prog, g, i0, i1, j0, j1, k0, k1);
+				EvalSlice<8, K, false, true>(prog, g, i0, i1, j0, j1, k0, k1, (int)(packed & 0x7FFFFFFFu), (packed >> 31) != 0u, warp, lane,
+					prog.Code, lattice, spill, box);
 				__syncthreads();
-				uint32_t at = warpBase[warp];
-				const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-				for (int r = 0; r < kTiledRounds; ++r)
-				{
-					if ((ballots[r] >> lane) & 1u) cells[at + __popc(ballots[r] & below)] = cellOf[r];
-					at += (uint32_t)__popc(ballots[r]);
-				}
+				BrickCellFlags<kTiledBox - 1>(box, CellsOf(b, bg, cg), cg, words, cells, cell_count, warpBase);
 			}
 		}
 
@@ -548,6 +615,42 @@ namespace tg
 		if (B + 1 <= 24) return LaunchEvalBricksC<24>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
 		if (B + 1 <= 40) return LaunchEvalBricksC<40>(prog, g, B, list, count, tops, lattice, sms, stream, lanes, staged, status);
 		return cudaErrorInvalidValue;
+	}
+
+	namespace
+	{
+		template<int K>
+		cudaError_t LaunchEvalBricksCellsK(const DeviceProgram& prog, const GridSpec& g, const uint32_t* list, const uint32_t* count,
+			const uint32_t* tops, float* lattice, uint32_t* words, uint32_t* cells, uint32_t* cell_count, int sms, cudaStream_t stream,
+			int* status)
+		{
+			const int depth = prog.MaxStack > 1 ? prog.MaxStack - 1 : 1;
+			const size_t smem = (size_t)depth * K * kBrickThreads * sizeof(float);
+			if (smem > 40 * 1024)
+			{
+				cudaError_t e = cudaFuncSetAttribute(EvalBricksCellsKernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+				if (e != cudaSuccess) return e;
+			}
+			EvalBricksCellsKernel<K><<<sms * EvalBricksCtasPerSm<8>(), kBrickThreads, smem, stream>>>(prog, g, MakeBrickGrid(g, kTiledBox - 1),
+				list, count, tops, lattice, words, cells, cell_count, reinterpret_cast<uint32_t*>(status) + 1);
+			return cudaGetLastError();
+		}
+	}
+
+	cudaError_t LaunchEvalBricksCells(const DeviceProgram& prog, const GridSpec& g, const uint32_t* list, const uint32_t* count,
+		const uint32_t* tops, float* lattice, uint32_t* words, uint32_t* cells, uint32_t* cell_count, int sms, cudaStream_t stream,
+		int lanes, int* status)
+	{
+		const int64_t total = (int64_t)(g.NX - 1) * (g.NY - 1) * (g.NZ - 1);
+		cudaError_t e = cudaMemsetAsync(words, 0, (size_t)((total + 31) / 32) * 4, stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(cell_count, 0, sizeof(uint32_t), stream);
+		if (e != cudaSuccess) return e;
+		switch (lanes)
+		{
+		case 1: return LaunchEvalBricksCellsK<1>(prog, g, list, count, tops, lattice, words, cells, cell_count, sms, stream, status);
+		case 2: return LaunchEvalBricksCellsK<2>(prog, g, list, count, tops, lattice, words, cells, cell_count, sms, stream, status);
+		default: return LaunchEvalBricksCellsK<4>(prog, g, list, count, tops, lattice, words, cells, cell_count, sms, stream, status);
+		}
 	}
 
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,

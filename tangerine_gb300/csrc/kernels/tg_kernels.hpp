@@ -85,6 +85,12 @@ namespace tg
 	// tops: the classifier's brick_tops for every listed brick, or nullptr (the kernel descends).
 	cudaError_t LaunchEvalBricks(const DeviceProgram& prog, const GridSpec& g, int B, const uint32_t* list, const uint32_t* count,
 		const uint32_t* tops, float* lattice, int sms, cudaStream_t stream, int lanes, bool staged, int* status);
+	// LaunchEvalBricks and LaunchCellFlagsListed in one launch, for 7^3-cell bricks with the
+	// programs read from global memory: the same lattice, cell bits and active-cell list
+	// (list order differs).  status as LaunchEvalBricks's.
+	cudaError_t LaunchEvalBricksCells(const DeviceProgram& prog, const GridSpec& g, const uint32_t* list, const uint32_t* count,
+		const uint32_t* tops, float* lattice, uint32_t* words, uint32_t* cells, uint32_t* cell_count, int sms, cudaStream_t stream,
+		int lanes, int* status);
 	cudaError_t LaunchCellFlagsBricks(const float* lattice, const GridSpec& g, int B, const uint32_t* brick_bits, uint32_t* words,
 		cudaStream_t stream);
 	// Cell pass over the cells of listed bricks only: clears and fills the bitmask and
