@@ -608,8 +608,8 @@ def our_arm(args, rank, world, local_rank):
     eval_grid_ms = sdf.profile_read("eval_grid")[0] / args.steps
 
     value = world * samples * args.steps / (total_ms * 1e-3)
-    # Launches of our kernels per step: classify, brick list (scan 3 + compaction), eval
-    # bricks, cell flags, scan (3), vertices, scan (3), faces, attributes.
+    # Launches of our kernels per step: classify, brick list (scan 3 + compaction), brick
+    # evaluation with the cell pass, scan (3), vertices, scan (3), faces, normals, colours.
     launches_per_step = 16
 
     # The surrogate-culled form: the network trained on this tree decides which bricks to
@@ -671,12 +671,13 @@ def our_arm(args, rank, world, local_rank):
     fp32 = _lib.C.c_double()
     _lib.check(lib.tg_measure_fp32_peak(_lib.C.byref(fp32), sp), "fp32 peak")
     achieved = brick_fl / (eval_bricks_ms * 1e-3) / 1e12
-    traffic = committed_traffic("EvalBricksKernel")
+    traffic = committed_traffic("EvalBricksCellsKernel")
     dense_achieved = flops / (eval_grid_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32.value, "unit": "TFLOP/s",
                 "frac": achieved / fp32.value, "traffic": traffic["bytes_per_launch"] if traffic else None,
                 "traffic_source": traffic["source"] if traffic else None,
-                "kernel": "EvalBricksKernel (distance interpreter on the kept bricks of the timed export)",
+                "kernel": "EvalBricksCellsKernel (distance interpreter on the kept bricks of the timed export, with the "
+                          "cell pass on each brick's values in shared memory folded in; its time counts both)",
                 "flops_per_launch": brick_fl, "lattice_points_per_launch": brick_points,
                 "algorithmic_bytes_per_launch": 4 * brick_points,
                 "peak_source": "measured in this run: FFMA throughput probe (tg_measure_fp32_peak), of measured",

@@ -2,6 +2,7 @@
 #include "tg_engine.hpp"
 #include "tg_surrogate.hpp"
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
@@ -349,7 +350,9 @@ namespace tg
 				End(s);
 			}
 			Begin("list_bricks", s);
-			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s));
+			TG_TRY(ClassCounts.Reserve(8 * sizeof(uint32_t)));
+			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s,
+				&p.View, tops, ClassCounts.As<uint32_t>()));
 			End(s);
 			LastBrickSize = B;
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.
@@ -524,6 +527,7 @@ namespace tg
 		brick_size = LastBrickSize;
 		if (ActiveBricks <= 0) return cudaSuccess;
 		TG_TRY(cudaMemcpy(out.data(), BrickList.Ptr, (size_t)ActiveBricks * 4, cudaMemcpyDeviceToHost));
+		std::sort(out.begin(), out.end());      // the evaluation's list is in cost order
 		return cudaSuccess;
 	}
 

@@ -177,7 +177,7 @@ namespace tg
 		cudaStream_t CopyStream = nullptr;          // early device-to-host copies of an export
 		cudaEvent_t MeshReady = nullptr;
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
-		DeviceBuffer Points, PointOut, BrickBits, BrickList, BrickTops, ProgramScratch, ActiveCells;
+		DeviceBuffer Points, PointOut, BrickBits, BrickList, BrickTops, ClassCounts, ProgramScratch, ActiveCells;
 		DeviceBuffer RayIn, RayOut, Cameras, Image, RenderCounters;
 		DeviceBuffer SodaBoxes, SodaCache, SodaColors;
 		void* Staging = nullptr;

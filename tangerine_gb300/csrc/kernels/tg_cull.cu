@@ -82,6 +82,51 @@ namespace tg
 			}
 		}
 
+		// Cost class of a kept brick, for the order the evaluation takes bricks in: the length
+		// of its descended cell's distance program (for a brick whose box straddles a pivot,
+		// an ancestor's, which is longer) in four classes, the longest first.  Bricks that
+		// come last in brick-index order can be the costliest (long programs where the tree
+		// is dense); taken last, one of them keeps its CTA busy long after the others are
+		// done.
+		constexpr int kCostClasses = 4;
+
+		__device__ __forceinline__ int CostClass(const DeviceProgram& prog, uint32_t packed_top)
+		{
+			const int cell = (int)(packed_top & 0x7FFFFFFFu);
+			const int len = __ldg(&prog.Nodes[cell].SurfaceCode) - __ldg(&prog.Nodes[cell].DistanceCode);
+			return len >= 512 ? 0 : len >= 128 ? 1 : len >= 32 ? 2 : 3;
+		}
+
+		// Kept bricks by cost class, a thread per brick.  Place = false adds each class's
+		// bricks to counts[c] and all of them to *total; Place = true (counts[0..3] complete,
+		// counts[4..7] zeroed) writes class c's bricks after those of the classes before it,
+		// in about brick-index order within a class (warps append in the order they run).
+		template<bool Place>
+		__global__ void ListBricksByCostKernel(const uint32_t* __restrict__ bits, int64_t bricks, DeviceProgram prog,
+			const uint32_t* __restrict__ tops, uint32_t* counts, uint32_t* total, uint32_t* __restrict__ list)
+		{
+			const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+			const int lane = (int)(threadIdx.x & 31);
+			int cls = kCostClasses;           // not kept
+			if (b < bricks && ((__ldg(bits + (b >> 5)) >> (b & 31)) & 1u)) cls = CostClass(prog, __ldg(tops + b));
+			const unsigned peers = __match_any_sync(0xFFFFFFFFu, cls);
+			if (cls == kCostClasses) return;
+			const int leader = __ffs((int)peers) - 1;
+			const uint32_t k = (uint32_t)__popc(peers);
+			if (!Place)
+			{
+				if (lane == leader) { atomicAdd(counts + cls, k); atomicAdd(total, k); }
+				return;
+			}
+			uint32_t at = 0;
+			if (lane == leader) at = atomicAdd(counts + kCostClasses + cls, k);
+			at = __shfl_sync(peers, at, leader);
+			uint32_t start = 0;
+#pragma unroll
+			for (int c = 0; c < kCostClasses - 1; ++c) if (c < cls) start += counts[c];
+			list[start + at + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = (uint32_t)b;
+		}
+
 		// Bricks whose bit is set, in brick-index order (x fastest): consecutive list entries
 		// are neighbours, so the CTAs evaluating them at the same time share octree cells and
 		// their record streams in cache.
@@ -545,10 +590,20 @@ namespace tg
 	}
 
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
-		uint32_t* count, cudaStream_t stream)
+		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog, const uint32_t* tops, uint32_t* class_counts)
 	{
 		const int64_t words = (bricks + 31) / 32;
 		if (words <= 0) return cudaMemsetAsync(count, 0, 4, stream);
+		if (prog && tops && class_counts)
+		{
+			cudaError_t e = cudaMemsetAsync(class_counts, 0, 2 * kCostClasses * sizeof(uint32_t), stream);
+			if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(uint32_t), stream);
+			if (e != cudaSuccess) return e;
+			const unsigned blocks = (unsigned)((bricks + 255) / 256);
+			ListBricksByCostKernel<false><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, tops, class_counts, count, list);
+			ListBricksByCostKernel<true><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, tops, class_counts, count, list);
+			return cudaGetLastError();
+		}
 		cudaError_t e = LaunchExclusiveScan(brick_bits, words, true, base, count, scratch, stream);
 		if (e != cudaSuccess) return e;
 		ListBricksKernel<<<(unsigned)((words + 255) / 256), 256, 0, stream>>>(brick_bits, words, base, list);

@@ -75,8 +75,12 @@ namespace tg
 		const uint32_t* candidates = nullptr, uint32_t* brick_tops = nullptr);
 	// Set bits as a list in brick-index order (scan + compaction); *count (device) gets the
 	// length.  base: (bricks + 31) / 32 words; scratch: ScanScratchWords of that.
+	// With the classifier's brick_tops (and `prog`, and eight scratch words in class_counts),
+	// the list is ordered instead by the cost of the bricks' programs, the costliest first,
+	// so that a persistent evaluation does not end on them; base and scratch are then unused.
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
-		uint32_t* count, cudaStream_t stream);
+		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog = nullptr, const uint32_t* tops = nullptr,
+		uint32_t* class_counts = nullptr);
 	// The brick kernels below run persistent grids sized from the SM count (`sms`).
 	// Brick evaluation.  status[0..1], zeroed by the caller: status[0] becomes nonzero if a
 	// staged program copy does not complete in time; status[1] is the warps' work counter.
