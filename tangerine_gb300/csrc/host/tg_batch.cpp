@@ -39,7 +39,7 @@ namespace tg
 	void Batch::Release()
 	{
 		DropGraph();
-		for (DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &CellBits,
+		for (DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &BrickTops, &CellBits,
 			&CellWordBase, &ActiveCells, &Lattice, &Vertices, &Normals, &Colors, &Cubes, &FaceCounts, &FaceBase, &Faces,
 			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status, &Knobs })
 			b->Release();
@@ -161,12 +161,13 @@ namespace tg
 		TG_TRY(BrickBits.Reserve(4 * (size_t)bword));
 		TG_TRY(BrickWordBase.Reserve(4 * (size_t)bword));
 		TG_TRY(BrickList.Reserve(4 * (size_t)bword * 32));
+		TG_TRY(BrickTops.Reserve(4 * (size_t)bword * 32));
 		TG_TRY(CellBits.Reserve(4 * (size_t)cword));
 		TG_TRY(CellWordBase.Reserve(4 * (size_t)cword));
 		TG_TRY(Lattice.Reserve(4 * (size_t)lat));
 		TG_TRY(VertexBase.Reserve(4 * ((size_t)n + 1)));
 		TG_TRY(FaceBaseModel.Reserve(4 * ((size_t)n + 1)));
-		TG_TRY(Counters.Reserve(8 * 4));
+		TG_TRY(Counters.Reserve(16 * 4));
 		TG_TRY(Barrier.Reserve(8));
 		TG_TRY(Status.Reserve(4));
 		TG_TRY(Knobs.Reserve(4 * sizeof(uint64_t)));
@@ -196,6 +197,7 @@ namespace tg
 		State.BrickBits = BrickBits.As<uint32_t>();
 		State.BrickWordBase = BrickWordBase.As<uint32_t>();
 		State.BrickList = BrickList.As<uint32_t>();
+		State.BrickTops = BrickTops.As<uint32_t>();
 		State.CellBits = CellBits.As<uint32_t>();
 		State.CellWordBase = CellWordBase.As<uint32_t>();
 		State.Lattice = Lattice.As<float>();
@@ -237,7 +239,7 @@ namespace tg
 		State.Colors = Colors.As<uint8_t>();
 
 		auto enqueue = [&]() -> cudaError_t {
-			TG_TRY(cudaMemsetAsync(Counters.Ptr, 0, 8 * 4, s));
+			TG_TRY(cudaMemsetAsync(Counters.Ptr, 0, 16 * 4, s));
 			TG_TRY(cudaMemsetAsync(Barrier.Ptr, 0, 8, s));
 			TG_TRY(cudaMemsetAsync(Status.Ptr, 0, 4, s));
 			// Models with a learned bound: its brick bits first, into the model's words.
@@ -332,7 +334,7 @@ namespace tg
 		TG_TRY(cudaMemcpyAsync(HostFaceBase.data(), FaceBaseModel.Ptr, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
 		TG_TRY(cudaStreamSynchronize(s));
 		int64_t bytes = 0;
-		for (const DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &CellBits,
+		for (const DeviceBuffer* b : { &Models, &BrickWord0, &CellBit0, &CellWords, &BrickBits, &BrickWordBase, &BrickList, &BrickTops, &CellBits,
 			&CellWordBase, &ActiveCells, &Lattice, &Vertices, &Normals, &Colors, &Cubes, &FaceCounts, &FaceBase, &Faces,
 			&VertexBase, &FaceBaseModel, &Counters, &ScanPartials, &Barrier, &Status, &Knobs })
 			bytes += (int64_t)b->Bytes;

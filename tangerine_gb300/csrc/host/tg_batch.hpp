@@ -70,7 +70,7 @@ namespace tg
 		uint32_t CapVertices = 0, CapFaces = 0;
 		uint32_t ReqVertices = 0, ReqFaces = 0;     // capacities asked for by Reserve (0: estimate)
 		BatchState State{};
-		DeviceBuffer Models, BrickWord0, Tile0, CellBit0, CellWords, BrickBits, BrickWordBase, BrickList, CellBits, CellWordBase,
+		DeviceBuffer Models, BrickWord0, Tile0, CellBit0, CellWords, BrickBits, BrickWordBase, BrickList, BrickTops, CellBits, CellWordBase,
 			ActiveCells, Lattice, Vertices, Normals, Colors, Cubes, FaceCounts, FaceBase, Faces, VertexBase, FaceBaseModel,
 			Counters, ScanPartials, Barrier, Status, Knobs;
 		int* CancelHost = nullptr;                 // host-mapped page-locked flag

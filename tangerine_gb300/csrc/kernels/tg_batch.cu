@@ -192,8 +192,12 @@ namespace tg
 		// ---- per-item work ---------------------------------------------------------------
 
 		template<int K>
-		__device__ void EvalBrickK(const BatchModel& m, float* __restrict__ lattice, uint32_t b, float* spill)
+		__device__ void EvalBrickK(const BatchModel& m, float* __restrict__ lattice, uint32_t b, uint32_t packed_top, float* spill)
 		{
+			// The brick's descent from phase 2: every point below the cell reached by the whole
+			// box, and only where the box straddles a pivot a per-point descent from there.
+			const int top = (int)(packed_top & 0x7FFFFFFFu);
+			const bool shared = (packed_top >> 31) != 0u;
 			const GridSpec& g = m.Grid;
 			const DeviceProgram& prog = m.Prog;
 			constexpr int ZSpan = 2 * K;
@@ -220,7 +224,7 @@ namespace tg
 					px[k] = x;
 					py[k] = y;
 					pz[k] = LatticeCoord(g.Z0, min(iz, k1), g.DZ);
-					cell[k] = DescendOctree(prog.Nodes, px[k], py[k], pz[k]);
+					cell[k] = shared ? top : DescendOctreeFrom(prog.Nodes, top, px[k], py[k], pz[k]);
 					res[k] = 0.0f;
 					if (inPlane && iz <= k1) todo |= 1u << k;
 				}
@@ -333,17 +337,75 @@ namespace tg
 			}
 			if (!GridSync(s)) return;
 
-			// 2. Kept bricks as a list in global brick order.
-			if (!GridScan(s, s.BrickBits, s.BrickWordsTotal, true, s.BrickWordBase, s.Counters + 0)) return;
-			for (int64_t w = gtid; w < s.BrickWordsTotal; w += gthreads)
+			// 2. Kept bricks as a list, the costliest programs first (cost classes of the
+			//    bricks' descended cells, as the single export's list): bricks with long
+			//    programs drawn last would leave the end of phase 3 to a few CTAs.  A thread
+			//    per brick-bit word, its kept bricks one per round; counts per class with one
+			//    atomic per class and warp, then the places.
+			uint32_t* classCounts = s.Counters + 8;
+			uint32_t* classCursors = s.Counters + 12;
+			for (int64_t w = gtid; w - (int64_t)lane < s.BrickWordsTotal; w += gthreads)
 			{
-				uint32_t bits = s.BrickBits[w];
-				uint32_t at = s.BrickWordBase[w];
-				while (bits)
+				uint32_t bits = w < s.BrickWordsTotal ? s.BrickBits[w] : 0u;
+				const BatchModel* m = bits ? &s.Models[ModelOf(s.BrickWord0, s.Count, w)] : nullptr;
+				while (__any_sync(0xFFFFFFFFu, bits != 0u))
 				{
-					const int j = __ffs(bits) - 1;
-					bits &= bits - 1u;
-					s.BrickList[at++] = (uint32_t)(w * 32 + j);
+					int cls = kCostClasses;
+					if (bits)
+					{
+						const int j = __ffs((int)bits) - 1;
+						bits &= bits - 1u;
+						const int64_t gb = w * 32 + j;
+						const int64_t b = gb - m->BrickWord0 * 32;
+						const int bx = (int)(b % m->NBX), by = (int)((b / m->NBX) % m->NBY), bz = (int)(b / ((int64_t)m->NBX * m->NBY));
+						const int i0 = bx * m->B, j0 = by * m->B, k0 = bz * m->B;
+						const uint32_t top = BrickTop(m->Prog, m->Grid, i0, min(i0 + m->B, m->Grid.NX - 1), j0, min(j0 + m->B, m->Grid.NY - 1),
+							k0, min(k0 + m->B, m->Grid.NZ - 1));
+						s.BrickTops[gb] = top;
+						cls = CostClass(m->Prog, top);
+					}
+					const unsigned peers = __match_any_sync(0xFFFFFFFFu, cls);
+					if (cls < kCostClasses && lane == __ffs((int)peers) - 1)
+					{
+						atomicAdd(classCounts + cls, (uint32_t)__popc(peers));
+						atomicAdd(s.Counters + 0, (uint32_t)__popc(peers));
+					}
+				}
+			}
+			if (!GridSync(s)) return;
+			uint32_t classStart[kCostClasses];
+			{
+				uint32_t o = 0;
+#pragma unroll
+				for (int c = 0; c < kCostClasses; ++c) { classStart[c] = o; o += classCounts[c]; }
+			}
+			for (int64_t w = gtid; w - (int64_t)lane < s.BrickWordsTotal; w += gthreads)
+			{
+				uint32_t bits = w < s.BrickWordsTotal ? s.BrickBits[w] : 0u;
+				const BatchModel* m = bits ? &s.Models[ModelOf(s.BrickWord0, s.Count, w)] : nullptr;
+				while (__any_sync(0xFFFFFFFFu, bits != 0u))
+				{
+					int cls = kCostClasses;
+					int64_t gb = 0;
+					if (bits)
+					{
+						const int j = __ffs((int)bits) - 1;
+						bits &= bits - 1u;
+						gb = w * 32 + j;
+						cls = CostClass(m->Prog, s.BrickTops[gb]);
+					}
+					const unsigned peers = __match_any_sync(0xFFFFFFFFu, cls);
+					if (cls < kCostClasses)
+					{
+						const int leader = __ffs((int)peers) - 1;
+						uint32_t at = 0;
+						if (lane == leader) at = atomicAdd(classCursors + cls, (uint32_t)__popc(peers));
+						at = __shfl_sync(peers, at, leader);
+						uint32_t start = classStart[0];
+#pragma unroll
+						for (int c = 1; c < kCostClasses; ++c) if (cls == c) start = classStart[c];
+						s.BrickList[start + at + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = (uint32_t)gb;
+					}
 				}
 			}
 			if (!GridSync(s)) return;
@@ -357,9 +419,10 @@ namespace tg
 				const BatchModel& m = s.Models[mi];
 				const uint32_t b = gb - (uint32_t)(m.BrickWord0 * 32);
 				float* lat = s.Lattice + m.Lattice;
-				if (m.Lanes == 1) EvalBrickK<1>(m, lat, b, spill);
-				else if (m.Lanes == 4) EvalBrickK<4>(m, lat, b, spill);
-				else EvalBrickK<2>(m, lat, b, spill);
+				const uint32_t top = s.BrickTops[gb];
+				if (m.Lanes == 1) EvalBrickK<1>(m, lat, b, top, spill);
+				else if (m.Lanes == 4) EvalBrickK<4>(m, lat, b, top, spill);
+				else EvalBrickK<2>(m, lat, b, top, spill);
 			}
 			if (!GridSync(s)) return;
 

@@ -48,18 +48,6 @@ namespace tg
 		// Kept bricks set their bit with atomicOr into the zeroed bit words.
 		constexpr int kTileX = 8, kTileY = 4, kTileZ = kClassifyThreads / (kTileX * kTileY);
 
-		// A kept brick's descent for the evaluation (DescendBox over its corner box): the cell
-		// reached in the low 31 bits, bit 31 set when every point of the box descends to it.
-		__device__ __forceinline__ uint32_t BrickTop(const DeviceProgram& prog, const GridSpec& g, int i0, int i1, int j0, int j1, int k0,
-			int k1)
-		{
-			bool shared;
-			const int top = DescendBox(prog.Nodes, LatticeCoord(g.X0, i0, g.DX), LatticeCoord(g.X0, i1, g.DX),
-				LatticeCoord(g.Y0, j0, g.DY), LatticeCoord(g.Y0, j1, g.DY), LatticeCoord(g.Z0, k0, g.DZ),
-				LatticeCoord(g.Z0, k1, g.DZ), shared);
-			return (uint32_t)top | (shared ? 0x80000000u : 0u);
-		}
-
 		__global__ void __launch_bounds__(kClassifyThreads) ClassifyBricksKernel(DeviceProgram prog, GridSpec g, BrickGrid bg,
 			const uint32_t* __restrict__ candidates, uint32_t* __restrict__ brick_bits, uint32_t* __restrict__ brick_tops)
 		{
@@ -80,21 +68,6 @@ namespace tg
 				atomicOr(brick_bits + (b >> 5), 1u << (b & 31));
 				if (brick_tops) brick_tops[b] = BrickTop(prog, g, i0, i1, j0, j1, k0, k1);
 			}
-		}
-
-		// Cost class of a kept brick, for the order the evaluation takes bricks in: the length
-		// of its descended cell's distance program (for a brick whose box straddles a pivot,
-		// an ancestor's, which is longer) in four classes, the longest first.  Bricks that
-		// come last in brick-index order can be the costliest (long programs where the tree
-		// is dense); taken last, one of them keeps its CTA busy long after the others are
-		// done.
-		constexpr int kCostClasses = 4;
-
-		__device__ __forceinline__ int CostClass(const DeviceProgram& prog, uint32_t packed_top)
-		{
-			const int cell = (int)(packed_top & 0x7FFFFFFFu);
-			const int len = __ldg(&prog.Nodes[cell].SurfaceCode) - __ldg(&prog.Nodes[cell].DistanceCode);
-			return len >= 512 ? 0 : len >= 128 ? 1 : len >= 32 ? 2 : 3;
 		}
 
 		// Kept bricks by cost class, a thread per brick.  Place = false adds each class's

@@ -339,6 +339,7 @@ namespace tg
 		uint32_t* BrickBits;
 		uint32_t* BrickWordBase;
 		uint32_t* BrickList;
+		uint32_t* BrickTops;           // per global brick: the kept brick's descent (cell | shared << 31)
 		uint32_t* CellBits;
 		uint32_t* CellWordBase;
 		uint64_t* ActiveCells;
@@ -353,7 +354,8 @@ namespace tg
 		uint32_t* Faces;
 		uint32_t* VertexBase;          // per model + 1: first vertex (global numbering)
 		uint32_t* FaceBaseModel;       // per model + 1: first face
-		uint32_t* Counters;            // kept bricks, active cells, vertices, faces, overflow bits
+		uint32_t* Counters;            // kept bricks, active cells, vertices, faces, overflow bits; [8..15]: cost
+		                               // classes' brick counts and cursors
 		uint32_t* ScanPartials;        // blocks + 1
 		unsigned* Barrier;             // arrival count, generation
 		int* Status;                   // 2: a barrier wait ran out; 3: cancelled
