@@ -352,7 +352,7 @@ def test_culled_export_on_ragged_grids(lib, lanes, staged):
         for grid in grids:
             dense = prog.export_mesh(grid, dense=True)
             assert dense.vertices.shape[0] > 0
-            for brick in (3, 7, 10, 32):
+            for brick in (1, 3, 4, 7, 10, 11, 15, 32):
                 culled = prog.export_mesh(grid, brick=brick, lanes=lanes, staged=staged)
                 for a, b in ((dense.vertices, culled.vertices), (dense.faces, culled.faces),
                              (dense.normals, culled.normals), (dense.colors, culled.colors), (dense.cubes, culled.cubes)):
