@@ -216,10 +216,10 @@ namespace tg
 		// z-group s >> 1; a lane runs K z-consecutive points of its column through one pass
 		// over their octree cell's records, so one pass of a slice covers an 8 x 4 x K box.
 		// A warp draws (brick, slice) items from a counter and goes on to its next item when it
-		// is done: a brick's cost follows its cell programs' lengths, and a fixed stride over
-		// the list left some SMs working for 1.3 times the mean.  The four slices of a brick
-		// are consecutive items, so they mostly run at the same time and share the records in
-		// L1.
+		// is done; a brick's cost follows its cell programs' lengths, and the list holds the
+		// costliest bricks first (LaunchListBricks), so the launch does not end on them.  The
+		// four slices of a brick are consecutive items, so they mostly run at the same time
+		// and share the records in L1.
 		// Stage = true: a warp whose brick's points all descend to one octree cell (the common
 		// case) first copies that cell's distance program into its own shared memory with one
 		// bulk copy (cp.async.bulk, completion on the warp's mbarrier, bounded wait) and reads
