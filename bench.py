@@ -654,7 +654,7 @@ def our_arm(args, rank, world, local_rank):
                "host_compile_split_s": {"octree": oct_s.value, "programs": comp_s.value - oct_s.value},
                "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
                "meshes_per_s": world * e2e_steps / e2e_s,
-               "call": "tg_export_tree (octree build + compile + upload + GPU export + copy to host)"}
+               "call": "tg_export_tree (octree build + compile, the GPU testing bricks on the root cell's program meanwhile; upload + rest of the GPU export + copy to host)"}
 
     # Roofline of the dominant kernel of the timed export (the distance interpreter on the
     # kept bricks): exact algorithmic flops over the lattice points of those bricks.

@@ -210,6 +210,12 @@ TANGERINE_API int64_t tg_debug_meshing_octree(void* tree, float* cells, int32_t*
 /* Host-only: builds and compiles the export (or meshing) octree without uploading it and
  * reports the seconds spent in the octree and in all of the compile. */
 TANGERINE_API tg_status tg_debug_compile_seconds(void* tree, int meshing, double* octree_seconds, double* total_seconds);
+/* Host-only check of the early brick test's input: compiles the export octree with the
+ * root-cell hook tg_export_tree uses and checks that the root program it handed out (before
+ * the levels below the root existed) has node 0's pivot and clip radius and, record for
+ * record, node 0's distance program.  TG_OK with the program's quads (stop included) and
+ * stack depth; TG_ERR_INVALID with the difference in tg_last_error otherwise. */
+TANGERINE_API tg_status tg_debug_root_program_check(void* tree, int64_t* code_quads, int32_t* stack_size);
 /* Host-only plan of tg_sodapop_mesh: grid gets origin xyz, step xyz, cells xyz, the point
  * cache's limit and the lattice's z layers (11 floats); boxes the leaves' inclusive integer
  * point-cache spans (6 per leaf, up to box_capacity leaves); leaves the leaf count. */

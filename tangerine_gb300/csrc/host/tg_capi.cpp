@@ -509,6 +509,35 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API tg_status tg_debug_root_program_check(void* tree, int64_t* code_quads, int32_t* stack_size)
+	{
+		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
+		RootProgram seen;
+		bool called = false;
+		const RootHook hook = [&](const RootProgram& r) { seen = r; called = true; };
+		CompiledTree t;
+		std::string err;
+		if (!CompileTree(Borrow(tree), t, err, OctreeKind::Export, &hook)) { SetError(err); return TG_ERR_UNBOUNDED; }
+		if (!called) { SetError("no root program was handed out"); return TG_ERR_INVALID; }
+		const OctNode& n0 = t.Nodes[0];
+		std::vector<float> image(t.CodeFloats);
+		t.CopyCode(image.data());
+		const size_t from = (size_t)n0.DistanceCode * 4, to = (size_t)n0.SurfaceCode * 4;
+		const bool samePlace = std::memcmp(seen.Node.Pivot, n0.Pivot, sizeof n0.Pivot) == 0 &&
+			std::memcmp(&seen.Node.ClipRadius, &n0.ClipRadius, sizeof(float)) == 0;
+		const bool sameCode = to - from == seen.Code.size() && to <= image.size() &&
+			std::memcmp(image.data() + from, seen.Code.data(), seen.Code.size() * sizeof(float)) == 0;
+		if (!samePlace || !sameCode || seen.Node.StackSize > n0.StackSize || seen.Node.StackSize < 1)
+		{
+			SetError(!samePlace ? "root pivot or clip radius differs from node 0" : !sameCode ?
+				"root program differs from node 0's distance program" : "root program stack size out of range");
+			return TG_ERR_INVALID;
+		}
+		if (code_quads) *code_quads = (int64_t)(seen.Code.size() / 4);
+		if (stack_size) *stack_size = seen.Node.StackSize;
+		return TG_OK;
+	}
+
 	TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* grid, int64_t* boxes, int64_t box_capacity,
 		int64_t* leaves)
 	{
@@ -691,17 +720,26 @@ extern "C"
 		std::unique_ptr<tg_program> prog(new (std::nothrow) tg_program());
 		if (!prog) { SetError("out of host memory"); return TG_ERR_MEMORY; }
 		std::string err;
-		if (!CompileTree(Borrow(tree), prog->Host, err))
+		const cudaStream_t s = StreamOf(stream);
+		ExportOptions opt = OptionsOf(TG_MESH_ATTRIBUTES);
+		// The exact brick test runs on the root cell's program, which exists right after
+		// the root clip: the GPU classifies the bricks while the host builds the octree
+		// below the root and emits its programs.
+		cudaError_t pre = cudaErrorNotReady;
+		const RootHook onRoot = [&](const RootProgram& r) { pre = eng.PreClassify(r, gs, opt.BrickSize, s); };
+		if (!CompileTree(Borrow(tree), prog->Host, err, OctreeKind::Export, opt.Dense ? nullptr : &onRoot))
 		{
 			SetError(err);
 			return TG_ERR_UNBOUNDED;
 		}
-		const cudaStream_t s = StreamOf(stream);
+		// Without the early test (an allocation failed, or none ran) the export classifies
+		// as usual.
+		if (pre != cudaSuccess && pre != cudaErrorNotReady) cudaGetLastError();
+		opt.PreClassified = pre == cudaSuccess;
 		cudaError_t ue = eng.UploadScratch(*prog, s);
 		if (ue != cudaSuccess) return CudaFail(ue, "uploading the program");
 		const auto t1 = clock();
 		DeviceMesh dm;
-		ExportOptions opt = OptionsOf(TG_MESH_ATTRIBUTES);
 		HostMeshOut host;
 		opt.Host = &host;
 		const cudaError_t e = eng.Export(*prog, gs, opt, dm, s);

@@ -270,8 +270,57 @@ namespace tg
 		return cudaSuccess;
 	}
 
+	cudaError_t Engine::PreClassify(const RootProgram& root, const GridSpec& g, int B, cudaStream_t s)
+	{
+		PreValid = false;
+		if (B < 1 || B > 15 || root.Code.empty()) return cudaErrorInvalidValue;
+		const int64_t nb = BrickCount(g, B);
+		if (nb <= 0) return cudaErrorInvalidValue;
+		TG_TRY(BrickBits.Reserve((size_t)((nb + 31) / 32) * 4));
+		// One node (64 bytes), then the records at a 256-byte boundary, as Pack lays out a
+		// program.
+		const size_t codeOff = 256, total = codeOff + root.Code.size() * sizeof(float);
+		TG_TRY(RootScratch.Reserve(total));
+		if (RootCopyPending)
+		{
+			TG_TRY(cudaEventSynchronize(RootCopied));
+			RootCopyPending = false;
+		}
+		if (RootStagingBytes < total)
+		{
+			if (RootStaging) cudaFreeHost(RootStaging);
+			RootStaging = nullptr;
+			RootStagingBytes = 0;
+			TG_TRY(cudaMallocHost(&RootStaging, total + total / 4));
+			RootStagingBytes = total + total / 4;
+		}
+		uint8_t* st = static_cast<uint8_t*>(RootStaging);
+		std::memcpy(st, &root.Node, sizeof(OctNode));
+		std::memcpy(st + codeOff, root.Code.data(), root.Code.size() * sizeof(float));
+		if (!RootCopied) TG_TRY(cudaEventCreateWithFlags(&RootCopied, cudaEventDisableTiming));
+		TG_TRY(cudaMemcpyAsync(RootScratch.Ptr, RootStaging, total, cudaMemcpyHostToDevice, s));
+		TG_TRY(cudaEventRecord(RootCopied, s));
+		RootCopyPending = true;
+		DeviceProgram v{};
+		v.Nodes = RootScratch.As<OctNode>();
+		v.Code = reinterpret_cast<const float4*>(RootScratch.As<uint8_t>() + codeOff);
+		v.MaxStack = root.Node.StackSize;
+		v.Lipschitz = root.Node.ClipRadius >= 0.0f ? 1 : 0;
+		Begin("classify_root", s);
+		TG_TRY(LaunchClassifyBricks(v, g, B, BrickBits.As<uint32_t>(), s));
+		End(s);
+		PreValid = true;
+		PreGrid = g;
+		PreBrickSize = B;
+		return cudaSuccess;
+	}
+
 	cudaError_t Engine::Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s)
 	{
+		// Bits PreClassify left for this export (any other export voids them).
+		const bool pre = opt.PreClassified && PreValid && !opt.Dense && !opt.Field && PreBrickSize == opt.BrickSize &&
+			std::memcmp(&PreGrid, &g, sizeof(GridSpec)) == 0;
+		PreValid = false;
 		out = DeviceMesh();
 		// Asynchronous exports stop at a synchronisation point once cancelled.
 		auto stopped = [&](float done) -> bool
@@ -315,7 +364,7 @@ namespace tg
 			TG_TRY(BrickTops.Reserve((size_t)nb * 4));
 			// The exact classifier stores each kept brick's descent for the evaluation; the
 			// network alone leaves the evaluation to descend.
-			const uint32_t* tops = (!opt.Field || opt.Refine) ? BrickTops.As<uint32_t>() : nullptr;
+			uint32_t* tops = (!opt.Field || opt.Refine) ? BrickTops.As<uint32_t>() : nullptr;
 			if (!SmCount)
 			{
 				int dev = 0;
@@ -343,7 +392,7 @@ namespace tg
 					bits = kept;
 				}
 			}
-			else
+			else if (!pre)
 			{
 				Begin("classify_bricks", s);
 				TG_TRY(LaunchClassifyBricks(p.View, g, B, bits, s, nullptr, BrickTops.As<uint32_t>()));
@@ -352,7 +401,7 @@ namespace tg
 			Begin("list_bricks", s);
 			TG_TRY(ClassCounts.Reserve(8 * sizeof(uint32_t)));
 			TG_TRY(LaunchListBricks(bits, nb, WordBase.As<uint32_t>(), Scratch.As<uint32_t>(), BrickList.As<uint32_t>(), brickCount, s,
-				&p.View, tops, ClassCounts.As<uint32_t>()));
+				&p.View, tops, ClassCounts.As<uint32_t>(), pre ? &g : nullptr, B));
 			End(s);
 			LastBrickSize = B;
 			// Active cells lie in listed bricks: bound the list by the bricks' cells.

@@ -73,6 +73,10 @@ namespace tg
 		bool Staged = false;        // brick evaluation reads single-cell bricks' programs from shared memory
 		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
 		bool Refine = true;                 // with Field: network-kept bricks also take the exact test
+		// The exact brick test already ran on the root cell's program (Engine::PreClassify,
+		// same grid and brick size, same stream): the export lists its bricks and descends
+		// them instead of classifying.
+		bool PreClassified = false;
 		HostMeshOut* Host = nullptr;        // also copy the mesh to host memory (see HostMeshOut)
 		// Host-side control of an asynchronous export (MeshExport): when *Active turns false
 		// the export stops at its next synchronisation point, sets *Cancelled and returns an
@@ -128,6 +132,12 @@ namespace tg
 		cudaError_t EvalGrid(const Program& p, const GridSpec& g, float* device_out, cudaStream_t s);
 		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
 		cudaError_t Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s);
+		// The exact brick test of a culled export on the root cell's program alone (the
+		// root's own sphere holds every ball it decides, so it is the test's holder of last
+		// resort), launched on `s` while the host is still building the octree below the
+		// root.  An export of the same grid and brick size on `s` with PreClassified set
+		// takes its brick bits; any other engine call in between voids them.
+		cudaError_t PreClassify(const RootProgram& root, const GridSpec& g, int brick_size, cudaStream_t s);
 		int64_t LastActiveBricks() const { return ActiveBricks; }
 		// The kept bricks of the last culled export (brick index order), copied to host.
 		cudaError_t LastBrickList(std::vector<uint32_t>& out, int& brick_size);
@@ -182,6 +192,17 @@ namespace tg
 		DeviceBuffer SodaBoxes, SodaCache, SodaColors;
 		void* Staging = nullptr;
 		size_t StagingBytes = 0;
+		// PreClassify's one-cell program: pinned staging, its device copy, the event after
+		// the copy (the staging is rewritten only once the last copy out of it is done),
+		// and the grid and brick size whose bits it left in BrickBits.
+		DeviceBuffer RootScratch;
+		void* RootStaging = nullptr;
+		size_t RootStagingBytes = 0;
+		cudaEvent_t RootCopied = nullptr;
+		bool RootCopyPending = false;
+		bool PreValid = false;
+		GridSpec PreGrid{};
+		int PreBrickSize = 0;
 		uint32_t* HostCounts = nullptr;
 		int SmCount = 0;
 		int64_t ActiveBricks = 0, Bricks = 0;

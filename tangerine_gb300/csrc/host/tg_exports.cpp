@@ -99,6 +99,7 @@ namespace tg
 		TG_TRY(WordBase.Reserve((size_t)(words ? words : 1) * 4));
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4 + 4));
+		PreValid = false;   // these bits replace a pending PreClassify's
 		TG_TRY(BrickBits.Reserve(VoxelBrickWords(s.IX, s.IY, s.IZ) * 4));
 		Begin("cloud_flags", st);
 		TG_TRY(LaunchCloudFlags(p.View, s, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), st));
@@ -162,6 +163,7 @@ namespace tg
 		TG_TRY(Counts.Reserve(4 * sizeof(uint32_t)));
 		TG_TRY(Scratch.Reserve(ScanScratchWords(words) * 4 + 4));
 		TG_TRY(Cubes.Reserve((size_t)(words ? words : 1) * 32 * 4));
+		PreValid = false;   // these bits replace a pending PreClassify's
 		TG_TRY(BrickBits.Reserve(VoxelBrickWords(s.SX, s.SY, s.SZ) * 4));
 		Begin("vox_flags", st);
 		TG_TRY(LaunchVoxFlags(p.View, s, BrickBits.As<uint32_t>(), Words.As<uint32_t>(), st));

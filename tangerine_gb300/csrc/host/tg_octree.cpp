@@ -255,7 +255,7 @@ namespace tg
 		}
 	}
 
-	bool Octree::Build(const NodeRef& root, float target, bool coalesce, int max_depth)
+	bool Octree::Build(const NodeRef& root, float target, bool coalesce, int max_depth, const RootSeen* on_root)
 	{
 		Cells.clear();
 		if (!root || !root->HasFiniteBounds()) return false;
@@ -273,6 +273,10 @@ namespace tg
 		top->Bounds = cube;
 		InitCell(*top, root, bp);
 		if (!top->Eval) return false;
+		// The levels below change the root's bounds but not its pivot, clip radius or
+		// evaluator (FinishCell only drops the evaluator when every octant is empty, and
+		// then the build fails).
+		if (on_root && *on_root) (*on_root)(top->Pivot, top->Radius, top->Eval);
 		BuildLevels({ top }, bp, 1, arena);
 		// SDFOctree::Create returns nullptr when the root lost its evaluator while
 		// populating (every octant clipped away).
@@ -773,23 +777,57 @@ namespace tg
 		else for (size_t i = 0; i < CodeChunks.size(); ++i) copy((int)i);
 	}
 
-	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind)
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind, const RootHook* on_root)
 	{
 		const auto t0 = std::chrono::steady_clock::now();
+		if (!root)
+		{
+			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
+			return false;
+		}
+		std::unordered_map<const Material*, int> materials;
+		std::vector<const Material*> materialList;
+		CollectMaterials(*root, materials, materialList);
+		// Every brush of the full tree (clipped trees share them) gets its records once, up
+		// front; the emitters only copy spans of them.
+		std::vector<float> unused;
+		Emitter shared(unused, materials);
+		shared.BuildAllRecords(*root);
+		// The root cell's program, emitted as the programs below emit node 0's.
+		Octree::RootSeen rootSeen;
+		if (on_root && *on_root && kind == OctreeKind::Export)
+		{
+			rootSeen = [&](const Vec3& pivot, float radius, const NodeRef& evaluator)
+			{
+				RootProgram rp;
+				Emitter em(rp.Code, materials, &shared);
+				em.Distance(*evaluator);
+				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				const int depth = ProgramDepth(rp.Code.data(), 0);
+				if (depth > kMaxStack) return;   // the compile fails on it below
+				OctNode& n = rp.Node;
+				n.Pivot[0] = pivot.x; n.Pivot[1] = pivot.y; n.Pivot[2] = pivot.z;
+				n.Flags = kNodeTerminus;
+				for (int k = 0; k < 8; ++k) n.Child[k] = -1;
+				n.DistanceCode = 0;
+				n.SurfaceCode = (int32_t)(rp.Code.size() / 4);
+				n.StackSize = depth;
+				n.ClipRadius = em.NonLipschitz ? -radius : radius;
+				(*on_root)(rp);
+			};
+		}
+		const auto ta = std::chrono::steady_clock::now();
 		Octree octree;
-		if (!(kind == OctreeKind::Meshing ? octree.BuildMeshing(root) : octree.Build(root)))
+		if (!(kind == OctreeKind::Meshing ? octree.BuildMeshing(root) : octree.Build(root, 0.25f, true, -1, &rootSeen)))
 		{
 			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
 			return false;
 		}
 		const auto t1 = std::chrono::steady_clock::now();
 		out = CompiledTree();
-		out.OctreeSeconds = std::chrono::duration<double>(t1 - t0).count();
+		out.OctreeSeconds = std::chrono::duration<double>(t1 - ta).count();
 		out.Bounds = root->Bounds();
 		out.OctreeBounds = octree.Cells[0].Bounds;
-		std::unordered_map<const Material*, int> materials;
-		std::vector<const Material*> materialList;
-		CollectMaterials(*root, materials, materialList);
 		// Each distinct evaluator's two programs are emitted once (cells whose clip left the
 		// parent's subtree untouched share its node, RebuildSet), in parallel over chunks of
 		// the distinct evaluators, each chunk into its own buffer with its own emitter; the
@@ -817,11 +855,6 @@ namespace tg
 				programOf[i] = index[h].second;
 			}
 		}
-		// Every brush of the full tree (clipped trees share them) gets its records once, up
-		// front; the emitters only copy spans of them.
-		std::vector<float> unused;
-		Emitter shared(unused, materials);
-		shared.BuildAllRecords(*root);
 		// The last item is the whole tree's surface program, for SDFNode::RayMarch / Eval.
 		const size_t items = distinct.size() + 1;
 		const int chunkCount = (int)std::min<size_t>(items, (size_t)WorkerPool::Get().Workers() * 4 + 4);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -28,9 +29,13 @@ namespace tg
 		};
 		std::vector<Cell> Cells;   // depth-first, root first
 
+		// The root cell as soon as its clip is done, before the levels below it are built:
+		// its pivot, clip radius and evaluator are already the ones Cells[0] ends with.
+		using RootSeen = std::function<void(const Vec3& pivot, float clip_radius, const NodeRef& evaluator)>;
 		// Returns false (and leaves Cells empty) when the tree has infinite or empty
 		// bounds, or clips away entirely, as SDFOctree::Create returns nullptr.
-		bool Build(const NodeRef& root, float target_size = 0.25f, bool coalesce = true, int max_depth = -1);
+		bool Build(const NodeRef& root, float target_size = 0.25f, bool coalesce = true, int max_depth = -1,
+			const RootSeen* on_root = nullptr);
 		// Sodapop's meshing octree (sodapop.cpp:565-567): SDFOctree::Create(.25, false, 3),
 		// then every cell left incomplete at depth 3 populated on its own with
 		// Populate(false, 3, -1).  The second stage does not revisit the ancestors, so they
@@ -64,9 +69,25 @@ namespace tg
 		int64_t DistanceQuadsTotal = 0;
 	};
 
+	// The export octree's root cell on its own, as a one-cell program image: Node is the
+	// compiled tree's node 0 (terminus, no children, its distance program at quad 0,
+	// StackSize that program's depth) and Code that distance program with its stop
+	// record -- the same records the compiled tree gives node 0.  It exists a few tens of
+	// microseconds into the compile, long before the octree below it: the root's program
+	// has the whole tree's sign everywhere in the root sphere, so the exact brick test can
+	// run on it while the host builds the rest.
+	struct RootProgram
+	{
+		OctNode Node{};
+		std::vector<float> Code;
+	};
+	using RootHook = std::function<void(const RootProgram&)>;
+
 	enum class OctreeKind { Export, Meshing };
 	// Builds the octree of the given kind (Export: target 0.25 with coalescing, as the
 	// export and the point queries use; Meshing: Octree::BuildMeshing) and compiles every
-	// cell's clipped subtree.
-	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind = OctreeKind::Export);
+	// cell's clipped subtree.  `on_root` (Export only) is called on the compiling thread
+	// with the root cell's program as soon as the root is clipped.
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind = OctreeKind::Export,
+		const RootHook* on_root = nullptr);
 }

@@ -74,14 +74,31 @@ namespace tg
 		// bricks to counts[c] and all of them to *total; Place = true (counts[0..3] complete,
 		// counts[4..7] zeroed) writes class c's bricks after those of the classes before it,
 		// in about brick-index order within a class (warps append in the order they run).
-		template<bool Place>
-		__global__ void ListBricksByCostKernel(const uint32_t* __restrict__ bits, int64_t bricks, DeviceProgram prog,
-			const uint32_t* __restrict__ tops, uint32_t* counts, uint32_t* total, uint32_t* __restrict__ list)
+		// Descend (with Place = false): the kept bricks' descents are not stored yet; each
+		// thread writes its brick's into tops first, for the placing pass and the evaluation.
+		template<bool Place, bool Descend>
+		__global__ void ListBricksByCostKernel(const uint32_t* __restrict__ bits, int64_t bricks, DeviceProgram prog, GridSpec g,
+			BrickGrid bg, uint32_t* __restrict__ tops, uint32_t* counts, uint32_t* total, uint32_t* __restrict__ list)
 		{
 			const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
 			const int lane = (int)(threadIdx.x & 31);
 			int cls = kCostClasses;           // not kept
-			if (b < bricks && ((__ldg(bits + (b >> 5)) >> (b & 31)) & 1u)) cls = CostClass(prog, __ldg(tops + b));
+			if (b < bricks && ((__ldg(bits + (b >> 5)) >> (b & 31)) & 1u))
+			{
+				uint32_t top;
+				if constexpr (Descend)
+				{
+					const int bx = (int)(b % bg.NBX), by = (int)((b / bg.NBX) % bg.NBY), bz = (int)(b / ((int64_t)bg.NBX * bg.NBY));
+					const int i0 = bx * bg.B, j0 = by * bg.B, k0 = bz * bg.B;
+					top = BrickTop(prog, g, i0, min(i0 + bg.B, g.NX - 1), j0, min(j0 + bg.B, g.NY - 1), k0, min(k0 + bg.B, g.NZ - 1));
+					tops[b] = top;
+				}
+				else
+				{
+					top = __ldg(tops + b);
+				}
+				cls = CostClass(prog, top);
+			}
 			const unsigned peers = __match_any_sync(0xFFFFFFFFu, cls);
 			if (cls == kCostClasses) return;
 			const int leader = __ffs((int)peers) - 1;
@@ -563,18 +580,30 @@ namespace tg
 	}
 
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
-		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog, const uint32_t* tops, uint32_t* class_counts)
+		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog, uint32_t* tops, uint32_t* class_counts, const GridSpec* descend,
+		int B)
 	{
 		const int64_t words = (bricks + 31) / 32;
 		if (words <= 0) return cudaMemsetAsync(count, 0, 4, stream);
 		if (prog && tops && class_counts)
 		{
+			GridSpec g{};
+			BrickGrid bg{};
+			if (descend)
+			{
+				g = *descend;
+				bg = MakeBrickGrid(g, B);
+				if ((int64_t)bg.NBX * bg.NBY * bg.NBZ != bricks) return cudaErrorInvalidValue;
+			}
 			cudaError_t e = cudaMemsetAsync(class_counts, 0, 2 * kCostClasses * sizeof(uint32_t), stream);
 			if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(uint32_t), stream);
 			if (e != cudaSuccess) return e;
 			const unsigned blocks = (unsigned)((bricks + 255) / 256);
-			ListBricksByCostKernel<false><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, tops, class_counts, count, list);
-			ListBricksByCostKernel<true><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, tops, class_counts, count, list);
+			if (descend)
+				ListBricksByCostKernel<false, true><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, g, bg, tops, class_counts, count, list);
+			else
+				ListBricksByCostKernel<false, false><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, g, bg, tops, class_counts, count, list);
+			ListBricksByCostKernel<true, false><<<blocks, 256, 0, stream>>>(brick_bits, bricks, *prog, g, bg, tops, class_counts, count, list);
 			return cudaGetLastError();
 		}
 		cudaError_t e = LaunchExclusiveScan(brick_bits, words, true, base, count, scratch, stream);

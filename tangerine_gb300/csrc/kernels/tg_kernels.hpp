@@ -78,9 +78,11 @@ namespace tg
 	// With the classifier's brick_tops (and `prog`, and eight scratch words in class_counts),
 	// the list is ordered instead by the cost of the bricks' programs, the costliest first,
 	// so that a persistent evaluation does not end on them; base and scratch are then unused.
+	// With `descend` (the export grid, and brick size B), the listing first writes each kept
+	// brick's descent into `tops` itself (bits from a classification that stored none).
 	cudaError_t LaunchListBricks(const uint32_t* brick_bits, int64_t bricks, uint32_t* base, uint32_t* scratch, uint32_t* list,
-		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog = nullptr, const uint32_t* tops = nullptr,
-		uint32_t* class_counts = nullptr);
+		uint32_t* count, cudaStream_t stream, const DeviceProgram* prog = nullptr, uint32_t* tops = nullptr,
+		uint32_t* class_counts = nullptr, const GridSpec* descend = nullptr, int B = 0);
 	// The brick kernels below run persistent grids sized from the SM count (`sms`).
 	// Brick evaluation.  status[0..1], zeroed by the caller: status[0] becomes nonzero if a
 	// staged program copy does not complete in time; status[1] is the warps' work counter.

@@ -156,12 +156,16 @@ def test_full_size_mesh_matches_oracle(lib, port):
     (515^3 lattice points).  Every lattice distance, every vertex (in the reference's serial
     order), cube index, face, normal and colour byte of the GPU's culled export against the
     oracle's surface nets (FirstLoopInnerThunk / SecondLoopThunk, surface_nets.cpp:864-1121)
-    and its per-vertex Gradient + GetMaterial (export.cpp:283-317) on all host cores."""
+    and its per-vertex Gradient + GetMaterial (export.cpp:283-317) on all host cores.  The
+    end-to-end call (tg_export_tree: tree handle in, host mesh out, bricks classified on the
+    root cell's program during the compile) gives the same mesh."""
     spec = W.random_tree(1, 256)
     grid = W.export_grid(resolution=512)
-    with sdf.compile(sdf.from_spec(spec)) as prog:
+    tree = sdf.from_spec(spec)
+    with sdf.compile(tree) as prog:
         m = prog.export_mesh(grid)
         lat = prog.eval_grid(grid)
+    e = sdf.export_tree(tree, (-2, -2, -2), (2, 2, 2), 4.0 / 512)
     h = port.build(spec)
     o = port.octree(h)
     try:
@@ -169,12 +173,14 @@ def test_full_size_mesh_matches_oracle(lib, port):
         del lat
         want = port.surface_nets(o, grid)
         assert want.vertices.shape[0] > 1000000
-        np.testing.assert_array_equal(m.vertices, want.vertices)
-        np.testing.assert_array_equal(m.cubes.astype(np.uint64), want.cubes)
-        np.testing.assert_array_equal(sorted_faces(m.faces), sorted_faces(want.faces))
         normals, colors = port.vertex_attributes(o, want.vertices)
-        np.testing.assert_array_equal(m.normals, normals)
-        np.testing.assert_array_equal(m.colors, colors)
+        for got in (m, e):
+            np.testing.assert_array_equal(got.vertices, want.vertices)
+            np.testing.assert_array_equal(got.cubes.astype(np.uint64), want.cubes)
+            np.testing.assert_array_equal(sorted_faces(got.faces), sorted_faces(want.faces))
+            np.testing.assert_array_equal(got.normals, normals)
+            np.testing.assert_array_equal(got.colors, colors)
+        np.testing.assert_array_equal(e.faces, m.faces)
     finally:
         port.octree_free(o)
         port.free(h)
@@ -212,13 +218,67 @@ def test_culled_export_full_size(lib):
             np.testing.assert_array_equal(a, b)
 
 
-def test_export_tree_matches_program_export(lib):
-    spec = W.random_tree(5, 16, ops=W.OPS_UNIFORM4)
-    grid = W.export_grid(resolution=64)
-    t = sdf.from_spec(spec)
-    a = sdf.export_tree(t, (-2, -2, -2), (2, 2, 2), 4.0 / 64)
+def _spec(which):
+    if isinstance(which, str):
+        return np.load(GOLDEN / f"{which}.npz", allow_pickle=False)["spec"]
+    seed, n, ops = which
+    return W.random_tree(seed, n, **({"ops": ops} if ops is not None else {}))
+
+
+# (tree, lattice min, max, step): trees with blends, stencils and paint, a non-Lipschitz
+# ellipsoid (nothing may be culled), a single brush, the 256-brush workload on a ragged
+# brick grid, and lattices that reach past the root cube on some sides.
+EXPORT_TREE_CASES = [
+    ((5, 16, W.OPS_UNIFORM4), (-2, -2, -2), (2, 2, 2), 4.0 / 64),
+    ((1, 256, None), (-2, -2, -2), (2, 2, 2), 4.0 / 150),
+    ((3, 64, None), (-2.5, -1.0, -2.0), (1.0, 2.5, 2.0), 0.045),
+    ((7, 1, None), (-1.5, -1.5, -1.5), (1.5, 1.5, 1.5), 0.05),
+    ("ellipsoid_cone", (-2, -2, -2), (2, 2, 2), 4.0 / 80),
+    ("stencil_align", (-2, -2, -2), (2, 2, 2), 4.0 / 90),
+    ("scaled_blend", (-2.2, -1.7, -2.0), (1.9, 2.3, 1.6), 0.04),
+    ("coninder_flate_scale", (-2, -2, -2), (2, 2, 2), 4.0 / 70),
+]
+
+
+@pytest.mark.parametrize("case", range(len(EXPORT_TREE_CASES)))
+def test_export_tree_matches_program_export(lib, case):
+    """tg_export_tree classifies the bricks on the root cell's program while the host is
+    still building the octree, and the list pass descends the kept bricks itself: its mesh
+    must be the program export's (holder-cell classification) and the dense export's, bit
+    for bit."""
+    which, lo, hi, step = EXPORT_TREE_CASES[case]
+    t = sdf.from_spec(_spec(which))
+    sdf.profile_enable(True)
+    sdf.profile_reset()
+    try:
+        a = sdf.export_tree(t, lo, hi, step)
+        _, early = sdf.profile_read("classify_root")
+        _, late = sdf.profile_read("classify_bricks")
+    finally:
+        sdf.profile_enable(False)
+    assert (early, late) == (1, 0)
+    grid = sdf.export_grid(lo, hi, step)
     with sdf.compile(t) as prog:
         b = prog.export_mesh(grid)
+        dense = prog.export_mesh(grid, dense=True)
+    assert a.vertices.shape[0] > 0
+    for m in (b, dense):
+        for x, y in ((a.vertices, m.vertices), (a.cubes, m.cubes), (a.faces, m.faces), (a.normals, m.normals),
+                     (a.colors, m.colors)):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_export_tree_of_a_tree_without_octree_then_recovers(lib):
+    """The root is clipped (and its early brick test launched) before the build finds that
+    every octant clips away: the call fails as SDFOctree::Create would, and the next export
+    is whole."""
+    t = sdf.from_spec(W.random_tree(100010, 8))
+    with pytest.raises(_lib.TangerineError):
+        sdf.export_tree(t, (-2, -2, -2), (2, 2, 2), 4.0 / 64)
+    u = sdf.from_spec(W.random_tree(5, 16, ops=W.OPS_UNIFORM4))
+    a = sdf.export_tree(u, (-2, -2, -2), (2, 2, 2), 4.0 / 64)
+    with sdf.compile(u) as prog:
+        b = prog.export_mesh(sdf.export_grid((-2, -2, -2), (2, 2, 2), 4.0 / 64), dense=True)
     for x, y in ((a.vertices, b.vertices), (a.faces, b.faces), (a.normals, b.normals), (a.colors, b.colors)):
         np.testing.assert_array_equal(x, y)
 

@@ -50,6 +50,37 @@ def test_host_octree_matches_reference(lib, golden, name):
     np.testing.assert_array_equal(words, g["octree_words"])
 
 
+@pytest.mark.parametrize("name", golden_names())
+def test_root_program_is_node_zero_program(lib, golden, name):
+    """tg_export_tree runs the exact brick test on the root cell's program as soon as the
+    root is clipped, before the octree below it exists: that program must be the one the
+    finished compile gives node 0 (pivot, clip radius with its non-Lipschitz sign, and
+    every record)."""
+    g = golden[name]
+    t = sdf.from_spec(g["spec"])
+    q, d = C.c_int64(), C.c_int32()
+    st = lib.tg_debug_root_program_check(t.handle, C.byref(q), C.byref(d))
+    if "octree_nodes" not in g:
+        assert st == 2   # TG_ERR_UNBOUNDED: no octree, so no export either
+        return
+    assert st == 0, lib.tg_last_error()
+    assert q.value >= 2 and d.value >= 1
+
+
+@pytest.mark.parametrize("ops", [None, "uniform4"])
+def test_root_program_is_node_zero_program_random_trees(lib, ops):
+    q, d = C.c_int64(), C.c_int32()
+    kw = {} if ops is None else {"ops": W.OPS_UNIFORM4}
+    for seed in range(12):
+        for n in (1, 2, 9, 64, 256):
+            t = sdf.from_spec(W.random_tree(seed, n, **kw))
+            st = lib.tg_debug_root_program_check(t.handle, C.byref(q), C.byref(d))
+            if not sdf.has_export_octree(t):
+                assert st == 2
+                continue
+            assert st == 0, (seed, n, lib.tg_last_error())
+
+
 def test_operators_take_over_operands(lib):
     a = sdf.sphere(0.5)
     b = sdf.box(0.3, 0.3, 0.3).move(0.4, 0, 0)
