@@ -216,6 +216,11 @@ TANGERINE_API tg_status tg_debug_compile_seconds(void* tree, int meshing, double
  * record, node 0's distance program.  TG_OK with the program's quads (stop included) and
  * stack depth; TG_ERR_INVALID with the difference in tg_last_error otherwise. */
 TANGERINE_API tg_status tg_debug_root_program_check(void* tree, int64_t* code_quads, int32_t* stack_size);
+/* Host-only check of tg_export_tree's deferred surface programs: the export tree compiled
+ * whole and compiled with its surface programs left out, then emitted into a separate
+ * image as the export does into its staging buffer, must give the same program image,
+ * node table and header bit for bit.  TG_OK, or TG_ERR_INVALID with the difference. */
+TANGERINE_API tg_status tg_debug_deferred_surfaces_check(void* tree);
 /* Host-only plan of tg_sodapop_mesh: grid gets origin xyz, step xyz, cells xyz, the point
  * cache's limit and the lattice's z layers (11 floats); boxes the leaves' inclusive integer
  * point-cache spans (6 per leaf, up to box_capacity leaves); leaves the leaf count. */

@@ -131,6 +131,7 @@ SIGNATURES = {
     "tg_debug_meshing_octree": (_i64, [_vp, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i64)]),
     "tg_debug_compile_seconds": (_i, [_vp, _i, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "tg_debug_root_program_check": (_i, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "tg_debug_deferred_surfaces_check": (_i, [_vp]),
     "tg_debug_sodapop_plan": (_i, [_vp, _f, _vp, _vp, _i64, C.POINTER(_i64)]),
     "tg_sodapop_mesh": (_i, [_vp, _f, C.POINTER(Drawable), _vp]),
     "tg_export_point_cloud": (_i, [_vp, _vp, _vp, _vp, _i, _u32, C.POINTER(HostMesh), _vp]),

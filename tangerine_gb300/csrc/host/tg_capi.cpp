@@ -538,6 +538,26 @@ extern "C"
 		return TG_OK;
 	}
 
+	TANGERINE_API tg_status tg_debug_deferred_surfaces_check(void* tree)
+	{
+		if (!tree) { SetError("null tree handle"); return TG_ERR_INVALID; }
+		CompiledTree whole, later;
+		std::string err;
+		if (!CompileTree(Borrow(tree), whole, err)) { SetError(err); return TG_ERR_UNBOUNDED; }
+		if (!CompileTree(Borrow(tree), later, err, OctreeKind::Export, nullptr, true)) { SetError(err); return TG_ERR_UNBOUNDED; }
+		if (!later.Pending) { SetError("the deferred compile left nothing pending"); return TG_ERR_INVALID; }
+		std::vector<float> a(whole.CodeFloats), b(later.CodeFloats);
+		whole.CopyCode(a.data());
+		later.CopyCode(b.data());
+		if (!FinishSurfaces(later, b.data(), err)) { SetError(err); return TG_ERR_INVALID; }
+		const bool same = a.size() == b.size() && std::memcmp(a.data(), b.data(), a.size() * sizeof(float)) == 0 &&
+			whole.Nodes.size() == later.Nodes.size() &&
+			std::memcmp(whole.Nodes.data(), later.Nodes.data(), whole.Nodes.size() * sizeof(OctNode)) == 0 &&
+			std::memcmp(&whole.Header, &later.Header, sizeof(ProgramHeader)) == 0;
+		if (!same) { SetError("the image with deferred surface programs differs from the whole compile's"); return TG_ERR_INVALID; }
+		return TG_OK;
+	}
+
 	TANGERINE_API tg_status tg_debug_sodapop_plan(void* tree, float density, float* grid, int64_t* boxes, int64_t box_capacity,
 		int64_t* leaves)
 	{
@@ -727,7 +747,10 @@ extern "C"
 		// below the root and emits its programs.
 		cudaError_t pre = cudaErrorNotReady;
 		const RootHook onRoot = [&](const RootProgram& r) { pre = eng.PreClassify(r, gs, opt.BrickSize, s); };
-		if (!CompileTree(Borrow(tree), prog->Host, err, OctreeKind::Export, opt.Dense ? nullptr : &onRoot))
+		// The surface programs (read by the normal and colour pass only) are left out of the
+		// compile: the export emits them into the staged image while it waits for its
+		// first read-back, and copies the code to the device again before that pass.
+		if (!CompileTree(Borrow(tree), prog->Host, err, OctreeKind::Export, opt.Dense ? nullptr : &onRoot, true))
 		{
 			SetError(err);
 			return TG_ERR_UNBOUNDED;
@@ -739,11 +762,24 @@ extern "C"
 		cudaError_t ue = eng.UploadScratch(*prog, s);
 		if (ue != cudaSuccess) return CudaFail(ue, "uploading the program");
 		const auto t1 = clock();
+		std::string surfaceError;
+		opt.WhileWaiting = [&]() -> cudaError_t
+		{
+			return FinishSurfaces(prog->Host, eng.StagedCode(*prog), surfaceError) ? cudaSuccess : cudaErrorInvalidValue;
+		};
+		opt.RestageCode = true;
 		DeviceMesh dm;
 		HostMeshOut host;
 		opt.Host = &host;
 		const cudaError_t e = eng.Export(*prog, gs, opt, dm, s);
 		const auto t2 = clock();
+		if (!surfaceError.empty())
+		{
+			FreeHostMesh(host);
+			std::memset(out, 0, sizeof *out);
+			SetError(surfaceError);
+			return TG_ERR_INVALID;
+		}
 		st = TakeHostMesh(e, host, out, "exporting the mesh");
 		const auto t3 = clock();
 		tm.CompileSeconds = prog->Host.BuildSeconds;

@@ -175,6 +175,18 @@ namespace tg
 		return cudaSuccess;
 	}
 
+	float* Engine::StagedCode(const Program& p)
+	{
+		return reinterpret_cast<float*>(static_cast<uint8_t*>(Staging) + LayoutOf(p).CodeOff);
+	}
+
+	cudaError_t Engine::RestageCode(const Program& p, cudaStream_t s)
+	{
+		const ProgramLayout l = LayoutOf(p);
+		return cudaMemcpyAsync(static_cast<uint8_t*>(ProgramScratch.Ptr) + l.CodeOff, static_cast<uint8_t*>(Staging) + l.CodeOff,
+			l.CodeBytes, cudaMemcpyHostToDevice, s);
+	}
+
 	// One allocation: nodes (64-byte records), code quads, colour bytes, material RGB.
 	cudaError_t Engine::Upload(Program& p)
 	{
@@ -321,6 +333,13 @@ namespace tg
 		const bool pre = opt.PreClassified && PreValid && !opt.Dense && !opt.Field && PreBrickSize == opt.BrickSize &&
 			std::memcmp(&PreGrid, &g, sizeof(GridSpec)) == 0;
 		PreValid = false;
+		// A code copy RestageCode started reads the staging buffer: whatever way this export
+		// ends, it is over before the next upload rewrites that buffer.
+		struct RestageWait
+		{
+			cudaEvent_t Event = nullptr;
+			~RestageWait() { if (Event) cudaEventSynchronize(Event); }
+		} restaged;
 		out = DeviceMesh();
 		// Asynchronous exports stop at a synchronisation point once cancelled.
 		auto stopped = [&](float done) -> bool
@@ -435,7 +454,18 @@ namespace tg
 		TG_TRY(LaunchExclusiveScan(Words.As<uint32_t>(), words, true, WordBase.As<uint32_t>(), Counts.As<uint32_t>(), Scratch.As<uint32_t>(), s));
 		End(s);
 		TG_TRY(cudaMemcpyAsync(HostCounts, Counts.Ptr, 4, cudaMemcpyDeviceToHost, s));
+		if (opt.WhileWaiting) TG_TRY(opt.WhileWaiting());
 		TG_TRY(cudaStreamSynchronize(s));
+		if (opt.RestageCode)
+		{
+			// The kernels that read distance programs are done; the ones up to the attribute
+			// pass read no program, so the copy runs beside them.
+			if (!CopyStream) TG_TRY(cudaStreamCreateWithFlags(&CopyStream, cudaStreamNonBlocking));
+			if (!CodeReady) TG_TRY(cudaEventCreateWithFlags(&CodeReady, cudaEventDisableTiming));
+			TG_TRY(RestageCode(p, CopyStream));
+			TG_TRY(cudaEventRecord(CodeReady, CopyStream));
+			restaged.Event = CodeReady;
+		}
 		const uint32_t vcount = HostCounts[0];
 		if (!opt.Dense) ActiveBricks = HostCounts[2];
 		if (!opt.Dense && HostCounts[4] != 0)
@@ -537,6 +567,7 @@ namespace tg
 			// grouped by brick, so a warp's vertices mostly share one surface program).
 			VertexOrder order;
 			if (!opt.Dense) order = { ActiveCells.As<uint32_t>(), Words.As<uint32_t>(), WordBase.As<uint32_t>() };
+			if (restaged.Event) TG_TRY(cudaStreamWaitEvent(s, restaged.Event, 0));
 			Begin("attributes", s);
 			TG_TRY(LaunchVertexAttributes(p.View, Vertices.As<float>(), vcount, Normals.As<float>(), colors, s, order));
 			End(s);

@@ -4,6 +4,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -77,6 +78,14 @@ namespace tg
 		// same grid and brick size, same stream): the export lists its bricks and descends
 		// them instead of classifying.
 		bool PreClassified = false;
+		// Host work to run while the export waits for its first count read-back (an error
+		// from it ends the export), and RestageCode: the program's code region is copied to
+		// the device again from the engine's staging buffer once the kernels that read
+		// distance programs are done, and the vertex attribute pass waits for that copy --
+		// for a program uploaded with UploadScratch whose surface programs that host work
+		// wrote into the staged image (FinishSurfaces).
+		std::function<cudaError_t()> WhileWaiting;
+		bool RestageCode = false;
 		HostMeshOut* Host = nullptr;        // also copy the mesh to host memory (see HostMeshOut)
 		// Host-side control of an asynchronous export (MeshExport): when *Active turns false
 		// the export stops at its next synchronisation point, sets *Cancelled and returns an
@@ -129,6 +138,10 @@ namespace tg
 		// Upload into the engine's reusable program buffer, asynchronously on `s` (for a
 		// program used by one call only, such as tg_export_tree's).
 		cudaError_t UploadScratch(Program& p, cudaStream_t s);
+		// The code image UploadScratch last staged for `p` (pinned host memory, quad 0
+		// first), and a copy of that code region to the device again on `s`.
+		float* StagedCode(const Program& p);
+		cudaError_t RestageCode(const Program& p, cudaStream_t s);
 		cudaError_t EvalGrid(const Program& p, const GridSpec& g, float* device_out, cudaStream_t s);
 		cudaError_t EvalPoints(const Program& p, const float* host_points, int64_t n, float* host_out, cudaStream_t s);
 		cudaError_t Export(const Program& p, const GridSpec& g, const ExportOptions& opt, DeviceMesh& out, cudaStream_t s);
@@ -186,6 +199,7 @@ namespace tg
 		cudaStream_t Stream = nullptr;
 		cudaStream_t CopyStream = nullptr;          // early device-to-host copies of an export
 		cudaEvent_t MeshReady = nullptr;
+		cudaEvent_t CodeReady = nullptr;            // RestageCode's copy of an export is done
 		DeviceBuffer LatticeBuf, Words, WordBase, Scratch, Counts, Vertices, Cubes, FaceCounts, FaceBase, Faces, Normals, Colors;
 		DeviceBuffer Points, PointOut, BrickBits, BrickList, BrickTops, ClassCounts, ProgramScratch, ActiveCells;
 		DeviceBuffer RayIn, RayOut, Cameras, Image, RenderCounters;

@@ -409,8 +409,10 @@ namespace tg
 				const Node* Key;
 				int32_t Record;     // -1: not built
 				int8_t Paint;       // -1: not known
+				int32_t SurfQuads;  // -1: not known; else the surface program's quads
+				int32_t SurfPeak;   // and the stack depth it reaches
 			};
-			NodeFacts() { Slots.assign(1024, Entry{ nullptr, -1, -1 }); }
+			NodeFacts() { Slots.assign(1024, Entry{ nullptr, -1, -1, -1, 0 }); }
 			// The entry of n, or null (no insertion).
 			const Entry* Find(const Node* n) const
 			{
@@ -434,7 +436,7 @@ namespace tg
 					if (e.Key == n) return e;
 					if (!e.Key)
 					{
-						e = Entry{ n, -1, -1 };
+						e = Entry{ n, -1, -1, -1, 0 };
 						++Size;
 						return e;
 					}
@@ -455,7 +457,7 @@ namespace tg
 			{
 				std::vector<Entry> old;
 				old.swap(Slots);
-				Slots.assign(old.size() * 2, Entry{ nullptr, -1, -1 });
+				Slots.assign(old.size() * 2, Entry{ nullptr, -1, -1, -1, 0 });
 				Size = 0;
 				for (const Entry& e : old)
 				{
@@ -463,6 +465,8 @@ namespace tg
 					Entry& n = At(e.Key);
 					n.Record = e.Record;
 					n.Paint = e.Paint;
+					n.SurfQuads = e.SurfQuads;
+					n.SurfPeak = e.SurfPeak;
 				}
 			}
 			std::vector<Entry> Slots;
@@ -532,10 +536,9 @@ namespace tg
 
 			// Records of one brush: [distance quads, surface quads], built once per emitter
 			// (or taken from the shared emitter's arena).
-			void AppendRecords(const Node& n, bool surface)
+			// The arena holding a brush's records and their spans there.
+			void SpansOf(const Node& n, const float*& arena, const RecordSpans*& sp)
 			{
-				const float* arena;
-				const RecordSpans* sp;
 				const NodeFacts::Entry* shared = Shared ? Shared->Facts.Find(&n) : nullptr;
 				if (shared && shared->Record >= 0)
 				{
@@ -548,6 +551,13 @@ namespace tg
 					arena = Arena.data();
 					sp = &Spans[(size_t)r];
 				}
+			}
+
+			void AppendRecords(const Node& n, bool surface)
+			{
+				const float* arena;
+				const RecordSpans* sp;
+				SpansOf(n, arena, sp);
 				const float* from = arena + (surface ? sp->SurfaceAt : sp->DistanceAt);
 				(surface ? LastSurfaceBrushAt : LastBrushAt) = Code.size();
 				Code.insert(Code.end(), from, from + (surface ? sp->SurfaceFloats : sp->DistanceFloats));
@@ -613,71 +623,136 @@ namespace tg
 			}
 
 			// Distance program: Tangerine's postfix program with each brush's transform,
-			// primitive and field scale fused into one record.
-			void Distance(const Node& n)
+			// primitive and field scale fused into one record.  Returns the deepest stack the
+			// program reaches (accumulator + spilled operands) counting every brush as a push,
+			// fused or not: a set holds its left operand while its right one runs.
+			int Distance(const Node& n)
 			{
 				switch (n.Kind)
 				{
 				case NodeKind::Brush:
 					if (n.Op == OpEllipsoid) NonLipschitz = true;
 					AppendRecords(n, false);
-					break;
+					return 1;
 				case NodeKind::Set:
-					Distance(*n.Lhs);
-					Distance(*n.Rhs);
+				{
+					const int l = Distance(*n.Lhs);
+					const int r = Distance(*n.Rhs);
 					// A brush right operand (the usual case: the tree leans left) is combined
 					// with the left operand in the brush's own step, without a stack push.
 					if (n.Rhs->Kind == NodeKind::Brush)
 						Code[LastBrushAt] = BitsFloat(FloatBits(Code[LastBrushAt]) | RecThenSet);
 					Quad(n.Op, IsBlendOp(n.Op) ? n.Threshold : 0.0f, 0.0f, 0.0f);
-					break;
+					return l > r + 1 ? l : r + 1;
+				}
 				case NodeKind::Flate:
-					Distance(*n.Lhs);
+				{
+					const int d = Distance(*n.Lhs);
 					Quad(OpFlate, n.Threshold, 0.0f, 0.0f);
-					break;
+					return d;
+				}
 				case NodeKind::Stencil:
-					Distance(*n.Lhs);
+					return Distance(*n.Lhs);
+				}
+				return 0;
+			}
+
+			// The quads Surface(n) emits and the deepest stack its program reaches (every
+			// brush a push, every set and stencil end a pop), without emitting it: both depend
+			// on the subtree alone, so they are kept per node (the shared emitter's table first).
+			void SurfaceSize(const Node& n, int& quads, int& peak)
+			{
+				const NodeFacts::Entry* known = Shared ? Shared->Facts.Find(&n) : nullptr;
+				if (!(known && known->SurfQuads >= 0)) known = Facts.Find(&n);
+				if (known && known->SurfQuads >= 0)
+				{
+					quads = known->SurfQuads;
+					peak = known->SurfPeak;
+					return;
+				}
+				int q = 0, p = 0;
+				switch (n.Kind)
+				{
+				case NodeKind::Brush:
+				{
+					const float* arena;
+					const RecordSpans* sp;
+					SpansOf(n, arena, sp);
+					q = sp->SurfaceFloats / 4;
+					p = 1;
 					break;
 				}
+				case NodeKind::Set:
+				{
+					int ql, pl, qr, pr;
+					SurfaceSize(*n.Lhs, ql, pl);
+					SurfaceSize(*n.Rhs, qr, pr);
+					q = ql + qr + 1;
+					p = pl > pr + 1 ? pl : pr + 1;
+					break;
+				}
+				case NodeKind::Flate:
+					SurfaceSize(*n.Lhs, q, p);
+					q += 1;
+					break;
+				case NodeKind::Stencil:
+				{
+					int ql, pl, qm, pm;
+					SurfaceSize(*n.Lhs, ql, pl);
+					SurfaceSize(*n.Mask, qm, pm);
+					q = ql + 1 + qm + 1;
+					p = pl > pm + 1 ? pl : pm + 1;
+					break;
+				}
+				}
+				NodeFacts::Entry& e = Facts.At(&n);
+				e.SurfQuads = q;
+				e.SurfPeak = p;
+				quads = q;
+				peak = p;
 			}
 
 			// Surface program: the subtree as SDFNode::Eval / GetMaterial walk it.
-			void Surface(const Node& n)
+			// Returns the deepest stack the program reaches, counted as SurfaceSize counts it.
+			int Surface(const Node& n)
 			{
 				switch (n.Kind)
 				{
 				case NodeKind::Brush:
 					AppendRecords(n, true);
-					break;
+					return 1;
 				case NodeKind::Set:
 				{
-					Surface(*n.Lhs);
-					Surface(*n.Rhs);
+					const int l = Surface(*n.Lhs);
+					const int r = Surface(*n.Rhs);
 					uint32_t flags = 0;
 					if (HasPaint(*n.Lhs)) flags |= RecLhsPaint;
 					if (HasPaint(*n.Rhs)) flags |= RecRhsPaint;
 					if (n.Rhs->Kind == NodeKind::Brush)
 						Code[LastSurfaceBrushAt] = BitsFloat(FloatBits(Code[LastSurfaceBrushAt]) | RecThenSet);
 					Quad(n.Op | flags, n.Threshold, 0.0f, 0.0f);
-					break;
+					return l > r + 1 ? l : r + 1;
 				}
 				case NodeKind::Flate:
-					Surface(*n.Lhs);
+				{
+					const int d = Surface(*n.Lhs);
 					Quad(OpFlate, n.Threshold, 0.0f, 0.0f);
-					break;
+					return d;
+				}
 				case NodeKind::Stencil:
 				{
-					Surface(*n.Lhs);
+					const int l = Surface(*n.Lhs);
 					const size_t begin = Code.size();
 					Quad(OpMaskBegin, 0.0f, 0.0f, 0.0f);
-					Surface(*n.Mask);
+					const int m = Surface(*n.Mask);
 					Quad(OpStencilEnd | (n.Negative ? RecNegative : 0u), BitsFloat((uint32_t)MaterialIndex(n.Mat.get())), 0.0f, 0.0f);
 					// Quads to skip after the MaskBegin record when only distances are needed.
 					const int skip = (int)((Code.size() - begin) / 4) - 1;
 					Code[begin + 1] = BitsFloat((uint32_t)skip);
-					break;
+					return l > m + 1 ? l : m + 1;
 				}
 				}
+				return 0;
 			}
 		};
 
@@ -702,45 +777,6 @@ namespace tg
 			}
 		}
 
-		// Deepest stack a record program reaches (accumulator + spilled operands).
-		int ProgramDepth(const float* code, int start)
-		{
-			int depth = 0, peak = 0;
-			for (int q = start;; )
-			{
-				const uint32_t head = FloatBits(code[q * 4]);
-				const uint32_t op = head & 0xFFu;
-				if (op == OpStop) break;
-				if (IsBrushOp(op))
-				{
-					++depth;
-					if (depth > peak) peak = depth;
-					int extra = 0;
-					if (head & RecMatrix) extra += 3;
-					if (head & RecOffset) extra += 1;
-					if (head & RecScale) extra += 1;
-					q += 1 + extra;
-				}
-				else if (IsSetOp(op)) { --depth; q += 1; }
-				else if (op == OpStencilEnd) { --depth; q += 1; }
-				else { q += 1; }
-			}
-			return peak;
-		}
-
-		int SurfaceDepth(const float* code, int start)
-		{
-			int depth = 0, peak = 0;
-			for (int q = start;; )
-			{
-				const uint32_t op = FloatBits(code[q * 4]) & 0xFFu;
-				if (op == OpStop) break;
-				if (IsBrushOp(op)) { ++depth; if (depth > peak) peak = depth; q += 4; }
-				else if (IsSetOp(op) || op == OpStencilEnd) { --depth; q += 1; }
-				else q += 1;
-			}
-			return peak;
-		}
 	}
 
 	// Ellipsoid distances are a bound estimate, not 1-Lipschitz; every other primitive and
@@ -777,7 +813,68 @@ namespace tg
 		else for (size_t i = 0; i < CodeChunks.size(); ++i) copy((int)i);
 	}
 
-	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind, const RootHook* on_root)
+	// What FinishSurfaces needs: the trees (the full tree and, through the octree's cells,
+	// every distinct evaluator), the brush records, and where each surface program goes.
+	// Dropping it hands the octree's clipped trees to the background thread.
+	struct DeferredSurfaces
+	{
+		NodeRef Root;
+		std::shared_ptr<std::vector<Octree::Cell>> Cells;
+		std::unordered_map<const Material*, int> Materials;
+		std::vector<float> Unused;
+		std::unique_ptr<Emitter> Shared;
+		std::vector<const Node*> Items;     // the distinct evaluators, then the full tree
+		std::vector<int> SurfaceAt;         // each item's surface program: first quad in the image
+		std::vector<int> SurfaceQuads;      // and its quads, stop included
+		std::vector<int> ChunkFirst;        // first item of each emission chunk (chunks + 1)
+		std::vector<int> ChunkBase;         // first quad of each chunk in the image
+		~DeferredSurfaces()
+		{
+			Shared.reset();
+			if (Cells)
+			{
+				auto cells = std::move(Cells);
+				WorkerPool::Get().Later([cells]() { cells->clear(); });
+			}
+		}
+	};
+
+	bool FinishSurfaces(CompiledTree& t, float* image, std::string& error)
+	{
+		std::shared_ptr<DeferredSurfaces> ds = std::move(t.Pending);
+		if (!ds) return true;
+		const int chunks = (int)ds->ChunkFirst.size() - 1;
+		std::atomic<bool> ok{ true };
+		WorkerPool::Get().ParallelFor(chunks, [&](int ch)
+		{
+			std::vector<float> code;
+			code.reserve(1 << 12);
+			Emitter em(code, ds->Materials, ds->Shared.get());
+			float* dst = image ? image : t.CodeChunks[(size_t)ch + 1].data();
+			const int base = image ? 0 : ds->ChunkBase[(size_t)ch];
+			for (int u = ds->ChunkFirst[(size_t)ch]; u < ds->ChunkFirst[(size_t)ch + 1]; ++u)
+			{
+				code.clear();
+				em.Surface(*ds->Items[(size_t)u]);
+				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				if (code.size() != (size_t)ds->SurfaceQuads[(size_t)u] * 4)
+				{
+					ok.store(false);
+					continue;
+				}
+				std::memcpy(dst + (size_t)(ds->SurfaceAt[(size_t)u] - base) * 4, code.data(), code.size() * sizeof(float));
+			}
+		});
+		if (!ok.load())
+		{
+			error = "a surface program's size differs from its laid-out size";
+			return false;
+		}
+		return true;
+	}
+
+	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind, const RootHook* on_root,
+		bool defer_surfaces)
 	{
 		const auto t0 = std::chrono::steady_clock::now();
 		if (!root)
@@ -785,14 +882,21 @@ namespace tg
 			error = "the tree has infinite or empty bounds (SDFOctree::Create would return null)";
 			return false;
 		}
-		std::unordered_map<const Material*, int> materials;
+		auto ds = std::make_shared<DeferredSurfaces>();
+		ds->Root = root;
 		std::vector<const Material*> materialList;
-		CollectMaterials(*root, materials, materialList);
+		CollectMaterials(*root, ds->Materials, materialList);
 		// Every brush of the full tree (clipped trees share them) gets its records once, up
-		// front; the emitters only copy spans of them.
-		std::vector<float> unused;
-		Emitter shared(unused, materials);
+		// front, and every node of it its surface program's size; the emitters only copy
+		// spans of the records.
+		ds->Shared.reset(new Emitter(ds->Unused, ds->Materials));
+		Emitter& shared = *ds->Shared;
 		shared.BuildAllRecords(*root);
+		if (defer_surfaces)
+		{
+			int q, pk;
+			shared.SurfaceSize(*root, q, pk);
+		}
 		// The root cell's program, emitted as the programs below emit node 0's.
 		Octree::RootSeen rootSeen;
 		if (on_root && *on_root && kind == OctreeKind::Export)
@@ -800,10 +904,9 @@ namespace tg
 			rootSeen = [&](const Vec3& pivot, float radius, const NodeRef& evaluator)
 			{
 				RootProgram rp;
-				Emitter em(rp.Code, materials, &shared);
-				em.Distance(*evaluator);
+				Emitter em(rp.Code, ds->Materials, &shared);
+				const int depth = em.Distance(*evaluator);
 				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-				const int depth = ProgramDepth(rp.Code.data(), 0);
 				if (depth > kMaxStack) return;   // the compile fails on it below
 				OctNode& n = rp.Node;
 				n.Pivot[0] = pivot.x; n.Pivot[1] = pivot.y; n.Pivot[2] = pivot.z;
@@ -828,13 +931,15 @@ namespace tg
 		out.OctreeSeconds = std::chrono::duration<double>(t1 - ta).count();
 		out.Bounds = root->Bounds();
 		out.OctreeBounds = octree.Cells[0].Bounds;
-		// Each distinct evaluator's two programs are emitted once (cells whose clip left the
+		// Each distinct evaluator's two programs are laid out once (cells whose clip left the
 		// parent's subtree untouched share its node, RebuildSet), in parallel over chunks of
 		// the distinct evaluators, each chunk into its own buffer with its own emitter; the
 		// buffers are then laid end to end in chunk order, so the layout does not depend on
-		// the threads' timing.
+		// the threads' timing.  A chunk holds, per evaluator, its distance program and stop,
+		// then its surface program and stop; with defer_surfaces the surface program's place
+		// is only sized and zero-filled here, and FinishSurfaces emits it.
 		struct EmittedPrograms { int Distance, Surface, Stack; bool NonLipschitz; };
-		std::vector<const Node*> distinct;
+		std::vector<const Node*>& distinct = ds->Items;
 		std::vector<int> programOf(octree.Cells.size(), -1);
 		{
 			// Open addressing on the node address, first appearance order.
@@ -856,36 +961,49 @@ namespace tg
 			}
 		}
 		// The last item is the whole tree's surface program, for SDFNode::RayMarch / Eval.
-		const size_t items = distinct.size() + 1;
+		const size_t evaluators = distinct.size();
+		distinct.push_back(root.get());
+		const size_t items = distinct.size();
 		const int chunkCount = (int)std::min<size_t>(items, (size_t)WorkerPool::Get().Workers() * 4 + 4);
 		std::vector<std::vector<float>> chunkCode((size_t)chunkCount);
 		std::vector<EmittedPrograms> programs(items);
-		auto chunkBegin = [&](int ch) { return (size_t)((uint64_t)items * (uint64_t)ch / (uint64_t)chunkCount); };
+		ds->SurfaceQuads.assign(items, 0);
+		ds->ChunkFirst.resize((size_t)chunkCount + 1);
+		for (int ch = 0; ch <= chunkCount; ++ch) ds->ChunkFirst[(size_t)ch] = (int)((uint64_t)items * (uint64_t)ch / (uint64_t)chunkCount);
 		WorkerPool::Get().ParallelFor(chunkCount, [&](int ch)
 		{
 			std::vector<float>& code = chunkCode[(size_t)ch];
 			code.reserve(1 << 14);
-			Emitter em(code, materials, &shared);
-			for (size_t u = chunkBegin(ch); u < chunkBegin(ch + 1); ++u)
+			Emitter em(code, ds->Materials, &shared);
+			for (int u = ds->ChunkFirst[(size_t)ch]; u < ds->ChunkFirst[(size_t)ch + 1]; ++u)
 			{
-				if (u == distinct.size())
-				{
-					const int surf = (int)(code.size() / 4);
-					em.Surface(*root);
-					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-					programs[u] = EmittedPrograms{ surf, surf, SurfaceDepth(code.data(), surf), false };
-					continue;
-				}
+				const Node& n = *distinct[(size_t)u];
+				int d1 = 0;
+				bool nonLipschitz = false;
 				const int dist = (int)(code.size() / 4);
-				em.NonLipschitz = false;
-				em.Distance(*distinct[u]);
-				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+				if ((size_t)u != evaluators)
+				{
+					em.NonLipschitz = false;
+					d1 = em.Distance(n);
+					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+					nonLipschitz = em.NonLipschitz;
+				}
 				const int surf = (int)(code.size() / 4);
-				em.Surface(*distinct[u]);
-				em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
-				const int d1 = ProgramDepth(code.data(), dist);
-				const int d2 = SurfaceDepth(code.data(), surf);
-				programs[u] = EmittedPrograms{ dist, surf, d1 > d2 ? d1 : d2, em.NonLipschitz };
+				int quads, peak;
+				if (defer_surfaces)
+				{
+					em.SurfaceSize(n, quads, peak);
+					code.resize(code.size() + (size_t)(quads + 1) * 4, 0.0f);
+				}
+				else
+				{
+					peak = em.Surface(n);
+					em.Quad(OpStop, 0.0f, 0.0f, 0.0f);
+					quads = (int)(code.size() / 4) - surf - 1;
+				}
+				programs[(size_t)u] = (size_t)u == evaluators ? EmittedPrograms{ surf, surf, peak, false }
+					: EmittedPrograms{ dist, surf, d1 > peak ? d1 : peak, nonLipschitz };
+				ds->SurfaceQuads[(size_t)u] = quads + 1;
 			}
 		});
 		// One stop record first (the programs of cells without an evaluator), then the
@@ -894,13 +1012,17 @@ namespace tg
 		out.CodeChunks.push_back({ BitsFloat(OpStop), 0.0f, 0.0f, 0.0f });
 		out.CodeFloats = 4;
 		const int stopQuad = 0;
+		ds->ChunkBase.resize((size_t)chunkCount);
+		ds->SurfaceAt.resize(items);
 		for (int ch = 0; ch < chunkCount; ++ch)
 		{
 			const int base = (int)(out.CodeFloats / 4);
-			for (size_t u = chunkBegin(ch); u < chunkBegin(ch + 1); ++u)
+			ds->ChunkBase[(size_t)ch] = base;
+			for (int u = ds->ChunkFirst[(size_t)ch]; u < ds->ChunkFirst[(size_t)ch + 1]; ++u)
 			{
-				programs[u].Distance += base;
-				programs[u].Surface += base;
+				programs[(size_t)u].Distance += base;
+				programs[(size_t)u].Surface += base;
+				ds->SurfaceAt[(size_t)u] = programs[(size_t)u].Surface;
 			}
 			out.CodeFloats += chunkCode[(size_t)ch].size();
 			out.CodeChunks.push_back(std::move(chunkCode[(size_t)ch]));
@@ -933,8 +1055,8 @@ namespace tg
 			if (n.StackSize > maxStack) maxStack = n.StackSize;
 			out.DistanceQuadsTotal += e.Surface - e.Distance;
 		}
-		const int full = programs[distinct.size()].Surface;
-		if (programs[distinct.size()].Stack > maxStack) maxStack = programs[distinct.size()].Stack;
+		const int full = programs[evaluators].Surface;
+		if (programs[evaluators].Stack > maxStack) maxStack = programs[evaluators].Stack;
 		out.Header.FullSurfaceCode = full;
 		out.Header.Lipschitz = HasNonLipschitzBrush(*root) ? 0 : 1;
 		if (maxStack > kMaxStack)
@@ -964,12 +1086,12 @@ namespace tg
 		out.Header.MaterialCount = (int32_t)materialList.size();
 		out.Header.HasPaint = octree.Cells[0].Evaluator->HasPaint() ? 1 : 0;
 		out.Header.MaxStack = maxStack;
-		out.BuildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 		// Releasing thousands of clipped subtrees takes about a millisecond; the caller does
 		// not need to wait for it (it touches only the nodes the clips made: the rest are
-		// borrowed, and counts are atomic).
-		auto cells = std::make_shared<std::vector<Octree::Cell>>(std::move(octree.Cells));
-		WorkerPool::Get().Later([cells]() { cells->clear(); });
+		// borrowed, and counts are atomic).  They go once the surface programs are emitted.
+		ds->Cells = std::make_shared<std::vector<Octree::Cell>>(std::move(octree.Cells));
+		if (defer_surfaces) out.Pending = std::move(ds);
+		out.BuildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 		return true;
 	}
 }

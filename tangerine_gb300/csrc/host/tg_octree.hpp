@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -50,6 +51,8 @@ namespace tg
 	std::vector<uint32_t> CompileReferenceWords(const Node& tree);
 	bool HasNonLipschitzBrush(const Node& tree);
 
+	struct DeferredSurfaces;   // what a compile needs to emit the surface programs later
+
 	struct CompiledTree
 	{
 		ProgramHeader Header{};
@@ -59,6 +62,10 @@ namespace tg
 		std::vector<std::vector<float>> CodeChunks;
 		size_t CodeFloats = 0;
 		void CopyCode(float* dst) const;
+		// Set while the surface programs are still to be emitted (a compile that deferred
+		// them): their places in the image are laid out and zero-filled, every offset,
+		// stack size and the distance programs are final (FinishSurfaces).
+		std::shared_ptr<DeferredSurfaces> Pending;
 		std::vector<uint8_t> Colors;      // 4 bytes per material
 		std::vector<float> MaterialRgb;   // 4 floats per material: stored RGB, 1
 		AABB Bounds{};                    // root evaluator bounds
@@ -87,7 +94,15 @@ namespace tg
 	// Builds the octree of the given kind (Export: target 0.25 with coalescing, as the
 	// export and the point queries use; Meshing: Octree::BuildMeshing) and compiles every
 	// cell's clipped subtree.  `on_root` (Export only) is called on the compiling thread
-	// with the root cell's program as soon as the root is clipped.
+	// with the root cell's program as soon as the root is clipped.  `defer_surfaces`: the
+	// surface programs (read only by the per-vertex normal and colour pass and by queries
+	// of the surface) are laid out but left for FinishSurfaces.
 	bool CompileTree(const NodeRef& root, CompiledTree& out, std::string& error, OctreeKind kind = OctreeKind::Export,
-		const RootHook* on_root = nullptr);
+		const RootHook* on_root = nullptr, bool defer_surfaces = false);
+	// Emits the surface programs a deferred compile left out, on the worker pool, into
+	// `image` (the whole code image as CopyCode lays it out: quad 0 first) or, with
+	// image == nullptr, into CodeChunks.  Only the surface programs' places are written.
+	// No-op when nothing is pending; false (with `error`) if a program's size is not the
+	// one laid out.
+	bool FinishSurfaces(CompiledTree& t, float* image, std::string& error);
 }

@@ -67,6 +67,29 @@ def test_root_program_is_node_zero_program(lib, golden, name):
     assert q.value >= 2 and d.value >= 1
 
 
+@pytest.mark.parametrize("name", golden_names())
+def test_deferred_surface_programs_give_the_whole_image(lib, golden, name):
+    """tg_export_tree compiles without the surface programs, uploads, and emits them into
+    the staged image while the GPU runs the first stages; the finished image must be the
+    whole compile's, record for record."""
+    g = golden[name]
+    t = sdf.from_spec(g["spec"])
+    st = lib.tg_debug_deferred_surfaces_check(t.handle)
+    if "octree_nodes" not in g:
+        assert st == 2
+        return
+    assert st == 0, lib.tg_last_error()
+
+
+def test_deferred_surface_programs_random_trees(lib):
+    for ops in (None, W.OPS_UNIFORM4):
+        for seed in range(10):
+            for n in (1, 3, 17, 96, 256):
+                t = sdf.from_spec(W.random_tree(seed, n, **({} if ops is None else {"ops": ops})))
+                st = lib.tg_debug_deferred_surfaces_check(t.handle)
+                assert st == (0 if sdf.has_export_octree(t) else 2), (seed, n, lib.tg_last_error())
+
+
 @pytest.mark.parametrize("ops", [None, "uniform4"])
 def test_root_program_is_node_zero_program_random_trees(lib, ops):
     q, d = C.c_int64(), C.c_int32()
