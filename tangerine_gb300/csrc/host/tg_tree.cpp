@@ -265,13 +265,6 @@ namespace tg
 		thread_local std::vector<Evaluations8::Slot> Evaluations8::Table;
 		thread_local uint32_t Evaluations8::Epoch = 0;
 
-		struct LaneOf8
-		{
-			Evaluations8& E;
-			int Lane;
-			float At(const Node& n) { const uint32_t i = E.Index(n); return E.Values[8 * i + Lane]; }
-		};
-
 		// The clip works on plain pointers: an untouched subtree is the input node itself, and
 		// only rebuilt nodes are allocated, kept alive in `keep` until the caller holds the
 		// result.  Reference counts (atomics on nodes that every thread's clips share) are
@@ -363,6 +356,104 @@ namespace tg
 			}
 			return nullptr;
 		}
+
+		// ClipAt for the eight spheres of an Evaluations8 at once: out[i] for each lane i set
+		// in `lanes` (the other entries are left alone).  Every lane takes the branches and
+		// rebuilds the nodes its own ClipAt would, in the same order of operands; the tree is
+		// walked once for all of them, and each node's eight values are looked up once per
+		// visit instead of once per lane.
+		void ClipAt8(const Node& n, const float (&radius)[8], uint32_t lanes, const Node* (&out)[8], Evaluations8& ev,
+			ClipScratch& cs)
+		{
+			float v[8];
+			if (n.Kind != NodeKind::Stencil)
+			{
+				const uint32_t at = ev.Index(n);
+				for (int i = 0; i < 8; ++i) v[i] = ev.Values[8 * (size_t)at + (size_t)i];
+			}
+			switch (n.Kind)
+			{
+			case NodeKind::Brush:
+				for (int i = 0; i < 8; ++i)
+					if ((lanes >> i) & 1u) out[i] = v[i] <= radius[i] ? &n : nullptr;
+				return;
+			case NodeKind::Stencil:
+			{
+				const Node* child[8];
+				ClipAt8(*n.Lhs, radius, lanes, child, ev, cs);
+				for (int i = 0; i < 8; ++i)
+				{
+					if (!((lanes >> i) & 1u)) continue;
+					out[i] = child[i] ? cs.Hold(SDF::Stencil(cs.Ref(child[i]), cs.BorrowInputs ? NodeRef::Borrow(n.Mask.get()) : n.Mask,
+						n.Mat, n.Negative)) : nullptr;
+				}
+				return;
+			}
+			case NodeKind::Flate:
+			{
+				uint32_t live = 0;
+				float wide[8];
+				for (int i = 0; i < 8; ++i)
+				{
+					wide[i] = radius[i];
+					if (!((lanes >> i) & 1u)) continue;
+					if (v[i] <= radius[i]) { live |= 1u << i; wide[i] = radius[i] + n.Threshold; }
+					else out[i] = nullptr;
+				}
+				if (!live) return;
+				const Node* child[8];
+				ClipAt8(*n.Lhs, wide, live, child, ev, cs);
+				for (int i = 0; i < 8; ++i)
+					if ((live >> i) & 1u) out[i] = child[i] ? cs.Hold(SDF::Flate(cs.Ref(child[i]), n.Threshold)) : nullptr;
+				return;
+			}
+			case NodeKind::Set:
+			{
+				uint32_t live = 0;
+				for (int i = 0; i < 8; ++i)
+				{
+					if (!((lanes >> i) & 1u)) continue;
+					if (v[i] <= radius[i]) live |= 1u << i;
+					else out[i] = nullptr;
+				}
+				if (!live) return;
+				const bool unionFamily = (n.Op == OpUnion || n.Op == OpBlendUnion);
+				const bool diffFamily = (n.Op == OpDiff || n.Op == OpBlendDiff);
+				uint32_t plain = live;     // lanes that go on to the clip at their own radius
+				if (IsBlendOp(n.Op))
+				{
+					float wide[8];
+					for (int i = 0; i < 8; ++i) wide[i] = radius[i] + n.Threshold;
+					const Node* l[8];
+					const Node* r[8];
+					ClipAt8(*n.Lhs, wide, live, l, ev, cs);
+					ClipAt8(*n.Rhs, wide, live, r, ev, cs);
+					plain = 0;
+					for (int i = 0; i < 8; ++i)
+					{
+						if (!((live >> i) & 1u)) continue;
+						if (l[i] && r[i]) out[i] = RebuildSet(n, l[i], r[i], cs);
+						else if (!unionFamily && !diffFamily) out[i] = nullptr;
+						else plain |= 1u << i;
+					}
+					if (!plain) return;
+				}
+				const Node* l[8];
+				const Node* r[8];
+				ClipAt8(*n.Lhs, radius, plain, l, ev, cs);
+				ClipAt8(*n.Rhs, radius, plain, r, ev, cs);
+				for (int i = 0; i < 8; ++i)
+				{
+					if (!((plain >> i) & 1u)) continue;
+					if (l[i] && r[i]) out[i] = RebuildSet(n, l[i], r[i], cs);
+					else if (unionFamily) out[i] = l[i] ? l[i] : r[i];
+					else if (diffFamily) out[i] = l[i];
+					else out[i] = nullptr;
+				}
+				return;
+			}
+			}
+		}
 	}
 
 	NodeRef Node::Clip(Vec3 p, float radius, bool borrow) const
@@ -377,12 +468,9 @@ namespace tg
 	{
 		Evaluations8 ev(p);
 		ClipScratch cs(borrow);
-		for (int i = 0; i < 8; ++i)
-		{
-			LaneOf8 lane{ ev, i };
-			const Node* r = ClipAt(*this, radius[i], lane, cs);
-			out[i] = r ? cs.Ref(r) : NodeRef();
-		}
+		const Node* r[8];
+		ClipAt8(*this, radius, 0xFFu, r, ev, cs);
+		for (int i = 0; i < 8; ++i) out[i] = r[i] ? cs.Ref(r[i]) : NodeRef();
 	}
 
 	AABB Node::Bounds() const { return BoundsImpl(false); }
