@@ -201,17 +201,8 @@ namespace tg
 				expanded.push_back(std::move(parents));
 				++depth;
 			}
-			// The cells of one depth finish independently (each reads only its own children).
-			WorkerPool& pool = WorkerPool::Get();
 			for (size_t d = expanded.size(); d-- > 0;)
-			{
-				const std::vector<TmpCell*>& cells = expanded[d];
-				const int cellDepth = top_depth + (int)d;
-				if ((int)cells.size() >= 2 * pool.Workers())
-					pool.ParallelFor((int)cells.size(), [&](int j) { FinishCell(*cells[(size_t)j], bp, cellDepth); });
-				else
-					for (TmpCell* c : cells) FinishCell(*c, bp, cellDepth);
-			}
+				for (TmpCell* c : expanded[d]) FinishCell(*c, bp, top_depth + (int)d);
 		}
 
 		// SDFOctree::Walk's incomplete search (sodapop.cpp:108-124): cells that were never
@@ -236,59 +227,31 @@ namespace tg
 			return n;
 		}
 
-		void FillCell(TmpCell& t, Octree::Cell& c)
+		void Flatten(TmpCell& t, std::vector<Octree::Cell>& out)
 		{
-			c.Bounds = t.Bounds;
-			c.Pivot = t.Pivot;
-			c.ClipRadius = t.Radius;
-			c.NullOctants = t.NullOctants;
-			c.Terminus = t.Terminus;
-			c.Incomplete = t.Incomplete;
-			c.EvaluatorLeaves = t.Leaves;
-			c.Evaluator = std::move(t.Eval);   // the build is done with it
-		}
-
-		// Writes t's subtree depth first from out[at] on (out already sized) and returns the
-		// index after it.
-		int FlattenAt(TmpCell& t, int at, std::vector<Octree::Cell>& out)
-		{
-			Octree::Cell& c = out[(size_t)at];
-			FillCell(t, c);
-			int next = at + 1;
-			if (t.Terminus) return next;
+			const int index = (int)out.size();
+			out.emplace_back();
+			{
+				Octree::Cell& c = out.back();
+				c.Bounds = t.Bounds;
+				c.Pivot = t.Pivot;
+				c.ClipRadius = t.Radius;
+				c.NullOctants = t.NullOctants;
+				c.Terminus = t.Terminus;
+				c.Incomplete = t.Incomplete;
+				c.EvaluatorLeaves = t.Leaves;
+				c.Evaluator = std::move(t.Eval);   // the build is done with it
+			}
+			if (t.Terminus) return;
 			for (int i = 0; i < 8; ++i)
 			{
 				if (t.Kids[i])
 				{
-					c.Children[i] = next;
-					next = FlattenAt(*t.Kids[i], next, out);
+					const int child = (int)out.size();
+					Flatten(*t.Kids[i], out);
+					out[index].Children[i] = child;
 				}
 			}
-			return next;
-		}
-
-		// The cells depth first, root first: each of the root's octant subtrees is written
-		// into its own range (known from the subtrees' sizes), the eight in parallel.
-		void Flatten(TmpCell& top, std::vector<Octree::Cell>& out)
-		{
-			int starts[8];
-			size_t total = 1;
-			for (int i = 0; i < 8; ++i)
-			{
-				starts[i] = -1;
-				if (top.Terminus || !top.Kids[i]) continue;
-				starts[i] = (int)total;
-				total += CountCells(*top.Kids[i]);
-			}
-			out.clear();
-			out.resize(total);
-			FillCell(top, out[0]);
-			for (int i = 0; i < 8; ++i) out[0].Children[i] = starts[i];
-			if (top.Terminus) return;
-			WorkerPool::Get().ParallelFor(8, [&](int i)
-			{
-				if (starts[i] >= 0) FlattenAt(*top.Kids[i], starts[i], out);
-			});
 		}
 	}
 
@@ -322,6 +285,7 @@ namespace tg
 			arena.ReleaseLater();
 			return false;
 		}
+		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
 		arena.ReleaseLater();
 		return true;
@@ -357,6 +321,7 @@ namespace tg
 		FindIncomplete(*top, incomplete);
 		const BuildParams second{ 0.25f, false, -1 };
 		BuildLevels(incomplete, second, 3, arena);
+		Cells.reserve(CountCells(*top));
 		Flatten(*top, Cells);
 		arena.ReleaseLater();
 		return true;
