@@ -190,11 +190,16 @@ namespace tg
 						c->Kids[i]->Bounds = b;
 					}
 				}
+				// The clips are handed out largest tree first (leaf count), so that no long one
+				// starts last; each writes only its own parent's children.
 				WorkerPool& pool = WorkerPool::Get();
+				std::vector<int> order(parents.size());
+				for (size_t j = 0; j < order.size(); ++j) order[j] = (int)j;
+				std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return parents[(size_t)a]->Leaves > parents[(size_t)b]->Leaves; });
 				if ((int)parents.size() <= pool.Workers())
-					pool.ParallelFor((int)parents.size() * 8, [&](int j) { InitChild(*parents[j / 8], j % 8, bp); });
+					pool.ParallelFor((int)parents.size() * 8, [&](int j) { InitChild(*parents[(size_t)order[(size_t)(j / 8)]], j % 8, bp); });
 				else
-					pool.ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[j], bp); });
+					pool.ParallelFor((int)parents.size(), [&](int j) { InitChildren(*parents[(size_t)order[(size_t)j]], bp); });
 				level.clear();
 				for (TmpCell* c : parents)
 					for (TmpCell* k : c->Kids) level.push_back(k);
@@ -502,14 +507,6 @@ namespace tg
 				Code.push_back(b);
 				Code.push_back(c);
 			}
-			static void Quad(std::vector<float>& v, uint32_t head, float a, float b, float c)
-			{
-				v.push_back(BitsFloat(head)); v.push_back(a); v.push_back(b); v.push_back(c);
-			}
-			static void Quad4(std::vector<float>& v, float a, float b, float c, float d)
-			{
-				v.push_back(a); v.push_back(b); v.push_back(c); v.push_back(d);
-			}
 			int MaterialIndex(const Material* m) const
 			{
 				if (!m) return -1;
@@ -565,13 +562,22 @@ namespace tg
 			size_t LastBrushAt = 0;         // float index of the last distance brush record's head
 			size_t LastSurfaceBrushAt = 0;  // and of the last surface brush record's
 
-			int Records(const Node& n)
+			// A brush's two records: its distance quads (at most 5), then its surface quads (4).
+			struct BrushRecords
 			{
+				float Data[36];
+				int DistanceFloats, SurfaceFloats;
+			};
+
+			// The records of brush n.  Touches no table of the emitter: safe on any thread.
+			void MakeRecords(const Node& n, BrushRecords& out) const
+			{
+				int k = 0;
+				auto put = [&](float a, float b, float c, float d)
 				{
-					const NodeFacts::Entry& e = Facts.At(&n);
-					if (e.Record >= 0) return e.Record;
-				}
-				std::vector<float> dist, surf;
+					out.Data[k] = a; out.Data[k + 1] = b; out.Data[k + 2] = c; out.Data[k + 3] = d;
+					k += 4;
+				};
 				const Transform& t = n.Xf;
 				const bool rot = !t.Rotation.IsIdentity();
 				const bool scl = t.Scalation != 1.0f;
@@ -580,46 +586,86 @@ namespace tg
 				if (rot || scl) flags |= RecMatrix;
 				else if (trn) flags |= RecOffset;
 				if (scl) flags |= RecScale;
-				Quad(dist, n.Op | flags, n.Params[0], n.Params[1], n.Params[2]);
+				put(BitsFloat(n.Op | flags), n.Params[0], n.Params[1], n.Params[2]);
 				if (flags & RecMatrix)
 				{
 					const Mat4 inv = MatInverse(t.ToMatrix());
 					// Row r of the 3x4 affine part: (m[0][r], m[1][r], m[2][r], m[3][r]).
-					for (int r = 0; r < 3; ++r) Quad4(dist, inv.at(0, r), inv.at(1, r), inv.at(2, r), inv.at(3, r));
+					for (int r = 0; r < 3; ++r) put(inv.at(0, r), inv.at(1, r), inv.at(2, r), inv.at(3, r));
 				}
 				else if (flags & RecOffset)
 				{
-					Quad4(dist, -t.Translation.x, -t.Translation.y, -t.Translation.z, 0.0f);
+					put(-t.Translation.x, -t.Translation.y, -t.Translation.z, 0.0f);
 				}
-				if (flags & RecScale) Quad4(dist, t.Scalation, 0.0f, 0.0f, 0.0f);
+				if (flags & RecScale) put(t.Scalation, 0.0f, 0.0f, 0.0f);
+				out.DistanceFloats = k;
 				const Quat qi = Inverse(t.Rotation);
-				Quad(surf, n.Op, n.Params[0], n.Params[1], n.Params[2]);
-				Quad4(surf, qi.w, qi.x, qi.y, qi.z);
-				Quad4(surf, t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
-				Quad(surf, (uint32_t)MaterialIndex(n.Mat.get()), 0.0f, 0.0f, 0.0f);
+				put(BitsFloat(n.Op), n.Params[0], n.Params[1], n.Params[2]);
+				put(qi.w, qi.x, qi.y, qi.z);
+				put(t.Translation.x, t.Translation.y, t.Translation.z, t.Scalation);
+				put(BitsFloat((uint32_t)MaterialIndex(n.Mat.get())), 0.0f, 0.0f, 0.0f);
+				out.SurfaceFloats = k - out.DistanceFloats;
+			}
+
+			// Appends brush n's records to this emitter's arena; returns their slot.
+			int AddRecords(const Node& n, const BrushRecords& r)
+			{
 				const int32_t slot = (int32_t)Spans.size();
 				RecordSpans sp;
 				sp.DistanceAt = (int)Arena.size();
-				sp.DistanceFloats = (int)dist.size();
-				Arena.insert(Arena.end(), dist.begin(), dist.end());
-				sp.SurfaceAt = (int)Arena.size();
-				sp.SurfaceFloats = (int)surf.size();
-				Arena.insert(Arena.end(), surf.begin(), surf.end());
+				sp.DistanceFloats = r.DistanceFloats;
+				sp.SurfaceAt = sp.DistanceAt + r.DistanceFloats;
+				sp.SurfaceFloats = r.SurfaceFloats;
+				Arena.insert(Arena.end(), r.Data, r.Data + r.DistanceFloats + r.SurfaceFloats);
 				Spans.push_back(sp);
 				Facts.At(&n).Record = slot;
 				return slot;
 			}
 
-			// Builds the records of every brush under n (the full tree, before emission).
-			void BuildAllRecords(const Node& n)
+			int Records(const Node& n)
+			{
+				{
+					const NodeFacts::Entry& e = Facts.At(&n);
+					if (e.Record >= 0) return e.Record;
+				}
+				BrushRecords r;
+				MakeRecords(n, r);
+				return AddRecords(n, r);
+			}
+
+			// Each brush under n once, depth first (a brush being collected has Record -2).
+			void CollectBrushes(const Node& n, std::vector<const Node*>& out)
 			{
 				switch (n.Kind)
 				{
-				case NodeKind::Brush: Records(n); break;
-				case NodeKind::Set: BuildAllRecords(*n.Lhs); BuildAllRecords(*n.Rhs); break;
-				case NodeKind::Flate: BuildAllRecords(*n.Lhs); break;
-				case NodeKind::Stencil: BuildAllRecords(*n.Lhs); BuildAllRecords(*n.Mask); break;
+				case NodeKind::Brush:
+				{
+					NodeFacts::Entry& e = Facts.At(&n);
+					if (e.Record == -1)
+					{
+						e.Record = -2;
+						out.push_back(&n);
+					}
+					break;
 				}
+				case NodeKind::Set: CollectBrushes(*n.Lhs, out); CollectBrushes(*n.Rhs, out); break;
+				case NodeKind::Flate: CollectBrushes(*n.Lhs, out); break;
+				case NodeKind::Stencil: CollectBrushes(*n.Lhs, out); CollectBrushes(*n.Mask, out); break;
+				}
+			}
+
+			// Builds the records of every brush under n (the full tree, before emission): the
+			// brushes' records are computed on the worker pool, then appended in depth-first
+			// order.
+			void BuildAllRecords(const Node& n)
+			{
+				std::vector<const Node*> brushes;
+				CollectBrushes(n, brushes);
+				std::vector<BrushRecords> built(brushes.size());
+				WorkerPool::Get().ParallelFor((int)brushes.size(), [&](int i) { MakeRecords(*brushes[(size_t)i], built[(size_t)i]); });
+				Arena.reserve(Arena.size() + brushes.size() * 36);
+				Spans.reserve(Spans.size() + brushes.size());
+				for (size_t i = 0; i < brushes.size(); ++i) AddRecords(*brushes[i], built[i]);
 			}
 
 			// Distance program: Tangerine's postfix program with each brush's transform,
@@ -968,8 +1014,30 @@ namespace tg
 		std::vector<std::vector<float>> chunkCode((size_t)chunkCount);
 		std::vector<EmittedPrograms> programs(items);
 		ds->SurfaceQuads.assign(items, 0);
-		ds->ChunkFirst.resize((size_t)chunkCount + 1);
-		for (int ch = 0; ch <= chunkCount; ++ch) ds->ChunkFirst[(size_t)ch] = (int)((uint64_t)items * (uint64_t)ch / (uint64_t)chunkCount);
+		// Chunks of about equal cost, a program's cost taken as its tree's leaf count: the
+		// largest programs come first in depth-first order (the root's, its children's), and
+		// equal item counts left one chunk far longer than the rest.  Where the boundaries
+		// fall does not change the image (chunks are laid end to end in item order).
+		{
+			std::vector<uint64_t> cost(items, 0);
+			for (size_t i = 0; i < octree.Cells.size(); ++i)
+			{
+				const int u = programOf[i];
+				if (u >= 0 && cost[(size_t)u] == 0) cost[(size_t)u] = (uint64_t)std::max(1, octree.Cells[i].EvaluatorLeaves);
+			}
+			cost[evaluators] = (uint64_t)std::max(1, root->LeafCount());
+			uint64_t total = 0;
+			for (uint64_t c : cost) total += c;
+			ds->ChunkFirst.assign((size_t)chunkCount + 1, (int)items);
+			ds->ChunkFirst[0] = 0;
+			uint64_t sum = 0;
+			int ch = 1;
+			for (size_t u = 0; u < items && ch < chunkCount; ++u)
+			{
+				sum += cost[u];
+				while (ch < chunkCount && sum * (uint64_t)chunkCount >= total * (uint64_t)ch) ds->ChunkFirst[(size_t)ch++] = (int)u + 1;
+			}
+		}
 		WorkerPool::Get().ParallelFor(chunkCount, [&](int ch)
 		{
 			std::vector<float>& code = chunkCode[(size_t)ch];
