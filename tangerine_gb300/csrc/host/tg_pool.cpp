@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <chrono>
 
+#include <sched.h>
+
 namespace tg
 {
 	WorkerPool& WorkerPool::Get()
@@ -11,9 +13,27 @@ namespace tg
 		return pool;
 	}
 
+	namespace
+	{
+		// The CPUs this process may run on (a container's CPU set can be smaller than the
+		// machine, which is all hardware_concurrency counts): polling workers beyond them
+		// would take the cores from the ones that work.
+		unsigned UsableCpus()
+		{
+			cpu_set_t set;
+			CPU_ZERO(&set);
+			if (sched_getaffinity(0, sizeof set, &set) == 0)
+			{
+				const int n = CPU_COUNT(&set);
+				if (n > 0) return (unsigned)n;
+			}
+			return std::thread::hardware_concurrency();
+		}
+	}
+
 	WorkerPool::WorkerPool()
 	{
-		const unsigned hw = std::thread::hardware_concurrency();
+		const unsigned hw = UsableCpus();
 		const int n = (int)std::min(hw > 1 ? hw - 1 : 1u, 31u);
 		for (int i = 0; i < n; ++i) Threads.emplace_back([this]() { Run(); });
 	}
