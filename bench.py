@@ -638,12 +638,16 @@ def our_arm(args, rank, world, local_rank):
             c_export()     # warm
         torch.cuda.synchronize()
         barrier()
+        calls = []
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            tc = time.perf_counter()
             nv, nf, has_colors = c_export()
+            calls.append(time.perf_counter() - tc)
         torch.cuda.synchronize()
         barrier()
         e2e_s = time.perf_counter() - t0
+        calls.sort()
         e2e_s = group.max(e2e_s)
         prog_bytes = info.octree_cells * 64 + info.code_quads * 16 + info.materials * 4
         d2h = nv * (12 + 12 + 4 + (3 if has_colors else 0)) + nf * 12
@@ -656,6 +660,7 @@ def our_arm(args, rank, world, local_rank):
                "host_compile_split_s": {"octree": oct_s.value, "programs": comp_s.value - oct_s.value},
                "h2d_bytes_per_step": int(prog_bytes), "d2h_bytes_per_step": int(d2h),
                "meshes_per_s": world * e2e_steps / e2e_s,
+               "calls": e2e_steps, "median_call_ms": calls[len(calls) // 2] * 1e3, "slowest_call_ms": calls[-1] * 1e3,
                "call": "tg_export_tree (octree build + compile, the GPU testing bricks on the root cell's program meanwhile; upload + rest of the GPU export + copy to host)"}
 
     # Roofline of the dominant kernel of the timed export (the distance interpreter on the
