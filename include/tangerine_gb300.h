@@ -284,7 +284,11 @@ TANGERINE_API tg_status tg_export_mesh_noalloc(tg_program* program, const tg_gri
                                                uint64_t* counts, void* stream);
 
 /* Whole reference export path from a tree: octree + compile, lattice, surface nets,
- * normals, colours, copy back to the host (MeshExportThread minus the file write). */
+ * normals, colours, copy back to the host (MeshExportThread minus the file write).  The
+ * fastest form for a tree exported once: the GPU tests the bricks on the root cell's
+ * program while the host builds the rest of the octree, and the surface programs are
+ * emitted while the GPU runs the first export stages; the mesh is the one tg_compile +
+ * tg_export_mesh give, bit for bit.  Holds the library's engine for the whole call. */
 TANGERINE_API tg_status tg_export_tree(void* tree, const float model_min[3], const float model_max[3], float step,
                                        tg_mesh* out, void* stream);
 
