@@ -285,7 +285,7 @@ namespace tg
 	cudaError_t Engine::PreClassify(const RootProgram& root, const GridSpec& g, int B, cudaStream_t s)
 	{
 		PreValid = false;
-		if (B < 1 || B > 15 || root.Code.empty()) return cudaErrorInvalidValue;
+		if (B < 1 || B > 32 || root.Code.empty()) return cudaErrorInvalidValue;
 		const int64_t nb = BrickCount(g, B);
 		if (nb <= 0) return cudaErrorInvalidValue;
 		TG_TRY(BrickBits.Reserve((size_t)((nb + 31) / 32) * 4));

@@ -69,7 +69,7 @@ namespace tg
 	{
 		bool Attributes = true;     // gradient normals and colours
 		bool Dense = false;         // evaluate every lattice point (no brick culling)
-		int BrickSize = 7;          // cells per brick edge when culling (1..15)
+		int BrickSize = 7;          // cells per brick edge when culling (1..32)
 		int Lanes = 2;              // lattice points per thread sharing one pass over records
 		bool Staged = false;        // brick evaluation reads single-cell bricks' programs from shared memory
 		const FieldNet* Field = nullptr;    // learned bound for the brick test (else exact)
